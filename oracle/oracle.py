@@ -1,0 +1,145 @@
+"""ctypes wrapper of the oracle (test infrastructure only).
+
+The oracle is a CPU restatement of OpenQP's direct two-electron Fock build
+(see oracle_core.cpp / oracle_fock.cpp for the function-by-function citations)
+plus an independent McMurchie-Davidson integral code.  Only the tests, the
+smoke check and the CPU-baseline leg of bench.py load it, and only as the
+checker: the product never routes through it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboqp_oracle.so")
+_lib = None
+
+_d = ctypes.POINTER(ctypes.c_double)
+_i = ctypes.POINTER(ctypes.c_int)
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_create.restype = ctypes.c_void_p
+        L.orc_create.argtypes = [ctypes.c_int, _i, _i, _i, _d, _d, _i, ctypes.c_int, _d, ctypes.c_double]
+        L.orc_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_nbf.argtypes = [ctypes.c_void_p]
+        L.orc_fock_jk.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_int, ctypes.c_int, _d, _d]
+        L.orc_schwarz.argtypes = [ctypes.c_void_p, _d, ctypes.c_int]
+        L.orc_shlden.argtypes = [ctypes.c_void_p, _d, ctypes.c_int, _d]
+        L.orc_eri_quartet.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 4 + [_d]
+        L.orc_md_quartet.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 4 + [_d]
+        L.orc_eri_dense.argtypes = [ctypes.c_void_p, _d]
+        L.orc_one_electron.argtypes = [ctypes.c_void_p, ctypes.c_int, _d, _d]
+        L.orc_rys.argtypes = [ctypes.c_int, ctypes.c_double, _d, _d]
+        L.orc_boys.argtypes = [ctypes.c_int, ctypes.c_double, _d]
+        _lib = L
+    return _lib
+
+
+def _p(a, t=_d):
+    return a.ctypes.data_as(t)
+
+
+class Oracle:
+    """One basis/geometry registered with the oracle."""
+
+    def __init__(self, bas, cutoff=1e-10):
+        self.bas = bas
+        self._keep = [np.ascontiguousarray(bas.am, dtype=np.int32), np.ascontiguousarray(bas.ncontr, dtype=np.int32),
+                      np.ascontiguousarray(bas.origin, dtype=np.int32), np.ascontiguousarray(bas.ex),
+                      np.ascontiguousarray(bas.cc), np.ascontiguousarray(bas.harmonic, dtype=np.int32),
+                      np.ascontiguousarray(bas.xyz.reshape(-1))]
+        k = self._keep
+        self.h = lib().orc_create(len(bas.am), _p(k[0], _i), _p(k[1], _i), _p(k[2], _i), _p(k[3]), _p(k[4]),
+                                  _p(k[5], _i), int(bas.natom), _p(k[6]), float(cutoff))
+        self.nbf = lib().orc_nbf(self.h)
+        self.ntri = self.nbf * (self.nbf + 1) // 2
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def fock_jk(self, d, se=1.0, sc=1.0, urohf=None, nthreads=None, schwarz=None):
+        """Two-electron Fock part in OpenQP's packed convention.
+
+        d: (ntri,) or (nfocks, ntri).  nfocks == 1 -> RHF consumer, 2 -> UROHF
+        consumer (unless urohf is given)."""
+        d = np.ascontiguousarray(np.atleast_2d(d), dtype=np.float64)
+        nf = d.shape[0]
+        if urohf is None:
+            urohf = nf == 2
+        f = np.zeros_like(d)
+        st = np.zeros(8)
+        nt = nthreads or os.cpu_count()
+        q = None if schwarz is None else _p(np.ascontiguousarray(schwarz))
+        lib().orc_fock_jk(self.h, _p(d), _p(f), nf, se, sc, int(urohf), nt, q, _p(st))
+        self.last_stats = dict(t_init=st[0], t_schwarz=st[1], t_twoei=st[2], t_total=st[3], quartets=int(st[4]),
+                               screened=int(st[5]), prim_quartets=int(st[6]), stored=int(st[7]))
+        return f
+
+    def schwarz(self, nthreads=None):
+        ns = len(self.bas.am)
+        q = np.zeros(ns * ns)
+        lib().orc_schwarz(self.h, _p(q), nthreads or os.cpu_count())
+        return q.reshape(ns, ns)
+
+    def shlden(self, d):
+        d = np.ascontiguousarray(np.atleast_2d(d))
+        ns = len(self.bas.am)
+        out = np.zeros(ns * ns)
+        lib().orc_shlden(self.h, _p(d), d.shape[0], _p(out))
+        return out.reshape(ns, ns)
+
+    def _shape(self, i, j, k, l):
+        return tuple(int(self.bas.naos[s]) for s in (i, j, k, l))
+
+    def eri_quartet(self, i, j, k, l):
+        sh = self._shape(i, j, k, l)
+        out = np.zeros(int(np.prod(sh)))
+        lib().orc_eri_quartet(self.h, i, j, k, l, _p(out))
+        return out.reshape(sh)
+
+    def md_quartet(self, i, j, k, l):
+        sh = self._shape(i, j, k, l)
+        out = np.zeros(int(np.prod(sh)))
+        lib().orc_md_quartet(self.h, i, j, k, l, _p(out))
+        return out.reshape(sh)
+
+    def eri_dense(self):
+        n = self.nbf
+        out = np.zeros(n ** 4)
+        lib().orc_eri_dense(self.h, _p(out))
+        return out.reshape(n, n, n, n)
+
+    def one_electron(self, which, charges=None):
+        n = self.nbf
+        out = np.zeros(n * n)
+        z = np.ascontiguousarray(self.bas.charges if charges is None else charges, dtype=np.float64)
+        lib().orc_one_electron(self.h, {"S": 0, "T": 1, "V": 2}[which], _p(z), _p(out))
+        return out.reshape(n, n)
+
+
+def rys(n, X):
+    x = np.zeros(n)
+    w = np.zeros(n)
+    lib().orc_rys(n, float(X), _p(x), _p(w))
+    return x, w
+
+
+def boys(m, T):
+    F = np.zeros(m + 1)
+    lib().orc_boys(m, float(T), _p(F))
+    return F

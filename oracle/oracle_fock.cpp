@@ -1,0 +1,419 @@
+// Oracle (test infrastructure only): the Fock-build driver of the CPU
+// restatement -- Schwarz bounds, shell density, the OpenMP quartet loop,
+// storeints and the RHF/UROHF digestion -- and the C entry points the tests
+// and the CPU-baseline leg of bench.py call through ctypes.
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <omp.h>
+
+#include "oracle_basis.h"
+
+using namespace orc;
+
+using OrcHandle = orc::Handle;
+
+struct OrcStats {
+  double t_init, t_schwarz, t_twoei, t_total;
+  long long quartets, screened, prim_quartets, stored;
+};
+
+// ints_exchange (int2.F90:1582-1737): Q(i,j) = sqrt(max |(ij|ij)|) with the
+// very tight cutoffs 1e-15 / 1e-17 / 1e-17 / 50.
+static void schwarz(const Basis& B, std::vector<double>& Q, int nthreads) {
+  const Cutoffs cut = Cutoffs::make(1e-15, 1e-17, 1e-17, 50.0);
+  PairStore PS;
+  PS.build(B, cut);
+  const int ns = B.nshell;
+  Q.assign((size_t)ns * ns, 0.0);
+#pragma omp parallel num_threads(nthreads)
+  {
+    QuartetWork W;
+    std::vector<double> blk(6 * 6 * 6 * 6);
+#pragma omp for schedule(dynamic, 4)
+    for (int i = 0; i < ns; ++i) {
+      for (int j = 0; j <= i; ++j) {
+        int ids[4] = {i, j, i, j}, s[4], fl[4];
+        flip_quartet(B, ids, s, fl);
+        double vmax = 0.0;
+        if (rys_quartet(B, PS, cut, s, blk.data(), W) > 0) {
+          int n = 1;
+          for (int t = 0; t < 4; ++t) n *= B.sh[s[t]].nao;
+          for (int e = 0; e < n; ++e) vmax = std::max(vmax, std::fabs(blk[e]));
+        }
+        Q[(size_t)i * ns + j] = Q[(size_t)j * ns + i] = std::sqrt(vmax);
+      }
+    }
+  }
+}
+
+// shlden (int2.F90:999-1047): max |D| over the AO block of every shell pair
+// and over the density matrices.
+static void shlden(const Basis& B, const double* d, int nfocks, std::vector<double>& dsh) {
+  const int ns = B.nshell;
+  const size_t ntri = (size_t)B.nbf * (B.nbf + 1) / 2;
+  dsh.assign((size_t)ns * ns, 0.0);
+  for (int f = 0; f < nfocks; ++f) {
+    const double* df = d + f * ntri;
+    for (int si = 0; si < ns; ++si) {
+      const int mini = B.sh[si].aoff, maxi = mini + B.sh[si].nao - 1;
+      for (int sj = 0; sj <= si; ++sj) {
+        const int minj = B.sh[sj].aoff;
+        int maxj = minj + B.sh[sj].nao - 1;
+        double dmax = 0;
+        for (int i = mini; i <= maxi; ++i) {
+          if (si == sj) maxj = i;
+          for (int j = minj; j <= maxj; ++j) {
+            const size_t ij = (size_t)i * (i + 1) / 2 + j;
+            dmax = std::max(std::fabs(df[ij]), dmax);
+          }
+        }
+        double& t = dsh[(size_t)si * ns + sj];
+        t = std::max(dmax, t);
+      }
+    }
+  }
+  for (int si = 0; si < ns; ++si)
+    for (int sj = si + 1; sj < ns; ++sj) dsh[(size_t)si * ns + sj] = dsh[(size_t)sj * ns + si];
+}
+
+// int2_build_shell_pair_map (int2.F90:864-921): pairs in descending estimated
+// cost (counting sort over log2 classes), i descending as the secondary key.
+static void pair_map(const Basis& B, const std::vector<double>& Q, std::vector<int>& pi, std::vector<int>& pj) {
+  const int ns = B.nshell, NCLASS = 64, OFFS = 42;
+  const int np = ns * (ns + 1) / 2;
+  pi.assign(np, 0); pj.assign(np, 0);
+  std::vector<int> cnt(NCLASS + 1, 0), off(NCLASS + 1, 0);
+  auto cls_of = [&](int i, int j) {
+    // shell numbers are 1-based in the cost formula
+    const int nbfi = ncart(B.sh[i].am), nbfj = ncart(B.sh[j].am);
+    const double sw = std::max(Q[(size_t)i * ns + j], 1e-30);
+    const double cost = sw * (double)(nbfi * nbfj) * (double)(i + 1);
+    const int lg = (int)(std::log(cost) / std::log(2.0));
+    return NCLASS - std::max(0, std::min(NCLASS, lg + OFFS));
+  };
+  for (int i = ns - 1; i >= 0; --i)
+    for (int j = 0; j <= i; ++j) cnt[cls_of(i, j)]++;
+  off[0] = 0;
+  for (int c = 1; c <= NCLASS; ++c) off[c] = off[c - 1] + cnt[c - 1];
+  for (int i = ns - 1; i >= 0; --i)
+    for (int j = 0; j <= i; ++j) {
+      const int c = cls_of(i, j);
+      const int p = off[c]++;
+      pi[p] = i; pj[p] = j;
+    }
+}
+
+struct Store {
+  std::vector<int> ids;     // 4 per element, 0-based AO indices
+  std::vector<double> val;
+  int n = 0;
+  explicit Store(int cap) : ids(4 * (size_t)cap), val(cap) {}
+};
+
+// int2_rhf_data_t_update / int2_urohf_data_t_update (int2.F90:1414-1578)
+static void update(Store& st, const double* d, double* f, int nfocks, size_t ntri, bool urohf, double se,
+                   double sc) {
+  for (int n = 0; n < st.n; ++n) {
+    const long ii = st.ids[4 * n] + 1, jj = st.ids[4 * n + 1] + 1, kk = st.ids[4 * n + 2] + 1,
+               ll = st.ids[4 * n + 3] + 1;
+    const double val = st.val[n];
+    const long ii2 = ii * (ii - 1) / 2, jj2 = jj * (jj - 1) / 2, kk2 = kk * (kk - 1) / 2;
+    const long ij = ii2 + jj - 1, ik = ii2 + kk - 1, il = ii2 + ll - 1, kl = kk2 + ll - 1;
+    long jk = jj2 + kk - 1, jl = jj2 + ll - 1;
+    if (jj < kk) jk = kk2 + jj - 1;
+    if (jj < ll) jl = ll * (ll - 1) / 2 + jj - 1;
+    if (!urohf) {
+      const double val1 = val * se, val4 = val * 4 * sc;
+      for (int q = 0; q < nfocks; ++q) {
+        const double* dq = d + q * ntri;
+        double* fq = f + q * ntri;
+        fq[ij] += val4 * dq[kl];
+        fq[kl] += val4 * dq[ij];
+        fq[ik] -= val1 * dq[jl];
+        fq[jl] -= val1 * dq[ik];
+        fq[il] -= val1 * dq[jk];
+        fq[jk] -= val1 * dq[il];
+      }
+    } else {
+      const double val1 = val * 2 * se, val4 = val * 4 * sc;
+      const double* da = d;
+      const double* db = d + ntri;
+      const double cij = val4 * (da[ij] + db[ij]);
+      const double ckl = val4 * (da[kl] + db[kl]);
+      for (int q = 0; q < 2; ++q) {
+        const double* dq = d + q * ntri;
+        double* fq = f + q * ntri;
+        fq[ij] += ckl;
+        fq[kl] += cij;
+        fq[ik] -= val1 * dq[jl];
+        fq[jl] -= val1 * dq[ik];
+        fq[il] -= val1 * dq[jk];
+        fq[jk] -= val1 * dq[il];
+      }
+    }
+  }
+  st.n = 0;
+}
+
+// int2_compute_data_t_storeints (int2.F90:1741-1865)
+static long storeints(const Basis& B, const int ids[4], const double* blk, double cutoff, Store& st, const double* d,
+                      double* f, int nfocks, size_t ntri, bool urohf, double se, double sc) {
+  const int n1 = B.sh[ids[0]].nao, n2 = B.sh[ids[1]].nao, n3 = B.sh[ids[2]].nao, n4 = B.sh[ids[3]].nao;
+  const bool same = ids[0] == ids[2] && ids[1] == ids[3];
+  const bool iandj = ids[0] == ids[1];
+  const bool kandl = ids[2] == ids[3];
+  const int loci = B.sh[ids[0]].aoff, locj = B.sh[ids[1]].aoff, lock = B.sh[ids[2]].aoff,
+            locl = B.sh[ids[3]].aoff;
+  long nint = 0;
+  int nij = 0;
+  int maxj = n2;
+  for (int i = 0; i < n1; ++i) {
+    if (iandj) maxj = i + 1;
+    for (int j = 0; j < maxj; ++j) {
+      ++nij;
+      int nkl = nij;
+      int maxl = n4;
+      bool next_j = false;
+      for (int k = 0; k < n3 && !next_j; ++k) {
+        if (kandl) maxl = k + 1;
+        if (same) {
+          const int itmp = std::min(maxl, nkl);
+          if (itmp == 0) { next_j = true; break; }
+          maxl = itmp;
+          nkl -= itmp;
+        }
+        for (int l = 0; l < maxl; ++l) {
+          double val = blk[((i * n2 + j) * n3 + k) * n4 + l];
+          if (std::fabs(val) < cutoff) continue;
+          ++nint;
+          int i1 = i + loci, j1 = j + locj, k1 = k + lock, l1 = l + locl;
+          if (i1 < j1) std::swap(i1, j1);
+          if (k1 < l1) std::swap(k1, l1);
+          int ii = i1, jj = j1, kk = k1, ll = l1;
+          if (ii < kk) { ii = k1; jj = l1; kk = i1; ll = j1; }
+          else if (ii == kk && jj < ll) { ii = i1; jj = l1; kk = k1; ll = j1; }
+          if (ii == jj) val *= 0.5;
+          if (kk == ll) val *= 0.5;
+          if (ii == kk && jj == ll) val *= 0.5;
+          int* p = &st.ids[4 * (size_t)st.n];
+          p[0] = ii; p[1] = jj; p[2] = kk; p[3] = ll;
+          st.val[st.n++] = val;
+          if (st.n == (int)st.val.size()) update(st, d, f, nfocks, ntri, urohf, se, sc);
+        }
+      }
+    }
+  }
+  return nint;
+}
+
+static double now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// fock_jk (scf_addons.F90:1063-1214) with int2_twoei (int2.F90:589-923).
+static int fock_jk(OrcHandle* H, const double* d, double* fout, int nfocks, double se, double sc, int urohf,
+                   int nthreads, const double* qext, OrcStats* stats) {
+  const Basis& B = H->B;
+  const double t0 = now();
+  const double cut = H->cutoff;
+  const Cutoffs cutoffs = Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0));
+  PairStore PS;
+  PS.build(B, cutoffs);
+  const double t1 = now();
+  std::vector<double> Q;
+  if (qext) Q.assign(qext, qext + (size_t)B.nshell * B.nshell);
+  else schwarz(B, Q, nthreads);
+  const double t2 = now();
+  std::vector<double> dsh;
+  shlden(B, d, nfocks, dsh);
+  double max_den = 0;
+  for (double v : dsh) max_den = std::max(max_den, std::fabs(v));
+  std::vector<int> pi, pj;
+  pair_map(B, Q, pi, pj);
+  const int ns = B.nshell;
+  const int np = ns * (ns + 1) / 2;
+  const size_t ntri = (size_t)B.nbf * (B.nbf + 1) / 2;
+  const int nf = urohf ? 2 : nfocks;
+  std::vector<double> facc((size_t)nthreads * nf * ntri, 0.0);
+  long long nq = 0, nsk = 0, npq = 0, nst = 0;
+#pragma omp parallel num_threads(nthreads) reduction(+ : nq, nsk, npq, nst)
+  {
+    const int tid = omp_get_thread_num();
+    double* f = facc.data() + (size_t)tid * nf * ntri;
+    QuartetWork W;
+    std::vector<double> blk(6 * 6 * 6 * 6);
+    Store st(50000);
+#pragma omp for schedule(dynamic, 1)
+    for (int p = 0; p < np; ++p) {
+      const int i = pi[p], j = pj[p];
+      const double qij = Q[(size_t)i * ns + j];
+      if (qij * max_den < cut) { nsk += (long long)(i + 1) * i / 2 + j + 1; continue; }
+      for (int k = 0; k <= i; ++k) {
+        const int jork = (k == i) ? j : k;
+        for (int l = 0; l <= jork; ++l) {
+          double test = qij * Q[(size_t)k * ns + l];
+          const double* D = dsh.data();
+          test *= std::max({4 * D[(size_t)i * ns + j], 4 * D[(size_t)k * ns + l], D[(size_t)j * ns + l],
+                            D[(size_t)j * ns + k], D[(size_t)i * ns + l], D[(size_t)i * ns + k]});
+          if (test < cut) { ++nsk; continue; }
+          ++nq;
+          const int ids0[4] = {i, j, k, l};
+          int s[4], fl[4];
+          flip_quartet(B, ids0, s, fl);
+          const long pq = rys_quartet(B, PS, cutoffs, s, blk.data(), W);
+          if (pq == 0) continue;
+          npq += pq;
+          nst += storeints(B, s, blk.data(), cut, st, d, f, nfocks, ntri, urohf, se, sc);
+        }
+      }
+    }
+    update(st, d, f, nfocks, ntri, urohf, se, sc);
+  }
+  // parallel_stop: reduce the replicated copies
+  for (int t = 1; t < nthreads; ++t)
+    for (size_t e = 0; e < (size_t)nf * ntri; ++e) facc[e] += facc[(size_t)t * nf * ntri + e];
+  // scaling: f = 0.5 f, diagonal doubled
+  for (int q = 0; q < nf; ++q) {
+    for (size_t e = 0; e < ntri; ++e) fout[q * ntri + e] = 0.5 * facc[q * ntri + e];
+    size_t ii = 0;
+    for (int i = 0; i < B.nbf; ++i) { ii += i + 1; fout[q * ntri + ii - 1] *= 2; }
+  }
+  const double t3 = now();
+  if (stats) {
+    stats->t_init = t1 - t0; stats->t_schwarz = t2 - t1; stats->t_twoei = t3 - t2; stats->t_total = t3 - t0;
+    stats->quartets = nq; stats->screened = nsk; stats->prim_quartets = npq; stats->stored = nst;
+  }
+  return 0;
+}
+
+extern "C" {
+
+// Basis registration in OpenQP's basis_set layout (basis_tools.F90:32-84):
+// per shell am, ncontr, origin (1-based atom), harmonic; ex/cc concatenated
+// (cc primitive-normalised); xyz(3, natom) in Bohr.
+void* orc_create(int nshell, const int* am, const int* ncontr, const int* origin, const double* ex,
+                 const double* cc, const int* harmonic, int natom, const double* xyz, double cutoff) {
+  auto* H = new OrcHandle;
+  Basis& B = H->B;
+  B.nshell = nshell; B.natom = natom;
+  B.xyz.assign(xyz, xyz + 3 * natom);
+  int poff = 0, aoff = 0;
+  for (int s = 0; s < nshell; ++s) {
+    Shell S;
+    S.am = am[s]; S.nprim = ncontr[s]; S.atom = origin[s] - 1; S.harm = harmonic ? harmonic[s] : 0;
+    S.poff = poff; S.aoff = aoff;
+    S.nao = (S.harm && S.am >= 2) ? 2 * S.am + 1 : ncart(S.am);
+    for (int d = 0; d < 3; ++d) S.c[d] = xyz[3 * S.atom + d];
+    poff += S.nprim; aoff += S.nao;
+    B.maxam = std::max(B.maxam, S.am);
+    B.sh.push_back(S);
+  }
+  B.nbf = aoff;
+  B.ex.assign(ex, ex + poff);
+  B.cc.assign(cc, cc + poff);
+  H->cutoff = cutoff;
+  return H;
+}
+
+void orc_destroy(void* h) { delete (OrcHandle*)h; }
+int orc_nbf(void* h) { return ((OrcHandle*)h)->B.nbf; }
+
+int orc_fock_jk(void* h, const double* d, double* f, int nfocks, double se, double sc, int urohf, int nthreads,
+                const double* schwarz_in, double* stats6) {
+  OrcStats st;
+  const int rc = fock_jk((OrcHandle*)h, d, f, nfocks, se, sc, urohf, nthreads, schwarz_in, &st);
+  if (stats6) {
+    stats6[0] = st.t_init; stats6[1] = st.t_schwarz; stats6[2] = st.t_twoei; stats6[3] = st.t_total;
+    stats6[4] = (double)st.quartets; stats6[5] = (double)st.screened; stats6[6] = (double)st.prim_quartets;
+    stats6[7] = (double)st.stored;
+  }
+  return rc;
+}
+
+void orc_schwarz(void* h, double* q, int nthreads) {
+  std::vector<double> Q;
+  schwarz(((OrcHandle*)h)->B, Q, nthreads);
+  std::memcpy(q, Q.data(), sizeof(double) * Q.size());
+}
+
+void orc_shlden(void* h, const double* d, int nfocks, double* dsh) {
+  std::vector<double> v;
+  shlden(((OrcHandle*)h)->B, d, nfocks, v);
+  std::memcpy(dsh, v.data(), sizeof(double) * v.size());
+}
+
+// Normalised (pure) shell-quartet block in the caller's (i,j,k,l) order,
+// out[a][b][c][d]; screening cutoffs of a Fock build with the handle's cutoff.
+int orc_eri_quartet(void* h, int i, int j, int k, int l, double* out) {
+  const Basis& B = ((OrcHandle*)h)->B;
+  const double cut = ((OrcHandle*)h)->cutoff;
+  const Cutoffs cutoffs = Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0));
+  PairStore PS;
+  PS.build(B, cutoffs);
+  const int ids[4] = {i, j, k, l};
+  int s[4], fl[4];
+  flip_quartet(B, ids, s, fl);
+  QuartetWork W;
+  std::vector<double> blk(6 * 6 * 6 * 6, 0.0);
+  rys_quartet(B, PS, cutoffs, s, blk.data(), W);
+  int n[4], nf[4];
+  for (int t = 0; t < 4; ++t) { n[t] = B.sh[ids[t]].nao; nf[t] = B.sh[s[t]].nao; }
+  // blk is in flipped order; position t of the flipped block holds ids[fl[t]]
+  int inv[4];
+  for (int t = 0; t < 4; ++t) inv[fl[t]] = t;
+  int idx[4];
+  for (idx[0] = 0; idx[0] < n[0]; ++idx[0])
+    for (idx[1] = 0; idx[1] < n[1]; ++idx[1])
+      for (idx[2] = 0; idx[2] < n[2]; ++idx[2])
+        for (idx[3] = 0; idx[3] < n[3]; ++idx[3]) {
+          int fi[4];
+          for (int t = 0; t < 4; ++t) fi[inv[t]] = idx[t];
+          out[((idx[0] * n[1] + idx[1]) * n[2] + idx[2]) * n[3] + idx[3]] =
+              blk[((fi[0] * nf[1] + fi[1]) * nf[2] + fi[2]) * nf[3] + fi[3]];
+        }
+  return 0;
+}
+
+// Dense (nbf^4) ERI tensor through the same engine without any screening
+// (tests of the J/K semantics on small systems).
+int orc_eri_dense(void* h, double* eri) {
+  const Basis& B = ((OrcHandle*)h)->B;
+  const int nb = B.nbf, ns = B.nshell;
+  const Cutoffs cutoffs = Cutoffs::make(0.0, 0.0, 0.0, 1e300);
+  PairStore PS;
+  PS.build(B, cutoffs);
+  QuartetWork W;
+  std::vector<double> blk(6 * 6 * 6 * 6, 0.0);
+  for (int i = 0; i < ns; ++i)
+    for (int j = 0; j < ns; ++j)
+      for (int k = 0; k < ns; ++k)
+        for (int l = 0; l < ns; ++l) {
+          const int ids[4] = {i, j, k, l};
+          int s[4], fl[4];
+          flip_quartet(B, ids, s, fl);
+          rys_quartet(B, PS, cutoffs, s, blk.data(), W);
+          int nf[4], inv[4];
+          for (int t = 0; t < 4; ++t) { nf[t] = B.sh[s[t]].nao; inv[fl[t]] = t; }
+          const Shell* S[4] = {&B.sh[i], &B.sh[j], &B.sh[k], &B.sh[l]};
+          int idx[4];
+          for (idx[0] = 0; idx[0] < S[0]->nao; ++idx[0])
+            for (idx[1] = 0; idx[1] < S[1]->nao; ++idx[1])
+              for (idx[2] = 0; idx[2] < S[2]->nao; ++idx[2])
+                for (idx[3] = 0; idx[3] < S[3]->nao; ++idx[3]) {
+                  int fi[4];
+                  for (int t = 0; t < 4; ++t) fi[inv[t]] = idx[t];
+                  const size_t o = (((size_t)(S[0]->aoff + idx[0]) * nb + S[1]->aoff + idx[1]) * nb +
+                                    S[2]->aoff + idx[2]) * nb + S[3]->aoff + idx[3];
+                  eri[o] = blk[((fi[0] * nf[1] + fi[1]) * nf[2] + fi[2]) * nf[3] + fi[3]];
+                }
+        }
+  return 0;
+}
+
+void orc_rys(int n, double X, double* x, double* w) { rys_eval(n, X, x, w); }
+void orc_boys(int m, double T, double* F) { boys(m, T, F); }
+
+}  // extern "C"

@@ -1,0 +1,41 @@
+"""Extract OpenQP's own HF golden results into a small fixture.
+
+Reads the example inputs/outputs that OpenQP's ``--validate_examples`` checks
+(``examples/HF/*.json``, ``examples/NMR/*.json``): atoms, coordinates (Bohr,
+as stored in the JSON) and the reference total energy (and gradient where
+present).  Run once where the OpenQP checkout exists; the fixture is committed.
+
+Usage: python make_golden.py <openqp checkout> > hf_golden.json
+"""
+import json
+import os
+import sys
+
+CASES = [
+    ("examples/HF/H2O_RHF-HF_ENERGY.json", "6-31g*", "rhf", 1),
+    ("examples/HF/H2O_UHF-HF_ENERGY.json", "6-31g*", "uhf", 3),
+    ("examples/HF/H2O_ROHF-HF_ENERGY.json", "6-31g*", "rohf", 3),
+    ("examples/HF/H2O_RHF-HF_GRADIENT.json", "6-31g*", "rhf", 1),
+    ("examples/HF/H2O_UHF-HF_GRADIENT.json", "6-31g*", "uhf", 3),
+    ("examples/HF/H2O_ROHF-HF_GRADIENT.json", "6-31g*", "rohf", 3),
+    ("examples/NMR/H2O_RHF-NMR.json", "sto-3g", "rhf", 1),
+    ("examples/NMR/CH3_UHF-GIAO-NMR.json", "sto-3g", "uhf", 2),
+    ("examples/NMR/CH3_ROHF-GIAO-NMR.json", "sto-3g", "rohf", 2),
+]
+
+
+def main(root):
+    out = []
+    for rel, basis, kind, mult in CASES:
+        with open(os.path.join(root, rel)) as fh:
+            d = json.load(fh)
+        case = {"source": rel, "basis": basis, "scf": kind, "multiplicity": mult, "atoms": d["atoms"],
+                "coord_bohr": d["coord"], "energy": d["energy"]}
+        if "grad" in d:
+            case["grad"] = d["grad"]
+        out.append(case)
+    json.dump({"cases": out}, sys.stdout, indent=1)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
