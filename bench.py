@@ -1,0 +1,267 @@
+"""Benchmark of the GB300 direct J/K Fock build.
+
+Workload (one "step" = one full RHF J+K Fock build): a seeded (H2O)32 cluster
+in a 14 A cube, cc-pVDZ with spherical d (768 basis functions), density
+D = 2 C C^T from 160 Loewdin-orthonormalised random columns, Schwarz / density
+screening threshold 1e-10.
+
+  value  builds/s with D and F resident in device memory (C-ABI device entry)
+  e2e    builds/s through OpenQP's seam routec_fock_jk with host buffers
+         (H2D of D and D2H of F inside every timed step)
+  roofline  FP64 roofline of the dominant class kernel: algorithmic flops
+            (3 R N_c per primitive quartet + digestion) / its event-timed
+            duration, against the measured FP64 FMA peak of this device
+  cpu_baseline  the oracle (CPU restatement of OpenQP's int2 path, OpenMP, all
+            host cores) on a bounded sample: the shell pairs of one rank of a
+            round-robin split of the cost-sorted pair list, plus the Schwarz
+            set-up the reference repeats in every fock_jk call.
+
+--impl reference times that CPU implementation alone (rank 0 only).
+Multi-GPU runs are independent replicas (one molecule per rank, no collective).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="(H2O)32 cc-pVDZ spherical RHF J+K Fock build", nwater=32, edge=14.0, seed=0, basis="cc-pvdz",
+                cutoff=1e-10)
+
+
+def make_workload():
+    from openqp_gb300 import workloads
+    from openqp_gb300.onee import overlap_kinetic
+    bas = workloads.water_cluster_basis(WORKLOAD["nwater"], WORKLOAD["edge"], WORKLOAD["seed"], WORKLOAD["basis"])
+    S, _ = overlap_kinetic(bas)
+    d = workloads.density(bas, workloads.nelectrons(bas) // 2, WORKLOAD["seed"], S=S)
+    return bas, d
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % gpu_index)
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [v.strip() for v in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = max(mx, float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(bas, d, budget_s=20.0):
+    """Oracle on a bounded sample; returns builds/s and a description."""
+    from oracle import oracle
+    oracle.build()
+    o = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"])
+    cores = os.cpu_count()
+    t0 = time.perf_counter()
+    q = o.schwarz(nthreads=cores)
+    t_schwarz = time.perf_counter() - t0
+    _, st = o.fock_jk_sample(d, 997, 0, nthreads=cores, schwarz=q)
+    est_full = max(st["t_twoei"] * 997, 1e-3)
+    stride = max(1, int(math.ceil(est_full / budget_s)))
+    _, st = o.fock_jk_sample(d, stride, 0, nthreads=cores, schwarz=q)
+    t_build = st["t_twoei"] * stride + st["t_init"] + t_schwarz
+    return dict(value=1.0 / t_build, unit="builds/s", cores=cores, kind="port",
+                sample="oracle fock_jk over 1/%d of the cost-sorted shell pairs (offset 0), x%d, plus the full "
+                       "Schwarz set-up (%.2f s) the reference repeats per build; %d quartets in the sample"
+                       % (stride, stride, t_schwarz, st["quartets"])), dict(sample_s=st["t_twoei"], stride=stride)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    bas, d = make_workload()
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        pass
+    vals = []
+    info = None
+    for _ in range(max(1, args.steps)):
+        cb, info = cpu_baseline(bas, d, budget_s=args.cpu_budget)
+        vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    line = {"impl": "reference", "metric": "J+K Fock builds/s", "value": v, "unit": "builds/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "cutoff": WORKLOAD["cutoff"]},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "builds/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from openqp_gb300 import build as bld
+    bld.build()
+    from openqp_gb300.fock import FockBuilder, class_flops, class_labels, fp64_peak_tflops, routec_init, \
+        routec_fock_jk
+    bas, d = make_workload()
+    fb = FockBuilder(bas, cutoff=WORKLOAD["cutoff"])
+    ntri = fb.ntri
+    dt = torch.from_numpy(d[None]).cuda()
+    out = torch.empty_like(dt)
+    st = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        fb.fock_jk_device(dt, out=out)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    times = []
+    stats = []
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fb.fock_jk_device(dt, out=out, stream=st)
+        e1.record(st)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        stats.append(fb.stats())
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    tsum = sum(times) / 1000.0
+    if ws > 1:
+        t = torch.tensor([tsum], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tsum = float(t.item())
+    value = ws * args.steps / tsum
+    # e2e through the seam with host buffers
+    routec_init(bas, WORKLOAD["cutoff"])
+    dflat = np.ascontiguousarray(d)
+    routec_fock_jk(dflat, bas.nbf, 1)
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        f_host, info = routec_fock_jk(dflat, bas.nbf, 1)
+        e2e_t.append(time.perf_counter() - t0)
+        if info != 0:
+            raise RuntimeError("routec_fock_jk returned info=%d" % info)
+    e2e_sum = sum(e2e_t)
+    if ws > 1:
+        t = torch.tensor([e2e_sum], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_sum = float(t.item())
+    e2e = ws * args.steps / e2e_sum
+    # roofline of the dominant class kernel (mean over the timed steps)
+    labels = class_labels()
+    ms = np.mean([s["ms_per_class"] for s in stats], axis=0)
+    cdom = int(np.argmax(ms))
+    s0 = stats[-1]
+    flops = class_flops(cdom, s0["prim_per_class"][cdom], s0["per_class"][cdom], nk=1, pure=True)
+    achieved = flops / (ms[cdom] * 1e-3) / 1e12
+    total_flops = sum(class_flops(c, s0["prim_per_class"][c], s0["per_class"][c], nk=1, pure=True)
+                      for c in range(21))
+    peak = fp64_peak_tflops()
+    if rank == 0:
+        line = {"metric": "J+K Fock builds/s", "value": value, "unit": "builds/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tsum / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded water cluster and Loewdin density)",
+                "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "nshell": int(len(bas.am)),
+                           "cutoff": WORKLOAD["cutoff"], "l2": "flushed (256 MB write) before every timed step",
+                           "parallelism": "replicas" if ws > 1 else "single GPU"},
+                "e2e": {"value": e2e, "unit": "builds/s", "h2d_bytes_per_step": int(8 * ntri),
+                        "d2h_bytes_per_step": int(8 * ntri)},
+                "roofline": {"bound": "fp64", "kernel": labels[cdom], "achieved": achieved, "peak": peak,
+                             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                             "peak_source": "measured: FP64 FMA-chain probe on this device",
+                             "kernel_ms": float(ms[cdom]), "build_fp64_tflops": total_flops / (tsum / args.steps) / 1e12},
+                "quartets_per_s": s0["quartets"] / (tsum / args.steps),
+                "prim_quartets_per_s": s0["prim_quartets"] / (tsum / args.steps),
+                "gpu_launches": int(sum(s["launches"] for s in stats)),
+                "wall_s": wall, "clocks": clocks,
+                "class_ms": {labels[c]: round(float(ms[c]), 3) for c in range(21) if ms[c] > 0}}
+        if not args.no_cpu:
+            cb, _ = cpu_baseline(bas, d, budget_s=args.cpu_budget)
+            line["cpu_baseline"] = cb
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

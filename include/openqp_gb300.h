@@ -1,0 +1,110 @@
+/*
+ * openqp_gb300 -- GB300-native direct two-electron Fock (J/K) build for OpenQP.
+ *
+ * C ABI of libopenqp_gb300.so.  Plain pointers and sizes only; every pointer
+ * is host memory unless the name says _device.  All entry points return (or
+ * store in *info) an OpenQP route-C status code:
+ *   0 success, 1 not initialised, 2 out of memory, 3 unsupported input
+ *   (angular momentum above d, mixed Cartesian/pure d shells, CAM), 4 device
+ *   error.  A non-zero status means the caller's native path must run, which
+ *   is exactly the contract of OpenQP's seam (source/modules/routec_bridge.F90:20-22).
+ *
+ * Two layers:
+ *   - routec_*: the reference-facing seam.  routec_fock_jk has the signature
+ *     OpenQP binds by dlopen/dlsym or at link time
+ *     (source/modules/routec_bridge.F90:33-40, 81-89, 204-216); it works on a
+ *     process-global context registered once by routec_fock_init.
+ *   - oqpg_*: an explicit-context API (several molecules at once, device
+ *     pointers, CUDA streams) used by the Python/torch front end and the
+ *     batched builds.
+ *
+ * Matrices are OpenQP's packed lower triangles, row-major with
+ * ij = i(i+1)/2 + j (0-based, i >= j), stacked per density:
+ *   d[nfocks][nbf(nbf+1)/2], f[nfocks][nbf(nbf+1)/2].
+ * nfocks = 1: RHF, F = sc J[D] - se/2 K[D];
+ * nfocks = 2: UHF/ROHF, F_s = sc J[Da + Db] - se K[D_s]
+ * (source/integrals/int2.F90:1414-1578 with the scaling of
+ *  source/scf_addons.F90:1177-1185 folded in: f comes back ready to use).
+ */
+#ifndef OPENQP_GB300_H
+#define OPENQP_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- reference-facing seam ------------------------------------------- */
+
+/* Register the basis and geometry used by the following routec_fock_jk
+ * calls, in the layout of OpenQP's basis_set (source/basis_tools.F90:32-84):
+ *   am[nshell], ncontr[nshell], origin[nshell] (1-based atom), harmonic[nshell]
+ *   (1 = pure spherical shell), ex/cc[sum ncontr] (cc primitive-normalised,
+ *   as after basis%normalize_primitives, source/basis_tools.F90:277-303),
+ *   xyz[3*natom] in Bohr, cutoff = OpenQP's int2e_cutoff (source/types.F90:121).
+ * Computes the Schwarz bounds on the device (ints_exchange,
+ * source/integrals/int2.F90:1582-1737).  There is no counterpart in the
+ * reference seam, which carries no basis (routec_bridge.F90:33-40); OpenQP
+ * would call this next to scf_addons.F90:1141.  Returns a status code. */
+int routec_fock_init(int nshell, const int* am, const int* ncontr, const int* origin, const double* ex,
+                     const double* cc, const int* harmonic, int natom, const double* xyz, double cutoff);
+
+/* The seam itself: replaces fock_jk's native int2 path
+ * (source/scf_addons.F90:1138-1146, routec_bridge.F90:33-40).  All arguments
+ * by reference, Fortran style.  f is overwritten. */
+void routec_fock_jk(const double* d, double* f, const int* nbf, const int* nfocks, const double* se,
+                    const double* sc, int* info);
+
+/* Incremental build F = F_old + G(D - D_old), F_old <- F: the branch of fock_jk
+ * taken when f_old is present (source/scf_addons.F90:1207-1210, 2036-2043),
+ * which the reference seam declines (scf_addons.F90:1141).  dd = D - D_old. */
+void routec_fock_jk_inc(const double* dd, double* f, double* f_old, const int* nbf, const int* nfocks,
+                        const double* se, const double* sc, int* info);
+
+/* Release the process-global context. */
+void routec_fock_finalize(void);
+
+/* ---- explicit-context API -------------------------------------------- */
+
+typedef struct oqpg_ctx oqpg_ctx;
+
+/* Same arguments as routec_fock_init; *out receives a new context. */
+int oqpg_create(oqpg_ctx** out, int nshell, const int* am, const int* ncontr, const int* origin,
+                const double* ex, const double* cc, const int* harmonic, int natom, const double* xyz,
+                double cutoff);
+int oqpg_destroy(oqpg_ctx* ctx);
+
+/* Number of basis functions, shells and shell pairs of a context. */
+int oqpg_nbf(const oqpg_ctx* ctx);
+
+/* Fock build from host buffers (H2D and D2H copies included). */
+int oqpg_fock_jk(oqpg_ctx* ctx, const double* d, double* f, int nfocks, double se, double sc);
+
+/* Fock build on device buffers: d_device / f_device are packed matrices in
+ * device memory, stream a cudaStream_t (0 = the context's own stream).
+ * Nothing is copied to or from the host except the per-class quartet counts. */
+int oqpg_fock_jk_device(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, double se,
+                        double sc, void* stream);
+
+/* Schwarz bounds sqrt(max |(ab|ab)|) per shell pair, nshell x nshell (host). */
+int oqpg_schwarz(const oqpg_ctx* ctx, double* q);
+
+/* Statistics of the last build, up to n (<= 71) doubles:
+ * [0] quartets computed, [1] primitive quartets, [2] list build ms,
+ * [3] integral kernels ms, [4] total device ms, [5] nbf, [6] shell pairs,
+ * [7 .. 28) quartets per class (la lb|lc ld) in the order of oqpg_class_l,
+ * [28 .. 49) primitive quartets per class, [49 .. 70) kernel ms per class,
+ * [70] kernels launched by the build. */
+int oqpg_stats(const oqpg_ctx* ctx, double* out, int n);
+
+/* Angular momenta (la, lb, lc, ld) of class c (0 <= c < 21). */
+int oqpg_class_l(int c, int* l4);
+
+/* FP64 FMA throughput of the current device (TFLOP/s, FMA = 2 flops) from an
+ * FMA-chain probe kernel; the denominator of the kernels' FP64 roofline. */
+int oqpg_measure_fp64_peak(int iters, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPENQP_GB300_H */

@@ -1,0 +1,54 @@
+"""Loader of libopenqp_gb300.so (the CUDA library behind the C ABI).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+usable, every entry point raises.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+_lib = None
+_d = ctypes.POINTER(ctypes.c_double)
+_i = ctypes.POINTER(ctypes.c_int)
+
+STATUS = {0: "ok", 1: "not initialised", 2: "out of device memory", 3: "unsupported input", 4: "device error"}
+
+
+class FockError(RuntimeError):
+    def __init__(self, code, what):
+        super().__init__("%s failed: %s (status %d)" % (what, STATUS.get(code, "unknown"), code))
+        self.code = code
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            raise RuntimeError("libopenqp_gb300.so is not built (%s); run openqp_gb300.build.build() "
+                               "or __graft_entry__.build() first" % path)
+        L = ctypes.CDLL(path)
+        L.oqpg_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _i, _i, _i, _d, _d, _i, ctypes.c_int,
+                                  _d, ctypes.c_double]
+        L.oqpg_destroy.argtypes = [ctypes.c_void_p]
+        L.oqpg_nbf.argtypes = [ctypes.c_void_p]
+        L.oqpg_fock_jk.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.oqpg_fock_jk_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+        L.oqpg_schwarz.argtypes = [ctypes.c_void_p, _d]
+        L.oqpg_stats.argtypes = [ctypes.c_void_p, _d, ctypes.c_int]
+        L.oqpg_class_l.argtypes = [ctypes.c_int, _i]
+        L.oqpg_measure_fp64_peak.argtypes = [ctypes.c_int, _d]
+        L.routec_fock_init.argtypes = [ctypes.c_int, _i, _i, _i, _d, _d, _i, ctypes.c_int, _d, ctypes.c_double]
+        L.routec_fock_jk.argtypes = [_d, _d, _i, _i, _d, _d, _i]
+        L.routec_fock_jk.restype = None
+        L.routec_fock_jk_inc.argtypes = [_d, _d, _d, _i, _i, _d, _d, _i]
+        L.routec_fock_jk_inc.restype = None
+        L.routec_fock_finalize.restype = None
+        _lib = L
+    return _lib
+
+
+def ptr(a, t=_d):
+    return a.ctypes.data_as(t)

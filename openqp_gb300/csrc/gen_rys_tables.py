@@ -153,24 +153,27 @@ def main():
         "// Interval k covers [a_k, a_k + h_k): unit width below %d, width %d above," % (X_SPLIT, W_HI),
         "// up to RYS_XMAX[n]; per interval and root: %d monomial coefficients of x_i," % NCOEF,
         "// then %d of w_i, in s = 2 (X - a_k) / h_k - 1, lowest order first." % NCOEF,
+        "#ifndef RYS_STORAGE",
+        "#define RYS_STORAGE static const",
+        "#endif",
         "#define RYS_NMAX %d" % NMAX,
         "#define RYS_NCOEF %d" % NCOEF,
         "#define RYS_X_SPLIT %d" % X_SPLIT,
         "#define RYS_W_HI %d" % W_HI,
     ]
-    lines.append("static const double RYS_XMAX[%d] = {0.0, %s};" % (
+    lines.append("RYS_STORAGE double RYS_XMAX[%d] = {0.0, %s};" % (
         NMAX + 1, ", ".join("%d.0" % XMAX[n] for n in range(1, NMAX + 1))))
     offs = [0]
     for n in range(1, NMAX + 1):
         offs.append(offs[-1] + len(tables[n]) * 2 * n * NCOEF)
-    lines.append("static const int RYS_OFFSET[%d] = {%s};" % (NMAX + 1, ", ".join(str(o) for o in offs[:-1])))
+    lines.append("RYS_STORAGE int RYS_OFFSET[%d] = {%s};" % (NMAX + 1, ", ".join(str(o) for o in offs[:-1])))
     lines.append("#define RYS_TABLE_SIZE %d" % offs[-1])
     vals = []
     for n in range(1, NMAX + 1):
         for rows in tables[n]:
             for c in rows:
                 vals.extend(repr(float(v)) for v in c)
-    lines.append("static const double RYS_TABLE[RYS_TABLE_SIZE] = {")
+    lines.append("RYS_STORAGE double RYS_TABLE[RYS_TABLE_SIZE] = {")
     for i in range(0, len(vals), 4):
         lines.append("  " + ", ".join(vals[i:i + 4]) + ",")
     lines.append("};")
@@ -179,8 +182,8 @@ def main():
         hr.extend(repr(float(v)) for v in herm[n][0])
         hw.extend(repr(float(v)) for v in herm[n][1])
     lines.append("// large-X limit: x_i = RYS_HERM_R2[o+i] / X, w_i = RYS_HERM_W[o+i] / sqrt(X), o = n(n-1)/2")
-    lines.append("static const double RYS_HERM_R2[%d] = {%s};" % (len(hr), ", ".join(hr)))
-    lines.append("static const double RYS_HERM_W[%d] = {%s};" % (len(hw), ", ".join(hw)))
+    lines.append("RYS_STORAGE double RYS_HERM_R2[%d] = {%s};" % (len(hr), ", ".join(hr)))
+    lines.append("RYS_STORAGE double RYS_HERM_W[%d] = {%s};" % (len(hw), ", ".join(hw)))
     with open(os.path.join(here, "rys_tables.inc"), "w") as fh:
         fh.write("\n".join(lines) + "\n")
 

@@ -1,0 +1,38 @@
+// The 21 (la lb | lc ld) classes of s-d quartets in kernel orientation and
+// the launchers of their kernels (one translation unit per group of classes).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "oqpg_common.cuh"
+
+namespace oqpg {
+
+constexpr int NPAIRTYPE = 6;   // ss sp sd pp pd dd  (la <= lb)
+constexpr int NCLASS = 21;     // pair type of bra <= pair type of ket
+constexpr int PAIR_L[NPAIRTYPE][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+
+inline int pair_type(int la, int lb) {  // la <= lb
+  return la == 0 ? lb : (la == 1 ? 2 + lb : 5);
+}
+inline int class_index(int tbra, int tket) {  // tbra <= tket
+  return tbra * NPAIRTYPE - tbra * (tbra - 1) / 2 + (tket - tbra);
+}
+
+struct ClassInfo {
+  int l[4];
+  int team;        // 1: one warp per quartet, 0: one thread per quartet
+  int smem_warp;   // doubles of shared memory per warp (team kernels), Cartesian / pure
+  int smem_warp_pure;
+};
+const ClassInfo& class_info(int c);
+
+// Launch the Fock-build (sch = false) or Schwarz (sch = true) kernel of class c.
+cudaError_t launch_class(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st);
+
+// group launchers (defined in oqpg_cls_*.cu)
+cudaError_t launch_group0(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group1(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group2(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group3(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st);
+
+}  // namespace oqpg

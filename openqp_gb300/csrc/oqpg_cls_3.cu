@@ -1,0 +1,16 @@
+// Kernel instantiations of one group of (la lb | lc ld) classes.
+// Generated layout: each group is its own translation unit so the build compiles them in parallel.
+#include "oqpg_launch.cuh"
+
+namespace oqpg {
+
+cudaError_t launch_group3(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st) {
+  switch (c) {
+    case 18: return launch_cls<1, 2, 1, 2>(pure, sch, a, nsm, st);
+    case 19: return launch_cls<1, 2, 2, 2>(pure, sch, a, nsm, st);
+    case 20: return launch_cls<2, 2, 2, 2>(pure, sch, a, nsm, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace oqpg

@@ -1,0 +1,93 @@
+// Device-side building blocks of the GB300 direct J/K Fock build: shell and
+// pair tables, Cartesian component tables, Rys root evaluation and the
+// per-primitive-quartet Rys coefficients.
+//
+// FP64 is the binding resource on GB300 (about 2 FP64 FMA lanes per clock per
+// SM, 64x below FP32), so everything here is written to minimise FP64
+// instructions: integer/FP32 work is effectively free next to it.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace oqpg {
+
+// ---------------------------------------------------------------------------
+// Tables resident in device memory (one set per registered molecule).
+struct ShellDev {
+  double x, y, z;
+  int am, nao, aoff, harm;
+};
+
+// One primitive pair of a shell pair (bra or ket), 80 bytes.
+struct PrimPair {
+  double p;      // exponent sum
+  double hp;     // 0.5 / p
+  double px, py, pz;     // Gaussian product centre
+  double ax, ay, az;     // P - A (A: first shell of the pair in kernel orientation)
+  double sp;     // K / p with K = sqrt(2) pi^(5/4) c_a c_b exp(-a b |AB|^2 / p)
+  double pad;
+};
+
+struct PairDev {
+  int sha, shb;    // kernel orientation: am(sha) <= am(shb)
+  int poff, pcnt;  // primitive-pair range
+};
+
+// Parameters of one Fock build (or Schwarz pass) shared by the class kernels.
+struct BuildArgs {
+  const ShellDev* shells;
+  const PairDev* pairs;
+  const PrimPair* prims;
+  const uint2* quartets;   // (bra pair, ket pair) per quartet of this class
+  long long nquartets;
+  int nbf;
+  int nk;                  // number of exchange densities (1 RHF, 2 UHF/ROHF)
+  double prim_cut;         // |K/p| pre-screen of a primitive pair
+  double prim_cut2;        // (sp sq)^2 < prim_cut2 (p + q) skips a primitive quartet
+  double elem_cut;         // element cutoff on |(ab|cd)|
+  const double* dj;        // full nbf x nbf density for Coulomb
+  const double* dk;        // nk full densities for exchange
+  double* gj;              // nbf x nbf Coulomb accumulator
+  double* gk;              // nk x nbf x nbf exchange accumulators
+  double* schwarz_out;     // Schwarz mode: per pair sqrt(max |(ab|ab)|)
+  unsigned long long* counters;  // [0] primitive quartets evaluated by this launch
+};
+
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+
+// Cartesian exponents in OpenQP order: s; x y z; xx yy zz xy xz yz.
+__host__ __device__ constexpr int cart_e(int l, int idx, int dim) {
+  return l == 0 ? 0
+       : l == 1 ? (idx == dim ? 1 : 0)
+       : (idx < 3 ? (idx == dim ? 2 : 0)
+          : idx == 3 ? (dim < 2 ? 1 : 0)
+          : idx == 4 ? (dim != 1 ? 1 : 0)
+                     : (dim > 0 ? 1 : 0));
+}
+// shells_pnrm2 for l <= 2 (individually normalised Cartesians)
+__host__ __device__ constexpr double cart_norm(int l, int idx) {
+  return (l == 2 && idx >= 3) ? 1.7320508075688772 : 1.0;
+}
+
+// FP64 reciprocal / reciprocal square root: hardware approximation refined by
+// two Newton steps (4 FP64 FMA for 1/x, 6 for 1/sqrt(x)); exact to ~1 ulp.
+__device__ __forceinline__ double rcp64(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+__device__ __forceinline__ double rsqrt64(double x) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  const double hx = 0.5 * x;
+  double t = fma(-hx * y, y, 0.5);
+  y = fma(y, t, y);
+  t = fma(-hx * y, y, 0.5);
+  return fma(y, t, y);
+}
+
+}  // namespace oqpg

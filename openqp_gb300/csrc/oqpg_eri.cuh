@@ -1,0 +1,636 @@
+// Class-specialised FP64 shell-quartet kernels: Rys quadrature ERIs contracted
+// on the fly into Coulomb / exchange accumulators.
+//
+// One instantiation per (la lb | lc ld) class (la <= lb, lc <= ld, bra pair
+// type <= ket pair type), per AO convention of the d shells (Cartesian or
+// pure), and per mode (Fock build or Schwarz bound).
+//
+//   k_small : one thread per quartet, everything in registers (classes with at
+//             most 27 Cartesian elements).
+//   k_team  : one warp per quartet.  Lanes share the primitive loop: Rys
+//             roots/weights (one quantity per lane), the 2D integrals (one
+//             root x dimension per lane) go to shared memory, each lane
+//             accumulates its own subset of the Cartesian elements; the
+//             digestion distributes the J/K target elements over the lanes.
+//
+// The integral algebra follows Rys, Dupuis & King (J. Comput. Chem. 4, 154
+// (1983)): per root t^2 = u, with s = p + q,
+//   B00 = u / 2s, B10 = (1 - u q/s) / 2p, B01 = (1 - u p/s) / 2q,
+//   C00 = (P - A) - u (q/s) (P - Q),   D00 = (Q - C) + u (p/s) (P - Q),
+//   I(n+1,0) = C00 I(n,0) + n B10 I(n-1,0)
+//   I(n,m+1) = D00 I(n,m) + m B01 I(n,m-1) + n B00 I(n-1,m)
+// followed by the horizontal transfers I(i,j+1) = I(i+1,j) + (A-B) I(i,j)
+// on each pair (the structure of OpenQP's int_rys.F90:529-661).  Screening
+// thresholds and the element cutoff follow OpenQP's s-d path
+// (int_rotaxis.F90:292-306,629; int2.F90:1806-1812).
+#pragma once
+#include "oqpg_common.cuh"
+
+namespace oqpg {
+
+#define RYS_STORAGE static __device__ const
+#include "rys_tables.inc"
+#undef RYS_STORAGE
+
+__host__ __device__ constexpr int rys_xmax(int n) { return 32 + 8 * n; }
+__host__ __device__ constexpr int rys_offset(int n) {  // start of the n-root table
+  return n <= 1 ? 0 : rys_offset(n - 1) + (32 + 2 * (n - 1)) * 2 * (n - 1) * RYS_NCOEF;
+}
+
+// Quantity q of the N-root rule at X: q even -> node x_{q/2}, q odd -> weight w_{q/2}.
+template <int N>
+__device__ __forceinline__ double rys_quantity(double X, int q) {
+  if (X >= (double)rys_xmax(N)) {
+    const int r = (N * (N - 1)) / 2 + (q >> 1);
+    return (q & 1) ? RYS_HERM_W[r] * rsqrt64(X) : RYS_HERM_R2[r] * rcp64(X);
+  }
+  int k;
+  double s;
+  if (X < (double)RYS_X_SPLIT) {
+    k = __double2int_rz(X);
+    s = fma(2.0, X, -(double)(2 * k + 1));
+  } else {
+    k = RYS_X_SPLIT + __double2int_rz((X - (double)RYS_X_SPLIT) * 0.25);
+    s = fma(0.5, X, -(double)(RYS_X_SPLIT / 2 + 2 * (k - RYS_X_SPLIT) + 1));
+  }
+  const double* c = RYS_TABLE + rys_offset(N) + (k * 2 * N + q) * RYS_NCOEF;
+  double v = __ldg(c + RYS_NCOEF - 1);
+#pragma unroll
+  for (int i = RYS_NCOEF - 2; i >= 0; --i) v = fma(v, s, __ldg(c + i));
+  return v;
+}
+
+__host__ __device__ constexpr int naos(int l, bool pure) { return (pure && l == 2) ? 5 : ncart(l); }
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+
+// Pure-d projection row m, Cartesian component c (m = -2..2: xy, yz, z^2, xz, x^2-y^2)
+__host__ __device__ constexpr double pure_d(int m, int c) {
+  return m == 0 ? (c == 3 ? 1.0 : 0.0)
+       : m == 1 ? (c == 5 ? 1.0 : 0.0)
+       : m == 2 ? (c == 2 ? 1.0 : (c < 2 ? -0.5 : 0.0))
+       : m == 3 ? (c == 4 ? 1.0 : 0.0)
+                : (c == 0 ? 0.86602540378443865 : (c == 1 ? -0.86602540378443865 : 0.0));
+}
+
+// Per-primitive-quartet scalars shared by all roots.
+struct PrimQuartet {
+  double inv, qi, pi, pref, X;
+  double PQ[3];
+};
+
+__device__ __forceinline__ bool prim_quartet(const PrimPair& bp, const PrimPair& kp, double cut2, PrimQuartet& o) {
+  const double fqz = bp.sp * kp.sp;
+  const double s = bp.p + kp.p;
+  if (fqz * fqz < cut2 * s) return false;
+  o.inv = rcp64(s);
+  o.qi = kp.p * o.inv;
+  o.pi = bp.p * o.inv;
+  o.PQ[0] = bp.px - kp.px;
+  o.PQ[1] = bp.py - kp.py;
+  o.PQ[2] = bp.pz - kp.pz;
+  const double r2 = fma(o.PQ[0], o.PQ[0], fma(o.PQ[1], o.PQ[1], o.PQ[2] * o.PQ[2]));
+  o.X = bp.p * o.qi * r2;
+  o.pref = fqz * rsqrt64(s);
+  return true;
+}
+
+// 2D integrals of one root and one Cartesian dimension:
+// out[((i*(LB+1)+j)*(LC+1)+k)*(LD+1)+l], i<=LA, j<=LB, k<=LC, l<=LD.
+template <int LA, int LB, int LC, int LD, typename Out>
+__device__ __forceinline__ void twod(double g00, double c00, double d00, double b00, double b10, double b01,
+                                     double ab, double cd, Out&& out) {
+  constexpr int NMAX = LA + LB, MMAX = LC + LD;
+  double G[NMAX + 1][MMAX + 1];
+  G[0][0] = g00;
+  if (NMAX > 0) G[1][0] = c00 * g00;
+#pragma unroll
+  for (int n = 1; n < NMAX; ++n) G[n + 1][0] = fma(c00, G[n][0], (double)n * b10 * G[n - 1][0]);
+#pragma unroll
+  for (int m = 0; m < MMAX; ++m) {
+#pragma unroll
+    for (int n = 0; n <= NMAX; ++n) {
+      double v = d00 * G[n][m];
+      if (m > 0) v = fma((double)m * b01, G[n][m - 1], v);
+      if (n > 0) v = fma((double)n * b00, G[n - 1][m], v);
+      G[n][m + 1] = v;
+    }
+  }
+  // bra transfer: H[i][j][m]
+  double H[LA + 1][LB + 1][MMAX + 1];
+#pragma unroll
+  for (int m = 0; m <= MMAX; ++m) {
+    double col[NMAX + 1];
+#pragma unroll
+    for (int i = 0; i <= NMAX; ++i) col[i] = G[i][m];
+#pragma unroll
+    for (int i = 0; i <= LA; ++i) H[i][0][m] = col[i];
+#pragma unroll
+    for (int j = 1; j <= LB; ++j) {
+#pragma unroll
+      for (int i = 0; i <= NMAX - j; ++i) col[i] = fma(ab, col[i], col[i + 1]);
+#pragma unroll
+      for (int i = 0; i <= LA; ++i) H[i][j][m] = col[i];
+    }
+  }
+  // ket transfer
+#pragma unroll
+  for (int i = 0; i <= LA; ++i)
+#pragma unroll
+    for (int j = 0; j <= LB; ++j) {
+      double col[MMAX + 1];
+#pragma unroll
+      for (int k = 0; k <= MMAX; ++k) col[k] = H[i][j][k];
+#pragma unroll
+      for (int k = 0; k <= LC; ++k) out(((i * (LB + 1) + j) * (LC + 1) + k) * (LD + 1) + 0, col[k]);
+#pragma unroll
+      for (int l = 1; l <= LD; ++l) {
+#pragma unroll
+        for (int k = 0; k <= MMAX - l; ++k) col[k] = fma(cd, col[k], col[k + 1]);
+#pragma unroll
+        for (int k = 0; k <= LC; ++k) out(((i * (LB + 1) + j) * (LC + 1) + k) * (LD + 1) + l, col[k]);
+      }
+    }
+}
+
+template <int LA, int LB, int LC, int LD>
+struct Cls {
+  static constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+  static constexpr int NE = NA * NB * NC * ND;
+  static constexpr int NR = (LA + LB + LC + LD) / 2 + 1;
+  static constexpr int N2D = (LA + 1) * (LB + 1) * (LC + 1) * (LD + 1);
+  // 2D-table offset of Cartesian element e along dimension dim
+  __host__ __device__ static constexpr int off2d(int e, int dim) {
+    return ((cart_e(LA, e / (NB * NC * ND), dim) * (LB + 1) + cart_e(LB, (e / (NC * ND)) % NB, dim)) * (LC + 1) +
+            cart_e(LC, (e / ND) % NC, dim)) * (LD + 1) + cart_e(LD, e % ND, dim);
+  }
+  __host__ __device__ static constexpr double norm(int e) {
+    return cart_norm(LA, e / (NB * NC * ND)) * cart_norm(LB, (e / (NC * ND)) % NB) * cart_norm(LC, (e / ND) % NC) *
+           cart_norm(LD, e % ND);
+  }
+};
+
+__device__ __forceinline__ void prim_load(const PrimPair* __restrict__ src, PrimPair& d) {
+  const double2* s = reinterpret_cast<const double2*>(src);
+  double2 v0 = __ldg(s), v1 = __ldg(s + 1), v2 = __ldg(s + 2), v3 = __ldg(s + 3), v4 = __ldg(s + 4);
+  d.p = v0.x; d.hp = v0.y; d.px = v1.x; d.py = v1.y; d.pz = v2.x; d.ax = v2.y; d.ay = v3.x; d.az = v3.y;
+  d.sp = v4.x; d.pad = v4.y;
+}
+
+__device__ __forceinline__ double pick3(int d, double a, double b, double c) { return d == 0 ? a : (d == 1 ? b : c); }
+
+// ---------------------------------------------------------------------------
+// Epilogue shared by both paths once the contracted Cartesian block is known:
+// normalisation, optional pure-d projection, element cutoff, and either the
+// Schwarz maximum or the J/K digestion with degeneracy factor f.
+template <int LA, int LB, int LC, int LD, bool PURE>
+struct Epi {
+  static constexpr int A = naos(LA, PURE), B = naos(LB, PURE), C = naos(LC, PURE), D = naos(LD, PURE);
+  static constexpr int NEP = A * B * C * D;
+};
+
+// In-register pure projection of one index (compile-time dims).
+template <int D0, int D1, int D2, int D3, int POS, bool DO>
+__device__ __forceinline__ void project_regs(const double* in, double* out) {
+  constexpr int DIMS[4] = {D0, D1, D2, D3};
+  constexpr int PRE = POS == 0 ? 1 : (POS == 1 ? D0 : (POS == 2 ? D0 * D1 : D0 * D1 * D2));
+  constexpr int N = DIMS[POS];
+  constexpr int POST = POS == 3 ? 1 : (POS == 2 ? D3 : (POS == 1 ? D2 * D3 : D1 * D2 * D3));
+  if (!DO) {
+#pragma unroll
+    for (int i = 0; i < PRE * N * POST; ++i) out[i] = in[i];
+    return;
+  }
+#pragma unroll
+  for (int a = 0; a < PRE; ++a)
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+#pragma unroll
+      for (int p = 0; p < POST; ++p) {
+        double v = 0.0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c)
+          if (pure_d(m, c) != 0.0) v = fma(pure_d(m, c), in[(a * N + c) * POST + p], v);
+        out[(a * 5 + m) * POST + p] = v;
+      }
+}
+
+__device__ __forceinline__ double cut_elem(double v, double cut) { return fabs(v) < cut ? 0.0 : v; }
+
+// ===========================================================================
+// Small classes: one thread per quartet.
+template <int LA, int LB, int LC, int LD, bool PURE, bool SCH>
+__global__ void __launch_bounds__(128) k_small(const BuildArgs a) {
+  using K = Cls<LA, LB, LC, LD>;
+  using E = Epi<LA, LB, LC, LD, PURE>;
+  constexpr int NE = K::NE, NR = K::NR, N2D = K::N2D;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  unsigned long long nprim = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < a.nquartets; t += stride) {
+    const uint2 qd = a.quartets[t];
+    const PairDev P = a.pairs[qd.x], Q = a.pairs[qd.y];
+    const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
+    const double AB[3] = {SA.x - SB.x, SA.y - SB.y, SA.z - SB.z};
+    const double CD[3] = {SC.x - SD.x, SC.y - SD.y, SC.z - SD.z};
+    double acc[NE];
+#pragma unroll
+    for (int e = 0; e < NE; ++e) acc[e] = 0.0;
+    for (int kq = 0; kq < Q.pcnt; ++kq) {
+      PrimPair kp;
+      prim_load(a.prims + Q.poff + kq, kp);
+      for (int kb = 0; kb < P.pcnt; ++kb) {
+        PrimPair bp;
+        prim_load(a.prims + P.poff + kb, bp);
+        PrimQuartet pq;
+        if (!prim_quartet(bp, kp, a.prim_cut2, pq)) continue;
+        ++nprim;
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+          const double u = rys_quantity<NR>(pq.X, 2 * r);
+          const double w = rys_quantity<NR>(pq.X, 2 * r + 1) * pq.pref;
+          const double uq = u * pq.qi, up = u * pq.pi;
+          const double b00 = 0.5 * pq.inv * u;
+          const double b10 = fma(-bp.hp, uq, bp.hp);
+          const double b01 = fma(-kp.hp, up, kp.hp);
+          double I[3][N2D];
+          const double PA[3] = {bp.ax, bp.ay, bp.az}, QC[3] = {kp.ax, kp.ay, kp.az};
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const double c00 = fma(-uq, pq.PQ[d], PA[d]);
+            const double d00 = fma(up, pq.PQ[d], QC[d]);
+            twod<LA, LB, LC, LD>(d == 2 ? w : 1.0, c00, d00, b00, b10, b01, AB[d], CD[d],
+                                 [&](int i, double v) { I[d][i] = v; });
+          }
+#pragma unroll
+          for (int e = 0; e < NE; ++e)
+            acc[e] = fma(I[0][K::off2d(e, 0)] * I[1][K::off2d(e, 1)], I[2][K::off2d(e, 2)], acc[e]);
+        }
+      }
+    }
+    // normalise and project
+#pragma unroll
+    for (int e = 0; e < NE; ++e) acc[e] *= K::norm(e);
+    constexpr int DA = K::NA, DB = K::NB, DC = K::NC, DD = K::ND;
+    double t1[NE], t2[NE];
+    project_regs<DA, DB, DC, DD, 0, PURE && LA == 2>(acc, t1);
+    project_regs<E::A, DB, DC, DD, 1, PURE && LB == 2>(t1, t2);
+    project_regs<E::A, E::B, DC, DD, 2, PURE && LC == 2>(t2, t1);
+    project_regs<E::A, E::B, E::C, DD, 3, PURE && LD == 2>(t1, t2);
+    double* V = t2;
+    if (SCH) {
+      double m = 0.0;
+#pragma unroll
+      for (int e = 0; e < E::NEP; ++e) m = fmax(m, fabs(V[e]));
+      a.schwarz_out[qd.x] = sqrt(m);
+      continue;
+    }
+#pragma unroll
+    for (int e = 0; e < E::NEP; ++e) V[e] = cut_elem(V[e], a.elem_cut);
+    double f = 1.0;
+    if (P.sha == P.shb) f *= 0.5;
+    if (Q.sha == Q.shb) f *= 0.5;
+    if (qd.x == qd.y) f *= 0.5;
+    const int n = a.nbf;
+    const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
+    // Coulomb: G_J[ab] += 2f sum_cd V D_cd ; G_J[cd] += 2f sum_ab V D_ab
+    {
+      double dab[E::A * E::B], dcd[E::C * E::D];
+#pragma unroll
+      for (int i = 0; i < E::A; ++i)
+#pragma unroll
+        for (int j = 0; j < E::B; ++j) dab[i * E::B + j] = __ldg(a.dj + (size_t)(oa + i) * n + ob + j);
+#pragma unroll
+      for (int i = 0; i < E::C; ++i)
+#pragma unroll
+        for (int j = 0; j < E::D; ++j) dcd[i * E::D + j] = __ldg(a.dj + (size_t)(oc + i) * n + od + j);
+      double jab[E::A * E::B], jcd[E::C * E::D];
+#pragma unroll
+      for (int i = 0; i < E::A * E::B; ++i) jab[i] = 0.0;
+#pragma unroll
+      for (int i = 0; i < E::C * E::D; ++i) jcd[i] = 0.0;
+#pragma unroll
+      for (int ab = 0; ab < E::A * E::B; ++ab)
+#pragma unroll
+        for (int cd = 0; cd < E::C * E::D; ++cd) {
+          const double v = V[ab * E::C * E::D + cd];
+          jab[ab] = fma(v, dcd[cd], jab[ab]);
+          jcd[cd] = fma(v, dab[ab], jcd[cd]);
+        }
+      const double f2 = 2.0 * f;
+#pragma unroll
+      for (int i = 0; i < E::A; ++i)
+#pragma unroll
+        for (int j = 0; j < E::B; ++j) atomicAdd(a.gj + (size_t)(oa + i) * n + ob + j, f2 * jab[i * E::B + j]);
+#pragma unroll
+      for (int i = 0; i < E::C; ++i)
+#pragma unroll
+        for (int j = 0; j < E::D; ++j) atomicAdd(a.gj + (size_t)(oc + i) * n + od + j, f2 * jcd[i * E::D + j]);
+    }
+    // Exchange: G_K[ac] += f sum V D_bd ; [ad] += f V D_bc ; [bc] += f V D_ad ; [bd] += f V D_ac
+    for (int kk = 0; kk < a.nk; ++kk) {
+      const double* dk = a.dk + (size_t)kk * n * n;
+      double* gk = a.gk + (size_t)kk * n * n;
+      double dac[E::A * E::C], dad[E::A * E::D], dbc[E::B * E::C], dbd[E::B * E::D];
+#pragma unroll
+      for (int i = 0; i < E::A; ++i) {
+#pragma unroll
+        for (int j = 0; j < E::C; ++j) dac[i * E::C + j] = __ldg(dk + (size_t)(oa + i) * n + oc + j);
+#pragma unroll
+        for (int j = 0; j < E::D; ++j) dad[i * E::D + j] = __ldg(dk + (size_t)(oa + i) * n + od + j);
+      }
+#pragma unroll
+      for (int i = 0; i < E::B; ++i) {
+#pragma unroll
+        for (int j = 0; j < E::C; ++j) dbc[i * E::C + j] = __ldg(dk + (size_t)(ob + i) * n + oc + j);
+#pragma unroll
+        for (int j = 0; j < E::D; ++j) dbd[i * E::D + j] = __ldg(dk + (size_t)(ob + i) * n + od + j);
+      }
+      double kac[E::A * E::C], kad[E::A * E::D], kbc[E::B * E::C], kbd[E::B * E::D];
+#pragma unroll
+      for (int i = 0; i < E::A * E::C; ++i) kac[i] = 0.0;
+#pragma unroll
+      for (int i = 0; i < E::A * E::D; ++i) kad[i] = 0.0;
+#pragma unroll
+      for (int i = 0; i < E::B * E::C; ++i) kbc[i] = 0.0;
+#pragma unroll
+      for (int i = 0; i < E::B * E::D; ++i) kbd[i] = 0.0;
+#pragma unroll
+      for (int i = 0; i < E::A; ++i)
+#pragma unroll
+        for (int j = 0; j < E::B; ++j)
+#pragma unroll
+          for (int k = 0; k < E::C; ++k)
+#pragma unroll
+            for (int l = 0; l < E::D; ++l) {
+              const double v = V[((i * E::B + j) * E::C + k) * E::D + l];
+              kac[i * E::C + k] = fma(v, dbd[j * E::D + l], kac[i * E::C + k]);
+              kad[i * E::D + l] = fma(v, dbc[j * E::C + k], kad[i * E::D + l]);
+              kbc[j * E::C + k] = fma(v, dad[i * E::D + l], kbc[j * E::C + k]);
+              kbd[j * E::D + l] = fma(v, dac[i * E::C + k], kbd[j * E::D + l]);
+            }
+#pragma unroll
+      for (int i = 0; i < E::A; ++i) {
+#pragma unroll
+        for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(oa + i) * n + oc + j, f * kac[i * E::C + j]);
+#pragma unroll
+        for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(oa + i) * n + od + j, f * kad[i * E::D + j]);
+      }
+#pragma unroll
+      for (int i = 0; i < E::B; ++i) {
+#pragma unroll
+        for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(ob + i) * n + oc + j, f * kbc[i * E::C + j]);
+#pragma unroll
+        for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(ob + i) * n + od + j, f * kbd[i * E::D + j]);
+      }
+    }
+  }
+  if (a.counters && nprim) atomicAdd(a.counters, nprim);
+}
+
+// ===========================================================================
+// Large classes: one warp per quartet.
+template <int LA, int LB, int LC, int LD, bool PURE>
+struct TeamSmem {
+  using K = Cls<LA, LB, LC, LD>;
+  using E = Epi<LA, LB, LC, LD, PURE>;
+  static constexpr int PH1 = 2 * K::NR + K::NR * 3 * K::N2D;
+  static constexpr int DJ = E::A * E::B + E::C * E::D;
+  static constexpr int DK = E::A * E::C + E::A * E::D + E::B * E::C + E::B * E::D;
+  static constexpr int PH2 = 2 * K::NE + DJ + 2 * DK;
+  static constexpr int PER_WARP = cmax(PH1, PH2);
+};
+
+template <int LA, int LB, int LC, int LD, bool PURE, bool SCH>
+__global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
+  using K = Cls<LA, LB, LC, LD>;
+  using E = Epi<LA, LB, LC, LD, PURE>;
+  using SM = TeamSmem<LA, LB, LC, LD, PURE>;
+  constexpr int NE = K::NE, NR = K::NR, N2D = K::N2D, KE = (NE + 31) / 32;
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double* W = smem + warp * SM::PER_WARP;
+  double* RT = W;               // 2*NR: x_r, w_r * pref
+  double* I2 = W + 2 * NR;      // [r][d][N2D]
+  // packed 2D offsets of this lane's elements (same for every quartet)
+  int offs[KE];
+#pragma unroll
+  for (int k = 0; k < KE; ++k) {
+    const int e = lane + 32 * k;
+    int o = 0;
+    if (e < NE) {
+      const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
+                id = e % K::ND;
+      int ox[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const int ea = (LA == 0) ? 0 : (LA == 1 ? (ia == d) : (ia < 3 ? 2 * (ia == d) : (ia == 3 ? (d < 2) : ia == 4 ? (d != 1) : (d > 0))));
+        const int eb = (LB == 0) ? 0 : (LB == 1 ? (ib == d) : (ib < 3 ? 2 * (ib == d) : (ib == 3 ? (d < 2) : ib == 4 ? (d != 1) : (d > 0))));
+        const int ec = (LC == 0) ? 0 : (LC == 1 ? (ic == d) : (ic < 3 ? 2 * (ic == d) : (ic == 3 ? (d < 2) : ic == 4 ? (d != 1) : (d > 0))));
+        const int ed = (LD == 0) ? 0 : (LD == 1 ? (id == d) : (id < 3 ? 2 * (id == d) : (id == 3 ? (d < 2) : id == 4 ? (d != 1) : (d > 0))));
+        ox[d] = ((ea * (LB + 1) + eb) * (LC + 1) + ec) * (LD + 1) + ed;
+      }
+      o = ox[0] | (ox[1] << 10) | (ox[2] << 20);
+    }
+    offs[k] = o;
+  }
+  const long long nteams = (long long)gridDim.x * (blockDim.x >> 5);
+  unsigned long long nprim = 0;
+  for (long long t = (long long)blockIdx.x * (blockDim.x >> 5) + warp; t < a.nquartets; t += nteams) {
+    const uint2 qd = a.quartets[t];
+    const PairDev P = a.pairs[qd.x], Q = a.pairs[qd.y];
+    const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
+    const double AB[3] = {SA.x - SB.x, SA.y - SB.y, SA.z - SB.z};
+    const double CD[3] = {SC.x - SD.x, SC.y - SD.y, SC.z - SD.z};
+    double acc[KE];
+#pragma unroll
+    for (int k = 0; k < KE; ++k) acc[k] = 0.0;
+    for (int kq = 0; kq < Q.pcnt; ++kq) {
+      PrimPair kp;
+      prim_load(a.prims + Q.poff + kq, kp);
+      for (int kb = 0; kb < P.pcnt; ++kb) {
+        PrimPair bp;
+        prim_load(a.prims + P.poff + kb, bp);
+        PrimQuartet pq;
+        if (!prim_quartet(bp, kp, a.prim_cut2, pq)) continue;
+        ++nprim;
+        if (lane < 2 * NR) {
+          const double v = rys_quantity<NR>(pq.X, lane);
+          RT[lane] = (lane & 1) ? v * pq.pref : v;
+        }
+        __syncwarp();
+        if (lane < 3 * NR) {
+          const int r = lane / 3, d = lane - 3 * r;
+          const double u = RT[2 * r], w = RT[2 * r + 1];
+          const double uq = u * pq.qi, up = u * pq.pi;
+          const double b00 = 0.5 * pq.inv * u;
+          const double b10 = fma(-bp.hp, uq, bp.hp);
+          const double b01 = fma(-kp.hp, up, kp.hp);
+          const double pqd = pick3(d, pq.PQ[0], pq.PQ[1], pq.PQ[2]);
+          const double c00 = fma(-uq, pqd, pick3(d, bp.ax, bp.ay, bp.az));
+          const double d00 = fma(up, pqd, pick3(d, kp.ax, kp.ay, kp.az));
+          double* dst = I2 + (r * 3 + d) * N2D;
+          twod<LA, LB, LC, LD>(d == 2 ? w : 1.0, c00, d00, b00, b10, b01, pick3(d, AB[0], AB[1], AB[2]),
+                               pick3(d, CD[0], CD[1], CD[2]), [&](int i, double v) { dst[i] = v; });
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < KE; ++k) {
+          if (lane + 32 * k < NE) {
+            const int ox = offs[k] & 1023, oy = (offs[k] >> 10) & 1023, oz = offs[k] >> 20;
+            double v = acc[k];
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+              const double* g = I2 + r * 3 * N2D;
+              v = fma(g[ox] * g[N2D + oy], g[2 * N2D + oz], v);
+            }
+            acc[k] = v;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    // ---- epilogue: V = normalised block in smem, pure projection in place
+    double* V = W;
+    double* T = W + NE;
+#pragma unroll
+    for (int k = 0; k < KE; ++k) {
+      const int e = lane + 32 * k;
+      if (e < NE) {
+        const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
+                  id = e % K::ND;
+        const double nrm = (LA == 2 && ia >= 3 ? 1.7320508075688772 : 1.0) * (LB == 2 && ib >= 3 ? 1.7320508075688772 : 1.0) *
+                           (LC == 2 && ic >= 3 ? 1.7320508075688772 : 1.0) * (LD == 2 && id >= 3 ? 1.7320508075688772 : 1.0);
+        V[e] = (LA == 2 || LB == 2 || LC == 2 || LD == 2) ? acc[k] * nrm : acc[k];
+      }
+    }
+    __syncwarp();
+    int dims[4] = {K::NA, K::NB, K::NC, K::ND};
+    if (PURE) {
+      const int ls[4] = {LA, LB, LC, LD};
+#pragma unroll
+      for (int pos = 0; pos < 4; ++pos) {
+        if (ls[pos] != 2) continue;
+        int pre = 1, post = 1;
+        for (int i = 0; i < pos; ++i) pre *= dims[i];
+        for (int i = pos + 1; i < 4; ++i) post *= dims[i];
+        const int nout = pre * 5 * post;
+        for (int o = lane; o < nout; o += 32) {
+          const int p = o % post, m = (o / post) % 5, q = o / (5 * post);
+          const double* src = V + (size_t)q * 6 * post + p;
+          double v;
+          if (m == 0) v = src[3 * post];
+          else if (m == 1) v = src[5 * post];
+          else if (m == 2) v = src[2 * post] - 0.5 * (src[0] + src[post]);
+          else if (m == 3) v = src[4 * post];
+          else v = 0.86602540378443865 * (src[0] - src[post]);
+          T[o] = v;
+        }
+        __syncwarp();
+        for (int o = lane; o < nout; o += 32) V[o] = T[o];
+        __syncwarp();
+        dims[pos] = 5;
+      }
+    }
+    constexpr int NEP = E::NEP;
+    if (SCH) {
+      double m = 0.0;
+      for (int e = lane; e < NEP; e += 32) m = fmax(m, fabs(V[e]));
+#pragma unroll
+      for (int s = 16; s > 0; s >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, s));
+      if (lane == 0) a.schwarz_out[qd.x] = sqrt(m);
+      __syncwarp();
+      continue;
+    }
+    for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], a.elem_cut);
+    // density blocks
+    const int n = a.nbf;
+    const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
+    double* Dab = W + NE;                 // after V (NE >= NEP)
+    double* Dcd = Dab + E::A * E::B;
+    double* Dk = Dcd + E::C * E::D;       // per k: ac, ad, bc, bd
+    constexpr int DKS = SM::DK;
+    for (int i = lane; i < E::A * E::B; i += 32) Dab[i] = __ldg(a.dj + (size_t)(oa + i / E::B) * n + ob + i % E::B);
+    for (int i = lane; i < E::C * E::D; i += 32) Dcd[i] = __ldg(a.dj + (size_t)(oc + i / E::D) * n + od + i % E::D);
+    for (int kk = 0; kk < a.nk; ++kk) {
+      const double* dk = a.dk + (size_t)kk * n * n;
+      double* base = Dk + kk * DKS;
+      for (int i = lane; i < E::A * E::C; i += 32) base[i] = __ldg(dk + (size_t)(oa + i / E::C) * n + oc + i % E::C);
+      base += E::A * E::C;
+      for (int i = lane; i < E::A * E::D; i += 32) base[i] = __ldg(dk + (size_t)(oa + i / E::D) * n + od + i % E::D);
+      base += E::A * E::D;
+      for (int i = lane; i < E::B * E::C; i += 32) base[i] = __ldg(dk + (size_t)(ob + i / E::C) * n + oc + i % E::C);
+      base += E::B * E::C;
+      for (int i = lane; i < E::B * E::D; i += 32) base[i] = __ldg(dk + (size_t)(ob + i / E::D) * n + od + i % E::D);
+    }
+    __syncwarp();
+    double f = 1.0;
+    if (P.sha == P.shb) f *= 0.5;
+    if (Q.sha == Q.shb) f *= 0.5;
+    if (qd.x == qd.y) f *= 0.5;
+    constexpr int NAB = E::A * E::B, NCD = E::C * E::D;
+    constexpr int NAC = E::A * E::C, NAD = E::A * E::D, NBC = E::B * E::C, NBD = E::B * E::D;
+    const int ntarget = NAB + NCD + a.nk * (NAC + NAD + NBC + NBD);
+    for (int o = lane; o < ntarget; o += 32) {
+      double s = 0.0;
+      double* dst;
+      double fac;
+      if (o < NAB) {
+        const int i = o / E::B, j = o % E::B;
+        const double* v = V + (size_t)o * NCD;
+#pragma unroll 4
+        for (int cd = 0; cd < NCD; ++cd) s = fma(v[cd], Dcd[cd], s);
+        dst = a.gj + (size_t)(oa + i) * n + ob + j;
+        fac = 2.0 * f;
+      } else if (o < NAB + NCD) {
+        const int cd = o - NAB, k = cd / E::D, l = cd % E::D;
+#pragma unroll 4
+        for (int ab = 0; ab < NAB; ++ab) s = fma(V[(size_t)ab * NCD + cd], Dab[ab], s);
+        dst = a.gj + (size_t)(oc + k) * n + od + l;
+        fac = 2.0 * f;
+      } else {
+        int r = o - NAB - NCD;
+        const int kk = r / (NAC + NAD + NBC + NBD);
+        r -= kk * (NAC + NAD + NBC + NBD);
+        const double* dk = Dk + kk * DKS;
+        const double* dac = dk;
+        const double* dad = dac + NAC;
+        const double* dbc = dad + NAD;
+        const double* dbd = dbc + NBC;
+        double* gk = a.gk + (size_t)kk * n * n;
+        fac = f;
+        if (r < NAC) {  // K[a][c] += sum_bd V[a b c d] D[b][d]
+          const int i = r / E::C, k = r % E::C;
+          for (int j = 0; j < E::B; ++j)
+#pragma unroll
+            for (int l = 0; l < E::D; ++l) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dbd[j * E::D + l], s);
+          dst = gk + (size_t)(oa + i) * n + oc + k;
+        } else if (r < NAC + NAD) {  // K[a][d] += sum_bc V D[b][c]
+          r -= NAC;
+          const int i = r / E::D, l = r % E::D;
+          for (int j = 0; j < E::B; ++j)
+#pragma unroll
+            for (int k = 0; k < E::C; ++k) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dbc[j * E::C + k], s);
+          dst = gk + (size_t)(oa + i) * n + od + l;
+        } else if (r < NAC + NAD + NBC) {  // K[b][c] += sum_ad V D[a][d]
+          r -= NAC + NAD;
+          const int j = r / E::C, k = r % E::C;
+          for (int i = 0; i < E::A; ++i)
+#pragma unroll
+            for (int l = 0; l < E::D; ++l) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dad[i * E::D + l], s);
+          dst = gk + (size_t)(ob + j) * n + oc + k;
+        } else {  // K[b][d] += sum_ac V D[a][c]
+          r -= NAC + NAD + NBC;
+          const int j = r / E::D, l = r % E::D;
+          for (int i = 0; i < E::A; ++i)
+#pragma unroll
+            for (int k = 0; k < E::C; ++k) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dac[i * E::C + k], s);
+          dst = gk + (size_t)(ob + j) * n + od + l;
+        }
+      }
+      atomicAdd(dst, fac * s);
+    }
+    __syncwarp();
+  }
+  if (a.counters && lane == 0 && nprim) atomicAdd(a.counters, nprim);
+}
+
+}  // namespace oqpg

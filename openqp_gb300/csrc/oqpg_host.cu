@@ -1,0 +1,727 @@
+// Host side of the GB300 Fock build: contexts, shell-pair tables, device
+// screening and quartet-list construction, class-kernel dispatch, the final
+// symmetrisation into OpenQP's packed layout, and the C ABI.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/openqp_gb300.h"
+#include "oqpg_classes.h"
+
+namespace oqpg {
+
+enum Status { OK = 0, NOT_INIT = 1, NO_MEM = 2, UNSUPPORTED = 3, DEV_ERR = 4 };
+
+static const ClassInfo kClasses[NCLASS] = {
+#define C_(a, b, c, d) {{a, b, c, d}, (ncart(a) * ncart(b) * ncart(c) * ncart(d) > 27), 0, 0}
+    C_(0, 0, 0, 0), C_(0, 0, 0, 1), C_(0, 0, 0, 2), C_(0, 0, 1, 1), C_(0, 0, 1, 2), C_(0, 0, 2, 2),
+    C_(0, 1, 0, 1), C_(0, 1, 0, 2), C_(0, 1, 1, 1), C_(0, 1, 1, 2), C_(0, 1, 2, 2),
+    C_(0, 2, 0, 2), C_(0, 2, 1, 1), C_(0, 2, 1, 2), C_(0, 2, 2, 2),
+    C_(1, 1, 1, 1), C_(1, 1, 1, 2), C_(1, 1, 2, 2),
+    C_(1, 2, 1, 2), C_(1, 2, 2, 2),
+    C_(2, 2, 2, 2),
+#undef C_
+};
+const ClassInfo& class_info(int c) { return kClasses[c]; }
+
+cudaError_t launch_class(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st) {
+  switch (c) {
+    case 0: case 1: case 2: case 3: case 4: case 6: case 7: case 8:
+      return launch_group0(c, pure, sch, a, nsm, st);
+    case 5: case 9: case 10: case 11: case 12: case 15:
+      return launch_group1(c, pure, sch, a, nsm, st);
+    case 13: case 14: case 16: case 17:
+      return launch_group2(c, pure, sch, a, nsm, st);
+    default:
+      return launch_group3(c, pure, sch, a, nsm, st);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Small device kernels
+
+__device__ __forceinline__ int d_class_index(int tb, int tk) { return tb * 6 - tb * (tb - 1) / 2 + (tk - tb); }
+
+// Packed D -> full symmetric Coulomb density (Da + Db) and exchange densities.
+__global__ void k_unpack(const double* __restrict__ dp, int nfocks, int nbf, double* dj, double* dk) {
+  const long long n2 = (long long)nbf * nbf;
+  const long long ntri = (long long)nbf * (nbf + 1) / 2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n2; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / nbf), j = (int)(t % nbf);
+    const int hi = i > j ? i : j, lo = i > j ? j : i;
+    const long long p = (long long)hi * (hi + 1) / 2 + lo;
+    if (nfocks == 1) {
+      dj[t] = dp[p];
+    } else {
+      const double a = dp[p], b = dp[ntri + p];
+      dj[t] = a + b;
+      dk[t] = a;
+      dk[n2 + t] = b;
+    }
+  }
+}
+
+// shlden (OpenQP int2.F90:999-1047): max |D| over each shell-pair block and
+// over the densities; also the global maximum (max_den).
+__global__ void k_dsh(const double* __restrict__ dp, int nfocks, int nbf, int ns, const int* __restrict__ aoff,
+                      const int* __restrict__ nao, double* dsh, float* dshf, unsigned long long* dmax_bits) {
+  const long long npair = (long long)ns * (ns + 1) / 2;
+  const long long ntri = (long long)nbf * (nbf + 1) / 2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npair; t += (long long)gridDim.x * blockDim.x) {
+    int si = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((long long)si * (si + 1) / 2 > t) --si;
+    while ((long long)(si + 1) * (si + 2) / 2 <= t) ++si;
+    const int sj = (int)(t - (long long)si * (si + 1) / 2);
+    double m = 0.0;
+    const int i0 = aoff[si], i1 = i0 + nao[si], j0 = aoff[sj];
+    int j1 = j0 + nao[sj];
+    for (int f = 0; f < nfocks; ++f) {
+      const double* d = dp + f * ntri;
+      for (int i = i0; i < i1; ++i) {
+        const int je = (si == sj) ? i + 1 : j1;
+        for (int j = j0; j < je; ++j) m = fmax(m, fabs(d[(long long)i * (i + 1) / 2 + j]));
+      }
+    }
+    dsh[(long long)si * ns + sj] = m;
+    dsh[(long long)sj * ns + si] = m;
+    dshf[(long long)si * ns + sj] = (float)m;
+    dshf[(long long)sj * ns + si] = (float)m;
+    atomicMax(dmax_bits, (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+struct ListArgs {
+  int npair, ns;
+  const int2* pair_ij;      // shells (i >= j) of each pair, canonical order
+  const int* pair_type;
+  const double* q;          // Schwarz bound per pair
+  const float* qf;
+  const double* dsh;
+  const float* dshf;
+  const unsigned long long* dmax_bits;
+  double tau;
+  unsigned long long* counts;   // NCLASS
+  uint2* lists[NCLASS];
+  unsigned long long caps[NCLASS];
+  int write;
+};
+
+// Screened quartet lists, one CTA per bra pair P (the larger pair index of the
+// canonical quartet, int2.F90:755-805): pair screen Q_P Dmax >= tau, then for
+// every Q <= P the quartet screen Q_P Q_Q max(4D_ij, 4D_kl, D_jl, D_jk, D_il, D_ik)
+// >= tau (int2.F90:975-986).  FP32 decides when it is clear by a 1e-5 margin,
+// FP64 with the reference's operation order otherwise.
+__global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
+  __shared__ unsigned cnt[NCLASS];
+  __shared__ unsigned long long base[NCLASS];
+  const int P = blockIdx.x;
+  const double dmax = __longlong_as_double((long long)*a.dmax_bits);
+  const double qP = a.q[P];
+  if (qP * dmax < a.tau) return;
+  const int2 ij = a.pair_ij[P];
+  const int tP = a.pair_type[P];
+  const float qPf = a.qf[P];
+  const float* di = a.dshf + (long long)ij.x * a.ns;
+  const float* dj = a.dshf + (long long)ij.y * a.ns;
+  const float dij4 = 4.0f * di[ij.y];
+  const float tlo = (float)(a.tau * (1.0 - 1e-5)), thi = (float)(a.tau * (1.0 + 1e-5));
+  for (int q0 = 0; q0 <= P; q0 += blockDim.x) {
+    if (threadIdx.x < NCLASS) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int Q = q0 + threadIdx.x;
+    int c = -1;
+    unsigned slot = 0;
+    uint2 ent;
+    if (Q <= P) {
+      const int2 kl = a.pair_ij[Q];
+      const float m = fmaxf(fmaxf(fmaxf(dij4, 4.0f * a.dshf[(long long)kl.x * a.ns + kl.y]), fmaxf(dj[kl.y], dj[kl.x])),
+                            fmaxf(di[kl.y], di[kl.x]));
+      const float tf = qPf * a.qf[Q] * m;
+      bool pass;
+      if (tf < tlo) pass = false;
+      else if (tf > thi) pass = true;
+      else {
+        const double* Di = a.dsh + (long long)ij.x * a.ns;
+        const double* Dj = a.dsh + (long long)ij.y * a.ns;
+        double t = qP * a.q[Q];
+        t *= fmax(fmax(fmax(4.0 * Di[ij.y], 4.0 * a.dsh[(long long)kl.x * a.ns + kl.y]), fmax(Dj[kl.y], Dj[kl.x])),
+                  fmax(Di[kl.y], Di[kl.x]));
+        pass = !(t < a.tau);
+      }
+      if (pass) {
+        const int tQ = a.pair_type[Q];
+        if (tP <= tQ) { c = d_class_index(tP, tQ); ent = make_uint2(P, Q); }
+        else { c = d_class_index(tQ, tP); ent = make_uint2(Q, P); }
+        slot = atomicAdd(&cnt[c], 1u);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < NCLASS && cnt[threadIdx.x]) base[threadIdx.x] = atomicAdd(&a.counts[threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
+    __syncthreads();
+    if (c >= 0 && a.write) {
+      const unsigned long long pos = base[c] + slot;
+      if (pos < a.caps[c]) a.lists[c][pos] = ent;
+    }
+    __syncthreads();
+  }
+}
+
+// F = sc (GJ + GJ^T) - cK (GK + GK^T) on the packed lower triangle (+ F_old).
+__global__ void k_finalize(const double* __restrict__ gj, const double* __restrict__ gk, int nk, int nbf, double sc,
+                           double ck, double* f, double* f_old) {
+  const long long ntri = (long long)nbf * (nbf + 1) / 2;
+  const long long n2 = (long long)nbf * nbf;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ntri; t += (long long)gridDim.x * blockDim.x) {
+    int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((long long)i * (i + 1) / 2 > t) --i;
+    while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
+    const int j = (int)(t - (long long)i * (i + 1) / 2);
+    const double J = gj[(long long)i * nbf + j] + gj[(long long)j * nbf + i];
+    for (int k = 0; k < nk; ++k) {
+      const double* g = gk + k * n2;
+      double v = sc * J - ck * (g[(long long)i * nbf + j] + g[(long long)j * nbf + i]);
+      if (f_old) {
+        v += f_old[k * ntri + t];
+        f_old[k * ntri + t] = v;
+      }
+      f[k * ntri + t] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T> T* as() const { return (T*)p; }
+};
+
+}  // namespace oqpg
+
+using namespace oqpg;
+
+struct oqpg_ctx {
+  int dev = 0, nsm = 152;
+  cudaStream_t stream = nullptr;
+  int nshell = 0, nbf = 0, natom = 0, npair = 0;
+  bool pure = false;
+  double tau = 1e-10;
+  std::vector<ShellDev> shells;
+  std::vector<int> aoff, naos;
+  std::vector<double> schwarz_pair;   // per pair (canonical index)
+  // device tables
+  DevBuf d_shells, d_pairs, d_prims, d_pair_ij, d_pair_type, d_q, d_qf, d_aoff, d_naos;
+  // per-build buffers
+  DevBuf d_dp, d_dj, d_dk, d_gj, d_gk, d_f, d_fold, d_dsh, d_dshf, d_dmax, d_counts, d_prim_counter;
+  DevBuf d_lists[NCLASS];
+  unsigned long long caps[NCLASS] = {0};
+  unsigned long long counts[NCLASS] = {0};
+  bool have_caps = false;
+  // pinned staging
+  double* h_in = nullptr;
+  double* h_out = nullptr;
+  size_t h_bytes = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t evc[NCLASS][2] = {};
+  double last_stats[8 + 3 * NCLASS] = {0};
+};
+
+namespace {
+
+std::mutex g_mutex;
+oqpg_ctx* g_ctx = nullptr;
+
+int to_status(cudaError_t e) {
+  if (e == cudaSuccess) return OK;
+  if (e == cudaErrorMemoryAllocation) return NO_MEM;
+  return DEV_ERR;
+}
+
+#define CK(x)                                         \
+  do {                                                \
+    cudaError_t e_ = (x);                             \
+    if (e_ != cudaSuccess) {                          \
+      if (std::getenv("OQPG_VERBOSE"))                \
+        std::fprintf(stderr, "openqp_gb300: %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return to_status(e_);                           \
+    }                                                 \
+  } while (0)
+
+struct HostPairs {
+  std::vector<PairDev> pairs;
+  std::vector<PrimPair> prims;
+  std::vector<int2> ij;
+  std::vector<int> type;
+};
+
+// OpenQP's int2_prepare_pair (int2_pairs.F90:179-266) with the rotated-axis
+// pre-screen |K/p| >= quartet cutoff (int_rotaxis.F90:292-306) applied once.
+void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vector<int>& ncontr,
+                 const std::vector<int>& poff, const double* ex, const double* cc, double qcut, double ecut,
+                 HostPairs& out) {
+  const double sqrtpito52 = std::sqrt(2.0) * std::pow(3.14159265358979323846, 1.25);
+  out.pairs.clear(); out.prims.clear(); out.ij.clear(); out.type.clear();
+  for (int i = 0; i < c.nshell; ++i)
+    for (int j = 0; j <= i; ++j) {
+      int sa = i, sb = j;
+      if (am[sa] > am[sb]) std::swap(sa, sb);
+      const ShellDev& A = c.shells[sa];
+      const ShellDev& B = c.shells[sb];
+      const double ab2 = (A.x - B.x) * (A.x - B.x) + (A.y - B.y) * (A.y - B.y) + (A.z - B.z) * (A.z - B.z);
+      PairDev pd;
+      pd.sha = sa; pd.shb = sb; pd.poff = (int)out.prims.size();
+      for (int p1 = 0; p1 < ncontr[sa]; ++p1)
+        for (int p2 = 0; p2 < ncontr[sb]; ++p2) {
+          const double a1 = ex[poff[sa] + p1], a2 = ex[poff[sb] + p2];
+          const double g = a1 + a2;
+          double e12 = a1 * a2 * ab2;
+          if (e12 > g * ecut) continue;
+          const double gi = 1.0 / g;
+          e12 *= gi;
+          const double k1 = cc[poff[sa] + p1] * cc[poff[sb] + p2] * std::exp(-e12);
+          if (std::fabs(k1) < qcut) continue;
+          const double sp = sqrtpito52 * k1 * gi;
+          if (std::fabs(sp) < qcut) continue;
+          PrimPair pp;
+          pp.p = g; pp.hp = 0.5 * gi;
+          pp.px = (a1 * A.x + a2 * B.x) * gi;
+          pp.py = (a1 * A.y + a2 * B.y) * gi;
+          pp.pz = (a1 * A.z + a2 * B.z) * gi;
+          pp.ax = pp.px - A.x; pp.ay = pp.py - A.y; pp.az = pp.pz - A.z;
+          pp.sp = sp; pp.pad = 0.0;
+          out.prims.push_back(pp);
+        }
+      pd.pcnt = (int)out.prims.size() - pd.poff;
+      out.pairs.push_back(pd);
+      out.ij.push_back(make_int2(i, j));
+      out.type.push_back(pair_type(am[sa], am[sb]));
+    }
+}
+
+template <typename T>
+int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
+  CK(b.ensure(std::max<size_t>(sizeof(T) * v.size(), 16)));
+  if (!v.empty()) CK(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st));
+  return OK;
+}
+
+int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const int* origin, const double* ex,
+             const double* cc, const int* harmonic, int natom, const double* xyz, double cutoff) {
+  if (nshell <= 0 || natom <= 0 || !am_ || !ncontr_ || !origin || !ex || !cc || !xyz) return UNSUPPORTED;
+  std::vector<int> am(am_, am_ + nshell), ncontr(ncontr_, ncontr_ + nshell), poff(nshell);
+  int npure = 0, nd = 0, off = 0, aoff = 0;
+  c->nshell = nshell; c->natom = natom; c->tau = cutoff;
+  c->shells.resize(nshell); c->aoff.resize(nshell); c->naos.resize(nshell);
+  for (int s = 0; s < nshell; ++s) {
+    if (am[s] < 0 || am[s] > 2 || ncontr[s] <= 0 || origin[s] < 1 || origin[s] > natom) return UNSUPPORTED;
+    if (am[s] == 2) { ++nd; if (harmonic && harmonic[s]) ++npure; }
+    poff[s] = off; off += ncontr[s];
+  }
+  if (npure != 0 && npure != nd) return UNSUPPORTED;  // mixed Cartesian / pure d shells
+  c->pure = nd > 0 && npure == nd;
+  for (int s = 0; s < nshell; ++s) {
+    ShellDev& S = c->shells[s];
+    const int at = origin[s] - 1;
+    S.x = xyz[3 * at]; S.y = xyz[3 * at + 1]; S.z = xyz[3 * at + 2];
+    S.am = am[s]; S.harm = (c->pure && am[s] == 2) ? 1 : 0;
+    S.nao = (S.harm ? 5 : ncart(am[s]));
+    S.aoff = aoff;
+    c->aoff[s] = aoff; c->naos[s] = S.nao;
+    aoff += S.nao;
+  }
+  c->nbf = aoff;
+  c->npair = nshell * (nshell + 1) / 2;
+  CK(cudaGetDevice(&c->dev));
+  CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->dev));
+  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  for (auto& e : c->ev) CK(cudaEventCreate(&e));
+  for (auto& p : c->evc) for (auto& e : p) CK(cudaEventCreate(&e));
+  cudaStream_t st = c->stream;
+  int rc;
+  if ((rc = upload(c->d_shells, c->shells, st))) return rc;
+  if ((rc = upload(c->d_aoff, c->aoff, st))) return rc;
+  if ((rc = upload(c->d_naos, c->naos, st))) return rc;
+
+  // --- Schwarz bounds with OpenQP's very tight cutoffs (int2.F90:1600-1604)
+  HostPairs sp;
+  build_pairs(*c, am, ncontr, poff, ex, cc, 1e-17, 50.0, sp);
+  if ((rc = upload(c->d_pairs, sp.pairs, st))) return rc;
+  if ((rc = upload(c->d_prims, sp.prims, st))) return rc;
+  std::vector<std::vector<uint2>> diag(NCLASS);
+  for (int p = 0; p < c->npair; ++p) {
+    if (sp.pairs[p].pcnt == 0) continue;
+    diag[class_index(sp.type[p], sp.type[p])].push_back(make_uint2(p, p));
+  }
+  DevBuf d_diag, d_q;
+  CK(d_q.ensure(sizeof(double) * c->npair));
+  CK(cudaMemsetAsync(d_q.p, 0, sizeof(double) * c->npair, st));
+  for (int cl = 0; cl < NCLASS; ++cl) {
+    if (diag[cl].empty()) continue;
+    if ((rc = upload(d_diag, diag[cl], st))) return rc;
+    BuildArgs a{};
+    a.shells = c->d_shells.as<ShellDev>();
+    a.pairs = c->d_pairs.as<PairDev>();
+    a.prims = c->d_prims.as<PrimPair>();
+    a.quartets = d_diag.as<uint2>();
+    a.nquartets = (long long)diag[cl].size();
+    a.nbf = c->nbf;
+    a.prim_cut = 1e-17;
+    a.prim_cut2 = 1e-34;
+    a.schwarz_out = d_q.as<double>();
+    CK(launch_class(cl, c->pure, true, a, c->nsm, st));
+    CK(cudaStreamSynchronize(st));  // d_diag is reused by the next class
+  }
+  c->schwarz_pair.resize(c->npair);
+  CK(cudaMemcpyAsync(c->schwarz_pair.data(), d_q.p, sizeof(double) * c->npair, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  d_diag.release();
+  d_q.release();
+
+  // --- pair tables of the Fock build (cutoffs 1e-2 tau, 1e-4 tau, 25 ln 10; int2.F90:260-272)
+  HostPairs fp;
+  build_pairs(*c, am, ncontr, poff, ex, cc, 1e-4 * cutoff, 25.0 * std::log(10.0), fp);
+  if ((rc = upload(c->d_pairs, fp.pairs, st))) return rc;
+  if ((rc = upload(c->d_prims, fp.prims, st))) return rc;
+  if ((rc = upload(c->d_pair_ij, fp.ij, st))) return rc;
+  if ((rc = upload(c->d_pair_type, fp.type, st))) return rc;
+  if ((rc = upload(c->d_q, c->schwarz_pair, st))) return rc;
+  std::vector<float> qf(c->npair);
+  for (int p = 0; p < c->npair; ++p) qf[p] = (float)c->schwarz_pair[p];
+  if ((rc = upload(c->d_qf, qf, st))) return rc;
+  CK(cudaStreamSynchronize(st));
+  return OK;
+}
+
+void ctx_free(oqpg_ctx* c) {
+  if (!c) return;
+  DevBuf* bufs[] = {&c->d_shells, &c->d_pairs, &c->d_prims, &c->d_pair_ij, &c->d_pair_type, &c->d_q, &c->d_qf,
+                    &c->d_aoff, &c->d_naos, &c->d_dp, &c->d_dj, &c->d_dk, &c->d_gj, &c->d_gk, &c->d_f,
+                    &c->d_fold, &c->d_dsh, &c->d_dshf, &c->d_dmax, &c->d_counts, &c->d_prim_counter};
+  for (DevBuf* b : bufs) b->release();
+  for (auto& b : c->d_lists) b.release();
+  if (c->h_in) cudaFreeHost(c->h_in);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+  for (auto& p : c->evc) for (auto& e : p) if (e) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+// Core build on device buffers.  dp: packed densities (device), f: packed
+// output (device), f_old: optional packed previous Fock (device, updated).
+int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfocks, double se, double sc,
+              cudaStream_t st) {
+  if (nfocks != 1 && nfocks != 2) return UNSUPPORTED;
+  const int n = c->nbf, ns = c->nshell;
+  const size_t n2 = (size_t)n * n;
+  const int nk = nfocks;
+  CK(c->d_dj.ensure(sizeof(double) * n2));
+  if (nk == 2) CK(c->d_dk.ensure(sizeof(double) * 2 * n2));
+  CK(c->d_gj.ensure(sizeof(double) * n2));
+  CK(c->d_gk.ensure(sizeof(double) * nk * n2));
+  CK(c->d_dsh.ensure(sizeof(double) * ns * ns));
+  CK(c->d_dshf.ensure(sizeof(float) * ns * ns));
+  CK(c->d_dmax.ensure(sizeof(unsigned long long)));
+  CK(c->d_counts.ensure(sizeof(unsigned long long) * NCLASS));
+  CK(c->d_prim_counter.ensure(sizeof(unsigned long long) * NCLASS));
+  CK(cudaEventRecord(c->ev[0], st));
+  k_unpack<<<std::min<long long>((n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(dp, nfocks, n, c->d_dj.as<double>(),
+                                                                                 c->d_dk.as<double>());
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(c->d_dmax.p, 0, sizeof(unsigned long long), st));
+  const long long npair = c->npair;
+  k_dsh<<<std::min<long long>((npair + 127) / 128, c->nsm * 8LL), 128, 0, st>>>(
+      dp, nfocks, n, ns, c->d_aoff.as<int>(), c->d_naos.as<int>(), c->d_dsh.as<double>(), c->d_dshf.as<float>(),
+      c->d_dmax.as<unsigned long long>());
+  CK(cudaGetLastError());
+  // --- quartet lists: count (first build) or fill directly with the previous capacities
+  ListArgs la{};
+  la.npair = c->npair; la.ns = ns;
+  la.pair_ij = c->d_pair_ij.as<int2>();
+  la.pair_type = c->d_pair_type.as<int>();
+  la.q = c->d_q.as<double>(); la.qf = c->d_qf.as<float>();
+  la.dsh = c->d_dsh.as<double>(); la.dshf = c->d_dshf.as<float>();
+  la.dmax_bits = c->d_dmax.as<unsigned long long>();
+  la.tau = c->tau;
+  la.counts = c->d_counts.as<unsigned long long>();
+  bool lists_ok = false;
+  for (int pass = 0; pass < 3 && !lists_ok; ++pass) {
+    la.write = c->have_caps ? 1 : 0;
+    for (int k = 0; k < NCLASS; ++k) { la.lists[k] = c->d_lists[k].as<uint2>(); la.caps[k] = c->caps[k]; }
+    CK(cudaMemsetAsync(c->d_counts.p, 0, sizeof(unsigned long long) * NCLASS, st));
+    k_lists<<<c->npair, 256, 0, st>>>(la);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c->counts, c->d_counts.p, sizeof(unsigned long long) * NCLASS, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    bool ok = c->have_caps;
+    for (int k = 0; k < NCLASS; ++k)
+      if (c->counts[k] > c->caps[k]) ok = false;
+    if (ok) {
+      lists_ok = true;
+      break;
+    }
+    for (int k = 0; k < NCLASS; ++k) {
+      if (c->counts[k] > c->caps[k] || !c->have_caps) {
+        const unsigned long long cap = c->counts[k] + c->counts[k] / 8 + 1024;
+        if (cap > c->caps[k]) {
+          CK(c->d_lists[k].ensure(sizeof(uint2) * cap));
+          c->caps[k] = cap;
+        }
+      }
+    }
+    c->have_caps = true;
+  }
+  if (!lists_ok) return DEV_ERR;  // quartet lists never fitted: do not launch on partial lists
+  CK(cudaEventRecord(c->ev[1], st));
+  // --- integrals + digestion
+  CK(cudaMemsetAsync(c->d_gj.p, 0, sizeof(double) * n2, st));
+  CK(cudaMemsetAsync(c->d_gk.p, 0, sizeof(double) * nk * n2, st));
+  CK(cudaMemsetAsync(c->d_prim_counter.p, 0, sizeof(unsigned long long) * NCLASS, st));
+  BuildArgs a{};
+  a.shells = c->d_shells.as<ShellDev>();
+  a.pairs = c->d_pairs.as<PairDev>();
+  a.prims = c->d_prims.as<PrimPair>();
+  a.nbf = n;
+  a.nk = nk;
+  a.prim_cut = 1e-4 * c->tau;
+  a.prim_cut2 = a.prim_cut * a.prim_cut;
+  a.elem_cut = c->tau;
+  a.dj = c->d_dj.as<double>();
+  a.dk = (nk == 1) ? c->d_dj.as<double>() : c->d_dk.as<double>();
+  a.gj = c->d_gj.as<double>();
+  a.gk = c->d_gk.as<double>();
+  double nq = 0;
+  // heaviest classes first; every class launch is bracketed by events
+  int nlaunch = 0;
+  for (int cl = NCLASS - 1; cl >= 0; --cl) {
+    if (c->counts[cl] == 0) continue;
+    a.quartets = c->d_lists[cl].as<uint2>();
+    a.nquartets = (long long)c->counts[cl];
+    a.counters = c->d_prim_counter.as<unsigned long long>() + cl;
+    nq += (double)c->counts[cl];
+    CK(cudaEventRecord(c->evc[cl][0], st));
+    CK(launch_class(cl, c->pure, false, a, c->nsm, st));
+    CK(cudaEventRecord(c->evc[cl][1], st));
+    ++nlaunch;
+  }
+  CK(cudaEventRecord(c->ev[2], st));
+  const long long ntri = (long long)n * (n + 1) / 2;
+  const double ck = (nk == 1) ? 0.5 * se : se;
+  k_finalize<<<std::min<long long>((ntri + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
+      c->d_gj.as<double>(), c->d_gk.as<double>(), nk, n, sc, ck, f, f_old);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(c->ev[3], st));
+  unsigned long long nprim[NCLASS];
+  CK(cudaMemcpyAsync(nprim, c->d_prim_counter.p, sizeof(nprim), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  float t01 = 0, t12 = 0, t03 = 0;
+  cudaEventElapsedTime(&t01, c->ev[0], c->ev[1]);
+  cudaEventElapsedTime(&t12, c->ev[1], c->ev[2]);
+  cudaEventElapsedTime(&t03, c->ev[0], c->ev[3]);
+  double* S = c->last_stats;
+  S[1] = 0;
+  for (int k = 0; k < NCLASS; ++k) {
+    S[7 + k] = (double)c->counts[k];
+    S[7 + NCLASS + k] = c->counts[k] ? (double)nprim[k] : 0.0;
+    float tk = 0;
+    if (c->counts[k]) cudaEventElapsedTime(&tk, c->evc[k][0], c->evc[k][1]);
+    S[7 + 2 * NCLASS + k] = tk;
+    S[1] += S[7 + NCLASS + k];
+  }
+  S[0] = nq;
+  S[2] = t01;
+  S[3] = t12;
+  S[4] = t03;
+  S[5] = n;
+  S[6] = c->npair;
+  S[7 + 3 * NCLASS] = nlaunch + 4;  // class kernels + unpack, dsh, lists, finalize
+  return OK;
+}
+
+int ctx_build_host(oqpg_ctx* c, const double* d, double* f, double* f_old, int nfocks, double se, double sc) {
+  const size_t ntri = (size_t)c->nbf * (c->nbf + 1) / 2;
+  const size_t bytes = sizeof(double) * ntri * nfocks;
+  if (bytes > c->h_bytes) {
+    if (c->h_in) cudaFreeHost(c->h_in);
+    if (c->h_out) cudaFreeHost(c->h_out);
+    c->h_in = c->h_out = nullptr;
+    c->h_bytes = 0;
+    CK(cudaMallocHost(&c->h_in, bytes));
+    CK(cudaMallocHost(&c->h_out, bytes));
+    c->h_bytes = bytes;
+  }
+  CK(c->d_dp.ensure(bytes));
+  CK(c->d_f.ensure(bytes));
+  if (f_old) CK(c->d_fold.ensure(bytes));
+  cudaStream_t st = c->stream;
+  std::memcpy(c->h_in, d, bytes);
+  CK(cudaMemcpyAsync(c->d_dp.p, c->h_in, bytes, cudaMemcpyHostToDevice, st));
+  if (f_old) {
+    std::memcpy(c->h_out, f_old, bytes);
+    CK(cudaMemcpyAsync(c->d_fold.p, c->h_out, bytes, cudaMemcpyHostToDevice, st));
+  }
+  int rc = ctx_build(c, c->d_dp.as<double>(), c->d_f.as<double>(), f_old ? c->d_fold.as<double>() : nullptr, nfocks,
+                     se, sc, st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(c->h_out, c->d_f.p, bytes, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::memcpy(f, c->h_out, bytes);
+  if (f_old) std::memcpy(f_old, c->h_out, bytes);
+  return OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int oqpg_create(oqpg_ctx** out, int nshell, const int* am, const int* ncontr, const int* origin, const double* ex,
+                const double* cc, const int* harmonic, int natom, const double* xyz, double cutoff) {
+  if (!out) return UNSUPPORTED;
+  *out = nullptr;
+  oqpg_ctx* c = new (std::nothrow) oqpg_ctx;
+  if (!c) return NO_MEM;
+  const int rc = ctx_init(c, nshell, am, ncontr, origin, ex, cc, harmonic, natom, xyz, cutoff);
+  if (rc) {
+    ctx_free(c);
+    return rc;
+  }
+  *out = c;
+  return OK;
+}
+
+int oqpg_destroy(oqpg_ctx* ctx) {
+  ctx_free(ctx);
+  return OK;
+}
+
+int oqpg_nbf(const oqpg_ctx* ctx) { return ctx ? ctx->nbf : -1; }
+
+int oqpg_fock_jk(oqpg_ctx* ctx, const double* d, double* f, int nfocks, double se, double sc) {
+  if (!ctx) return NOT_INIT;
+  return ctx_build_host(ctx, d, f, nullptr, nfocks, se, sc);
+}
+
+int oqpg_fock_jk_device(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, double se, double sc,
+                        void* stream) {
+  if (!ctx) return NOT_INIT;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  return ctx_build(ctx, d_device, f_device, nullptr, nfocks, se, sc, st);
+}
+
+int oqpg_schwarz(const oqpg_ctx* ctx, double* q) {
+  if (!ctx) return NOT_INIT;
+  const int ns = ctx->nshell;
+  for (int i = 0; i < ns; ++i)
+    for (int j = 0; j <= i; ++j) {
+      const double v = ctx->schwarz_pair[(size_t)i * (i + 1) / 2 + j];
+      q[(size_t)i * ns + j] = q[(size_t)j * ns + i] = v;
+    }
+  return OK;
+}
+
+int oqpg_stats(const oqpg_ctx* ctx, double* out, int n) {
+  if (!ctx) return NOT_INIT;
+  for (int i = 0; i < n && i < 8 + 3 * NCLASS; ++i) out[i] = ctx->last_stats[i];
+  return OK;
+}
+
+// FP64 FMA throughput probe: every thread runs 8 independent FMA chains.
+__global__ void k_fp64_peak(double* out, int iters, double a, double b) {
+  double x[8];
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3 + k;
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  double s = 0;
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 1234.5) out[0] = s;  // keeps the chains alive
+}
+
+int oqpg_measure_fp64_peak(int iters, double* tflops) {
+  double* d = nullptr;
+  CK(cudaMalloc(&d, sizeof(double)));
+  int dev = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int blocks = nsm * 4, threads = 256;
+  k_fp64_peak<<<blocks, threads>>>(d, 1000, 0.999999, 1e-9);  // warm-up
+  CK(cudaEventRecord(e0));
+  k_fp64_peak<<<blocks, threads>>>(d, iters, 0.999999, 1e-9);
+  CK(cudaEventRecord(e1));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (ms * 1e-3) / 1e12;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  return OK;
+}
+
+int oqpg_class_l(int c, int* l4) {
+  if (c < 0 || c >= NCLASS) return UNSUPPORTED;
+  for (int i = 0; i < 4; ++i) l4[i] = class_info(c).l[i];
+  return OK;
+}
+
+int routec_fock_init(int nshell, const int* am, const int* ncontr, const int* origin, const double* ex,
+                     const double* cc, const int* harmonic, int natom, const double* xyz, double cutoff) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (g_ctx) {
+    ctx_free(g_ctx);
+    g_ctx = nullptr;
+  }
+  return oqpg_create(&g_ctx, nshell, am, ncontr, origin, ex, cc, harmonic, natom, xyz, cutoff);
+}
+
+void routec_fock_jk(const double* d, double* f, const int* nbf, const int* nfocks, const double* se,
+                    const double* sc, int* info) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!d || !f || !nbf || !nfocks || !se || !sc) rc = UNSUPPORTED;
+  else if (*nbf != g_ctx->nbf) rc = NOT_INIT;   // registered basis does not match the caller's
+  else rc = ctx_build_host(g_ctx, d, f, nullptr, *nfocks, *se, *sc);
+  if (info) *info = rc;
+}
+
+void routec_fock_jk_inc(const double* dd, double* f, double* f_old, const int* nbf, const int* nfocks,
+                        const double* se, const double* sc, int* info) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!dd || !f || !f_old || !nbf || !nfocks || !se || !sc) rc = UNSUPPORTED;
+  else if (*nbf != g_ctx->nbf) rc = NOT_INIT;
+  else rc = ctx_build_host(g_ctx, dd, f, f_old, *nfocks, *se, *sc);
+  if (info) *info = rc;
+}
+
+void routec_fock_finalize(void) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  ctx_free(g_ctx);
+  g_ctx = nullptr;
+}
+
+}  // extern "C"

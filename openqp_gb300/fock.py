@@ -1,0 +1,161 @@
+"""Python front end of the GB300 Fock build.
+
+``FockBuilder`` mirrors OpenQP's operator for this path,
+``fock_jk(basis, d, f, infos, scale_exch, nschwz, f_old, scale_coul)``
+(``source/scf_addons.F90:1063-1214``): the same packed-triangle density in,
+the same ready-to-use packed two-electron Fock matrix out (``nfocks = 1``:
+RHF, F = sc J - se/2 K; ``nfocks = 2``: UHF/ROHF, F_s = sc J[Da+Db] - se K[D_s]).
+Every call goes through the C ABI of ``libopenqp_gb300.so``; there is no CPU
+path.  ``routec_*`` wrap the reference-facing seam itself.
+"""
+import ctypes
+
+import numpy as np
+
+from ._lib import FockError, lib, ptr, _i
+
+NCLASS = 21
+
+
+def class_labels():
+    names = "spd"
+    out = []
+    for c in range(NCLASS):
+        l4 = (ctypes.c_int * 4)()
+        lib().oqpg_class_l(c, l4)
+        out.append("(%s%s|%s%s)" % tuple(names[v] for v in l4))
+    return out
+
+
+def _basis_arrays(bas):
+    return [np.ascontiguousarray(bas.am, dtype=np.int32), np.ascontiguousarray(bas.ncontr, dtype=np.int32),
+            np.ascontiguousarray(bas.origin, dtype=np.int32), np.ascontiguousarray(bas.ex, dtype=np.float64),
+            np.ascontiguousarray(bas.cc, dtype=np.float64), np.ascontiguousarray(bas.harmonic, dtype=np.int32),
+            np.ascontiguousarray(bas.xyz.reshape(-1), dtype=np.float64)]
+
+
+class FockBuilder:
+    """Direct J/K builder for one basis and geometry (one device context)."""
+
+    def __init__(self, bas, cutoff=1e-10):
+        self.bas = bas
+        self.cutoff = cutoff
+        k = _basis_arrays(bas)
+        self._keep = k
+        h = ctypes.c_void_p()
+        rc = lib().oqpg_create(ctypes.byref(h), len(bas.am), ptr(k[0], _i), ptr(k[1], _i), ptr(k[2], _i), ptr(k[3]),
+                               ptr(k[4]), ptr(k[5], _i), int(bas.natom), ptr(k[6]), float(cutoff))
+        if rc != 0:
+            raise FockError(rc, "oqpg_create")
+        self.h = h
+        self.nbf = lib().oqpg_nbf(h)
+        self.ntri = self.nbf * (self.nbf + 1) // 2
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().oqpg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def fock_jk(self, d, scale_exch=1.0, scale_coul=1.0):
+        """d: (ntri,) or (nfocks, ntri) packed densities (host) -> packed F, same shape as 2-D."""
+        d = np.ascontiguousarray(np.atleast_2d(d), dtype=np.float64)
+        if d.shape[1] != self.ntri:
+            raise ValueError("density has %d packed elements, basis needs %d" % (d.shape[1], self.ntri))
+        f = np.empty_like(d)
+        rc = lib().oqpg_fock_jk(self.h, ptr(d), ptr(f), d.shape[0], float(scale_exch), float(scale_coul))
+        if rc != 0:
+            raise FockError(rc, "oqpg_fock_jk")
+        return f
+
+    def fock_jk_device(self, d, scale_exch=1.0, scale_coul=1.0, out=None, stream=None):
+        """d: torch CUDA tensor (nfocks, ntri) float64 -> torch tensor, no host copies."""
+        import torch
+        if not (d.is_cuda and d.dtype == torch.float64 and d.is_contiguous()):
+            raise ValueError("d must be a contiguous float64 CUDA tensor")
+        d2 = d if d.dim() == 2 else d.unsqueeze(0)
+        if out is None:
+            out = torch.empty_like(d2)
+        st = stream if stream is not None else torch.cuda.current_stream(d.device)
+        rc = lib().oqpg_fock_jk_device(self.h, ctypes.c_void_p(d2.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                       d2.shape[0], float(scale_exch), float(scale_coul),
+                                       ctypes.c_void_p(st.cuda_stream))
+        if rc != 0:
+            raise FockError(rc, "oqpg_fock_jk_device")
+        return out
+
+    def schwarz(self):
+        ns = len(self.bas.am)
+        q = np.zeros(ns * ns)
+        rc = lib().oqpg_schwarz(self.h, ptr(q))
+        if rc != 0:
+            raise FockError(rc, "oqpg_schwarz")
+        return q.reshape(ns, ns)
+
+    def stats(self):
+        s = np.zeros(8 + 3 * NCLASS)
+        lib().oqpg_stats(self.h, ptr(s), len(s))
+        return dict(quartets=int(s[0]), prim_quartets=int(s[1]), list_ms=s[2], eri_ms=s[3], total_ms=s[4],
+                    nbf=int(s[5]), npair=int(s[6]), per_class=[int(v) for v in s[7:7 + NCLASS]],
+                    prim_per_class=[int(v) for v in s[7 + NCLASS:7 + 2 * NCLASS]],
+                    ms_per_class=[float(v) for v in s[7 + 2 * NCLASS:7 + 3 * NCLASS]],
+                    launches=int(s[7 + 3 * NCLASS]))
+
+
+def fp64_peak_tflops(iters=20000):
+    v = ctypes.c_double(0)
+    rc = lib().oqpg_measure_fp64_peak(int(iters), ctypes.byref(v))
+    if rc != 0:
+        raise FockError(rc, "oqpg_measure_fp64_peak")
+    return v.value
+
+
+def class_flops(c, nprim, nquart, nk=1, pure=False):
+    """Algorithmic FP64 flops of class c: assembly 3 R N_c per primitive
+    quartet (x*y, then FMA with z, per Rys root) plus digestion per
+    contracted quartet, 12 flops (6 FMA) per element for RHF, 2 + 4 nk FMA
+    per element for UHF/ROHF."""
+    l4 = (ctypes.c_int * 4)()
+    lib().oqpg_class_l(c, l4)
+    L = list(l4)
+    R = sum(L) // 2 + 1
+    nc = 1
+    nao = 1
+    for l in L:
+        nc *= (l + 1) * (l + 2) // 2
+        nao *= (5 if (pure and l == 2) else (l + 1) * (l + 2) // 2)
+    dig = 12 if nk == 1 else 2 * (2 + 4 * nk)
+    return 3.0 * R * nc * nprim + dig * nao * nquart
+
+
+# ---- the reference-facing seam ------------------------------------------------
+
+def routec_init(bas, cutoff=1e-10):
+    k = _basis_arrays(bas)
+    rc = lib().routec_fock_init(len(bas.am), ptr(k[0], _i), ptr(k[1], _i), ptr(k[2], _i), ptr(k[3]), ptr(k[4]),
+                                ptr(k[5], _i), int(bas.natom), ptr(k[6]), float(cutoff))
+    return rc
+
+
+def routec_fock_jk(d, nbf, nfocks, se=1.0, sc=1.0):
+    """Calls routec_fock_jk exactly as OpenQP's bridge does (all by reference).
+    Returns (f, info)."""
+    d = np.ascontiguousarray(d, dtype=np.float64).reshape(-1)
+    f = np.zeros_like(d)
+    n = ctypes.c_int(nbf)
+    nf = ctypes.c_int(nfocks)
+    se_ = ctypes.c_double(se)
+    sc_ = ctypes.c_double(sc)
+    info = ctypes.c_int(1)
+    lib().routec_fock_jk(ptr(d), ptr(f), ctypes.byref(n), ctypes.byref(nf), ctypes.byref(se_), ctypes.byref(sc_),
+                         ctypes.byref(info))
+    return f.reshape(nfocks, -1), info.value
+
+
+def routec_finalize():
+    lib().routec_fock_finalize()

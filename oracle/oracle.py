@@ -36,6 +36,8 @@ def lib():
         L.orc_nbf.argtypes = [ctypes.c_void_p]
         L.orc_fock_jk.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_int, ctypes.c_int, _d, _d]
+        L.orc_fock_jk_sample.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_int, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int, _d]
         L.orc_schwarz.argtypes = [ctypes.c_void_p, _d, ctypes.c_int]
         L.orc_shlden.argtypes = [ctypes.c_void_p, _d, ctypes.c_int, _d]
         L.orc_eri_quartet.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 4 + [_d]
@@ -89,6 +91,21 @@ class Oracle:
         self.last_stats = dict(t_init=st[0], t_schwarz=st[1], t_twoei=st[2], t_total=st[3], quartets=int(st[4]),
                                screened=int(st[5]), prim_quartets=int(st[6]), stored=int(st[7]))
         return f
+
+    def fock_jk_sample(self, d, stride, offset=0, se=1.0, sc=1.0, urohf=None, nthreads=None, schwarz=None):
+        """fock_jk over the shell pairs p (cost-sorted order) with p % stride == offset:
+        one rank of the reference's round-robin split.  Returns (f, stats)."""
+        d = np.ascontiguousarray(np.atleast_2d(d), dtype=np.float64)
+        nf = d.shape[0]
+        if urohf is None:
+            urohf = nf == 2
+        f = np.zeros_like(d)
+        st = np.zeros(8)
+        q = None if schwarz is None else _p(np.ascontiguousarray(schwarz))
+        lib().orc_fock_jk_sample(self.h, _p(d), _p(f), nf, se, sc, int(urohf), nthreads or os.cpu_count(), q,
+                                 int(stride), int(offset), _p(st))
+        return f, dict(t_init=st[0], t_schwarz=st[1], t_twoei=st[2], t_total=st[3], quartets=int(st[4]),
+                       screened=int(st[5]), prim_quartets=int(st[6]), stored=int(st[7]))
 
     def schwarz(self, nthreads=None):
         ns = len(self.bas.am)

@@ -214,8 +214,11 @@ static double now() {
 }
 
 // fock_jk (scf_addons.F90:1063-1214) with int2_twoei (int2.F90:589-923).
+// stride/offset > 1 keep only the shell pairs p of the cost-sorted list with
+// p mod stride == offset: the reference's own MPI work split
+// (int2.F90:759-761), used to time a bounded sample of a large build.
 static int fock_jk(OrcHandle* H, const double* d, double* fout, int nfocks, double se, double sc, int urohf,
-                   int nthreads, const double* qext, OrcStats* stats) {
+                   int nthreads, const double* qext, OrcStats* stats, int stride = 1, int offset = 0) {
   const Basis& B = H->B;
   const double t0 = now();
   const double cut = H->cutoff;
@@ -248,6 +251,7 @@ static int fock_jk(OrcHandle* H, const double* d, double* fout, int nfocks, doub
     Store st(50000);
 #pragma omp for schedule(dynamic, 1)
     for (int p = 0; p < np; ++p) {
+      if (stride > 1 && p % stride != offset) continue;
       const int i = pi[p], j = pj[p];
       const double qij = Q[(size_t)i * ns + j];
       if (qij * max_den < cut) { nsk += (long long)(i + 1) * i / 2 + j + 1; continue; }
@@ -325,6 +329,19 @@ int orc_fock_jk(void* h, const double* d, double* f, int nfocks, double se, doub
                 const double* schwarz_in, double* stats6) {
   OrcStats st;
   const int rc = fock_jk((OrcHandle*)h, d, f, nfocks, se, sc, urohf, nthreads, schwarz_in, &st);
+  if (stats6) {
+    stats6[0] = st.t_init; stats6[1] = st.t_schwarz; stats6[2] = st.t_twoei; stats6[3] = st.t_total;
+    stats6[4] = (double)st.quartets; stats6[5] = (double)st.screened; stats6[6] = (double)st.prim_quartets;
+    stats6[7] = (double)st.stored;
+  }
+  return rc;
+}
+
+// Same build restricted to the shell pairs p with p mod stride == offset.
+int orc_fock_jk_sample(void* h, const double* d, double* f, int nfocks, double se, double sc, int urohf,
+                       int nthreads, const double* schwarz_in, int stride, int offset, double* stats6) {
+  OrcStats st;
+  const int rc = fock_jk((OrcHandle*)h, d, f, nfocks, se, sc, urohf, nthreads, schwarz_in, &st, stride, offset);
   if (stats6) {
     stats6[0] = st.t_init; stats6[1] = st.t_schwarz; stats6[2] = st.t_twoei; stats6[3] = st.t_total;
     stats6[4] = (double)st.quartets; stats6[5] = (double)st.screened; stats6[6] = (double)st.prim_quartets;
