@@ -33,16 +33,44 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = dict(name="(H2O)32 cc-pVDZ spherical RHF J+K Fock build", nwater=32, edge=14.0, seed=0, basis="cc-pvdz",
-                cutoff=1e-10)
+WORKLOADS = {
+    # the headline workload (the metric's configuration)
+    "water32_ccpvdz": dict(name="(H2O)32 cc-pVDZ spherical RHF J+K Fock build", nwater=32, edge=14.0, seed=0,
+                           basis="cc-pvdz", cutoff=1e-10),
+    # the plain-FP64 parity configuration
+    "water4_631gd": dict(name="(H2O)4 6-31G(d) Cartesian RHF J+K Fock build", nwater=4, edge=6.0, seed=0,
+                         basis="6-31g(d)", cutoff=1e-10),
+    # small cases for profiling
+    "water8_ccpvdz": dict(name="(H2O)8 cc-pVDZ spherical RHF J+K Fock build", nwater=8, edge=8.82, seed=0,
+                          basis="cc-pvdz", cutoff=1e-10),
+    "water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian RHF J+K Fock build", nwater=16, edge=9.52, seed=0,
+                          basis="6-31g(d)", cutoff=1e-10),
+    # only the d shells of a (H2O)64 6-31G(d) cluster: every quartet is (dd|dd)
+    "dd_only": dict(name="(dd|dd)-only: the 64 d shells of a (H2O)64 6-31G(d) cluster", nwater=64, edge=15.1,
+                    seed=0, basis="6-31g(d)", cutoff=1e-10, only_l=2),
+}
+WORKLOAD = dict(WORKLOADS["water32_ccpvdz"])
 
 
 def make_workload():
     from openqp_gb300 import workloads
+    from openqp_gb300.basis import BasisArrays
     from openqp_gb300.onee import overlap_kinetic
     bas = workloads.water_cluster_basis(WORKLOAD["nwater"], WORKLOAD["edge"], WORKLOAD["seed"], WORKLOAD["basis"])
+    if "only_l" in WORKLOAD:
+        keep = np.where(bas.am == WORKLOAD["only_l"])[0]
+        offs = np.concatenate([[0], np.cumsum(bas.ncontr)])
+        ex = np.concatenate([bas.ex[offs[s]:offs[s + 1]] for s in keep])
+        cc = np.concatenate([bas.cc[offs[s]:offs[s + 1]] for s in keep])
+        naos = bas.naos[keep]
+        bas = BasisArrays(bas.am[keep], bas.ncontr[keep], bas.origin[keep], bas.harmonic[keep], ex, cc, bas.xyz,
+                          bas.charges, int(naos.sum()), np.concatenate([[0], np.cumsum(naos)[:-1]]).astype(np.int32),
+                          naos)
+        nocc = bas.nbf // 4
+    else:
+        nocc = workloads.nelectrons(bas) // 2
     S, _ = overlap_kinetic(bas)
-    d = workloads.density(bas, workloads.nelectrons(bas) // 2, WORKLOAD["seed"], S=S)
+    d = workloads.density(bas, nocc, WORKLOAD["seed"], S=S)
     return bas, d
 
 
@@ -195,11 +223,13 @@ def run_ours(args):
         tsum = float(t.item())
     value = ws * args.steps / tsum
     # e2e through the seam with host buffers
-    routec_init(bas, WORKLOAD["cutoff"])
-    dflat = np.ascontiguousarray(d)
-    routec_fock_jk(dflat, bas.nbf, 1)
-    e2e_t = []
-    for _ in range(args.steps):
+    e2e_t = [float("nan")]
+    if not args.no_e2e:
+        routec_init(bas, WORKLOAD["cutoff"])
+        dflat = np.ascontiguousarray(d)
+        routec_fock_jk(dflat, bas.nbf, 1)
+        e2e_t = []
+    for _ in range(0 if args.no_e2e else args.steps):
         t0 = time.perf_counter()
         f_host, info = routec_fock_jk(dflat, bas.nbf, 1)
         e2e_t.append(time.perf_counter() - t0)
@@ -216,9 +246,9 @@ def run_ours(args):
     ms = np.mean([s["ms_per_class"] for s in stats], axis=0)
     cdom = int(np.argmax(ms))
     s0 = stats[-1]
-    flops = class_flops(cdom, s0["prim_per_class"][cdom], s0["per_class"][cdom], nk=1, pure=True)
+    flops = class_flops(cdom, s0["prim_per_class"][cdom], s0["per_class"][cdom], nk=1, pure=bool(bas.harmonic.any()))
     achieved = flops / (ms[cdom] * 1e-3) / 1e12
-    total_flops = sum(class_flops(c, s0["prim_per_class"][c], s0["per_class"][c], nk=1, pure=True)
+    total_flops = sum(class_flops(c, s0["prim_per_class"][c], s0["per_class"][c], nk=1, pure=bool(bas.harmonic.any()))
                       for c in range(21))
     peak = fp64_peak_tflops()
     if rank == 0:
@@ -239,7 +269,11 @@ def run_ours(args):
                 "prim_quartets_per_s": s0["prim_quartets"] / (tsum / args.steps),
                 "gpu_launches": int(sum(s["launches"] for s in stats)),
                 "wall_s": wall, "clocks": clocks,
-                "class_ms": {labels[c]: round(float(ms[c]), 3) for c in range(21) if ms[c] > 0}}
+                "class_ms": {labels[c]: round(float(ms[c]), 3) for c in range(21) if ms[c] > 0},
+                "class_quartets": {labels[c]: s0["per_class"][c] for c in range(21) if s0["per_class"][c]},
+                "class_prim_quartets": {labels[c]: s0["prim_per_class"][c] for c in range(21)
+                                        if s0["prim_per_class"][c]},
+                "list_ms": s0["list_ms"]}
         if not args.no_cpu:
             cb, _ = cpu_baseline(bas, d, budget_s=args.cpu_budget)
             line["cpu_baseline"] = cb
@@ -256,7 +290,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="water32_ccpvdz", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer seam timing (profiling runs)")
     args = ap.parse_args()
+    WORKLOAD.clear()
+    WORKLOAD.update(WORKLOADS[args.workload])
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -11,8 +11,8 @@ Method (our own, not the polynomial fits of OpenQP's rys.F90):
     (series for the top order, downward recursion), the Chebyshev algorithm
     for the three-term recurrence, and the eigen-decomposition of the Jacobi
     matrix (Golub-Welsch), all with mpmath;
-  * X in [0, 32) is cut into unit intervals, X in [32, XMAX(n)) into intervals
-    of width 4; on each interval every x_i and w_i is fitted by a degree-10
+  * X in [0, 32) is cut into intervals of width 1/4, X in [32, XMAX(n)) into
+    unit intervals; on each interval every x_i and w_i is fitted by a degree-7
     Chebyshev interpolant, stored as monomial coefficients in the local
     variable s = 2 (X - a) / h - 1 in [-1, 1] (Horner evaluation: one FMA per
     coefficient);
@@ -35,9 +35,10 @@ import numpy as np
 
 DPS = 60
 NMAX = 5
-NCOEF = 11            # degree-10 interpolants
-X_SPLIT = 32          # unit intervals below, width-4 intervals above
-W_HI = 4
+NCOEF = 8             # degree-7 interpolants
+X_SPLIT = 32          # quarter-unit intervals below, unit intervals above
+H_LO = 0.25
+W_HI = 1
 XMAX = {1: 40, 2: 48, 3: 56, 4: 64, 5: 72}
 
 
@@ -102,12 +103,22 @@ def hermite_half(n):
 
 
 def intervals(n):
-    iv = [(float(a), 1.0) for a in range(X_SPLIT)]
+    iv = [(k * H_LO, H_LO) for k in range(int(X_SPLIT / H_LO))]
     a = X_SPLIT
     while a < XMAX[n]:
         iv.append((float(a), float(W_HI)))
         a += W_HI
     return iv
+
+
+def interval_of(X):
+    """(index, start, width) of the interval holding X < XMAX."""
+    if X < X_SPLIT:
+        k = int(X / H_LO)
+        return k, k * H_LO, H_LO
+    k0 = int(X_SPLIT / H_LO)
+    k = k0 + int((X - X_SPLIT) / W_HI)
+    return k, X_SPLIT + (k - k0) * W_HI, float(W_HI)
 
 
 def fit_interval(args):
@@ -150,7 +161,7 @@ def main():
     lines = [
         "// Generated by gen_rys_tables.py -- do not edit.",
         "// Rys nodes x_i = t_i^2 and weights w_i for n = 1..%d roots." % NMAX,
-        "// Interval k covers [a_k, a_k + h_k): unit width below %d, width %d above," % (X_SPLIT, W_HI),
+        "// Interval k covers [a_k, a_k + h_k): width %g below %d, width %d above," % (H_LO, X_SPLIT, W_HI),
         "// up to RYS_XMAX[n]; per interval and root: %d monomial coefficients of x_i," % NCOEF,
         "// then %d of w_i, in s = 2 (X - a_k) / h_k - 1, lowest order first." % NCOEF,
         "#ifndef RYS_STORAGE",
@@ -159,6 +170,7 @@ def main():
         "#define RYS_NMAX %d" % NMAX,
         "#define RYS_NCOEF %d" % NCOEF,
         "#define RYS_X_SPLIT %d" % X_SPLIT,
+        "#define RYS_LO_PER_UNIT %d" % int(round(1 / H_LO)),
         "#define RYS_W_HI %d" % W_HI,
     ]
     lines.append("RYS_STORAGE double RYS_XMAX[%d] = {0.0, %s};" % (
@@ -199,12 +211,7 @@ def main():
             golden["cases"].append({"n": n, "X": float(X), "x": [float(v) for v in ex[0]],
                                     "w": [float(v) for v in ex[1]]})
             if X < XMAX[n]:
-                if X < X_SPLIT:
-                    k = int(X)
-                    a, h = float(k), 1.0
-                else:
-                    k = X_SPLIT + int((X - X_SPLIT) / W_HI)
-                    a, h = X_SPLIT + (k - X_SPLIT) * W_HI, float(W_HI)
+                k, a, h = interval_of(X)
                 s = 2 * (X - a) / h - 1
                 rows = tables[n][k]
                 ap = [(horner(rows[2 * r], s), horner(rows[2 * r + 1], s)) for r in range(n)]

@@ -26,13 +26,18 @@ struct ClassInfo {
 };
 const ClassInfo& class_info(int c);
 
-// Launch the Fock-build (sch = false) or Schwarz (sch = true) kernel of class c.
-cudaError_t launch_class(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st);
+// Kernel variants of a class.
+constexpr int MODE_FOCK = 0;     // Fock build
+constexpr int MODE_SCHWARZ = 1;  // Schwarz bounds of diagonal quartets
+constexpr int MODE_PRIM = 2;     // Fock build, one warp per heavily contracted small-class quartet
+
+// Launch the kernel of class c in the given mode.
+cudaError_t launch_class(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 
 // group launchers (defined in oqpg_cls_*.cu)
-cudaError_t launch_group0(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st);
-cudaError_t launch_group1(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st);
-cudaError_t launch_group2(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st);
-cudaError_t launch_group3(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group0(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group1(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group2(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group3(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 
 }  // namespace oqpg

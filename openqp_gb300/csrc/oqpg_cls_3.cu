@@ -4,11 +4,11 @@
 
 namespace oqpg {
 
-cudaError_t launch_group3(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st) {
+cudaError_t launch_group3(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
   switch (c) {
-    case 18: return launch_cls<1, 2, 1, 2>(pure, sch, a, nsm, st);
-    case 19: return launch_cls<1, 2, 2, 2>(pure, sch, a, nsm, st);
-    case 20: return launch_cls<2, 2, 2, 2>(pure, sch, a, nsm, st);
+    case 18: return launch_cls<1, 2, 1, 2>(pure, mode, a, nsm, st);
+    case 19: return launch_cls<1, 2, 2, 2>(pure, mode, a, nsm, st);
+    case 20: return launch_cls<2, 2, 2, 2>(pure, mode, a, nsm, st);
     default: return cudaErrorInvalidValue;
   }
 }

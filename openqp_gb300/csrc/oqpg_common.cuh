@@ -25,7 +25,7 @@ struct PrimPair {
   double px, py, pz;     // Gaussian product centre
   double ax, ay, az;     // P - A (A: first shell of the pair in kernel orientation)
   double sp;     // K / p with K = sqrt(2) pi^(5/4) c_a c_b exp(-a b |AB|^2 / p)
-  double pad;
+  float spf, pf; // FP32 copies of sp and p for the primitive-quartet pre-screen
 };
 
 struct PairDev {
@@ -44,6 +44,8 @@ struct BuildArgs {
   int nk;                  // number of exchange densities (1 RHF, 2 UHF/ROHF)
   double prim_cut;         // |K/p| pre-screen of a primitive pair
   double prim_cut2;        // (sp sq)^2 < prim_cut2 (p + q) skips a primitive quartet
+  float prim_cut_lo;       // FP32 decision band of that test: |sp sq| / sqrt(p+q) below lo
+  float prim_cut_hi;       // skips, above hi keeps, in between FP64 decides
   double elem_cut;         // element cutoff on |(ab|cd)|
   const double* dj;        // full nbf x nbf density for Coulomb
   const double* dk;        // nk full densities for exchange
@@ -51,6 +53,7 @@ struct BuildArgs {
   double* gk;              // nk x nbf x nbf exchange accumulators
   double* schwarz_out;     // Schwarz mode: per pair sqrt(max |(ab|ab)|)
   unsigned long long* counters;  // [0] primitive quartets evaluated by this launch
+  unsigned long long* work;      // work-distribution counter of this launch (zeroed before it)
 };
 
 // ---------------------------------------------------------------------------

@@ -33,25 +33,31 @@ namespace oqpg {
 #undef RYS_STORAGE
 
 __host__ __device__ constexpr int rys_xmax(int n) { return 32 + 8 * n; }
+__host__ __device__ constexpr int rys_nint(int n) { return RYS_X_SPLIT * RYS_LO_PER_UNIT + (rys_xmax(n) - RYS_X_SPLIT); }
 __host__ __device__ constexpr int rys_offset(int n) {  // start of the n-root table
-  return n <= 1 ? 0 : rys_offset(n - 1) + (32 + 2 * (n - 1)) * 2 * (n - 1) * RYS_NCOEF;
+  return n <= 1 ? 0 : rys_offset(n - 1) + rys_nint(n - 1) * 2 * (n - 1) * RYS_NCOEF;
 }
 
 // Quantity q of the N-root rule at X: q even -> node x_{q/2}, q odd -> weight w_{q/2}.
+// Interval k: width 1/4 below 32 (s = 8X - (2k+1)), unit width above
+// (s = 2X - (2 floor(X) + 1)).  X >= 0, so the range tests compare bit patterns
+// as integers (no FP64 instruction).
 template <int N>
 __device__ __forceinline__ double rys_quantity(double X, int q) {
-  if (X >= (double)rys_xmax(N)) {
+  const long long xb = __double_as_longlong(X);
+  if (xb >= __double_as_longlong((double)rys_xmax(N))) {
     const int r = (N * (N - 1)) / 2 + (q >> 1);
     return (q & 1) ? RYS_HERM_W[r] * rsqrt64(X) : RYS_HERM_R2[r] * rcp64(X);
   }
   int k;
   double s;
-  if (X < (double)RYS_X_SPLIT) {
-    k = __double2int_rz(X);
-    s = fma(2.0, X, -(double)(2 * k + 1));
+  if (xb < __double_as_longlong((double)RYS_X_SPLIT)) {
+    k = __double2int_rz(X * (double)RYS_LO_PER_UNIT);
+    s = fma(2.0 * RYS_LO_PER_UNIT, X, -(double)(2 * k + 1));
   } else {
-    k = RYS_X_SPLIT + __double2int_rz((X - (double)RYS_X_SPLIT) * 0.25);
-    s = fma(0.5, X, -(double)(RYS_X_SPLIT / 2 + 2 * (k - RYS_X_SPLIT) + 1));
+    const int f = __double2int_rz(X);
+    k = RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
+    s = fma(2.0, X, -(double)(2 * f + 1));
   }
   const double* c = RYS_TABLE + rys_offset(N) + (k * 2 * N + q) * RYS_NCOEF;
   double v = __ldg(c + RYS_NCOEF - 1);
@@ -78,11 +84,22 @@ struct PrimQuartet {
   double PQ[3];
 };
 
-__device__ __forceinline__ bool prim_quartet(const PrimPair& bp, const PrimPair& kp, double cut2, PrimQuartet& o) {
+// Primitive-quartet screen (sp sq)^2 < cut2 (p + q) of the rotated-axis engine
+// (int_rotaxis.F90:629), decided in FP32 unless |sp sq| / sqrt(p + q) falls in
+// the narrow band [lo, hi] around the cutoff, where FP64 decides.
+__device__ __forceinline__ bool prim_keep(const PrimPair& bp, const PrimPair& kp, const BuildArgs& a) {
+  const float r = fabsf(bp.spf * kp.spf) * rsqrtf(bp.pf + kp.pf);
+  if (r < a.prim_cut_lo) return false;
+  if (r > a.prim_cut_hi) return true;
+  const double fqz = bp.sp * kp.sp;
+  return !(fqz * fqz < a.prim_cut2 * (bp.p + kp.p));
+}
+
+__device__ __forceinline__ void prim_setup(const PrimPair& bp, const PrimPair& kp, PrimQuartet& o) {
   const double fqz = bp.sp * kp.sp;
   const double s = bp.p + kp.p;
-  if (fqz * fqz < cut2 * s) return false;
-  o.inv = rcp64(s);
+  const double y = rsqrt64(s);
+  o.inv = y * y;
   o.qi = kp.p * o.inv;
   o.pi = bp.p * o.inv;
   o.PQ[0] = bp.px - kp.px;
@@ -90,8 +107,7 @@ __device__ __forceinline__ bool prim_quartet(const PrimPair& bp, const PrimPair&
   o.PQ[2] = bp.pz - kp.pz;
   const double r2 = fma(o.PQ[0], o.PQ[0], fma(o.PQ[1], o.PQ[1], o.PQ[2] * o.PQ[2]));
   o.X = bp.p * o.qi * r2;
-  o.pref = fqz * rsqrt64(s);
-  return true;
+  o.pref = fqz * y;
 }
 
 // 2D integrals of one root and one Cartesian dimension:
@@ -173,7 +189,10 @@ __device__ __forceinline__ void prim_load(const PrimPair* __restrict__ src, Prim
   const double2* s = reinterpret_cast<const double2*>(src);
   double2 v0 = __ldg(s), v1 = __ldg(s + 1), v2 = __ldg(s + 2), v3 = __ldg(s + 3), v4 = __ldg(s + 4);
   d.p = v0.x; d.hp = v0.y; d.px = v1.x; d.py = v1.y; d.pz = v2.x; d.ax = v2.y; d.ay = v3.x; d.az = v3.y;
-  d.sp = v4.x; d.pad = v4.y;
+  d.sp = v4.x;
+  const long long bits = __double_as_longlong(v4.y);
+  d.spf = __int_as_float((int)(bits & 0xffffffffll));
+  d.pf = __int_as_float((int)(bits >> 32));
 }
 
 __device__ __forceinline__ double pick3(int d, double a, double b, double c) { return d == 0 ? a : (d == 1 ? b : c); }
@@ -216,33 +235,67 @@ __device__ __forceinline__ void project_regs(const double* in, double* out) {
 
 __device__ __forceinline__ double cut_elem(double v, double cut) { return fabs(v) < cut ? 0.0 : v; }
 
+// FP32 screening data (spf, pf) of a primitive pair: the last 8 bytes.
+__device__ __forceinline__ float2 prim_screen(const PrimPair* p) {
+  const long long bits = __double_as_longlong(__ldg(reinterpret_cast<const double*>(p) + 9));
+  return make_float2(__int_as_float((int)(bits & 0xffffffffll)), __int_as_float((int)(bits >> 32)));
+}
+__device__ __forceinline__ bool screen_keep(const PrimPair* bp, float2 bs, const PrimPair* kp, float2 ks,
+                                            const BuildArgs& a) {
+  const float r = fabsf(bs.x * ks.x) * rsqrtf(bs.y + ks.y);
+  if (r < a.prim_cut_lo) return false;
+  if (r > a.prim_cut_hi) return true;
+  const double* b = reinterpret_cast<const double*>(bp);
+  const double* k = reinterpret_cast<const double*>(kp);
+  const double fqz = __ldg(b + 8) * __ldg(k + 8);
+  return !(fqz * fqz < a.prim_cut2 * (__ldg(b) + __ldg(k)));
+}
+
+// Persistent-warp work distribution: warps take chunks of the (sorted) class
+// list from a global counter, heaviest quartets first.
+__device__ __forceinline__ long long grab(unsigned long long* counter, unsigned chunk, int lane) {
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk);
+  return (long long)__shfl_sync(0xffffffffu, base, 0);
+}
+
 // ===========================================================================
-// Small classes: one thread per quartet.
-template <int LA, int LB, int LC, int LD, bool PURE, bool SCH>
-__global__ void __launch_bounds__(128) k_small(const BuildArgs a) {
+// Small classes (at most 27 Cartesian elements): everything in registers.
+//
+// small_prims accumulates the primitive quartets c = first, first + step, ...
+// (c = kq * nP + kb) of one contracted quartet.  Each iteration of the FP64
+// body computes one surviving candidate of this lane: the cheap FP32 scan
+// skips screened candidates without holding the warp in the FP64 body.
+template <int LA, int LB, int LC, int LD>
+__device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P, const PairDev& Q,
+                                            const double AB[3], const double CD[3], int first, int step,
+                                            double* acc, unsigned long long& nprim) {
   using K = Cls<LA, LB, LC, LD>;
-  using E = Epi<LA, LB, LC, LD, PURE>;
   constexpr int NE = K::NE, NR = K::NR, N2D = K::N2D;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  unsigned long long nprim = 0;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < a.nquartets; t += stride) {
-    const uint2 qd = a.quartets[t];
-    const PairDev P = a.pairs[qd.x], Q = a.pairs[qd.y];
-    const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
-    const double AB[3] = {SA.x - SB.x, SA.y - SB.y, SA.z - SB.z};
-    const double CD[3] = {SC.x - SD.x, SC.y - SD.y, SC.z - SD.z};
-    double acc[NE];
-#pragma unroll
-    for (int e = 0; e < NE; ++e) acc[e] = 0.0;
-    for (int kq = 0; kq < Q.pcnt; ++kq) {
-      PrimPair kp;
-      prim_load(a.prims + Q.poff + kq, kp);
-      for (int kb = 0; kb < P.pcnt; ++kb) {
-        PrimPair bp;
-        prim_load(a.prims + P.poff + kb, bp);
-        PrimQuartet pq;
-        if (!prim_quartet(bp, kp, a.prim_cut2, pq)) continue;
-        ++nprim;
+  const PrimPair* bpp = a.prims + P.poff;
+  const PrimPair* kpp = a.prims + Q.poff;
+  const int nP = P.pcnt, nQ = Q.pcnt;
+  if (nP == 0 || nQ == 0) return;
+  int kq = first / nP, kb = first - kq * nP;
+  int kq_loaded = -1;
+  float2 ks = make_float2(0.f, 1.f);
+  for (;;) {
+    int cb = -1, cq = -1;
+    while (kq < nQ) {
+      if (kq != kq_loaded) { ks = prim_screen(kpp + kq); kq_loaded = kq; }
+      const int b = kb, q = kq;
+      kb += step;
+      while (kb >= nP) { kb -= nP; ++kq; }
+      if (screen_keep(bpp + b, prim_screen(bpp + b), kpp + q, ks, a)) { cb = b; cq = q; break; }
+    }
+    if (cb < 0) break;
+    {
+      PrimPair bp, kp;
+      prim_load(bpp + cb, bp);
+      prim_load(kpp + cq, kp);
+      PrimQuartet pq;
+      prim_setup(bp, kp, pq);
+      ++nprim;
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
           const double u = rys_quantity<NR>(pq.X, 2 * r);
@@ -266,7 +319,18 @@ __global__ void __launch_bounds__(128) k_small(const BuildArgs a) {
         }
       }
     }
-    // normalise and project
+}
+
+// Normalisation, pure projection, element cutoff and digestion of one
+// contracted small-class quartet (single lane).
+template <int LA, int LB, int LC, int LD, bool PURE, bool SCH>
+__device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, const PairDev& P, const PairDev& Q,
+                                               double* acc) {
+  using K = Cls<LA, LB, LC, LD>;
+  using E = Epi<LA, LB, LC, LD, PURE>;
+  constexpr int NE = K::NE;
+  {
+    const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
 #pragma unroll
     for (int e = 0; e < NE; ++e) acc[e] *= K::norm(e);
     constexpr int DA = K::NA, DB = K::NB, DC = K::NC, DD = K::ND;
@@ -281,7 +345,7 @@ __global__ void __launch_bounds__(128) k_small(const BuildArgs a) {
 #pragma unroll
       for (int e = 0; e < E::NEP; ++e) m = fmax(m, fabs(V[e]));
       a.schwarz_out[qd.x] = sqrt(m);
-      continue;
+      return;
     }
 #pragma unroll
     for (int e = 0; e < E::NEP; ++e) V[e] = cut_elem(V[e], a.elem_cut);
@@ -383,6 +447,72 @@ __global__ void __launch_bounds__(128) k_small(const BuildArgs a) {
       }
     }
   }
+}
+
+template <int LA, int LB, int LC, int LD>
+__device__ __forceinline__ void quartet_geometry(const BuildArgs& a, uint2 qd, PairDev& P, PairDev& Q, double AB[3],
+                                                 double CD[3]) {
+  P = a.pairs[qd.x];
+  Q = a.pairs[qd.y];
+  const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
+  AB[0] = SA.x - SB.x; AB[1] = SA.y - SB.y; AB[2] = SA.z - SB.z;
+  CD[0] = SC.x - SD.x; CD[1] = SC.y - SD.y; CD[2] = SC.z - SD.z;
+}
+
+// One thread per quartet; warps take chunks of 32 consecutive quartets of the
+// sorted list (similar primitive counts on all lanes).
+template <int LA, int LB, int LC, int LD, bool PURE, bool SCH>
+__global__ void __launch_bounds__(128) k_small(const BuildArgs a) {
+  constexpr int NE = Cls<LA, LB, LC, LD>::NE;
+  const int lane = threadIdx.x & 31;
+  unsigned long long nprim = 0;
+  for (;;) {
+    const long long base = grab(a.work, 32u, lane);
+    if (base >= a.nquartets) break;
+    const long long t = base + lane;
+    if (t < a.nquartets) {
+      const uint2 qd = a.quartets[t];
+      PairDev P, Q;
+      double AB[3], CD[3];
+      quartet_geometry<LA, LB, LC, LD>(a, qd, P, Q, AB, CD);
+      double acc[NE];
+#pragma unroll
+      for (int e = 0; e < NE; ++e) acc[e] = 0.0;
+      small_prims<LA, LB, LC, LD>(a, P, Q, AB, CD, 0, 1, acc, nprim);
+      small_epilogue<LA, LB, LC, LD, PURE, SCH>(a, qd, P, Q, acc);
+    }
+  }
+  if (a.counters && nprim) atomicAdd(a.counters, nprim);
+}
+
+// Heavily contracted small-class quartets: one warp per quartet, the lanes
+// split its primitive quartets, the partial blocks are summed across the warp.
+template <int LA, int LB, int LC, int LD, bool PURE>
+__global__ void __launch_bounds__(128) k_prim(const BuildArgs a) {
+  constexpr int NE = Cls<LA, LB, LC, LD>::NE;
+  const int lane = threadIdx.x & 31;
+  unsigned long long nprim = 0;
+  for (;;) {
+    const long long t = grab(a.work, 1u, lane);
+    if (t >= a.nquartets) break;
+    const uint2 qd = a.quartets[t];
+    PairDev P, Q;
+    double AB[3], CD[3];
+    quartet_geometry<LA, LB, LC, LD>(a, qd, P, Q, AB, CD);
+    double acc[NE];
+#pragma unroll
+    for (int e = 0; e < NE; ++e) acc[e] = 0.0;
+    small_prims<LA, LB, LC, LD>(a, P, Q, AB, CD, lane, 32, acc, nprim);
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+      double v = acc[e];
+#pragma unroll
+      for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+      acc[e] = v;
+    }
+    if (lane == 0) small_epilogue<LA, LB, LC, LD, PURE, false>(a, qd, P, Q, acc);
+    __syncwarp();
+  }
   if (a.counters && nprim) atomicAdd(a.counters, nprim);
 }
 
@@ -432,9 +562,10 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
     }
     offs[k] = o;
   }
-  const long long nteams = (long long)gridDim.x * (blockDim.x >> 5);
   unsigned long long nprim = 0;
-  for (long long t = (long long)blockIdx.x * (blockDim.x >> 5) + warp; t < a.nquartets; t += nteams) {
+  for (;;) {
+    const long long t = grab(a.work, 1u, lane);
+    if (t >= a.nquartets) break;
     const uint2 qd = a.quartets[t];
     const PairDev P = a.pairs[qd.x], Q = a.pairs[qd.y];
     const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
@@ -444,13 +575,15 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
 #pragma unroll
     for (int k = 0; k < KE; ++k) acc[k] = 0.0;
     for (int kq = 0; kq < Q.pcnt; ++kq) {
-      PrimPair kp;
+      PrimPair kp, bn;
       prim_load(a.prims + Q.poff + kq, kp);
+      if (P.pcnt > 0) prim_load(a.prims + P.poff, bn);
       for (int kb = 0; kb < P.pcnt; ++kb) {
-        PrimPair bp;
-        prim_load(a.prims + P.poff + kb, bp);
+        const PrimPair bp = bn;
+        if (kb + 1 < P.pcnt) prim_load(a.prims + P.poff + kb + 1, bn);  // prefetch
+        if (!prim_keep(bp, kp, a)) continue;
         PrimQuartet pq;
-        if (!prim_quartet(bp, kp, a.prim_cut2, pq)) continue;
+        prim_setup(bp, kp, pq);
         ++nprim;
         if (lane < 2 * NR) {
           const double v = rys_quantity<NR>(pq.X, lane);

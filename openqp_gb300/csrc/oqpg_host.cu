@@ -28,16 +28,16 @@ static const ClassInfo kClasses[NCLASS] = {
 };
 const ClassInfo& class_info(int c) { return kClasses[c]; }
 
-cudaError_t launch_class(int c, bool pure, bool sch, const BuildArgs& a, int nsm, cudaStream_t st) {
+cudaError_t launch_class(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
   switch (c) {
     case 0: case 1: case 2: case 3: case 4: case 6: case 7: case 8:
-      return launch_group0(c, pure, sch, a, nsm, st);
+      return launch_group0(c, pure, mode, a, nsm, st);
     case 5: case 9: case 10: case 11: case 12: case 15:
-      return launch_group1(c, pure, sch, a, nsm, st);
+      return launch_group1(c, pure, mode, a, nsm, st);
     case 13: case 14: case 16: case 17:
-      return launch_group2(c, pure, sch, a, nsm, st);
+      return launch_group2(c, pure, mode, a, nsm, st);
     default:
-      return launch_group3(c, pure, sch, a, nsm, st);
+      return launch_group3(c, pure, mode, a, nsm, st);
   }
 }
 
@@ -100,6 +100,8 @@ struct ListArgs {
   const int* pair_type;
   const double* q;          // Schwarz bound per pair
   const float* qf;
+  const int* sorted_idx;    // pairs by descending Schwarz bound
+  const double* sorted_q;
   const double* dsh;
   const float* dshf;
   const unsigned long long* dmax_bits;
@@ -113,15 +115,32 @@ struct ListArgs {
 // Screened quartet lists, one CTA per bra pair P (the larger pair index of the
 // canonical quartet, int2.F90:755-805): pair screen Q_P Dmax >= tau, then for
 // every Q <= P the quartet screen Q_P Q_Q max(4D_ij, 4D_kl, D_jl, D_jk, D_il, D_ik)
-// >= tau (int2.F90:975-986).  FP32 decides when it is clear by a 1e-5 margin,
-// FP64 with the reference's operation order otherwise.
+// >= tau (int2.F90:975-986).  Since the max is at most 4 Dmax, only the pairs
+// with Q_Q >= tau / (4 Q_P Dmax) can pass: they are a prefix of the pairs
+// sorted by Schwarz bound, and only that prefix is walked.  FP32 decides when
+// it is clear by a 1e-5 margin, FP64 with the reference's operation order
+// otherwise.
 __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
   __shared__ unsigned cnt[NCLASS];
   __shared__ unsigned long long base[NCLASS];
+  __shared__ int s_len;
   const int P = blockIdx.x;
   const double dmax = __longlong_as_double((long long)*a.dmax_bits);
   const double qP = a.q[P];
   if (qP * dmax < a.tau) return;
+  if (threadIdx.x == 0) {
+    // number of pairs with q >= thr (q descending), with a rounding margin
+    const double thr = a.tau / (4.0 * qP * dmax) * (1.0 - 1e-9);
+    int lo = 0, hi = a.npair;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (a.sorted_q[mid] >= thr) lo = mid + 1;
+      else hi = mid;
+    }
+    s_len = lo;
+  }
+  __syncthreads();
+  const int len = s_len;
   const int2 ij = a.pair_ij[P];
   const int tP = a.pair_type[P];
   const float qPf = a.qf[P];
@@ -129,10 +148,11 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
   const float* dj = a.dshf + (long long)ij.y * a.ns;
   const float dij4 = 4.0f * di[ij.y];
   const float tlo = (float)(a.tau * (1.0 - 1e-5)), thi = (float)(a.tau * (1.0 + 1e-5));
-  for (int q0 = 0; q0 <= P; q0 += blockDim.x) {
+  for (int s0 = 0; s0 < len; s0 += blockDim.x) {
     if (threadIdx.x < NCLASS) cnt[threadIdx.x] = 0;
     __syncthreads();
-    const int Q = q0 + threadIdx.x;
+    const int s = s0 + threadIdx.x;
+    const int Q = s < len ? a.sorted_idx[s] : a.npair;
     int c = -1;
     unsigned slot = 0;
     uint2 ent;
@@ -167,6 +187,58 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
       if (pos < a.caps[c]) a.lists[c][pos] = ent;
     }
     __syncthreads();
+  }
+}
+
+// Counting sort of a class list by primitive-quartet count (descending, in
+// quarter-octave bins), so that the lanes of a warp run loops of similar
+// length.  k_bin_hist: per-bin counts; k_bin_scatter: stable-per-CTA scatter
+// into the bin ranges given by the exclusive scan in cursors.
+constexpr int NBIN = 64;
+constexpr int PRIM_SPLIT_LOG2 = 8;  // >= 256 primitive quartets: warp per quartet
+
+__device__ __forceinline__ int prim_bin(const PairDev* pairs, uint2 q) {
+  const int n = pairs[q.x].pcnt * pairs[q.y].pcnt;
+  if (n <= 1) return NBIN - 1;
+  const int k = (int)(4.0f * __log2f((float)n));
+  return NBIN - 1 - (k < NBIN - 1 ? k : NBIN - 1);
+}
+
+__global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const PairDev* __restrict__ pairs,
+                           unsigned long long* hist) {
+  __shared__ unsigned h[NBIN];
+  for (int i = threadIdx.x; i < NBIN; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    atomicAdd(&h[prim_bin(pairs, list[t])], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < NBIN; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], (unsigned long long)h[i]);
+}
+
+// Each CTA takes a contiguous chunk, reserves its per-bin ranges once, then
+// places its entries.
+__global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ list, long long n,
+                                                     const PairDev* __restrict__ pairs, unsigned long long* cursors,
+                                                     uint2* out, long long chunk) {
+  __shared__ unsigned h[NBIN];
+  __shared__ unsigned long long b[NBIN];
+  const long long lo = blockIdx.x * chunk;
+  const long long hi = lo + chunk < n ? lo + chunk : n;
+  for (int i = threadIdx.x; i < NBIN; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) atomicAdd(&h[prim_bin(pairs, list[t])], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < NBIN; i += blockDim.x) {
+    b[i] = h[i] ? atomicAdd(&cursors[i], (unsigned long long)h[i]) : 0ull;
+    h[i] = 0;
+  }
+  __syncthreads();
+  for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+    const uint2 q = list[t];
+    const int bin = prim_bin(pairs, q);
+    const unsigned r = atomicAdd(&h[bin], 1u);
+    out[b[bin] + r] = q;
   }
 }
 
@@ -231,7 +303,8 @@ struct oqpg_ctx {
   DevBuf d_shells, d_pairs, d_prims, d_pair_ij, d_pair_type, d_q, d_qf, d_aoff, d_naos;
   // per-build buffers
   DevBuf d_dp, d_dj, d_dk, d_gj, d_gk, d_f, d_fold, d_dsh, d_dshf, d_dmax, d_counts, d_prim_counter;
-  DevBuf d_lists[NCLASS];
+  DevBuf d_lists[NCLASS], d_slists[NCLASS];
+  DevBuf d_sorted_idx, d_sorted_q, d_hist, d_cursor, d_work;
   unsigned long long caps[NCLASS] = {0};
   unsigned long long counts[NCLASS] = {0};
   bool have_caps = false;
@@ -306,7 +379,7 @@ void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vecto
           pp.py = (a1 * A.y + a2 * B.y) * gi;
           pp.pz = (a1 * A.z + a2 * B.z) * gi;
           pp.ax = pp.px - A.x; pp.ay = pp.py - A.y; pp.az = pp.pz - A.z;
-          pp.sp = sp; pp.pad = 0.0;
+          pp.sp = sp; pp.spf = (float)sp; pp.pf = (float)g;
           out.prims.push_back(pp);
         }
       pd.pcnt = (int)out.prims.size() - pd.poff;
@@ -314,6 +387,20 @@ void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vecto
       out.ij.push_back(make_int2(i, j));
       out.type.push_back(pair_type(am[sa], am[sb]));
     }
+}
+
+// FP32 decision band of the primitive-quartet screen: |sp sq| / sqrt(p+q)
+// against sqrt(prim_cut2).  FP32 products of two screened prefactors stay
+// normal down to prim_cut ~ 1e-18; below that every decision goes to FP64.
+void set_band(BuildArgs& a) {
+  const double c = std::sqrt(a.prim_cut2);
+  if (c >= 1e-18) {
+    a.prim_cut_lo = (float)(c * (1.0 - 1e-4));
+    a.prim_cut_hi = (float)(c * (1.0 + 1e-4));
+  } else {
+    a.prim_cut_lo = 0.0f;
+    a.prim_cut_hi = 3.0e38f;
+  }
 }
 
 template <typename T>
@@ -385,8 +472,12 @@ int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const 
     a.nbf = c->nbf;
     a.prim_cut = 1e-17;
     a.prim_cut2 = 1e-34;
+    set_band(a);
     a.schwarz_out = d_q.as<double>();
-    CK(launch_class(cl, c->pure, true, a, c->nsm, st));
+    CK(c->d_work.ensure(sizeof(unsigned long long) * 2 * NCLASS));
+    CK(cudaMemsetAsync(c->d_work.p, 0, sizeof(unsigned long long), st));
+    a.work = c->d_work.as<unsigned long long>();
+    CK(launch_class(cl, c->pure, MODE_SCHWARZ, a, c->nsm, st));
     CK(cudaStreamSynchronize(st));  // d_diag is reused by the next class
   }
   c->schwarz_pair.resize(c->npair);
@@ -406,6 +497,14 @@ int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const 
   std::vector<float> qf(c->npair);
   for (int p = 0; p < c->npair; ++p) qf[p] = (float)c->schwarz_pair[p];
   if ((rc = upload(c->d_qf, qf, st))) return rc;
+  std::vector<int> order(c->npair);
+  for (int p = 0; p < c->npair; ++p) order[p] = p;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return c->schwarz_pair[x] > c->schwarz_pair[y]; });
+  std::vector<double> sq(c->npair);
+  for (int p = 0; p < c->npair; ++p) sq[p] = c->schwarz_pair[order[p]];
+  if ((rc = upload(c->d_sorted_idx, order, st))) return rc;
+  if ((rc = upload(c->d_sorted_q, sq, st))) return rc;
   CK(cudaStreamSynchronize(st));
   return OK;
 }
@@ -417,6 +516,9 @@ void ctx_free(oqpg_ctx* c) {
                     &c->d_fold, &c->d_dsh, &c->d_dshf, &c->d_dmax, &c->d_counts, &c->d_prim_counter};
   for (DevBuf* b : bufs) b->release();
   for (auto& b : c->d_lists) b.release();
+  for (auto& b : c->d_slists) b.release();
+  c->d_sorted_idx.release(); c->d_sorted_q.release(); c->d_hist.release(); c->d_cursor.release();
+  c->d_work.release();
   if (c->h_in) cudaFreeHost(c->h_in);
   if (c->h_out) cudaFreeHost(c->h_out);
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);
@@ -442,6 +544,7 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
   CK(c->d_dmax.ensure(sizeof(unsigned long long)));
   CK(c->d_counts.ensure(sizeof(unsigned long long) * NCLASS));
   CK(c->d_prim_counter.ensure(sizeof(unsigned long long) * NCLASS));
+  CK(c->d_work.ensure(sizeof(unsigned long long) * 2 * NCLASS));
   CK(cudaEventRecord(c->ev[0], st));
   k_unpack<<<std::min<long long>((n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(dp, nfocks, n, c->d_dj.as<double>(),
                                                                                  c->d_dk.as<double>());
@@ -458,6 +561,7 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
   la.pair_ij = c->d_pair_ij.as<int2>();
   la.pair_type = c->d_pair_type.as<int>();
   la.q = c->d_q.as<double>(); la.qf = c->d_qf.as<float>();
+  la.sorted_idx = c->d_sorted_idx.as<int>(); la.sorted_q = c->d_sorted_q.as<double>();
   la.dsh = c->d_dsh.as<double>(); la.dshf = c->d_dshf.as<float>();
   la.dmax_bits = c->d_dmax.as<unsigned long long>();
   la.tau = c->tau;
@@ -490,11 +594,42 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
     c->have_caps = true;
   }
   if (!lists_ok) return DEV_ERR;  // quartet lists never fitted: do not launch on partial lists
+  // --- order every class list by primitive-quartet count (counting sort)
+  CK(c->d_hist.ensure(sizeof(unsigned long long) * NCLASS * NBIN));
+  CK(c->d_cursor.ensure(sizeof(unsigned long long) * NCLASS * NBIN));
+  CK(cudaMemsetAsync(c->d_hist.p, 0, sizeof(unsigned long long) * NCLASS * NBIN, st));
+  for (int k = 0; k < NCLASS; ++k) {
+    if (!c->counts[k]) continue;
+    const long long nk_ = (long long)c->counts[k];
+    k_bin_hist<<<(unsigned)std::min<long long>((nk_ + 255) / 256, c->nsm * 4LL), 256, 0, st>>>(
+        c->d_lists[k].as<uint2>(), nk_, c->d_pairs.as<PairDev>(), c->d_hist.as<unsigned long long>() + k * NBIN);
+    CK(cudaGetLastError());
+  }
+  std::vector<unsigned long long> hist(NCLASS * NBIN), cur(NCLASS * NBIN);
+  CK(cudaMemcpyAsync(hist.data(), c->d_hist.p, sizeof(unsigned long long) * NCLASS * NBIN, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (int k = 0; k < NCLASS; ++k) {
+    unsigned long long s = 0;
+    for (int b = 0; b < NBIN; ++b) { cur[k * NBIN + b] = s; s += hist[k * NBIN + b]; }
+    if (s != c->counts[k]) return DEV_ERR;
+  }
+  CK(cudaMemcpyAsync(c->d_cursor.p, cur.data(), sizeof(unsigned long long) * NCLASS * NBIN, cudaMemcpyHostToDevice, st));
+  for (int k = 0; k < NCLASS; ++k) {
+    if (!c->counts[k]) continue;
+    const long long nk_ = (long long)c->counts[k];
+    CK(c->d_slists[k].ensure(sizeof(uint2) * nk_));
+    const long long chunk = 4096;
+    k_bin_scatter<<<(unsigned)((nk_ + chunk - 1) / chunk), 256, 0, st>>>(
+        c->d_lists[k].as<uint2>(), nk_, c->d_pairs.as<PairDev>(), c->d_cursor.as<unsigned long long>() + k * NBIN,
+        c->d_slists[k].as<uint2>(), chunk);
+    CK(cudaGetLastError());
+  }
   CK(cudaEventRecord(c->ev[1], st));
   // --- integrals + digestion
   CK(cudaMemsetAsync(c->d_gj.p, 0, sizeof(double) * n2, st));
   CK(cudaMemsetAsync(c->d_gk.p, 0, sizeof(double) * nk * n2, st));
   CK(cudaMemsetAsync(c->d_prim_counter.p, 0, sizeof(unsigned long long) * NCLASS, st));
+  CK(cudaMemsetAsync(c->d_work.p, 0, sizeof(unsigned long long) * 2 * NCLASS, st));
   BuildArgs a{};
   a.shells = c->d_shells.as<ShellDev>();
   a.pairs = c->d_pairs.as<PairDev>();
@@ -503,6 +638,7 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
   a.nk = nk;
   a.prim_cut = 1e-4 * c->tau;
   a.prim_cut2 = a.prim_cut * a.prim_cut;
+  set_band(a);
   a.elem_cut = c->tau;
   a.dj = c->d_dj.as<double>();
   a.dk = (nk == 1) ? c->d_dj.as<double>() : c->d_dk.as<double>();
@@ -513,14 +649,30 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
   int nlaunch = 0;
   for (int cl = NCLASS - 1; cl >= 0; --cl) {
     if (c->counts[cl] == 0) continue;
-    a.quartets = c->d_lists[cl].as<uint2>();
-    a.nquartets = (long long)c->counts[cl];
     a.counters = c->d_prim_counter.as<unsigned long long>() + cl;
     nq += (double)c->counts[cl];
     CK(cudaEventRecord(c->evc[cl][0], st));
-    CK(launch_class(cl, c->pure, false, a, c->nsm, st));
+    long long head = 0;
+    if (!class_info(cl).team) {
+      // quartets with >= 2^PRIM_SPLIT_LOG2 primitive quartets (a prefix of the
+      // sorted list) go to the warp-per-quartet primitive-parallel kernel
+      for (int b = 0; b <= NBIN - 1 - 4 * PRIM_SPLIT_LOG2; ++b) head += (long long)hist[cl * NBIN + b];
+      if (head > 0) {
+        a.quartets = c->d_slists[cl].as<uint2>();
+        a.nquartets = head;
+        a.work = c->d_work.as<unsigned long long>() + NCLASS + cl;
+        CK(launch_class(cl, c->pure, MODE_PRIM, a, c->nsm, st));
+        ++nlaunch;
+      }
+    }
+    if ((long long)c->counts[cl] > head) {
+      a.quartets = c->d_slists[cl].as<uint2>() + head;
+      a.nquartets = (long long)c->counts[cl] - head;
+      a.work = c->d_work.as<unsigned long long>() + cl;
+      CK(launch_class(cl, c->pure, MODE_FOCK, a, c->nsm, st));
+      ++nlaunch;
+    }
     CK(cudaEventRecord(c->evc[cl][1], st));
-    ++nlaunch;
   }
   CK(cudaEventRecord(c->ev[2], st));
   const long long ntri = (long long)n * (n + 1) / 2;

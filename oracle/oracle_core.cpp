@@ -62,8 +62,9 @@ void rys_eval(int n, double X, double* x, double* w) {
   }
   int k;
   double a, h;
-  if (X < RYS_X_SPLIT) { k = (int)X; a = k; h = 1.0; }
-  else { k = RYS_X_SPLIT + (int)((X - RYS_X_SPLIT) / RYS_W_HI); a = RYS_X_SPLIT + (k - RYS_X_SPLIT) * RYS_W_HI; h = RYS_W_HI; }
+  const int k0 = RYS_X_SPLIT * RYS_LO_PER_UNIT;
+  if (X < RYS_X_SPLIT) { k = (int)(X * RYS_LO_PER_UNIT); h = 1.0 / RYS_LO_PER_UNIT; a = k * h; }
+  else { k = k0 + (int)((X - RYS_X_SPLIT) / RYS_W_HI); a = RYS_X_SPLIT + (k - k0) * RYS_W_HI; h = RYS_W_HI; }
   const double s = 2.0 * (X - a) / h - 1.0;
   const double* t = RYS_TABLE + RYS_OFFSET[n - 1] + (size_t)k * 2 * n * RYS_NCOEF;
   for (int i = 0; i < n; ++i) {
