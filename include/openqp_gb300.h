@@ -85,6 +85,22 @@ int oqpg_fock_jk(oqpg_ctx* ctx, const double* d, double* f, int nfocks, double s
 int oqpg_fock_jk_device(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, double se,
                         double sc, void* stream);
 
+/* The same build as oqpg_fock_jk_device for callers that cannot allocate
+ * device memory while they build Fock matrices (a host whose own pool
+ * allocator owns all device memory, or a loop that cannot take the device
+ * synchronisation of cudaMalloc/cudaFree).  It calls no cudaMalloc, cudaFree
+ * or other allocating routine: every per-build buffer lives in one static
+ * 24 MiB device array that each GPU loading the library holds until exit.
+ * Limits: nbf <= 128, nshell <= 128, at most ~1.5 million screened quartets;
+ * larger inputs return 5 before any kernel runs.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current, so make that first call before any stream capture.  All calls share
+ * the array and each clears what must start at zero; calls that overlap on the
+ * GPU race on it.  The context itself (read-only tables) comes from
+ * oqpg_create.  There is no counterpart of this entry point in the reference. */
+int oqpg_fock_jk_noalloc(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, double se,
+                         double sc, void* stream);
+
 /* Schwarz bounds sqrt(max |(ab|ab)|) per shell pair, nshell x nshell (host). */
 int oqpg_schwarz(const oqpg_ctx* ctx, double* q);
 

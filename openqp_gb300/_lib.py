@@ -36,6 +36,8 @@ def lib():
         L.oqpg_fock_jk.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.oqpg_fock_jk_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+        L.oqpg_fock_jk_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
         L.oqpg_schwarz.argtypes = [ctypes.c_void_p, _d]
         L.oqpg_stats.argtypes = [ctypes.c_void_p, _d, ctypes.c_int]
         L.oqpg_class_l.argtypes = [ctypes.c_int, _i]

@@ -10,11 +10,9 @@
 #include <vector>
 
 #include "../../include/openqp_gb300.h"
-#include "oqpg_classes.h"
+#include "oqpg_internal.h"
 
 namespace oqpg {
-
-enum Status { OK = 0, NOT_INIT = 1, NO_MEM = 2, UNSUPPORTED = 3, DEV_ERR = 4 };
 
 static const ClassInfo kClasses[NCLASS] = {
 #define C_(a, b, c, d) {{a, b, c, d}, (ncart(a) * ncart(b) * ncart(c) * ncart(d) > 27), 0, 0}
@@ -94,23 +92,6 @@ __global__ void k_dsh(const double* __restrict__ dp, int nfocks, int nbf, int ns
   }
 }
 
-struct ListArgs {
-  int npair, ns;
-  const int2* pair_ij;      // shells (i >= j) of each pair, canonical order
-  const int* pair_type;
-  const double* q;          // Schwarz bound per pair
-  const float* qf;
-  const int* sorted_idx;    // pairs by descending Schwarz bound
-  const double* sorted_q;
-  const double* dsh;
-  const float* dshf;
-  const unsigned long long* dmax_bits;
-  double tau;
-  unsigned long long* counts;   // NCLASS
-  uint2* lists[NCLASS];
-  unsigned long long caps[NCLASS];
-  int write;
-};
 
 // Screened quartet lists, one CTA per bra pair P (the larger pair index of the
 // canonical quartet, int2.F90:755-805): pair screen Q_P Dmax >= tau, then for
@@ -194,8 +175,6 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
 // quarter-octave bins), so that the lanes of a warp run loops of similar
 // length.  k_bin_hist: per-bin counts; k_bin_scatter: stable-per-CTA scatter
 // into the bin ranges given by the exclusive scan in cursors.
-constexpr int NBIN = 64;
-constexpr int PRIM_SPLIT_LOG2 = 8;  // >= 256 primitive quartets: warp per quartet
 
 __device__ __forceinline__ int prim_bin(const PairDev* pairs, uint2 q) {
   const int n = pairs[q.x].pcnt * pairs[q.y].pcnt;
@@ -265,57 +244,10 @@ __global__ void k_finalize(const double* __restrict__ gj, const double* __restri
   }
 }
 
-// ---------------------------------------------------------------------------
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  cudaError_t ensure(size_t b) {
-    if (b <= bytes) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    cudaError_t e = cudaMalloc(&p, b);
-    if (e == cudaSuccess) bytes = b;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-  template <typename T> T* as() const { return (T*)p; }
-};
 
 }  // namespace oqpg
 
 using namespace oqpg;
-
-struct oqpg_ctx {
-  int dev = 0, nsm = 152;
-  cudaStream_t stream = nullptr;
-  int nshell = 0, nbf = 0, natom = 0, npair = 0;
-  bool pure = false;
-  double tau = 1e-10;
-  std::vector<ShellDev> shells;
-  std::vector<int> aoff, naos;
-  std::vector<double> schwarz_pair;   // per pair (canonical index)
-  // device tables
-  DevBuf d_shells, d_pairs, d_prims, d_pair_ij, d_pair_type, d_q, d_qf, d_aoff, d_naos;
-  // per-build buffers
-  DevBuf d_dp, d_dj, d_dk, d_gj, d_gk, d_f, d_fold, d_dsh, d_dshf, d_dmax, d_counts, d_prim_counter;
-  DevBuf d_lists[NCLASS], d_slists[NCLASS];
-  DevBuf d_sorted_idx, d_sorted_q, d_hist, d_cursor, d_work;
-  unsigned long long caps[NCLASS] = {0};
-  unsigned long long counts[NCLASS] = {0};
-  bool have_caps = false;
-  // pinned staging
-  double* h_in = nullptr;
-  double* h_out = nullptr;
-  size_t h_bytes = 0;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  cudaEvent_t evc[NCLASS][2] = {};
-  double last_stats[8 + 3 * NCLASS] = {0};
-};
 
 namespace {
 
@@ -389,10 +321,12 @@ void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vecto
     }
 }
 
+}  // namespace
+
 // FP32 decision band of the primitive-quartet screen: |sp sq| / sqrt(p+q)
 // against sqrt(prim_cut2).  FP32 products of two screened prefactors stay
 // normal down to prim_cut ~ 1e-18; below that every decision goes to FP64.
-void set_band(BuildArgs& a) {
+void oqpg::set_band(BuildArgs& a) {
   const double c = std::sqrt(a.prim_cut2);
   if (c >= 1e-18) {
     a.prim_cut_lo = (float)(c * (1.0 - 1e-4));
@@ -402,6 +336,8 @@ void set_band(BuildArgs& a) {
     a.prim_cut_hi = 3.0e38f;
   }
 }
+
+namespace {
 
 template <typename T>
 int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
