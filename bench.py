@@ -45,6 +45,9 @@ WORKLOADS = {
                           basis="cc-pvdz", cutoff=1e-10),
     "water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian RHF J+K Fock build", nwater=16, edge=9.52, seed=0,
                           basis="6-31g(d)", cutoff=1e-10),
+    # linear all-trans C40H82, 6-31G(d) Cartesian (the precision-split configuration)
+    "alkane40_631gd": dict(name="C40H82 6-31G(d) Cartesian RHF J+K Fock build", alkane=40, seed=0,
+                           basis="6-31g(d)", cutoff=1e-10),
     # only the d shells of a (H2O)64 6-31G(d) cluster: every quartet is (dd|dd)
     "dd_only": dict(name="(dd|dd)-only: the 64 d shells of a (H2O)64 6-31G(d) cluster", nwater=64, edge=15.1,
                     seed=0, basis="6-31g(d)", cutoff=1e-10, only_l=2),
@@ -56,7 +59,13 @@ def make_workload():
     from openqp_gb300 import workloads
     from openqp_gb300.basis import BasisArrays
     from openqp_gb300.onee import overlap_kinetic
-    bas = workloads.water_cluster_basis(WORKLOAD["nwater"], WORKLOAD["edge"], WORKLOAD["seed"], WORKLOAD["basis"])
+    from openqp_gb300.basis import build_basis
+    if "alkane" in WORKLOAD:
+        z, xyz = workloads.alkane(WORKLOAD["alkane"], WORKLOAD["seed"])
+        bas = build_basis(z, xyz, WORKLOAD["basis"])
+    else:
+        bas = workloads.water_cluster_basis(WORKLOAD["nwater"], WORKLOAD["edge"], WORKLOAD["seed"],
+                                            WORKLOAD["basis"])
     if "only_l" in WORKLOAD:
         keep = np.where(bas.am == WORKLOAD["only_l"])[0]
         offs = np.concatenate([[0], np.cumsum(bas.ncontr)])
@@ -190,38 +199,53 @@ def run_ours(args):
     out = torch.empty_like(dt)
     st = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    for _ in range(args.warmup):
-        fb.fock_jk_device(dt, out=out)
-    torch.cuda.synchronize()
+
+    def timed(precision):
+        fb.set_precision(precision, args.mixed_threshold)
+        for _ in range(args.warmup):
+            fb.fock_jk_device(dt, out=out)
+        torch.cuda.synchronize()
+        times, stats = [], []
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fb.fock_jk_device(dt, out=out, stream=st)
+            e1.record(st)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            stats.append(fb.stats())
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        tsum = sum(times) / 1000.0
+        if ws > 1:
+            t = torch.tensor([tsum], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            tsum = float(t.item())
+        return tsum, stats, out.clone()
+
+    mixed = None
+    if args.precision == "mixed":
+        t64, _, f64 = timed("fp64")
     sampler = ClockSampler(local)
     sampler.start()
-    times = []
-    stats = []
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
     wall0 = time.perf_counter()
-    for _ in range(args.steps):
-        flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        fb.fock_jk_device(dt, out=out, stream=st)
-        e1.record(st)
-        e1.synchronize()
-        times.append(e0.elapsed_time(e1))
-        stats.append(fb.stats())
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
+    tsum, stats, fval = timed(args.precision)
     wall = time.perf_counter() - wall0
     clocks = sampler.stop()
-    tsum = sum(times) / 1000.0
-    if ws > 1:
-        t = torch.tensor([tsum], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tsum = float(t.item())
     value = ws * args.steps / tsum
+    if args.precision == "mixed":
+        from openqp_gb300.basis import unpack
+        df = (fval - f64).cpu().numpy()[0]
+        de2 = 0.5 * float(np.sum(unpack(d, bas.nbf) * unpack(df, bas.nbf)))
+        mixed = {"threshold": args.mixed_threshold, "fp64_builds_per_s": ws * args.steps / t64,
+                 "speedup_vs_fp64": t64 / tsum, "max_abs_dF": float(np.abs(df).max()),
+                 "dE2_Eh": de2, "f32_quartet_fraction": stats[-1]["f32_quartets"] / max(1, stats[-1]["quartets"])}
     # e2e through the seam with host buffers
     e2e_t = [float("nan")]
     if not args.no_e2e:
@@ -274,6 +298,9 @@ def run_ours(args):
                 "class_prim_quartets": {labels[c]: s0["prim_per_class"][c] for c in range(21)
                                         if s0["prim_per_class"][c]},
                 "list_ms": s0["list_ms"]}
+        if mixed is not None:
+            line["dtype"] = "f32+f64"
+            line["precision_split"] = mixed
         if not args.no_cpu:
             cb, _ = cpu_baseline(bas, d, budget_s=args.cpu_budget)
             line["cpu_baseline"] = cb
@@ -292,6 +319,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="water32_ccpvdz", choices=sorted(WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer seam timing (profiling runs)")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--mixed-threshold", type=float, default=1e-6)
     args = ap.parse_args()
     WORKLOAD.clear()
     WORKLOAD.update(WORKLOADS[args.workload])

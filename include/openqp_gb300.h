@@ -60,6 +60,10 @@ void routec_fock_jk(const double* d, double* f, const int* nbf, const int* nfock
 void routec_fock_jk_inc(const double* dd, double* f, double* f_old, const int* nbf, const int* nfocks,
                         const double* se, const double* sc, int* info);
 
+/* Precision split of the following builds on the process-global context
+ * (see oqpg_set_precision).  No counterpart in the reference seam. */
+int routec_fock_set_precision(int mode, double threshold);
+
 /* Release the process-global context. */
 void routec_fock_finalize(void);
 
@@ -104,13 +108,34 @@ int oqpg_fock_jk_noalloc(oqpg_ctx* ctx, const double* d_device, double* f_device
 /* Schwarz bounds sqrt(max |(ab|ab)|) per shell pair, nshell x nshell (host). */
 int oqpg_schwarz(const oqpg_ctx* ctx, double* q);
 
-/* Statistics of the last build, up to n (<= 71) doubles:
+/* Precision split of the following builds.  mode 0: every quartet in FP64
+ * (the plain path, default).  mode 1: quartets whose screening value (Schwarz
+ * bound x shell density, as in OpenQP's quartet screen) is below threshold are
+ * evaluated in FP32 -- Rys roots and weights still in FP64 -- and their FP32
+ * partial J/K blocks are added into the FP64 accumulators.  mode 2: as mode 1
+ * with the FP32 quartets' roots and weights in FP32 as well.  No counterpart
+ * in the reference. */
+int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold);
+
+/* Statistics of the last build, up to n (<= 73) doubles:
  * [0] quartets computed, [1] primitive quartets, [2] list build ms,
  * [3] integral kernels ms, [4] total device ms, [5] nbf, [6] shell pairs,
  * [7 .. 28) quartets per class (la lb|lc ld) in the order of oqpg_class_l,
  * [28 .. 49) primitive quartets per class, [49 .. 70) kernel ms per class,
- * [70] kernels launched by the build. */
+ * [70] kernels launched by the build, [71] FP32 quartets, [72] FP32
+ * primitive quartets. */
 int oqpg_stats(const oqpg_ctx* ctx, double* out, int n);
+
+/* One-electron integrals on the host for the SCF around the Fock build
+ * (nbf x nbf, row-major, same AO order and normalisation as the Fock build):
+ * which = 0 overlap S, 1 kinetic energy T, 2 nuclear attraction V of the
+ * point charges charges[natom] at xyz.  Basis arguments as routec_fock_init.
+ * Runs on host threads; needs no GPU.  OpenQP computes these in its own
+ * one-electron module (omp_hst, source/integrals/int1.F90:147-268); this is no seam
+ * replacement, only the set-up the SCF loop around the seam needs. */
+int oqpg_one_electron(int nshell, const int* am, const int* ncontr, const int* origin, const double* ex,
+                      const double* cc, const int* harmonic, int natom, const double* xyz, const double* charges,
+                      int which, double* out);
 
 /* Angular momenta (la, lb, lc, ld) of class c (0 <= c < 21). */
 int oqpg_class_l(int c, int* l4);

@@ -36,6 +36,7 @@ import numpy as np
 DPS = 60
 NMAX = 5
 NCOEF = 8             # degree-7 interpolants
+NCOEF_F32 = 5         # degree-4 interpolants for the FP32 quartets
 X_SPLIT = 32          # quarter-unit intervals below, unit intervals above
 H_LO = 0.25
 W_HI = 1
@@ -122,9 +123,9 @@ def interval_of(X):
 
 
 def fit_interval(args):
-    n, a, h = args
+    n, a, h, ncoef = args
     mp.mp.dps = DPS
-    D = NCOEF - 1
+    D = ncoef - 1
     k = np.arange(D + 1)
     nodes = np.cos(np.pi * (k + 0.5) / (D + 1))
     vals = [rys_exact(mp.mpf(a) + mp.mpf(h) * (mp.mpf(float(s)) + 1) / 2, n) for s in nodes]
@@ -135,6 +136,19 @@ def fit_interval(args):
             c = np.polynomial.chebyshev.chebfit(nodes, f, D)
             rows.append(np.polynomial.chebyshev.cheb2poly(c))
     return rows
+
+
+def emit_table(lines, name, tables, ncoef):
+    vals = []
+    for n in range(1, NMAX + 1):
+        for rows in tables[n]:
+            for c in rows:
+                vals.extend(repr(float(v)) for v in c)
+    lines.append("#define %s_SIZE %d" % (name, len(vals)))
+    lines.append("RYS_STORAGE double %s[%s_SIZE] = {" % (name, name))
+    for i in range(0, len(vals), 4):
+        lines.append("  " + ", ".join(vals[i:i + 4]) + ",")
+    lines.append("};")
 
 
 def horner(c, s):
@@ -148,14 +162,16 @@ def main():
     here = os.path.dirname(os.path.abspath(__file__))
     golden_path = sys.argv[1] if len(sys.argv) > 1 else None
     jobs = []
-    for n in range(1, NMAX + 1):
-        for (a, h) in intervals(n):
-            jobs.append((n, a, h))
+    for ncoef in (NCOEF, NCOEF_F32):
+        for n in range(1, NMAX + 1):
+            for (a, h) in intervals(n):
+                jobs.append((n, a, h, ncoef))
     with mpr.get_context("spawn").Pool() as pool:
         fits = pool.map(fit_interval, jobs)
     tables = {n: [] for n in range(1, NMAX + 1)}
-    for (n, a, h), rows in zip(jobs, fits):
-        tables[n].append(rows)
+    tables_f32 = {n: [] for n in range(1, NMAX + 1)}
+    for (n, a, h, ncoef), rows in zip(jobs, fits):
+        (tables if ncoef == NCOEF else tables_f32)[n].append(rows)
     herm = {n: hermite_half(n) for n in range(1, NMAX + 1)}
 
     lines = [
@@ -179,13 +195,18 @@ def main():
     for n in range(1, NMAX + 1):
         offs.append(offs[-1] + len(tables[n]) * 2 * n * NCOEF)
     lines.append("RYS_STORAGE int RYS_OFFSET[%d] = {%s};" % (NMAX + 1, ", ".join(str(o) for o in offs[:-1])))
-    lines.append("#define RYS_TABLE_SIZE %d" % offs[-1])
+    emit_table(lines, "RYS_TABLE", tables, NCOEF)
+    lines.append("// Same intervals, degree-%d interpolants (relative error ~1e-8): the root" % (NCOEF_F32 - 1))
+    lines.append("// evaluation of the FP32 quartets of the precision-split build.")
+    lines.append("#define RYS_NCOEF_F32 %d" % NCOEF_F32)
+    emit_table(lines, "RYS_TABLE_F32", tables_f32, NCOEF_F32)
     vals = []
     for n in range(1, NMAX + 1):
-        for rows in tables[n]:
+        for rows in tables_f32[n]:
             for c in rows:
-                vals.extend(repr(float(v)) for v in c)
-    lines.append("RYS_STORAGE double RYS_TABLE[RYS_TABLE_SIZE] = {")
+                vals.extend("%.9ef" % float(v) for v in c)
+    lines.append("// The same degree-%d table rounded to FP32." % (NCOEF_F32 - 1))
+    lines.append("RYS_STORAGE float RYS_TABLE_F32F[RYS_TABLE_F32_SIZE] = {")
     for i in range(0, len(vals), 4):
         lines.append("  " + ", ".join(vals[i:i + 4]) + ",")
     lines.append("};")

@@ -30,6 +30,7 @@ const ClassInfo& class_info(int c);
 constexpr int MODE_FOCK = 0;     // Fock build
 constexpr int MODE_SCHWARZ = 1;  // Schwarz bounds of diagonal quartets
 constexpr int MODE_PRIM = 2;     // Fock build, one warp per heavily contracted small-class quartet
+constexpr int MODE_F32 = 8;      // flag: FP32 quartets of the precision-split build
 
 // Launch the kernel of class c in the given mode.
 cudaError_t launch_class(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);

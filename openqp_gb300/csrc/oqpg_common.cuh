@@ -28,6 +28,12 @@ struct PrimPair {
   float spf, pf; // FP32 copies of sp and p for the primitive-quartet pre-screen
 };
 
+// FP32 copy of a primitive pair for the small-bound quartets of the
+// precision-split build, 40 bytes: p, 0.5/p, P, P - A, K/p, pad.
+struct PrimPairF {
+  float p, hp, px, py, pz, ax, ay, az, sp, pad;
+};
+
 struct PairDev {
   int sha, shb;    // kernel orientation: am(sha) <= am(shb)
   int poff, pcnt;  // primitive-pair range
@@ -38,6 +44,7 @@ struct BuildArgs {
   const ShellDev* shells;
   const PairDev* pairs;
   const PrimPair* prims;
+  const PrimPairF* primsf; // FP32 copy (precision-split builds)
   const uint2* quartets;   // (bra pair, ket pair) per quartet of this class
   long long nquartets;
   int nbf;
@@ -49,11 +56,14 @@ struct BuildArgs {
   double elem_cut;         // element cutoff on |(ab|cd)|
   const double* dj;        // full nbf x nbf density for Coulomb
   const double* dk;        // nk full densities for exchange
+  const float* djf;        // FP32 copies of dj / dk for the FP32 quartets
+  const float* dkf;
   double* gj;              // nbf x nbf Coulomb accumulator
   double* gk;              // nk x nbf x nbf exchange accumulators
   double* schwarz_out;     // Schwarz mode: per pair sqrt(max |(ab|ab)|)
   unsigned long long* counters;  // [0] primitive quartets evaluated by this launch
   unsigned long long* work;      // work-distribution counter of this launch (zeroed before it)
+  int roots_f32;                 // FP32 quartets: evaluate Rys roots/weights in FP32 too
 };
 
 // ---------------------------------------------------------------------------

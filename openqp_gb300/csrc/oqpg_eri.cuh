@@ -1,12 +1,18 @@
-// Class-specialised FP64 shell-quartet kernels: Rys quadrature ERIs contracted
-// on the fly into Coulomb / exchange accumulators.
+// Class-specialised shell-quartet kernels: Rys quadrature ERIs contracted on
+// the fly into Coulomb / exchange accumulators.
 //
 // One instantiation per (la lb | lc ld) class (la <= lb, lc <= ld, bra pair
 // type <= ket pair type), per AO convention of the d shells (Cartesian or
-// pure), and per mode (Fock build or Schwarz bound).
+// pure), per mode (Fock build or Schwarz bound) and per arithmetic type T:
+// double for the plain path and the large-bound quartets of the precision
+// split, float for its small-bound quartets.  FP32 quartets keep the Rys
+// root/weight evaluation in FP64 (degree-4 tables, ~1e-8 relative) and add
+// their digested blocks into the same FP64 accumulators.
 //
 //   k_small : one thread per quartet, everything in registers (classes with at
 //             most 27 Cartesian elements).
+//   k_prim  : heavily contracted small-class quartets, one warp per quartet,
+//             lanes split the primitive loop.
 //   k_team  : one warp per quartet.  Lanes share the primitive loop: Rys
 //             roots/weights (one quantity per lane), the 2D integrals (one
 //             root x dimension per lane) go to shared memory, each lane
@@ -34,16 +40,16 @@ namespace oqpg {
 
 __host__ __device__ constexpr int rys_xmax(int n) { return 32 + 8 * n; }
 __host__ __device__ constexpr int rys_nint(int n) { return RYS_X_SPLIT * RYS_LO_PER_UNIT + (rys_xmax(n) - RYS_X_SPLIT); }
-__host__ __device__ constexpr int rys_offset(int n) {  // start of the n-root table
-  return n <= 1 ? 0 : rys_offset(n - 1) + rys_nint(n - 1) * 2 * (n - 1) * RYS_NCOEF;
+__host__ __device__ constexpr int rys_offset(int n, int ncoef) {  // start of the n-root table
+  return n <= 1 ? 0 : rys_offset(n - 1, ncoef) + rys_nint(n - 1) * 2 * (n - 1) * ncoef;
 }
 
-// Quantity q of the N-root rule at X: q even -> node x_{q/2}, q odd -> weight w_{q/2}.
-// Interval k: width 1/4 below 32 (s = 8X - (2k+1)), unit width above
-// (s = 2X - (2 floor(X) + 1)).  X >= 0, so the range tests compare bit patterns
-// as integers (no FP64 instruction).
-template <int N>
-__device__ __forceinline__ double rys_quantity(double X, int q) {
+// Quantity q of the N-root rule at X (FP64): q even -> node x_{q/2}, q odd ->
+// weight w_{q/2}.  Interval k: width 1/4 below 32 (s = 8X - (2k+1)), unit
+// width above (s = 2X - (2 floor(X) + 1)).  X >= 0, so the range tests compare
+// bit patterns as integers (no FP64 instruction).
+template <int N, int NCOEF>
+__device__ __forceinline__ double rys_eval(const double* table, double X, int q) {
   const long long xb = __double_as_longlong(X);
   if (xb >= __double_as_longlong((double)rys_xmax(N))) {
     const int r = (N * (N - 1)) / 2 + (q >> 1);
@@ -59,11 +65,47 @@ __device__ __forceinline__ double rys_quantity(double X, int q) {
     k = RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
     s = fma(2.0, X, -(double)(2 * f + 1));
   }
-  const double* c = RYS_TABLE + rys_offset(N) + (k * 2 * N + q) * RYS_NCOEF;
-  double v = __ldg(c + RYS_NCOEF - 1);
+  const double* c = table + rys_offset(N, NCOEF) + (k * 2 * N + q) * NCOEF;
+  double v = __ldg(c + NCOEF - 1);
 #pragma unroll
-  for (int i = RYS_NCOEF - 2; i >= 0; --i) v = fma(v, s, __ldg(c + i));
+  for (int i = NCOEF - 2; i >= 0; --i) v = fma(v, s, __ldg(c + i));
   return v;
+}
+
+// FP32 variant of the same evaluation (the degree-4 table rounded to FP32),
+// for the FP32 quartets when the split is asked to keep no FP64 at all.
+template <int N>
+__device__ __forceinline__ float rys_eval_f32(float X, int q) {
+  if (X >= (float)rys_xmax(N)) {
+    const int r = (N * (N - 1)) / 2 + (q >> 1);
+    return (q & 1) ? (float)RYS_HERM_W[r] * rsqrtf(X) : (float)RYS_HERM_R2[r] / X;
+  }
+  int k;
+  float s;
+  if (X < (float)RYS_X_SPLIT) {
+    k = min(__float2int_rz(X * (float)RYS_LO_PER_UNIT), RYS_X_SPLIT * RYS_LO_PER_UNIT - 1);
+    s = fmaf(2.0f * RYS_LO_PER_UNIT, X, -(float)(2 * k + 1));
+  } else {
+    const int f = min(__float2int_rz(X), rys_xmax(N) - 1);
+    k = RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
+    s = fmaf(2.0f, X, -(float)(2 * f + 1));
+  }
+  const float* c = RYS_TABLE_F32F + rys_offset(N, RYS_NCOEF_F32) + (k * 2 * N + q) * RYS_NCOEF_F32;
+  float v = __ldg(c + RYS_NCOEF_F32 - 1);
+#pragma unroll
+  for (int i = RYS_NCOEF_F32 - 2; i >= 0; --i) v = fmaf(v, s, __ldg(c + i));
+  return v;
+}
+
+// FP64 kernels: the degree-7 FP64 tables.  FP32 kernels: the degree-4 tables,
+// evaluated in FP64 (default) or, with roots_f32, in FP32.
+template <int N, typename T>
+__device__ __forceinline__ T rys_quantity(T X, int q, bool roots_f32 = false) {
+  if constexpr (sizeof(T) == 8) return rys_eval<N, RYS_NCOEF>(RYS_TABLE, X, q);
+  else {
+    if (roots_f32) return rys_eval_f32<N>(X, q);
+    return (float)rys_eval<N, RYS_NCOEF_F32>(RYS_TABLE_F32, (double)X, q);
+  }
 }
 
 __host__ __device__ constexpr int naos(int l, bool pure) { return (pure && l == 2) ? 5 : ncart(l); }
@@ -78,64 +120,119 @@ __host__ __device__ constexpr double pure_d(int m, int c) {
                 : (c == 0 ? 0.86602540378443865 : (c == 1 ? -0.86602540378443865 : 0.0));
 }
 
-// Per-primitive-quartet scalars shared by all roots.
-struct PrimQuartet {
-  double inv, qi, pi, pref, X;
-  double PQ[3];
-};
+// ---------------------------------------------------------------------------
+// Primitive pairs in the arithmetic type of the kernel.
+template <typename T> struct PrimT;
+template <> struct PrimT<double> { using type = PrimPair; };
+template <> struct PrimT<float> { using type = PrimPairF; };
+
+template <typename T> __device__ __forceinline__ const typename PrimT<T>::type* prims_of(const BuildArgs& a);
+template <> __device__ __forceinline__ const PrimPair* prims_of<double>(const BuildArgs& a) { return a.prims; }
+template <> __device__ __forceinline__ const PrimPairF* prims_of<float>(const BuildArgs& a) { return a.primsf; }
+
+template <typename T> __device__ __forceinline__ const T* dj_of(const BuildArgs& a);
+template <> __device__ __forceinline__ const double* dj_of<double>(const BuildArgs& a) { return a.dj; }
+template <> __device__ __forceinline__ const float* dj_of<float>(const BuildArgs& a) { return a.djf; }
+template <typename T> __device__ __forceinline__ const T* dk_of(const BuildArgs& a);
+template <> __device__ __forceinline__ const double* dk_of<double>(const BuildArgs& a) { return a.dk; }
+template <> __device__ __forceinline__ const float* dk_of<float>(const BuildArgs& a) { return a.dkf; }
+
+__device__ __forceinline__ void prim_load(const PrimPair* __restrict__ src, PrimPair& d) {
+  const double2* s = reinterpret_cast<const double2*>(src);
+  double2 v0 = __ldg(s), v1 = __ldg(s + 1), v2 = __ldg(s + 2), v3 = __ldg(s + 3), v4 = __ldg(s + 4);
+  d.p = v0.x; d.hp = v0.y; d.px = v1.x; d.py = v1.y; d.pz = v2.x; d.ax = v2.y; d.ay = v3.x; d.az = v3.y;
+  d.sp = v4.x;
+  const long long bits = __double_as_longlong(v4.y);
+  d.spf = __int_as_float((int)(bits & 0xffffffffll));
+  d.pf = __int_as_float((int)(bits >> 32));
+}
+__device__ __forceinline__ void prim_load(const PrimPairF* __restrict__ src, PrimPairF& d) {
+  const float2* s = reinterpret_cast<const float2*>(src);
+  float2 v0 = __ldg(s), v1 = __ldg(s + 1), v2 = __ldg(s + 2), v3 = __ldg(s + 3), v4 = __ldg(s + 4);
+  d.p = v0.x; d.hp = v0.y; d.px = v1.x; d.py = v1.y; d.pz = v2.x; d.ax = v2.y; d.ay = v3.x; d.az = v3.y;
+  d.sp = v4.x; d.pad = v4.y;
+}
+
+// FP32 screening data (K/p, p) of a primitive pair.
+__device__ __forceinline__ float2 prim_screen(const PrimPair* p) {
+  const long long bits = __double_as_longlong(__ldg(reinterpret_cast<const double*>(p) + 9));
+  return make_float2(__int_as_float((int)(bits & 0xffffffffll)), __int_as_float((int)(bits >> 32)));
+}
+__device__ __forceinline__ float2 prim_screen(const PrimPairF* p) {
+  const float* f = reinterpret_cast<const float*>(p);
+  return make_float2(__ldg(f + 8), __ldg(f));
+}
 
 // Primitive-quartet screen (sp sq)^2 < cut2 (p + q) of the rotated-axis engine
 // (int_rotaxis.F90:629), decided in FP32 unless |sp sq| / sqrt(p + q) falls in
-// the narrow band [lo, hi] around the cutoff, where FP64 decides.
-__device__ __forceinline__ bool prim_keep(const PrimPair& bp, const PrimPair& kp, const BuildArgs& a) {
-  const float r = fabsf(bp.spf * kp.spf) * rsqrtf(bp.pf + kp.pf);
+// the narrow band [lo, hi] around the cutoff, where FP64 decides (FP64 pairs).
+__device__ __forceinline__ bool screen_keep(const PrimPair* bp, float2 bs, const PrimPair* kp, float2 ks,
+                                            const BuildArgs& a) {
+  const float r = fabsf(bs.x * ks.x) * rsqrtf(bs.y + ks.y);
   if (r < a.prim_cut_lo) return false;
   if (r > a.prim_cut_hi) return true;
-  const double fqz = bp.sp * kp.sp;
-  return !(fqz * fqz < a.prim_cut2 * (bp.p + kp.p));
+  const double* b = reinterpret_cast<const double*>(bp);
+  const double* k = reinterpret_cast<const double*>(kp);
+  const double fqz = __ldg(b + 8) * __ldg(k + 8);
+  return !(fqz * fqz < a.prim_cut2 * (__ldg(b) + __ldg(k)));
+}
+__device__ __forceinline__ bool screen_keep(const PrimPairF*, float2 bs, const PrimPairF*, float2 ks,
+                                            const BuildArgs& a) {
+  const float r = fabsf(bs.x * ks.x) * rsqrtf(bs.y + ks.y);
+  return !(r < 0.5f * (a.prim_cut_lo + a.prim_cut_hi));
 }
 
-__device__ __forceinline__ void prim_setup(const PrimPair& bp, const PrimPair& kp, PrimQuartet& o) {
-  const double fqz = bp.sp * kp.sp;
-  const double s = bp.p + kp.p;
-  const double y = rsqrt64(s);
+// Per-primitive-quartet scalars shared by all roots.
+template <typename T>
+struct PrimQuartet {
+  T inv, qi, pi, pref, X;
+  T PQ[3];
+};
+
+__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt64(x); }
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+
+template <typename T, typename PP>
+__device__ __forceinline__ void prim_setup(const PP& bp, const PP& kp, PrimQuartet<T>& o) {
+  const T fqz = bp.sp * kp.sp;
+  const T s = bp.p + kp.p;
+  const T y = rsqrt_t(s);
   o.inv = y * y;
   o.qi = kp.p * o.inv;
   o.pi = bp.p * o.inv;
   o.PQ[0] = bp.px - kp.px;
   o.PQ[1] = bp.py - kp.py;
   o.PQ[2] = bp.pz - kp.pz;
-  const double r2 = fma(o.PQ[0], o.PQ[0], fma(o.PQ[1], o.PQ[1], o.PQ[2] * o.PQ[2]));
+  const T r2 = fma(o.PQ[0], o.PQ[0], fma(o.PQ[1], o.PQ[1], o.PQ[2] * o.PQ[2]));
   o.X = bp.p * o.qi * r2;
   o.pref = fqz * y;
 }
 
 // 2D integrals of one root and one Cartesian dimension:
 // out[((i*(LB+1)+j)*(LC+1)+k)*(LD+1)+l], i<=LA, j<=LB, k<=LC, l<=LD.
-template <int LA, int LB, int LC, int LD, typename Out>
-__device__ __forceinline__ void twod(double g00, double c00, double d00, double b00, double b10, double b01,
-                                     double ab, double cd, Out&& out) {
+template <int LA, int LB, int LC, int LD, typename T, typename Out>
+__device__ __forceinline__ void twod(T g00, T c00, T d00, T b00, T b10, T b01, T ab, T cd, Out&& out) {
   constexpr int NMAX = LA + LB, MMAX = LC + LD;
-  double G[NMAX + 1][MMAX + 1];
+  T G[NMAX + 1][MMAX + 1];
   G[0][0] = g00;
   if (NMAX > 0) G[1][0] = c00 * g00;
 #pragma unroll
-  for (int n = 1; n < NMAX; ++n) G[n + 1][0] = fma(c00, G[n][0], (double)n * b10 * G[n - 1][0]);
+  for (int n = 1; n < NMAX; ++n) G[n + 1][0] = fma(c00, G[n][0], (T)n * b10 * G[n - 1][0]);
 #pragma unroll
   for (int m = 0; m < MMAX; ++m) {
 #pragma unroll
     for (int n = 0; n <= NMAX; ++n) {
-      double v = d00 * G[n][m];
-      if (m > 0) v = fma((double)m * b01, G[n][m - 1], v);
-      if (n > 0) v = fma((double)n * b00, G[n - 1][m], v);
+      T v = d00 * G[n][m];
+      if (m > 0) v = fma((T)m * b01, G[n][m - 1], v);
+      if (n > 0) v = fma((T)n * b00, G[n - 1][m], v);
       G[n][m + 1] = v;
     }
   }
   // bra transfer: H[i][j][m]
-  double H[LA + 1][LB + 1][MMAX + 1];
+  T H[LA + 1][LB + 1][MMAX + 1];
 #pragma unroll
   for (int m = 0; m <= MMAX; ++m) {
-    double col[NMAX + 1];
+    T col[NMAX + 1];
 #pragma unroll
     for (int i = 0; i <= NMAX; ++i) col[i] = G[i][m];
 #pragma unroll
@@ -153,7 +250,7 @@ __device__ __forceinline__ void twod(double g00, double c00, double d00, double 
   for (int i = 0; i <= LA; ++i)
 #pragma unroll
     for (int j = 0; j <= LB; ++j) {
-      double col[MMAX + 1];
+      T col[MMAX + 1];
 #pragma unroll
       for (int k = 0; k <= MMAX; ++k) col[k] = H[i][j][k];
 #pragma unroll
@@ -185,22 +282,9 @@ struct Cls {
   }
 };
 
-__device__ __forceinline__ void prim_load(const PrimPair* __restrict__ src, PrimPair& d) {
-  const double2* s = reinterpret_cast<const double2*>(src);
-  double2 v0 = __ldg(s), v1 = __ldg(s + 1), v2 = __ldg(s + 2), v3 = __ldg(s + 3), v4 = __ldg(s + 4);
-  d.p = v0.x; d.hp = v0.y; d.px = v1.x; d.py = v1.y; d.pz = v2.x; d.ax = v2.y; d.ay = v3.x; d.az = v3.y;
-  d.sp = v4.x;
-  const long long bits = __double_as_longlong(v4.y);
-  d.spf = __int_as_float((int)(bits & 0xffffffffll));
-  d.pf = __int_as_float((int)(bits >> 32));
-}
+template <typename T>
+__device__ __forceinline__ T pick3(int d, T a, T b, T c) { return d == 0 ? a : (d == 1 ? b : c); }
 
-__device__ __forceinline__ double pick3(int d, double a, double b, double c) { return d == 0 ? a : (d == 1 ? b : c); }
-
-// ---------------------------------------------------------------------------
-// Epilogue shared by both paths once the contracted Cartesian block is known:
-// normalisation, optional pure-d projection, element cutoff, and either the
-// Schwarz maximum or the J/K digestion with degeneracy factor f.
 template <int LA, int LB, int LC, int LD, bool PURE>
 struct Epi {
   static constexpr int A = naos(LA, PURE), B = naos(LB, PURE), C = naos(LC, PURE), D = naos(LD, PURE);
@@ -208,8 +292,8 @@ struct Epi {
 };
 
 // In-register pure projection of one index (compile-time dims).
-template <int D0, int D1, int D2, int D3, int POS, bool DO>
-__device__ __forceinline__ void project_regs(const double* in, double* out) {
+template <int D0, int D1, int D2, int D3, int POS, bool DO, typename T>
+__device__ __forceinline__ void project_regs(const T* in, T* out) {
   constexpr int DIMS[4] = {D0, D1, D2, D3};
   constexpr int PRE = POS == 0 ? 1 : (POS == 1 ? D0 : (POS == 2 ? D0 * D1 : D0 * D1 * D2));
   constexpr int N = DIMS[POS];
@@ -225,31 +309,16 @@ __device__ __forceinline__ void project_regs(const double* in, double* out) {
     for (int m = 0; m < 5; ++m)
 #pragma unroll
       for (int p = 0; p < POST; ++p) {
-        double v = 0.0;
+        T v = 0;
 #pragma unroll
         for (int c = 0; c < 6; ++c)
-          if (pure_d(m, c) != 0.0) v = fma(pure_d(m, c), in[(a * N + c) * POST + p], v);
+          if (pure_d(m, c) != 0.0) v = fma((T)pure_d(m, c), in[(a * N + c) * POST + p], v);
         out[(a * 5 + m) * POST + p] = v;
       }
 }
 
-__device__ __forceinline__ double cut_elem(double v, double cut) { return fabs(v) < cut ? 0.0 : v; }
-
-// FP32 screening data (spf, pf) of a primitive pair: the last 8 bytes.
-__device__ __forceinline__ float2 prim_screen(const PrimPair* p) {
-  const long long bits = __double_as_longlong(__ldg(reinterpret_cast<const double*>(p) + 9));
-  return make_float2(__int_as_float((int)(bits & 0xffffffffll)), __int_as_float((int)(bits >> 32)));
-}
-__device__ __forceinline__ bool screen_keep(const PrimPair* bp, float2 bs, const PrimPair* kp, float2 ks,
-                                            const BuildArgs& a) {
-  const float r = fabsf(bs.x * ks.x) * rsqrtf(bs.y + ks.y);
-  if (r < a.prim_cut_lo) return false;
-  if (r > a.prim_cut_hi) return true;
-  const double* b = reinterpret_cast<const double*>(bp);
-  const double* k = reinterpret_cast<const double*>(kp);
-  const double fqz = __ldg(b + 8) * __ldg(k + 8);
-  return !(fqz * fqz < a.prim_cut2 * (__ldg(b) + __ldg(k)));
-}
+template <typename T>
+__device__ __forceinline__ T cut_elem(T v, T cut) { return fabs(v) < cut ? (T)0 : v; }
 
 // Persistent-warp work distribution: warps take chunks of the (sorted) class
 // list from a global counter, heaviest quartets first.
@@ -259,21 +328,31 @@ __device__ __forceinline__ long long grab(unsigned long long* counter, unsigned 
   return (long long)__shfl_sync(0xffffffffu, base, 0);
 }
 
+template <typename T>
+__device__ __forceinline__ void quartet_geometry(const BuildArgs& a, uint2 qd, PairDev& P, PairDev& Q, T AB[3],
+                                                 T CD[3]) {
+  P = a.pairs[qd.x];
+  Q = a.pairs[qd.y];
+  const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
+  AB[0] = (T)(SA.x - SB.x); AB[1] = (T)(SA.y - SB.y); AB[2] = (T)(SA.z - SB.z);
+  CD[0] = (T)(SC.x - SD.x); CD[1] = (T)(SC.y - SD.y); CD[2] = (T)(SC.z - SD.z);
+}
+
 // ===========================================================================
 // Small classes (at most 27 Cartesian elements): everything in registers.
 //
 // small_prims accumulates the primitive quartets c = first, first + step, ...
-// (c = kq * nP + kb) of one contracted quartet.  Each iteration of the FP64
-// body computes one surviving candidate of this lane: the cheap FP32 scan
-// skips screened candidates without holding the warp in the FP64 body.
-template <int LA, int LB, int LC, int LD>
-__device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P, const PairDev& Q,
-                                            const double AB[3], const double CD[3], int first, int step,
-                                            double* acc, unsigned long long& nprim) {
+// (c = kq * nP + kb) of one contracted quartet.  Each iteration of the
+// arithmetic body computes one surviving candidate of this lane: the cheap
+// FP32 scan skips screened candidates without holding the warp in the body.
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P, const PairDev& Q, const T AB[3],
+                                            const T CD[3], int first, int step, T* acc, unsigned long long& nprim) {
   using K = Cls<LA, LB, LC, LD>;
+  using PP = typename PrimT<T>::type;
   constexpr int NE = K::NE, NR = K::NR, N2D = K::N2D;
-  const PrimPair* bpp = a.prims + P.poff;
-  const PrimPair* kpp = a.prims + Q.poff;
+  const PP* bpp = prims_of<T>(a) + P.poff;
+  const PP* kpp = prims_of<T>(a) + Q.poff;
   const int nP = P.pcnt, nQ = Q.pcnt;
   if (nP == 0 || nQ == 0) return;
   int kq = first / nP, kb = first - kq * nP;
@@ -289,179 +368,167 @@ __device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P
       if (screen_keep(bpp + b, prim_screen(bpp + b), kpp + q, ks, a)) { cb = b; cq = q; break; }
     }
     if (cb < 0) break;
-    {
-      PrimPair bp, kp;
-      prim_load(bpp + cb, bp);
-      prim_load(kpp + cq, kp);
-      PrimQuartet pq;
-      prim_setup(bp, kp, pq);
-      ++nprim;
+    PP bp, kp;
+    prim_load(bpp + cb, bp);
+    prim_load(kpp + cq, kp);
+    PrimQuartet<T> pq;
+    prim_setup<T>(bp, kp, pq);
+    ++nprim;
 #pragma unroll
-        for (int r = 0; r < NR; ++r) {
-          const double u = rys_quantity<NR>(pq.X, 2 * r);
-          const double w = rys_quantity<NR>(pq.X, 2 * r + 1) * pq.pref;
-          const double uq = u * pq.qi, up = u * pq.pi;
-          const double b00 = 0.5 * pq.inv * u;
-          const double b10 = fma(-bp.hp, uq, bp.hp);
-          const double b01 = fma(-kp.hp, up, kp.hp);
-          double I[3][N2D];
-          const double PA[3] = {bp.ax, bp.ay, bp.az}, QC[3] = {kp.ax, kp.ay, kp.az};
+    for (int r = 0; r < NR; ++r) {
+      const T u = rys_quantity<NR, T>(pq.X, 2 * r, a.roots_f32 != 0);
+      const T w = rys_quantity<NR, T>(pq.X, 2 * r + 1, a.roots_f32 != 0) * pq.pref;
+      const T uq = u * pq.qi, up = u * pq.pi;
+      const T b00 = (T)0.5 * pq.inv * u;
+      const T b10 = fma(-bp.hp, uq, bp.hp);
+      const T b01 = fma(-kp.hp, up, kp.hp);
+      T I[3][N2D];
+      const T PA[3] = {bp.ax, bp.ay, bp.az}, QC[3] = {kp.ax, kp.ay, kp.az};
 #pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            const double c00 = fma(-uq, pq.PQ[d], PA[d]);
-            const double d00 = fma(up, pq.PQ[d], QC[d]);
-            twod<LA, LB, LC, LD>(d == 2 ? w : 1.0, c00, d00, b00, b10, b01, AB[d], CD[d],
-                                 [&](int i, double v) { I[d][i] = v; });
-          }
-#pragma unroll
-          for (int e = 0; e < NE; ++e)
-            acc[e] = fma(I[0][K::off2d(e, 0)] * I[1][K::off2d(e, 1)], I[2][K::off2d(e, 2)], acc[e]);
-        }
-      }
-    }
-}
-
-// Normalisation, pure projection, element cutoff and digestion of one
-// contracted small-class quartet (single lane).
-template <int LA, int LB, int LC, int LD, bool PURE, bool SCH>
-__device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, const PairDev& P, const PairDev& Q,
-                                               double* acc) {
-  using K = Cls<LA, LB, LC, LD>;
-  using E = Epi<LA, LB, LC, LD, PURE>;
-  constexpr int NE = K::NE;
-  {
-    const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
-#pragma unroll
-    for (int e = 0; e < NE; ++e) acc[e] *= K::norm(e);
-    constexpr int DA = K::NA, DB = K::NB, DC = K::NC, DD = K::ND;
-    double t1[NE], t2[NE];
-    project_regs<DA, DB, DC, DD, 0, PURE && LA == 2>(acc, t1);
-    project_regs<E::A, DB, DC, DD, 1, PURE && LB == 2>(t1, t2);
-    project_regs<E::A, E::B, DC, DD, 2, PURE && LC == 2>(t2, t1);
-    project_regs<E::A, E::B, E::C, DD, 3, PURE && LD == 2>(t1, t2);
-    double* V = t2;
-    if (SCH) {
-      double m = 0.0;
-#pragma unroll
-      for (int e = 0; e < E::NEP; ++e) m = fmax(m, fabs(V[e]));
-      a.schwarz_out[qd.x] = sqrt(m);
-      return;
-    }
-#pragma unroll
-    for (int e = 0; e < E::NEP; ++e) V[e] = cut_elem(V[e], a.elem_cut);
-    double f = 1.0;
-    if (P.sha == P.shb) f *= 0.5;
-    if (Q.sha == Q.shb) f *= 0.5;
-    if (qd.x == qd.y) f *= 0.5;
-    const int n = a.nbf;
-    const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
-    // Coulomb: G_J[ab] += 2f sum_cd V D_cd ; G_J[cd] += 2f sum_ab V D_ab
-    {
-      double dab[E::A * E::B], dcd[E::C * E::D];
-#pragma unroll
-      for (int i = 0; i < E::A; ++i)
-#pragma unroll
-        for (int j = 0; j < E::B; ++j) dab[i * E::B + j] = __ldg(a.dj + (size_t)(oa + i) * n + ob + j);
-#pragma unroll
-      for (int i = 0; i < E::C; ++i)
-#pragma unroll
-        for (int j = 0; j < E::D; ++j) dcd[i * E::D + j] = __ldg(a.dj + (size_t)(oc + i) * n + od + j);
-      double jab[E::A * E::B], jcd[E::C * E::D];
-#pragma unroll
-      for (int i = 0; i < E::A * E::B; ++i) jab[i] = 0.0;
-#pragma unroll
-      for (int i = 0; i < E::C * E::D; ++i) jcd[i] = 0.0;
-#pragma unroll
-      for (int ab = 0; ab < E::A * E::B; ++ab)
-#pragma unroll
-        for (int cd = 0; cd < E::C * E::D; ++cd) {
-          const double v = V[ab * E::C * E::D + cd];
-          jab[ab] = fma(v, dcd[cd], jab[ab]);
-          jcd[cd] = fma(v, dab[ab], jcd[cd]);
-        }
-      const double f2 = 2.0 * f;
-#pragma unroll
-      for (int i = 0; i < E::A; ++i)
-#pragma unroll
-        for (int j = 0; j < E::B; ++j) atomicAdd(a.gj + (size_t)(oa + i) * n + ob + j, f2 * jab[i * E::B + j]);
-#pragma unroll
-      for (int i = 0; i < E::C; ++i)
-#pragma unroll
-        for (int j = 0; j < E::D; ++j) atomicAdd(a.gj + (size_t)(oc + i) * n + od + j, f2 * jcd[i * E::D + j]);
-    }
-    // Exchange: G_K[ac] += f sum V D_bd ; [ad] += f V D_bc ; [bc] += f V D_ad ; [bd] += f V D_ac
-    for (int kk = 0; kk < a.nk; ++kk) {
-      const double* dk = a.dk + (size_t)kk * n * n;
-      double* gk = a.gk + (size_t)kk * n * n;
-      double dac[E::A * E::C], dad[E::A * E::D], dbc[E::B * E::C], dbd[E::B * E::D];
-#pragma unroll
-      for (int i = 0; i < E::A; ++i) {
-#pragma unroll
-        for (int j = 0; j < E::C; ++j) dac[i * E::C + j] = __ldg(dk + (size_t)(oa + i) * n + oc + j);
-#pragma unroll
-        for (int j = 0; j < E::D; ++j) dad[i * E::D + j] = __ldg(dk + (size_t)(oa + i) * n + od + j);
+      for (int d = 0; d < 3; ++d) {
+        const T c00 = fma(-uq, pq.PQ[d], PA[d]);
+        const T d00 = fma(up, pq.PQ[d], QC[d]);
+        twod<LA, LB, LC, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01, AB[d], CD[d],
+                                [&](int i, T v) { I[d][i] = v; });
       }
 #pragma unroll
-      for (int i = 0; i < E::B; ++i) {
-#pragma unroll
-        for (int j = 0; j < E::C; ++j) dbc[i * E::C + j] = __ldg(dk + (size_t)(ob + i) * n + oc + j);
-#pragma unroll
-        for (int j = 0; j < E::D; ++j) dbd[i * E::D + j] = __ldg(dk + (size_t)(ob + i) * n + od + j);
-      }
-      double kac[E::A * E::C], kad[E::A * E::D], kbc[E::B * E::C], kbd[E::B * E::D];
-#pragma unroll
-      for (int i = 0; i < E::A * E::C; ++i) kac[i] = 0.0;
-#pragma unroll
-      for (int i = 0; i < E::A * E::D; ++i) kad[i] = 0.0;
-#pragma unroll
-      for (int i = 0; i < E::B * E::C; ++i) kbc[i] = 0.0;
-#pragma unroll
-      for (int i = 0; i < E::B * E::D; ++i) kbd[i] = 0.0;
-#pragma unroll
-      for (int i = 0; i < E::A; ++i)
-#pragma unroll
-        for (int j = 0; j < E::B; ++j)
-#pragma unroll
-          for (int k = 0; k < E::C; ++k)
-#pragma unroll
-            for (int l = 0; l < E::D; ++l) {
-              const double v = V[((i * E::B + j) * E::C + k) * E::D + l];
-              kac[i * E::C + k] = fma(v, dbd[j * E::D + l], kac[i * E::C + k]);
-              kad[i * E::D + l] = fma(v, dbc[j * E::C + k], kad[i * E::D + l]);
-              kbc[j * E::C + k] = fma(v, dad[i * E::D + l], kbc[j * E::C + k]);
-              kbd[j * E::D + l] = fma(v, dac[i * E::C + k], kbd[j * E::D + l]);
-            }
-#pragma unroll
-      for (int i = 0; i < E::A; ++i) {
-#pragma unroll
-        for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(oa + i) * n + oc + j, f * kac[i * E::C + j]);
-#pragma unroll
-        for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(oa + i) * n + od + j, f * kad[i * E::D + j]);
-      }
-#pragma unroll
-      for (int i = 0; i < E::B; ++i) {
-#pragma unroll
-        for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(ob + i) * n + oc + j, f * kbc[i * E::C + j]);
-#pragma unroll
-        for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(ob + i) * n + od + j, f * kbd[i * E::D + j]);
-      }
+      for (int e = 0; e < NE; ++e)
+        acc[e] = fma(I[0][K::off2d(e, 0)] * I[1][K::off2d(e, 1)], I[2][K::off2d(e, 2)], acc[e]);
     }
   }
 }
 
-template <int LA, int LB, int LC, int LD>
-__device__ __forceinline__ void quartet_geometry(const BuildArgs& a, uint2 qd, PairDev& P, PairDev& Q, double AB[3],
-                                                 double CD[3]) {
-  P = a.pairs[qd.x];
-  Q = a.pairs[qd.y];
+// Normalisation, pure projection, element cutoff and digestion of one
+// contracted small-class quartet (single lane).
+template <int LA, int LB, int LC, int LD, bool PURE, bool SCH, typename T>
+__device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, const PairDev& P, const PairDev& Q,
+                                               T* acc) {
+  using K = Cls<LA, LB, LC, LD>;
+  using E = Epi<LA, LB, LC, LD, PURE>;
+  constexpr int NE = K::NE;
   const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
-  AB[0] = SA.x - SB.x; AB[1] = SA.y - SB.y; AB[2] = SA.z - SB.z;
-  CD[0] = SC.x - SD.x; CD[1] = SC.y - SD.y; CD[2] = SC.z - SD.z;
+#pragma unroll
+  for (int e = 0; e < NE; ++e) acc[e] *= (T)K::norm(e);
+  constexpr int DA = K::NA, DB = K::NB, DC = K::NC, DD = K::ND;
+  T t1[NE], t2[NE];
+  project_regs<DA, DB, DC, DD, 0, PURE && LA == 2>(acc, t1);
+  project_regs<E::A, DB, DC, DD, 1, PURE && LB == 2>(t1, t2);
+  project_regs<E::A, E::B, DC, DD, 2, PURE && LC == 2>(t2, t1);
+  project_regs<E::A, E::B, E::C, DD, 3, PURE && LD == 2>(t1, t2);
+  T* V = t2;
+  if (SCH) {
+    T m = 0;
+#pragma unroll
+    for (int e = 0; e < E::NEP; ++e) m = fmax(m, fabs(V[e]));
+    a.schwarz_out[qd.x] = sqrt((double)m);
+    return;
+  }
+  const T cut = (T)a.elem_cut;
+#pragma unroll
+  for (int e = 0; e < E::NEP; ++e) V[e] = cut_elem(V[e], cut);
+  double f = 1.0;
+  if (P.sha == P.shb) f *= 0.5;
+  if (Q.sha == Q.shb) f *= 0.5;
+  if (qd.x == qd.y) f *= 0.5;
+  const int n = a.nbf;
+  const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
+  const T* djt = dj_of<T>(a);
+  // Coulomb: G_J[ab] += 2f sum_cd V D_cd ; G_J[cd] += 2f sum_ab V D_ab
+  {
+    T dab[E::A * E::B], dcd[E::C * E::D];
+#pragma unroll
+    for (int i = 0; i < E::A; ++i)
+#pragma unroll
+      for (int j = 0; j < E::B; ++j) dab[i * E::B + j] = __ldg(djt + (size_t)(oa + i) * n + ob + j);
+#pragma unroll
+    for (int i = 0; i < E::C; ++i)
+#pragma unroll
+      for (int j = 0; j < E::D; ++j) dcd[i * E::D + j] = __ldg(djt + (size_t)(oc + i) * n + od + j);
+    T jab[E::A * E::B], jcd[E::C * E::D];
+#pragma unroll
+    for (int i = 0; i < E::A * E::B; ++i) jab[i] = 0;
+#pragma unroll
+    for (int i = 0; i < E::C * E::D; ++i) jcd[i] = 0;
+#pragma unroll
+    for (int ab = 0; ab < E::A * E::B; ++ab)
+#pragma unroll
+      for (int cd = 0; cd < E::C * E::D; ++cd) {
+        const T v = V[ab * E::C * E::D + cd];
+        jab[ab] = fma(v, dcd[cd], jab[ab]);
+        jcd[cd] = fma(v, dab[ab], jcd[cd]);
+      }
+    const double f2 = 2.0 * f;
+#pragma unroll
+    for (int i = 0; i < E::A; ++i)
+#pragma unroll
+      for (int j = 0; j < E::B; ++j) atomicAdd(a.gj + (size_t)(oa + i) * n + ob + j, f2 * (double)jab[i * E::B + j]);
+#pragma unroll
+    for (int i = 0; i < E::C; ++i)
+#pragma unroll
+      for (int j = 0; j < E::D; ++j) atomicAdd(a.gj + (size_t)(oc + i) * n + od + j, f2 * (double)jcd[i * E::D + j]);
+  }
+  // Exchange: G_K[ac] += f sum V D_bd ; [ad] += f V D_bc ; [bc] += f V D_ad ; [bd] += f V D_ac
+  for (int kk = 0; kk < a.nk; ++kk) {
+    const T* dk = dk_of<T>(a) + (size_t)kk * n * n;
+    double* gk = a.gk + (size_t)kk * n * n;
+    T dac[E::A * E::C], dad[E::A * E::D], dbc[E::B * E::C], dbd[E::B * E::D];
+#pragma unroll
+    for (int i = 0; i < E::A; ++i) {
+#pragma unroll
+      for (int j = 0; j < E::C; ++j) dac[i * E::C + j] = __ldg(dk + (size_t)(oa + i) * n + oc + j);
+#pragma unroll
+      for (int j = 0; j < E::D; ++j) dad[i * E::D + j] = __ldg(dk + (size_t)(oa + i) * n + od + j);
+    }
+#pragma unroll
+    for (int i = 0; i < E::B; ++i) {
+#pragma unroll
+      for (int j = 0; j < E::C; ++j) dbc[i * E::C + j] = __ldg(dk + (size_t)(ob + i) * n + oc + j);
+#pragma unroll
+      for (int j = 0; j < E::D; ++j) dbd[i * E::D + j] = __ldg(dk + (size_t)(ob + i) * n + od + j);
+    }
+    T kac[E::A * E::C], kad[E::A * E::D], kbc[E::B * E::C], kbd[E::B * E::D];
+#pragma unroll
+    for (int i = 0; i < E::A * E::C; ++i) kac[i] = 0;
+#pragma unroll
+    for (int i = 0; i < E::A * E::D; ++i) kad[i] = 0;
+#pragma unroll
+    for (int i = 0; i < E::B * E::C; ++i) kbc[i] = 0;
+#pragma unroll
+    for (int i = 0; i < E::B * E::D; ++i) kbd[i] = 0;
+#pragma unroll
+    for (int i = 0; i < E::A; ++i)
+#pragma unroll
+      for (int j = 0; j < E::B; ++j)
+#pragma unroll
+        for (int k = 0; k < E::C; ++k)
+#pragma unroll
+          for (int l = 0; l < E::D; ++l) {
+            const T v = V[((i * E::B + j) * E::C + k) * E::D + l];
+            kac[i * E::C + k] = fma(v, dbd[j * E::D + l], kac[i * E::C + k]);
+            kad[i * E::D + l] = fma(v, dbc[j * E::C + k], kad[i * E::D + l]);
+            kbc[j * E::C + k] = fma(v, dad[i * E::D + l], kbc[j * E::C + k]);
+            kbd[j * E::D + l] = fma(v, dac[i * E::C + k], kbd[j * E::D + l]);
+          }
+#pragma unroll
+    for (int i = 0; i < E::A; ++i) {
+#pragma unroll
+      for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(oa + i) * n + oc + j, f * (double)kac[i * E::C + j]);
+#pragma unroll
+      for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(oa + i) * n + od + j, f * (double)kad[i * E::D + j]);
+    }
+#pragma unroll
+    for (int i = 0; i < E::B; ++i) {
+#pragma unroll
+      for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(ob + i) * n + oc + j, f * (double)kbc[i * E::C + j]);
+#pragma unroll
+      for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(ob + i) * n + od + j, f * (double)kbd[i * E::D + j]);
+    }
+  }
 }
 
 // One thread per quartet; warps take chunks of 32 consecutive quartets of the
 // sorted list (similar primitive counts on all lanes).
-template <int LA, int LB, int LC, int LD, bool PURE, bool SCH>
+template <int LA, int LB, int LC, int LD, bool PURE, bool SCH, typename T>
 __global__ void __launch_bounds__(128) k_small(const BuildArgs a) {
   constexpr int NE = Cls<LA, LB, LC, LD>::NE;
   const int lane = threadIdx.x & 31;
@@ -473,13 +540,13 @@ __global__ void __launch_bounds__(128) k_small(const BuildArgs a) {
     if (t < a.nquartets) {
       const uint2 qd = a.quartets[t];
       PairDev P, Q;
-      double AB[3], CD[3];
-      quartet_geometry<LA, LB, LC, LD>(a, qd, P, Q, AB, CD);
-      double acc[NE];
+      T AB[3], CD[3];
+      quartet_geometry<T>(a, qd, P, Q, AB, CD);
+      T acc[NE];
 #pragma unroll
-      for (int e = 0; e < NE; ++e) acc[e] = 0.0;
-      small_prims<LA, LB, LC, LD>(a, P, Q, AB, CD, 0, 1, acc, nprim);
-      small_epilogue<LA, LB, LC, LD, PURE, SCH>(a, qd, P, Q, acc);
+      for (int e = 0; e < NE; ++e) acc[e] = 0;
+      small_prims<LA, LB, LC, LD, T>(a, P, Q, AB, CD, 0, 1, acc, nprim);
+      small_epilogue<LA, LB, LC, LD, PURE, SCH, T>(a, qd, P, Q, acc);
     }
   }
   if (a.counters && nprim) atomicAdd(a.counters, nprim);
@@ -487,7 +554,7 @@ __global__ void __launch_bounds__(128) k_small(const BuildArgs a) {
 
 // Heavily contracted small-class quartets: one warp per quartet, the lanes
 // split its primitive quartets, the partial blocks are summed across the warp.
-template <int LA, int LB, int LC, int LD, bool PURE>
+template <int LA, int LB, int LC, int LD, bool PURE, typename T>
 __global__ void __launch_bounds__(128) k_prim(const BuildArgs a) {
   constexpr int NE = Cls<LA, LB, LC, LD>::NE;
   const int lane = threadIdx.x & 31;
@@ -497,20 +564,20 @@ __global__ void __launch_bounds__(128) k_prim(const BuildArgs a) {
     if (t >= a.nquartets) break;
     const uint2 qd = a.quartets[t];
     PairDev P, Q;
-    double AB[3], CD[3];
-    quartet_geometry<LA, LB, LC, LD>(a, qd, P, Q, AB, CD);
-    double acc[NE];
+    T AB[3], CD[3];
+    quartet_geometry<T>(a, qd, P, Q, AB, CD);
+    T acc[NE];
 #pragma unroll
-    for (int e = 0; e < NE; ++e) acc[e] = 0.0;
-    small_prims<LA, LB, LC, LD>(a, P, Q, AB, CD, lane, 32, acc, nprim);
+    for (int e = 0; e < NE; ++e) acc[e] = 0;
+    small_prims<LA, LB, LC, LD, T>(a, P, Q, AB, CD, lane, 32, acc, nprim);
 #pragma unroll
     for (int e = 0; e < NE; ++e) {
-      double v = acc[e];
+      T v = acc[e];
 #pragma unroll
       for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
       acc[e] = v;
     }
-    if (lane == 0) small_epilogue<LA, LB, LC, LD, PURE, false>(a, qd, P, Q, acc);
+    if (lane == 0) small_epilogue<LA, LB, LC, LD, PURE, false, T>(a, qd, P, Q, acc);
     __syncwarp();
   }
   if (a.counters && nprim) atomicAdd(a.counters, nprim);
@@ -526,20 +593,22 @@ struct TeamSmem {
   static constexpr int DJ = E::A * E::B + E::C * E::D;
   static constexpr int DK = E::A * E::C + E::A * E::D + E::B * E::C + E::B * E::D;
   static constexpr int PH2 = 2 * K::NE + DJ + 2 * DK;
-  static constexpr int PER_WARP = cmax(PH1, PH2);
+  static constexpr int PER_WARP = cmax(PH1, PH2);   // elements of the kernel's type
 };
 
-template <int LA, int LB, int LC, int LD, bool PURE, bool SCH>
+template <int LA, int LB, int LC, int LD, bool PURE, bool SCH, typename T>
 __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
   using K = Cls<LA, LB, LC, LD>;
   using E = Epi<LA, LB, LC, LD, PURE>;
   using SM = TeamSmem<LA, LB, LC, LD, PURE>;
+  using PP = typename PrimT<T>::type;
   constexpr int NE = K::NE, NR = K::NR, N2D = K::N2D, KE = (NE + 31) / 32;
-  extern __shared__ double smem[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double* W = smem + warp * SM::PER_WARP;
-  double* RT = W;               // 2*NR: x_r, w_r * pref
-  double* I2 = W + 2 * NR;      // [r][d][N2D]
+  T* W = smem + warp * SM::PER_WARP;
+  T* RT = W;               // 2*NR: x_r, w_r * pref
+  T* I2 = W + 2 * NR;      // [r][d][N2D]
   // packed 2D offsets of this lane's elements (same for every quartet)
   int offs[KE];
 #pragma unroll
@@ -551,13 +620,9 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
                 id = e % K::ND;
       int ox[3];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const int ea = (LA == 0) ? 0 : (LA == 1 ? (ia == d) : (ia < 3 ? 2 * (ia == d) : (ia == 3 ? (d < 2) : ia == 4 ? (d != 1) : (d > 0))));
-        const int eb = (LB == 0) ? 0 : (LB == 1 ? (ib == d) : (ib < 3 ? 2 * (ib == d) : (ib == 3 ? (d < 2) : ib == 4 ? (d != 1) : (d > 0))));
-        const int ec = (LC == 0) ? 0 : (LC == 1 ? (ic == d) : (ic < 3 ? 2 * (ic == d) : (ic == 3 ? (d < 2) : ic == 4 ? (d != 1) : (d > 0))));
-        const int ed = (LD == 0) ? 0 : (LD == 1 ? (id == d) : (id < 3 ? 2 * (id == d) : (id == 3 ? (d < 2) : id == 4 ? (d != 1) : (d > 0))));
-        ox[d] = ((ea * (LB + 1) + eb) * (LC + 1) + ec) * (LD + 1) + ed;
-      }
+      for (int d = 0; d < 3; ++d)
+        ox[d] = ((cart_e(LA, ia, d) * (LB + 1) + cart_e(LB, ib, d)) * (LC + 1) + cart_e(LC, ic, d)) * (LD + 1) +
+                cart_e(LD, id, d);
       o = ox[0] | (ox[1] << 10) | (ox[2] << 20);
     }
     offs[k] = o;
@@ -567,52 +632,55 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
     const long long t = grab(a.work, 1u, lane);
     if (t >= a.nquartets) break;
     const uint2 qd = a.quartets[t];
-    const PairDev P = a.pairs[qd.x], Q = a.pairs[qd.y];
+    PairDev P, Q;
+    T AB[3], CD[3];
+    quartet_geometry<T>(a, qd, P, Q, AB, CD);
     const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
-    const double AB[3] = {SA.x - SB.x, SA.y - SB.y, SA.z - SB.z};
-    const double CD[3] = {SC.x - SD.x, SC.y - SD.y, SC.z - SD.z};
-    double acc[KE];
+    T acc[KE];
 #pragma unroll
-    for (int k = 0; k < KE; ++k) acc[k] = 0.0;
+    for (int k = 0; k < KE; ++k) acc[k] = 0;
+    const PP* bpp = prims_of<T>(a) + P.poff;
+    const PP* kpp = prims_of<T>(a) + Q.poff;
     for (int kq = 0; kq < Q.pcnt; ++kq) {
-      PrimPair kp, bn;
-      prim_load(a.prims + Q.poff + kq, kp);
-      if (P.pcnt > 0) prim_load(a.prims + P.poff, bn);
+      PP kp, bn;
+      prim_load(kpp + kq, kp);
+      const float2 ks = prim_screen(kpp + kq);
+      if (P.pcnt > 0) prim_load(bpp, bn);
       for (int kb = 0; kb < P.pcnt; ++kb) {
-        const PrimPair bp = bn;
-        if (kb + 1 < P.pcnt) prim_load(a.prims + P.poff + kb + 1, bn);  // prefetch
-        if (!prim_keep(bp, kp, a)) continue;
-        PrimQuartet pq;
-        prim_setup(bp, kp, pq);
+        const PP bp = bn;
+        if (kb + 1 < P.pcnt) prim_load(bpp + kb + 1, bn);  // prefetch
+        if (!screen_keep(bpp + kb, prim_screen(bpp + kb), kpp + kq, ks, a)) continue;
+        PrimQuartet<T> pq;
+        prim_setup<T>(bp, kp, pq);
         ++nprim;
         if (lane < 2 * NR) {
-          const double v = rys_quantity<NR>(pq.X, lane);
+          const T v = rys_quantity<NR, T>(pq.X, lane, a.roots_f32 != 0);
           RT[lane] = (lane & 1) ? v * pq.pref : v;
         }
         __syncwarp();
         if (lane < 3 * NR) {
           const int r = lane / 3, d = lane - 3 * r;
-          const double u = RT[2 * r], w = RT[2 * r + 1];
-          const double uq = u * pq.qi, up = u * pq.pi;
-          const double b00 = 0.5 * pq.inv * u;
-          const double b10 = fma(-bp.hp, uq, bp.hp);
-          const double b01 = fma(-kp.hp, up, kp.hp);
-          const double pqd = pick3(d, pq.PQ[0], pq.PQ[1], pq.PQ[2]);
-          const double c00 = fma(-uq, pqd, pick3(d, bp.ax, bp.ay, bp.az));
-          const double d00 = fma(up, pqd, pick3(d, kp.ax, kp.ay, kp.az));
-          double* dst = I2 + (r * 3 + d) * N2D;
-          twod<LA, LB, LC, LD>(d == 2 ? w : 1.0, c00, d00, b00, b10, b01, pick3(d, AB[0], AB[1], AB[2]),
-                               pick3(d, CD[0], CD[1], CD[2]), [&](int i, double v) { dst[i] = v; });
+          const T u = RT[2 * r], w = RT[2 * r + 1];
+          const T uq = u * pq.qi, up = u * pq.pi;
+          const T b00 = (T)0.5 * pq.inv * u;
+          const T b10 = fma(-bp.hp, uq, bp.hp);
+          const T b01 = fma(-kp.hp, up, kp.hp);
+          const T pqd = pick3(d, pq.PQ[0], pq.PQ[1], pq.PQ[2]);
+          const T c00 = fma(-uq, pqd, pick3(d, bp.ax, bp.ay, bp.az));
+          const T d00 = fma(up, pqd, pick3(d, kp.ax, kp.ay, kp.az));
+          T* dst = I2 + (r * 3 + d) * N2D;
+          twod<LA, LB, LC, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01, pick3(d, AB[0], AB[1], AB[2]),
+                                  pick3(d, CD[0], CD[1], CD[2]), [&](int i, T v) { dst[i] = v; });
         }
         __syncwarp();
 #pragma unroll
         for (int k = 0; k < KE; ++k) {
           if (lane + 32 * k < NE) {
             const int ox = offs[k] & 1023, oy = (offs[k] >> 10) & 1023, oz = offs[k] >> 20;
-            double v = acc[k];
+            T v = acc[k];
 #pragma unroll
             for (int r = 0; r < NR; ++r) {
-              const double* g = I2 + r * 3 * N2D;
+              const T* g = I2 + r * 3 * N2D;
               v = fma(g[ox] * g[N2D + oy], g[2 * N2D + oz], v);
             }
             acc[k] = v;
@@ -622,16 +690,17 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
       }
     }
     // ---- epilogue: V = normalised block in smem, pure projection in place
-    double* V = W;
-    double* T = W + NE;
+    T* V = W;
+    T* Tm = W + NE;
 #pragma unroll
     for (int k = 0; k < KE; ++k) {
       const int e = lane + 32 * k;
       if (e < NE) {
         const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
                   id = e % K::ND;
-        const double nrm = (LA == 2 && ia >= 3 ? 1.7320508075688772 : 1.0) * (LB == 2 && ib >= 3 ? 1.7320508075688772 : 1.0) *
-                           (LC == 2 && ic >= 3 ? 1.7320508075688772 : 1.0) * (LD == 2 && id >= 3 ? 1.7320508075688772 : 1.0);
+        const T s3 = (T)1.7320508075688772;
+        const T nrm = (LA == 2 && ia >= 3 ? s3 : (T)1) * (LB == 2 && ib >= 3 ? s3 : (T)1) *
+                      (LC == 2 && ic >= 3 ? s3 : (T)1) * (LD == 2 && id >= 3 ? s3 : (T)1);
         V[e] = (LA == 2 || LB == 2 || LC == 2 || LD == 2) ? acc[k] * nrm : acc[k];
       }
     }
@@ -648,44 +717,46 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
         const int nout = pre * 5 * post;
         for (int o = lane; o < nout; o += 32) {
           const int p = o % post, m = (o / post) % 5, q = o / (5 * post);
-          const double* src = V + (size_t)q * 6 * post + p;
-          double v;
+          const T* src = V + (size_t)q * 6 * post + p;
+          T v;
           if (m == 0) v = src[3 * post];
           else if (m == 1) v = src[5 * post];
-          else if (m == 2) v = src[2 * post] - 0.5 * (src[0] + src[post]);
+          else if (m == 2) v = src[2 * post] - (T)0.5 * (src[0] + src[post]);
           else if (m == 3) v = src[4 * post];
-          else v = 0.86602540378443865 * (src[0] - src[post]);
-          T[o] = v;
+          else v = (T)0.86602540378443865 * (src[0] - src[post]);
+          Tm[o] = v;
         }
         __syncwarp();
-        for (int o = lane; o < nout; o += 32) V[o] = T[o];
+        for (int o = lane; o < nout; o += 32) V[o] = Tm[o];
         __syncwarp();
         dims[pos] = 5;
       }
     }
     constexpr int NEP = E::NEP;
     if (SCH) {
-      double m = 0.0;
+      T m = 0;
       for (int e = lane; e < NEP; e += 32) m = fmax(m, fabs(V[e]));
 #pragma unroll
       for (int s = 16; s > 0; s >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, s));
-      if (lane == 0) a.schwarz_out[qd.x] = sqrt(m);
+      if (lane == 0) a.schwarz_out[qd.x] = sqrt((double)m);
       __syncwarp();
       continue;
     }
-    for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], a.elem_cut);
+    const T cut = (T)a.elem_cut;
+    for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], cut);
     // density blocks
     const int n = a.nbf;
     const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
-    double* Dab = W + NE;                 // after V (NE >= NEP)
-    double* Dcd = Dab + E::A * E::B;
-    double* Dk = Dcd + E::C * E::D;       // per k: ac, ad, bc, bd
+    const T* djt = dj_of<T>(a);
+    T* Dab = W + NE;                 // after V (NE >= NEP)
+    T* Dcd = Dab + E::A * E::B;
+    T* Dk = Dcd + E::C * E::D;       // per k: ac, ad, bc, bd
     constexpr int DKS = SM::DK;
-    for (int i = lane; i < E::A * E::B; i += 32) Dab[i] = __ldg(a.dj + (size_t)(oa + i / E::B) * n + ob + i % E::B);
-    for (int i = lane; i < E::C * E::D; i += 32) Dcd[i] = __ldg(a.dj + (size_t)(oc + i / E::D) * n + od + i % E::D);
+    for (int i = lane; i < E::A * E::B; i += 32) Dab[i] = __ldg(djt + (size_t)(oa + i / E::B) * n + ob + i % E::B);
+    for (int i = lane; i < E::C * E::D; i += 32) Dcd[i] = __ldg(djt + (size_t)(oc + i / E::D) * n + od + i % E::D);
     for (int kk = 0; kk < a.nk; ++kk) {
-      const double* dk = a.dk + (size_t)kk * n * n;
-      double* base = Dk + kk * DKS;
+      const T* dk = dk_of<T>(a) + (size_t)kk * n * n;
+      T* base = Dk + kk * DKS;
       for (int i = lane; i < E::A * E::C; i += 32) base[i] = __ldg(dk + (size_t)(oa + i / E::C) * n + oc + i % E::C);
       base += E::A * E::C;
       for (int i = lane; i < E::A * E::D; i += 32) base[i] = __ldg(dk + (size_t)(oa + i / E::D) * n + od + i % E::D);
@@ -703,12 +774,12 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
     constexpr int NAC = E::A * E::C, NAD = E::A * E::D, NBC = E::B * E::C, NBD = E::B * E::D;
     const int ntarget = NAB + NCD + a.nk * (NAC + NAD + NBC + NBD);
     for (int o = lane; o < ntarget; o += 32) {
-      double s = 0.0;
+      T s = 0;
       double* dst;
       double fac;
       if (o < NAB) {
         const int i = o / E::B, j = o % E::B;
-        const double* v = V + (size_t)o * NCD;
+        const T* v = V + (size_t)o * NCD;
 #pragma unroll 4
         for (int cd = 0; cd < NCD; ++cd) s = fma(v[cd], Dcd[cd], s);
         dst = a.gj + (size_t)(oa + i) * n + ob + j;
@@ -723,11 +794,11 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
         int r = o - NAB - NCD;
         const int kk = r / (NAC + NAD + NBC + NBD);
         r -= kk * (NAC + NAD + NBC + NBD);
-        const double* dk = Dk + kk * DKS;
-        const double* dac = dk;
-        const double* dad = dac + NAC;
-        const double* dbc = dad + NAD;
-        const double* dbd = dbc + NBC;
+        const T* dk = Dk + kk * DKS;
+        const T* dac = dk;
+        const T* dad = dac + NAC;
+        const T* dbc = dad + NAD;
+        const T* dbd = dbc + NBC;
         double* gk = a.gk + (size_t)kk * n * n;
         fac = f;
         if (r < NAC) {  // K[a][c] += sum_bd V[a b c d] D[b][d]
@@ -759,7 +830,7 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
           dst = gk + (size_t)(ob + j) * n + od + l;
         }
       }
-      atomicAdd(dst, fac * s);
+      atomicAdd(dst, fac * (double)s);
     }
     __syncwarp();
   }

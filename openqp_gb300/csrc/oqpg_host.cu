@@ -63,6 +63,11 @@ __global__ void k_unpack(const double* __restrict__ dp, int nfocks, int nbf, dou
   }
 }
 
+__global__ void k_to_f32(const double* __restrict__ x, long long n, float* y) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    y[t] = (float)x[t];
+}
+
 // shlden (OpenQP int2.F90:999-1047): max |D| over each shell-pair block and
 // over the densities; also the global maximum (max_den).
 __global__ void k_dsh(const double* __restrict__ dp, int nfocks, int nbf, int ns, const int* __restrict__ aoff,
@@ -100,10 +105,11 @@ __global__ void k_dsh(const double* __restrict__ dp, int nfocks, int nbf, int ns
 // with Q_Q >= tau / (4 Q_P Dmax) can pass: they are a prefix of the pairs
 // sorted by Schwarz bound, and only that prefix is walked.  FP32 decides when
 // it is clear by a 1e-5 margin, FP64 with the reference's operation order
-// otherwise.
+// otherwise.  With tau_f32 > 0 the surviving quartets whose test value (Schwarz
+// bound x shell density) is below tau_f32 go to the FP32 lists.
 __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
-  __shared__ unsigned cnt[NCLASS];
-  __shared__ unsigned long long base[NCLASS];
+  __shared__ unsigned cnt[2 * NCLASS];
+  __shared__ unsigned long long base[2 * NCLASS];
   __shared__ int s_len;
   const int P = blockIdx.x;
   const double dmax = __longlong_as_double((long long)*a.dmax_bits);
@@ -129,8 +135,9 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
   const float* dj = a.dshf + (long long)ij.y * a.ns;
   const float dij4 = 4.0f * di[ij.y];
   const float tlo = (float)(a.tau * (1.0 - 1e-5)), thi = (float)(a.tau * (1.0 + 1e-5));
+  const float mlo = (float)(a.tau_f32 * (1.0 - 1e-5)), mhi = (float)(a.tau_f32 * (1.0 + 1e-5));
   for (int s0 = 0; s0 < len; s0 += blockDim.x) {
-    if (threadIdx.x < NCLASS) cnt[threadIdx.x] = 0;
+    if (threadIdx.x < 2 * NCLASS) cnt[threadIdx.x] = 0;
     __syncthreads();
     const int s = s0 + threadIdx.x;
     const int Q = s < len ? a.sorted_idx[s] : a.npair;
@@ -142,26 +149,41 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
       const float m = fmaxf(fmaxf(fmaxf(dij4, 4.0f * a.dshf[(long long)kl.x * a.ns + kl.y]), fmaxf(dj[kl.y], dj[kl.x])),
                             fmaxf(di[kl.y], di[kl.x]));
       const float tf = qPf * a.qf[Q] * m;
+      double t = -1.0;  // exact test value, computed only near a threshold
+      auto exact = [&]() {
+        const double* Di = a.dsh + (long long)ij.x * a.ns;
+        const double* Dj = a.dsh + (long long)ij.y * a.ns;
+        double v = qP * a.q[Q];
+        v *= fmax(fmax(fmax(4.0 * Di[ij.y], 4.0 * a.dsh[(long long)kl.x * a.ns + kl.y]), fmax(Dj[kl.y], Dj[kl.x])),
+                  fmax(Di[kl.y], Di[kl.x]));
+        return v;
+      };
       bool pass;
       if (tf < tlo) pass = false;
       else if (tf > thi) pass = true;
       else {
-        const double* Di = a.dsh + (long long)ij.x * a.ns;
-        const double* Dj = a.dsh + (long long)ij.y * a.ns;
-        double t = qP * a.q[Q];
-        t *= fmax(fmax(fmax(4.0 * Di[ij.y], 4.0 * a.dsh[(long long)kl.x * a.ns + kl.y]), fmax(Dj[kl.y], Dj[kl.x])),
-                  fmax(Di[kl.y], Di[kl.x]));
+        t = exact();
         pass = !(t < a.tau);
       }
       if (pass) {
+        bool f32 = false;
+        if (a.tau_f32 > 0.0) {
+          if (tf < mlo) f32 = true;
+          else if (tf <= mhi) {
+            if (t < 0.0) t = exact();
+            f32 = t < a.tau_f32;
+          }
+        }
         const int tQ = a.pair_type[Q];
         if (tP <= tQ) { c = d_class_index(tP, tQ); ent = make_uint2(P, Q); }
         else { c = d_class_index(tQ, tP); ent = make_uint2(Q, P); }
+        if (f32) c += NCLASS;
         slot = atomicAdd(&cnt[c], 1u);
       }
     }
     __syncthreads();
-    if (threadIdx.x < NCLASS && cnt[threadIdx.x]) base[threadIdx.x] = atomicAdd(&a.counts[threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
+    if (threadIdx.x < 2 * NCLASS && cnt[threadIdx.x])
+      base[threadIdx.x] = atomicAdd(&a.counts[threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
     __syncthreads();
     if (c >= 0 && a.write) {
       const unsigned long long pos = base[c] + slot;
@@ -427,6 +449,13 @@ int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const 
   build_pairs(*c, am, ncontr, poff, ex, cc, 1e-4 * cutoff, 25.0 * std::log(10.0), fp);
   if ((rc = upload(c->d_pairs, fp.pairs, st))) return rc;
   if ((rc = upload(c->d_prims, fp.prims, st))) return rc;
+  std::vector<PrimPairF> pf(fp.prims.size());
+  for (size_t i = 0; i < pf.size(); ++i) {
+    const PrimPair& s = fp.prims[i];
+    pf[i] = PrimPairF{(float)s.p, (float)s.hp, (float)s.px, (float)s.py, (float)s.pz,
+                      (float)s.ax, (float)s.ay, (float)s.az, (float)s.sp, 0.0f};
+  }
+  if ((rc = upload(c->d_primsf, pf, st))) return rc;
   if ((rc = upload(c->d_pair_ij, fp.ij, st))) return rc;
   if ((rc = upload(c->d_pair_type, fp.type, st))) return rc;
   if ((rc = upload(c->d_q, c->schwarz_pair, st))) return rc;
@@ -449,7 +478,8 @@ void ctx_free(oqpg_ctx* c) {
   if (!c) return;
   DevBuf* bufs[] = {&c->d_shells, &c->d_pairs, &c->d_prims, &c->d_pair_ij, &c->d_pair_type, &c->d_q, &c->d_qf,
                     &c->d_aoff, &c->d_naos, &c->d_dp, &c->d_dj, &c->d_dk, &c->d_gj, &c->d_gk, &c->d_f,
-                    &c->d_fold, &c->d_dsh, &c->d_dshf, &c->d_dmax, &c->d_counts, &c->d_prim_counter};
+                    &c->d_fold, &c->d_dsh, &c->d_dshf, &c->d_dmax, &c->d_counts, &c->d_prim_counter,
+                    &c->d_primsf, &c->d_djf, &c->d_dkf};
   for (DevBuf* b : bufs) b->release();
   for (auto& b : c->d_lists) b.release();
   for (auto& b : c->d_slists) b.release();
@@ -465,26 +495,44 @@ void ctx_free(oqpg_ctx* c) {
 
 // Core build on device buffers.  dp: packed densities (device), f: packed
 // output (device), f_old: optional packed previous Fock (device, updated).
+// Lists 0..20 hold the FP64 quartets of each class, lists 21..41 the FP32
+// quartets of the precision-split build (empty in the plain FP64 mode).
 int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfocks, double se, double sc,
               cudaStream_t st) {
   if (nfocks != 1 && nfocks != 2) return UNSUPPORTED;
+  constexpr int NL = 2 * NCLASS;
   const int n = c->nbf, ns = c->nshell;
   const size_t n2 = (size_t)n * n;
   const int nk = nfocks;
+  const bool split = (c->precision_mode == 1 || c->precision_mode == 2) && c->tau_f32 > 0.0;
   CK(c->d_dj.ensure(sizeof(double) * n2));
   if (nk == 2) CK(c->d_dk.ensure(sizeof(double) * 2 * n2));
+  if (split) {
+    CK(c->d_djf.ensure(sizeof(float) * n2));
+    if (nk == 2) CK(c->d_dkf.ensure(sizeof(float) * 2 * n2));
+  }
   CK(c->d_gj.ensure(sizeof(double) * n2));
   CK(c->d_gk.ensure(sizeof(double) * nk * n2));
   CK(c->d_dsh.ensure(sizeof(double) * ns * ns));
   CK(c->d_dshf.ensure(sizeof(float) * ns * ns));
   CK(c->d_dmax.ensure(sizeof(unsigned long long)));
-  CK(c->d_counts.ensure(sizeof(unsigned long long) * NCLASS));
-  CK(c->d_prim_counter.ensure(sizeof(unsigned long long) * NCLASS));
-  CK(c->d_work.ensure(sizeof(unsigned long long) * 2 * NCLASS));
+  CK(c->d_counts.ensure(sizeof(unsigned long long) * NL));
+  CK(c->d_prim_counter.ensure(sizeof(unsigned long long) * NL));
+  CK(c->d_work.ensure(sizeof(unsigned long long) * 2 * NL));
   CK(cudaEventRecord(c->ev[0], st));
   k_unpack<<<std::min<long long>((n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(dp, nfocks, n, c->d_dj.as<double>(),
                                                                                  c->d_dk.as<double>());
   CK(cudaGetLastError());
+  if (split) {
+    k_to_f32<<<std::min<long long>((n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(c->d_dj.as<double>(), (long long)n2,
+                                                                                   c->d_djf.as<float>());
+    CK(cudaGetLastError());
+    if (nk == 2) {
+      k_to_f32<<<std::min<long long>((2 * n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
+          c->d_dk.as<double>(), (long long)(2 * n2), c->d_dkf.as<float>());
+      CK(cudaGetLastError());
+    }
+  }
   CK(cudaMemsetAsync(c->d_dmax.p, 0, sizeof(unsigned long long), st));
   const long long npair = c->npair;
   k_dsh<<<std::min<long long>((npair + 127) / 128, c->nsm * 8LL), 128, 0, st>>>(
@@ -501,24 +549,25 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
   la.dsh = c->d_dsh.as<double>(); la.dshf = c->d_dshf.as<float>();
   la.dmax_bits = c->d_dmax.as<unsigned long long>();
   la.tau = c->tau;
+  la.tau_f32 = split ? c->tau_f32 : 0.0;
   la.counts = c->d_counts.as<unsigned long long>();
   bool lists_ok = false;
   for (int pass = 0; pass < 3 && !lists_ok; ++pass) {
     la.write = c->have_caps ? 1 : 0;
-    for (int k = 0; k < NCLASS; ++k) { la.lists[k] = c->d_lists[k].as<uint2>(); la.caps[k] = c->caps[k]; }
-    CK(cudaMemsetAsync(c->d_counts.p, 0, sizeof(unsigned long long) * NCLASS, st));
+    for (int k = 0; k < NL; ++k) { la.lists[k] = c->d_lists[k].as<uint2>(); la.caps[k] = c->caps[k]; }
+    CK(cudaMemsetAsync(c->d_counts.p, 0, sizeof(unsigned long long) * NL, st));
     k_lists<<<c->npair, 256, 0, st>>>(la);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(c->counts, c->d_counts.p, sizeof(unsigned long long) * NCLASS, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(c->counts, c->d_counts.p, sizeof(unsigned long long) * NL, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     bool ok = c->have_caps;
-    for (int k = 0; k < NCLASS; ++k)
+    for (int k = 0; k < NL; ++k)
       if (c->counts[k] > c->caps[k]) ok = false;
     if (ok) {
       lists_ok = true;
       break;
     }
-    for (int k = 0; k < NCLASS; ++k) {
+    for (int k = 0; k < NL; ++k) {
       if (c->counts[k] > c->caps[k] || !c->have_caps) {
         const unsigned long long cap = c->counts[k] + c->counts[k] / 8 + 1024;
         if (cap > c->caps[k]) {
@@ -530,27 +579,27 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
     c->have_caps = true;
   }
   if (!lists_ok) return DEV_ERR;  // quartet lists never fitted: do not launch on partial lists
-  // --- order every class list by primitive-quartet count (counting sort)
-  CK(c->d_hist.ensure(sizeof(unsigned long long) * NCLASS * NBIN));
-  CK(c->d_cursor.ensure(sizeof(unsigned long long) * NCLASS * NBIN));
-  CK(cudaMemsetAsync(c->d_hist.p, 0, sizeof(unsigned long long) * NCLASS * NBIN, st));
-  for (int k = 0; k < NCLASS; ++k) {
+  // --- order every list by primitive-quartet count (counting sort)
+  CK(c->d_hist.ensure(sizeof(unsigned long long) * NL * NBIN));
+  CK(c->d_cursor.ensure(sizeof(unsigned long long) * NL * NBIN));
+  CK(cudaMemsetAsync(c->d_hist.p, 0, sizeof(unsigned long long) * NL * NBIN, st));
+  for (int k = 0; k < NL; ++k) {
     if (!c->counts[k]) continue;
     const long long nk_ = (long long)c->counts[k];
     k_bin_hist<<<(unsigned)std::min<long long>((nk_ + 255) / 256, c->nsm * 4LL), 256, 0, st>>>(
         c->d_lists[k].as<uint2>(), nk_, c->d_pairs.as<PairDev>(), c->d_hist.as<unsigned long long>() + k * NBIN);
     CK(cudaGetLastError());
   }
-  std::vector<unsigned long long> hist(NCLASS * NBIN), cur(NCLASS * NBIN);
-  CK(cudaMemcpyAsync(hist.data(), c->d_hist.p, sizeof(unsigned long long) * NCLASS * NBIN, cudaMemcpyDeviceToHost, st));
+  unsigned long long hist[NL * NBIN], cur[NL * NBIN];
+  CK(cudaMemcpyAsync(hist, c->d_hist.p, sizeof(hist), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  for (int k = 0; k < NCLASS; ++k) {
+  for (int k = 0; k < NL; ++k) {
     unsigned long long s = 0;
     for (int b = 0; b < NBIN; ++b) { cur[k * NBIN + b] = s; s += hist[k * NBIN + b]; }
     if (s != c->counts[k]) return DEV_ERR;
   }
-  CK(cudaMemcpyAsync(c->d_cursor.p, cur.data(), sizeof(unsigned long long) * NCLASS * NBIN, cudaMemcpyHostToDevice, st));
-  for (int k = 0; k < NCLASS; ++k) {
+  CK(cudaMemcpyAsync(c->d_cursor.p, cur, sizeof(cur), cudaMemcpyHostToDevice, st));
+  for (int k = 0; k < NL; ++k) {
     if (!c->counts[k]) continue;
     const long long nk_ = (long long)c->counts[k];
     CK(c->d_slists[k].ensure(sizeof(uint2) * nk_));
@@ -564,12 +613,13 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
   // --- integrals + digestion
   CK(cudaMemsetAsync(c->d_gj.p, 0, sizeof(double) * n2, st));
   CK(cudaMemsetAsync(c->d_gk.p, 0, sizeof(double) * nk * n2, st));
-  CK(cudaMemsetAsync(c->d_prim_counter.p, 0, sizeof(unsigned long long) * NCLASS, st));
-  CK(cudaMemsetAsync(c->d_work.p, 0, sizeof(unsigned long long) * 2 * NCLASS, st));
+  CK(cudaMemsetAsync(c->d_prim_counter.p, 0, sizeof(unsigned long long) * NL, st));
+  CK(cudaMemsetAsync(c->d_work.p, 0, sizeof(unsigned long long) * 2 * NL, st));
   BuildArgs a{};
   a.shells = c->d_shells.as<ShellDev>();
   a.pairs = c->d_pairs.as<PairDev>();
   a.prims = c->d_prims.as<PrimPair>();
+  a.primsf = c->d_primsf.as<PrimPairF>();
   a.nbf = n;
   a.nk = nk;
   a.prim_cut = 1e-4 * c->tau;
@@ -578,35 +628,43 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
   a.elem_cut = c->tau;
   a.dj = c->d_dj.as<double>();
   a.dk = (nk == 1) ? c->d_dj.as<double>() : c->d_dk.as<double>();
+  a.djf = c->d_djf.as<float>();
+  a.dkf = (nk == 1) ? c->d_djf.as<float>() : c->d_dkf.as<float>();
   a.gj = c->d_gj.as<double>();
   a.gk = c->d_gk.as<double>();
+  a.roots_f32 = c->precision_mode == 2 ? 1 : 0;
   double nq = 0;
-  // heaviest classes first; every class launch is bracketed by events
+  // heaviest classes first; every class launch (both precisions) is bracketed by events
   int nlaunch = 0;
   for (int cl = NCLASS - 1; cl >= 0; --cl) {
-    if (c->counts[cl] == 0) continue;
-    a.counters = c->d_prim_counter.as<unsigned long long>() + cl;
-    nq += (double)c->counts[cl];
+    if (c->counts[cl] == 0 && c->counts[NCLASS + cl] == 0) continue;
     CK(cudaEventRecord(c->evc[cl][0], st));
-    long long head = 0;
-    if (!class_info(cl).team) {
-      // quartets with >= 2^PRIM_SPLIT_LOG2 primitive quartets (a prefix of the
-      // sorted list) go to the warp-per-quartet primitive-parallel kernel
-      for (int b = 0; b <= NBIN - 1 - 4 * PRIM_SPLIT_LOG2; ++b) head += (long long)hist[cl * NBIN + b];
-      if (head > 0) {
-        a.quartets = c->d_slists[cl].as<uint2>();
-        a.nquartets = head;
-        a.work = c->d_work.as<unsigned long long>() + NCLASS + cl;
-        CK(launch_class(cl, c->pure, MODE_PRIM, a, c->nsm, st));
+    for (int prec = 0; prec < 2; ++prec) {
+      const int li = cl + prec * NCLASS;
+      if (!c->counts[li]) continue;
+      const int fl = prec ? MODE_F32 : 0;
+      a.counters = c->d_prim_counter.as<unsigned long long>() + li;
+      nq += (double)c->counts[li];
+      long long head = 0;
+      if (!class_info(cl).team) {
+        // quartets with >= 2^PRIM_SPLIT_LOG2 primitive quartets (a prefix of the
+        // sorted list) go to the warp-per-quartet primitive-parallel kernel
+        for (int b = 0; b <= NBIN - 1 - 4 * PRIM_SPLIT_LOG2; ++b) head += (long long)hist[li * NBIN + b];
+        if (head > 0) {
+          a.quartets = c->d_slists[li].as<uint2>();
+          a.nquartets = head;
+          a.work = c->d_work.as<unsigned long long>() + NL + li;
+          CK(launch_class(cl, c->pure, MODE_PRIM | fl, a, c->nsm, st));
+          ++nlaunch;
+        }
+      }
+      if ((long long)c->counts[li] > head) {
+        a.quartets = c->d_slists[li].as<uint2>() + head;
+        a.nquartets = (long long)c->counts[li] - head;
+        a.work = c->d_work.as<unsigned long long>() + li;
+        CK(launch_class(cl, c->pure, MODE_FOCK | fl, a, c->nsm, st));
         ++nlaunch;
       }
-    }
-    if ((long long)c->counts[cl] > head) {
-      a.quartets = c->d_slists[cl].as<uint2>() + head;
-      a.nquartets = (long long)c->counts[cl] - head;
-      a.work = c->d_work.as<unsigned long long>() + cl;
-      CK(launch_class(cl, c->pure, MODE_FOCK, a, c->nsm, st));
-      ++nlaunch;
     }
     CK(cudaEventRecord(c->evc[cl][1], st));
   }
@@ -617,7 +675,7 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
       c->d_gj.as<double>(), c->d_gk.as<double>(), nk, n, sc, ck, f, f_old);
   CK(cudaGetLastError());
   CK(cudaEventRecord(c->ev[3], st));
-  unsigned long long nprim[NCLASS];
+  unsigned long long nprim[NL];
   CK(cudaMemcpyAsync(nprim, c->d_prim_counter.p, sizeof(nprim), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   float t01 = 0, t12 = 0, t03 = 0;
@@ -626,11 +684,15 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
   cudaEventElapsedTime(&t03, c->ev[0], c->ev[3]);
   double* S = c->last_stats;
   S[1] = 0;
+  double q32 = 0, p32 = 0;
   for (int k = 0; k < NCLASS; ++k) {
-    S[7 + k] = (double)c->counts[k];
-    S[7 + NCLASS + k] = c->counts[k] ? (double)nprim[k] : 0.0;
+    const unsigned long long q = c->counts[k] + c->counts[NCLASS + k];
+    S[7 + k] = (double)q;
+    S[7 + NCLASS + k] = (c->counts[k] ? (double)nprim[k] : 0.0) + (c->counts[NCLASS + k] ? (double)nprim[NCLASS + k] : 0.0);
+    q32 += (double)c->counts[NCLASS + k];
+    p32 += c->counts[NCLASS + k] ? (double)nprim[NCLASS + k] : 0.0;
     float tk = 0;
-    if (c->counts[k]) cudaEventElapsedTime(&tk, c->evc[k][0], c->evc[k][1]);
+    if (q) cudaEventElapsedTime(&tk, c->evc[k][0], c->evc[k][1]);
     S[7 + 2 * NCLASS + k] = tk;
     S[1] += S[7 + NCLASS + k];
   }
@@ -641,6 +703,8 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
   S[5] = n;
   S[6] = c->npair;
   S[7 + 3 * NCLASS] = nlaunch + 4;  // class kernels + unpack, dsh, lists, finalize
+  S[8 + 3 * NCLASS] = q32;
+  S[9 + 3 * NCLASS] = p32;
   return OK;
 }
 
@@ -728,7 +792,7 @@ int oqpg_schwarz(const oqpg_ctx* ctx, double* q) {
 
 int oqpg_stats(const oqpg_ctx* ctx, double* out, int n) {
   if (!ctx) return NOT_INIT;
-  for (int i = 0; i < n && i < 8 + 3 * NCLASS; ++i) out[i] = ctx->last_stats[i];
+  for (int i = 0; i < n && i < 10 + 3 * NCLASS; ++i) out[i] = ctx->last_stats[i];
   return OK;
 }
 
@@ -766,6 +830,21 @@ int oqpg_measure_fp64_peak(int iters, double* tflops) {
   cudaEventDestroy(e1);
   cudaFree(d);
   return OK;
+}
+
+int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold) {
+  if (!ctx) return NOT_INIT;
+  if (mode < 0 || mode > 2) return UNSUPPORTED;
+  if (mode != 0 && !(threshold > 0.0)) return UNSUPPORTED;
+  ctx->precision_mode = mode;
+  ctx->tau_f32 = mode != 0 ? threshold : 0.0;
+  return OK;
+}
+
+int routec_fock_set_precision(int mode, double threshold) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (!g_ctx) return NOT_INIT;
+  return oqpg_set_precision(g_ctx, mode, threshold);
 }
 
 int oqpg_class_l(int c, int* l4) {

@@ -27,9 +27,10 @@ struct ListArgs {
   const float* dshf;
   const unsigned long long* dmax_bits;
   double tau;
-  unsigned long long* counts;   // NCLASS
-  uint2* lists[NCLASS];
-  unsigned long long caps[NCLASS];
+  double tau_f32;               // quartets with bound < tau_f32 go to the FP32 lists (0: none)
+  unsigned long long* counts;   // 2 NCLASS: FP64 lists, then FP32 lists
+  uint2* lists[2 * NCLASS];
+  unsigned long long caps[2 * NCLASS];
   int write;
 };
 
@@ -55,6 +56,7 @@ struct DevBuf {
 
 // Build-pipeline kernels (oqpg_host.cu).
 __global__ void k_unpack(const double* __restrict__ dp, int nfocks, int nbf, double* dj, double* dk);
+__global__ void k_to_f32(const double* __restrict__ x, long long n, float* y);
 __global__ void k_dsh(const double* __restrict__ dp, int nfocks, int nbf, int ns, const int* __restrict__ aoff,
                       const int* __restrict__ nao, double* dsh, float* dshf, unsigned long long* dmax_bits);
 __global__ void k_lists(const ListArgs a);
@@ -77,14 +79,18 @@ struct oqpg_ctx {
   std::vector<oqpg::ShellDev> shells;
   std::vector<int> aoff, naos;
   std::vector<double> schwarz_pair;   // per pair (canonical index)
+  // precision split: 0 = every quartet in FP64, 1 = bound < tau_f32 in FP32
+  int precision_mode = 0;
+  double tau_f32 = 0.0;
   // device tables
-  oqpg::DevBuf d_shells, d_pairs, d_prims, d_pair_ij, d_pair_type, d_q, d_qf, d_aoff, d_naos;
+  oqpg::DevBuf d_shells, d_pairs, d_prims, d_primsf, d_pair_ij, d_pair_type, d_q, d_qf, d_aoff, d_naos;
   // per-build buffers
-  oqpg::DevBuf d_dp, d_dj, d_dk, d_gj, d_gk, d_f, d_fold, d_dsh, d_dshf, d_dmax, d_counts, d_prim_counter;
-  oqpg::DevBuf d_lists[oqpg::NCLASS], d_slists[oqpg::NCLASS];
+  oqpg::DevBuf d_dp, d_dj, d_dk, d_djf, d_dkf, d_gj, d_gk, d_f, d_fold, d_dsh, d_dshf, d_dmax, d_counts,
+      d_prim_counter;
+  oqpg::DevBuf d_lists[2 * oqpg::NCLASS], d_slists[2 * oqpg::NCLASS];
   oqpg::DevBuf d_sorted_idx, d_sorted_q, d_hist, d_cursor, d_work;
-  unsigned long long caps[oqpg::NCLASS] = {0};
-  unsigned long long counts[oqpg::NCLASS] = {0};
+  unsigned long long caps[2 * oqpg::NCLASS] = {0};
+  unsigned long long counts[2 * oqpg::NCLASS] = {0};
   bool have_caps = false;
   // pinned staging
   double* h_in = nullptr;
@@ -92,5 +98,5 @@ struct oqpg_ctx {
   size_t h_bytes = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t evc[oqpg::NCLASS][2] = {};
-  double last_stats[8 + 3 * oqpg::NCLASS] = {0};
+  double last_stats[10 + 3 * oqpg::NCLASS] = {0};
 };

@@ -25,51 +25,52 @@ cudaError_t launch_persistent(Kern kern, size_t smem, long long per_block_items,
   return cudaGetLastError();
 }
 
-template <int LA, int LB, int LC, int LD, bool PURE, bool SCH>
-cudaError_t launch_small(const BuildArgs& a, int nsm, cudaStream_t st) {
-  return launch_persistent(k_small<LA, LB, LC, LD, PURE, SCH>, 0, 128, a, nsm, st);
-}
-
-template <int LA, int LB, int LC, int LD, bool PURE, bool SCH>
-cudaError_t launch_team(const BuildArgs& a, int nsm, cudaStream_t st) {
-  const size_t smem = sizeof(double) * 4 * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
-  return launch_persistent(k_team<LA, LB, LC, LD, PURE, SCH>, smem, 4, a, nsm, st);
-}
-
 // Classes with more than 27 Cartesian elements run one warp per quartet.
 template <int LA, int LB, int LC, int LD>
 constexpr bool is_team() { return Cls<LA, LB, LC, LD>::NE > 27; }
 
+template <int LA, int LB, int LC, int LD, bool PURE, typename T>
+cudaError_t launch_fock(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
+  if constexpr (is_team<LA, LB, LC, LD>()) {
+    if (kind == MODE_PRIM) return cudaErrorInvalidValue;
+    const size_t smem = sizeof(T) * 4 * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
+    return launch_persistent(k_team<LA, LB, LC, LD, PURE, false, T>, smem, 4, a, nsm, st);
+  } else {
+    if (kind == MODE_PRIM) return launch_persistent(k_prim<LA, LB, LC, LD, PURE, T>, 0, 4, a, nsm, st);
+    return launch_persistent(k_small<LA, LB, LC, LD, PURE, false, T>, 0, 128, a, nsm, st);
+  }
+}
+
+template <int LA, int LB, int LC, int LD, bool PURE>
+cudaError_t launch_schwarz(const BuildArgs& a, int nsm, cudaStream_t st) {
+  if constexpr (LA == LC && LB == LD) {
+    if constexpr (is_team<LA, LB, LC, LD>()) {
+      const size_t smem = sizeof(double) * 4 * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
+      return launch_persistent(k_team<LA, LB, LC, LD, PURE, true, double>, smem, 4, a, nsm, st);
+    } else {
+      return launch_persistent(k_small<LA, LB, LC, LD, PURE, true, double>, 0, 128, a, nsm, st);
+    }
+  } else {
+    return cudaErrorInvalidValue;
+  }
+}
+
 // mode: MODE_FOCK, MODE_SCHWARZ (diagonal classes only), MODE_PRIM (small
-// classes only: the heavily contracted head of a sorted list).
+// classes only: the heavily contracted head of a sorted list), each optionally
+// with MODE_F32 (FP32 quartets of the precision-split build; not Schwarz).
 template <int LA, int LB, int LC, int LD>
 cudaError_t launch_cls(bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
-  constexpr bool DIAG = (LA == LC && LB == LD);
-  const bool sch = mode == MODE_SCHWARZ;
-  if (sch && !DIAG) return cudaErrorInvalidValue;
-  if (mode == MODE_PRIM) {
-    if constexpr (is_team<LA, LB, LC, LD>()) {
-      return cudaErrorInvalidValue;
-    } else {
-      return pure ? launch_persistent(k_prim<LA, LB, LC, LD, true>, 0, 4, a, nsm, st)
-                  : launch_persistent(k_prim<LA, LB, LC, LD, false>, 0, 4, a, nsm, st);
-    }
+  const bool f32 = (mode & MODE_F32) != 0;
+  const int kind = mode & ~MODE_F32;
+  if (kind == MODE_SCHWARZ) {
+    if (f32) return cudaErrorInvalidValue;
+    return pure ? launch_schwarz<LA, LB, LC, LD, true>(a, nsm, st) : launch_schwarz<LA, LB, LC, LD, false>(a, nsm, st);
   }
-  if constexpr (is_team<LA, LB, LC, LD>()) {
-    if constexpr (DIAG) {
-      if (sch) return pure ? launch_team<LA, LB, LC, LD, true, true>(a, nsm, st)
-                           : launch_team<LA, LB, LC, LD, false, true>(a, nsm, st);
-    }
-    return pure ? launch_team<LA, LB, LC, LD, true, false>(a, nsm, st)
-                : launch_team<LA, LB, LC, LD, false, false>(a, nsm, st);
-  } else {
-    if constexpr (DIAG) {
-      if (sch) return pure ? launch_small<LA, LB, LC, LD, true, true>(a, nsm, st)
-                           : launch_small<LA, LB, LC, LD, false, true>(a, nsm, st);
-    }
-    return pure ? launch_small<LA, LB, LC, LD, true, false>(a, nsm, st)
-                : launch_small<LA, LB, LC, LD, false, false>(a, nsm, st);
-  }
+  if (f32)
+    return pure ? launch_fock<LA, LB, LC, LD, true, float>(kind, a, nsm, st)
+                : launch_fock<LA, LB, LC, LD, false, float>(kind, a, nsm, st);
+  return pure ? launch_fock<LA, LB, LC, LD, true, double>(kind, a, nsm, st)
+              : launch_fock<LA, LB, LC, LD, false, double>(kind, a, nsm, st);
 }
 
 }  // namespace oqpg

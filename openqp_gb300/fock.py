@@ -89,6 +89,15 @@ class FockBuilder:
             raise FockError(rc, "oqpg_fock_jk_device")
         return out
 
+    def set_precision(self, mode, threshold=1e-6):
+        """mode "fp64": plain path; mode "mixed": quartets whose screening value
+        (Schwarz bound x shell density) is below threshold run in FP32 with their
+        Rys roots/weights in FP64; "mixed-fast": the same with FP32 roots."""
+        m = {"fp64": 0, "mixed": 1, "mixed-fast": 2}[mode]
+        rc = lib().oqpg_set_precision(self.h, m, float(threshold))
+        if rc != 0:
+            raise FockError(rc, "oqpg_set_precision")
+
     def schwarz(self):
         ns = len(self.bas.am)
         q = np.zeros(ns * ns)
@@ -98,13 +107,14 @@ class FockBuilder:
         return q.reshape(ns, ns)
 
     def stats(self):
-        s = np.zeros(8 + 3 * NCLASS)
+        s = np.zeros(10 + 3 * NCLASS)
         lib().oqpg_stats(self.h, ptr(s), len(s))
         return dict(quartets=int(s[0]), prim_quartets=int(s[1]), list_ms=s[2], eri_ms=s[3], total_ms=s[4],
                     nbf=int(s[5]), npair=int(s[6]), per_class=[int(v) for v in s[7:7 + NCLASS]],
                     prim_per_class=[int(v) for v in s[7 + NCLASS:7 + 2 * NCLASS]],
                     ms_per_class=[float(v) for v in s[7 + 2 * NCLASS:7 + 3 * NCLASS]],
-                    launches=int(s[7 + 3 * NCLASS]))
+                    launches=int(s[7 + 3 * NCLASS]), f32_quartets=int(s[8 + 3 * NCLASS]),
+                    f32_prim_quartets=int(s[9 + 3 * NCLASS]))
 
 
 def fp64_peak_tflops(iters=20000):

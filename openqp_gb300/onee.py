@@ -185,3 +185,28 @@ def nuclear_repulsion(bas: BasisArrays):
         for j in range(i):
             e += bas.charges[i] * bas.charges[j] / np.linalg.norm(bas.xyz[i] - bas.xyz[j])
     return e
+
+
+def one_electron(bas: BasisArrays, charges=None):
+    """S, T, V (nbf x nbf) from the library's threaded C++ routine
+    (McMurchie-Davidson); the numpy functions above are its slow restatement."""
+    from ._lib import FockError, lib, ptr, _i
+    if charges is None:
+        charges = bas.charges
+    am = np.ascontiguousarray(bas.am, dtype=np.int32)
+    nc = np.ascontiguousarray(bas.ncontr, dtype=np.int32)
+    org = np.ascontiguousarray(bas.origin, dtype=np.int32)
+    ex = np.ascontiguousarray(bas.ex, dtype=np.float64)
+    cc = np.ascontiguousarray(bas.cc, dtype=np.float64)
+    hm = np.ascontiguousarray(bas.harmonic, dtype=np.int32)
+    xyz = np.ascontiguousarray(bas.xyz.reshape(-1), dtype=np.float64)
+    ch = np.ascontiguousarray(charges, dtype=np.float64)
+    out = []
+    for which in range(3):
+        m = np.empty((bas.nbf, bas.nbf))
+        rc = lib().oqpg_one_electron(len(am), ptr(am, _i), ptr(nc, _i), ptr(org, _i), ptr(ex), ptr(cc), ptr(hm, _i),
+                                     int(bas.natom), ptr(xyz), ptr(ch), which, ptr(m))
+        if rc != 0:
+            raise FockError(rc, "oqpg_one_electron")
+        out.append(m)
+    return tuple(out)

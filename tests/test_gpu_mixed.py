@@ -1,0 +1,74 @@
+"""Precision-split builds (form (b)): FP32 for the quartets whose screening
+value is below the threshold, FP64 for the rest, against the FP64 paths.
+
+Tolerances: the FP32 quartets contribute at most ~threshold each, so with a
+threshold of 1e-6 the Fock matrix may move by ~1e-7 and the two-electron
+energy 1/2 tr(D G) by ~1e-7 Eh here; the SCF energy must stay within 1e-6 Eh
+of the FP64 oracle (the benchmark spec's bound).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail("no CUDA device")
+    from openqp_gb300 import build
+    build.build()
+    from openqp_gb300 import fock
+    return fock
+
+
+def _e2(d, f, n):
+    from openqp_gb300.basis import unpack
+    return 0.5 * sum(np.sum(unpack(d[i], n) * unpack(f[i], n)) for i in range(d.shape[0]))
+
+
+@pytest.mark.parametrize("basis", ["6-31g(d)", "cc-pvdz"])
+def test_mixed_fock_close_to_fp64(gpu, oracle_lib, basis):
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(8, workloads.cube_edge_like_c1(8), seed=2, basis=basis)
+    d = workloads.density(bas, 40, 2)
+    fb = gpu.FockBuilder(bas, cutoff=1e-10)
+    f64 = fb.fock_jk(d)
+    ref = oracle_lib.Oracle(bas, cutoff=1e-10).fock_jk(d)
+    assert np.abs(f64 - ref).max() < 1e-10
+    fb.set_precision("mixed", 1e-6)
+    fmx = fb.fock_jk(d)
+    st = fb.stats()
+    assert st["f32_quartets"] > 0 and st["f32_quartets"] < st["quartets"]
+    assert np.abs(fmx - ref).max() < 1e-6
+    assert abs(_e2(d[None], fmx, bas.nbf) - _e2(d[None], ref, bas.nbf)) < 1e-6
+    fb.set_precision("fp64")
+    assert np.abs(fb.fock_jk(d) - ref).max() < 1e-10
+
+
+def test_mixed_uhf(gpu, oracle_lib):
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(6, workloads.cube_edge_like_c1(6), seed=4, basis="6-31g(d)")
+    d = workloads.density_open(bas, 31, 29, 4)
+    fb = gpu.FockBuilder(bas, cutoff=1e-10)
+    fb.set_precision("mixed", 1e-6)
+    fmx = fb.fock_jk(d)
+    ref = oracle_lib.Oracle(bas, cutoff=1e-10).fock_jk(d)
+    assert np.abs(fmx - ref).max() < 1e-6
+
+
+def test_mixed_scf_energy_within_1e6(gpu, oracle_lib):
+    """RHF SCF of (H2O)4 with incremental mixed builds vs the FP64 oracle SCF."""
+    from openqp_gb300 import onee, scf, workloads
+    bas = workloads.water_cluster_basis(4, 6.0, seed=1, basis="6-31g(d)")
+    S, T = onee.overlap_kinetic(bas)
+    H = T + onee.nuclear(bas)
+    enuc = onee.nuclear_repulsion(bas)
+    o = oracle_lib.Oracle(bas, cutoff=1e-10)
+    ref = scf.run_scf(bas.nbf, S, H, enuc, 20, 20, lambda d: o.fock_jk(d), conv=1e-10)
+    fb = gpu.FockBuilder(bas, cutoff=1e-10)
+    fb.set_precision("mixed", 1e-6)
+    mx = scf.run_scf(bas.nbf, S, H, enuc, 20, 20, fb.fock_jk, conv=1e-10, incremental=True)
+    assert ref["converged"] and mx["converged"]
+    assert abs(mx["energy"] - ref["energy"]) < 1e-6
