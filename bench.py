@@ -48,6 +48,9 @@ WORKLOADS = {
     # linear all-trans C40H82, 6-31G(d) Cartesian (the precision-split configuration)
     "alkane40_631gd": dict(name="C40H82 6-31G(d) Cartesian RHF J+K Fock build", alkane=40, seed=0,
                            basis="6-31g(d)", cutoff=1e-10),
+    # 256 water clusters of 1-16 molecules (uniform), 6-31G, built together
+    "batch256_631g": dict(name="256 water clusters (1-16 H2O, uniform), 6-31G, batched RHF J+K builds", batch=256,
+                          seed=0, basis="6-31g", cutoff=1e-10),
     # only the d shells of a (H2O)64 6-31G(d) cluster: every quartet is (dd|dd)
     "dd_only": dict(name="(dd|dd)-only: the 64 d shells of a (H2O)64 6-31G(d) cluster", nwater=64, edge=15.1,
                     seed=0, basis="6-31g(d)", cutoff=1e-10, only_l=2),
@@ -55,10 +58,12 @@ WORKLOADS = {
 WORKLOAD = dict(WORKLOADS["water32_ccpvdz"])
 
 
-def make_workload():
+def make_workload(overlap="library"):
+    """Basis and seeded density of the workload.  The overlap for the Loewdin
+    step comes from the library's host routine, or from the oracle in the
+    reference arm (identical to 1e-14)."""
     from openqp_gb300 import workloads
     from openqp_gb300.basis import BasisArrays
-    from openqp_gb300.onee import overlap_kinetic
     from openqp_gb300.basis import build_basis
     if "alkane" in WORKLOAD:
         z, xyz = workloads.alkane(WORKLOAD["alkane"], WORKLOAD["seed"])
@@ -78,7 +83,13 @@ def make_workload():
         nocc = bas.nbf // 4
     else:
         nocc = workloads.nelectrons(bas) // 2
-    S, _ = overlap_kinetic(bas)
+    if overlap == "library":
+        from openqp_gb300.onee import one_electron
+        S = one_electron(bas)[0]
+    else:
+        from oracle import oracle
+        oracle.build()
+        S = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"]).one_electron("S")
     d = workloads.density(bas, nocc, WORKLOAD["seed"], S=S)
     return bas, d
 
@@ -162,9 +173,28 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    bas, d = make_workload()
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
+    if "batch" in WORKLOAD:
+        from openqp_gb300 import workloads
+        from oracle import oracle
+        oracle.build()
+        _, bases, dens = workloads.water_batch(WORKLOAD["batch"], WORKLOAD["seed"], basis=WORKLOAD["basis"],
+                                               overlap=lambda b: oracle.Oracle(b).one_electron("S"))
+        vals = []
+        for _ in range(max(1, args.steps)):
+            cb = cpu_baseline_batch(bases, dens, args.cpu_budget)
+            vals.append(cb["value"])
+        v = statistics.median(vals)
+        cb["value"] = v
+        line = {"impl": "reference", "metric": "J+K Fock builds/s (molecule builds, batched)", "value": v,
+                "unit": "builds/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD["name"], "nmol": len(bases), "cutoff": WORKLOAD["cutoff"]},
+                "cpu_baseline": cb, "e2e": {"value": v, "unit": "builds/s", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    bas, d = make_workload(overlap="oracle")
     vals = []
     info = None
     for _ in range(max(1, args.steps)):
@@ -230,7 +260,7 @@ def run_ours(args):
         return tsum, stats, out.clone()
 
     mixed = None
-    if args.precision == "mixed":
+    if args.precision != "fp64":
         t64, _, f64 = timed("fp64")
     sampler = ClockSampler(local)
     sampler.start()
@@ -239,11 +269,11 @@ def run_ours(args):
     wall = time.perf_counter() - wall0
     clocks = sampler.stop()
     value = ws * args.steps / tsum
-    if args.precision == "mixed":
+    if args.precision != "fp64":
         from openqp_gb300.basis import unpack
         df = (fval - f64).cpu().numpy()[0]
         de2 = 0.5 * float(np.sum(unpack(d, bas.nbf) * unpack(df, bas.nbf)))
-        mixed = {"threshold": args.mixed_threshold, "fp64_builds_per_s": ws * args.steps / t64,
+        mixed = {"mode": args.precision, "threshold": args.mixed_threshold, "fp64_builds_per_s": ws * args.steps / t64,
                  "speedup_vs_fp64": t64 / tsum, "max_abs_dF": float(np.abs(df).max()),
                  "dE2_Eh": de2, "f32_quartet_fraction": stats[-1]["f32_quartets"] / max(1, stats[-1]["quartets"])}
     # e2e through the seam with host buffers
@@ -309,6 +339,207 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def pct(v, q):
+    return float(np.percentile(np.asarray(v), q))
+
+
+def run_batch(args):
+    """Batched builds: one context over all clusters, replayed from one CUDA
+    graph, against the plain FP64 path building each cluster on its own."""
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from openqp_gb300 import build as bld
+    bld.build()
+    from openqp_gb300 import autotune, workloads
+    from openqp_gb300.basis import unpack
+    from openqp_gb300.fock import BatchFockBuilder, FockBuilder, class_flops, class_labels, fp64_peak_tflops
+    sizes, bases, dens = workloads.water_batch(WORKLOAD["batch"], WORKLOAD["seed"] + rank, basis=WORKLOAD["basis"])
+    nmol = len(bases)
+    st = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    # --- plain FP64 path, one cluster per build (device-resident densities)
+    singles = [FockBuilder(b, cutoff=WORKLOAD["cutoff"]) for b in bases]
+    dts = [torch.from_numpy(d[None]).cuda() for d in dens]
+    outs = [torch.empty_like(x) for x in dts]
+    for _ in range(args.warmup):
+        for fb, x, o in zip(singles, dts, outs):
+            fb.fock_jk_device(x, out=o)
+    torch.cuda.synchronize()
+    lat1 = []
+    t_single = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        for fb, x, o in zip(singles, dts, outs):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fb.fock_jk_device(x, out=o, stream=st)
+            e1.record(st)
+            e1.synchronize()
+            lat1.append(e0.elapsed_time(e1))
+    t_single = sum(lat1) / 1000.0
+    plain_rate = nmol * args.steps / t_single
+    f_single = [o.clone() for o in outs]
+    del singles
+    # --- batched context, tuned per class, replayed from its graph
+    bb = BatchFockBuilder(bases, cutoff=WORKLOAD["cutoff"])
+    dflat = bb.pack(dens)
+    d = torch.from_numpy(dflat[None]).cuda()
+    out = torch.empty_like(d)
+    tune = autotune.autotune(bb, d, "batch%d-%s-seed%d" % (nmol, WORKLOAD["basis"], WORKLOAD["seed"]), reps=1)
+
+    def replay(precision):
+        if precision == "fp64":
+            bb.set_precision("fp64")
+        else:
+            bb.set_precision(precision, args.mixed_threshold)
+        for _ in range(max(args.warmup, 2)):
+            bb.fock_jk_graph(d, out=out)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            bb.fock_jk_graph(d, out=out, stream=st)
+            e1.record(st)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        tsum = sum(times) / 1000.0
+        if ws > 1:
+            t = torch.tensor([tsum], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            tsum = float(t.item())
+        return tsum, times, out.clone(), bb.stats(), bb.graph_info()
+
+    t64, times64, f64, st64, gi64 = replay("fp64")
+    prec = args.precision if args.precision != "fp64" else "mixed-fast"
+    sampler = ClockSampler(local)
+    sampler.start()
+    wall0 = time.perf_counter()
+    tm, timesm, fm, stm, gim = replay(prec)
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    value = ws * nmol * args.steps / tm
+    # errors of the batched builds against the single FP64 builds, per molecule
+    f64n, fmn = f64.cpu().numpy()[0], fm.cpu().numpy()[0]
+    de_max, df_max, d64_max = 0.0, 0.0, 0.0
+    for m, bas in enumerate(bases):
+        o, n = bb.tri0[m], bas.nbf
+        t = n * (n + 1) // 2
+        ref = f_single[m].cpu().numpy()[0]
+        d64_max = max(d64_max, float(np.abs(f64n[o:o + t] - ref).max()))
+        dfm = fmn[o:o + t] - ref
+        df_max = max(df_max, float(np.abs(dfm).max()))
+        de_max = max(de_max, abs(0.5 * float(np.sum(unpack(dens[m], n) * unpack(dfm, n)))))
+    # e2e through the batch seam with host buffers (H2D + graph + D2H per step)
+    e2e = None
+    if not args.no_e2e:
+        import ctypes
+        from openqp_gb300._lib import lib, ptr, _i
+        from openqp_gb300.fock import _batch_arrays
+        nsh, nat, k = _batch_arrays(bases)
+        rc = lib().routec_fock_init_batch(nmol, ptr(nsh, _i), ptr(nat, _i), ptr(k[0], _i), ptr(k[1], _i),
+                                          ptr(k[2], _i), ptr(k[3]), ptr(k[4]), ptr(k[5], _i), ptr(k[6]),
+                                          WORKLOAD["cutoff"])
+        if rc != 0:
+            raise RuntimeError("routec_fock_init_batch returned %d" % rc)
+        lib().routec_fock_set_precision({"mixed": 1, "mixed-fast": 2}[prec], args.mixed_threshold)
+        fh = np.zeros_like(dflat)
+        info = ctypes.c_int(1)
+        nm, nf = ctypes.c_int(nmol), ctypes.c_int(1)
+        se, sc = ctypes.c_double(1.0), ctypes.c_double(1.0)
+        for _ in range(max(args.warmup, 2)):
+            lib().routec_fock_jk_batch(ptr(dflat), ptr(fh), ctypes.byref(nm), ctypes.byref(nf), ctypes.byref(se),
+                                       ctypes.byref(sc), ctypes.byref(info))
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            lib().routec_fock_jk_batch(ptr(dflat), ptr(fh), ctypes.byref(nm), ctypes.byref(nf), ctypes.byref(se),
+                                       ctypes.byref(sc), ctypes.byref(info))
+            if info.value != 0:
+                raise RuntimeError("routec_fock_jk_batch returned info=%d" % info.value)
+        e2e_t = time.perf_counter() - t0
+        lib().routec_fock_finalize()
+        e2e = {"value": ws * nmol * args.steps / e2e_t, "unit": "builds/s", "h2d_bytes_per_step": int(dflat.nbytes),
+               "d2h_bytes_per_step": int(dflat.nbytes)}
+    # roofline of the dominant class from a direct (event-timed) build in the same precision
+    bb.fock_jk_device(d, out=out)
+    s0 = bb.stats()
+    labels = class_labels()
+    ms = np.array(s0["ms_per_class"])
+    cdom = int(np.argmax(ms))
+    flops = class_flops(cdom, s0["prim_per_class"][cdom], s0["per_class"][cdom], nk=1, pure=False)
+    achieved = flops / (ms[cdom] * 1e-3) / 1e12
+    peak = fp64_peak_tflops()
+    if rank == 0:
+        line = {"metric": "J+K Fock builds/s (molecule builds, batched)", "value": value, "unit": "builds/s",
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tm / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (seeded water clusters, Loewdin random densities)",
+                "config": {"workload": WORKLOAD["name"], "nmol": nmol, "waters": {"min": min(sizes), "max": max(sizes),
+                           "mean": float(np.mean(sizes))}, "nbf_total": bb.nbf, "basis": WORKLOAD["basis"],
+                           "cutoff": WORKLOAD["cutoff"], "precision": prec, "mixed_threshold": args.mixed_threshold,
+                           "l2": "flushed (256 MB write) before every timed step",
+                           "parallelism": "replicas" if ws > 1 else "single GPU"},
+                "e2e": e2e,
+                "plain_fp64_unbatched": {"builds_per_s": plain_rate, "latency_ms_p50": pct(lat1, 50),
+                                         "latency_ms_p99": pct(lat1, 99)},
+                "batched_fp64_graph": {"builds_per_s": ws * nmol * args.steps / t64,
+                                       "replay_ms_p50": pct(times64, 50), "replay_ms_p99": pct(times64, 99),
+                                       "max_abs_dF_vs_single": d64_max},
+                "batched_mixed_graph": {"builds_per_s": value, "replay_ms_p50": pct(timesm, 50),
+                                        "replay_ms_p99": pct(timesm, 99), "max_abs_dF_vs_fp64": df_max,
+                                        "max_abs_dE2_Eh": de_max,
+                                        "f32_quartet_fraction": stm["f32_quartets"] / max(1, stm["quartets"])},
+                "speedup_vs_plain_fp64": value / plain_rate,
+                "per_molecule_latency_ms": {"p50": pct(timesm, 50), "p99": pct(timesm, 99),
+                                            "note": "every molecule of a batch completes with its graph replay"},
+                "roofline": {"bound": "fp64", "kernel": labels[cdom], "achieved": achieved, "peak": peak,
+                             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                             "peak_source": "measured: FP64 FMA-chain probe on this device",
+                             "kernel_ms": float(ms[cdom])},
+                "autotune": {"split_log2": tune["split_log2"], "chunk": tune["chunk"],
+                             "ctas_per_sm": tune["ctas_per_sm"], "class_ms_sum_tuned": float(sum(tune["class_ms"])),
+                             "class_ms_sum_default": float(sum(tune.get("default_class_ms", tune["class_ms"])))},
+                "gpu_launches": int(gim["kernels"]) * args.steps,
+                "graph": gim, "wall_s": wall, "clocks": clocks}
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline_batch(bases, dens, args.cpu_budget)
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline_batch(bases, dens, budget_s):
+    """The oracle (all host cores) building the clusters one by one, in order,
+    until the budget is spent; builds/s over the clusters it finished."""
+    from oracle import oracle
+    oracle.build()
+    cores = os.cpu_count()
+    t_all, done, nbf = 0.0, 0, 0
+    for bas, d in zip(bases, dens):
+        o = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"])
+        t0 = time.perf_counter()
+        q = o.schwarz(nthreads=cores)
+        o.fock_jk(d, nthreads=cores, schwarz=q)
+        t_all += time.perf_counter() - t0
+        done += 1
+        nbf += bas.nbf
+        if t_all > budget_s:
+            break
+    return dict(value=done / t_all, unit="builds/s", cores=cores, kind="port",
+                sample="oracle fock_jk (with its Schwarz set-up) on the first %d of %d clusters (%d bf in all)"
+                       % (done, len(bases), nbf))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -319,13 +550,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="water32_ccpvdz", choices=sorted(WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer seam timing (profiling runs)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed-fast"])
     ap.add_argument("--mixed-threshold", type=float, default=1e-6)
     args = ap.parse_args()
     WORKLOAD.clear()
     WORKLOAD.update(WORKLOADS[args.workload])
     if args.impl == "reference":
         run_reference(args)
+    elif "batch" in WORKLOAD:
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -60,6 +60,19 @@ void routec_fock_jk(const double* d, double* f, const int* nbf, const int* nfock
 void routec_fock_jk_inc(const double* dd, double* f, double* f_old, const int* nbf, const int* nfocks,
                         const double* se, const double* sc, int* info);
 
+/* Batched builds (many molecules in one build, one captured CUDA graph):
+ * register nmol molecules on the process-global context, then build all their
+ * Fock matrices in one call.  Arguments as oqpg_create_batch; d and f are the
+ * molecules' packed matrices one after the other (layout of oqpg_fock_jk on a
+ * batch context).  routec_fock_jk_batch checks *nmol against the registered
+ * batch.  No counterpart in the reference, which builds one molecule per
+ * fock_jk call. */
+int routec_fock_init_batch(int nmol, const int* nshell, const int* natom, const int* am, const int* ncontr,
+                           const int* origin, const double* ex, const double* cc, const int* harmonic,
+                           const double* xyz, double cutoff);
+void routec_fock_jk_batch(const double* d, double* f, const int* nmol, const int* nfocks, const double* se,
+                          const double* sc, int* info);
+
 /* Precision split of the following builds on the process-global context
  * (see oqpg_set_precision).  No counterpart in the reference seam. */
 int routec_fock_set_precision(int mode, double threshold);
@@ -77,7 +90,24 @@ int oqpg_create(oqpg_ctx** out, int nshell, const int* am, const int* ncontr, co
                 double cutoff);
 int oqpg_destroy(oqpg_ctx* ctx);
 
-/* Number of basis functions, shells and shell pairs of a context. */
+/* A context over a batch of nmol molecules built together: molecule m has
+ * nshell[m] shells on natom[m] atoms; am/ncontr/origin/harmonic, ex/cc and xyz
+ * are the molecules' arrays of routec_fock_init one after the other (origin
+ * 1-based within its molecule).  Every build of the context builds all
+ * molecules: its d and f hold, molecule after molecule, nfocks packed
+ * triangles of that molecule's nbf.  Shell quartets never mix molecules; the
+ * quartet lists of each class span the whole batch, so one class launch
+ * serves all molecules.  All molecules must agree on Cartesian or pure d. */
+int oqpg_create_batch(oqpg_ctx** out, int nmol, const int* nshell, const int* natom, const int* am,
+                      const int* ncontr, const int* origin, const double* ex, const double* cc, const int* harmonic,
+                      const double* xyz, double cutoff);
+
+/* Per molecule: nbf[m] and tri0[m], the offset of its packed block in units of
+ * nfocks triangle elements (its block starts at nfocks * tri0[m]).  Either
+ * pointer may be null.  Returns the number of molecules. */
+int oqpg_batch_info(const oqpg_ctx* ctx, int* nbf, long long* tri0);
+
+/* Number of basis functions of a context (summed over a batch). */
 int oqpg_nbf(const oqpg_ctx* ctx);
 
 /* Fock build from host buffers (H2D and D2H copies included). */
@@ -105,7 +135,34 @@ int oqpg_fock_jk_device(oqpg_ctx* ctx, const double* d_device, double* f_device,
 int oqpg_fock_jk_noalloc(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, double se,
                          double sc, void* stream);
 
-/* Schwarz bounds sqrt(max |(ab|ab)|) per shell pair, nshell x nshell (host). */
+/* The build of oqpg_fock_jk_device replayed from a CUDA graph.  The first
+ * call (and any call after a change of nfocks, se, sc, precision split or
+ * tuning) builds directly, then captures the whole device-driven build --
+ * density screening, quartet lists, primitive-count sort, every class kernel,
+ * finalize -- into one graph on the context's buffers, with list capacities
+ * sized from that density plus headroom.  Later calls copy d_device into the
+ * graph's input, replay it and copy its output to f_device, all on stream, then
+ * wait for the stream: when the density screens in more quartets than a list
+ * holds, the replay leaves its output alone, and the call builds directly and
+ * recaptures.  No counterpart in the reference. */
+int oqpg_fock_jk_graph(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, double se,
+                       double sc, void* stream);
+
+/* Graph captures and replays so far, and kernels in the captured graph. */
+int oqpg_graph_info(const oqpg_ctx* ctx, int* captures, int* replays, int* kernels);
+
+/* Per-class launch parameters, 21 entries each in the class order of
+ * oqpg_class_l (null: leave unchanged): split_log2 -- quartets of the <= 27
+ * element classes with >= 2^split_log2 primitive quartets run one warp per
+ * quartet (64: never); chunk -- quartets a warp takes per work grab in the
+ * thread-per-quartet kernels (multiple of 32); ctas_per_sm -- grid cap per SM
+ * (0: as many as fit).  The autotuner of the Python front end picks them.
+ * No counterpart in the reference. */
+int oqpg_set_tuning(oqpg_ctx* ctx, const int* split_log2, const int* chunk, const int* ctas_per_sm);
+int oqpg_get_tuning(const oqpg_ctx* ctx, int* split_log2, int* chunk, int* ctas_per_sm);
+
+/* Schwarz bounds sqrt(max |(ab|ab)|) per shell pair, nshell x nshell (host);
+ * single-molecule contexts only. */
 int oqpg_schwarz(const oqpg_ctx* ctx, double* q);
 
 /* Precision split of the following builds.  mode 0: every quartet in FP64

@@ -50,6 +50,17 @@ def lib():
         L.routec_fock_jk_inc.argtypes = [_d, _d, _d, _i, _i, _d, _d, _i]
         L.routec_fock_jk_inc.restype = None
         L.routec_fock_finalize.restype = None
+        L.oqpg_create_batch.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _i, _i, _i, _i, _i, _d, _d, _i,
+                                        _d, ctypes.c_double]
+        L.oqpg_batch_info.argtypes = [ctypes.c_void_p, _i, ctypes.POINTER(ctypes.c_longlong)]
+        L.oqpg_fock_jk_graph.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+        L.oqpg_graph_info.argtypes = [ctypes.c_void_p, _i, _i, _i]
+        L.oqpg_set_tuning.argtypes = [ctypes.c_void_p, _i, _i, _i]
+        L.oqpg_get_tuning.argtypes = [ctypes.c_void_p, _i, _i, _i]
+        L.routec_fock_init_batch.argtypes = [ctypes.c_int, _i, _i, _i, _i, _i, _d, _d, _i, _d, ctypes.c_double]
+        L.routec_fock_jk_batch.argtypes = [_d, _d, _i, _i, _d, _d, _i]
+        L.routec_fock_jk_batch.restype = None
         L.oqpg_one_electron.argtypes = [ctypes.c_int, _i, _i, _i, _d, _d, _i, ctypes.c_int, _d, _d, ctypes.c_int, _d]
         _lib = L
     return _lib

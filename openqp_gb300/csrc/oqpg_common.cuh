@@ -15,7 +15,8 @@ namespace oqpg {
 // Tables resident in device memory (one set per registered molecule).
 struct ShellDev {
   double x, y, z;
-  int am, nao, aoff, harm;
+  int am, nao, aoff, harm;  // aoff: first AO within the shell's molecule (matrix column)
+  int mrow;                 // first row of the shell's molecule in the stacked matrices
 };
 
 // One primitive pair of a shell pair (bra or ket), 80 bytes.
@@ -46,8 +47,10 @@ struct BuildArgs {
   const PrimPair* prims;
   const PrimPairF* primsf; // FP32 copy (precision-split builds)
   const uint2* quartets;   // (bra pair, ket pair) per quartet of this class
-  long long nquartets;
-  int nbf;
+  long long nquartets;     // quartets (or, with range, the capacity that sizes the grid)
+  const unsigned long long* range;  // optional device [begin, end) into quartets, read at kernel start
+  int nbf;                 // row stride of the stacked matrices (largest nbf of the batch)
+  size_t kstride;          // elements between the exchange densities / accumulators of one batch
   int nk;                  // number of exchange densities (1 RHF, 2 UHF/ROHF)
   double prim_cut;         // |K/p| pre-screen of a primitive pair
   double prim_cut2;        // (sp sq)^2 < prim_cut2 (p + q) skips a primitive quartet
@@ -64,6 +67,8 @@ struct BuildArgs {
   unsigned long long* counters;  // [0] primitive quartets evaluated by this launch
   unsigned long long* work;      // work-distribution counter of this launch (zeroed before it)
   int roots_f32;                 // FP32 quartets: evaluate Rys roots/weights in FP32 too
+  int chunk;                     // thread-per-quartet kernels: quartets per warp grab (multiple of 32)
+  int ctas_per_sm;               // launch: grid cap per SM (0: as many as fit)
 };
 
 // ---------------------------------------------------------------------------

@@ -328,6 +328,20 @@ __device__ __forceinline__ long long grab(unsigned long long* counter, unsigned 
   return (long long)__shfl_sync(0xffffffffu, base, 0);
 }
 
+// The quartets this launch works on: [0, nquartets) of a.quartets, or the
+// device-resident range [range[0], range[1]) when the launch was issued before
+// the list lengths were known (device-driven builds, graph replay).
+__device__ __forceinline__ void work_range(const BuildArgs& a, const uint2*& q, long long& n) {
+  if (a.range) {
+    const unsigned long long b = a.range[0], e = a.range[1];
+    q = a.quartets + b;
+    n = e > b ? (long long)(e - b) : 0;
+  } else {
+    q = a.quartets;
+    n = a.nquartets;
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void quartet_geometry(const BuildArgs& a, uint2 qd, PairDev& P, PairDev& Q, T AB[3],
                                                  T CD[3]) {
@@ -431,7 +445,9 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
   if (Q.sha == Q.shb) f *= 0.5;
   if (qd.x == qd.y) f *= 0.5;
   const int n = a.nbf;
+  // columns within the molecule, rows in the stacked matrices
   const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
+  const int ra = SA.mrow + oa, rb = SB.mrow + ob, rc = SC.mrow + oc;
   const T* djt = dj_of<T>(a);
   // Coulomb: G_J[ab] += 2f sum_cd V D_cd ; G_J[cd] += 2f sum_ab V D_ab
   {
@@ -439,11 +455,11 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
 #pragma unroll
     for (int i = 0; i < E::A; ++i)
 #pragma unroll
-      for (int j = 0; j < E::B; ++j) dab[i * E::B + j] = __ldg(djt + (size_t)(oa + i) * n + ob + j);
+      for (int j = 0; j < E::B; ++j) dab[i * E::B + j] = __ldg(djt + (size_t)(ra + i) * n + ob + j);
 #pragma unroll
     for (int i = 0; i < E::C; ++i)
 #pragma unroll
-      for (int j = 0; j < E::D; ++j) dcd[i * E::D + j] = __ldg(djt + (size_t)(oc + i) * n + od + j);
+      for (int j = 0; j < E::D; ++j) dcd[i * E::D + j] = __ldg(djt + (size_t)(rc + i) * n + od + j);
     T jab[E::A * E::B], jcd[E::C * E::D];
 #pragma unroll
     for (int i = 0; i < E::A * E::B; ++i) jab[i] = 0;
@@ -461,30 +477,30 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
 #pragma unroll
     for (int i = 0; i < E::A; ++i)
 #pragma unroll
-      for (int j = 0; j < E::B; ++j) atomicAdd(a.gj + (size_t)(oa + i) * n + ob + j, f2 * (double)jab[i * E::B + j]);
+      for (int j = 0; j < E::B; ++j) atomicAdd(a.gj + (size_t)(ra + i) * n + ob + j, f2 * (double)jab[i * E::B + j]);
 #pragma unroll
     for (int i = 0; i < E::C; ++i)
 #pragma unroll
-      for (int j = 0; j < E::D; ++j) atomicAdd(a.gj + (size_t)(oc + i) * n + od + j, f2 * (double)jcd[i * E::D + j]);
+      for (int j = 0; j < E::D; ++j) atomicAdd(a.gj + (size_t)(rc + i) * n + od + j, f2 * (double)jcd[i * E::D + j]);
   }
   // Exchange: G_K[ac] += f sum V D_bd ; [ad] += f V D_bc ; [bc] += f V D_ad ; [bd] += f V D_ac
   for (int kk = 0; kk < a.nk; ++kk) {
-    const T* dk = dk_of<T>(a) + (size_t)kk * n * n;
-    double* gk = a.gk + (size_t)kk * n * n;
+    const T* dk = dk_of<T>(a) + (size_t)kk * a.kstride;
+    double* gk = a.gk + (size_t)kk * a.kstride;
     T dac[E::A * E::C], dad[E::A * E::D], dbc[E::B * E::C], dbd[E::B * E::D];
 #pragma unroll
     for (int i = 0; i < E::A; ++i) {
 #pragma unroll
-      for (int j = 0; j < E::C; ++j) dac[i * E::C + j] = __ldg(dk + (size_t)(oa + i) * n + oc + j);
+      for (int j = 0; j < E::C; ++j) dac[i * E::C + j] = __ldg(dk + (size_t)(ra + i) * n + oc + j);
 #pragma unroll
-      for (int j = 0; j < E::D; ++j) dad[i * E::D + j] = __ldg(dk + (size_t)(oa + i) * n + od + j);
+      for (int j = 0; j < E::D; ++j) dad[i * E::D + j] = __ldg(dk + (size_t)(ra + i) * n + od + j);
     }
 #pragma unroll
     for (int i = 0; i < E::B; ++i) {
 #pragma unroll
-      for (int j = 0; j < E::C; ++j) dbc[i * E::C + j] = __ldg(dk + (size_t)(ob + i) * n + oc + j);
+      for (int j = 0; j < E::C; ++j) dbc[i * E::C + j] = __ldg(dk + (size_t)(rb + i) * n + oc + j);
 #pragma unroll
-      for (int j = 0; j < E::D; ++j) dbd[i * E::D + j] = __ldg(dk + (size_t)(ob + i) * n + od + j);
+      for (int j = 0; j < E::D; ++j) dbd[i * E::D + j] = __ldg(dk + (size_t)(rb + i) * n + od + j);
     }
     T kac[E::A * E::C], kad[E::A * E::D], kbc[E::B * E::C], kbd[E::B * E::D];
 #pragma unroll
@@ -512,33 +528,37 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
 #pragma unroll
     for (int i = 0; i < E::A; ++i) {
 #pragma unroll
-      for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(oa + i) * n + oc + j, f * (double)kac[i * E::C + j]);
+      for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(ra + i) * n + oc + j, f * (double)kac[i * E::C + j]);
 #pragma unroll
-      for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(oa + i) * n + od + j, f * (double)kad[i * E::D + j]);
+      for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(ra + i) * n + od + j, f * (double)kad[i * E::D + j]);
     }
 #pragma unroll
     for (int i = 0; i < E::B; ++i) {
 #pragma unroll
-      for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(ob + i) * n + oc + j, f * (double)kbc[i * E::C + j]);
+      for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(rb + i) * n + oc + j, f * (double)kbc[i * E::C + j]);
 #pragma unroll
-      for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(ob + i) * n + od + j, f * (double)kbd[i * E::D + j]);
+      for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(rb + i) * n + od + j, f * (double)kbd[i * E::D + j]);
     }
   }
 }
 
-// One thread per quartet; warps take chunks of 32 consecutive quartets of the
-// sorted list (similar primitive counts on all lanes).
+// One thread per quartet; warps take chunks of a.chunk (32 by default)
+// consecutive quartets of the sorted list (similar primitive counts on all lanes).
 template <int LA, int LB, int LC, int LD, bool PURE, bool SCH, typename T>
 __global__ void __launch_bounds__(128) k_small(const BuildArgs a) {
   constexpr int NE = Cls<LA, LB, LC, LD>::NE;
   const int lane = threadIdx.x & 31;
+  const uint2* quartets;
+  long long nquartets;
+  work_range(a, quartets, nquartets);
   unsigned long long nprim = 0;
+  const unsigned chunk = a.chunk >= 32 ? (unsigned)a.chunk : 32u;
   for (;;) {
-    const long long base = grab(a.work, 32u, lane);
-    if (base >= a.nquartets) break;
-    const long long t = base + lane;
-    if (t < a.nquartets) {
-      const uint2 qd = a.quartets[t];
+    const long long base = grab(a.work, chunk, lane);
+    if (base >= nquartets) break;
+    const long long end = base + chunk < nquartets ? base + chunk : nquartets;
+    for (long long t = base + lane; t < end; t += 32) {
+      const uint2 qd = quartets[t];
       PairDev P, Q;
       T AB[3], CD[3];
       quartet_geometry<T>(a, qd, P, Q, AB, CD);
@@ -558,11 +578,14 @@ template <int LA, int LB, int LC, int LD, bool PURE, typename T>
 __global__ void __launch_bounds__(128) k_prim(const BuildArgs a) {
   constexpr int NE = Cls<LA, LB, LC, LD>::NE;
   const int lane = threadIdx.x & 31;
+  const uint2* quartets;
+  long long nquartets;
+  work_range(a, quartets, nquartets);
   unsigned long long nprim = 0;
   for (;;) {
     const long long t = grab(a.work, 1u, lane);
-    if (t >= a.nquartets) break;
-    const uint2 qd = a.quartets[t];
+    if (t >= nquartets) break;
+    const uint2 qd = quartets[t];
     PairDev P, Q;
     T AB[3], CD[3];
     quartet_geometry<T>(a, qd, P, Q, AB, CD);
@@ -627,11 +650,14 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
     }
     offs[k] = o;
   }
+  const uint2* quartets;
+  long long nquartets;
+  work_range(a, quartets, nquartets);
   unsigned long long nprim = 0;
   for (;;) {
     const long long t = grab(a.work, 1u, lane);
-    if (t >= a.nquartets) break;
-    const uint2 qd = a.quartets[t];
+    if (t >= nquartets) break;
+    const uint2 qd = quartets[t];
     PairDev P, Q;
     T AB[3], CD[3];
     quartet_geometry<T>(a, qd, P, Q, AB, CD);
@@ -747,23 +773,24 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
     // density blocks
     const int n = a.nbf;
     const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
+    const int ra = SA.mrow + oa, rb = SB.mrow + ob, rc = SC.mrow + oc;
     const T* djt = dj_of<T>(a);
     T* Dab = W + NE;                 // after V (NE >= NEP)
     T* Dcd = Dab + E::A * E::B;
     T* Dk = Dcd + E::C * E::D;       // per k: ac, ad, bc, bd
     constexpr int DKS = SM::DK;
-    for (int i = lane; i < E::A * E::B; i += 32) Dab[i] = __ldg(djt + (size_t)(oa + i / E::B) * n + ob + i % E::B);
-    for (int i = lane; i < E::C * E::D; i += 32) Dcd[i] = __ldg(djt + (size_t)(oc + i / E::D) * n + od + i % E::D);
+    for (int i = lane; i < E::A * E::B; i += 32) Dab[i] = __ldg(djt + (size_t)(ra + i / E::B) * n + ob + i % E::B);
+    for (int i = lane; i < E::C * E::D; i += 32) Dcd[i] = __ldg(djt + (size_t)(rc + i / E::D) * n + od + i % E::D);
     for (int kk = 0; kk < a.nk; ++kk) {
-      const T* dk = dk_of<T>(a) + (size_t)kk * n * n;
+      const T* dk = dk_of<T>(a) + (size_t)kk * a.kstride;
       T* base = Dk + kk * DKS;
-      for (int i = lane; i < E::A * E::C; i += 32) base[i] = __ldg(dk + (size_t)(oa + i / E::C) * n + oc + i % E::C);
+      for (int i = lane; i < E::A * E::C; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::C) * n + oc + i % E::C);
       base += E::A * E::C;
-      for (int i = lane; i < E::A * E::D; i += 32) base[i] = __ldg(dk + (size_t)(oa + i / E::D) * n + od + i % E::D);
+      for (int i = lane; i < E::A * E::D; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::D) * n + od + i % E::D);
       base += E::A * E::D;
-      for (int i = lane; i < E::B * E::C; i += 32) base[i] = __ldg(dk + (size_t)(ob + i / E::C) * n + oc + i % E::C);
+      for (int i = lane; i < E::B * E::C; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::C) * n + oc + i % E::C);
       base += E::B * E::C;
-      for (int i = lane; i < E::B * E::D; i += 32) base[i] = __ldg(dk + (size_t)(ob + i / E::D) * n + od + i % E::D);
+      for (int i = lane; i < E::B * E::D; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::D) * n + od + i % E::D);
     }
     __syncwarp();
     double f = 1.0;
@@ -782,13 +809,13 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
         const T* v = V + (size_t)o * NCD;
 #pragma unroll 4
         for (int cd = 0; cd < NCD; ++cd) s = fma(v[cd], Dcd[cd], s);
-        dst = a.gj + (size_t)(oa + i) * n + ob + j;
+        dst = a.gj + (size_t)(ra + i) * n + ob + j;
         fac = 2.0 * f;
       } else if (o < NAB + NCD) {
         const int cd = o - NAB, k = cd / E::D, l = cd % E::D;
 #pragma unroll 4
         for (int ab = 0; ab < NAB; ++ab) s = fma(V[(size_t)ab * NCD + cd], Dab[ab], s);
-        dst = a.gj + (size_t)(oc + k) * n + od + l;
+        dst = a.gj + (size_t)(rc + k) * n + od + l;
         fac = 2.0 * f;
       } else {
         int r = o - NAB - NCD;
@@ -799,35 +826,35 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
         const T* dad = dac + NAC;
         const T* dbc = dad + NAD;
         const T* dbd = dbc + NBC;
-        double* gk = a.gk + (size_t)kk * n * n;
+        double* gk = a.gk + (size_t)kk * a.kstride;
         fac = f;
         if (r < NAC) {  // K[a][c] += sum_bd V[a b c d] D[b][d]
           const int i = r / E::C, k = r % E::C;
           for (int j = 0; j < E::B; ++j)
 #pragma unroll
             for (int l = 0; l < E::D; ++l) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dbd[j * E::D + l], s);
-          dst = gk + (size_t)(oa + i) * n + oc + k;
+          dst = gk + (size_t)(ra + i) * n + oc + k;
         } else if (r < NAC + NAD) {  // K[a][d] += sum_bc V D[b][c]
           r -= NAC;
           const int i = r / E::D, l = r % E::D;
           for (int j = 0; j < E::B; ++j)
 #pragma unroll
             for (int k = 0; k < E::C; ++k) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dbc[j * E::C + k], s);
-          dst = gk + (size_t)(oa + i) * n + od + l;
+          dst = gk + (size_t)(ra + i) * n + od + l;
         } else if (r < NAC + NAD + NBC) {  // K[b][c] += sum_ad V D[a][d]
           r -= NAC + NAD;
           const int j = r / E::C, k = r % E::C;
           for (int i = 0; i < E::A; ++i)
 #pragma unroll
             for (int l = 0; l < E::D; ++l) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dad[i * E::D + l], s);
-          dst = gk + (size_t)(ob + j) * n + oc + k;
+          dst = gk + (size_t)(rb + j) * n + oc + k;
         } else {  // K[b][d] += sum_ac V D[a][c]
           r -= NAC + NAD + NBC;
           const int j = r / E::D, l = r % E::D;
           for (int i = 0; i < E::A; ++i)
 #pragma unroll
             for (int k = 0; k < E::C; ++k) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dac[i * E::C + k], s);
-          dst = gk + (size_t)(ob + j) * n + od + l;
+          dst = gk + (size_t)(rb + j) * n + od + l;
         }
       }
       atomicAdd(dst, fac * (double)s);

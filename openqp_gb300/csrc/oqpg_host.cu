@@ -44,18 +44,29 @@ cudaError_t launch_class(int c, bool pure, int mode, const BuildArgs& a, int nsm
 
 __device__ __forceinline__ int d_class_index(int tb, int tk) { return tb * 6 - tb * (tb - 1) / 2 + (tk - tb); }
 
-// Packed D -> full symmetric Coulomb density (Da + Db) and exchange densities.
-__global__ void k_unpack(const double* __restrict__ dp, int nfocks, int nbf, double* dj, double* dk) {
-  const long long n2 = (long long)nbf * nbf;
-  const long long ntri = (long long)nbf * (nbf + 1) / 2;
+// Packed D -> full symmetric Coulomb density (Da + Db) and exchange densities,
+// every molecule of the batch into its rows of the stacked matrices (columns
+// beyond a molecule's nbf are zeroed).
+__global__ void k_unpack(const double* __restrict__ dp, int nfocks, const MolDev* __restrict__ mols,
+                         const int* __restrict__ row_mol, int nrows, int stride, double* dj, double* dk) {
+  const long long n2 = (long long)nrows * stride;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n2; t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t / nbf), j = (int)(t % nbf);
+    const int r = (int)(t / stride), j = (int)(t % stride);
+    const MolDev m = mols[row_mol[r]];
+    const int i = r - m.row0;
+    if (j >= m.nbf) {
+      dj[t] = 0.0;
+      if (nfocks == 2) { dk[t] = 0.0; dk[n2 + t] = 0.0; }
+      continue;
+    }
     const int hi = i > j ? i : j, lo = i > j ? j : i;
+    const long long ntri = (long long)m.nbf * (m.nbf + 1) / 2;
+    const double* d = dp + nfocks * m.tri0;
     const long long p = (long long)hi * (hi + 1) / 2 + lo;
     if (nfocks == 1) {
-      dj[t] = dp[p];
+      dj[t] = d[p];
     } else {
-      const double a = dp[p], b = dp[ntri + p];
+      const double a = d[p], b = d[ntri + p];
       dj[t] = a + b;
       dk[t] = a;
       dk[n2 + t] = b;
@@ -69,31 +80,32 @@ __global__ void k_to_f32(const double* __restrict__ x, long long n, float* y) {
 }
 
 // shlden (OpenQP int2.F90:999-1047): max |D| over each shell-pair block and
-// over the densities; also the global maximum (max_den).
-__global__ void k_dsh(const double* __restrict__ dp, int nfocks, int nbf, int ns, const int* __restrict__ aoff,
-                      const int* __restrict__ nao, double* dsh, float* dshf, unsigned long long* dmax_bits) {
-  const long long npair = (long long)ns * (ns + 1) / 2;
-  const long long ntri = (long long)nbf * (nbf + 1) / 2;
+// over the densities; also each molecule's maximum (max_den).
+__global__ void k_dsh(const double* __restrict__ dp, int nfocks, const MolDev* __restrict__ mols,
+                      const int* __restrict__ pair_mol, const int2* __restrict__ pair_ij, int npair,
+                      const int* __restrict__ aoff, const int* __restrict__ nao, double* dsh, float* dshf,
+                      unsigned long long* dmax_bits) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npair; t += (long long)gridDim.x * blockDim.x) {
-    int si = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while ((long long)si * (si + 1) / 2 > t) --si;
-    while ((long long)(si + 1) * (si + 2) / 2 <= t) ++si;
-    const int sj = (int)(t - (long long)si * (si + 1) / 2);
+    const int mi = pair_mol[t];
+    const MolDev M = mols[mi];
+    const int2 ij = pair_ij[t];
+    const int si = ij.x, sj = ij.y;
+    const long long ntri = (long long)M.nbf * (M.nbf + 1) / 2;
     double m = 0.0;
-    const int i0 = aoff[si], i1 = i0 + nao[si], j0 = aoff[sj];
-    int j1 = j0 + nao[sj];
+    const int i0 = aoff[M.shell0 + si], i1 = i0 + nao[M.shell0 + si], j0 = aoff[M.shell0 + sj];
+    const int j1 = j0 + nao[M.shell0 + sj];
     for (int f = 0; f < nfocks; ++f) {
-      const double* d = dp + f * ntri;
+      const double* d = dp + nfocks * M.tri0 + f * ntri;
       for (int i = i0; i < i1; ++i) {
         const int je = (si == sj) ? i + 1 : j1;
         for (int j = j0; j < je; ++j) m = fmax(m, fabs(d[(long long)i * (i + 1) / 2 + j]));
       }
     }
-    dsh[(long long)si * ns + sj] = m;
-    dsh[(long long)sj * ns + si] = m;
-    dshf[(long long)si * ns + sj] = (float)m;
-    dshf[(long long)sj * ns + si] = (float)m;
-    atomicMax(dmax_bits, (unsigned long long)__double_as_longlong(m));
+    dsh[M.dsh0 + (long long)si * M.ns + sj] = m;
+    dsh[M.dsh0 + (long long)sj * M.ns + si] = m;
+    dshf[M.dsh0 + (long long)si * M.ns + sj] = (float)m;
+    dshf[M.dsh0 + (long long)sj * M.ns + si] = (float)m;
+    atomicMax(dmax_bits + mi, (unsigned long long)__double_as_longlong(m));
   }
 }
 
@@ -112,27 +124,34 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
   __shared__ unsigned long long base[2 * NCLASS];
   __shared__ int s_len;
   const int P = blockIdx.x;
-  const double dmax = __longlong_as_double((long long)*a.dmax_bits);
+  const int mi = a.pair_mol[P];
+  const MolDev M = a.mols[mi];
+  const double dmax = __longlong_as_double((long long)a.dmax_bits[mi]);
   const double qP = a.q[P];
   if (qP * dmax < a.tau) return;
+  const int* sorted_idx = a.sorted_idx + M.pair0;
   if (threadIdx.x == 0) {
-    // number of pairs with q >= thr (q descending), with a rounding margin
+    // number of the molecule's pairs with q >= thr (q descending), with a rounding margin
     const double thr = a.tau / (4.0 * qP * dmax) * (1.0 - 1e-9);
-    int lo = 0, hi = a.npair;
+    const double* sq = a.sorted_q + M.pair0;
+    int lo = 0, hi = M.npair;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
-      if (a.sorted_q[mid] >= thr) lo = mid + 1;
+      if (sq[mid] >= thr) lo = mid + 1;
       else hi = mid;
     }
     s_len = lo;
   }
   __syncthreads();
   const int len = s_len;
+  const int ns = M.ns;
+  const float* dshf = a.dshf + M.dsh0;
+  const double* dshd = a.dsh + M.dsh0;
   const int2 ij = a.pair_ij[P];
   const int tP = a.pair_type[P];
   const float qPf = a.qf[P];
-  const float* di = a.dshf + (long long)ij.x * a.ns;
-  const float* dj = a.dshf + (long long)ij.y * a.ns;
+  const float* di = dshf + (long long)ij.x * ns;
+  const float* dj = dshf + (long long)ij.y * ns;
   const float dij4 = 4.0f * di[ij.y];
   const float tlo = (float)(a.tau * (1.0 - 1e-5)), thi = (float)(a.tau * (1.0 + 1e-5));
   const float mlo = (float)(a.tau_f32 * (1.0 - 1e-5)), mhi = (float)(a.tau_f32 * (1.0 + 1e-5));
@@ -140,21 +159,21 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
     if (threadIdx.x < 2 * NCLASS) cnt[threadIdx.x] = 0;
     __syncthreads();
     const int s = s0 + threadIdx.x;
-    const int Q = s < len ? a.sorted_idx[s] : a.npair;
+    const int Q = s < len ? sorted_idx[s] : 0x7fffffff;
     int c = -1;
     unsigned slot = 0;
     uint2 ent;
     if (Q <= P) {
       const int2 kl = a.pair_ij[Q];
-      const float m = fmaxf(fmaxf(fmaxf(dij4, 4.0f * a.dshf[(long long)kl.x * a.ns + kl.y]), fmaxf(dj[kl.y], dj[kl.x])),
+      const float m = fmaxf(fmaxf(fmaxf(dij4, 4.0f * dshf[(long long)kl.x * ns + kl.y]), fmaxf(dj[kl.y], dj[kl.x])),
                             fmaxf(di[kl.y], di[kl.x]));
       const float tf = qPf * a.qf[Q] * m;
       double t = -1.0;  // exact test value, computed only near a threshold
       auto exact = [&]() {
-        const double* Di = a.dsh + (long long)ij.x * a.ns;
-        const double* Dj = a.dsh + (long long)ij.y * a.ns;
+        const double* Di = dshd + (long long)ij.x * ns;
+        const double* Dj = dshd + (long long)ij.y * ns;
         double v = qP * a.q[Q];
-        v *= fmax(fmax(fmax(4.0 * Di[ij.y], 4.0 * a.dsh[(long long)kl.x * a.ns + kl.y]), fmax(Dj[kl.y], Dj[kl.x])),
+        v *= fmax(fmax(fmax(4.0 * Di[ij.y], 4.0 * dshd[(long long)kl.x * ns + kl.y]), fmax(Dj[kl.y], Dj[kl.x])),
                   fmax(Di[kl.y], Di[kl.x]));
         return v;
       };
@@ -205,9 +224,16 @@ __device__ __forceinline__ int prim_bin(const PairDev* pairs, uint2 q) {
   return NBIN - 1 - (k < NBIN - 1 ? k : NBIN - 1);
 }
 
-__global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const PairDev* __restrict__ pairs,
-                           unsigned long long* hist) {
+__device__ __forceinline__ long long list_len(long long n, const unsigned long long* n_dev) {
+  if (!n_dev) return n;
+  const unsigned long long c = *n_dev;
+  return c < (unsigned long long)n ? (long long)c : n;
+}
+
+__global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const unsigned long long* n_dev,
+                           const PairDev* __restrict__ pairs, unsigned long long* hist) {
   __shared__ unsigned h[NBIN];
+  n = list_len(n, n_dev);
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x) h[i] = 0;
   __syncthreads();
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
@@ -220,11 +246,15 @@ __global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const Pa
 // Each CTA takes a contiguous chunk, reserves its per-bin ranges once, then
 // places its entries.
 __global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ list, long long n,
+                                                     const unsigned long long* n_dev,
                                                      const PairDev* __restrict__ pairs, unsigned long long* cursors,
-                                                     uint2* out, long long chunk) {
+                                                     uint2* out, long long chunk, const unsigned* flag) {
   __shared__ unsigned h[NBIN];
   __shared__ unsigned long long b[NBIN];
+  if (flag && *flag) return;  // a list overflowed: the cursors were not written
+  n = list_len(n, n_dev);
   const long long lo = blockIdx.x * chunk;
+  if (lo >= n) return;
   const long long hi = lo + chunk < n ? lo + chunk : n;
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x) h[i] = 0;
   __syncthreads();
@@ -243,25 +273,82 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ l
   }
 }
 
-// F = sc (GJ + GJ^T) - cK (GK + GK^T) on the packed lower triangle (+ F_old).
-__global__ void k_finalize(const double* __restrict__ gj, const double* __restrict__ gk, int nk, int nbf, double sc,
-                           double ck, double* f, double* f_old) {
-  const long long ntri = (long long)nbf * (nbf + 1) / 2;
-  const long long n2 = (long long)nbf * nbf;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ntri; t += (long long)gridDim.x * blockDim.x) {
-    int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while ((long long)i * (i + 1) / 2 > t) --i;
-    while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
-    const int j = (int)(t - (long long)i * (i + 1) / 2);
-    const double J = gj[(long long)i * nbf + j] + gj[(long long)j * nbf + i];
+// Device-side bookkeeping of a device-driven build, one thread per list (one
+// CTA of 64 threads): the exclusive scan of its bin counts (scatter cursors)
+// and the two work ranges of the sorted list, [0, head) for the
+// primitive-parallel kernel and [head, count) for the class kernel, head = the
+// entries in the bins of >= 2^split primitive quartets (split_bins[list] bins;
+// 0 for none).  If any list's count exceeded its capacity, overflow is set
+// and every range is empty: the scatter and the class kernels then do
+// nothing and the build is redone by the host.
+__global__ void k_bin_scan(const unsigned long long* counts, const unsigned long long* caps, const int* split_bins,
+                           const unsigned long long* hist, unsigned long long* cursors, unsigned long long* ranges,
+                           unsigned* overflow) {
+  __shared__ unsigned s_over;
+  const int li = threadIdx.x;
+  if (li == 0) s_over = 0;
+  __syncthreads();
+  const bool mine = li < NLIST;
+  const unsigned long long cnt = mine ? counts[li] : 0ull;
+  if (mine && cnt > caps[li]) atomicOr(&s_over, 1u);
+  __syncthreads();
+  if (!mine) return;
+  unsigned long long* rg = ranges + 4 * li;
+  if (s_over) {
+    rg[0] = rg[1] = rg[2] = rg[3] = 0;
+    if (li == 0) atomicOr(overflow, 1u);
+    return;
+  }
+  unsigned long long s = 0, head = 0;
+  const int nb = split_bins[li];
+  for (int b = 0; b < NBIN; ++b) {
+    cursors[li * NBIN + b] = s;
+    s += hist[li * NBIN + b];
+    if (b < nb) head = s;
+  }
+  if (s != cnt) {  // bookkeeping disagrees with the list: run nothing from it
+    atomicOr(overflow, 2u);
+    rg[0] = rg[1] = rg[2] = rg[3] = 0;
+    return;
+  }
+  rg[0] = 0; rg[1] = head; rg[2] = head; rg[3] = cnt;
+}
+
+// F = sc (GJ + GJ^T) - cK (GK + GK^T) on the packed lower triangles of every
+// molecule (+ F_old), molecule-major [molecule][density][triangle].  Skipped
+// when a list of this build overflowed (flag set), so that f and f_old stay
+// as they were for the rebuild.
+__global__ void k_finalize(const double* __restrict__ gj, const double* __restrict__ gk, int nk,
+                           const MolDev* __restrict__ mols, int nmol, long long ntri_total, int stride,
+                           size_t kstride, double sc, double ck, double* f, double* f_old,
+                           const unsigned* __restrict__ flag) {
+  if (flag && *flag) return;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ntri_total;
+       t += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nmol - 1;  // last molecule with tri0 <= t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (mols[mid].tri0 <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const MolDev M = mols[lo];
+    const long long u = t - M.tri0;
+    const long long ntri = (long long)M.nbf * (M.nbf + 1) / 2;
+    int i = (int)((sqrt(8.0 * (double)u + 1.0) - 1.0) * 0.5);
+    while ((long long)i * (i + 1) / 2 > u) --i;
+    while ((long long)(i + 1) * (i + 2) / 2 <= u) ++i;
+    const int j = (int)(u - (long long)i * (i + 1) / 2);
+    const long long ij = (long long)(M.row0 + i) * stride + j, ji = (long long)(M.row0 + j) * stride + i;
+    const double J = gj[ij] + gj[ji];
+    const long long ob = nk * M.tri0 + u;
     for (int k = 0; k < nk; ++k) {
-      const double* g = gk + k * n2;
-      double v = sc * J - ck * (g[(long long)i * nbf + j] + g[(long long)j * nbf + i]);
+      const double* g = gk + k * kstride;
+      double v = sc * J - ck * (g[ij] + g[ji]);
       if (f_old) {
-        v += f_old[k * ntri + t];
-        f_old[k * ntri + t] = v;
+        v += f_old[ob + k * ntri];
+        f_old[ob + k * ntri] = v;
       }
-      f[k * ntri + t] = v;
+      f[ob + k * ntri] = v;
     }
   }
 }
@@ -295,52 +382,58 @@ int to_status(cudaError_t e) {
 struct HostPairs {
   std::vector<PairDev> pairs;
   std::vector<PrimPair> prims;
-  std::vector<int2> ij;
+  std::vector<int2> ij;    // molecule-local shells of each pair
   std::vector<int> type;
+  std::vector<int> mol;
 };
 
 // OpenQP's int2_prepare_pair (int2_pairs.F90:179-266) with the rotated-axis
 // pre-screen |K/p| >= quartet cutoff (int_rotaxis.F90:292-306) applied once.
+// Pairs are numbered molecule by molecule, canonical (i >= j) within each.
 void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vector<int>& ncontr,
                  const std::vector<int>& poff, const double* ex, const double* cc, double qcut, double ecut,
                  HostPairs& out) {
   const double sqrtpito52 = std::sqrt(2.0) * std::pow(3.14159265358979323846, 1.25);
-  out.pairs.clear(); out.prims.clear(); out.ij.clear(); out.type.clear();
-  for (int i = 0; i < c.nshell; ++i)
-    for (int j = 0; j <= i; ++j) {
-      int sa = i, sb = j;
-      if (am[sa] > am[sb]) std::swap(sa, sb);
-      const ShellDev& A = c.shells[sa];
-      const ShellDev& B = c.shells[sb];
-      const double ab2 = (A.x - B.x) * (A.x - B.x) + (A.y - B.y) * (A.y - B.y) + (A.z - B.z) * (A.z - B.z);
-      PairDev pd;
-      pd.sha = sa; pd.shb = sb; pd.poff = (int)out.prims.size();
-      for (int p1 = 0; p1 < ncontr[sa]; ++p1)
-        for (int p2 = 0; p2 < ncontr[sb]; ++p2) {
-          const double a1 = ex[poff[sa] + p1], a2 = ex[poff[sb] + p2];
-          const double g = a1 + a2;
-          double e12 = a1 * a2 * ab2;
-          if (e12 > g * ecut) continue;
-          const double gi = 1.0 / g;
-          e12 *= gi;
-          const double k1 = cc[poff[sa] + p1] * cc[poff[sb] + p2] * std::exp(-e12);
-          if (std::fabs(k1) < qcut) continue;
-          const double sp = sqrtpito52 * k1 * gi;
-          if (std::fabs(sp) < qcut) continue;
-          PrimPair pp;
-          pp.p = g; pp.hp = 0.5 * gi;
-          pp.px = (a1 * A.x + a2 * B.x) * gi;
-          pp.py = (a1 * A.y + a2 * B.y) * gi;
-          pp.pz = (a1 * A.z + a2 * B.z) * gi;
-          pp.ax = pp.px - A.x; pp.ay = pp.py - A.y; pp.az = pp.pz - A.z;
-          pp.sp = sp; pp.spf = (float)sp; pp.pf = (float)g;
-          out.prims.push_back(pp);
-        }
-      pd.pcnt = (int)out.prims.size() - pd.poff;
-      out.pairs.push_back(pd);
-      out.ij.push_back(make_int2(i, j));
-      out.type.push_back(pair_type(am[sa], am[sb]));
-    }
+  out.pairs.clear(); out.prims.clear(); out.ij.clear(); out.type.clear(); out.mol.clear();
+  for (int m = 0; m < c.nmol; ++m) {
+    const MolDev& M = c.mols[m];
+    for (int li = 0; li < M.ns; ++li)
+      for (int lj = 0; lj <= li; ++lj) {
+        int sa = M.shell0 + li, sb = M.shell0 + lj;
+        if (am[sa] > am[sb]) std::swap(sa, sb);
+        const ShellDev& A = c.shells[sa];
+        const ShellDev& B = c.shells[sb];
+        const double ab2 = (A.x - B.x) * (A.x - B.x) + (A.y - B.y) * (A.y - B.y) + (A.z - B.z) * (A.z - B.z);
+        PairDev pd;
+        pd.sha = sa; pd.shb = sb; pd.poff = (int)out.prims.size();
+        for (int p1 = 0; p1 < ncontr[sa]; ++p1)
+          for (int p2 = 0; p2 < ncontr[sb]; ++p2) {
+            const double a1 = ex[poff[sa] + p1], a2 = ex[poff[sb] + p2];
+            const double g = a1 + a2;
+            double e12 = a1 * a2 * ab2;
+            if (e12 > g * ecut) continue;
+            const double gi = 1.0 / g;
+            e12 *= gi;
+            const double k1 = cc[poff[sa] + p1] * cc[poff[sb] + p2] * std::exp(-e12);
+            if (std::fabs(k1) < qcut) continue;
+            const double sp = sqrtpito52 * k1 * gi;
+            if (std::fabs(sp) < qcut) continue;
+            PrimPair pp;
+            pp.p = g; pp.hp = 0.5 * gi;
+            pp.px = (a1 * A.x + a2 * B.x) * gi;
+            pp.py = (a1 * A.y + a2 * B.y) * gi;
+            pp.pz = (a1 * A.z + a2 * B.z) * gi;
+            pp.ax = pp.px - A.x; pp.ay = pp.py - A.y; pp.az = pp.pz - A.z;
+            pp.sp = sp; pp.spf = (float)sp; pp.pf = (float)g;
+            out.prims.push_back(pp);
+          }
+        pd.pcnt = (int)out.prims.size() - pd.poff;
+        out.pairs.push_back(pd);
+        out.ij.push_back(make_int2(li, lj));
+        out.type.push_back(pair_type(am[sa], am[sb]));
+        out.mol.push_back(m);
+      }
+  }
 }
 
 }  // namespace
@@ -368,32 +461,74 @@ int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
   return OK;
 }
 
-int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const int* origin, const double* ex,
-             const double* cc, const int* harmonic, int natom, const double* xyz, double cutoff) {
-  if (nshell <= 0 || natom <= 0 || !am_ || !ncontr_ || !origin || !ex || !cc || !xyz) return UNSUPPORTED;
+void default_tuning(oqpg_tuning& t) {
+  for (int k = 0; k < NCLASS; ++k) {
+    t.split_log2[k] = PRIM_SPLIT_LOG2;
+    t.chunk[k] = 32;
+    t.ctas_per_sm[k] = 0;
+  }
+}
+
+// A batch of nmol molecules: nshell_m[m] shells on natom_m[m] atoms each, the
+// shell and atom arrays concatenated molecule by molecule (origin 1-based
+// within the molecule).  One molecule is the batch of one.
+int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, const int* am_, const int* ncontr_,
+             const int* origin, const double* ex, const double* cc, const int* harmonic, const double* xyz,
+             double cutoff) {
+  if (nmol <= 0 || !nshell_m || !natom_m || !am_ || !ncontr_ || !origin || !ex || !cc || !xyz) return UNSUPPORTED;
+  int nshell = 0, natom = 0;
+  for (int m = 0; m < nmol; ++m) {
+    if (nshell_m[m] <= 0 || natom_m[m] <= 0) return UNSUPPORTED;
+    nshell += nshell_m[m];
+    natom += natom_m[m];
+  }
   std::vector<int> am(am_, am_ + nshell), ncontr(ncontr_, ncontr_ + nshell), poff(nshell);
-  int npure = 0, nd = 0, off = 0, aoff = 0;
-  c->nshell = nshell; c->natom = natom; c->tau = cutoff;
-  c->shells.resize(nshell); c->aoff.resize(nshell); c->naos.resize(nshell);
-  for (int s = 0; s < nshell; ++s) {
-    if (am[s] < 0 || am[s] > 2 || ncontr[s] <= 0 || origin[s] < 1 || origin[s] > natom) return UNSUPPORTED;
-    if (am[s] == 2) { ++nd; if (harmonic && harmonic[s]) ++npure; }
-    poff[s] = off; off += ncontr[s];
+  int npure = 0, nd = 0, off = 0;
+  c->nmol = nmol; c->nshell = nshell; c->natom = natom; c->tau = cutoff;
+  default_tuning(c->tune);
+  c->shells.resize(nshell); c->aoff.resize(nshell); c->naos.resize(nshell); c->mols.resize(nmol);
+  {
+    int s = 0;
+    for (int m = 0; m < nmol; ++m)
+      for (int k = 0; k < nshell_m[m]; ++k, ++s) {
+        if (am[s] < 0 || am[s] > 2 || ncontr[s] <= 0 || origin[s] < 1 || origin[s] > natom_m[m]) return UNSUPPORTED;
+        if (am[s] == 2) { ++nd; if (harmonic && harmonic[s]) ++npure; }
+        poff[s] = off; off += ncontr[s];
+      }
   }
   if (npure != 0 && npure != nd) return UNSUPPORTED;  // mixed Cartesian / pure d shells
   c->pure = nd > 0 && npure == nd;
-  for (int s = 0; s < nshell; ++s) {
-    ShellDev& S = c->shells[s];
-    const int at = origin[s] - 1;
-    S.x = xyz[3 * at]; S.y = xyz[3 * at + 1]; S.z = xyz[3 * at + 2];
-    S.am = am[s]; S.harm = (c->pure && am[s] == 2) ? 1 : 0;
-    S.nao = (S.harm ? 5 : ncart(am[s]));
-    S.aoff = aoff;
-    c->aoff[s] = aoff; c->naos[s] = S.nao;
-    aoff += S.nao;
+  int s = 0, atom0 = 0, row0 = 0, pair0 = 0, stride = 0;
+  long long tri0 = 0, dsh0 = 0;
+  std::vector<int> row_mol;
+  for (int m = 0; m < nmol; ++m) {
+    MolDev& M = c->mols[m];
+    M.shell0 = s; M.ns = nshell_m[m]; M.row0 = row0; M.pair0 = pair0;
+    M.npair = M.ns * (M.ns + 1) / 2;
+    int aoff = 0;
+    for (int k = 0; k < M.ns; ++k, ++s) {
+      ShellDev& S = c->shells[s];
+      const int at = atom0 + origin[s] - 1;
+      S.x = xyz[3 * at]; S.y = xyz[3 * at + 1]; S.z = xyz[3 * at + 2];
+      S.am = am[s]; S.harm = (c->pure && am[s] == 2) ? 1 : 0;
+      S.nao = (S.harm ? 5 : ncart(am[s]));
+      S.aoff = aoff;
+      S.mrow = row0;
+      c->aoff[s] = aoff; c->naos[s] = S.nao;
+      aoff += S.nao;
+    }
+    M.nbf = aoff;
+    M.tri0 = tri0;
+    M.dsh0 = dsh0;
+    for (int r = 0; r < M.nbf; ++r) row_mol.push_back(m);
+    tri0 += (long long)M.nbf * (M.nbf + 1) / 2;
+    dsh0 += (long long)M.ns * M.ns;
+    row0 += M.nbf;
+    pair0 += M.npair;
+    atom0 += natom_m[m];
+    stride = std::max(stride, M.nbf);
   }
-  c->nbf = aoff;
-  c->npair = nshell * (nshell + 1) / 2;
+  c->nbf = row0; c->stride = stride; c->ntri = tri0; c->dsh_elems = dsh0; c->npair = pair0;
   CK(cudaGetDevice(&c->dev));
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->dev));
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
@@ -404,6 +539,8 @@ int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const 
   if ((rc = upload(c->d_shells, c->shells, st))) return rc;
   if ((rc = upload(c->d_aoff, c->aoff, st))) return rc;
   if ((rc = upload(c->d_naos, c->naos, st))) return rc;
+  if ((rc = upload(c->d_mols, c->mols, st))) return rc;
+  if ((rc = upload(c->d_row_mol, row_mol, st))) return rc;
 
   // --- Schwarz bounds with OpenQP's very tight cutoffs (int2.F90:1600-1604)
   HostPairs sp;
@@ -415,8 +552,9 @@ int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const 
     if (sp.pairs[p].pcnt == 0) continue;
     diag[class_index(sp.type[p], sp.type[p])].push_back(make_uint2(p, p));
   }
-  DevBuf d_diag, d_q;
+  DevBuf d_diag, d_q, d_w;
   CK(d_q.ensure(sizeof(double) * c->npair));
+  CK(d_w.ensure(sizeof(unsigned long long)));
   CK(cudaMemsetAsync(d_q.p, 0, sizeof(double) * c->npair, st));
   for (int cl = 0; cl < NCLASS; ++cl) {
     if (diag[cl].empty()) continue;
@@ -427,14 +565,14 @@ int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const 
     a.prims = c->d_prims.as<PrimPair>();
     a.quartets = d_diag.as<uint2>();
     a.nquartets = (long long)diag[cl].size();
-    a.nbf = c->nbf;
+    a.nbf = c->stride;
+    a.kstride = (size_t)c->nbf * c->stride;
     a.prim_cut = 1e-17;
     a.prim_cut2 = 1e-34;
     set_band(a);
     a.schwarz_out = d_q.as<double>();
-    CK(c->d_work.ensure(sizeof(unsigned long long) * 2 * NCLASS));
-    CK(cudaMemsetAsync(c->d_work.p, 0, sizeof(unsigned long long), st));
-    a.work = c->d_work.as<unsigned long long>();
+    CK(cudaMemsetAsync(d_w.p, 0, sizeof(unsigned long long), st));
+    a.work = d_w.as<unsigned long long>();
     CK(launch_class(cl, c->pure, MODE_SCHWARZ, a, c->nsm, st));
     CK(cudaStreamSynchronize(st));  // d_diag is reused by the next class
   }
@@ -443,6 +581,7 @@ int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const 
   CK(cudaStreamSynchronize(st));
   d_diag.release();
   d_q.release();
+  d_w.release();
 
   // --- pair tables of the Fock build (cutoffs 1e-2 tau, 1e-4 tau, 25 ln 10; int2.F90:260-272)
   HostPairs fp;
@@ -451,21 +590,24 @@ int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const 
   if ((rc = upload(c->d_prims, fp.prims, st))) return rc;
   std::vector<PrimPairF> pf(fp.prims.size());
   for (size_t i = 0; i < pf.size(); ++i) {
-    const PrimPair& s = fp.prims[i];
-    pf[i] = PrimPairF{(float)s.p, (float)s.hp, (float)s.px, (float)s.py, (float)s.pz,
-                      (float)s.ax, (float)s.ay, (float)s.az, (float)s.sp, 0.0f};
+    const PrimPair& q = fp.prims[i];
+    pf[i] = PrimPairF{(float)q.p, (float)q.hp, (float)q.px, (float)q.py, (float)q.pz,
+                      (float)q.ax, (float)q.ay, (float)q.az, (float)q.sp, 0.0f};
   }
   if ((rc = upload(c->d_primsf, pf, st))) return rc;
   if ((rc = upload(c->d_pair_ij, fp.ij, st))) return rc;
   if ((rc = upload(c->d_pair_type, fp.type, st))) return rc;
+  if ((rc = upload(c->d_pair_mol, fp.mol, st))) return rc;
   if ((rc = upload(c->d_q, c->schwarz_pair, st))) return rc;
   std::vector<float> qf(c->npair);
   for (int p = 0; p < c->npair; ++p) qf[p] = (float)c->schwarz_pair[p];
   if ((rc = upload(c->d_qf, qf, st))) return rc;
+  // each molecule's pairs by descending Schwarz bound (global pair indices)
   std::vector<int> order(c->npair);
   for (int p = 0; p < c->npair; ++p) order[p] = p;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int x, int y) { return c->schwarz_pair[x] > c->schwarz_pair[y]; });
+  for (const MolDev& M : c->mols)
+    std::stable_sort(order.begin() + M.pair0, order.begin() + M.pair0 + M.npair,
+                     [&](int x, int y) { return c->schwarz_pair[x] > c->schwarz_pair[y]; });
   std::vector<double> sq(c->npair);
   for (int p = 0; p < c->npair; ++p) sq[p] = c->schwarz_pair[order[p]];
   if ((rc = upload(c->d_sorted_idx, order, st))) return rc;
@@ -476,223 +618,275 @@ int ctx_init(oqpg_ctx* c, int nshell, const int* am_, const int* ncontr_, const 
 
 void ctx_free(oqpg_ctx* c) {
   if (!c) return;
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
   DevBuf* bufs[] = {&c->d_shells, &c->d_pairs, &c->d_prims, &c->d_pair_ij, &c->d_pair_type, &c->d_q, &c->d_qf,
-                    &c->d_aoff, &c->d_naos, &c->d_dp, &c->d_dj, &c->d_dk, &c->d_gj, &c->d_gk, &c->d_f,
-                    &c->d_fold, &c->d_dsh, &c->d_dshf, &c->d_dmax, &c->d_counts, &c->d_prim_counter,
-                    &c->d_primsf, &c->d_djf, &c->d_dkf};
+                    &c->d_aoff, &c->d_naos, &c->d_mols, &c->d_pair_mol, &c->d_row_mol, &c->d_primsf,
+                    &c->d_sorted_idx, &c->d_sorted_q, &c->d_dp, &c->d_f, &c->d_fold, &c->d_gin, &c->d_gout};
   for (DevBuf* b : bufs) b->release();
-  for (auto& b : c->d_lists) b.release();
-  for (auto& b : c->d_slists) b.release();
-  c->d_sorted_idx.release(); c->d_sorted_q.release(); c->d_hist.release(); c->d_cursor.release();
-  c->d_work.release();
+  c->hb.release();
+  c->gb.release();
   if (c->h_in) cudaFreeHost(c->h_in);
   if (c->h_out) cudaFreeHost(c->h_out);
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);
   for (auto& p : c->evc) for (auto& e : p) if (e) cudaEventDestroy(e);
+  if (c->gstream) cudaStreamDestroy(c->gstream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
 
-// Core build on device buffers.  dp: packed densities (device), f: packed
-// output (device), f_old: optional packed previous Fock (device, updated).
-// Lists 0..20 hold the FP64 quartets of each class, lists 21..41 the FP32
-// quartets of the precision-split build (empty in the plain FP64 mode).
-int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfocks, double se, double sc,
-              cudaStream_t st) {
-  if (nfocks != 1 && nfocks != 2) return UNSUPPORTED;
-  constexpr int NL = 2 * NCLASS;
-  const int n = c->nbf, ns = c->nshell;
-  const size_t n2 = (size_t)n * n;
-  const int nk = nfocks;
-  const bool split = (c->precision_mode == 1 || c->precision_mode == 2) && c->tau_f32 > 0.0;
-  CK(c->d_dj.ensure(sizeof(double) * n2));
-  if (nk == 2) CK(c->d_dk.ensure(sizeof(double) * 2 * n2));
-  if (split) {
-    CK(c->d_djf.ensure(sizeof(float) * n2));
-    if (nk == 2) CK(c->d_dkf.ensure(sizeof(float) * 2 * n2));
+bool split_on(const oqpg_ctx* c) { return (c->precision_mode == 1 || c->precision_mode == 2) && c->tau_f32 > 0.0; }
+
+// Buffers of one pipeline whose sizes follow from the batch alone.
+int ensure_bufs(oqpg_ctx* c, BuildBufs& B, int nk) {
+  const size_t n2 = (size_t)c->nbf * c->stride;
+  CK(B.dj.ensure(sizeof(double) * n2));
+  if (nk == 2) CK(B.dk.ensure(sizeof(double) * 2 * n2));
+  if (split_on(c)) {
+    CK(B.djf.ensure(sizeof(float) * n2));
+    if (nk == 2) CK(B.dkf.ensure(sizeof(float) * 2 * n2));
   }
-  CK(c->d_gj.ensure(sizeof(double) * n2));
-  CK(c->d_gk.ensure(sizeof(double) * nk * n2));
-  CK(c->d_dsh.ensure(sizeof(double) * ns * ns));
-  CK(c->d_dshf.ensure(sizeof(float) * ns * ns));
-  CK(c->d_dmax.ensure(sizeof(unsigned long long)));
-  CK(c->d_counts.ensure(sizeof(unsigned long long) * NL));
-  CK(c->d_prim_counter.ensure(sizeof(unsigned long long) * NL));
-  CK(c->d_work.ensure(sizeof(unsigned long long) * 2 * NL));
-  CK(cudaEventRecord(c->ev[0], st));
-  k_unpack<<<std::min<long long>((n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(dp, nfocks, n, c->d_dj.as<double>(),
-                                                                                 c->d_dk.as<double>());
-  CK(cudaGetLastError());
-  if (split) {
-    k_to_f32<<<std::min<long long>((n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(c->d_dj.as<double>(), (long long)n2,
-                                                                                   c->d_djf.as<float>());
-    CK(cudaGetLastError());
-    if (nk == 2) {
-      k_to_f32<<<std::min<long long>((2 * n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
-          c->d_dk.as<double>(), (long long)(2 * n2), c->d_dkf.as<float>());
-      CK(cudaGetLastError());
-    }
-  }
-  CK(cudaMemsetAsync(c->d_dmax.p, 0, sizeof(unsigned long long), st));
-  const long long npair = c->npair;
-  k_dsh<<<std::min<long long>((npair + 127) / 128, c->nsm * 8LL), 128, 0, st>>>(
-      dp, nfocks, n, ns, c->d_aoff.as<int>(), c->d_naos.as<int>(), c->d_dsh.as<double>(), c->d_dshf.as<float>(),
-      c->d_dmax.as<unsigned long long>());
-  CK(cudaGetLastError());
-  // --- quartet lists: count (first build) or fill directly with the previous capacities
+  CK(B.gj.ensure(sizeof(double) * n2));
+  CK(B.gk.ensure(sizeof(double) * nk * n2));
+  CK(B.dsh.ensure(sizeof(double) * std::max<long long>(c->dsh_elems, 1)));
+  CK(B.dshf.ensure(sizeof(float) * std::max<long long>(c->dsh_elems, 1)));
+  CK(B.dmax.ensure(sizeof(unsigned long long) * c->nmol));
+  CK(B.counts.ensure(sizeof(unsigned long long) * NLIST));
+  CK(B.primc.ensure(sizeof(unsigned long long) * NLIST));
+  CK(B.hist.ensure(sizeof(unsigned long long) * NLIST * NBIN));
+  CK(B.cursor.ensure(sizeof(unsigned long long) * NLIST * NBIN));
+  CK(B.work.ensure(sizeof(unsigned long long) * 2 * NLIST));
+  CK(B.ranges.ensure(sizeof(unsigned long long) * 4 * NLIST));
+  CK(B.caps.ensure(sizeof(unsigned long long) * NLIST));
+  CK(B.split.ensure(sizeof(int) * NLIST));
+  CK(B.flag.ensure(sizeof(unsigned)));
+  if (!B.h_rb) CK(cudaMallocHost(&B.h_rb, sizeof(unsigned long long) * (1 + 2 * NLIST)));
+  return OK;
+}
+
+ListArgs list_args(const oqpg_ctx* c, BuildBufs& B) {
   ListArgs la{};
-  la.npair = c->npair; la.ns = ns;
+  la.npair = c->npair;
+  la.mols = c->d_mols.as<MolDev>();
+  la.pair_mol = c->d_pair_mol.as<int>();
   la.pair_ij = c->d_pair_ij.as<int2>();
   la.pair_type = c->d_pair_type.as<int>();
   la.q = c->d_q.as<double>(); la.qf = c->d_qf.as<float>();
   la.sorted_idx = c->d_sorted_idx.as<int>(); la.sorted_q = c->d_sorted_q.as<double>();
-  la.dsh = c->d_dsh.as<double>(); la.dshf = c->d_dshf.as<float>();
-  la.dmax_bits = c->d_dmax.as<unsigned long long>();
+  la.dsh = B.dsh.as<double>(); la.dshf = B.dshf.as<float>();
+  la.dmax_bits = B.dmax.as<unsigned long long>();
   la.tau = c->tau;
-  la.tau_f32 = split ? c->tau_f32 : 0.0;
-  la.counts = c->d_counts.as<unsigned long long>();
-  bool lists_ok = false;
-  for (int pass = 0; pass < 3 && !lists_ok; ++pass) {
-    la.write = c->have_caps ? 1 : 0;
-    for (int k = 0; k < NL; ++k) { la.lists[k] = c->d_lists[k].as<uint2>(); la.caps[k] = c->caps[k]; }
-    CK(cudaMemsetAsync(c->d_counts.p, 0, sizeof(unsigned long long) * NL, st));
-    k_lists<<<c->npair, 256, 0, st>>>(la);
+  la.tau_f32 = split_on(c) ? c->tau_f32 : 0.0;
+  la.counts = B.counts.as<unsigned long long>();
+  for (int k = 0; k < NLIST; ++k) { la.lists[k] = B.lists[k].as<uint2>(); la.caps[k] = B.cap[k]; }
+  return la;
+}
+
+// Screening stage shared by the count pass and the build: unpacked densities
+// (and FP32 copies), shell densities and their per-molecule maxima.
+int issue_densities(oqpg_ctx* c, BuildBufs& B, const double* dp, int nfocks, cudaStream_t st) {
+  const size_t n2 = (size_t)c->nbf * c->stride;
+  const unsigned g = (unsigned)std::min<long long>((n2 + 255) / 256, c->nsm * 8LL);
+  k_unpack<<<g, 256, 0, st>>>(dp, nfocks, c->d_mols.as<MolDev>(), c->d_row_mol.as<int>(), c->nbf, c->stride,
+                              B.dj.as<double>(), B.dk.as<double>());
+  CK(cudaGetLastError());
+  if (split_on(c)) {
+    k_to_f32<<<g, 256, 0, st>>>(B.dj.as<double>(), (long long)n2, B.djf.as<float>());
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(c->counts, c->d_counts.p, sizeof(unsigned long long) * NL, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    bool ok = c->have_caps;
-    for (int k = 0; k < NL; ++k)
-      if (c->counts[k] > c->caps[k]) ok = false;
-    if (ok) {
-      lists_ok = true;
-      break;
+    if (nfocks == 2) {
+      k_to_f32<<<(unsigned)std::min<long long>((2 * n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
+          B.dk.as<double>(), (long long)(2 * n2), B.dkf.as<float>());
+      CK(cudaGetLastError());
     }
-    for (int k = 0; k < NL; ++k) {
-      if (c->counts[k] > c->caps[k] || !c->have_caps) {
-        const unsigned long long cap = c->counts[k] + c->counts[k] / 8 + 1024;
-        if (cap > c->caps[k]) {
-          CK(c->d_lists[k].ensure(sizeof(uint2) * cap));
-          c->caps[k] = cap;
-        }
-      }
+  }
+  CK(cudaMemsetAsync(B.dmax.p, 0, sizeof(unsigned long long) * c->nmol, st));
+  k_dsh<<<(unsigned)std::min<long long>((c->npair + 127) / 128, c->nsm * 8LL), 128, 0, st>>>(
+      dp, nfocks, c->d_mols.as<MolDev>(), c->d_pair_mol.as<int>(), c->d_pair_ij.as<int2>(), c->npair,
+      c->d_aoff.as<int>(), c->d_naos.as<int>(), B.dsh.as<double>(), B.dshf.as<float>(),
+      B.dmax.as<unsigned long long>());
+  CK(cudaGetLastError());
+  return OK;
+}
+
+// (Re)size the lists of a pipeline for the given per-list counts, with headroom
+// for the screening of later densities.
+int size_lists(oqpg_ctx* c, BuildBufs& B, const unsigned long long* counts, cudaStream_t st) {
+  for (int k = 0; k < NLIST; ++k) {
+    if (counts[k] <= B.cap[k] && B.sized) continue;
+    const unsigned long long cap = counts[k] ? counts[k] + counts[k] / 4 + 1024 : 0;
+    if (cap > B.cap[k]) {
+      CK(B.lists[k].ensure(sizeof(uint2) * cap));
+      CK(B.slists[k].ensure(sizeof(uint2) * cap));
+      B.cap[k] = cap;
     }
-    c->have_caps = true;
   }
-  if (!lists_ok) return DEV_ERR;  // quartet lists never fitted: do not launch on partial lists
-  // --- order every list by primitive-quartet count (counting sort)
-  CK(c->d_hist.ensure(sizeof(unsigned long long) * NL * NBIN));
-  CK(c->d_cursor.ensure(sizeof(unsigned long long) * NL * NBIN));
-  CK(cudaMemsetAsync(c->d_hist.p, 0, sizeof(unsigned long long) * NL * NBIN, st));
-  for (int k = 0; k < NL; ++k) {
-    if (!c->counts[k]) continue;
-    const long long nk_ = (long long)c->counts[k];
-    k_bin_hist<<<(unsigned)std::min<long long>((nk_ + 255) / 256, c->nsm * 4LL), 256, 0, st>>>(
-        c->d_lists[k].as<uint2>(), nk_, c->d_pairs.as<PairDev>(), c->d_hist.as<unsigned long long>() + k * NBIN);
-    CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(B.caps.p, B.cap, sizeof(B.cap), cudaMemcpyHostToDevice, st));
+  int split[NLIST];
+  for (int k = 0; k < NLIST; ++k) {
+    const int cl = k % NCLASS;
+    split[k] = class_info(cl).team ? 0 : std::max(0, NBIN - 4 * c->tune.split_log2[cl]);
   }
-  unsigned long long hist[NL * NBIN], cur[NL * NBIN];
-  CK(cudaMemcpyAsync(hist, c->d_hist.p, sizeof(hist), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(B.split.p, split, sizeof(split), cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));  // the host arrays above are stack memory
+  B.sized = true;
+  return OK;
+}
+
+// Count pass: list lengths for the current density without writing the lists.
+int count_lists(oqpg_ctx* c, BuildBufs& B, const double* dp, int nfocks, cudaStream_t st,
+                unsigned long long* counts) {
+  int rc;
+  if ((rc = issue_densities(c, B, dp, nfocks, st))) return rc;
+  ListArgs la = list_args(c, B);
+  la.write = 0;
+  CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * NLIST, st));
+  k_lists<<<c->npair, 256, 0, st>>>(la);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(counts, B.counts.p, sizeof(unsigned long long) * NLIST, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  for (int k = 0; k < NL; ++k) {
-    unsigned long long s = 0;
-    for (int b = 0; b < NBIN; ++b) { cur[k * NBIN + b] = s; s += hist[k * NBIN + b]; }
-    if (s != c->counts[k]) return DEV_ERR;
-  }
-  CK(cudaMemcpyAsync(c->d_cursor.p, cur, sizeof(cur), cudaMemcpyHostToDevice, st));
-  for (int k = 0; k < NL; ++k) {
-    if (!c->counts[k]) continue;
-    const long long nk_ = (long long)c->counts[k];
-    CK(c->d_slists[k].ensure(sizeof(uint2) * nk_));
-    const long long chunk = 4096;
-    k_bin_scatter<<<(unsigned)((nk_ + chunk - 1) / chunk), 256, 0, st>>>(
-        c->d_lists[k].as<uint2>(), nk_, c->d_pairs.as<PairDev>(), c->d_cursor.as<unsigned long long>() + k * NBIN,
-        c->d_slists[k].as<uint2>(), chunk);
+  return OK;
+}
+
+// Device-driven build: every launch is sized by the pipeline's list
+// capacities; list lengths, sort cursors and work ranges stay on the device,
+// so the sequence can be captured into a CUDA graph.  A list longer than its
+// capacity sets the overflow flag; the finalize kernel then leaves f alone.
+int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* f_old, int nfocks, double se,
+                double sc, cudaStream_t st, bool timing, int* nlaunch_out) {
+  const int nk = nfocks;
+  const size_t n2 = (size_t)c->nbf * c->stride;
+  int rc;
+  int nlaunch = 0;
+  if (timing) CK(cudaEventRecord(c->ev[0], st));
+  CK(cudaMemsetAsync(B.flag.p, 0, sizeof(unsigned), st));
+  if ((rc = issue_densities(c, B, dp, nfocks, st))) return rc;
+  nlaunch += 2 + (split_on(c) ? (nk == 2 ? 2 : 1) : 0);
+  ListArgs la = list_args(c, B);
+  la.write = 1;
+  CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * NLIST, st));
+  k_lists<<<c->npair, 256, 0, st>>>(la);
+  CK(cudaGetLastError());
+  ++nlaunch;
+  // order every list by primitive-quartet count (counting sort, device-side scan)
+  CK(cudaMemsetAsync(B.hist.p, 0, sizeof(unsigned long long) * NLIST * NBIN, st));
+  unsigned long long* counts = B.counts.as<unsigned long long>();
+  for (int k = 0; k < NLIST; ++k) {
+    if (!B.cap[k]) continue;
+    const long long cap = (long long)B.cap[k];
+    k_bin_hist<<<(unsigned)std::min<long long>((cap + 255) / 256, c->nsm * 4LL), 256, 0, st>>>(
+        B.lists[k].as<uint2>(), cap, counts + k, c->d_pairs.as<PairDev>(),
+        B.hist.as<unsigned long long>() + k * NBIN);
     CK(cudaGetLastError());
+    ++nlaunch;
   }
-  CK(cudaEventRecord(c->ev[1], st));
+  static_assert(NLIST <= 64, "k_bin_scan runs one thread per list in one 64-thread CTA");
+  k_bin_scan<<<1, 64, 0, st>>>(counts, B.caps.as<unsigned long long>(), B.split.as<int>(),
+                               B.hist.as<unsigned long long>(), B.cursor.as<unsigned long long>(),
+                               B.ranges.as<unsigned long long>(), B.flag.as<unsigned>());
+  CK(cudaGetLastError());
+  ++nlaunch;
+  const long long chunk = 4096;
+  for (int k = 0; k < NLIST; ++k) {
+    if (!B.cap[k]) continue;
+    const long long cap = (long long)B.cap[k];
+    k_bin_scatter<<<(unsigned)((cap + chunk - 1) / chunk), 256, 0, st>>>(
+        B.lists[k].as<uint2>(), cap, counts + k, c->d_pairs.as<PairDev>(),
+        B.cursor.as<unsigned long long>() + k * NBIN, B.slists[k].as<uint2>(), chunk, B.flag.as<unsigned>());
+    CK(cudaGetLastError());
+    ++nlaunch;
+  }
+  if (timing) CK(cudaEventRecord(c->ev[1], st));
   // --- integrals + digestion
-  CK(cudaMemsetAsync(c->d_gj.p, 0, sizeof(double) * n2, st));
-  CK(cudaMemsetAsync(c->d_gk.p, 0, sizeof(double) * nk * n2, st));
-  CK(cudaMemsetAsync(c->d_prim_counter.p, 0, sizeof(unsigned long long) * NL, st));
-  CK(cudaMemsetAsync(c->d_work.p, 0, sizeof(unsigned long long) * 2 * NL, st));
+  CK(cudaMemsetAsync(B.gj.p, 0, sizeof(double) * n2, st));
+  CK(cudaMemsetAsync(B.gk.p, 0, sizeof(double) * nk * n2, st));
+  CK(cudaMemsetAsync(B.primc.p, 0, sizeof(unsigned long long) * NLIST, st));
+  CK(cudaMemsetAsync(B.work.p, 0, sizeof(unsigned long long) * 2 * NLIST, st));
   BuildArgs a{};
   a.shells = c->d_shells.as<ShellDev>();
   a.pairs = c->d_pairs.as<PairDev>();
   a.prims = c->d_prims.as<PrimPair>();
   a.primsf = c->d_primsf.as<PrimPairF>();
-  a.nbf = n;
+  a.nbf = c->stride;
+  a.kstride = n2;
   a.nk = nk;
   a.prim_cut = 1e-4 * c->tau;
   a.prim_cut2 = a.prim_cut * a.prim_cut;
   set_band(a);
   a.elem_cut = c->tau;
-  a.dj = c->d_dj.as<double>();
-  a.dk = (nk == 1) ? c->d_dj.as<double>() : c->d_dk.as<double>();
-  a.djf = c->d_djf.as<float>();
-  a.dkf = (nk == 1) ? c->d_djf.as<float>() : c->d_dkf.as<float>();
-  a.gj = c->d_gj.as<double>();
-  a.gk = c->d_gk.as<double>();
+  a.dj = B.dj.as<double>();
+  a.dk = (nk == 1) ? B.dj.as<double>() : B.dk.as<double>();
+  a.djf = B.djf.as<float>();
+  a.dkf = (nk == 1) ? B.djf.as<float>() : B.dkf.as<float>();
+  a.gj = B.gj.as<double>();
+  a.gk = B.gk.as<double>();
   a.roots_f32 = c->precision_mode == 2 ? 1 : 0;
-  double nq = 0;
-  // heaviest classes first; every class launch (both precisions) is bracketed by events
-  int nlaunch = 0;
+  unsigned long long* ranges = B.ranges.as<unsigned long long>();
+  // heaviest classes first
   for (int cl = NCLASS - 1; cl >= 0; --cl) {
-    if (c->counts[cl] == 0 && c->counts[NCLASS + cl] == 0) continue;
-    CK(cudaEventRecord(c->evc[cl][0], st));
+    if (!B.cap[cl] && !B.cap[NCLASS + cl]) continue;
+    if (timing) CK(cudaEventRecord(c->evc[cl][0], st));
+    a.chunk = c->tune.chunk[cl];
+    a.ctas_per_sm = c->tune.ctas_per_sm[cl];
     for (int prec = 0; prec < 2; ++prec) {
       const int li = cl + prec * NCLASS;
-      if (!c->counts[li]) continue;
+      if (!B.cap[li]) continue;
       const int fl = prec ? MODE_F32 : 0;
-      a.counters = c->d_prim_counter.as<unsigned long long>() + li;
-      nq += (double)c->counts[li];
-      long long head = 0;
-      if (!class_info(cl).team) {
-        // quartets with >= 2^PRIM_SPLIT_LOG2 primitive quartets (a prefix of the
-        // sorted list) go to the warp-per-quartet primitive-parallel kernel
-        for (int b = 0; b <= NBIN - 1 - 4 * PRIM_SPLIT_LOG2; ++b) head += (long long)hist[li * NBIN + b];
-        if (head > 0) {
-          a.quartets = c->d_slists[li].as<uint2>();
-          a.nquartets = head;
-          a.work = c->d_work.as<unsigned long long>() + NL + li;
-          CK(launch_class(cl, c->pure, MODE_PRIM | fl, a, c->nsm, st));
-          ++nlaunch;
-        }
-      }
-      if ((long long)c->counts[li] > head) {
-        a.quartets = c->d_slists[li].as<uint2>() + head;
-        a.nquartets = (long long)c->counts[li] - head;
-        a.work = c->d_work.as<unsigned long long>() + li;
-        CK(launch_class(cl, c->pure, MODE_FOCK | fl, a, c->nsm, st));
+      a.counters = B.primc.as<unsigned long long>() + li;
+      a.quartets = B.slists[li].as<uint2>();
+      a.nquartets = (long long)B.cap[li];
+      if (!class_info(cl).team && c->tune.split_log2[cl] < 64) {
+        // quartets with >= 2^split primitive quartets (a prefix of the sorted
+        // list) go to the warp-per-quartet primitive-parallel kernel
+        a.range = ranges + 4 * li;
+        a.work = B.work.as<unsigned long long>() + NLIST + li;
+        CK(launch_class(cl, c->pure, MODE_PRIM | fl, a, c->nsm, st));
         ++nlaunch;
       }
+      a.range = ranges + 4 * li + 2;
+      a.work = B.work.as<unsigned long long>() + li;
+      CK(launch_class(cl, c->pure, MODE_FOCK | fl, a, c->nsm, st));
+      ++nlaunch;
     }
-    CK(cudaEventRecord(c->evc[cl][1], st));
+    if (timing) CK(cudaEventRecord(c->evc[cl][1], st));
   }
-  CK(cudaEventRecord(c->ev[2], st));
-  const long long ntri = (long long)n * (n + 1) / 2;
+  if (timing) CK(cudaEventRecord(c->ev[2], st));
   const double ck = (nk == 1) ? 0.5 * se : se;
-  k_finalize<<<std::min<long long>((ntri + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
-      c->d_gj.as<double>(), c->d_gk.as<double>(), nk, n, sc, ck, f, f_old);
+  k_finalize<<<(unsigned)std::min<long long>((c->ntri + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
+      B.gj.as<double>(), B.gk.as<double>(), nk, c->d_mols.as<MolDev>(), c->nmol, c->ntri, c->stride, n2, sc, ck, f,
+      f_old, B.flag.as<unsigned>());
   CK(cudaGetLastError());
-  CK(cudaEventRecord(c->ev[3], st));
-  unsigned long long nprim[NL];
-  CK(cudaMemcpyAsync(nprim, c->d_prim_counter.p, sizeof(nprim), cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
+  ++nlaunch;
+  if (timing) CK(cudaEventRecord(c->ev[3], st));
+  // readback of the flag, the list lengths and the primitive counts (pinned)
+  CK(cudaMemcpyAsync(B.h_rb, B.flag.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(B.h_rb + 1, B.counts.p, sizeof(unsigned long long) * NLIST, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(B.h_rb + 1 + NLIST, B.primc.p, sizeof(unsigned long long) * NLIST, cudaMemcpyDeviceToHost,
+                     st));
+  if (nlaunch_out) *nlaunch_out = nlaunch;
+  return OK;
+}
+
+void record_stats(oqpg_ctx* c, const BuildBufs& B, int nlaunch, bool timing) {
+  const unsigned long long* cnt = B.h_rb + 1;
+  const unsigned long long* nprim = B.h_rb + 1 + NLIST;
+  for (int k = 0; k < NLIST; ++k) c->counts[k] = cnt[k];
   float t01 = 0, t12 = 0, t03 = 0;
-  cudaEventElapsedTime(&t01, c->ev[0], c->ev[1]);
-  cudaEventElapsedTime(&t12, c->ev[1], c->ev[2]);
-  cudaEventElapsedTime(&t03, c->ev[0], c->ev[3]);
+  if (timing) {
+    cudaEventElapsedTime(&t01, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&t12, c->ev[1], c->ev[2]);
+    cudaEventElapsedTime(&t03, c->ev[0], c->ev[3]);
+  }
   double* S = c->last_stats;
   S[1] = 0;
-  double q32 = 0, p32 = 0;
+  double nq = 0, q32 = 0, p32 = 0;
   for (int k = 0; k < NCLASS; ++k) {
-    const unsigned long long q = c->counts[k] + c->counts[NCLASS + k];
+    const unsigned long long q = cnt[k] + cnt[NCLASS + k];
+    nq += (double)q;
     S[7 + k] = (double)q;
-    S[7 + NCLASS + k] = (c->counts[k] ? (double)nprim[k] : 0.0) + (c->counts[NCLASS + k] ? (double)nprim[NCLASS + k] : 0.0);
-    q32 += (double)c->counts[NCLASS + k];
-    p32 += c->counts[NCLASS + k] ? (double)nprim[NCLASS + k] : 0.0;
+    S[7 + NCLASS + k] = (double)nprim[k] + (double)nprim[NCLASS + k];
+    q32 += (double)cnt[NCLASS + k];
+    p32 += (double)nprim[NCLASS + k];
     float tk = 0;
-    if (q) cudaEventElapsedTime(&tk, c->evc[k][0], c->evc[k][1]);
+    if (timing && (B.cap[k] || B.cap[NCLASS + k])) cudaEventElapsedTime(&tk, c->evc[k][0], c->evc[k][1]);
     S[7 + 2 * NCLASS + k] = tk;
     S[1] += S[7 + NCLASS + k];
   }
@@ -700,17 +894,46 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
   S[2] = t01;
   S[3] = t12;
   S[4] = t03;
-  S[5] = n;
+  S[5] = c->nbf;
   S[6] = c->npair;
-  S[7 + 3 * NCLASS] = nlaunch + 4;  // class kernels + unpack, dsh, lists, finalize
+  S[7 + 3 * NCLASS] = nlaunch;
   S[8 + 3 * NCLASS] = q32;
   S[9 + 3 * NCLASS] = p32;
-  return OK;
+}
+
+// Core build on device buffers (synchronous).  dp: packed densities (device),
+// f: packed output (device), f_old: optional packed previous Fock (device,
+// updated).  The first build of a context runs a count pass to size the
+// lists; a later build whose lists outgrow their capacities is redone with
+// larger ones (f and f_old untouched in between).
+int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfocks, double se, double sc,
+              cudaStream_t st) {
+  if (nfocks != 1 && nfocks != 2) return UNSUPPORTED;
+  BuildBufs& B = c->hb;
+  int rc;
+  if ((rc = ensure_bufs(c, B, nfocks))) return rc;
+  if (!B.sized) {
+    unsigned long long counts[NLIST];
+    if ((rc = count_lists(c, B, dp, nfocks, st, counts))) return rc;
+    if ((rc = size_lists(c, B, counts, st))) return rc;
+  }
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    int nlaunch = 0;
+    if ((rc = issue_build(c, B, dp, f, f_old, nfocks, se, sc, st, true, &nlaunch))) return rc;
+    CK(cudaStreamSynchronize(st));
+    const unsigned flag = (unsigned)(B.h_rb[0] & 0xffffffffu);
+    if (flag == 0) {
+      record_stats(c, B, nlaunch, true);
+      return OK;
+    }
+    if (flag & 2u) return DEV_ERR;  // sort bookkeeping disagreed with the list lengths
+    if ((rc = size_lists(c, B, B.h_rb + 1, st))) return rc;
+  }
+  return DEV_ERR;  // quartet lists never fitted: nothing was written
 }
 
 int ctx_build_host(oqpg_ctx* c, const double* d, double* f, double* f_old, int nfocks, double se, double sc) {
-  const size_t ntri = (size_t)c->nbf * (c->nbf + 1) / 2;
-  const size_t bytes = sizeof(double) * ntri * nfocks;
+  const size_t bytes = sizeof(double) * (size_t)c->ntri * nfocks;
   if (bytes > c->h_bytes) {
     if (c->h_in) cudaFreeHost(c->h_in);
     if (c->h_out) cudaFreeHost(c->h_out);
@@ -740,6 +963,75 @@ int ctx_build_host(oqpg_ctx* c, const double* d, double* f, double* f_old, int n
   return OK;
 }
 
+// --- captured builds ---------------------------------------------------------
+
+// Capture the device-driven build on the graph pipeline's buffers (d_gin ->
+// d_gout), sized from the lengths of a direct build of the same density.
+int graph_capture(oqpg_ctx* c, const double* dp, int nfocks, double se, double sc) {
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  if (!c->gstream) CK(cudaStreamCreateWithFlags(&c->gstream, cudaStreamNonBlocking));
+  cudaStream_t gs = c->gstream;
+  BuildBufs& B = c->gb;
+  int rc;
+  const size_t bytes = sizeof(double) * (size_t)c->ntri * nfocks;
+  CK(c->d_gin.ensure(bytes));
+  CK(c->d_gout.ensure(bytes));
+  if ((rc = ensure_bufs(c, B, nfocks))) return rc;
+  unsigned long long counts[NLIST];
+  if ((rc = count_lists(c, B, dp, nfocks, gs, counts))) return rc;
+  for (int k = 0; k < NLIST; ++k) counts[k] = std::max(counts[k], c->counts[k]);
+  if ((rc = size_lists(c, B, counts, gs))) return rc;
+  CK(cudaStreamSynchronize(gs));
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(gs, cudaStreamCaptureModeRelaxed));
+  int nlaunch = 0;
+  rc = issue_build(c, B, c->d_gin.as<double>(), c->d_gout.as<double>(), nullptr, nfocks, se, sc, gs, false, &nlaunch);
+  cudaError_t e = cudaStreamEndCapture(gs, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  CK(e);
+  e = cudaGraphInstantiate(&c->gexec, g, 0);
+  cudaGraphDestroy(g);
+  CK(e);
+  c->g_nfocks = nfocks; c->g_se = se; c->g_sc = sc; c->g_mode = c->precision_mode; c->g_tau32 = c->tau_f32;
+  c->g_nlaunch = nlaunch;
+  ++c->graph_captures;
+  return OK;
+}
+
+// Build through the captured graph: copy d into the graph's input, replay,
+// copy the graph's output to f (all on st), then check the overflow flag.  A
+// first call, a change of nfocks / scale factors / precision split, or an
+// overflow (the density screens in more quartets than the capture was sized
+// for) builds directly and recaptures.
+int graph_build(oqpg_ctx* c, const double* d_device, double* f_device, int nfocks, double se, double sc,
+                cudaStream_t st) {
+  if (nfocks != 1 && nfocks != 2) return UNSUPPORTED;
+  const size_t bytes = sizeof(double) * (size_t)c->ntri * nfocks;
+  const bool fresh = c->gexec && c->g_nfocks == nfocks && c->g_se == se && c->g_sc == sc &&
+                     c->g_mode == c->precision_mode && c->g_tau32 == c->tau_f32;
+  int rc;
+  if (fresh) {
+    CK(cudaMemcpyAsync(c->d_gin.p, d_device, bytes, cudaMemcpyDeviceToDevice, st));
+    CK(cudaGraphLaunch(c->gexec, st));
+    CK(cudaMemcpyAsync(f_device, c->d_gout.p, bytes, cudaMemcpyDeviceToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    if ((c->gb.h_rb[0] & 0xffffffffu) == 0) {
+      record_stats(c, c->gb, c->g_nlaunch, false);
+      ++c->graph_replays;
+      return OK;
+    }
+  }
+  if ((rc = ctx_build(c, d_device, f_device, nullptr, nfocks, se, sc, st))) return rc;
+  CK(cudaStreamSynchronize(st));
+  return graph_capture(c, d_device, nfocks, se, sc);
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -747,17 +1039,32 @@ extern "C" {
 
 int oqpg_create(oqpg_ctx** out, int nshell, const int* am, const int* ncontr, const int* origin, const double* ex,
                 const double* cc, const int* harmonic, int natom, const double* xyz, double cutoff) {
+  return oqpg_create_batch(out, 1, &nshell, &natom, am, ncontr, origin, ex, cc, harmonic, xyz, cutoff);
+}
+
+int oqpg_create_batch(oqpg_ctx** out, int nmol, const int* nshell, const int* natom, const int* am,
+                      const int* ncontr, const int* origin, const double* ex, const double* cc, const int* harmonic,
+                      const double* xyz, double cutoff) {
   if (!out) return UNSUPPORTED;
   *out = nullptr;
   oqpg_ctx* c = new (std::nothrow) oqpg_ctx;
   if (!c) return NO_MEM;
-  const int rc = ctx_init(c, nshell, am, ncontr, origin, ex, cc, harmonic, natom, xyz, cutoff);
+  const int rc = ctx_init(c, nmol, nshell, natom, am, ncontr, origin, ex, cc, harmonic, xyz, cutoff);
   if (rc) {
     ctx_free(c);
     return rc;
   }
   *out = c;
   return OK;
+}
+
+int oqpg_batch_info(const oqpg_ctx* ctx, int* nbf, long long* tri0) {
+  if (!ctx) return NOT_INIT;
+  for (int m = 0; m < ctx->nmol; ++m) {
+    if (nbf) nbf[m] = ctx->mols[m].nbf;
+    if (tri0) tri0[m] = ctx->mols[m].tri0;
+  }
+  return ctx->nmol;
 }
 
 int oqpg_destroy(oqpg_ctx* ctx) {
@@ -781,12 +1088,60 @@ int oqpg_fock_jk_device(oqpg_ctx* ctx, const double* d_device, double* f_device,
 
 int oqpg_schwarz(const oqpg_ctx* ctx, double* q) {
   if (!ctx) return NOT_INIT;
+  if (ctx->nmol != 1) return UNSUPPORTED;
   const int ns = ctx->nshell;
   for (int i = 0; i < ns; ++i)
     for (int j = 0; j <= i; ++j) {
       const double v = ctx->schwarz_pair[(size_t)i * (i + 1) / 2 + j];
       q[(size_t)i * ns + j] = q[(size_t)j * ns + i] = v;
     }
+  return OK;
+}
+
+int oqpg_fock_jk_graph(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, double se, double sc,
+                       void* stream) {
+  if (!ctx) return NOT_INIT;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  return graph_build(ctx, d_device, f_device, nfocks, se, sc, st);
+}
+
+int oqpg_graph_info(const oqpg_ctx* ctx, int* captures, int* replays, int* kernels) {
+  if (!ctx) return NOT_INIT;
+  if (captures) *captures = ctx->graph_captures;
+  if (replays) *replays = ctx->graph_replays;
+  if (kernels) *kernels = ctx->g_nlaunch;
+  return OK;
+}
+
+int oqpg_set_tuning(oqpg_ctx* ctx, const int* split_log2, const int* chunk, const int* ctas_per_sm) {
+  if (!ctx) return NOT_INIT;
+  for (int k = 0; k < NCLASS; ++k) {
+    if (split_log2 && (split_log2[k] < 0 || split_log2[k] > 64)) return UNSUPPORTED;
+    if (chunk && (chunk[k] < 32 || chunk[k] > 4096 || chunk[k] % 32)) return UNSUPPORTED;
+    if (ctas_per_sm && (ctas_per_sm[k] < 0 || ctas_per_sm[k] > 64)) return UNSUPPORTED;
+  }
+  for (int k = 0; k < NCLASS; ++k) {
+    if (split_log2) ctx->tune.split_log2[k] = split_log2[k];
+    if (chunk) ctx->tune.chunk[k] = chunk[k];
+    if (ctas_per_sm) ctx->tune.ctas_per_sm[k] = ctas_per_sm[k];
+  }
+  // the split bins live on the device and in the captured graph: redo both
+  ctx->hb.sized = false;
+  ctx->gb.sized = false;
+  if (ctx->gexec) {
+    cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
+  }
+  return OK;
+}
+
+int oqpg_get_tuning(const oqpg_ctx* ctx, int* split_log2, int* chunk, int* ctas_per_sm) {
+  if (!ctx) return NOT_INIT;
+  for (int k = 0; k < NCLASS; ++k) {
+    if (split_log2) split_log2[k] = ctx->tune.split_log2[k];
+    if (chunk) chunk[k] = ctx->tune.chunk[k];
+    if (ctas_per_sm) ctas_per_sm[k] = ctx->tune.ctas_per_sm[k];
+  }
   return OK;
 }
 
@@ -838,6 +1193,7 @@ int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold) {
   if (mode != 0 && !(threshold > 0.0)) return UNSUPPORTED;
   ctx->precision_mode = mode;
   ctx->tau_f32 = mode != 0 ? threshold : 0.0;
+  ctx->hb.sized = false;  // the FP32 lists are sized by a fresh count pass
   return OK;
 }
 
@@ -869,7 +1225,7 @@ void routec_fock_jk(const double* d, double* f, const int* nbf, const int* nfock
   int rc;
   if (!g_ctx) rc = NOT_INIT;
   else if (!d || !f || !nbf || !nfocks || !se || !sc) rc = UNSUPPORTED;
-  else if (*nbf != g_ctx->nbf) rc = NOT_INIT;   // registered basis does not match the caller's
+  else if (*nbf != g_ctx->nbf || g_ctx->nmol != 1) rc = NOT_INIT;   // registered basis does not match the caller's
   else rc = ctx_build_host(g_ctx, d, f, nullptr, *nfocks, *se, *sc);
   if (info) *info = rc;
 }
@@ -880,8 +1236,56 @@ void routec_fock_jk_inc(const double* dd, double* f, double* f_old, const int* n
   int rc;
   if (!g_ctx) rc = NOT_INIT;
   else if (!dd || !f || !f_old || !nbf || !nfocks || !se || !sc) rc = UNSUPPORTED;
-  else if (*nbf != g_ctx->nbf) rc = NOT_INIT;
+  else if (*nbf != g_ctx->nbf || g_ctx->nmol != 1) rc = NOT_INIT;
   else rc = ctx_build_host(g_ctx, dd, f, f_old, *nfocks, *se, *sc);
+  if (info) *info = rc;
+}
+
+int routec_fock_init_batch(int nmol, const int* nshell, const int* natom, const int* am, const int* ncontr,
+                           const int* origin, const double* ex, const double* cc, const int* harmonic,
+                           const double* xyz, double cutoff) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (g_ctx) {
+    ctx_free(g_ctx);
+    g_ctx = nullptr;
+  }
+  return oqpg_create_batch(&g_ctx, nmol, nshell, natom, am, ncontr, origin, ex, cc, harmonic, xyz, cutoff);
+}
+
+void routec_fock_jk_batch(const double* d, double* f, const int* nmol, const int* nfocks, const double* se,
+                          const double* sc, int* info) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!d || !f || !nmol || !nfocks || !se || !sc) rc = UNSUPPORTED;
+  else if (*nmol != g_ctx->nmol) rc = NOT_INIT;
+  else if (*nfocks != 1 && *nfocks != 2) rc = UNSUPPORTED;
+  else {
+    oqpg_ctx* c = g_ctx;
+    const size_t bytes = sizeof(double) * (size_t)c->ntri * *nfocks;
+    rc = OK;
+    if (bytes > c->h_bytes) {
+      if (c->h_in) cudaFreeHost(c->h_in);
+      if (c->h_out) cudaFreeHost(c->h_out);
+      c->h_in = c->h_out = nullptr;
+      c->h_bytes = 0;
+      if (cudaMallocHost(&c->h_in, bytes) != cudaSuccess || cudaMallocHost(&c->h_out, bytes) != cudaSuccess) rc = NO_MEM;
+      else c->h_bytes = bytes;
+    }
+    if (!rc && (c->d_dp.ensure(bytes) != cudaSuccess || c->d_f.ensure(bytes) != cudaSuccess)) rc = NO_MEM;
+    if (!rc) {
+      std::memcpy(c->h_in, d, bytes);
+      if (cudaMemcpyAsync(c->d_dp.p, c->h_in, bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) rc = DEV_ERR;
+    }
+    if (!rc) rc = graph_build(c, c->d_dp.as<double>(), c->d_f.as<double>(), *nfocks, *se, *sc, c->stream);
+    if (!rc) {
+      if (cudaMemcpyAsync(c->h_out, c->d_f.p, bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+          cudaStreamSynchronize(c->stream) != cudaSuccess)
+        rc = DEV_ERR;
+      else
+        std::memcpy(f, c->h_out, bytes);
+    }
+  }
   if (info) *info = rc;
 }
 

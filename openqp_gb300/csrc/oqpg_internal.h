@@ -15,17 +15,30 @@ enum Status { OK = 0, NOT_INIT = 1, NO_MEM = 2, UNSUPPORTED = 3, DEV_ERR = 4 };
 constexpr int NBIN = 64;            // primitive-count bins of the class-list sort
 constexpr int PRIM_SPLIT_LOG2 = 8;  // >= 256 primitive quartets: warp per quartet
 
+// One molecule of a context (a context holds a batch of one or more).  Its
+// shells, pairs and AO rows are contiguous ranges of the context's tables;
+// its matrices are rows [row0, row0 + nbf) of the stacked nrows x stride
+// matrices (columns 0 .. nbf-1); its packed densities / Fock matrices start
+// at nfocks * tri0 of the caller's arrays, one nbf(nbf+1)/2 triangle per density.
+struct MolDev {
+  int nbf, ns, shell0, pair0, npair, row0;
+  long long tri0;  // packed elements (per density) of the molecules before it
+  long long dsh0;  // first element of its ns x ns shell-density block
+};
+
 struct ListArgs {
-  int npair, ns;
-  const int2* pair_ij;      // shells (i >= j) of each pair, canonical order
+  int npair;                // pairs of the whole batch (one CTA each)
+  const MolDev* mols;
+  const int* pair_mol;      // molecule of each pair
+  const int2* pair_ij;      // shells (i >= j, molecule-local) of each pair, canonical order
   const int* pair_type;
   const double* q;          // Schwarz bound per pair
   const float* qf;
-  const int* sorted_idx;    // pairs by descending Schwarz bound
+  const int* sorted_idx;    // per molecule: its pairs by descending Schwarz bound (segment at pair0)
   const double* sorted_q;
-  const double* dsh;
+  const double* dsh;        // per molecule ns x ns blocks at dsh0
   const float* dshf;
-  const unsigned long long* dmax_bits;
+  const unsigned long long* dmax_bits;  // per molecule
   double tau;
   double tau_f32;               // quartets with bound < tau_f32 go to the FP32 lists (0: none)
   unsigned long long* counts;   // 2 NCLASS: FP64 lists, then FP32 lists
@@ -55,47 +68,97 @@ struct DevBuf {
 };
 
 // Build-pipeline kernels (oqpg_host.cu).
-__global__ void k_unpack(const double* __restrict__ dp, int nfocks, int nbf, double* dj, double* dk);
+__global__ void k_unpack(const double* __restrict__ dp, int nfocks, const MolDev* __restrict__ mols,
+                         const int* __restrict__ row_mol, int nrows, int stride, double* dj, double* dk);
 __global__ void k_to_f32(const double* __restrict__ x, long long n, float* y);
-__global__ void k_dsh(const double* __restrict__ dp, int nfocks, int nbf, int ns, const int* __restrict__ aoff,
-                      const int* __restrict__ nao, double* dsh, float* dshf, unsigned long long* dmax_bits);
+__global__ void k_dsh(const double* __restrict__ dp, int nfocks, const MolDev* __restrict__ mols,
+                      const int* __restrict__ pair_mol, const int2* __restrict__ pair_ij, int npair,
+                      const int* __restrict__ aoff, const int* __restrict__ nao, double* dsh, float* dshf,
+                      unsigned long long* dmax_bits);
 __global__ void k_lists(const ListArgs a);
-__global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const PairDev* __restrict__ pairs,
-                           unsigned long long* hist);
-__global__ void k_bin_scatter(const uint2* __restrict__ list, long long n, const PairDev* __restrict__ pairs,
-                              unsigned long long* cursors, uint2* out, long long chunk);
-__global__ void k_finalize(const double* __restrict__ gj, const double* __restrict__ gk, int nk, int nbf, double sc,
-                           double ck, double* f, double* f_old);
+// n entries, or with n_dev the device count min(*n_dev, n) (n is then the capacity)
+__global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const unsigned long long* n_dev,
+                           const PairDev* __restrict__ pairs, unsigned long long* hist);
+__global__ void k_bin_scatter(const uint2* __restrict__ list, long long n, const unsigned long long* n_dev,
+                              const PairDev* __restrict__ pairs, unsigned long long* cursors, uint2* out,
+                              long long chunk, const unsigned* flag);
+__global__ void k_bin_scan(const unsigned long long* counts, const unsigned long long* caps, const int* split_bins,
+                           const unsigned long long* hist, unsigned long long* cursors, unsigned long long* ranges,
+                           unsigned* overflow);
+// (does nothing when *flag != 0: a list overflowed and the build is redone)
+__global__ void k_finalize(const double* __restrict__ gj, const double* __restrict__ gk, int nk,
+                           const MolDev* __restrict__ mols, int nmol, long long ntri_total, int stride,
+                           size_t kstride, double sc, double ck, double* f, double* f_old,
+                           const unsigned* __restrict__ flag);
 void set_band(BuildArgs& a);
 
+constexpr int NLIST = 2 * NCLASS;  // FP64 lists, then the FP32 lists of the precision split
+
+// Per-build device buffers of one build pipeline (a context has one for its
+// direct builds and one owned by its captured graph).
+struct BuildBufs {
+  DevBuf dj, dk, djf, dkf, gj, gk, dsh, dshf, dmax, counts, primc, hist, cursor, work, ranges, caps, split, flag;
+  DevBuf lists[NLIST], slists[NLIST];
+  unsigned long long cap[NLIST] = {0};
+  bool sized = false;
+  unsigned long long* h_rb = nullptr;  // pinned readback: [0] flag, [1, 1+NLIST) counts, then primitive counts
+  void release() {
+    DevBuf* b[] = {&dj, &dk, &djf, &dkf, &gj, &gk, &dsh, &dshf, &dmax, &counts, &primc, &hist, &cursor, &work,
+                   &ranges, &caps, &split, &flag};
+    for (DevBuf* x : b) x->release();
+    for (auto& x : lists) x.release();
+    for (auto& x : slists) x.release();
+    if (h_rb) cudaFreeHost(h_rb);
+    h_rb = nullptr;
+    sized = false;
+    for (auto& x : cap) x = 0;
+  }
+};
+
 }  // namespace oqpg
+
+// Per-class launch parameters picked by the autotuner.
+struct oqpg_tuning {
+  int split_log2[oqpg::NCLASS];  // small classes: quartets with >= 2^k primitive quartets run warp-per-quartet
+  int chunk[oqpg::NCLASS];       // small classes: quartets a warp takes per grab (multiple of 32)
+  int ctas_per_sm[oqpg::NCLASS]; // grid cap per SM (0: as many as fit)
+};
 
 struct oqpg_ctx {
   int dev = 0, nsm = 152;
   cudaStream_t stream = nullptr;
-  int nshell = 0, nbf = 0, natom = 0, npair = 0;
+  // nbf: AO rows of the whole batch (sum over molecules); stride: largest nbf
+  int nshell = 0, nbf = 0, natom = 0, npair = 0, nmol = 1, stride = 0;
+  long long ntri = 0, dsh_elems = 0;  // packed elements per density, shell-density elements (whole batch)
   bool pure = false;
   double tau = 1e-10;
   std::vector<oqpg::ShellDev> shells;
   std::vector<int> aoff, naos;
-  std::vector<double> schwarz_pair;   // per pair (canonical index)
+  std::vector<oqpg::MolDev> mols;
+  std::vector<double> schwarz_pair;   // per pair (canonical index within each molecule, molecules in order)
+  oqpg_tuning tune;
   // precision split: 0 = every quartet in FP64, 1 = bound < tau_f32 in FP32
   int precision_mode = 0;
   double tau_f32 = 0.0;
   // device tables
-  oqpg::DevBuf d_shells, d_pairs, d_prims, d_primsf, d_pair_ij, d_pair_type, d_q, d_qf, d_aoff, d_naos;
-  // per-build buffers
-  oqpg::DevBuf d_dp, d_dj, d_dk, d_djf, d_dkf, d_gj, d_gk, d_f, d_fold, d_dsh, d_dshf, d_dmax, d_counts,
-      d_prim_counter;
-  oqpg::DevBuf d_lists[2 * oqpg::NCLASS], d_slists[2 * oqpg::NCLASS];
-  oqpg::DevBuf d_sorted_idx, d_sorted_q, d_hist, d_cursor, d_work;
-  unsigned long long caps[2 * oqpg::NCLASS] = {0};
-  unsigned long long counts[2 * oqpg::NCLASS] = {0};
-  bool have_caps = false;
+  oqpg::DevBuf d_shells, d_pairs, d_prims, d_primsf, d_pair_ij, d_pair_type, d_q, d_qf, d_aoff, d_naos, d_mols,
+      d_pair_mol, d_row_mol;
+  oqpg::DevBuf d_sorted_idx, d_sorted_q;
+  // per-build buffers: direct builds, and the captured graph's own set
+  oqpg::BuildBufs hb, gb;
+  oqpg::DevBuf d_dp, d_f, d_fold;     // device copies of host-buffer builds
+  unsigned long long counts[oqpg::NLIST] = {0};
   // pinned staging
   double* h_in = nullptr;
   double* h_out = nullptr;
   size_t h_bytes = 0;
+  // captured device-driven build (graph replay)
+  cudaGraphExec_t gexec = nullptr;
+  cudaStream_t gstream = nullptr;
+  int g_nfocks = 0, g_mode = -1;
+  double g_se = 0, g_sc = 0, g_tau32 = 0;
+  oqpg::DevBuf d_gin, d_gout;        // the graph's packed input / output
+  int graph_replays = 0, graph_captures = 0, g_nlaunch = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t evc[oqpg::NCLASS][2] = {};
   double last_stats[10 + 3 * oqpg::NCLASS] = {0};

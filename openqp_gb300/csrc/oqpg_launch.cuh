@@ -6,7 +6,8 @@
 namespace oqpg {
 
 // Persistent launch: as many 128-thread CTAs as fit on the device at once
-// (never more than the work needs); the kernels pull work from a.work.
+// (or a.ctas_per_sm per SM; never more than a.nquartets needs); the kernels
+// pull work from a.work.
 template <typename Kern>
 cudaError_t launch_persistent(Kern kern, size_t smem, long long per_block_items, const BuildArgs& a, int nsm,
                               cudaStream_t st) {
@@ -17,6 +18,7 @@ cudaError_t launch_persistent(Kern kern, size_t smem, long long per_block_items,
   }
   int per_sm = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
+  if (a.ctas_per_sm > 0 && a.ctas_per_sm < per_sm) per_sm = a.ctas_per_sm;
   if (per_sm < 1) per_sm = 1;
   long long blocks = (a.nquartets + per_block_items - 1) / per_block_items;
   const long long cap = (long long)nsm * per_sm;

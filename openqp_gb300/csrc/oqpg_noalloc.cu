@@ -75,6 +75,7 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
                                     double sc, void* stream) {
   if (!c) return NOT_INIT;
   if (nfocks != 1 && nfocks != 2) return UNSUPPORTED;
+  if (c->nmol != 1) return UNSUPPORTED;
   if (c->nbf > NOALLOC_MAX_NBF || c->nshell > NOALLOC_MAX_SHELLS) return NOALLOC_TOO_LARGE;
   void* sp = nullptr;
   if (int rc = scratch_address(&sp)) return rc;
@@ -107,15 +108,19 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
   } while (0)
 
   NK(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), st));
-  k_unpack<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(d_device, nfocks, n, dj, dk);
+  k_unpack<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(d_device, nfocks, c->d_mols.as<MolDev>(),
+                                                         c->d_row_mol.as<int>(), n, n, dj, dk);
   NK(cudaGetLastError());
   const long long npair = c->npair;
-  k_dsh<<<(unsigned)((npair + 127) / 128), 128, 0, st>>>(d_device, nfocks, n, ns, c->d_aoff.as<int>(),
-                                                         c->d_naos.as<int>(), dsh, dshf, dmax);
+  k_dsh<<<(unsigned)((npair + 127) / 128), 128, 0, st>>>(d_device, nfocks, c->d_mols.as<MolDev>(),
+                                                         c->d_pair_mol.as<int>(), c->d_pair_ij.as<int2>(),
+                                                         c->npair, c->d_aoff.as<int>(), c->d_naos.as<int>(), dsh,
+                                                         dshf, dmax);
   NK(cudaGetLastError());
   ListArgs la{};
   la.npair = c->npair;
-  la.ns = ns;
+  la.mols = c->d_mols.as<MolDev>();
+  la.pair_mol = c->d_pair_mol.as<int>();
   la.pair_ij = c->d_pair_ij.as<int2>();
   la.pair_type = c->d_pair_type.as<int>();
   la.q = c->d_q.as<double>();
@@ -148,7 +153,7 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
   NK(cudaMemsetAsync(hist, 0, sizeof(unsigned long long) * NCLASS * NBIN, st));
   for (int k = 0; k < NCLASS; ++k) {
     if (!h_counts[k]) continue;
-    k_bin_hist<<<(unsigned)((h_counts[k] + 255) / 256), 256, 0, st>>>(lists + off[k], (long long)h_counts[k],
+    k_bin_hist<<<(unsigned)((h_counts[k] + 255) / 256), 256, 0, st>>>(lists + off[k], (long long)h_counts[k], nullptr,
                                                                       c->d_pairs.as<PairDev>(), hist + k * NBIN);
     NK(cudaGetLastError());
   }
@@ -165,7 +170,8 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
     if (!h_counts[k]) continue;
     const long long chunk = 4096;
     k_bin_scatter<<<(unsigned)((h_counts[k] + chunk - 1) / chunk), 256, 0, st>>>(
-        lists + off[k], (long long)h_counts[k], c->d_pairs.as<PairDev>(), cursor + k * NBIN, slists + off[k], chunk);
+        lists + off[k], (long long)h_counts[k], nullptr, c->d_pairs.as<PairDev>(), cursor + k * NBIN,
+        slists + off[k], chunk, nullptr);
     NK(cudaGetLastError());
   }
   // integrals and digestion
@@ -178,6 +184,7 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
   a.pairs = c->d_pairs.as<PairDev>();
   a.prims = c->d_prims.as<PrimPair>();
   a.nbf = n;
+  a.kstride = n2;
   a.nk = nk;
   a.prim_cut = 1e-4 * c->tau;
   a.prim_cut2 = a.prim_cut * a.prim_cut;
@@ -209,7 +216,8 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
   }
   const long long ntri = (long long)n * (n + 1) / 2;
   const double ck = (nk == 1) ? 0.5 * se : se;
-  k_finalize<<<(unsigned)((ntri + 255) / 256), 256, 0, st>>>(gj, gk, nk, n, sc, ck, f_device, nullptr);
+  k_finalize<<<(unsigned)((ntri + 255) / 256), 256, 0, st>>>(gj, gk, nk, c->d_mols.as<MolDev>(), 1, ntri, n, n2,
+                                                             sc, ck, f_device, nullptr, nullptr);
   NK(cudaGetLastError());
   NK(cudaStreamSynchronize(st));
 #undef NK

@@ -34,6 +34,15 @@ def _basis_arrays(bas):
             np.ascontiguousarray(bas.xyz.reshape(-1), dtype=np.float64)]
 
 
+def _batch_arrays(bases):
+    """Per-molecule counts and the concatenated basis arrays of a batch."""
+    parts = [_basis_arrays(b) for b in bases]
+    cat = [np.ascontiguousarray(np.concatenate([p[k] for p in parts])) for k in range(7)]
+    nshell = np.array([len(b.am) for b in bases], dtype=np.int32)
+    natom = np.array([b.natom for b in bases], dtype=np.int32)
+    return nshell, natom, cat
+
+
 class FockBuilder:
     """Direct J/K builder for one basis and geometry (one device context)."""
 
@@ -48,8 +57,18 @@ class FockBuilder:
         if rc != 0:
             raise FockError(rc, "oqpg_create")
         self.h = h
-        self.nbf = lib().oqpg_nbf(h)
-        self.ntri = self.nbf * (self.nbf + 1) // 2
+        self._layout()
+
+    def _layout(self):
+        n = lib().oqpg_batch_info(self.h, None, None)
+        nbf = (ctypes.c_int * n)()
+        tri0 = (ctypes.c_longlong * n)()
+        lib().oqpg_batch_info(self.h, nbf, tri0)
+        self.nmol = n
+        self.nbf_mol = [int(v) for v in nbf]
+        self.tri0 = [int(v) for v in tri0]
+        self.nbf = lib().oqpg_nbf(self.h)
+        self.ntri = sum(v * (v + 1) // 2 for v in self.nbf_mol)
 
     def close(self):
         if getattr(self, "h", None):
@@ -89,6 +108,42 @@ class FockBuilder:
             raise FockError(rc, "oqpg_fock_jk_device")
         return out
 
+    def fock_jk_graph(self, d, scale_exch=1.0, scale_coul=1.0, out=None, stream=None):
+        """As fock_jk_device, replayed from the context's captured CUDA graph
+        (captured on the first call; rebuilt and recaptured when needed)."""
+        import torch
+        if not (d.is_cuda and d.dtype == torch.float64 and d.is_contiguous()):
+            raise ValueError("d must be a contiguous float64 CUDA tensor")
+        d2 = d if d.dim() == 2 else d.unsqueeze(0)
+        if out is None:
+            out = torch.empty_like(d2)
+        st = stream if stream is not None else torch.cuda.current_stream(d.device)
+        rc = lib().oqpg_fock_jk_graph(self.h, ctypes.c_void_p(d2.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                      d2.shape[0], float(scale_exch), float(scale_coul),
+                                      ctypes.c_void_p(st.cuda_stream))
+        if rc != 0:
+            raise FockError(rc, "oqpg_fock_jk_graph")
+        return out
+
+    def graph_info(self):
+        c, r, k = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        lib().oqpg_graph_info(self.h, ctypes.byref(c), ctypes.byref(r), ctypes.byref(k))
+        return dict(captures=c.value, replays=r.value, kernels=k.value)
+
+    def set_tuning(self, split_log2=None, chunk=None, ctas_per_sm=None):
+        arrs = [None if v is None else np.ascontiguousarray(v, dtype=np.int32) for v in (split_log2, chunk, ctas_per_sm)]
+        for a in arrs:
+            if a is not None and a.shape != (NCLASS,):
+                raise ValueError("tuning arrays have one entry per class (%d)" % NCLASS)
+        rc = lib().oqpg_set_tuning(self.h, *[None if a is None else ptr(a, _i) for a in arrs])
+        if rc != 0:
+            raise FockError(rc, "oqpg_set_tuning")
+
+    def get_tuning(self):
+        arrs = [np.zeros(NCLASS, dtype=np.int32) for _ in range(3)]
+        lib().oqpg_get_tuning(self.h, *[ptr(a, _i) for a in arrs])
+        return dict(split_log2=arrs[0].tolist(), chunk=arrs[1].tolist(), ctas_per_sm=arrs[2].tolist())
+
     def set_precision(self, mode, threshold=1e-6):
         """mode "fp64": plain path; mode "mixed": quartets whose screening value
         (Schwarz bound x shell density) is below threshold run in FP32 with their
@@ -115,6 +170,51 @@ class FockBuilder:
                     ms_per_class=[float(v) for v in s[7 + 2 * NCLASS:7 + 3 * NCLASS]],
                     launches=int(s[7 + 3 * NCLASS]), f32_quartets=int(s[8 + 3 * NCLASS]),
                     f32_prim_quartets=int(s[9 + 3 * NCLASS]))
+
+
+class BatchFockBuilder(FockBuilder):
+    """One context over many molecules: every build builds all of them (one
+    launch per class for the whole batch).  Matrices go in and out as the
+    molecules' packed blocks one after the other; pack / unpack convert from and
+    to lists of per-molecule (nfocks, ntri_m) arrays."""
+
+    def __init__(self, bases, cutoff=1e-10):
+        self.bases = list(bases)
+        self.cutoff = cutoff
+        nshell, natom, k = _batch_arrays(self.bases)
+        self._keep = (nshell, natom, k)
+        h = ctypes.c_void_p()
+        rc = lib().oqpg_create_batch(ctypes.byref(h), len(self.bases), ptr(nshell, _i), ptr(natom, _i),
+                                     ptr(k[0], _i), ptr(k[1], _i), ptr(k[2], _i), ptr(k[3]), ptr(k[4]), ptr(k[5], _i),
+                                     ptr(k[6]), float(cutoff))
+        if rc != 0:
+            raise FockError(rc, "oqpg_create_batch")
+        self.h = h
+        self._layout()
+
+    def pack(self, ds):
+        """List of per-molecule (nfocks, ntri_m) densities -> (ntotal,) vector."""
+        return np.ascontiguousarray(np.concatenate([np.atleast_2d(d).reshape(-1) for d in ds]))
+
+    def unpack(self, flat, nfocks=1):
+        out = []
+        for m, n in enumerate(self.nbf_mol):
+            t = n * (n + 1) // 2
+            o = nfocks * self.tri0[m]
+            out.append(np.asarray(flat[o:o + nfocks * t]).reshape(nfocks, t))
+        return out
+
+    def fock_jk(self, ds, scale_exch=1.0, scale_coul=1.0):
+        """ds: list of per-molecule densities -> list of packed Fock matrices."""
+        nfocks = np.atleast_2d(ds[0]).shape[0]
+        d = self.pack(ds)
+        if d.size != nfocks * self.ntri:
+            raise ValueError("densities do not match the batch")
+        f = np.empty_like(d)
+        rc = lib().oqpg_fock_jk(self.h, ptr(d), ptr(f), nfocks, float(scale_exch), float(scale_coul))
+        if rc != 0:
+            raise FockError(rc, "oqpg_fock_jk")
+        return self.unpack(f, nfocks)
 
 
 def fp64_peak_tflops(iters=20000):

@@ -124,3 +124,25 @@ def water_cluster_basis(nwater, edge, seed, basis="6-31g(d)", spherical=None):
 
 def nelectrons(bas, charge=0):
     return int(round(bas.charges.sum())) - charge
+
+
+def water_batch(nclusters, seed, nmin=1, nmax=16, basis="6-31g", overlap=None):
+    """Batch of seeded water clusters of uneven size: n ~ U{nmin..nmax} waters
+    each, placed in a cube whose edge keeps the number density of four waters
+    in a 6 A cube.  Returns (sizes, bases, packed RHF densities); the overlap
+    for each Loewdin step comes from overlap(bas), by default the library's
+    host routine."""
+    if overlap is None:
+        from .onee import one_electron
+
+        def overlap(b):
+            return one_electron(b)[0]
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(nmin, nmax + 1, nclusters)
+    bases, dens = [], []
+    for k, n in enumerate(sizes):
+        bas = water_cluster_basis(int(n), cube_edge_like_c1(int(n)), seed * 100003 + k, basis)
+        S = overlap(bas)
+        bases.append(bas)
+        dens.append(density(bas, nelectrons(bas) // 2, seed * 100003 + k, S=S))
+    return [int(v) for v in sizes], bases, dens
