@@ -52,7 +52,8 @@ class DIIS:
 
 def run_scf(nbf, S, H, enuc, nalpha, nbeta, fock2e, kind="rhf", conv=1e-9, maxit=100, incremental=False,
             refresh=10, refresh_err=1e-4, dconv=1e-7, guess=None, log=None):
-    """Returns dict(energy, iterations, D (packed, per spin), F, builds)."""
+    """Returns dict(energy, iterations, D (packed, per spin), F (packed 2e part),
+    builds, C (alpha, beta orbitals of D), Fock (full AO Fock matrices of D))."""
     w, U = np.linalg.eigh(S)
     X = U / np.sqrt(w)
     Hp = pack(H)
@@ -74,6 +75,7 @@ def run_scf(nbf, S, H, enuc, nalpha, nbeta, fock2e, kind="rhf", conv=1e-9, maxit
         return [Ca[:, :nalpha] @ Ca[:, :nalpha].T, Cb[:, :nbeta] @ Cb[:, :nbeta].T]
 
     Dm = dens(Ca, Cb)
+    Cc = (Ca, Cb)   # orbitals of the current density
     diis = DIIS()
     e_old = 0.0
     Gp_prev = None
@@ -130,7 +132,34 @@ def run_scf(nbf, S, H, enuc, nalpha, nbeta, fock2e, kind="rhf", conv=1e-9, maxit
             log("iter %3d  E = %.12f  dE = %.3e  err = %.3e  %s" % (it, E, E - e_old, err_norm,
                                                                    "full" if full else "inc"))
         if abs(E - e_old) < conv and err_norm < 1e-6 and dD < dconv:
-            return dict(energy=E, iterations=it, D=Dp, F=Gp, builds=builds, converged=True)
+            return dict(energy=E, iterations=it, D=Dp, F=Gp, builds=builds, converged=True, C=Cc, Fock=Fs)
         e_old = E
         Dm = Dm_new
-    return dict(energy=E, iterations=maxit, D=Dp, F=Gp, builds=builds, converged=False)
+        Cc = (Ca, Cb)
+    return dict(energy=E, iterations=maxit, D=Dp, F=Gp, builds=builds, converged=False, C=Cc, Fock=Fs)
+
+
+def energy_weighted_density(res, nalpha, nbeta, kind="rhf"):
+    """W of the gradient's overlap term, -sum W dS/dR, for the orbitals of a
+    converged run: W = C lam C^T with the orbital Lagrangian
+    lam_pq = (C^T Fa C)_pq n^a_q + (C^T Fb C)_pq n^b_q (symmetrised).  For
+    RHF / UHF canonical orbitals this is sum_occ eps c c^T per spin."""
+    Ca, Cb = res["C"]
+    Fs = res["Fock"]
+    if kind == "rhf":
+        Fa = Fb = Fs[0]
+    else:
+        Fa, Fb = Fs
+    n = Ca.shape[1]
+    na = np.zeros(n)
+    na[:nalpha] = 1.0
+    nb_ = np.zeros(n)
+    nb_[:nbeta] = 1.0
+    if kind == "uhf":
+        Wa = (Ca * na) @ (Ca.T @ Fa @ Ca) @ (Ca * na).T
+        Wb = (Cb * nb_) @ (Cb.T @ Fb @ Cb) @ (Cb * nb_).T
+        return Wa + Wb
+    C = Ca
+    lam = (C.T @ Fa @ C) * na[None, :] + (C.T @ Fb @ C) * nb_[None, :]
+    lam = 0.5 * (lam + lam.T)
+    return C @ lam @ C.T

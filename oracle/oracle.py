@@ -46,6 +46,10 @@ def lib():
         L.orc_one_electron.argtypes = [ctypes.c_void_p, ctypes.c_int, _d, _d]
         L.orc_rys.argtypes = [ctypes.c_int, ctypes.c_double, _d, _d]
         L.orc_boys.argtypes = [ctypes.c_int, ctypes.c_double, _d]
+        L.orc_grad2e.restype = ctypes.c_longlong
+        L.orc_grad2e.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_int, _d]
+        L.orc_grad1e.argtypes = [ctypes.c_void_p, _d, _d, _d, _d]
         _lib = L
     return _lib
 
@@ -147,6 +151,40 @@ class Oracle:
         z = np.ascontiguousarray(self.bas.charges if charges is None else charges, dtype=np.float64)
         lib().orc_one_electron(self.h, {"S": 0, "T": 1, "V": 2}[which], _p(z), _p(out))
         return out.reshape(n, n)
+
+
+    def grad2e(self, dt, ds=None, coulscale=1.0, hfscale=1.0, cutoff=1e-10, nthreads=None):
+        """Two-electron HF gradient (natom, 3) of OpenQP's grd2 for the full AO
+        total density dt (and spin density ds for UHF/ROHF)."""
+        n = self.nbf
+        dt = np.ascontiguousarray(dt, dtype=np.float64).reshape(n, n)
+        dsp = None if ds is None else np.ascontiguousarray(ds, dtype=np.float64).reshape(n, n)
+        de = np.zeros(3 * self.bas.natom)
+        nt = nthreads or os.cpu_count()
+        nq = lib().orc_grad2e(self.h, _p(dt), None if dsp is None else _p(dsp), 4.0 * coulscale, hfscale, cutoff,
+                              nt, _p(de))
+        self.last_grad2e_quartets = int(nq)
+        return de.reshape(-1, 3)
+
+    def grad1e(self, d, w, charges=None):
+        """One-electron gradient (natom, 3): sum D dH/dR - W dS/dR."""
+        n = self.nbf
+        d = np.ascontiguousarray(d, dtype=np.float64).reshape(n, n)
+        w = np.ascontiguousarray(w, dtype=np.float64).reshape(n, n)
+        z = np.ascontiguousarray(self.bas.charges if charges is None else charges, dtype=np.float64)
+        de = np.zeros(3 * self.bas.natom)
+        lib().orc_grad1e(self.h, _p(d), _p(w), _p(z), _p(de))
+        return de.reshape(-1, 3)
+
+
+def nuclear_repulsion_gradient(bas):
+    g = np.zeros((bas.natom, 3))
+    for i in range(bas.natom):
+        for j in range(bas.natom):
+            if i != j:
+                r = bas.xyz[i] - bas.xyz[j]
+                g[i] -= bas.charges[i] * bas.charges[j] * r / np.linalg.norm(r) ** 3
+    return g
 
 
 def rys(n, X):

@@ -92,3 +92,67 @@ def test_golden_hf_energy(oracle_lib, case):
                     lambda d: o.fock_jk(d, urohf=(kind != "rhf")), kind=kind, conv=1e-11)
     assert r["converged"]
     assert abs(r["energy"] - case["energy"]) < 1e-7
+
+
+def _scf_case(oracle_lib, case, conv=1e-11):
+    from openqp_gb300 import onee, scf
+    from openqp_gb300.basis import build_basis
+    bas = build_basis(case["atoms"], np.array(case["coord_bohr"]).reshape(-1, 3), case["basis"])
+    o = oracle_lib.Oracle(bas, cutoff=1e-10)
+    S, T = onee.overlap_kinetic(bas)
+    H = T + onee.nuclear(bas)
+    nel = int(sum(case["atoms"]))
+    nunp = case["multiplicity"] - 1
+    na, nb = (nel + nunp) // 2, (nel - nunp) // 2
+    kind = case["scf"]
+    r = scf.run_scf(o.nbf, S, H, onee.nuclear_repulsion(bas), na, nb,
+                    lambda d: o.fock_jk(d, urohf=(kind != "rhf")), kind=kind, conv=conv, dconv=1e-9)
+    assert r["converged"]
+    return bas, o, r, na, nb, kind
+
+
+@pytest.mark.parametrize("case", [c for c in GOLD if "GRADIENT" in c["source"]], ids=lambda c: c["source"].split("/")[-1])
+def test_golden_hf_gradient(oracle_lib, case):
+    """OpenQP's example gradients: nuclear repulsion + one-electron part (oracle
+    grad1e) + two-electron part (the grd2 restatement, oracle grad2e)."""
+    from openqp_gb300 import scf
+    from openqp_gb300.basis import unpack
+    bas, o, r, na, nb, kind = _scf_case(oracle_lib, case)
+    n = bas.nbf
+    Ds = [unpack(d, n) for d in r["D"]]
+    if kind == "rhf":
+        Dt, Dsp = Ds[0], None
+    else:
+        Dt, Dsp = Ds[0] + Ds[1], Ds[0] - Ds[1]
+    W = scf.energy_weighted_density(r, na, nb, kind)
+    g = oracle_lib.nuclear_repulsion_gradient(bas) + o.grad1e(Dt, W) + o.grad2e(Dt, Dsp)
+    ref = np.array(case["grad"]).reshape(-1, 3)
+    assert np.abs(g - ref).max() < 2e-7
+    assert np.abs(g.sum(axis=0)).max() < 1e-9   # translational invariance
+
+
+def test_grad2e_matches_finite_difference_of_e2(oracle_lib):
+    """At a fixed AO density, dE2/dR of E2 = 1/2 Tr D G(D) (the two-electron
+    energy) by central differences (h = 1e-4 Bohr) against the grd2 restatement."""
+    from openqp_gb300 import workloads
+    from openqp_gb300.basis import unpack
+    bas = workloads.water_cluster_basis(2, 4.0, seed=3, basis="6-31g*")
+    d = workloads.density(bas, 10, 3)
+    n = bas.nbf
+    D = unpack(d, n)
+    o = oracle_lib.Oracle(bas)
+    g = o.grad2e(D)
+
+    def e2(xyz):
+        ob = oracle_lib.Oracle(bas.with_geometry(xyz))
+        f = ob.fock_jk(d)[0]
+        return 0.5 * np.sum(D * unpack(f, n))
+
+    h = 1e-4
+    for at, x in ((0, 2), (1, 0), (4, 1)):
+        xp = bas.xyz.copy()
+        xp[at, x] += h
+        xm = bas.xyz.copy()
+        xm[at, x] -= h
+        fd = (e2(xp) - e2(xm)) / (2 * h)
+        assert abs(fd - g[at, x]) < 2e-7, (at, x, fd, g[at, x])
