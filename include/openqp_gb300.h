@@ -77,6 +77,15 @@ void routec_fock_jk_batch(const double* d, double* f, const int* nmol, const int
  * (see oqpg_set_precision).  No counterpart in the reference seam. */
 int routec_fock_set_precision(int mode, double threshold);
 
+/* The reference's 2e-gradient seam (source/modules/routec_bridge.F90:51-61,
+ * 241, 292-310; caller source/modules/hf_gradient.F90:270-289): d is the
+ * packed total RHF density, xyz(3, natm) in Bohr must be the geometry
+ * registered by routec_fock_init, de(3, natm) is ACCUMULATED with dE2e/dR
+ * (Coulomb scaled by coulscale, exchange by hfscale).  All arguments by
+ * reference.  Declines (info = 1) for another basis or geometry. */
+void routec_grad2(const double* d, const double* xyz, double* de, const int* nbf, const int* natm,
+                  const double* hfscale, const double* coulscale, int* info);
+
 /* Release the process-global context. */
 void routec_fock_finalize(void);
 
@@ -193,6 +202,29 @@ int oqpg_stats(const oqpg_ctx* ctx, double* out, int n);
 int oqpg_one_electron(int nshell, const int* am, const int* ncontr, const int* origin, const double* ex,
                       const double* cc, const int* harmonic, int natom, const double* xyz, const double* charges,
                       int which, double* out);
+
+/* Two-electron HF gradient of a single-molecule context, accumulated into
+ * de[3*natom]: OpenQP's grd2 (source/integrals/grd2.F90:145-391) for the
+ * packed densities d (nfocks = 1: total RHF density; nfocks = 2: alpha and
+ * beta), two-particle density 4 coulscale D_ij D_kl - hfscale (D_ik D_jl +
+ * D_il D_jk [+ spin-density terms]) (source/modules/hf_gradient.F90:427-575),
+ * with its screens and cutoffs.  Derivative ERIs up to (fd|dd) on the GPU,
+ * contracted on the fly, nothing stored. */
+int oqpg_grad2(oqpg_ctx* ctx, const double* d, int nfocks, double hfscale, double coulscale, double* de);
+
+/* The same contraction for a general symmetric bilinear two-particle density
+ * of full nbf x nbf AO matrices (row-major):
+ *   G = cj sym(X_ab Y_cd) - ckt sym(X_ac Y_bd + X_ad Y_bc) - cks (spin pair xs, ys),
+ * sym = average over exchanging X and Y; xs/ys both null or both set.  With
+ * X = Y = D it is the energy gradient; with X = the upstream matrix of a
+ * Fock build and Y = D it is the geometry part of that build's adjoint.  No
+ * counterpart in the reference. */
+int oqpg_grad2_bilinear(oqpg_ctx* ctx, const double* x, const double* y, const double* xs, const double* ys,
+                        double cj, double ckt, double cks, double* de);
+
+/* Statistics of the last gradient: [0] quartets listed, [1] quartets
+ * evaluated, [2] primitive quartets, [3] ms (lists + kernels). */
+int oqpg_grad_stats(const oqpg_ctx* ctx, double* out, int n);
 
 /* Angular momenta (la, lb, lc, ld) of class c (0 <= c < 21). */
 int oqpg_class_l(int c, int* l4);

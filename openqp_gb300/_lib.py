@@ -61,6 +61,12 @@ def lib():
         L.routec_fock_init_batch.argtypes = [ctypes.c_int, _i, _i, _i, _i, _i, _d, _d, _i, _d, ctypes.c_double]
         L.routec_fock_jk_batch.argtypes = [_d, _d, _i, _i, _d, _d, _i]
         L.routec_fock_jk_batch.restype = None
+        L.oqpg_grad2.argtypes = [ctypes.c_void_p, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double, _d]
+        L.oqpg_grad2_bilinear.argtypes = [ctypes.c_void_p, _d, _d, _d, _d, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double, _d]
+        L.oqpg_grad_stats.argtypes = [ctypes.c_void_p, _d, ctypes.c_int]
+        L.routec_grad2.argtypes = [_d, _d, _d, _i, _i, _d, _d, _i]
+        L.routec_grad2.restype = None
         L.oqpg_one_electron.argtypes = [ctypes.c_int, _i, _i, _i, _d, _d, _i, ctypes.c_int, _d, _d, ctypes.c_int, _d]
         _lib = L
     return _lib

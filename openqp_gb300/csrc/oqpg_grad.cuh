@@ -1,0 +1,432 @@
+// Derivative-ERI kernels of the two-electron HF gradient, contracted on the
+// fly with the two-particle density (nothing is stored).
+//
+// For a canonical shell quartet (ab|cd) in kernel orientation the kernels
+// accumulate dE/dR for the centres A, B and C,
+//   g_X = f sum_e Gamma_e d(ab|cd)_e / dX,
+// and D follows from translational invariance, g_D = -(g_A + g_B + g_C).
+// f halves for A = B, C = D and AB = CD (OpenQP grd2_rys.F90:1333-1346).
+// The derivatives use the Gaussian rule d/dA_x phi_a = 2 alpha phi_{a+1x} -
+// a_x phi_{a-1x} (grd2_rys.F90:848-868) on one Rys 2D table per root and
+// dimension in which A and C are raised by one:
+//   dA = 2 a I(a+1,b,c,d) - a_x I(a-1,b,c,d)
+//   dB = 2 b [I(a+1,b,c,d) + (A-B) I(a,b,c,d)] - b_x I(a,b-1,c,d)   (HRR)
+//   dC = 2 c I(a,b,c+1,d) - c_x I(a,b,c-1,d)
+// The entries with both A and C raised are never used, so the root count of
+// one raised shell suffices: NR = (la+lb+lc+ld+1)/2 + 1.
+//
+// The two-particle density is the symmetric bilinear form of OpenQP's
+// get_density (source/modules/hf_gradient.F90:427-575),
+//   Gamma = cj sym(X_ab Y_cd) - ckt sym(X_ac Y_bd + X_ad Y_bc) - cks (same with the spin pair)
+// over Cartesian-effective matrices (AO density projected to Cartesian
+// components with their norms folded in); X = Y = D gives the energy
+// gradient, X != Y the geometry part of the adjoint of a Fock build.
+//
+//   k_grad_lane : small classes; one warp per quartet, the lanes split the
+//                 primitive quartets, each lane keeps its 2D tables in registers.
+//   k_grad_team : larger classes; one warp per quartet, the tables of each
+//                 primitive quartet go to shared memory (one root x dimension
+//                 per lane), derivative tables are built by all lanes, each
+//                 lane contracts its own Cartesian elements.
+#pragma once
+#include "oqpg_eri.cuh"
+
+namespace oqpg {
+
+struct GradArgs {
+  const ShellDev* shells;
+  const PairDev* pairs;     // same pair order as the Fock tables
+  const PrimPair* prims;    // primitive pairs with OpenQP's gradient cutoffs
+  const double* alpha;      // exponent of the pair's first shell, per primitive pair
+  const uint2* quartets;
+  long long nquartets;
+  unsigned long long* work;
+  const double* xt;         // Cartesian-effective matrices, ncart x ncart
+  const double* yt;
+  const double* xs;         // spin pair (null: none)
+  const double* ys;
+  int ncart;
+  const int* coff;          // Cartesian offset of each shell
+  const int* atom;          // atom of each shell
+  double cj, ckt, cks;
+  int pure;                 // screening value from the Cartesian-effective (pure) or AO (Cartesian) density
+  const double* q;          // Schwarz bound per pair
+  double cutoff2;           // quartet skipped if dabmax Q_P Q_Q < cutoff / 2
+  double dtol2;             // (sp sq)^2 < dtol2 (p + q): primitive quartet skipped
+  double dabcut2;           // (sp sq)^2 dabmax^2 < dabcut2 (p + q): skipped
+  double* de;               // 3 x natom, accumulated
+  unsigned long long* counters;  // [0] primitive quartets evaluated, [1] quartets evaluated
+  int ctas_per_sm;
+};
+
+template <int LA, int LB, int LC, int LD>
+struct GCls {
+  using K = Cls<LA, LB, LC, LD>;
+  static constexpr int NR = (LA + LB + LC + LD + 1) / 2 + 1;
+  static constexpr int N2D = K::N2D;
+  static constexpr int N2DX = (LA + 2) * (LB + 1) * (LC + 2) * (LD + 1);
+  static constexpr int SA = (LB + 1) * (LC + 2) * (LD + 1), SB = (LC + 2) * (LD + 1), SC = LD + 1;
+  __host__ __device__ static constexpr int ia(int e) { return e / (K::NB * K::NC * K::ND); }
+  __host__ __device__ static constexpr int ib(int e) { return (e / (K::NC * K::ND)) % K::NB; }
+  __host__ __device__ static constexpr int ic(int e) { return (e / K::ND) % K::NC; }
+  __host__ __device__ static constexpr int id(int e) { return e % K::ND; }
+  // offset of element e along dim in the extended (A, C raised) table
+  __host__ __device__ static constexpr int xoff(int e, int dim) {
+    return ((cart_e(LA, ia(e), dim) * (LB + 1) + cart_e(LB, ib(e), dim)) * (LC + 2) + cart_e(LC, ic(e), dim)) *
+               (LD + 1) + cart_e(LD, id(e), dim);
+  }
+};
+
+// Two-particle density of Cartesian element (ra, rb, rc, rd) (matrix rows /
+// columns in the Cartesian layout).
+__device__ __forceinline__ double gamma_elem(const GradArgs& g, int ra, int rb, int rc, int rd) {
+  const int n = g.ncart;
+  auto X = [&](const double* M, int r, int c) { return __ldg(M + (size_t)r * n + c); };
+  double v = 0.5 * g.cj * (X(g.xt, ra, rb) * X(g.yt, rc, rd) + X(g.yt, ra, rb) * X(g.xt, rc, rd));
+  v -= 0.5 * g.ckt * (X(g.xt, ra, rc) * X(g.yt, rb, rd) + X(g.yt, ra, rc) * X(g.xt, rb, rd) +
+                      X(g.xt, ra, rd) * X(g.yt, rb, rc) + X(g.yt, ra, rd) * X(g.xt, rb, rc));
+  if (g.xs)
+    v -= 0.5 * g.cks * (X(g.xs, ra, rc) * X(g.ys, rb, rd) + X(g.ys, ra, rc) * X(g.xs, rb, rd) +
+                        X(g.xs, ra, rd) * X(g.ys, rb, rc) + X(g.ys, ra, rd) * X(g.xs, rb, rc));
+  return v;
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, s));
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+  return v;
+}
+
+// Reduce the lanes' 9 partial sums (A, B, C x xyz), apply f, add to de.
+__device__ __forceinline__ void grad_store(const GradArgs& g, const PairDev& P, const PairDev& Q, uint2 qd,
+                                           double* acc, int lane) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) acc[k] = warp_sum(acc[k]);
+  if (lane == 0) {
+    double f = 1.0;
+    if (P.sha == P.shb) f *= 0.5;
+    if (Q.sha == Q.shb) f *= 0.5;
+    if (qd.x == qd.y) f *= 0.5;
+    const int at[4] = {__ldg(g.atom + P.sha), __ldg(g.atom + P.shb), __ldg(g.atom + Q.sha), __ldg(g.atom + Q.shb)};
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      const double a = f * acc[x], b = f * acc[3 + x], c = f * acc[6 + x];
+      atomicAdd(g.de + 3 * at[0] + x, a);
+      atomicAdd(g.de + 3 * at[1] + x, b);
+      atomicAdd(g.de + 3 * at[2] + x, c);
+      atomicAdd(g.de + 3 * at[3] + x, -(a + b + c));
+    }
+  }
+}
+
+template <int LA, int LB, int LC, int LD>
+__device__ __forceinline__ void quartet_setup(const GradArgs& g, uint2 qd, PairDev& P, PairDev& Q, double AB[3],
+                                              double CD[3], int ro[4]) {
+  P = g.pairs[qd.x];
+  Q = g.pairs[qd.y];
+  const ShellDev SA = g.shells[P.sha], SB = g.shells[P.shb], SC = g.shells[Q.sha], SD = g.shells[Q.shb];
+  AB[0] = SA.x - SB.x; AB[1] = SA.y - SB.y; AB[2] = SA.z - SB.z;
+  CD[0] = SC.x - SD.x; CD[1] = SC.y - SD.y; CD[2] = SC.z - SD.z;
+  ro[0] = __ldg(g.coff + P.sha); ro[1] = __ldg(g.coff + P.shb);
+  ro[2] = __ldg(g.coff + Q.sha); ro[3] = __ldg(g.coff + Q.shb);
+}
+
+// ---------------------------------------------------------------------------
+template <int LA, int LB, int LC, int LD>
+__global__ void __launch_bounds__(128) k_grad_lane(const GradArgs g) {
+  using K = Cls<LA, LB, LC, LD>;
+  using G = GCls<LA, LB, LC, LD>;
+  constexpr int NE = K::NE, NR = G::NR, N2DX = G::N2DX;
+  __shared__ double s_gam[4][NE];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double* gam = s_gam[warp];
+  unsigned long long nprim = 0, nq = 0;
+  for (;;) {
+    const long long t = grab(g.work, 1u, lane);
+    if (t >= g.nquartets) break;
+    const uint2 qd = g.quartets[t];
+    PairDev P, Q;
+    double AB[3], CD[3];
+    int ro[4];
+    quartet_setup<LA, LB, LC, LD>(g, qd, P, Q, AB, CD, ro);
+    double dmx = 0.0;
+    for (int e = lane; e < NE; e += 32) {
+      const double v = gamma_elem(g, ro[0] + G::ia(e), ro[1] + G::ib(e), ro[2] + G::ic(e), ro[3] + G::id(e));
+      gam[e] = v;
+      const double nrm = cart_norm(LA, G::ia(e)) * cart_norm(LB, G::ib(e)) * cart_norm(LC, G::ic(e)) *
+                         cart_norm(LD, G::id(e));
+      dmx = fmax(dmx, g.pure ? fabs(v) : fabs(v) / nrm);
+    }
+    const double dabmax = warp_max(dmx);
+    __syncwarp();
+    if (dabmax * __ldg(g.q + qd.x) * __ldg(g.q + qd.y) < g.cutoff2) continue;
+    ++nq;
+    double acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+    const int nP = P.pcnt, nQ = Q.pcnt;
+    for (int pq = lane; pq < nP * nQ; pq += 32) {
+      const int kq = pq / nP, kb = pq - kq * nP;
+      PrimPair bp, kp;
+      prim_load(g.prims + P.poff + kb, bp);
+      prim_load(g.prims + Q.poff + kq, kp);
+      const double pfac = bp.sp * kp.sp, test = pfac * pfac, s = bp.p + kp.p;
+      if (test < g.dtol2 * s || test * dabmax * dabmax < g.dabcut2 * s) continue;
+      ++nprim;
+      PrimQuartet<double> pqd;
+      prim_setup<double>(bp, kp, pqd);
+      const double a2 = 2.0 * __ldg(g.alpha + P.poff + kb);
+      const double b2 = 2.0 * bp.p - a2;
+      const double c2 = 2.0 * __ldg(g.alpha + Q.poff + kq);
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const double u = rys_quantity<NR, double>(pqd.X, 2 * r);
+        const double w = rys_quantity<NR, double>(pqd.X, 2 * r + 1) * pqd.pref;
+        const double uq = u * pqd.qi, up = u * pqd.pi;
+        const double b00 = 0.5 * pqd.inv * u;
+        const double b10 = fma(-bp.hp, uq, bp.hp);
+        const double b01 = fma(-kp.hp, up, kp.hp);
+        double X[3][N2DX];
+        const double PA[3] = {bp.ax, bp.ay, bp.az}, QC[3] = {kp.ax, kp.ay, kp.az};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const double c00 = fma(-uq, pqd.PQ[d], PA[d]);
+          const double d00 = fma(up, pqd.PQ[d], QC[d]);
+          twod<LA + 1, LB, LC + 1, LD, double>(d == 2 ? w : 1.0, c00, d00, b00, b10, b01, AB[d], CD[d],
+                                               [&](int i, double v) { X[d][i] = v; });
+        }
+#pragma unroll
+        for (int e = 0; e < NE; ++e) {
+          double I[3], dA[3], dB[3], dC[3];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const int o = G::xoff(e, d);
+            const int ea = cart_e(LA, G::ia(e), d), eb = cart_e(LB, G::ib(e), d), ec = cart_e(LC, G::ic(e), d);
+            I[d] = X[d][o];
+            const double up1 = X[d][o + G::SA];
+            dA[d] = a2 * up1;
+            if (ea > 0) dA[d] = fma(-(double)ea, X[d][o - G::SA], dA[d]);
+            dB[d] = b2 * fma(AB[d], I[d], up1);
+            if (eb > 0) dB[d] = fma(-(double)eb, X[d][o - G::SB], dB[d]);
+            dC[d] = c2 * X[d][o + G::SC];
+            if (ec > 0) dC[d] = fma(-(double)ec, X[d][o - G::SC], dC[d]);
+          }
+          const double ge = gam[e];
+          const double tz = ge * I[2];
+          const double yz = I[1] * tz, xz = I[0] * tz, xy = I[0] * I[1] * ge;
+          acc[0] = fma(dA[0], yz, acc[0]); acc[1] = fma(dA[1], xz, acc[1]); acc[2] = fma(dA[2], xy, acc[2]);
+          acc[3] = fma(dB[0], yz, acc[3]); acc[4] = fma(dB[1], xz, acc[4]); acc[5] = fma(dB[2], xy, acc[5]);
+          acc[6] = fma(dC[0], yz, acc[6]); acc[7] = fma(dC[1], xz, acc[7]); acc[8] = fma(dC[2], xy, acc[8]);
+        }
+      }
+    }
+    grad_store(g, P, Q, qd, acc, lane);
+    __syncwarp();
+  }
+  if (g.counters) {
+    if (nprim) atomicAdd(g.counters, nprim);
+    if (lane == 0 && nq) atomicAdd(g.counters + 1, nq);
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <int LA, int LB, int LC, int LD>
+struct GradTeamSmem {
+  using G = GCls<LA, LB, LC, LD>;
+  static constexpr int RT = 2 * G::NR;
+  static constexpr int XT = 3 * G::NR * G::N2DX;
+  static constexpr int TT = 3 * G::NR * 4 * G::N2D;   // per root x dim: I, dA, dB, dC
+  static constexpr int PER_WARP = RT + XT + TT;       // doubles
+};
+
+template <int LA, int LB, int LC, int LD>
+__global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
+  using K = Cls<LA, LB, LC, LD>;
+  using G = GCls<LA, LB, LC, LD>;
+  using SM = GradTeamSmem<LA, LB, LC, LD>;
+  constexpr int NE = K::NE, NR = G::NR, N2D = G::N2D, N2DX = G::N2DX, KE = (NE + 31) / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double* W = reinterpret_cast<double*>(smem_raw) + (size_t)warp * SM::PER_WARP;
+  double* RT = W;
+  double* XT = W + SM::RT;
+  double* TT = XT + SM::XT;
+  // this lane's elements: packed offsets into the per-dim tables
+  int offs[KE];
+#pragma unroll
+  for (int k = 0; k < KE; ++k) {
+    const int e = lane + 32 * k;
+    int o = 0;
+    if (e < NE) {
+      int ox[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) ox[d] = K::off2d(e, d);
+      o = ox[0] | (ox[1] << 10) | (ox[2] << 20);
+    }
+    offs[k] = o;
+  }
+  unsigned long long nprim = 0, nq = 0;
+  for (;;) {
+    const long long t = grab(g.work, 1u, lane);
+    if (t >= g.nquartets) break;
+    const uint2 qd = g.quartets[t];
+    PairDev P, Q;
+    double AB[3], CD[3];
+    int ro[4];
+    quartet_setup<LA, LB, LC, LD>(g, qd, P, Q, AB, CD, ro);
+    double gam[KE];
+    double dmx = 0.0;
+#pragma unroll
+    for (int k = 0; k < KE; ++k) {
+      const int e = lane + 32 * k;
+      gam[k] = 0.0;
+      if (e < NE) {
+        const double v = gamma_elem(g, ro[0] + G::ia(e), ro[1] + G::ib(e), ro[2] + G::ic(e), ro[3] + G::id(e));
+        gam[k] = v;
+        const double nrm = cart_norm(LA, G::ia(e)) * cart_norm(LB, G::ib(e)) * cart_norm(LC, G::ic(e)) *
+                           cart_norm(LD, G::id(e));
+        dmx = fmax(dmx, g.pure ? fabs(v) : fabs(v) / nrm);
+      }
+    }
+    const double dabmax = warp_max(dmx);
+    if (dabmax * __ldg(g.q + qd.x) * __ldg(g.q + qd.y) < g.cutoff2) continue;
+    ++nq;
+    double acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+    for (int kq = 0; kq < Q.pcnt; ++kq) {
+      PrimPair kp;
+      prim_load(g.prims + Q.poff + kq, kp);
+      const double c2 = 2.0 * __ldg(g.alpha + Q.poff + kq);
+      for (int kb = 0; kb < P.pcnt; ++kb) {
+        PrimPair bp;
+        prim_load(g.prims + P.poff + kb, bp);
+        const double pfac = bp.sp * kp.sp, test = pfac * pfac, s = bp.p + kp.p;
+        if (test < g.dtol2 * s || test * dabmax * dabmax < g.dabcut2 * s) continue;
+        ++nprim;
+        PrimQuartet<double> pqd;
+        prim_setup<double>(bp, kp, pqd);
+        const double a2 = 2.0 * __ldg(g.alpha + P.poff + kb);
+        const double b2 = 2.0 * bp.p - a2;
+        if (lane < 2 * NR) {
+          const double v = rys_quantity<NR, double>(pqd.X, lane);
+          RT[lane] = (lane & 1) ? v * pqd.pref : v;
+        }
+        __syncwarp();
+        if (lane < 3 * NR) {
+          const int r = lane / 3, d = lane - 3 * r;
+          const double u = RT[2 * r], w = RT[2 * r + 1];
+          const double uq = u * pqd.qi, up = u * pqd.pi;
+          const double b00 = 0.5 * pqd.inv * u;
+          const double b10 = fma(-bp.hp, uq, bp.hp);
+          const double b01 = fma(-kp.hp, up, kp.hp);
+          const double pqv = pick3(d, pqd.PQ[0], pqd.PQ[1], pqd.PQ[2]);
+          const double c00 = fma(-uq, pqv, pick3(d, bp.ax, bp.ay, bp.az));
+          const double d00 = fma(up, pqv, pick3(d, kp.ax, kp.ay, kp.az));
+          double* dst = XT + (r * 3 + d) * N2DX;
+          twod<LA + 1, LB, LC + 1, LD, double>(d == 2 ? w : 1.0, c00, d00, b00, b10, b01,
+                                               pick3(d, AB[0], AB[1], AB[2]), pick3(d, CD[0], CD[1], CD[2]),
+                                               [&](int i, double v) { dst[i] = v; });
+        }
+        __syncwarp();
+        // derivative tables: per root x dim, I, dA, dB, dC over the unraised entries
+        for (int idx = lane; idx < 3 * NR * N2D; idx += 32) {
+          const int rd = idx / N2D, n = idx - rd * N2D, d = rd % 3;
+          const int a = n / ((LB + 1) * (LC + 1) * (LD + 1)), b = (n / ((LC + 1) * (LD + 1))) % (LB + 1),
+                    c = (n / (LD + 1)) % (LC + 1), dd = n % (LD + 1);
+          const int o = ((a * (LB + 1) + b) * (LC + 2) + c) * (LD + 1) + dd;
+          const double* X = XT + rd * N2DX;
+          const double i0 = X[o], up1 = X[o + G::SA];
+          double vA = a2 * up1, vB = b2 * fma(pick3(d, AB[0], AB[1], AB[2]), i0, up1), vC = c2 * X[o + G::SC];
+          if (a > 0) vA = fma(-(double)a, X[o - G::SA], vA);
+          if (b > 0) vB = fma(-(double)b, X[o - G::SB], vB);
+          if (c > 0) vC = fma(-(double)c, X[o - G::SC], vC);
+          double* T = TT + rd * 4 * N2D;
+          T[n] = i0;
+          T[N2D + n] = vA;
+          T[2 * N2D + n] = vB;
+          T[3 * N2D + n] = vC;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < KE; ++k) {
+          if (lane + 32 * k < NE) {
+            const int ox = offs[k] & 1023, oy = (offs[k] >> 10) & 1023, oz = offs[k] >> 20;
+            const double ge = gam[k];
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+              const double* tx = TT + (r * 3 + 0) * 4 * N2D;
+              const double* ty = TT + (r * 3 + 1) * 4 * N2D;
+              const double* tz = TT + (r * 3 + 2) * 4 * N2D;
+              const double ix = tx[ox], iy = ty[oy], iz = tz[oz];
+              const double t1 = ge * iz;
+              const double yz = iy * t1, xz = ix * t1, xy = ix * iy * ge;
+              acc[0] = fma(tx[N2D + ox], yz, acc[0]);
+              acc[1] = fma(ty[N2D + oy], xz, acc[1]);
+              acc[2] = fma(tz[N2D + oz], xy, acc[2]);
+              acc[3] = fma(tx[2 * N2D + ox], yz, acc[3]);
+              acc[4] = fma(ty[2 * N2D + oy], xz, acc[4]);
+              acc[5] = fma(tz[2 * N2D + oz], xy, acc[5]);
+              acc[6] = fma(tx[3 * N2D + ox], yz, acc[6]);
+              acc[7] = fma(ty[3 * N2D + oy], xz, acc[7]);
+              acc[8] = fma(tz[3 * N2D + oz], xy, acc[8]);
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+    grad_store(g, P, Q, qd, acc, lane);
+    __syncwarp();
+  }
+  if (g.counters) {
+    if (lane == 0 && nprim) atomicAdd(g.counters, nprim);
+    if (lane == 0 && nq) atomicAdd(g.counters + 1, nq);
+  }
+}
+
+// Classes whose per-lane tables (3 x N2DX doubles per root) stay small run
+// lane-parallel over primitive quartets.
+template <int LA, int LB, int LC, int LD>
+constexpr bool grad_lane_class() { return 3 * GCls<LA, LB, LC, LD>::N2DX <= 48; }
+
+template <int LA, int LB, int LC, int LD>
+cudaError_t launch_grad_cls(const GradArgs& g, int nsm, cudaStream_t st) {
+  if (g.nquartets <= 0) return cudaSuccess;
+  if constexpr (grad_lane_class<LA, LB, LC, LD>()) {
+    auto kern = k_grad_lane<LA, LB, LC, LD>;
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0);
+    if (g.ctas_per_sm > 0 && g.ctas_per_sm < per_sm) per_sm = g.ctas_per_sm;
+    if (per_sm < 1) per_sm = 1;
+    long long blocks = (g.nquartets + 3) / 4;
+    if (blocks > (long long)nsm * per_sm) blocks = (long long)nsm * per_sm;
+    kern<<<(unsigned)blocks, 128, 0, st>>>(g);
+  } else {
+    auto kern = k_grad_team<LA, LB, LC, LD>;
+    constexpr size_t per_warp = sizeof(double) * GradTeamSmem<LA, LB, LC, LD>::PER_WARP;
+    int warps = (int)((200 * 1024) / per_warp);
+    if (warps > 4) warps = 4;
+    if (warps < 1) warps = 1;
+    const size_t smem = per_warp * warps;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * warps, smem);
+    if (g.ctas_per_sm > 0 && g.ctas_per_sm < per_sm) per_sm = g.ctas_per_sm;
+    if (per_sm < 1) per_sm = 1;
+    long long blocks = (g.nquartets + warps - 1) / warps;
+    if (blocks > (long long)nsm * per_sm) blocks = (long long)nsm * per_sm;
+    kern<<<(unsigned)blocks, 32 * warps, smem, st>>>(g);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace oqpg

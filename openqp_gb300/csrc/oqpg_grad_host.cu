@@ -1,0 +1,356 @@
+// Host side of the two-electron HF gradient: the gradient's pair tables
+// (OpenQP's grd2 cutoffs), Cartesian-effective densities, the screened
+// quartet lists, class dispatch and the C ABI (oqpg_grad2*, routec_grad2).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/openqp_gb300.h"
+#include "oqpg_grad.cuh"
+#include "oqpg_internal.h"
+
+namespace oqpg {
+
+// Screened gradient quartets, one CTA per bra pair P (OpenQP grd2.F90:306-371):
+// Schwarz Q_P Q_Q >= cutoff (a prefix of the Schwarz-sorted pairs), not all
+// four shells on one atom (zero by translational invariance), and an upper
+// bound of the two-particle density with the shell maxima Dm,
+// |cj| Dm_ij Dm_kl + ck (Dm_ik Dm_jl + Dm_il Dm_jk), not below cutoff / 2 /
+// (Q_P Q_Q); the kernels apply the exact dabmax test.
+struct GListArgs {
+  int npair, ns;
+  const int2* pair_ij;
+  const int* pair_type;
+  const PairDev* gpairs;
+  const double* q;
+  const int* sorted_idx;
+  const double* sorted_q;
+  const double* dsh;
+  const int* atom;
+  double cj, ck, cutoff, cutoff2;
+  unsigned long long* counts;
+  uint2* lists[NCLASS];
+  unsigned long long caps[NCLASS];
+  int write;
+};
+
+__global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
+  __shared__ unsigned cnt[NCLASS];
+  __shared__ unsigned long long base[NCLASS];
+  __shared__ int s_len;
+  const int P = blockIdx.x;
+  if (a.gpairs[P].pcnt == 0) return;
+  const double qP = a.q[P];
+  if (!(qP > 0.0)) return;
+  if (threadIdx.x == 0) {
+    const double thr = a.cutoff / qP * (1.0 - 1e-9);
+    int lo = 0, hi = a.npair;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (a.sorted_q[mid] >= thr) lo = mid + 1;
+      else hi = mid;
+    }
+    s_len = lo;
+  }
+  __syncthreads();
+  const int len = s_len;
+  const int2 ij = a.pair_ij[P];
+  const int tP = a.pair_type[P];
+  const double* di = a.dsh + (long long)ij.x * a.ns;
+  const double* dj = a.dsh + (long long)ij.y * a.ns;
+  const int ati = a.atom[ij.x], atj = a.atom[ij.y];
+  for (int s0 = 0; s0 < len; s0 += blockDim.x) {
+    if (threadIdx.x < NCLASS) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int s = s0 + threadIdx.x;
+    const int Q = s < len ? a.sorted_idx[s] : 0x7fffffff;
+    int c = -1;
+    unsigned slot = 0;
+    uint2 ent;
+    if (Q <= P && a.gpairs[Q].pcnt > 0) {
+      const int2 kl = a.pair_ij[Q];
+      const double g = qP * a.q[Q];
+      const bool same = ati == atj && ati == a.atom[kl.x] && ati == a.atom[kl.y];
+      const double bound = a.cj * di[ij.y] * a.dsh[(long long)kl.x * a.ns + kl.y] +
+                           a.ck * (di[kl.x] * dj[kl.y] + di[kl.y] * dj[kl.x]);
+      if (!(g < a.cutoff) && !same && !(g * bound < a.cutoff2)) {
+        const int tQ = a.pair_type[Q];
+        if (tP <= tQ) { c = tP * 6 - tP * (tP - 1) / 2 + (tQ - tP); ent = make_uint2(P, Q); }
+        else { c = tQ * 6 - tQ * (tQ - 1) / 2 + (tP - tQ); ent = make_uint2(Q, P); }
+        slot = atomicAdd(&cnt[c], 1u);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < NCLASS && cnt[threadIdx.x])
+      base[threadIdx.x] = atomicAdd(&a.counts[threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
+    __syncthreads();
+    if (c >= 0 && a.write) {
+      const unsigned long long pos = base[c] + slot;
+      if (pos < a.caps[c]) a.lists[c][pos] = ent;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace oqpg
+
+using namespace oqpg;
+
+namespace {
+
+std::mutex g_grad_mutex;
+
+int gstatus(cudaError_t e) {
+  if (e == cudaSuccess) return OK;
+  if (e == cudaErrorMemoryAllocation) return NO_MEM;
+  return DEV_ERR;
+}
+
+#define GK(x)                                          \
+  do {                                                 \
+    cudaError_t e_ = (x);                              \
+    if (e_ != cudaSuccess) {                           \
+      if (std::getenv("OQPG_VERBOSE"))                 \
+        std::fprintf(stderr, "openqp_gb300: %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return gstatus(e_);                              \
+    }                                                  \
+  } while (0)
+
+template <typename T>
+int gupload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
+  GK(b.ensure(std::max<size_t>(sizeof(T) * v.size(), 16)));
+  if (!v.empty()) GK(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st));
+  return OK;
+}
+
+// Pair tables with the cutoffs of grd2_driver_gen (grd2.F90:231-260): pair
+// prefactor 10^-20, exponent 20 ln 10, no |K/p| pre-screen.
+int grad_init(oqpg_ctx* c) {
+  if (c->grad_ready) return OK;
+  cudaStream_t st = c->stream;
+  HostPairs gp;
+  build_pairs(*c, c->h_am, c->h_ncontr, c->h_poff, c->h_ex.data(), c->h_cc.data(), 1e-20, 20.0 * std::log(10.0),
+              false, gp);
+  int rc;
+  if ((rc = gupload(c->d_gpairs, gp.pairs, st))) return rc;
+  if ((rc = gupload(c->d_gprims, gp.prims, st))) return rc;
+  if ((rc = gupload(c->d_galpha, gp.alpha, st))) return rc;
+  c->coff.resize(c->nshell);
+  int n = 0;
+  for (int s = 0; s < c->nshell; ++s) { c->coff[s] = n; n += ncart(c->h_am[s]); }
+  c->ncart = n;
+  if ((rc = gupload(c->d_coff, c->coff, st))) return rc;
+  if ((rc = gupload(c->d_atom, c->shell_atom, st))) return rc;
+  GK(cudaStreamSynchronize(st));
+  c->grad_ready = true;
+  return OK;
+}
+
+// Cartesian-effective matrix of one full AO matrix M (nbf x nbf): per shell
+// block N T^T M T N (T: pure-d projection, N: Cartesian norms); and its
+// screening version (AO values for Cartesian bases).
+void cart_effective(const oqpg_ctx* c, const double* M, double* Mc) {
+  const int nb = c->nbf, nc = c->ncart;
+  for (int si = 0; si < c->nshell; ++si)
+    for (int sj = 0; sj < c->nshell; ++sj) {
+      const ShellDev& A = c->shells[si];
+      const ShellDev& B = c->shells[sj];
+      const int na = ncart(A.am), nbc = ncart(B.am);
+      const bool pa = A.harm != 0, pb = B.harm != 0;
+      for (int x = 0; x < na; ++x)
+        for (int y = 0; y < nbc; ++y) {
+          double v = 0;
+          const int ma = pa ? 5 : na, mb = pb ? 5 : nbc;
+          for (int p = 0; p < ma; ++p) {
+            const double tp = pa ? pure_d(p, x) : (p == x ? 1.0 : 0.0);
+            if (tp == 0.0) continue;
+            for (int r = 0; r < mb; ++r) {
+              const double tr = pb ? pure_d(r, y) : (r == y ? 1.0 : 0.0);
+              if (tr == 0.0) continue;
+              v += tp * tr * M[(size_t)(A.aoff + p) * nb + B.aoff + r];
+            }
+          }
+          Mc[(size_t)(c->coff[si] + x) * nc + c->coff[sj] + y] = v * cart_norm(A.am, x) * cart_norm(B.am, y);
+        }
+    }
+}
+
+// dE/dR (accumulated into de[3 natom]) for the two-particle density of the
+// full AO matrices x, y (and the spin pair xs, ys, both null or both set).
+int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, const double* ys, double cj,
+               double ckt, double cks, double cutoff, double* de) {
+  if (c->nmol != 1) return UNSUPPORTED;
+  int rc;
+  if ((rc = grad_init(c))) return rc;
+  cudaStream_t st = c->stream;
+  const int nc = c->ncart, ns = c->nshell;
+  const size_t n2 = (size_t)nc * nc;
+  const int nmat = xs ? 4 : 2;
+  std::vector<double> mats(n2 * nmat);
+  const double* src[4] = {x, y, xs, ys};
+  for (int k = 0; k < nmat; ++k) cart_effective(c, src[k], mats.data() + k * n2);
+  // shell maxima of the screening matrices
+  std::vector<double> dsh((size_t)ns * ns, 0.0);
+  for (int k = 0; k < nmat; ++k)
+    for (int si = 0; si < ns; ++si)
+      for (int sj = 0; sj < ns; ++sj) {
+        double m = 0;
+        const int li = c->shells[si].am, lj = c->shells[sj].am;
+        for (int a = 0; a < ncart(li); ++a)
+          for (int b = 0; b < ncart(lj); ++b) {
+            double v = std::fabs(mats[k * n2 + (size_t)(c->coff[si] + a) * nc + c->coff[sj] + b]);
+            if (!c->pure) v /= cart_norm(li, a) * cart_norm(lj, b);
+            m = std::max(m, v);
+          }
+        double& d = dsh[(size_t)si * ns + sj];
+        d = std::max(d, m);
+      }
+  cudaEvent_t e0 = c->ev[0], e1 = c->ev[3];
+  GK(cudaEventRecord(e0, st));
+  if ((rc = gupload(c->d_gmat, mats, st))) return rc;
+  if ((rc = gupload(c->d_dshg, dsh, st))) return rc;
+  GK(c->d_gcounts.ensure(sizeof(unsigned long long) * NCLASS));
+  GK(c->d_gwork.ensure(sizeof(unsigned long long) * NCLASS));
+  GK(c->d_gcnt.ensure(sizeof(unsigned long long) * 2));
+  GK(c->d_de.ensure(sizeof(double) * 3 * c->natom));
+  GListArgs la{};
+  la.npair = c->npair; la.ns = ns;
+  la.pair_ij = c->d_pair_ij.as<int2>();
+  la.pair_type = c->d_pair_type.as<int>();
+  la.gpairs = c->d_gpairs.as<PairDev>();
+  la.q = c->d_q.as<double>();
+  la.sorted_idx = c->d_sorted_idx.as<int>();
+  la.sorted_q = c->d_sorted_q.as<double>();
+  la.dsh = c->d_dshg.as<double>();
+  la.atom = c->d_atom.as<int>();
+  la.cj = std::fabs(cj);
+  la.ck = std::fabs(ckt) + std::fabs(cks);
+  la.cutoff = cutoff;
+  la.cutoff2 = 0.5 * cutoff;
+  la.counts = c->d_gcounts.as<unsigned long long>();
+  unsigned long long counts[NCLASS];
+  for (int pass = 0; pass < 3; ++pass) {
+    la.write = 1;
+    for (int k = 0; k < NCLASS; ++k) { la.lists[k] = c->d_glists[k].as<uint2>(); la.caps[k] = c->gcaps[k]; }
+    GK(cudaMemsetAsync(c->d_gcounts.p, 0, sizeof(unsigned long long) * NCLASS, st));
+    k_grad_lists<<<c->npair, 256, 0, st>>>(la);
+    GK(cudaGetLastError());
+    GK(cudaMemcpyAsync(counts, c->d_gcounts.p, sizeof(counts), cudaMemcpyDeviceToHost, st));
+    GK(cudaStreamSynchronize(st));
+    bool ok = true;
+    for (int k = 0; k < NCLASS; ++k)
+      if (counts[k] > c->gcaps[k]) {
+        ok = false;
+        const unsigned long long cap = counts[k] + counts[k] / 8 + 1024;
+        GK(c->d_glists[k].ensure(sizeof(uint2) * cap));
+        c->gcaps[k] = cap;
+      }
+    if (ok) break;
+    if (pass == 2) return DEV_ERR;
+  }
+  GK(cudaMemsetAsync(c->d_de.p, 0, sizeof(double) * 3 * c->natom, st));
+  GK(cudaMemsetAsync(c->d_gwork.p, 0, sizeof(unsigned long long) * NCLASS, st));
+  GK(cudaMemsetAsync(c->d_gcnt.p, 0, sizeof(unsigned long long) * 2, st));
+  GradArgs g{};
+  g.shells = c->d_shells.as<ShellDev>();
+  g.pairs = c->d_gpairs.as<PairDev>();
+  g.prims = c->d_gprims.as<PrimPair>();
+  g.alpha = c->d_galpha.as<double>();
+  const double* dm = c->d_gmat.as<double>();
+  g.xt = dm; g.yt = dm + n2;
+  g.xs = xs ? dm + 2 * n2 : nullptr;
+  g.ys = xs ? dm + 3 * n2 : nullptr;
+  g.ncart = nc;
+  g.coff = c->d_coff.as<int>();
+  g.atom = c->d_atom.as<int>();
+  g.cj = cj; g.ckt = ckt; g.cks = cks;
+  g.pure = c->pure ? 1 : 0;
+  g.q = c->d_q.as<double>();
+  g.cutoff2 = 0.5 * cutoff;
+  // grd2: dtol = 10^-20 and dabcut = 1e-11 (smaller for very tight exponents), both squared
+  double zbig = 0;
+  for (double e : c->h_ex) zbig = std::max(zbig, e);
+  double dabcut = 1e-11;
+  if (zbig > 1e6) dabcut /= 10;
+  if (zbig > 1e7) dabcut /= 10;
+  g.dtol2 = 1e-40;
+  g.dabcut2 = dabcut * dabcut;
+  g.de = c->d_de.as<double>();
+  g.counters = c->d_gcnt.as<unsigned long long>();
+  double listed = 0;
+  for (int cl = NCLASS - 1; cl >= 0; --cl) {
+    if (!counts[cl]) continue;
+    listed += (double)counts[cl];
+    g.quartets = c->d_glists[cl].as<uint2>();
+    g.nquartets = (long long)counts[cl];
+    g.work = c->d_gwork.as<unsigned long long>() + cl;
+    GK(cl < 15 ? launch_grad_a(cl, g, c->nsm, st) : launch_grad_b(cl, g, c->nsm, st));
+  }
+  std::vector<double> h_de(3 * c->natom);
+  unsigned long long h_cnt[2];
+  GK(cudaMemcpyAsync(h_de.data(), c->d_de.p, sizeof(double) * h_de.size(), cudaMemcpyDeviceToHost, st));
+  GK(cudaMemcpyAsync(h_cnt, c->d_gcnt.p, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+  GK(cudaEventRecord(e1, st));
+  GK(cudaStreamSynchronize(st));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  for (size_t k = 0; k < h_de.size(); ++k) de[k] += h_de[k];
+  c->grad_stats[0] = listed;
+  c->grad_stats[1] = (double)h_cnt[1];
+  c->grad_stats[2] = (double)h_cnt[0];
+  c->grad_stats[3] = ms;
+  return OK;
+}
+
+void unpack_full(const double* dp, int n, double* D) {
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j <= i; ++j) D[(size_t)i * n + j] = D[(size_t)j * n + i] = dp[(size_t)i * (i + 1) / 2 + j];
+}
+
+int grad_packed(oqpg_ctx* c, const double* d, int nfocks, double hfscale, double coulscale, double* de) {
+  if (nfocks != 1 && nfocks != 2) return UNSUPPORTED;
+  const int n = c->nbf;
+  const size_t n2 = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
+  std::vector<double> Dt(n2), Ds;
+  unpack_full(d, n, Dt.data());
+  if (nfocks == 2) {
+    std::vector<double> Db(n2);
+    unpack_full(d + ntri, n, Db.data());
+    Ds.resize(n2);
+    for (size_t k = 0; k < n2; ++k) {
+      Ds[k] = Dt[k] - Db[k];
+      Dt[k] += Db[k];
+    }
+  }
+  const double* ds = nfocks == 2 ? Ds.data() : nullptr;
+  return grad_build(c, Dt.data(), Dt.data(), ds, ds, 4.0 * coulscale, hfscale, hfscale, c->tau, de);
+}
+
+}  // namespace
+
+extern "C" {
+
+int oqpg_grad2(oqpg_ctx* ctx, const double* d, int nfocks, double hfscale, double coulscale, double* de) {
+  if (!ctx) return NOT_INIT;
+  if (!d || !de) return UNSUPPORTED;
+  return grad_packed(ctx, d, nfocks, hfscale, coulscale, de);
+}
+
+int oqpg_grad2_bilinear(oqpg_ctx* ctx, const double* x, const double* y, const double* xs, const double* ys,
+                        double cj, double ckt, double cks, double* de) {
+  if (!ctx) return NOT_INIT;
+  if (!x || !y || !de || (!xs) != (!ys)) return UNSUPPORTED;
+  return grad_build(ctx, x, y, xs, ys, cj, ckt, cks, ctx->tau, de);
+}
+
+int oqpg_grad_stats(const oqpg_ctx* ctx, double* out, int n) {
+  if (!ctx) return NOT_INIT;
+  for (int i = 0; i < n && i < 4; ++i) out[i] = ctx->grad_stats[i];
+  return OK;
+}
+
+}  // extern "C"

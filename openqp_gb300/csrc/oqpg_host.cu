@@ -379,22 +379,17 @@ int to_status(cudaError_t e) {
     }                                                 \
   } while (0)
 
-struct HostPairs {
-  std::vector<PairDev> pairs;
-  std::vector<PrimPair> prims;
-  std::vector<int2> ij;    // molecule-local shells of each pair
-  std::vector<int> type;
-  std::vector<int> mol;
-};
+}  // namespace
 
-// OpenQP's int2_prepare_pair (int2_pairs.F90:179-266) with the rotated-axis
-// pre-screen |K/p| >= quartet cutoff (int_rotaxis.F90:292-306) applied once.
+// OpenQP's int2_prepare_pair (int2_pairs.F90:179-266); with sp_screen also
+// the rotated-axis pre-screen |K/p| >= quartet cutoff (int_rotaxis.F90:292-306),
+// applied once (the Fock build; the gradient's Rys path has no such screen).
 // Pairs are numbered molecule by molecule, canonical (i >= j) within each.
-void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vector<int>& ncontr,
-                 const std::vector<int>& poff, const double* ex, const double* cc, double qcut, double ecut,
-                 HostPairs& out) {
+void oqpg::build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vector<int>& ncontr,
+                       const std::vector<int>& poff, const double* ex, const double* cc, double qcut, double ecut,
+                       bool sp_screen, HostPairs& out) {
   const double sqrtpito52 = std::sqrt(2.0) * std::pow(3.14159265358979323846, 1.25);
-  out.pairs.clear(); out.prims.clear(); out.ij.clear(); out.type.clear(); out.mol.clear();
+  out.pairs.clear(); out.prims.clear(); out.ij.clear(); out.type.clear(); out.mol.clear(); out.alpha.clear();
   for (int m = 0; m < c.nmol; ++m) {
     const MolDev& M = c.mols[m];
     for (int li = 0; li < M.ns; ++li)
@@ -417,7 +412,7 @@ void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vecto
             const double k1 = cc[poff[sa] + p1] * cc[poff[sb] + p2] * std::exp(-e12);
             if (std::fabs(k1) < qcut) continue;
             const double sp = sqrtpito52 * k1 * gi;
-            if (std::fabs(sp) < qcut) continue;
+            if (sp_screen && std::fabs(sp) < qcut) continue;
             PrimPair pp;
             pp.p = g; pp.hp = 0.5 * gi;
             pp.px = (a1 * A.x + a2 * B.x) * gi;
@@ -426,6 +421,7 @@ void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vecto
             pp.ax = pp.px - A.x; pp.ay = pp.py - A.y; pp.az = pp.pz - A.z;
             pp.sp = sp; pp.spf = (float)sp; pp.pf = (float)g;
             out.prims.push_back(pp);
+            out.alpha.push_back(a1);
           }
         pd.pcnt = (int)out.prims.size() - pd.poff;
         out.pairs.push_back(pd);
@@ -435,8 +431,6 @@ void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vecto
       }
   }
 }
-
-}  // namespace
 
 // FP32 decision band of the primitive-quartet screen: |sp sq| / sqrt(p+q)
 // against sqrt(prim_cut2).  FP32 products of two screened prefactors stay
@@ -529,6 +523,16 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
     stride = std::max(stride, M.nbf);
   }
   c->nbf = row0; c->stride = stride; c->ntri = tri0; c->dsh_elems = dsh0; c->npair = pair0;
+  c->h_am = am; c->h_ncontr = ncontr; c->h_poff = poff;
+  c->h_ex.assign(ex, ex + off); c->h_cc.assign(cc, cc + off);
+  c->shell_atom.resize(nshell);
+  {
+    int s2 = 0, a0 = 0;
+    for (int m = 0; m < nmol; ++m) {
+      for (int k = 0; k < nshell_m[m]; ++k, ++s2) c->shell_atom[s2] = a0 + origin[s2] - 1;
+      a0 += natom_m[m];
+    }
+  }
   CK(cudaGetDevice(&c->dev));
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->dev));
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
@@ -544,7 +548,7 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
 
   // --- Schwarz bounds with OpenQP's very tight cutoffs (int2.F90:1600-1604)
   HostPairs sp;
-  build_pairs(*c, am, ncontr, poff, ex, cc, 1e-17, 50.0, sp);
+  build_pairs(*c, am, ncontr, poff, ex, cc, 1e-17, 50.0, true, sp);
   if ((rc = upload(c->d_pairs, sp.pairs, st))) return rc;
   if ((rc = upload(c->d_prims, sp.prims, st))) return rc;
   std::vector<std::vector<uint2>> diag(NCLASS);
@@ -585,7 +589,7 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
 
   // --- pair tables of the Fock build (cutoffs 1e-2 tau, 1e-4 tau, 25 ln 10; int2.F90:260-272)
   HostPairs fp;
-  build_pairs(*c, am, ncontr, poff, ex, cc, 1e-4 * cutoff, 25.0 * std::log(10.0), fp);
+  build_pairs(*c, am, ncontr, poff, ex, cc, 1e-4 * cutoff, 25.0 * std::log(10.0), true, fp);
   if ((rc = upload(c->d_pairs, fp.pairs, st))) return rc;
   if ((rc = upload(c->d_prims, fp.prims, st))) return rc;
   std::vector<PrimPairF> pf(fp.prims.size());
@@ -1285,6 +1289,28 @@ void routec_fock_jk_batch(const double* d, double* f, const int* nmol, const int
       else
         std::memcpy(f, c->h_out, bytes);
     }
+  }
+  if (info) *info = rc;
+}
+
+void routec_grad2(const double* d, const double* xyz, double* de, const int* nbf, const int* natm,
+                  const double* hfscale, const double* coulscale, int* info) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!d || !xyz || !de || !nbf || !natm || !hfscale || !coulscale) rc = UNSUPPORTED;
+  else if (*nbf != g_ctx->nbf || *natm != g_ctx->natom || g_ctx->nmol != 1) rc = NOT_INIT;
+  else {
+    // the registered geometry must be the caller's
+    rc = OK;
+    for (int s = 0; s < g_ctx->nshell && rc == OK; ++s) {
+      const int at = g_ctx->shell_atom[s];
+      const ShellDev& S = g_ctx->shells[s];
+      if (std::fabs(S.x - xyz[3 * at]) > 1e-10 || std::fabs(S.y - xyz[3 * at + 1]) > 1e-10 ||
+          std::fabs(S.z - xyz[3 * at + 2]) > 1e-10)
+        rc = NOT_INIT;
+    }
+    if (rc == OK) rc = oqpg_grad2(g_ctx, d, 1, *hfscale, *coulscale, de);
   }
   if (info) *info = rc;
 }

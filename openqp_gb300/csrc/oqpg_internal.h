@@ -92,6 +92,26 @@ __global__ void k_finalize(const double* __restrict__ gj, const double* __restri
                            const unsigned* __restrict__ flag);
 void set_band(BuildArgs& a);
 
+// Host-side primitive-pair tables of a context (oqpg_host.cu).
+struct HostPairs {
+  std::vector<PairDev> pairs;
+  std::vector<PrimPair> prims;
+  std::vector<double> alpha;  // exponent of the pair's first shell, per primitive pair
+  std::vector<int2> ij;       // molecule-local shells of each pair
+  std::vector<int> type;
+  std::vector<int> mol;
+};
+
+struct GradArgs;
+}  // namespace oqpg
+struct oqpg_ctx;
+namespace oqpg {
+void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vector<int>& ncontr,
+                 const std::vector<int>& poff, const double* ex, const double* cc, double qcut, double ecut,
+                 bool sp_screen, HostPairs& out);
+cudaError_t launch_grad_a(int c, const GradArgs& g, int nsm, cudaStream_t st);
+cudaError_t launch_grad_b(int c, const GradArgs& g, int nsm, cudaStream_t st);
+
 constexpr int NLIST = 2 * NCLASS;  // FP64 lists, then the FP32 lists of the precision split
 
 // Per-build device buffers of one build pipeline (a context has one for its
@@ -136,6 +156,9 @@ struct oqpg_ctx {
   std::vector<int> aoff, naos;
   std::vector<oqpg::MolDev> mols;
   std::vector<double> schwarz_pair;   // per pair (canonical index within each molecule, molecules in order)
+  // the registered basis (host copies; the gradient builds its own pair tables from them)
+  std::vector<int> h_am, h_ncontr, h_poff, shell_atom;
+  std::vector<double> h_ex, h_cc;
   oqpg_tuning tune;
   // precision split: 0 = every quartet in FP64, 1 = bound < tau_f32 in FP32
   int precision_mode = 0;
@@ -159,6 +182,14 @@ struct oqpg_ctx {
   double g_se = 0, g_sc = 0, g_tau32 = 0;
   oqpg::DevBuf d_gin, d_gout;        // the graph's packed input / output
   int graph_replays = 0, graph_captures = 0, g_nlaunch = 0;
+  // two-electron gradient: pair tables with the gradient cutoffs (built on first use)
+  bool grad_ready = false;
+  int ncart = 0;
+  std::vector<int> coff;
+  oqpg::DevBuf d_gpairs, d_gprims, d_galpha, d_coff, d_atom, d_gmat, d_dshg, d_gcounts, d_gwork, d_de, d_gcnt;
+  oqpg::DevBuf d_glists[oqpg::NCLASS];
+  unsigned long long gcaps[oqpg::NCLASS] = {0};
+  double grad_stats[4] = {0, 0, 0, 0};  // quartets listed, evaluated, primitive quartets, ms
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t evc[oqpg::NCLASS][2] = {};
   double last_stats[10 + 3 * oqpg::NCLASS] = {0};

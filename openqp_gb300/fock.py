@@ -153,6 +153,33 @@ class FockBuilder:
         if rc != 0:
             raise FockError(rc, "oqpg_set_precision")
 
+    def grad2(self, d, hfscale=1.0, coulscale=1.0):
+        """Two-electron gradient (natom, 3) for packed densities d ((ntri,) or
+        (nfocks, ntri): total RHF density, or alpha and beta)."""
+        d = np.ascontiguousarray(np.atleast_2d(d), dtype=np.float64)
+        de = np.zeros(3 * self.bas.natom)
+        rc = lib().oqpg_grad2(self.h, ptr(d), d.shape[0], float(hfscale), float(coulscale), ptr(de))
+        if rc != 0:
+            raise FockError(rc, "oqpg_grad2")
+        return de.reshape(-1, 3)
+
+    def grad2_bilinear(self, x, y, xs=None, ys=None, cj=4.0, ckt=1.0, cks=1.0):
+        """Gradient (natom, 3) of the symmetric bilinear two-particle density of
+        full AO matrices (see oqpg_grad2_bilinear)."""
+        n = self.nbf
+        mats = [None if m is None else np.ascontiguousarray(m, dtype=np.float64).reshape(n, n) for m in (x, y, xs, ys)]
+        de = np.zeros(3 * self.bas.natom)
+        rc = lib().oqpg_grad2_bilinear(self.h, *[None if m is None else ptr(m) for m in mats], float(cj), float(ckt),
+                                       float(cks), ptr(de))
+        if rc != 0:
+            raise FockError(rc, "oqpg_grad2_bilinear")
+        return de.reshape(-1, 3)
+
+    def grad_stats(self):
+        s = np.zeros(4)
+        lib().oqpg_grad_stats(self.h, ptr(s), 4)
+        return dict(quartets_listed=int(s[0]), quartets=int(s[1]), prim_quartets=int(s[2]), ms=float(s[3]))
+
     def schwarz(self):
         ns = len(self.bas.am)
         q = np.zeros(ns * ns)
@@ -265,6 +292,19 @@ def routec_fock_jk(d, nbf, nfocks, se=1.0, sc=1.0):
     lib().routec_fock_jk(ptr(d), ptr(f), ctypes.byref(n), ctypes.byref(nf), ctypes.byref(se_), ctypes.byref(sc_),
                          ctypes.byref(info))
     return f.reshape(nfocks, -1), info.value
+
+
+def routec_grad2(d, xyz, nbf, natom, hfscale=1.0, coulscale=1.0, de=None):
+    """Calls routec_grad2 as OpenQP's bridge does; de (natom, 3) is accumulated."""
+    d = np.ascontiguousarray(d, dtype=np.float64).reshape(-1)
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+    de = np.zeros(3 * natom) if de is None else np.ascontiguousarray(de, dtype=np.float64).reshape(-1)
+    n, na = ctypes.c_int(nbf), ctypes.c_int(natom)
+    hf, cs = ctypes.c_double(hfscale), ctypes.c_double(coulscale)
+    info = ctypes.c_int(1)
+    lib().routec_grad2(ptr(d), ptr(x), ptr(de), ctypes.byref(n), ctypes.byref(na), ctypes.byref(hf), ctypes.byref(cs),
+                       ctypes.byref(info))
+    return de.reshape(-1, 3), info.value
 
 
 def routec_finalize():
