@@ -51,9 +51,10 @@ WORKLOADS = {
     # 256 water clusters of 1-16 molecules (uniform), 6-31G, built together
     "batch256_631g": dict(name="256 water clusters (1-16 H2O, uniform), 6-31G, batched RHF J+K builds", batch=256,
                           seed=0, basis="6-31g", cutoff=1e-10),
-    # only the d shells of a (H2O)64 6-31G(d) cluster: every quartet is (dd|dd)
-    "dd_only": dict(name="(dd|dd)-only: the 64 d shells of a (H2O)64 6-31G(d) cluster", nwater=64, edge=15.1,
-                    seed=0, basis="6-31g(d)", cutoff=1e-10, only_l=2),
+    # (dd|dd) only: one Cartesian d shell (6-31G(d) carbon d, exponent 0.8) on each
+    # point of a 4 x 4 x 4 cubic lattice of spacing 1.54 A, so that all 2080 pairs overlap
+    "dd_only": dict(name="(dd|dd)-only: 64 Cartesian d shells (exponent 0.8) on a 4x4x4 lattice, 1.54 A spacing",
+                    lattice=4, spacing=1.54, dexp=0.8, seed=0, cutoff=1e-10),
 }
 WORKLOAD = dict(WORKLOADS["water32_ccpvdz"])
 
@@ -63,23 +64,16 @@ def make_workload(overlap="library"):
     step comes from the library's host routine, or from the oracle in the
     reference arm (identical to 1e-14)."""
     from openqp_gb300 import workloads
-    from openqp_gb300.basis import BasisArrays
     from openqp_gb300.basis import build_basis
-    if "alkane" in WORKLOAD:
+    if "lattice" in WORKLOAD:
+        bas = workloads.d_lattice(WORKLOAD["lattice"], WORKLOAD["spacing"], WORKLOAD["dexp"])
+    elif "alkane" in WORKLOAD:
         z, xyz = workloads.alkane(WORKLOAD["alkane"], WORKLOAD["seed"])
         bas = build_basis(z, xyz, WORKLOAD["basis"])
     else:
         bas = workloads.water_cluster_basis(WORKLOAD["nwater"], WORKLOAD["edge"], WORKLOAD["seed"],
                                             WORKLOAD["basis"])
-    if "only_l" in WORKLOAD:
-        keep = np.where(bas.am == WORKLOAD["only_l"])[0]
-        offs = np.concatenate([[0], np.cumsum(bas.ncontr)])
-        ex = np.concatenate([bas.ex[offs[s]:offs[s + 1]] for s in keep])
-        cc = np.concatenate([bas.cc[offs[s]:offs[s + 1]] for s in keep])
-        naos = bas.naos[keep]
-        bas = BasisArrays(bas.am[keep], bas.ncontr[keep], bas.origin[keep], bas.harmonic[keep], ex, cc, bas.xyz,
-                          bas.charges, int(naos.sum()), np.concatenate([[0], np.cumsum(naos)[:-1]]).astype(np.int32),
-                          naos)
+    if "lattice" in WORKLOAD:
         nocc = bas.nbf // 4
     else:
         nocc = workloads.nelectrons(bas) // 2

@@ -291,7 +291,9 @@ struct Epi {
   static constexpr int NEP = A * B * C * D;
 };
 
-// In-register pure projection of one index (compile-time dims).
+// In-register pure projection of one index (compile-time dims); the Cartesian
+// norms of the d components are folded into the coefficients, so projected
+// indices need no separate normalisation.
 template <int D0, int D1, int D2, int D3, int POS, bool DO, typename T>
 __device__ __forceinline__ void project_regs(const T* in, T* out) {
   constexpr int DIMS[4] = {D0, D1, D2, D3};
@@ -312,13 +314,28 @@ __device__ __forceinline__ void project_regs(const T* in, T* out) {
         T v = 0;
 #pragma unroll
         for (int c = 0; c < 6; ++c)
-          if (pure_d(m, c) != 0.0) v = fma((T)pure_d(m, c), in[(a * N + c) * POST + p], v);
+          if (pure_d(m, c) != 0.0) v = fma((T)(pure_d(m, c) * cart_norm(2, c)), in[(a * N + c) * POST + p], v);
         out[(a * 5 + m) * POST + p] = v;
       }
 }
 
-template <typename T>
-__device__ __forceinline__ T cut_elem(T v, T cut) { return fabs(v) < cut ? (T)0 : v; }
+__device__ __constant__ const double SQRT3_POW[5] = {1.0, 1.7320508075688772, 3.0, 5.196152422706632, 9.0};
+__device__ __constant__ const float SQRT3_POWF[5] = {1.0f, 1.7320508075688772f, 3.0f, 5.196152422706632f, 9.0f};
+template <typename T> __device__ __forceinline__ T sqrt3_pow(int n);
+template <> __device__ __forceinline__ double sqrt3_pow<double>(int n) { return SQRT3_POW[n]; }
+template <> __device__ __forceinline__ float sqrt3_pow<float>(int n) { return SQRT3_POWF[n]; }
+
+// Element cutoff |v| < cut -> 0 (cut > 0), decided on the bit patterns: for
+// non-negative IEEE values the order of the magnitudes is the integer order of
+// their bits, so no FP64 compare is spent.
+__device__ __forceinline__ double cut_elem(double v, double cut) {
+  const long long m = __double_as_longlong(v) & 0x7fffffffffffffffll;
+  return m < __double_as_longlong(cut) ? 0.0 : v;
+}
+__device__ __forceinline__ float cut_elem(float v, float cut) {
+  const int m = __float_as_int(v) & 0x7fffffff;
+  return m < __float_as_int(cut) ? 0.0f : v;
+}
 
 // Persistent-warp work distribution: warps take chunks of the (sorted) class
 // list from a global counter, heaviest quartets first.
@@ -421,8 +438,10 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
   using E = Epi<LA, LB, LC, LD, PURE>;
   constexpr int NE = K::NE;
   const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
+  // Cartesian d components carry their norms; projected (pure) indices get
+  // them inside project_regs
 #pragma unroll
-  for (int e = 0; e < NE; ++e) acc[e] *= (T)K::norm(e);
+  for (int e = 0; e < NE; ++e) acc[e] *= (T)(PURE ? 1.0 : K::norm(e));
   constexpr int DA = K::NA, DB = K::NB, DC = K::NC, DD = K::ND;
   T t1[NE], t2[NE];
   project_regs<DA, DB, DC, DD, 0, PURE && LA == 2>(acc, t1);
@@ -724,10 +743,10 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
       if (e < NE) {
         const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
                   id = e % K::ND;
-        const T s3 = (T)1.7320508075688772;
-        const T nrm = (LA == 2 && ia >= 3 ? s3 : (T)1) * (LB == 2 && ib >= 3 ? s3 : (T)1) *
-                      (LC == 2 && ic >= 3 ? s3 : (T)1) * (LD == 2 && id >= 3 ? s3 : (T)1);
-        V[e] = (LA == 2 || LB == 2 || LC == 2 || LD == 2) ? acc[k] * nrm : acc[k];
+        // product of the component norms: sqrt(3)^n for n off-diagonal d components,
+        // looked up rather than multiplied out (one FP64 multiply per element)
+        const int n3 = (LA == 2 && ia >= 3) + (LB == 2 && ib >= 3) + (LC == 2 && ic >= 3) + (LD == 2 && id >= 3);
+        V[e] = (LA == 2 || LB == 2 || LC == 2 || LD == 2) ? acc[k] * sqrt3_pow<T>(n3) : acc[k];
       }
     }
     __syncwarp();

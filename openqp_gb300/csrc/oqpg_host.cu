@@ -212,16 +212,36 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
   }
 }
 
-// Counting sort of a class list by primitive-quartet count (descending, in
+// Counting sort of a class list by primitive-quartet work (descending, in
 // quarter-octave bins), so that the lanes of a warp run loops of similar
-// length.  k_bin_hist: per-bin counts; k_bin_scatter: stable-per-CTA scatter
-// into the bin ranges given by the exclusive scan in cursors.
+// length.  The work of a quartet is the number of its primitive quartets that
+// pass the FP32 pre-screen |sp sq| / sqrt(p + q) >= lo, the loop trip count of
+// the FP64 body (without prims: the product of the pair primitive counts).
+// k_bin_hist: per-bin counts (and each entry's bin); k_bin_scatter:
+// stable-per-CTA scatter into the bin ranges given by the exclusive scan in
+// cursors.
 
-__device__ __forceinline__ int prim_bin(const PairDev* pairs, uint2 q) {
-  const int n = pairs[q.x].pcnt * pairs[q.y].pcnt;
+__device__ __forceinline__ int work_bin(int n) {
   if (n <= 1) return NBIN - 1;
   const int k = (int)(4.0f * __log2f((float)n));
   return NBIN - 1 - (k < NBIN - 1 ? k : NBIN - 1);
+}
+
+__device__ __forceinline__ int prim_bin(const PairDev* pairs, uint2 q) {
+  return work_bin(pairs[q.x].pcnt * pairs[q.y].pcnt);
+}
+
+__device__ __forceinline__ int survivor_bin(const PairDev* pairs, const PrimPair* prims, uint2 q, float lo) {
+  const PairDev P = pairs[q.x], Q = pairs[q.y];
+  int n = 0;
+  for (int j = 0; j < Q.pcnt; ++j) {
+    const float ks = __ldg(&prims[Q.poff + j].spf), kp = __ldg(&prims[Q.poff + j].pf);
+    for (int i = 0; i < P.pcnt; ++i) {
+      const float r = fabsf(__ldg(&prims[P.poff + i].spf) * ks) * rsqrtf(__ldg(&prims[P.poff + i].pf) + kp);
+      n += r >= lo ? 1 : 0;
+    }
+  }
+  return work_bin(n);
 }
 
 __device__ __forceinline__ long long list_len(long long n, const unsigned long long* n_dev) {
@@ -231,24 +251,31 @@ __device__ __forceinline__ long long list_len(long long n, const unsigned long l
 }
 
 __global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const unsigned long long* n_dev,
-                           const PairDev* __restrict__ pairs, unsigned long long* hist) {
+                           const PairDev* __restrict__ pairs, const PrimPair* __restrict__ prims, float lo,
+                           unsigned char* bins, unsigned long long* hist) {
   __shared__ unsigned h[NBIN];
   n = list_len(n, n_dev);
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x) h[i] = 0;
   __syncthreads();
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-    atomicAdd(&h[prim_bin(pairs, list[t])], 1u);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int b = prims ? survivor_bin(pairs, prims, list[t], lo) : prim_bin(pairs, list[t]);
+    if (bins) bins[t] = (unsigned char)b;
+    atomicAdd(&h[b], 1u);
+  }
   __syncthreads();
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x)
     if (h[i]) atomicAdd(&hist[i], (unsigned long long)h[i]);
 }
 
 // Each CTA takes a contiguous chunk, reserves its per-bin ranges once, then
-// places its entries.
+// places its entries (bins: the bins k_bin_hist stored; null: recomputed from
+// the primitive counts).
 __global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ list, long long n,
                                                      const unsigned long long* n_dev,
-                                                     const PairDev* __restrict__ pairs, unsigned long long* cursors,
-                                                     uint2* out, long long chunk, const unsigned* flag) {
+                                                     const PairDev* __restrict__ pairs,
+                                                     const unsigned char* __restrict__ bins,
+                                                     unsigned long long* cursors, uint2* out, long long chunk,
+                                                     const unsigned* flag) {
   __shared__ unsigned h[NBIN];
   __shared__ unsigned long long b[NBIN];
   if (flag && *flag) return;  // a list overflowed: the cursors were not written
@@ -258,7 +285,8 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ l
   const long long hi = lo + chunk < n ? lo + chunk : n;
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x) h[i] = 0;
   __syncthreads();
-  for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) atomicAdd(&h[prim_bin(pairs, list[t])], 1u);
+  for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x)
+    atomicAdd(&h[bins ? bins[t] : prim_bin(pairs, list[t])], 1u);
   __syncthreads();
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x) {
     b[i] = h[i] ? atomicAdd(&cursors[i], (unsigned long long)h[i]) : 0ull;
@@ -267,7 +295,7 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ l
   __syncthreads();
   for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
     const uint2 q = list[t];
-    const int bin = prim_bin(pairs, q);
+    const int bin = bins ? bins[t] : prim_bin(pairs, q);
     const unsigned r = atomicAdd(&h[bin], 1u);
     out[b[bin] + r] = q;
   }
@@ -720,6 +748,7 @@ int size_lists(oqpg_ctx* c, BuildBufs& B, const unsigned long long* counts, cuda
     if (cap > B.cap[k]) {
       CK(B.lists[k].ensure(sizeof(uint2) * cap));
       CK(B.slists[k].ensure(sizeof(uint2) * cap));
+      CK(B.bins[k].ensure(cap));
       B.cap[k] = cap;
     }
   }
@@ -770,15 +799,16 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
   k_lists<<<c->npair, 256, 0, st>>>(la);
   CK(cudaGetLastError());
   ++nlaunch;
-  // order every list by primitive-quartet count (counting sort, device-side scan)
+  // order every list by surviving primitive quartets (counting sort, device-side scan)
   CK(cudaMemsetAsync(B.hist.p, 0, sizeof(unsigned long long) * NLIST * NBIN, st));
+  const float lo = (float)(1e-4 * c->tau * (1.0 - 1e-4));
   unsigned long long* counts = B.counts.as<unsigned long long>();
   for (int k = 0; k < NLIST; ++k) {
     if (!B.cap[k]) continue;
     const long long cap = (long long)B.cap[k];
     k_bin_hist<<<(unsigned)std::min<long long>((cap + 255) / 256, c->nsm * 4LL), 256, 0, st>>>(
-        B.lists[k].as<uint2>(), cap, counts + k, c->d_pairs.as<PairDev>(),
-        B.hist.as<unsigned long long>() + k * NBIN);
+        B.lists[k].as<uint2>(), cap, counts + k, c->d_pairs.as<PairDev>(), c->d_prims.as<PrimPair>(), lo,
+        B.bins[k].as<unsigned char>(), B.hist.as<unsigned long long>() + k * NBIN);
     CK(cudaGetLastError());
     ++nlaunch;
   }
@@ -793,7 +823,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
     if (!B.cap[k]) continue;
     const long long cap = (long long)B.cap[k];
     k_bin_scatter<<<(unsigned)((cap + chunk - 1) / chunk), 256, 0, st>>>(
-        B.lists[k].as<uint2>(), cap, counts + k, c->d_pairs.as<PairDev>(),
+        B.lists[k].as<uint2>(), cap, counts + k, c->d_pairs.as<PairDev>(), B.bins[k].as<unsigned char>(),
         B.cursor.as<unsigned long long>() + k * NBIN, B.slists[k].as<uint2>(), chunk, B.flag.as<unsigned>());
     CK(cudaGetLastError());
     ++nlaunch;

@@ -77,11 +77,14 @@ __global__ void k_dsh(const double* __restrict__ dp, int nfocks, const MolDev* _
                       unsigned long long* dmax_bits);
 __global__ void k_lists(const ListArgs a);
 // n entries, or with n_dev the device count min(*n_dev, n) (n is then the capacity)
+// prims null: bins by the product of the pair primitive counts; else by the
+// primitive quartets passing the FP32 pre-screen at lo (bins[t] stores each bin)
 __global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const unsigned long long* n_dev,
-                           const PairDev* __restrict__ pairs, unsigned long long* hist);
+                           const PairDev* __restrict__ pairs, const PrimPair* __restrict__ prims, float lo,
+                           unsigned char* bins, unsigned long long* hist);
 __global__ void k_bin_scatter(const uint2* __restrict__ list, long long n, const unsigned long long* n_dev,
-                              const PairDev* __restrict__ pairs, unsigned long long* cursors, uint2* out,
-                              long long chunk, const unsigned* flag);
+                              const PairDev* __restrict__ pairs, const unsigned char* __restrict__ bins,
+                              unsigned long long* cursors, uint2* out, long long chunk, const unsigned* flag);
 __global__ void k_bin_scan(const unsigned long long* counts, const unsigned long long* caps, const int* split_bins,
                            const unsigned long long* hist, unsigned long long* cursors, unsigned long long* ranges,
                            unsigned* overflow);
@@ -118,7 +121,7 @@ constexpr int NLIST = 2 * NCLASS;  // FP64 lists, then the FP32 lists of the pre
 // direct builds and one owned by its captured graph).
 struct BuildBufs {
   DevBuf dj, dk, djf, dkf, gj, gk, dsh, dshf, dmax, counts, primc, hist, cursor, work, ranges, caps, split, flag;
-  DevBuf lists[NLIST], slists[NLIST];
+  DevBuf lists[NLIST], slists[NLIST], bins[NLIST];
   unsigned long long cap[NLIST] = {0};
   bool sized = false;
   unsigned long long* h_rb = nullptr;  // pinned readback: [0] flag, [1, 1+NLIST) counts, then primitive counts
@@ -128,6 +131,7 @@ struct BuildBufs {
     for (DevBuf* x : b) x->release();
     for (auto& x : lists) x.release();
     for (auto& x : slists) x.release();
+    for (auto& x : bins) x.release();
     if (h_rb) cudaFreeHost(h_rb);
     h_rb = nullptr;
     sized = false;

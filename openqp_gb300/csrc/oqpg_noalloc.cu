@@ -154,7 +154,8 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
   for (int k = 0; k < NCLASS; ++k) {
     if (!h_counts[k]) continue;
     k_bin_hist<<<(unsigned)((h_counts[k] + 255) / 256), 256, 0, st>>>(lists + off[k], (long long)h_counts[k], nullptr,
-                                                                      c->d_pairs.as<PairDev>(), hist + k * NBIN);
+                                                                      c->d_pairs.as<PairDev>(), nullptr, 0.0f,
+                                                                      nullptr, hist + k * NBIN);
     NK(cudaGetLastError());
   }
   unsigned long long h_hist[NCLASS * NBIN], h_cur[NCLASS * NBIN];
@@ -170,7 +171,7 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
     if (!h_counts[k]) continue;
     const long long chunk = 4096;
     k_bin_scatter<<<(unsigned)((h_counts[k] + chunk - 1) / chunk), 256, 0, st>>>(
-        lists + off[k], (long long)h_counts[k], nullptr, c->d_pairs.as<PairDev>(), cursor + k * NBIN,
+        lists + off[k], (long long)h_counts[k], nullptr, c->d_pairs.as<PairDev>(), nullptr, cursor + k * NBIN,
         slists + off[k], chunk, nullptr);
     NK(cudaGetLastError());
   }

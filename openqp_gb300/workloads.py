@@ -146,3 +146,21 @@ def water_batch(nclusters, seed, nmin=1, nmax=16, basis="6-31g", overlap=None):
         bases.append(bas)
         dens.append(density(bas, nelectrons(bas) // 2, seed * 100003 + k, S=S))
     return [int(v) for v in sizes], bases, dens
+
+
+def d_lattice(n, spacing_angstrom, dexp):
+    """One uncontracted Cartesian d shell of exponent dexp on every point of an
+    n x n x n cubic lattice (spacing in A), point charges 6 on the sites: a
+    synthetic basis in which every shell quartet is (dd|dd)."""
+    import math
+    from .basis import BasisArrays, gauss_norm
+    g = np.arange(n) * spacing_angstrom * ANGSTROM
+    xyz = np.array([[x, y, z] for x in g for y in g for z in g])
+    m = len(xyz)
+    am = np.full(m, 2, dtype=np.int32)
+    naos = np.full(m, 6, dtype=np.int32)
+    return BasisArrays(am=am, ncontr=np.ones(m, dtype=np.int32), origin=np.arange(1, m + 1, dtype=np.int32),
+                       harmonic=np.zeros(m, dtype=np.int32), ex=np.full(m, float(dexp)),
+                       cc=np.full(m, 1.0 / math.sqrt(gauss_norm(2.0 * dexp, 2))), xyz=xyz,
+                       charges=np.full(m, 6.0), nbf=6 * m,
+                       ao_offset=np.arange(0, 6 * m, 6, dtype=np.int32), naos=naos)
