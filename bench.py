@@ -51,6 +51,9 @@ WORKLOADS = {
     # 256 water clusters of 1-16 molecules (uniform), 6-31G, built together
     "batch256_631g": dict(name="256 water clusters (1-16 H2O, uniform), 6-31G, batched RHF J+K builds", batch=256,
                           seed=0, basis="6-31g", cutoff=1e-10),
+    # the differentiation configuration: two-electron gradient of (H2O)16 6-31G(d)
+    "grad_water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian RHF two-electron gradient (grd2)", nwater=16,
+                               edge=9.52, seed=0, basis="6-31g(d)", cutoff=1e-10, grad=True),
     # (dd|dd) only: one Cartesian d shell (6-31G(d) carbon d, exponent 0.8) on each
     # point of a 4 x 4 x 4 cubic lattice of spacing 1.54 A, so that all 2080 pairs overlap
     "dd_only": dict(name="(dd|dd)-only: 64 Cartesian d shells (exponent 0.8) on a 4x4x4 lattice, 1.54 A spacing",
@@ -333,6 +336,74 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_grad(args):
+    """Gradient evaluations/s: the two-electron HF gradient (derivative ERIs
+    contracted with the two-particle density), D resident on the host side
+    of the C ABI (one H2D of the packed density and one D2H of dE/dR per
+    evaluation are inside the timed call)."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    from openqp_gb300 import build as bld
+    bld.build()
+    from openqp_gb300.fock import FockBuilder, fp64_peak_tflops
+    bas, d = make_workload()
+    fb = FockBuilder(bas, cutoff=WORKLOAD["cutoff"])
+    for _ in range(args.warmup):
+        fb.grad2(d)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    sampler = ClockSampler(local)
+    sampler.start()
+    times, g = [], None
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g = fb.grad2(d)
+        times.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    st = fb.grad_stats()
+    value = ws * args.steps / sum(times)
+    line = {"metric": "two-electron gradient evaluations/s", "value": value, "unit": "grad evals/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded water cluster and Loewdin density)",
+            "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "natom": bas.natom, "cutoff": WORKLOAD["cutoff"],
+                       "l2": "flushed (256 MB write) before every timed step"},
+            "e2e": {"value": value, "unit": "grad evals/s", "h2d_bytes_per_step": int(d.nbytes),
+                    "d2h_bytes_per_step": int(8 * 3 * bas.natom)},
+            "grad_stats": st, "quartets_per_s": st["quartets"] / (sum(times) / args.steps),
+            "prim_quartets_per_s": st["prim_quartets"] / (sum(times) / args.steps),
+            "fp64_peak_tflops": fp64_peak_tflops(), "clocks": clocks,
+            "max_abs_grad": float(np.abs(g).max()), "sum_grad": float(np.abs(g.sum(axis=0)).max())}
+    if not args.no_cpu and rank == 0:
+        line["cpu_baseline"] = cpu_baseline_grad(bas, d, args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_grad(bas, d, budget_s):
+    """The oracle's grd2 restatement (all host cores) on 1/stride of the bra
+    shell pairs, scaled by stride."""
+    from openqp_gb300.basis import unpack
+    from oracle import oracle
+    oracle.build()
+    o = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"])
+    D = unpack(d, bas.nbf)
+    cores = os.cpu_count()
+    t0 = time.perf_counter()
+    o.grad2e(D, nthreads=cores, stride=997, offset=0)
+    est = max((time.perf_counter() - t0) * 997, 1e-3)
+    stride = max(1, int(math.ceil(est / budget_s)))
+    t0 = time.perf_counter()
+    o.grad2e(D, nthreads=cores, stride=stride, offset=0)
+    t = (time.perf_counter() - t0) * stride
+    return {"value": 1.0 / t, "unit": "grad evals/s", "cores": cores, "kind": "port",
+            "sample": "oracle grd2 restatement (McMurchie-Davidson derivative integrals) over 1/%d of the bra shell "
+                      "pairs, x%d; %d quartets in the sample" % (stride, stride, o.last_grad2e_quartets)}
+
+
 def pct(v, q):
     return float(np.percentile(np.asarray(v), q))
 
@@ -553,6 +624,8 @@ def main():
         run_reference(args)
     elif "batch" in WORKLOAD:
         run_batch(args)
+    elif WORKLOAD.get("grad"):
+        run_grad(args)
     else:
         run_ours(args)
 

@@ -634,8 +634,11 @@ struct TeamSmem {
   static constexpr int PH1 = 2 * K::NR + K::NR * 3 * K::N2D;
   static constexpr int DJ = E::A * E::B + E::C * E::D;
   static constexpr int DK = E::A * E::C + E::A * E::D + E::B * E::C + E::B * E::D;
-  static constexpr int PH2 = 2 * K::NE + DJ + 2 * DK;
-  static constexpr int PER_WARP = cmax(PH1, PH2);   // elements of the kernel's type
+  // [0, NE): the quartet's accumulators (lane-owned elements), then the
+  // region shared by the primitive loop (roots, 2D tables), the pure
+  // projection (NE) and the digestion (density blocks)
+  static constexpr int REST = cmax(PH1, cmax(K::NE, DJ + 2 * DK));
+  static constexpr int PER_WARP = K::NE + REST;   // elements of the kernel's type
 };
 
 template <int LA, int LB, int LC, int LD, bool PURE, bool SCH, typename T>
@@ -646,29 +649,26 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
   using PP = typename PrimT<T>::type;
   constexpr int NE = K::NE, NR = K::NR, N2D = K::N2D, KE = (NE + 31) / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // packed 2D offsets (10 bits per dimension) of every Cartesian element,
+  // shared by the CTA: keeping them out of registers leaves room for twod
+  __shared__ int s_offs[NE];
   T* smem = reinterpret_cast<T*>(smem_raw);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* W = smem + warp * SM::PER_WARP;
-  T* RT = W;               // 2*NR: x_r, w_r * pref
-  T* I2 = W + 2 * NR;      // [r][d][N2D]
-  // packed 2D offsets of this lane's elements (same for every quartet)
-  int offs[KE];
+  T* V = W;                // [NE] accumulators, then the normalised block
+  T* RT = W + NE;          // 2*NR: x_r, w_r * pref
+  T* I2 = RT + 2 * NR;     // [r][d][N2D]
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+    const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
+              id = e % K::ND;
+    int ox[3];
 #pragma unroll
-  for (int k = 0; k < KE; ++k) {
-    const int e = lane + 32 * k;
-    int o = 0;
-    if (e < NE) {
-      const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
-                id = e % K::ND;
-      int ox[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d)
-        ox[d] = ((cart_e(LA, ia, d) * (LB + 1) + cart_e(LB, ib, d)) * (LC + 1) + cart_e(LC, ic, d)) * (LD + 1) +
-                cart_e(LD, id, d);
-      o = ox[0] | (ox[1] << 10) | (ox[2] << 20);
-    }
-    offs[k] = o;
+    for (int d = 0; d < 3; ++d)
+      ox[d] = ((cart_e(LA, ia, d) * (LB + 1) + cart_e(LB, ib, d)) * (LC + 1) + cart_e(LC, ic, d)) * (LD + 1) +
+              cart_e(LD, id, d);
+    s_offs[e] = ox[0] | (ox[1] << 10) | (ox[2] << 20);
   }
+  __syncthreads();
   const uint2* quartets;
   long long nquartets;
   work_range(a, quartets, nquartets);
@@ -681,9 +681,9 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
     T AB[3], CD[3];
     quartet_geometry<T>(a, qd, P, Q, AB, CD);
     const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
-    T acc[KE];
 #pragma unroll
-    for (int k = 0; k < KE; ++k) acc[k] = 0;
+    for (int k = 0; k < KE; ++k)
+      if (lane + 32 * k < NE) V[lane + 32 * k] = 0;
     const PP* bpp = prims_of<T>(a) + P.poff;
     const PP* kpp = prims_of<T>(a) + Q.poff;
     for (int kq = 0; kq < Q.pcnt; ++kq) {
@@ -720,22 +720,23 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
         __syncwarp();
 #pragma unroll
         for (int k = 0; k < KE; ++k) {
-          if (lane + 32 * k < NE) {
-            const int ox = offs[k] & 1023, oy = (offs[k] >> 10) & 1023, oz = offs[k] >> 20;
-            T v = acc[k];
+          const int e = lane + 32 * k;
+          if (e < NE) {
+            const int o = s_offs[e];
+            const int ox = o & 1023, oy = (o >> 10) & 1023, oz = o >> 20;
+            T v = V[e];
 #pragma unroll
             for (int r = 0; r < NR; ++r) {
               const T* g = I2 + r * 3 * N2D;
               v = fma(g[ox] * g[N2D + oy], g[2 * N2D + oz], v);
             }
-            acc[k] = v;
+            V[e] = v;
           }
         }
         __syncwarp();
       }
     }
     // ---- epilogue: V = normalised block in smem, pure projection in place
-    T* V = W;
     T* Tm = W + NE;
 #pragma unroll
     for (int k = 0; k < KE; ++k) {
@@ -746,7 +747,7 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
         // product of the component norms: sqrt(3)^n for n off-diagonal d components,
         // looked up rather than multiplied out (one FP64 multiply per element)
         const int n3 = (LA == 2 && ia >= 3) + (LB == 2 && ib >= 3) + (LC == 2 && ic >= 3) + (LD == 2 && id >= 3);
-        V[e] = (LA == 2 || LB == 2 || LC == 2 || LD == 2) ? acc[k] * sqrt3_pow<T>(n3) : acc[k];
+        if (LA == 2 || LB == 2 || LC == 2 || LD == 2) V[e] *= sqrt3_pow<T>(n3);
       }
     }
     __syncwarp();

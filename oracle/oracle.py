@@ -48,7 +48,7 @@ def lib():
         L.orc_boys.argtypes = [ctypes.c_int, ctypes.c_double, _d]
         L.orc_grad2e.restype = ctypes.c_longlong
         L.orc_grad2e.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
-                                 ctypes.c_int, _d]
+                                 ctypes.c_int, ctypes.c_int, ctypes.c_int, _d]
         L.orc_grad1e.argtypes = [ctypes.c_void_p, _d, _d, _d, _d]
         _lib = L
     return _lib
@@ -153,16 +153,17 @@ class Oracle:
         return out.reshape(n, n)
 
 
-    def grad2e(self, dt, ds=None, coulscale=1.0, hfscale=1.0, cutoff=1e-10, nthreads=None):
+    def grad2e(self, dt, ds=None, coulscale=1.0, hfscale=1.0, cutoff=1e-10, nthreads=None, stride=1, offset=0):
         """Two-electron HF gradient (natom, 3) of OpenQP's grd2 for the full AO
-        total density dt (and spin density ds for UHF/ROHF)."""
+        total density dt (and spin density ds for UHF/ROHF); stride > 1: only
+        the bra shell pairs with index % stride == offset (timing samples)."""
         n = self.nbf
         dt = np.ascontiguousarray(dt, dtype=np.float64).reshape(n, n)
         dsp = None if ds is None else np.ascontiguousarray(ds, dtype=np.float64).reshape(n, n)
         de = np.zeros(3 * self.bas.natom)
         nt = nthreads or os.cpu_count()
         nq = lib().orc_grad2e(self.h, _p(dt), None if dsp is None else _p(dsp), 4.0 * coulscale, hfscale, cutoff,
-                              nt, _p(de))
+                              nt, int(stride), int(offset), _p(de))
         self.last_grad2e_quartets = int(nq)
         return de.reshape(-1, 3)
 

@@ -217,9 +217,11 @@ extern "C" {
 // Ds: spin density (UHF/ROHF; null for RHF), both full nbf x nbf AO matrices.
 // Two-particle density G = cj Dt_ij Dt_kl - ck (Dt_ik Dt_jl + Dt_il Dt_jk
 // [+ Ds_ik Ds_jl + Ds_il Ds_jk]); OpenQP's HF values are cj = 4 coulscale,
-// ck = hfscale.  Returns the number of shell quartets evaluated.
+// ck = hfscale.  stride > 1 evaluates only the bra pairs ij with
+// ij % stride == offset (a bounded sample for timing).  Returns the number of
+// shell quartets evaluated.
 long long orc_grad2e(void* h, const double* Dt, const double* Ds, double cj, double ck, double cutoff, int nthreads,
-                     double* de) {
+                     int stride, int offset, double* de) {
   const Basis& B = ((Handle*)h)->B;
   const int ns = B.nshell;
   // grd2 pair cutoffs (grd2.F90:238-260): dabcut, 10^-20, 10^-20, 20 ln 10
@@ -260,6 +262,7 @@ long long orc_grad2e(void* h, const double* Dt, const double* Ds, double cj, dou
       for (int j = 0; j <= i; ++j) {
         const int ij = pair_id(i, j);
         if (PS.cnt[ij] == 0) continue;
+        if (stride > 1 && ij % stride != offset) continue;
         for (int k = 0; k <= i; ++k)
           for (int l = 0; l <= (k == i ? j : k); ++l) {
             const int kl = pair_id(k, l);
