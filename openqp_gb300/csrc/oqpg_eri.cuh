@@ -820,21 +820,24 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
     constexpr int NAB = E::A * E::B, NCD = E::C * E::D;
     constexpr int NAC = E::A * E::C, NAD = E::A * E::D, NBC = E::B * E::C, NBD = E::B * E::D;
     const int ntarget = NAB + NCD + a.nk * (NAC + NAD + NBC + NBD);
+    // Every target element is a strided dot product of V with a density block:
+    //   s = sum_{u < n1, v < n2} V[vb + u s1 + v s2] Dv[u n2 + v].
+    // Only the (integer) descriptor depends on the target kind, so the lanes of
+    // a round share one FP64 instruction stream whatever kinds they hold.
+    constexpr int BCD = E::B * E::C * E::D, CD_ = E::C * E::D;
     for (int o = lane; o < ntarget; o += 32) {
-      T s = 0;
+      int vb, s1, s2, n1, n2;
+      const T* dv;
       double* dst;
       double fac;
-      if (o < NAB) {
+      if (o < NAB) {          // J[a][b] += sum_cd V D[c][d]
         const int i = o / E::B, j = o % E::B;
-        const T* v = V + (size_t)o * NCD;
-#pragma unroll 4
-        for (int cd = 0; cd < NCD; ++cd) s = fma(v[cd], Dcd[cd], s);
+        vb = o * NCD; s1 = 0; s2 = 1; n1 = 1; n2 = NCD; dv = Dcd;
         dst = a.gj + (size_t)(ra + i) * n + ob + j;
         fac = 2.0 * f;
-      } else if (o < NAB + NCD) {
+      } else if (o < NAB + NCD) {  // J[c][d] += sum_ab V D[a][b]
         const int cd = o - NAB, k = cd / E::D, l = cd % E::D;
-#pragma unroll 4
-        for (int ab = 0; ab < NAB; ++ab) s = fma(V[(size_t)ab * NCD + cd], Dab[ab], s);
+        vb = cd; s1 = NCD; s2 = 0; n1 = NAB; n2 = 1; dv = Dab;
         dst = a.gj + (size_t)(rc + k) * n + od + l;
         fac = 2.0 * f;
       } else {
@@ -842,40 +845,35 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
         const int kk = r / (NAC + NAD + NBC + NBD);
         r -= kk * (NAC + NAD + NBC + NBD);
         const T* dk = Dk + kk * DKS;
-        const T* dac = dk;
-        const T* dad = dac + NAC;
-        const T* dbc = dad + NAD;
-        const T* dbd = dbc + NBC;
         double* gk = a.gk + (size_t)kk * a.kstride;
         fac = f;
         if (r < NAC) {  // K[a][c] += sum_bd V[a b c d] D[b][d]
           const int i = r / E::C, k = r % E::C;
-          for (int j = 0; j < E::B; ++j)
-#pragma unroll
-            for (int l = 0; l < E::D; ++l) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dbd[j * E::D + l], s);
+          vb = i * BCD + k * E::D; s1 = CD_; s2 = 1; n1 = E::B; n2 = E::D; dv = dk + NAC + NAD + NBC;
           dst = gk + (size_t)(ra + i) * n + oc + k;
         } else if (r < NAC + NAD) {  // K[a][d] += sum_bc V D[b][c]
           r -= NAC;
           const int i = r / E::D, l = r % E::D;
-          for (int j = 0; j < E::B; ++j)
-#pragma unroll
-            for (int k = 0; k < E::C; ++k) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dbc[j * E::C + k], s);
+          vb = i * BCD + l; s1 = CD_; s2 = E::D; n1 = E::B; n2 = E::C; dv = dk + NAC + NAD;
           dst = gk + (size_t)(ra + i) * n + od + l;
         } else if (r < NAC + NAD + NBC) {  // K[b][c] += sum_ad V D[a][d]
           r -= NAC + NAD;
           const int j = r / E::C, k = r % E::C;
-          for (int i = 0; i < E::A; ++i)
-#pragma unroll
-            for (int l = 0; l < E::D; ++l) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dad[i * E::D + l], s);
+          vb = j * CD_ + k * E::D; s1 = BCD; s2 = 1; n1 = E::A; n2 = E::D; dv = dk + NAC;
           dst = gk + (size_t)(rb + j) * n + oc + k;
         } else {  // K[b][d] += sum_ac V D[a][c]
           r -= NAC + NAD + NBC;
           const int j = r / E::D, l = r % E::D;
-          for (int i = 0; i < E::A; ++i)
-#pragma unroll
-            for (int k = 0; k < E::C; ++k) s = fma(V[((i * E::B + j) * E::C + k) * E::D + l], dac[i * E::C + k], s);
+          vb = j * CD_ + l; s1 = BCD; s2 = E::D; n1 = E::A; n2 = E::C; dv = dk;
           dst = gk + (size_t)(rb + j) * n + od + l;
         }
+      }
+      T s = 0;
+      const int nt = n1 * n2;
+      int u = 0, v = 0;
+      for (int t = 0; t < nt; ++t) {
+        s = fma(V[vb + u * s1 + v * s2], dv[t], s);
+        if (++v == n2) { v = 0; ++u; }
       }
       atomicAdd(dst, fac * (double)s);
     }
