@@ -51,6 +51,12 @@ WORKLOADS = {
     # 256 water clusters of 1-16 molecules (uniform), 6-31G, built together
     "batch256_631g": dict(name="256 water clusters (1-16 H2O, uniform), 6-31G, batched RHF J+K builds", batch=256,
                           seed=0, basis="6-31g", cutoff=1e-10),
+    # full direct SCF (RHF, DIIS, |dE| < 1e-9) of the headline cluster: builds/s inside the SCF
+    "scf_water32_ccpvdz": dict(name="(H2O)32 cc-pVDZ spherical RHF direct SCF (dE 1e-9, DIIS)", nwater=32, edge=14.0,
+                               seed=0, basis="cc-pvdz", cutoff=1e-10, scf=True),
+    # the precision-split configuration over a whole SCF: FP64 full builds vs mixed + incremental
+    "scf_alkane40_631gd": dict(name="C40H82 6-31G(d) RHF SCF: mixed precision + incremental dD vs plain FP64",
+                               alkane=40, seed=0, basis="6-31g(d)", cutoff=1e-10, scf=True, mixed_scf=True),
     # the differentiation configuration: two-electron gradient of (H2O)16 6-31G(d)
     "grad_water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian RHF two-electron gradient (grd2)", nwater=16,
                                edge=9.52, seed=0, basis="6-31g(d)", cutoff=1e-10, grad=True),
@@ -334,6 +340,81 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_scf_bench(args):
+    """Direct SCF with the GPU Fock build as its two-electron part (host
+    buffers through the C ABI in every iteration).  With mixed_scf: the same
+    SCF in plain FP64 (the reference energy) and with the precision split plus
+    incremental dD builds, energy error against the FP64 run."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    from openqp_gb300 import build as bld
+    bld.build()
+    from openqp_gb300 import onee, scf, workloads
+    from openqp_gb300.fock import FockBuilder
+    bas, d_warm = make_workload()
+    S, T, V = onee.one_electron(bas)
+    H = T + V
+    enuc = onee.nuclear_repulsion(bas)
+    nocc = workloads.nelectrons(bas) // 2
+    fb = FockBuilder(bas, cutoff=WORKLOAD["cutoff"])
+
+    def run(precision, incremental):
+        if precision == "fp64":
+            fb.set_precision("fp64")
+        else:
+            fb.set_precision(precision, args.mixed_threshold)
+        tb = []
+        stats = []
+
+        def fock2e(dp):
+            t0 = time.perf_counter()
+            f = fb.fock_jk(dp)
+            tb.append(time.perf_counter() - t0)
+            stats.append(fb.stats())
+            return f
+
+        fock2e(d_warm)   # warm-up build on the seeded density (sizes the quartet lists)
+        tb.clear(); stats.clear()
+        w0 = time.perf_counter()
+        r = scf.run_scf(bas.nbf, S, H, enuc, nocc, nocc, fock2e, kind="rhf", conv=1e-9, maxit=60,
+                        incremental=incremental)
+        wall = time.perf_counter() - w0
+        q = sum(s_["quartets"] for s_ in stats)
+        return dict(energy=r["energy"], converged=bool(r["converged"]), iterations=r["iterations"], builds=len(tb),
+                    build_s=sum(tb), wall_s=wall, builds_per_s=len(tb) / sum(tb), quartets_per_s=q / sum(tb),
+                    f32_quartet_fraction=(sum(s_["f32_quartets"] for s_ in stats) / max(1, q)))
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    ref = run("fp64", False)
+    mixed = None
+    if WORKLOAD.get("mixed_scf"):
+        prec = args.precision if args.precision != "fp64" else "mixed-fast"
+        mixed = run(prec, True)
+        mixed.update(mode=prec, threshold=args.mixed_threshold, incremental=True,
+                     dE_vs_fp64_Eh=mixed["energy"] - ref["energy"],
+                     speedup_build_time=ref["build_s"] / mixed["build_s"])
+    clocks = sampler.stop()
+    main_run = mixed if mixed else ref
+    line = {"metric": "J+K Fock builds/s inside a direct SCF", "value": main_run["builds_per_s"], "unit": "builds/s",
+            "n_gpus": ws, "steps": main_run["builds"], "warmup": 1,
+            "ms_per_step": 1000.0 * main_run["build_s"] / main_run["builds"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
+            "data": "synthetic (seeded geometry; core-Hamiltonian guess)",
+            "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "cutoff": WORKLOAD["cutoff"],
+                       "conv": "dE < 1e-9, DIIS error < 1e-6", "guess": "core Hamiltonian",
+                       "l2": "not flushed: consecutive SCF iterations (inputs ~5 MB)"},
+            "e2e": {"value": main_run["builds"] / main_run["wall_s"], "unit": "SCF iterations/s (wall, incl. host DIIS "
+                    "and diagonalisation)", "h2d_bytes_per_step": int(8 * bas.nbf * (bas.nbf + 1) // 2),
+                    "d2h_bytes_per_step": int(8 * bas.nbf * (bas.nbf + 1) // 2)},
+            "scf_fp64": ref, "clocks": clocks}
+    if mixed:
+        line["scf_mixed_incremental"] = mixed
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def run_grad(args):
@@ -626,6 +707,8 @@ def main():
         run_batch(args)
     elif WORKLOAD.get("grad"):
         run_grad(args)
+    elif WORKLOAD.get("scf"):
+        run_scf_bench(args)
     else:
         run_ours(args)
 
