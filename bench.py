@@ -446,6 +446,23 @@ def run_grad(args):
     clocks = sampler.stop()
     st = fb.grad_stats()
     value = ws * args.steps / sum(times)
+    # the same gradient with the precision split (FP32 below the bound), error against FP64
+    prec = args.precision if args.precision != "fp64" else "mixed-fast"
+    fb.set_precision(prec, args.mixed_threshold)
+    for _ in range(2):
+        gm = fb.grad2(d)
+    tm = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gm = fb.grad2(d)
+        tm.append(time.perf_counter() - t0)
+    stm = fb.grad_stats()
+    split = {"mode": prec, "threshold": args.mixed_threshold, "grad_evals_per_s": args.steps / sum(tm),
+             "speedup_vs_fp64": sum(times) / sum(tm), "max_abs_grad_error_Eh_bohr": float(np.abs(gm - g).max()),
+             "f32_quartet_fraction": stm["f32_quartets_listed"] / max(1, stm["quartets_listed"])}
+    fb.set_precision("fp64")
     line = {"metric": "two-electron gradient evaluations/s", "value": value, "unit": "grad evals/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(times) / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -456,7 +473,7 @@ def run_grad(args):
                     "d2h_bytes_per_step": int(8 * 3 * bas.natom)},
             "grad_stats": st, "quartets_per_s": st["quartets"] / (sum(times) / args.steps),
             "prim_quartets_per_s": st["prim_quartets"] / (sum(times) / args.steps),
-            "fp64_peak_tflops": fp64_peak_tflops(), "clocks": clocks,
+            "fp64_peak_tflops": fp64_peak_tflops(), "clocks": clocks, "precision_split": split,
             "max_abs_grad": float(np.abs(g).max()), "sum_grad": float(np.abs(g.sum(axis=0)).max())}
     if not args.no_cpu and rank == 0:
         line["cpu_baseline"] = cpu_baseline_grad(bas, d, args.cpu_budget)

@@ -223,7 +223,11 @@ int oqpg_grad2_bilinear(oqpg_ctx* ctx, const double* x, const double* y, const d
                         double cj, double ckt, double cks, double* de);
 
 /* Statistics of the last gradient: [0] quartets listed, [1] quartets
- * evaluated, [2] primitive quartets, [3] ms (lists + kernels). */
+ * evaluated, [2] primitive quartets, [3] ms (lists + kernels), [4] quartets
+ * listed for FP32 (precision split).  The gradient follows the context's
+ * precision split (oqpg_set_precision): quartets whose Schwarz bound times the
+ * bound of their two-particle density is below the threshold run in FP32 and
+ * add into the FP64 gradient. */
 int oqpg_grad_stats(const oqpg_ctx* ctx, double* out, int n);
 
 /* Angular momenta (la, lb, lc, ld) of class c (0 <= c < 21). */

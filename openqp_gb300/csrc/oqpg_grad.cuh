@@ -38,6 +38,13 @@ struct GradArgs {
   const PairDev* pairs;     // same pair order as the Fock tables
   const PrimPair* prims;    // primitive pairs with OpenQP's gradient cutoffs
   const double* alpha;      // exponent of the pair's first shell, per primitive pair
+  const PrimPairF* primsf;  // FP32 copies for the small-bound quartets of the precision split
+  const float* alphaf;
+  const float* xtf;         // FP32 copies of the Cartesian-effective matrices
+  const float* ytf;
+  const float* xsf;
+  const float* ysf;
+  int roots_f32;            // FP32 quartets: Rys roots/weights in FP32 too
   const uint2* quartets;
   long long nquartets;
   unsigned long long* work;
@@ -57,6 +64,24 @@ struct GradArgs {
   double* de;               // 3 x natom, accumulated
   unsigned long long* counters;  // [0] primitive quartets evaluated, [1] quartets evaluated
   int ctas_per_sm;
+};
+
+template <typename T> struct GAcc;
+template <> struct GAcc<double> {
+  static __device__ __forceinline__ const PrimPair* prims(const GradArgs& g) { return g.prims; }
+  static __device__ __forceinline__ double alpha(const GradArgs& g, int i) { return __ldg(g.alpha + i); }
+  static __device__ __forceinline__ const double* xt(const GradArgs& g) { return g.xt; }
+  static __device__ __forceinline__ const double* yt(const GradArgs& g) { return g.yt; }
+  static __device__ __forceinline__ const double* xs(const GradArgs& g) { return g.xs; }
+  static __device__ __forceinline__ const double* ys(const GradArgs& g) { return g.ys; }
+};
+template <> struct GAcc<float> {
+  static __device__ __forceinline__ const PrimPairF* prims(const GradArgs& g) { return g.primsf; }
+  static __device__ __forceinline__ float alpha(const GradArgs& g, int i) { return __ldg(g.alphaf + i); }
+  static __device__ __forceinline__ const float* xt(const GradArgs& g) { return g.xtf; }
+  static __device__ __forceinline__ const float* yt(const GradArgs& g) { return g.ytf; }
+  static __device__ __forceinline__ const float* xs(const GradArgs& g) { return g.xsf; }
+  static __device__ __forceinline__ const float* ys(const GradArgs& g) { return g.ysf; }
 };
 
 template <int LA, int LB, int LC, int LD>
@@ -79,32 +104,41 @@ struct GCls {
 
 // Two-particle density of Cartesian element (ra, rb, rc, rd) (matrix rows /
 // columns in the Cartesian layout).
-__device__ __forceinline__ double gamma_elem(const GradArgs& g, int ra, int rb, int rc, int rd) {
+template <typename T>
+__device__ __forceinline__ T gamma_elem(const GradArgs& g, int ra, int rb, int rc, int rd) {
   const int n = g.ncart;
-  auto X = [&](const double* M, int r, int c) { return __ldg(M + (size_t)r * n + c); };
-  double v = 0.5 * g.cj * (X(g.xt, ra, rb) * X(g.yt, rc, rd) + X(g.yt, ra, rb) * X(g.xt, rc, rd));
-  v -= 0.5 * g.ckt * (X(g.xt, ra, rc) * X(g.yt, rb, rd) + X(g.yt, ra, rc) * X(g.xt, rb, rd) +
-                      X(g.xt, ra, rd) * X(g.yt, rb, rc) + X(g.yt, ra, rd) * X(g.xt, rb, rc));
-  if (g.xs)
-    v -= 0.5 * g.cks * (X(g.xs, ra, rc) * X(g.ys, rb, rd) + X(g.ys, ra, rc) * X(g.xs, rb, rd) +
-                        X(g.xs, ra, rd) * X(g.ys, rb, rc) + X(g.ys, ra, rd) * X(g.xs, rb, rc));
+  const T* xt = GAcc<T>::xt(g);
+  const T* yt = GAcc<T>::yt(g);
+  auto X = [&](const T* M, int r, int c) { return __ldg(M + (size_t)r * n + c); };
+  T v = (T)(0.5 * g.cj) * (X(xt, ra, rb) * X(yt, rc, rd) + X(yt, ra, rb) * X(xt, rc, rd));
+  v -= (T)(0.5 * g.ckt) * (X(xt, ra, rc) * X(yt, rb, rd) + X(yt, ra, rc) * X(xt, rb, rd) +
+                           X(xt, ra, rd) * X(yt, rb, rc) + X(yt, ra, rd) * X(xt, rb, rc));
+  if (g.xs) {
+    const T* xs = GAcc<T>::xs(g);
+    const T* ys = GAcc<T>::ys(g);
+    v -= (T)(0.5 * g.cks) * (X(xs, ra, rc) * X(ys, rb, rd) + X(ys, ra, rc) * X(xs, rb, rd) +
+                             X(xs, ra, rd) * X(ys, rb, rc) + X(ys, ra, rd) * X(xs, rb, rc));
+  }
   return v;
 }
 
-__device__ __forceinline__ double warp_max(double v) {
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
 #pragma unroll
   for (int s = 16; s > 0; s >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, s));
   return v;
 }
-__device__ __forceinline__ double warp_sum(double v) {
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
   return v;
 }
 
 // Reduce the lanes' 9 partial sums (A, B, C x xyz), apply f, add to de.
+template <typename T>
 __device__ __forceinline__ void grad_store(const GradArgs& g, const PairDev& P, const PairDev& Q, uint2 qd,
-                                           double* acc, int lane) {
+                                           T* acc, int lane) {
 #pragma unroll
   for (int k = 0; k < 9; ++k) acc[k] = warp_sum(acc[k]);
   if (lane == 0) {
@@ -115,7 +149,7 @@ __device__ __forceinline__ void grad_store(const GradArgs& g, const PairDev& P, 
     const int at[4] = {__ldg(g.atom + P.sha), __ldg(g.atom + P.shb), __ldg(g.atom + Q.sha), __ldg(g.atom + Q.shb)};
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
-      const double a = f * acc[x], b = f * acc[3 + x], c = f * acc[6 + x];
+      const double a = f * (double)acc[x], b = f * (double)acc[3 + x], c = f * (double)acc[6 + x];
       atomicAdd(g.de + 3 * at[0] + x, a);
       atomicAdd(g.de + 3 * at[1] + x, b);
       atomicAdd(g.de + 3 * at[2] + x, c);
@@ -124,108 +158,118 @@ __device__ __forceinline__ void grad_store(const GradArgs& g, const PairDev& P, 
   }
 }
 
-template <int LA, int LB, int LC, int LD>
-__device__ __forceinline__ void quartet_setup(const GradArgs& g, uint2 qd, PairDev& P, PairDev& Q, double AB[3],
-                                              double CD[3], int ro[4]) {
+template <typename T>
+__device__ __forceinline__ void quartet_setup(const GradArgs& g, uint2 qd, PairDev& P, PairDev& Q, T AB[3],
+                                              T CD[3], int ro[4]) {
   P = g.pairs[qd.x];
   Q = g.pairs[qd.y];
   const ShellDev SA = g.shells[P.sha], SB = g.shells[P.shb], SC = g.shells[Q.sha], SD = g.shells[Q.shb];
-  AB[0] = SA.x - SB.x; AB[1] = SA.y - SB.y; AB[2] = SA.z - SB.z;
-  CD[0] = SC.x - SD.x; CD[1] = SC.y - SD.y; CD[2] = SC.z - SD.z;
+  AB[0] = (T)(SA.x - SB.x); AB[1] = (T)(SA.y - SB.y); AB[2] = (T)(SA.z - SB.z);
+  CD[0] = (T)(SC.x - SD.x); CD[1] = (T)(SC.y - SD.y); CD[2] = (T)(SC.z - SD.z);
   ro[0] = __ldg(g.coff + P.sha); ro[1] = __ldg(g.coff + P.shb);
   ro[2] = __ldg(g.coff + Q.sha); ro[3] = __ldg(g.coff + Q.shb);
 }
 
+// Primitive-quartet screens of grd2_rys_compute (grd2_rys.F90:361-372),
+// (sp sq)^2 < dtol2 (p + q) and (sp sq)^2 dabmax^2 < dabcut2 (p + q), written
+// without the squares so that FP32 quartets do not underflow.
+template <typename T>
+__device__ __forceinline__ bool grad_prim_skip(const GradArgs& g, T pfac, T dabmax, T s) {
+  const T a = fabs(pfac), rs = sqrt(s);
+  return a < (T)sqrt(g.dtol2) * rs || a * dabmax < (T)sqrt(g.dabcut2) * rs;
+}
+
 // ---------------------------------------------------------------------------
-template <int LA, int LB, int LC, int LD>
+template <int LA, int LB, int LC, int LD, typename T>
 __global__ void __launch_bounds__(128) k_grad_lane(const GradArgs g) {
   using K = Cls<LA, LB, LC, LD>;
   using G = GCls<LA, LB, LC, LD>;
+  using PP = typename PrimT<T>::type;
   constexpr int NE = K::NE, NR = G::NR, N2DX = G::N2DX;
-  __shared__ double s_gam[4][NE];
+  __shared__ T s_gam[4][NE];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double* gam = s_gam[warp];
+  T* gam = s_gam[warp];
+  const PP* prims = GAcc<T>::prims(g);
   unsigned long long nprim = 0, nq = 0;
   for (;;) {
     const long long t = grab(g.work, 1u, lane);
     if (t >= g.nquartets) break;
     const uint2 qd = g.quartets[t];
     PairDev P, Q;
-    double AB[3], CD[3];
+    T AB[3], CD[3];
     int ro[4];
-    quartet_setup<LA, LB, LC, LD>(g, qd, P, Q, AB, CD, ro);
-    double dmx = 0.0;
+    quartet_setup<T>(g, qd, P, Q, AB, CD, ro);
+    T dmx = 0;
     for (int e = lane; e < NE; e += 32) {
-      const double v = gamma_elem(g, ro[0] + G::ia(e), ro[1] + G::ib(e), ro[2] + G::ic(e), ro[3] + G::id(e));
+      const T v = gamma_elem<T>(g, ro[0] + G::ia(e), ro[1] + G::ib(e), ro[2] + G::ic(e), ro[3] + G::id(e));
       gam[e] = v;
-      const double nrm = cart_norm(LA, G::ia(e)) * cart_norm(LB, G::ib(e)) * cart_norm(LC, G::ic(e)) *
-                         cart_norm(LD, G::id(e));
+      const T nrm = (T)(cart_norm(LA, G::ia(e)) * cart_norm(LB, G::ib(e)) * cart_norm(LC, G::ic(e)) *
+                        cart_norm(LD, G::id(e)));
       dmx = fmax(dmx, g.pure ? fabs(v) : fabs(v) / nrm);
     }
-    const double dabmax = warp_max(dmx);
+    const T dabmax = warp_max(dmx);
     __syncwarp();
-    if (dabmax * __ldg(g.q + qd.x) * __ldg(g.q + qd.y) < g.cutoff2) continue;
+    if ((double)dabmax * __ldg(g.q + qd.x) * __ldg(g.q + qd.y) < g.cutoff2) continue;
     ++nq;
-    double acc[9];
+    T acc[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+    for (int k = 0; k < 9; ++k) acc[k] = 0;
     const int nP = P.pcnt, nQ = Q.pcnt;
     for (int pq = lane; pq < nP * nQ; pq += 32) {
       const int kq = pq / nP, kb = pq - kq * nP;
-      PrimPair bp, kp;
-      prim_load(g.prims + P.poff + kb, bp);
-      prim_load(g.prims + Q.poff + kq, kp);
-      const double pfac = bp.sp * kp.sp, test = pfac * pfac, s = bp.p + kp.p;
-      if (test < g.dtol2 * s || test * dabmax * dabmax < g.dabcut2 * s) continue;
+      PP bp, kp;
+      prim_load(prims + P.poff + kb, bp);
+      prim_load(prims + Q.poff + kq, kp);
+      if (grad_prim_skip<T>(g, bp.sp * kp.sp, dabmax, bp.p + kp.p)) continue;
       ++nprim;
-      PrimQuartet<double> pqd;
-      prim_setup<double>(bp, kp, pqd);
-      const double a2 = 2.0 * __ldg(g.alpha + P.poff + kb);
-      const double b2 = 2.0 * bp.p - a2;
-      const double c2 = 2.0 * __ldg(g.alpha + Q.poff + kq);
+      PrimQuartet<T> pqd;
+      prim_setup<T>(bp, kp, pqd);
+      const T a2 = (T)2 * GAcc<T>::alpha(g, P.poff + kb);
+      const T b2 = (T)2 * bp.p - a2;
+      const T c2 = (T)2 * GAcc<T>::alpha(g, Q.poff + kq);
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
-        const double u = rys_quantity<NR, double>(pqd.X, 2 * r);
-        const double w = rys_quantity<NR, double>(pqd.X, 2 * r + 1) * pqd.pref;
-        const double uq = u * pqd.qi, up = u * pqd.pi;
-        const double b00 = 0.5 * pqd.inv * u;
-        const double b10 = fma(-bp.hp, uq, bp.hp);
-        const double b01 = fma(-kp.hp, up, kp.hp);
-        double X[3][N2DX];
-        const double PA[3] = {bp.ax, bp.ay, bp.az}, QC[3] = {kp.ax, kp.ay, kp.az};
+        const T u = rys_quantity<NR, T>(pqd.X, 2 * r, g.roots_f32 != 0);
+        const T w = rys_quantity<NR, T>(pqd.X, 2 * r + 1, g.roots_f32 != 0) * pqd.pref;
+        const T uq = u * pqd.qi, up = u * pqd.pi;
+        const T b00 = (T)0.5 * pqd.inv * u;
+        const T b10 = fma(-bp.hp, uq, bp.hp);
+        const T b01 = fma(-kp.hp, up, kp.hp);
+        T X[3][N2DX];
+        const T PA[3] = {bp.ax, bp.ay, bp.az}, QC[3] = {kp.ax, kp.ay, kp.az};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          const double c00 = fma(-uq, pqd.PQ[d], PA[d]);
-          const double d00 = fma(up, pqd.PQ[d], QC[d]);
-          twod<LA + 1, LB, LC + 1, LD, double>(d == 2 ? w : 1.0, c00, d00, b00, b10, b01, AB[d], CD[d],
-                                               [&](int i, double v) { X[d][i] = v; });
+          const T c00 = fma(-uq, pqd.PQ[d], PA[d]);
+          const T d00 = fma(up, pqd.PQ[d], QC[d]);
+          twod<LA + 1, LB, LC + 1, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01, AB[d], CD[d],
+                                          [&](int i, T v) { X[d][i] = v; });
         }
 #pragma unroll
         for (int e = 0; e < NE; ++e) {
-          double I[3], dA[3], dB[3], dC[3];
+          T I[3], dA[3], dB[3], dC[3];
 #pragma unroll
           for (int d = 0; d < 3; ++d) {
             const int o = G::xoff(e, d);
             const int ea = cart_e(LA, G::ia(e), d), eb = cart_e(LB, G::ib(e), d), ec = cart_e(LC, G::ic(e), d);
             I[d] = X[d][o];
-            const double up1 = X[d][o + G::SA];
+            const T up1 = X[d][o + G::SA];
             dA[d] = a2 * up1;
-            if (ea > 0) dA[d] = fma(-(double)ea, X[d][o - G::SA], dA[d]);
+            if (ea > 0) dA[d] = fma(-(T)ea, X[d][o - G::SA], dA[d]);
             dB[d] = b2 * fma(AB[d], I[d], up1);
-            if (eb > 0) dB[d] = fma(-(double)eb, X[d][o - G::SB], dB[d]);
+            if (eb > 0) dB[d] = fma(-(T)eb, X[d][o - G::SB], dB[d]);
             dC[d] = c2 * X[d][o + G::SC];
-            if (ec > 0) dC[d] = fma(-(double)ec, X[d][o - G::SC], dC[d]);
+            if (ec > 0) dC[d] = fma(-(T)ec, X[d][o - G::SC], dC[d]);
           }
-          const double ge = gam[e];
-          const double tz = ge * I[2];
-          const double yz = I[1] * tz, xz = I[0] * tz, xy = I[0] * I[1] * ge;
+          const T ge = gam[e];
+          const T tz = ge * I[2];
+          const T yz = I[1] * tz, xz = I[0] * tz, xy = I[0] * I[1] * ge;
           acc[0] = fma(dA[0], yz, acc[0]); acc[1] = fma(dA[1], xz, acc[1]); acc[2] = fma(dA[2], xy, acc[2]);
           acc[3] = fma(dB[0], yz, acc[3]); acc[4] = fma(dB[1], xz, acc[4]); acc[5] = fma(dB[2], xy, acc[5]);
           acc[6] = fma(dC[0], yz, acc[6]); acc[7] = fma(dC[1], xz, acc[7]); acc[8] = fma(dC[2], xy, acc[8]);
         }
       }
     }
-    grad_store(g, P, Q, qd, acc, lane);
+    grad_store<T>(g, P, Q, qd, acc, lane);
     __syncwarp();
   }
   if (g.counters) {
@@ -241,21 +285,23 @@ struct GradTeamSmem {
   static constexpr int RT = 2 * G::NR;
   static constexpr int XT = 3 * G::NR * G::N2DX;
   static constexpr int TT = 3 * G::NR * 4 * G::N2D;   // per root x dim: I, dA, dB, dC
-  static constexpr int PER_WARP = RT + XT + TT;       // doubles
+  static constexpr int PER_WARP = RT + XT + TT;       // elements of the kernel's type
 };
 
-template <int LA, int LB, int LC, int LD>
+template <int LA, int LB, int LC, int LD, typename T>
 __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
   using K = Cls<LA, LB, LC, LD>;
   using G = GCls<LA, LB, LC, LD>;
   using SM = GradTeamSmem<LA, LB, LC, LD>;
+  using PP = typename PrimT<T>::type;
   constexpr int NE = K::NE, NR = G::NR, N2D = G::N2D, N2DX = G::N2DX, KE = (NE + 31) / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double* W = reinterpret_cast<double*>(smem_raw) + (size_t)warp * SM::PER_WARP;
-  double* RT = W;
-  double* XT = W + SM::RT;
-  double* TT = XT + SM::XT;
+  T* W = reinterpret_cast<T*>(smem_raw) + (size_t)warp * SM::PER_WARP;
+  T* RT = W;
+  T* XT = W + SM::RT;
+  T* TT = XT + SM::XT;
+  const PP* prims = GAcc<T>::prims(g);
   // this lane's elements: packed offsets into the per-dim tables
   int offs[KE];
 #pragma unroll
@@ -276,62 +322,61 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
     if (t >= g.nquartets) break;
     const uint2 qd = g.quartets[t];
     PairDev P, Q;
-    double AB[3], CD[3];
+    T AB[3], CD[3];
     int ro[4];
-    quartet_setup<LA, LB, LC, LD>(g, qd, P, Q, AB, CD, ro);
-    double gam[KE];
-    double dmx = 0.0;
+    quartet_setup<T>(g, qd, P, Q, AB, CD, ro);
+    T gam[KE];
+    T dmx = 0;
 #pragma unroll
     for (int k = 0; k < KE; ++k) {
       const int e = lane + 32 * k;
-      gam[k] = 0.0;
+      gam[k] = 0;
       if (e < NE) {
-        const double v = gamma_elem(g, ro[0] + G::ia(e), ro[1] + G::ib(e), ro[2] + G::ic(e), ro[3] + G::id(e));
+        const T v = gamma_elem<T>(g, ro[0] + G::ia(e), ro[1] + G::ib(e), ro[2] + G::ic(e), ro[3] + G::id(e));
         gam[k] = v;
-        const double nrm = cart_norm(LA, G::ia(e)) * cart_norm(LB, G::ib(e)) * cart_norm(LC, G::ic(e)) *
-                           cart_norm(LD, G::id(e));
+        const T nrm = (T)(cart_norm(LA, G::ia(e)) * cart_norm(LB, G::ib(e)) * cart_norm(LC, G::ic(e)) *
+                          cart_norm(LD, G::id(e)));
         dmx = fmax(dmx, g.pure ? fabs(v) : fabs(v) / nrm);
       }
     }
-    const double dabmax = warp_max(dmx);
-    if (dabmax * __ldg(g.q + qd.x) * __ldg(g.q + qd.y) < g.cutoff2) continue;
+    const T dabmax = warp_max(dmx);
+    if ((double)dabmax * __ldg(g.q + qd.x) * __ldg(g.q + qd.y) < g.cutoff2) continue;
     ++nq;
-    double acc[9];
+    T acc[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+    for (int k = 0; k < 9; ++k) acc[k] = 0;
     for (int kq = 0; kq < Q.pcnt; ++kq) {
-      PrimPair kp;
-      prim_load(g.prims + Q.poff + kq, kp);
-      const double c2 = 2.0 * __ldg(g.alpha + Q.poff + kq);
+      PP kp;
+      prim_load(prims + Q.poff + kq, kp);
+      const T c2 = (T)2 * GAcc<T>::alpha(g, Q.poff + kq);
       for (int kb = 0; kb < P.pcnt; ++kb) {
-        PrimPair bp;
-        prim_load(g.prims + P.poff + kb, bp);
-        const double pfac = bp.sp * kp.sp, test = pfac * pfac, s = bp.p + kp.p;
-        if (test < g.dtol2 * s || test * dabmax * dabmax < g.dabcut2 * s) continue;
+        PP bp;
+        prim_load(prims + P.poff + kb, bp);
+        if (grad_prim_skip<T>(g, bp.sp * kp.sp, dabmax, bp.p + kp.p)) continue;
         ++nprim;
-        PrimQuartet<double> pqd;
-        prim_setup<double>(bp, kp, pqd);
-        const double a2 = 2.0 * __ldg(g.alpha + P.poff + kb);
-        const double b2 = 2.0 * bp.p - a2;
+        PrimQuartet<T> pqd;
+        prim_setup<T>(bp, kp, pqd);
+        const T a2 = (T)2 * GAcc<T>::alpha(g, P.poff + kb);
+        const T b2 = (T)2 * bp.p - a2;
         if (lane < 2 * NR) {
-          const double v = rys_quantity<NR, double>(pqd.X, lane);
+          const T v = rys_quantity<NR, T>(pqd.X, lane, g.roots_f32 != 0);
           RT[lane] = (lane & 1) ? v * pqd.pref : v;
         }
         __syncwarp();
         if (lane < 3 * NR) {
           const int r = lane / 3, d = lane - 3 * r;
-          const double u = RT[2 * r], w = RT[2 * r + 1];
-          const double uq = u * pqd.qi, up = u * pqd.pi;
-          const double b00 = 0.5 * pqd.inv * u;
-          const double b10 = fma(-bp.hp, uq, bp.hp);
-          const double b01 = fma(-kp.hp, up, kp.hp);
-          const double pqv = pick3(d, pqd.PQ[0], pqd.PQ[1], pqd.PQ[2]);
-          const double c00 = fma(-uq, pqv, pick3(d, bp.ax, bp.ay, bp.az));
-          const double d00 = fma(up, pqv, pick3(d, kp.ax, kp.ay, kp.az));
-          double* dst = XT + (r * 3 + d) * N2DX;
-          twod<LA + 1, LB, LC + 1, LD, double>(d == 2 ? w : 1.0, c00, d00, b00, b10, b01,
-                                               pick3(d, AB[0], AB[1], AB[2]), pick3(d, CD[0], CD[1], CD[2]),
-                                               [&](int i, double v) { dst[i] = v; });
+          const T u = RT[2 * r], w = RT[2 * r + 1];
+          const T uq = u * pqd.qi, up = u * pqd.pi;
+          const T b00 = (T)0.5 * pqd.inv * u;
+          const T b10 = fma(-bp.hp, uq, bp.hp);
+          const T b01 = fma(-kp.hp, up, kp.hp);
+          const T pqv = pick3(d, pqd.PQ[0], pqd.PQ[1], pqd.PQ[2]);
+          const T c00 = fma(-uq, pqv, pick3(d, bp.ax, bp.ay, bp.az));
+          const T d00 = fma(up, pqv, pick3(d, kp.ax, kp.ay, kp.az));
+          T* dst = XT + (r * 3 + d) * N2DX;
+          twod<LA + 1, LB, LC + 1, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01,
+                                          pick3(d, AB[0], AB[1], AB[2]), pick3(d, CD[0], CD[1], CD[2]),
+                                          [&](int i, T v) { dst[i] = v; });
         }
         __syncwarp();
         // derivative tables: per root x dim, I, dA, dB, dC over the unraised entries
@@ -340,32 +385,32 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
           const int a = n / ((LB + 1) * (LC + 1) * (LD + 1)), b = (n / ((LC + 1) * (LD + 1))) % (LB + 1),
                     c = (n / (LD + 1)) % (LC + 1), dd = n % (LD + 1);
           const int o = ((a * (LB + 1) + b) * (LC + 2) + c) * (LD + 1) + dd;
-          const double* X = XT + rd * N2DX;
-          const double i0 = X[o], up1 = X[o + G::SA];
-          double vA = a2 * up1, vB = b2 * fma(pick3(d, AB[0], AB[1], AB[2]), i0, up1), vC = c2 * X[o + G::SC];
-          if (a > 0) vA = fma(-(double)a, X[o - G::SA], vA);
-          if (b > 0) vB = fma(-(double)b, X[o - G::SB], vB);
-          if (c > 0) vC = fma(-(double)c, X[o - G::SC], vC);
-          double* T = TT + rd * 4 * N2D;
-          T[n] = i0;
-          T[N2D + n] = vA;
-          T[2 * N2D + n] = vB;
-          T[3 * N2D + n] = vC;
+          const T* X = XT + rd * N2DX;
+          const T i0 = X[o], up1 = X[o + G::SA];
+          T vA = a2 * up1, vB = b2 * fma(pick3(d, AB[0], AB[1], AB[2]), i0, up1), vC = c2 * X[o + G::SC];
+          if (a > 0) vA = fma(-(T)a, X[o - G::SA], vA);
+          if (b > 0) vB = fma(-(T)b, X[o - G::SB], vB);
+          if (c > 0) vC = fma(-(T)c, X[o - G::SC], vC);
+          T* Tb = TT + rd * 4 * N2D;
+          Tb[n] = i0;
+          Tb[N2D + n] = vA;
+          Tb[2 * N2D + n] = vB;
+          Tb[3 * N2D + n] = vC;
         }
         __syncwarp();
 #pragma unroll
         for (int k = 0; k < KE; ++k) {
           if (lane + 32 * k < NE) {
             const int ox = offs[k] & 1023, oy = (offs[k] >> 10) & 1023, oz = offs[k] >> 20;
-            const double ge = gam[k];
+            const T ge = gam[k];
 #pragma unroll
             for (int r = 0; r < NR; ++r) {
-              const double* tx = TT + (r * 3 + 0) * 4 * N2D;
-              const double* ty = TT + (r * 3 + 1) * 4 * N2D;
-              const double* tz = TT + (r * 3 + 2) * 4 * N2D;
-              const double ix = tx[ox], iy = ty[oy], iz = tz[oz];
-              const double t1 = ge * iz;
-              const double yz = iy * t1, xz = ix * t1, xy = ix * iy * ge;
+              const T* tx = TT + (r * 3 + 0) * 4 * N2D;
+              const T* ty = TT + (r * 3 + 1) * 4 * N2D;
+              const T* tz = TT + (r * 3 + 2) * 4 * N2D;
+              const T ix = tx[ox], iy = ty[oy], iz = tz[oz];
+              const T t1 = ge * iz;
+              const T yz = iy * t1, xz = ix * t1, xy = ix * iy * ge;
               acc[0] = fma(tx[N2D + ox], yz, acc[0]);
               acc[1] = fma(ty[N2D + oy], xz, acc[1]);
               acc[2] = fma(tz[N2D + oz], xy, acc[2]);
@@ -381,7 +426,7 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
         __syncwarp();
       }
     }
-    grad_store(g, P, Q, qd, acc, lane);
+    grad_store<T>(g, P, Q, qd, acc, lane);
     __syncwarp();
   }
   if (g.counters) {
@@ -395,11 +440,11 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
 template <int LA, int LB, int LC, int LD>
 constexpr bool grad_lane_class() { return 3 * GCls<LA, LB, LC, LD>::N2DX <= 48; }
 
-template <int LA, int LB, int LC, int LD>
-cudaError_t launch_grad_cls(const GradArgs& g, int nsm, cudaStream_t st) {
+template <int LA, int LB, int LC, int LD, typename T>
+cudaError_t launch_grad_t(const GradArgs& g, int nsm, cudaStream_t st) {
   if (g.nquartets <= 0) return cudaSuccess;
   if constexpr (grad_lane_class<LA, LB, LC, LD>()) {
-    auto kern = k_grad_lane<LA, LB, LC, LD>;
+    auto kern = k_grad_lane<LA, LB, LC, LD, T>;
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0);
     if (g.ctas_per_sm > 0 && g.ctas_per_sm < per_sm) per_sm = g.ctas_per_sm;
@@ -408,8 +453,8 @@ cudaError_t launch_grad_cls(const GradArgs& g, int nsm, cudaStream_t st) {
     if (blocks > (long long)nsm * per_sm) blocks = (long long)nsm * per_sm;
     kern<<<(unsigned)blocks, 128, 0, st>>>(g);
   } else {
-    auto kern = k_grad_team<LA, LB, LC, LD>;
-    constexpr size_t per_warp = sizeof(double) * GradTeamSmem<LA, LB, LC, LD>::PER_WARP;
+    auto kern = k_grad_team<LA, LB, LC, LD, T>;
+    constexpr size_t per_warp = sizeof(T) * GradTeamSmem<LA, LB, LC, LD>::PER_WARP;
     int warps = (int)((200 * 1024) / per_warp);
     if (warps > 4) warps = 4;
     if (warps < 1) warps = 1;
@@ -427,6 +472,12 @@ cudaError_t launch_grad_cls(const GradArgs& g, int nsm, cudaStream_t st) {
     kern<<<(unsigned)blocks, 32 * warps, smem, st>>>(g);
   }
   return cudaGetLastError();
+}
+
+// f32: the FP32 quartets of the precision split.
+template <int LA, int LB, int LC, int LD>
+cudaError_t launch_grad_cls(const GradArgs& g, bool f32, int nsm, cudaStream_t st) {
+  return f32 ? launch_grad_t<LA, LB, LC, LD, float>(g, nsm, st) : launch_grad_t<LA, LB, LC, LD, double>(g, nsm, st);
 }
 
 }  // namespace oqpg

@@ -4,14 +4,14 @@
 
 namespace oqpg {
 
-cudaError_t launch_grad_b(int c, const GradArgs& g, int nsm, cudaStream_t st) {
+cudaError_t launch_grad_b(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st) {
   switch (c) {
-    case 15: return launch_grad_cls<1, 1, 1, 1>(g, nsm, st);
-    case 16: return launch_grad_cls<1, 1, 1, 2>(g, nsm, st);
-    case 17: return launch_grad_cls<1, 1, 2, 2>(g, nsm, st);
-    case 18: return launch_grad_cls<1, 2, 1, 2>(g, nsm, st);
-    case 19: return launch_grad_cls<1, 2, 2, 2>(g, nsm, st);
-    case 20: return launch_grad_cls<2, 2, 2, 2>(g, nsm, st);
+    case 15: return launch_grad_cls<1, 1, 1, 1>(g, f32, nsm, st);
+    case 16: return launch_grad_cls<1, 1, 1, 2>(g, f32, nsm, st);
+    case 17: return launch_grad_cls<1, 1, 2, 2>(g, f32, nsm, st);
+    case 18: return launch_grad_cls<1, 2, 1, 2>(g, f32, nsm, st);
+    case 19: return launch_grad_cls<1, 2, 2, 2>(g, f32, nsm, st);
+    case 20: return launch_grad_cls<2, 2, 2, 2>(g, f32, nsm, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -20,7 +20,9 @@ namespace oqpg {
 // four shells on one atom (zero by translational invariance), and an upper
 // bound of the two-particle density with the shell maxima Dm,
 // |cj| Dm_ij Dm_kl + ck (Dm_ik Dm_jl + Dm_il Dm_jk), not below cutoff / 2 /
-// (Q_P Q_Q); the kernels apply the exact dabmax test.
+// (Q_P Q_Q); the kernels apply the exact dabmax test.  With the precision
+// split, quartets whose bound Q_P Q_Q x that density bound is below tau32 go
+// to the FP32 lists.
 struct GListArgs {
   int npair, ns;
   const int2* pair_ij;
@@ -32,15 +34,16 @@ struct GListArgs {
   const double* dsh;
   const int* atom;
   double cj, ck, cutoff, cutoff2;
-  unsigned long long* counts;
-  uint2* lists[NCLASS];
-  unsigned long long caps[NCLASS];
+  double tau32;                 // bound below tau32: FP32 list (0: none)
+  unsigned long long* counts;   // NLIST: FP64 lists, then FP32 lists
+  uint2* lists[NLIST];
+  unsigned long long caps[NLIST];
   int write;
 };
 
 __global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
-  __shared__ unsigned cnt[NCLASS];
-  __shared__ unsigned long long base[NCLASS];
+  __shared__ unsigned cnt[NLIST];
+  __shared__ unsigned long long base[NLIST];
   __shared__ int s_len;
   const int P = blockIdx.x;
   if (a.gpairs[P].pcnt == 0) return;
@@ -64,7 +67,7 @@ __global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
   const double* dj = a.dsh + (long long)ij.y * a.ns;
   const int ati = a.atom[ij.x], atj = a.atom[ij.y];
   for (int s0 = 0; s0 < len; s0 += blockDim.x) {
-    if (threadIdx.x < NCLASS) cnt[threadIdx.x] = 0;
+    if (threadIdx.x < NLIST) cnt[threadIdx.x] = 0;
     __syncthreads();
     const int s = s0 + threadIdx.x;
     const int Q = s < len ? a.sorted_idx[s] : 0x7fffffff;
@@ -81,11 +84,12 @@ __global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
         const int tQ = a.pair_type[Q];
         if (tP <= tQ) { c = tP * 6 - tP * (tP - 1) / 2 + (tQ - tP); ent = make_uint2(P, Q); }
         else { c = tQ * 6 - tQ * (tQ - 1) / 2 + (tP - tQ); ent = make_uint2(Q, P); }
+        if (g * bound < a.tau32) c += NCLASS;
         slot = atomicAdd(&cnt[c], 1u);
       }
     }
     __syncthreads();
-    if (threadIdx.x < NCLASS && cnt[threadIdx.x])
+    if (threadIdx.x < NLIST && cnt[threadIdx.x])
       base[threadIdx.x] = atomicAdd(&a.counts[threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
     __syncthreads();
     if (c >= 0 && a.write) {
@@ -101,8 +105,6 @@ __global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
 using namespace oqpg;
 
 namespace {
-
-std::mutex g_grad_mutex;
 
 int gstatus(cudaError_t e) {
   if (e == cudaSuccess) return OK;
@@ -139,6 +141,16 @@ int grad_init(oqpg_ctx* c) {
   if ((rc = gupload(c->d_gpairs, gp.pairs, st))) return rc;
   if ((rc = gupload(c->d_gprims, gp.prims, st))) return rc;
   if ((rc = gupload(c->d_galpha, gp.alpha, st))) return rc;
+  std::vector<PrimPairF> pf(gp.prims.size());
+  std::vector<float> af(gp.alpha.size());
+  for (size_t i = 0; i < pf.size(); ++i) {
+    const PrimPair& q = gp.prims[i];
+    pf[i] = PrimPairF{(float)q.p, (float)q.hp, (float)q.px, (float)q.py, (float)q.pz,
+                      (float)q.ax, (float)q.ay, (float)q.az, (float)q.sp, 0.0f};
+    af[i] = (float)gp.alpha[i];
+  }
+  if ((rc = gupload(c->d_gprimsf, pf, st))) return rc;
+  if ((rc = gupload(c->d_galphaf, af, st))) return rc;
   c->coff.resize(c->nshell);
   int n = 0;
   for (int s = 0; s < c->nshell; ++s) { c->coff[s] = n; n += ncart(c->h_am[s]); }
@@ -211,10 +223,17 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
       }
   cudaEvent_t e0 = c->ev[0], e1 = c->ev[3];
   GK(cudaEventRecord(e0, st));
+  const bool split = (c->precision_mode == 1 || c->precision_mode == 2) && c->tau_f32 > 0.0;
   if ((rc = gupload(c->d_gmat, mats, st))) return rc;
+  if (split) {
+    std::vector<float> matsf(mats.size());
+    for (size_t k = 0; k < mats.size(); ++k) matsf[k] = (float)mats[k];
+    if ((rc = gupload(c->d_gmatf, matsf, st))) return rc;
+    GK(cudaStreamSynchronize(st));  // matsf is freed at the end of this scope
+  }
   if ((rc = gupload(c->d_dshg, dsh, st))) return rc;
-  GK(c->d_gcounts.ensure(sizeof(unsigned long long) * NCLASS));
-  GK(c->d_gwork.ensure(sizeof(unsigned long long) * NCLASS));
+  GK(c->d_gcounts.ensure(sizeof(unsigned long long) * NLIST));
+  GK(c->d_gwork.ensure(sizeof(unsigned long long) * NLIST));
   GK(c->d_gcnt.ensure(sizeof(unsigned long long) * 2));
   GK(c->d_de.ensure(sizeof(double) * 3 * c->natom));
   GListArgs la{};
@@ -231,18 +250,19 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
   la.ck = std::fabs(ckt) + std::fabs(cks);
   la.cutoff = cutoff;
   la.cutoff2 = 0.5 * cutoff;
+  la.tau32 = split ? c->tau_f32 : 0.0;
   la.counts = c->d_gcounts.as<unsigned long long>();
-  unsigned long long counts[NCLASS];
+  unsigned long long counts[NLIST];
   for (int pass = 0; pass < 3; ++pass) {
     la.write = 1;
-    for (int k = 0; k < NCLASS; ++k) { la.lists[k] = c->d_glists[k].as<uint2>(); la.caps[k] = c->gcaps[k]; }
-    GK(cudaMemsetAsync(c->d_gcounts.p, 0, sizeof(unsigned long long) * NCLASS, st));
+    for (int k = 0; k < NLIST; ++k) { la.lists[k] = c->d_glists[k].as<uint2>(); la.caps[k] = c->gcaps[k]; }
+    GK(cudaMemsetAsync(c->d_gcounts.p, 0, sizeof(unsigned long long) * NLIST, st));
     k_grad_lists<<<c->npair, 256, 0, st>>>(la);
     GK(cudaGetLastError());
     GK(cudaMemcpyAsync(counts, c->d_gcounts.p, sizeof(counts), cudaMemcpyDeviceToHost, st));
     GK(cudaStreamSynchronize(st));
     bool ok = true;
-    for (int k = 0; k < NCLASS; ++k)
+    for (int k = 0; k < NLIST; ++k)
       if (counts[k] > c->gcaps[k]) {
         ok = false;
         const unsigned long long cap = counts[k] + counts[k] / 8 + 1024;
@@ -253,17 +273,26 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
     if (pass == 2) return DEV_ERR;
   }
   GK(cudaMemsetAsync(c->d_de.p, 0, sizeof(double) * 3 * c->natom, st));
-  GK(cudaMemsetAsync(c->d_gwork.p, 0, sizeof(unsigned long long) * NCLASS, st));
+  GK(cudaMemsetAsync(c->d_gwork.p, 0, sizeof(unsigned long long) * NLIST, st));
   GK(cudaMemsetAsync(c->d_gcnt.p, 0, sizeof(unsigned long long) * 2, st));
   GradArgs g{};
   g.shells = c->d_shells.as<ShellDev>();
   g.pairs = c->d_gpairs.as<PairDev>();
   g.prims = c->d_gprims.as<PrimPair>();
   g.alpha = c->d_galpha.as<double>();
+  g.primsf = c->d_gprimsf.as<PrimPairF>();
+  g.alphaf = c->d_galphaf.as<float>();
   const double* dm = c->d_gmat.as<double>();
   g.xt = dm; g.yt = dm + n2;
   g.xs = xs ? dm + 2 * n2 : nullptr;
   g.ys = xs ? dm + 3 * n2 : nullptr;
+  if (split) {
+    const float* fm = c->d_gmatf.as<float>();
+    g.xtf = fm; g.ytf = fm + n2;
+    g.xsf = xs ? fm + 2 * n2 : nullptr;
+    g.ysf = xs ? fm + 3 * n2 : nullptr;
+  }
+  g.roots_f32 = c->precision_mode == 2 ? 1 : 0;
   g.ncart = nc;
   g.coff = c->d_coff.as<int>();
   g.atom = c->d_atom.as<int>();
@@ -281,14 +310,17 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
   g.dabcut2 = dabcut * dabcut;
   g.de = c->d_de.as<double>();
   g.counters = c->d_gcnt.as<unsigned long long>();
-  double listed = 0;
-  for (int cl = NCLASS - 1; cl >= 0; --cl) {
-    if (!counts[cl]) continue;
-    listed += (double)counts[cl];
-    g.quartets = c->d_glists[cl].as<uint2>();
-    g.nquartets = (long long)counts[cl];
-    g.work = c->d_gwork.as<unsigned long long>() + cl;
-    GK(cl < 15 ? launch_grad_a(cl, g, c->nsm, st) : launch_grad_b(cl, g, c->nsm, st));
+  double listed = 0, listed32 = 0;
+  for (int li = NLIST - 1; li >= 0; --li) {
+    if (!counts[li]) continue;
+    const int cl = li % NCLASS;
+    const bool f32 = li >= NCLASS;
+    listed += (double)counts[li];
+    if (f32) listed32 += (double)counts[li];
+    g.quartets = c->d_glists[li].as<uint2>();
+    g.nquartets = (long long)counts[li];
+    g.work = c->d_gwork.as<unsigned long long>() + li;
+    GK(cl < 15 ? launch_grad_a(cl, g, f32, c->nsm, st) : launch_grad_b(cl, g, f32, c->nsm, st));
   }
   std::vector<double> h_de(3 * c->natom);
   unsigned long long h_cnt[2];
@@ -303,6 +335,7 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
   c->grad_stats[1] = (double)h_cnt[1];
   c->grad_stats[2] = (double)h_cnt[0];
   c->grad_stats[3] = ms;
+  c->grad_stats[4] = listed32;
   return OK;
 }
 
@@ -349,7 +382,7 @@ int oqpg_grad2_bilinear(oqpg_ctx* ctx, const double* x, const double* y, const d
 
 int oqpg_grad_stats(const oqpg_ctx* ctx, double* out, int n) {
   if (!ctx) return NOT_INIT;
-  for (int i = 0; i < n && i < 4; ++i) out[i] = ctx->grad_stats[i];
+  for (int i = 0; i < n && i < 5; ++i) out[i] = ctx->grad_stats[i];
   return OK;
 }
 

@@ -653,10 +653,14 @@ void ctx_free(oqpg_ctx* c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   DevBuf* bufs[] = {&c->d_shells, &c->d_pairs, &c->d_prims, &c->d_pair_ij, &c->d_pair_type, &c->d_q, &c->d_qf,
                     &c->d_aoff, &c->d_naos, &c->d_mols, &c->d_pair_mol, &c->d_row_mol, &c->d_primsf,
-                    &c->d_sorted_idx, &c->d_sorted_q, &c->d_dp, &c->d_f, &c->d_fold, &c->d_gin, &c->d_gout};
+                    &c->d_sorted_idx, &c->d_sorted_q, &c->d_dp, &c->d_f, &c->d_fold, &c->d_gin, &c->d_gout,
+                    &c->d_gpairs, &c->d_gprims, &c->d_galpha, &c->d_gprimsf, &c->d_galphaf, &c->d_coff,
+                    &c->d_atom, &c->d_gmat, &c->d_gmatf, &c->d_dshg, &c->d_gcounts, &c->d_gwork, &c->d_de,
+                    &c->d_gcnt};
   for (DevBuf* b : bufs) b->release();
   c->hb.release();
   c->gb.release();
+  for (auto& b : c->d_glists) b.release();
   if (c->h_in) cudaFreeHost(c->h_in);
   if (c->h_out) cudaFreeHost(c->h_out);
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);

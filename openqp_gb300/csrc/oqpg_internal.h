@@ -112,8 +112,8 @@ namespace oqpg {
 void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vector<int>& ncontr,
                  const std::vector<int>& poff, const double* ex, const double* cc, double qcut, double ecut,
                  bool sp_screen, HostPairs& out);
-cudaError_t launch_grad_a(int c, const GradArgs& g, int nsm, cudaStream_t st);
-cudaError_t launch_grad_b(int c, const GradArgs& g, int nsm, cudaStream_t st);
+cudaError_t launch_grad_a(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
+cudaError_t launch_grad_b(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
 
 constexpr int NLIST = 2 * NCLASS;  // FP64 lists, then the FP32 lists of the precision split
 
@@ -190,10 +190,11 @@ struct oqpg_ctx {
   bool grad_ready = false;
   int ncart = 0;
   std::vector<int> coff;
-  oqpg::DevBuf d_gpairs, d_gprims, d_galpha, d_coff, d_atom, d_gmat, d_dshg, d_gcounts, d_gwork, d_de, d_gcnt;
-  oqpg::DevBuf d_glists[oqpg::NCLASS];
-  unsigned long long gcaps[oqpg::NCLASS] = {0};
-  double grad_stats[4] = {0, 0, 0, 0};  // quartets listed, evaluated, primitive quartets, ms
+  oqpg::DevBuf d_gpairs, d_gprims, d_galpha, d_gprimsf, d_galphaf, d_coff, d_atom, d_gmat, d_gmatf, d_dshg,
+      d_gcounts, d_gwork, d_de, d_gcnt;
+  oqpg::DevBuf d_glists[oqpg::NLIST];   // FP64 lists, then the FP32 lists of the precision split
+  unsigned long long gcaps[oqpg::NLIST] = {0};
+  double grad_stats[5] = {0, 0, 0, 0, 0};  // quartets listed, evaluated, primitive quartets, ms, FP32 listed
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t evc[oqpg::NCLASS][2] = {};
   double last_stats[10 + 3 * oqpg::NCLASS] = {0};

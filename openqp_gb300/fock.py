@@ -147,7 +147,9 @@ class FockBuilder:
     def set_precision(self, mode, threshold=1e-6):
         """mode "fp64": plain path; mode "mixed": quartets whose screening value
         (Schwarz bound x shell density) is below threshold run in FP32 with their
-        Rys roots/weights in FP64; "mixed-fast": the same with FP32 roots."""
+        Rys roots/weights in FP64; "mixed-fast": the same with FP32 roots.  The
+        gradient (grad2) splits the same way on the bound of its two-particle
+        density."""
         m = {"fp64": 0, "mixed": 1, "mixed-fast": 2}[mode]
         rc = lib().oqpg_set_precision(self.h, m, float(threshold))
         if rc != 0:
@@ -176,9 +178,10 @@ class FockBuilder:
         return de.reshape(-1, 3)
 
     def grad_stats(self):
-        s = np.zeros(4)
-        lib().oqpg_grad_stats(self.h, ptr(s), 4)
-        return dict(quartets_listed=int(s[0]), quartets=int(s[1]), prim_quartets=int(s[2]), ms=float(s[3]))
+        s = np.zeros(5)
+        lib().oqpg_grad_stats(self.h, ptr(s), 5)
+        return dict(quartets_listed=int(s[0]), quartets=int(s[1]), prim_quartets=int(s[2]), ms=float(s[3]),
+                    f32_quartets_listed=int(s[4]))
 
     def schwarz(self):
         ns = len(self.bas.am)

@@ -187,3 +187,21 @@ def test_autograd_geometry_fd_uhf(gpu):
         xm = bas.xyz.copy(); xm[at, x] -= h
         fd = (L(xp) - L(xm)) / (2 * h)
         assert abs(fd - float(xyz.grad[at, x])) < 1e-6 * max(1.0, abs(fd)), (at, x, fd, float(xyz.grad[at, x]))
+
+
+@pytest.mark.parametrize("mode", ["mixed", "mixed-fast"])
+def test_grad2_precision_split(gpu, mode):
+    """FP32 derivative quartets below the bound: max gradient error against the
+    FP64 gradient well inside 1e-5 Eh/Bohr."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(6, workloads.cube_edge_like_c1(6), seed=12, basis="6-31g(d)")
+    d = workloads.density(bas, 30, 12)
+    fb = gpu.FockBuilder(bas)
+    g64 = fb.grad2(d)
+    fb.set_precision(mode, 1e-6)
+    g32 = fb.grad2(d)
+    st = fb.grad_stats()
+    assert st["f32_quartets_listed"] > 0
+    assert np.abs(g32 - g64).max() < 1e-7
+    fb.set_precision(mode, 1e-3)
+    assert np.abs(fb.grad2(d) - g64).max() < 1e-5
