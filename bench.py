@@ -104,6 +104,19 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x):
+    """The largest value of x over the ranks of the process group (one rank:
+    x).  NCCL groups reduce on the GPU, gloo groups on the host."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -255,11 +268,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         if ws > 1:
             torch.distributed.barrier()
-        tsum = sum(times) / 1000.0
-        if ws > 1:
-            t = torch.tensor([tsum], device="cuda", dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            tsum = float(t.item())
+        tsum = max_over_ranks(sum(times) / 1000.0)
         return tsum, stats, out.clone()
 
     mixed = None
@@ -292,11 +301,7 @@ def run_ours(args):
         e2e_t.append(time.perf_counter() - t0)
         if info != 0:
             raise RuntimeError("routec_fock_jk returned info=%d" % info)
-    e2e_sum = sum(e2e_t)
-    if ws > 1:
-        t = torch.tensor([e2e_sum], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_sum = float(t.item())
+    e2e_sum = max_over_ranks(sum(e2e_t))
     e2e = ws * args.steps / e2e_sum
     # roofline of the dominant class kernel (mean over the timed steps)
     labels = class_labels()
@@ -576,11 +581,7 @@ def run_batch(args):
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
         torch.cuda.synchronize()
-        tsum = sum(times) / 1000.0
-        if ws > 1:
-            t = torch.tensor([tsum], device="cuda", dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            tsum = float(t.item())
+        tsum = max_over_ranks(sum(times) / 1000.0)
         return tsum, times, out.clone(), bb.stats(), bb.graph_info()
 
     t64, times64, f64, st64, gi64 = replay("fp64")
