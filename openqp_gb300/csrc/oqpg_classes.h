@@ -21,15 +21,21 @@ inline int class_index(int tbra, int tket) {  // tbra <= tket
 struct ClassInfo {
   int l[4];
   int team;        // 1: one warp per quartet, 0: one thread per quartet
-  int smem_warp;   // doubles of shared memory per warp (team kernels), Cartesian / pure
-  int smem_warp_pure;
+  int prim;        // 1: has the primitive-parallel kernel for its heavily contracted quartets
 };
+
+// Classes whose Cartesian block and one root's 2D tables fit in registers get a
+// primitive-parallel kernel (lanes split the primitive quartets).
+__host__ __device__ constexpr bool prim_parallel(int la, int lb, int lc, int ld) {
+  return ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) <= 27 ||
+         ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) + 3 * (la + 1) * (lb + 1) * (lc + 1) * (ld + 1) <= 100;
+}
 const ClassInfo& class_info(int c);
 
 // Kernel variants of a class.
 constexpr int MODE_FOCK = 0;     // Fock build
 constexpr int MODE_SCHWARZ = 1;  // Schwarz bounds of diagonal quartets
-constexpr int MODE_PRIM = 2;     // Fock build, one warp per heavily contracted small-class quartet
+constexpr int MODE_PRIM = 2;     // Fock build, one warp per heavily contracted quartet, lanes split primitives
 constexpr int MODE_F32 = 8;      // flag: FP32 quartets of the precision-split build
 
 // Launch the kernel of class c in the given mode.

@@ -641,6 +641,162 @@ struct TeamSmem {
   static constexpr int PER_WARP = K::NE + REST;   // elements of the kernel's type
 };
 
+// Epilogue of a warp-owned contracted quartet whose raw Cartesian block is in
+// V = W[0, NE) (shared memory of the warp): normalisation, pure projection,
+// element cutoff and the J/K digestion (or the Schwarz bound), the lanes
+// splitting elements and targets.
+template <int LA, int LB, int LC, int LD, bool PURE, bool SCH, typename T>
+__device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, const PairDev& P, const PairDev& Q,
+                                              T* W, int lane) {
+  using K = Cls<LA, LB, LC, LD>;
+  using E = Epi<LA, LB, LC, LD, PURE>;
+  using SM = TeamSmem<LA, LB, LC, LD, PURE>;
+  constexpr int NE = K::NE, KE = (NE + 31) / 32;
+  T* V = W;
+  const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
+  // ---- epilogue: V = normalised block in smem, pure projection in place
+  T* Tm = W + NE;
+#pragma unroll
+  for (int k = 0; k < KE; ++k) {
+    const int e = lane + 32 * k;
+    if (e < NE) {
+      const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
+                id = e % K::ND;
+      // product of the component norms: sqrt(3)^n for n off-diagonal d components,
+      // looked up rather than multiplied out (one FP64 multiply per element)
+      const int n3 = (LA == 2 && ia >= 3) + (LB == 2 && ib >= 3) + (LC == 2 && ic >= 3) + (LD == 2 && id >= 3);
+      if (LA == 2 || LB == 2 || LC == 2 || LD == 2) V[e] *= sqrt3_pow<T>(n3);
+    }
+  }
+  __syncwarp();
+  int dims[4] = {K::NA, K::NB, K::NC, K::ND};
+  if (PURE) {
+    const int ls[4] = {LA, LB, LC, LD};
+#pragma unroll
+    for (int pos = 0; pos < 4; ++pos) {
+      if (ls[pos] != 2) continue;
+      int pre = 1, post = 1;
+      for (int i = 0; i < pos; ++i) pre *= dims[i];
+      for (int i = pos + 1; i < 4; ++i) post *= dims[i];
+      const int nout = pre * 5 * post;
+      for (int o = lane; o < nout; o += 32) {
+        const int p = o % post, m = (o / post) % 5, q = o / (5 * post);
+        const T* src = V + (size_t)q * 6 * post + p;
+        T v;
+        if (m == 0) v = src[3 * post];
+        else if (m == 1) v = src[5 * post];
+        else if (m == 2) v = src[2 * post] - (T)0.5 * (src[0] + src[post]);
+        else if (m == 3) v = src[4 * post];
+        else v = (T)0.86602540378443865 * (src[0] - src[post]);
+        Tm[o] = v;
+      }
+      __syncwarp();
+      for (int o = lane; o < nout; o += 32) V[o] = Tm[o];
+      __syncwarp();
+      dims[pos] = 5;
+    }
+  }
+  constexpr int NEP = E::NEP;
+  if (SCH) {
+    T m = 0;
+    for (int e = lane; e < NEP; e += 32) m = fmax(m, fabs(V[e]));
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, s));
+    if (lane == 0) a.schwarz_out[qd.x] = sqrt((double)m);
+    __syncwarp();
+    return;
+  }
+  const T cut = (T)a.elem_cut;
+  for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], cut);
+  // density blocks
+  const int n = a.nbf;
+  const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
+  const int ra = SA.mrow + oa, rb = SB.mrow + ob, rc = SC.mrow + oc;
+  const T* djt = dj_of<T>(a);
+  T* Dab = W + NE;                 // after V (NE >= NEP)
+  T* Dcd = Dab + E::A * E::B;
+  T* Dk = Dcd + E::C * E::D;       // per k: ac, ad, bc, bd
+  constexpr int DKS = SM::DK;
+  for (int i = lane; i < E::A * E::B; i += 32) Dab[i] = __ldg(djt + (size_t)(ra + i / E::B) * n + ob + i % E::B);
+  for (int i = lane; i < E::C * E::D; i += 32) Dcd[i] = __ldg(djt + (size_t)(rc + i / E::D) * n + od + i % E::D);
+  for (int kk = 0; kk < a.nk; ++kk) {
+    const T* dk = dk_of<T>(a) + (size_t)kk * a.kstride;
+    T* base = Dk + kk * DKS;
+    for (int i = lane; i < E::A * E::C; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::C) * n + oc + i % E::C);
+    base += E::A * E::C;
+    for (int i = lane; i < E::A * E::D; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::D) * n + od + i % E::D);
+    base += E::A * E::D;
+    for (int i = lane; i < E::B * E::C; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::C) * n + oc + i % E::C);
+    base += E::B * E::C;
+    for (int i = lane; i < E::B * E::D; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::D) * n + od + i % E::D);
+  }
+  __syncwarp();
+  double f = 1.0;
+  if (P.sha == P.shb) f *= 0.5;
+  if (Q.sha == Q.shb) f *= 0.5;
+  if (qd.x == qd.y) f *= 0.5;
+  constexpr int NAB = E::A * E::B, NCD = E::C * E::D;
+  constexpr int NAC = E::A * E::C, NAD = E::A * E::D, NBC = E::B * E::C, NBD = E::B * E::D;
+  const int ntarget = NAB + NCD + a.nk * (NAC + NAD + NBC + NBD);
+  // Every target element is a strided dot product of V with a density block:
+  //   s = sum_{u < n1, v < n2} V[vb + u s1 + v s2] Dv[u n2 + v].
+  // Only the (integer) descriptor depends on the target kind, so the lanes of
+  // a round share one FP64 instruction stream whatever kinds they hold.
+  constexpr int BCD = E::B * E::C * E::D, CD_ = E::C * E::D;
+  for (int o = lane; o < ntarget; o += 32) {
+    int vb, s1, s2, n1, n2;
+    const T* dv;
+    double* dst;
+    double fac;
+    if (o < NAB) {          // J[a][b] += sum_cd V D[c][d]
+      const int i = o / E::B, j = o % E::B;
+      vb = o * NCD; s1 = 0; s2 = 1; n1 = 1; n2 = NCD; dv = Dcd;
+      dst = a.gj + (size_t)(ra + i) * n + ob + j;
+      fac = 2.0 * f;
+    } else if (o < NAB + NCD) {  // J[c][d] += sum_ab V D[a][b]
+      const int cd = o - NAB, k = cd / E::D, l = cd % E::D;
+      vb = cd; s1 = NCD; s2 = 0; n1 = NAB; n2 = 1; dv = Dab;
+      dst = a.gj + (size_t)(rc + k) * n + od + l;
+      fac = 2.0 * f;
+    } else {
+      int r = o - NAB - NCD;
+      const int kk = r / (NAC + NAD + NBC + NBD);
+      r -= kk * (NAC + NAD + NBC + NBD);
+      const T* dk = Dk + kk * DKS;
+      double* gk = a.gk + (size_t)kk * a.kstride;
+      fac = f;
+      if (r < NAC) {  // K[a][c] += sum_bd V[a b c d] D[b][d]
+        const int i = r / E::C, k = r % E::C;
+        vb = i * BCD + k * E::D; s1 = CD_; s2 = 1; n1 = E::B; n2 = E::D; dv = dk + NAC + NAD + NBC;
+        dst = gk + (size_t)(ra + i) * n + oc + k;
+      } else if (r < NAC + NAD) {  // K[a][d] += sum_bc V D[b][c]
+        r -= NAC;
+        const int i = r / E::D, l = r % E::D;
+        vb = i * BCD + l; s1 = CD_; s2 = E::D; n1 = E::B; n2 = E::C; dv = dk + NAC + NAD;
+        dst = gk + (size_t)(ra + i) * n + od + l;
+      } else if (r < NAC + NAD + NBC) {  // K[b][c] += sum_ad V D[a][d]
+        r -= NAC + NAD;
+        const int j = r / E::C, k = r % E::C;
+        vb = j * CD_ + k * E::D; s1 = BCD; s2 = 1; n1 = E::A; n2 = E::D; dv = dk + NAC;
+        dst = gk + (size_t)(rb + j) * n + oc + k;
+      } else {  // K[b][d] += sum_ac V D[a][c]
+        r -= NAC + NAD + NBC;
+        const int j = r / E::D, l = r % E::D;
+        vb = j * CD_ + l; s1 = BCD; s2 = E::D; n1 = E::A; n2 = E::C; dv = dk;
+        dst = gk + (size_t)(rb + j) * n + od + l;
+      }
+    }
+    T s = 0;
+    const int nt = n1 * n2;
+    int u = 0, v = 0;
+    for (int t = 0; t < nt; ++t) {
+      s = fma(V[vb + u * s1 + v * s2], dv[t], s);
+      if (++v == n2) { v = 0; ++u; }
+    }
+    atomicAdd(dst, fac * (double)s);
+  }
+}
+
 template <int LA, int LB, int LC, int LD, bool PURE, bool SCH, typename T>
 __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
   using K = Cls<LA, LB, LC, LD>;
@@ -680,7 +836,6 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
     PairDev P, Q;
     T AB[3], CD[3];
     quartet_geometry<T>(a, qd, P, Q, AB, CD);
-    const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
 #pragma unroll
     for (int k = 0; k < KE; ++k)
       if (lane + 32 * k < NE) V[lane + 32 * k] = 0;
@@ -736,150 +891,65 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
         __syncwarp();
       }
     }
-    // ---- epilogue: V = normalised block in smem, pure projection in place
-    T* Tm = W + NE;
-#pragma unroll
-    for (int k = 0; k < KE; ++k) {
-      const int e = lane + 32 * k;
-      if (e < NE) {
-        const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
-                  id = e % K::ND;
-        // product of the component norms: sqrt(3)^n for n off-diagonal d components,
-        // looked up rather than multiplied out (one FP64 multiply per element)
-        const int n3 = (LA == 2 && ia >= 3) + (LB == 2 && ib >= 3) + (LC == 2 && ic >= 3) + (LD == 2 && id >= 3);
-        if (LA == 2 || LB == 2 || LC == 2 || LD == 2) V[e] *= sqrt3_pow<T>(n3);
-      }
-    }
-    __syncwarp();
-    int dims[4] = {K::NA, K::NB, K::NC, K::ND};
-    if (PURE) {
-      const int ls[4] = {LA, LB, LC, LD};
-#pragma unroll
-      for (int pos = 0; pos < 4; ++pos) {
-        if (ls[pos] != 2) continue;
-        int pre = 1, post = 1;
-        for (int i = 0; i < pos; ++i) pre *= dims[i];
-        for (int i = pos + 1; i < 4; ++i) post *= dims[i];
-        const int nout = pre * 5 * post;
-        for (int o = lane; o < nout; o += 32) {
-          const int p = o % post, m = (o / post) % 5, q = o / (5 * post);
-          const T* src = V + (size_t)q * 6 * post + p;
-          T v;
-          if (m == 0) v = src[3 * post];
-          else if (m == 1) v = src[5 * post];
-          else if (m == 2) v = src[2 * post] - (T)0.5 * (src[0] + src[post]);
-          else if (m == 3) v = src[4 * post];
-          else v = (T)0.86602540378443865 * (src[0] - src[post]);
-          Tm[o] = v;
-        }
-        __syncwarp();
-        for (int o = lane; o < nout; o += 32) V[o] = Tm[o];
-        __syncwarp();
-        dims[pos] = 5;
-      }
-    }
-    constexpr int NEP = E::NEP;
-    if (SCH) {
-      T m = 0;
-      for (int e = lane; e < NEP; e += 32) m = fmax(m, fabs(V[e]));
-#pragma unroll
-      for (int s = 16; s > 0; s >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, s));
-      if (lane == 0) a.schwarz_out[qd.x] = sqrt((double)m);
-      __syncwarp();
-      continue;
-    }
-    const T cut = (T)a.elem_cut;
-    for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], cut);
-    // density blocks
-    const int n = a.nbf;
-    const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
-    const int ra = SA.mrow + oa, rb = SB.mrow + ob, rc = SC.mrow + oc;
-    const T* djt = dj_of<T>(a);
-    T* Dab = W + NE;                 // after V (NE >= NEP)
-    T* Dcd = Dab + E::A * E::B;
-    T* Dk = Dcd + E::C * E::D;       // per k: ac, ad, bc, bd
-    constexpr int DKS = SM::DK;
-    for (int i = lane; i < E::A * E::B; i += 32) Dab[i] = __ldg(djt + (size_t)(ra + i / E::B) * n + ob + i % E::B);
-    for (int i = lane; i < E::C * E::D; i += 32) Dcd[i] = __ldg(djt + (size_t)(rc + i / E::D) * n + od + i % E::D);
-    for (int kk = 0; kk < a.nk; ++kk) {
-      const T* dk = dk_of<T>(a) + (size_t)kk * a.kstride;
-      T* base = Dk + kk * DKS;
-      for (int i = lane; i < E::A * E::C; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::C) * n + oc + i % E::C);
-      base += E::A * E::C;
-      for (int i = lane; i < E::A * E::D; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::D) * n + od + i % E::D);
-      base += E::A * E::D;
-      for (int i = lane; i < E::B * E::C; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::C) * n + oc + i % E::C);
-      base += E::B * E::C;
-      for (int i = lane; i < E::B * E::D; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::D) * n + od + i % E::D);
-    }
-    __syncwarp();
-    double f = 1.0;
-    if (P.sha == P.shb) f *= 0.5;
-    if (Q.sha == Q.shb) f *= 0.5;
-    if (qd.x == qd.y) f *= 0.5;
-    constexpr int NAB = E::A * E::B, NCD = E::C * E::D;
-    constexpr int NAC = E::A * E::C, NAD = E::A * E::D, NBC = E::B * E::C, NBD = E::B * E::D;
-    const int ntarget = NAB + NCD + a.nk * (NAC + NAD + NBC + NBD);
-    // Every target element is a strided dot product of V with a density block:
-    //   s = sum_{u < n1, v < n2} V[vb + u s1 + v s2] Dv[u n2 + v].
-    // Only the (integer) descriptor depends on the target kind, so the lanes of
-    // a round share one FP64 instruction stream whatever kinds they hold.
-    constexpr int BCD = E::B * E::C * E::D, CD_ = E::C * E::D;
-    for (int o = lane; o < ntarget; o += 32) {
-      int vb, s1, s2, n1, n2;
-      const T* dv;
-      double* dst;
-      double fac;
-      if (o < NAB) {          // J[a][b] += sum_cd V D[c][d]
-        const int i = o / E::B, j = o % E::B;
-        vb = o * NCD; s1 = 0; s2 = 1; n1 = 1; n2 = NCD; dv = Dcd;
-        dst = a.gj + (size_t)(ra + i) * n + ob + j;
-        fac = 2.0 * f;
-      } else if (o < NAB + NCD) {  // J[c][d] += sum_ab V D[a][b]
-        const int cd = o - NAB, k = cd / E::D, l = cd % E::D;
-        vb = cd; s1 = NCD; s2 = 0; n1 = NAB; n2 = 1; dv = Dab;
-        dst = a.gj + (size_t)(rc + k) * n + od + l;
-        fac = 2.0 * f;
-      } else {
-        int r = o - NAB - NCD;
-        const int kk = r / (NAC + NAD + NBC + NBD);
-        r -= kk * (NAC + NAD + NBC + NBD);
-        const T* dk = Dk + kk * DKS;
-        double* gk = a.gk + (size_t)kk * a.kstride;
-        fac = f;
-        if (r < NAC) {  // K[a][c] += sum_bd V[a b c d] D[b][d]
-          const int i = r / E::C, k = r % E::C;
-          vb = i * BCD + k * E::D; s1 = CD_; s2 = 1; n1 = E::B; n2 = E::D; dv = dk + NAC + NAD + NBC;
-          dst = gk + (size_t)(ra + i) * n + oc + k;
-        } else if (r < NAC + NAD) {  // K[a][d] += sum_bc V D[b][c]
-          r -= NAC;
-          const int i = r / E::D, l = r % E::D;
-          vb = i * BCD + l; s1 = CD_; s2 = E::D; n1 = E::B; n2 = E::C; dv = dk + NAC + NAD;
-          dst = gk + (size_t)(ra + i) * n + od + l;
-        } else if (r < NAC + NAD + NBC) {  // K[b][c] += sum_ad V D[a][d]
-          r -= NAC + NAD;
-          const int j = r / E::C, k = r % E::C;
-          vb = j * CD_ + k * E::D; s1 = BCD; s2 = 1; n1 = E::A; n2 = E::D; dv = dk + NAC;
-          dst = gk + (size_t)(rb + j) * n + oc + k;
-        } else {  // K[b][d] += sum_ac V D[a][c]
-          r -= NAC + NAD + NBC;
-          const int j = r / E::D, l = r % E::D;
-          vb = j * CD_ + l; s1 = BCD; s2 = E::D; n1 = E::A; n2 = E::C; dv = dk;
-          dst = gk + (size_t)(rb + j) * n + od + l;
-        }
-      }
-      T s = 0;
-      const int nt = n1 * n2;
-      int u = 0, v = 0;
-      for (int t = 0; t < nt; ++t) {
-        s = fma(V[vb + u * s1 + v * s2], dv[t], s);
-        if (++v == n2) { v = 0; ++u; }
-      }
-      atomicAdd(dst, fac * (double)s);
-    }
+    team_epilogue<LA, LB, LC, LD, PURE, SCH, T>(a, qd, P, Q, W, lane);
     __syncwarp();
   }
   if (a.counters && lane == 0 && nprim) atomicAdd(a.counters, nprim);
+}
+
+// Heavily contracted quartets of the warp-per-quartet classes whose Cartesian
+// block and one root's 2D tables fit in registers: one warp per quartet, the
+// lanes split the primitive quartets as in k_prim; a recursive-halving
+// reduce-scatter sums the lanes' blocks (lane l ends with elements
+// [KE l, KE l + KE)), which go to shared memory for the team epilogue.
+template <int LA, int LB, int LC, int LD, bool PURE, typename T>
+__global__ void __launch_bounds__(128) k_prim_team(const BuildArgs a) {
+  using K = Cls<LA, LB, LC, LD>;
+  using SM = TeamSmem<LA, LB, LC, LD, PURE>;
+  constexpr int NE = K::NE, KE = (NE + 31) / 32, MP = 32 * KE;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* W = smem + warp * SM::PER_WARP;
+  const uint2* quartets;
+  long long nquartets;
+  work_range(a, quartets, nquartets);
+  unsigned long long nprim = 0;
+  for (;;) {
+    const long long t = grab(a.work, 1u, lane);
+    if (t >= nquartets) break;
+    const uint2 qd = quartets[t];
+    PairDev P, Q;
+    T AB[3], CD[3];
+    quartet_geometry<T>(a, qd, P, Q, AB, CD);
+    T acc[MP];
+#pragma unroll
+    for (int e = 0; e < MP; ++e) acc[e] = 0;
+    small_prims<LA, LB, LC, LD, T>(a, P, Q, AB, CD, lane, 32, acc, nprim);
+    // reduce-scatter over the 32 lanes: at each level keep the half selected
+    // by the lane bit, add the partner's copy of it
+#pragma unroll
+    for (int lvl = 0; lvl < 5; ++lvl) {
+      const int off = 16 >> lvl;
+      const int m = MP >> (lvl + 1);
+      const bool up = (lane & off) != 0;
+#pragma unroll
+      for (int j = 0; j < (MP >> 1); ++j) {
+        if (j < m) {
+          const T keep = up ? acc[m + j] : acc[j];
+          const T send = up ? acc[j] : acc[m + j];
+          acc[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < KE; ++j)
+      if (KE * lane + j < NE) W[KE * lane + j] = acc[j];
+    __syncwarp();
+    team_epilogue<LA, LB, LC, LD, PURE, false, T>(a, qd, P, Q, W, lane);
+    __syncwarp();
+  }
+  if (a.counters && nprim) atomicAdd(a.counters, nprim);
 }
 
 }  // namespace oqpg

@@ -15,7 +15,7 @@
 namespace oqpg {
 
 static const ClassInfo kClasses[NCLASS] = {
-#define C_(a, b, c, d) {{a, b, c, d}, (ncart(a) * ncart(b) * ncart(c) * ncart(d) > 27), 0, 0}
+#define C_(a, b, c, d) {{a, b, c, d}, (ncart(a) * ncart(b) * ncart(c) * ncart(d) > 27), prim_parallel(a, b, c, d)}
     C_(0, 0, 0, 0), C_(0, 0, 0, 1), C_(0, 0, 0, 2), C_(0, 0, 1, 1), C_(0, 0, 1, 2), C_(0, 0, 2, 2),
     C_(0, 1, 0, 1), C_(0, 1, 0, 2), C_(0, 1, 1, 1), C_(0, 1, 1, 2), C_(0, 1, 2, 2),
     C_(0, 2, 0, 2), C_(0, 2, 1, 1), C_(0, 2, 1, 2), C_(0, 2, 2, 2),
@@ -485,7 +485,10 @@ int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
 
 void default_tuning(oqpg_tuning& t) {
   for (int k = 0; k < NCLASS; ++k) {
-    t.split_log2[k] = PRIM_SPLIT_LOG2;
+    // thread-per-quartet classes hand quartets of >= 256 surviving primitive
+    // quartets to the primitive-parallel kernel; warp-per-quartet classes
+    // already at 16, where 32 lanes on the primitives beat the team's 2D phase
+    t.split_log2[k] = class_info(k).team ? 4 : PRIM_SPLIT_LOG2;
     t.chunk[k] = 32;
     t.ctas_per_sm[k] = 0;
   }
@@ -760,7 +763,7 @@ int size_lists(oqpg_ctx* c, BuildBufs& B, const unsigned long long* counts, cuda
   int split[NLIST];
   for (int k = 0; k < NLIST; ++k) {
     const int cl = k % NCLASS;
-    split[k] = class_info(cl).team ? 0 : std::max(0, NBIN - 4 * c->tune.split_log2[cl]);
+    split[k] = class_info(cl).prim ? std::max(0, NBIN - 4 * c->tune.split_log2[cl]) : 0;
   }
   CK(cudaMemcpyAsync(B.split.p, split, sizeof(split), cudaMemcpyHostToDevice, st));
   CK(cudaStreamSynchronize(st));  // the host arrays above are stack memory
@@ -871,7 +874,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
       a.counters = B.primc.as<unsigned long long>() + li;
       a.quartets = B.slists[li].as<uint2>();
       a.nquartets = (long long)B.cap[li];
-      if (!class_info(cl).team && c->tune.split_log2[cl] < 64) {
+      if (class_info(cl).prim && c->tune.split_log2[cl] < 64) {
         // quartets with >= 2^split primitive quartets (a prefix of the sorted
         // list) go to the warp-per-quartet primitive-parallel kernel
         a.range = ranges + 4 * li;

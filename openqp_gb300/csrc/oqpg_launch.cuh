@@ -34,8 +34,13 @@ constexpr bool is_team() { return Cls<LA, LB, LC, LD>::NE > 27; }
 template <int LA, int LB, int LC, int LD, bool PURE, typename T>
 cudaError_t launch_fock(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
   if constexpr (is_team<LA, LB, LC, LD>()) {
-    if (kind == MODE_PRIM) return cudaErrorInvalidValue;
     const size_t smem = sizeof(T) * 4 * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
+    if (kind == MODE_PRIM) {
+      if constexpr (prim_parallel(LA, LB, LC, LD))
+        return launch_persistent(k_prim_team<LA, LB, LC, LD, PURE, T>, smem, 4, a, nsm, st);
+      else
+        return cudaErrorInvalidValue;
+    }
     return launch_persistent(k_team<LA, LB, LC, LD, PURE, false, T>, smem, 4, a, nsm, st);
   } else {
     if (kind == MODE_PRIM) return launch_persistent(k_prim<LA, LB, LC, LD, PURE, T>, 0, 4, a, nsm, st);
