@@ -714,7 +714,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="water32_ccpvdz", choices=sorted(WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer seam timing (profiling runs)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed-fast"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed-fast", "df"])
     ap.add_argument("--mixed-threshold", type=float, default=1e-6)
     args = ap.parse_args()
     WORKLOAD.clear()

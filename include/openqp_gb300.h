@@ -179,8 +179,12 @@ int oqpg_schwarz(const oqpg_ctx* ctx, double* q);
  * bound x shell density, as in OpenQP's quartet screen) is below threshold are
  * evaluated in FP32 -- Rys roots and weights still in FP64 -- and their FP32
  * partial J/K blocks are added into the FP64 accumulators.  mode 2: as mode 1
- * with the FP32 quartets' roots and weights in FP32 as well.  No counterpart
- * in the reference. */
+ * with the FP32 quartets' roots and weights in FP32 as well.  mode 3
+ * ("df"): no split; every quartet is evaluated in double-float arithmetic
+ * (pairs of FP32 numbers, ~44 significant bits, on the FP32 pipe): the
+ * thread-per-quartet classes digest in FP64, the warp-per-quartet classes in
+ * double-float; all blocks are added into the FP64 accumulators (threshold
+ * ignored).  No counterpart in the reference. */
 int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold);
 
 /* Statistics of the last build, up to n (<= 73) doubles:

@@ -37,6 +37,7 @@ constexpr int MODE_FOCK = 0;     // Fock build
 constexpr int MODE_SCHWARZ = 1;  // Schwarz bounds of diagonal quartets
 constexpr int MODE_PRIM = 2;     // Fock build, one warp per heavily contracted quartet, lanes split primitives
 constexpr int MODE_F32 = 8;      // flag: FP32 quartets of the precision-split build
+constexpr int MODE_DF = 16;      // flag: double-float kernels for the thread-per-quartet classes
 
 // Launch the kernel of class c in the given mode.
 cudaError_t launch_class(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);

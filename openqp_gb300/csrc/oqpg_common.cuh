@@ -35,6 +35,11 @@ struct PrimPairF {
   float p, hp, px, py, pz, ax, ay, az, sp, pad;
 };
 
+// Double-float copy of a primitive pair (the "df" precision mode), defined with
+// the double-float type in oqpg_df.cuh.
+struct PrimPairDF;
+struct dfl;
+
 struct PairDev {
   int sha, shb;    // kernel orientation: am(sha) <= am(shb)
   int poff, pcnt;  // primitive-pair range
@@ -46,6 +51,8 @@ struct BuildArgs {
   const PairDev* pairs;
   const PrimPair* prims;
   const PrimPairF* primsf; // FP32 copy (precision-split builds)
+  const PrimPairDF* primsdf;  // double-float copy (df mode)
+  const float2* rysdf;        // Rys table and large-X constants as FP32 pairs (df mode)
   const uint2* quartets;   // (bra pair, ket pair) per quartet of this class
   long long nquartets;     // quartets (or, with range, the capacity that sizes the grid)
   const unsigned long long* range;  // optional device [begin, end) into quartets, read at kernel start
@@ -61,6 +68,8 @@ struct BuildArgs {
   const double* dk;        // nk full densities for exchange
   const float* djf;        // FP32 copies of dj / dk for the FP32 quartets
   const float* dkf;
+  const struct dfl* djdf;  // double-float copies (df mode)
+  const struct dfl* dkdf;
   double* gj;              // nbf x nbf Coulomb accumulator
   double* gk;              // nk x nbf x nbf exchange accumulators
   double* schwarz_out;     // Schwarz mode: per pair sqrt(max |(ab|ab)|)

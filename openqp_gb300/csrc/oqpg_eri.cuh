@@ -30,12 +30,16 @@
 // thresholds and the element cutoff follow OpenQP's s-d path
 // (int_rotaxis.F90:292-306,629; int2.F90:1806-1812).
 #pragma once
+#include <type_traits>
+
 #include "oqpg_common.cuh"
+#include "oqpg_df.cuh"
 
 namespace oqpg {
 
 #define RYS_STORAGE static __device__ const
 #include "rys_tables.inc"
+#include "rys_tables_df.inc"
 #undef RYS_STORAGE
 
 __host__ __device__ constexpr int rys_xmax(int n) { return 32 + 8 * n; }
@@ -97,11 +101,43 @@ __device__ __forceinline__ float rys_eval_f32(float X, int q) {
   return v;
 }
 
+// Double-float evaluation of the degree-7 FP64 table (coefficients as FP32
+// pairs), interval selection on the leading FP32 word.
+template <int N>
+__device__ __forceinline__ dfl rys_eval_df(dfl X, int q) {
+  if (X.hi >= (float)rys_xmax(N)) {
+    const int r = (N * (N - 1)) / 2 + (q >> 1);
+    const float2 c = RYS_HERM_W_DF[r], c2 = RYS_HERM_R2_DF[r];
+    return (q & 1) ? dfl(c.x, c.y) * df_rsqrt(X) : dfl(c2.x, c2.y) * df_rcp(X);
+  }
+  int k;
+  dfl s;
+  if (X.hi < (float)RYS_X_SPLIT) {
+    k = min(__float2int_rz(X.hi * (float)RYS_LO_PER_UNIT), RYS_X_SPLIT * RYS_LO_PER_UNIT - 1);
+    s = dfl(X.hi * (2.0f * RYS_LO_PER_UNIT), X.lo * (2.0f * RYS_LO_PER_UNIT)) + dfl(-(2 * k + 1));
+  } else {
+    const int f = min(__float2int_rz(X.hi), rys_xmax(N) - 1);
+    k = RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
+    s = dfl(X.hi * 2.0f, X.lo * 2.0f) + dfl(-(2 * f + 1));
+  }
+  const float2* c = RYS_TABLE_DF + rys_offset(N, RYS_NCOEF) + (k * 2 * N + q) * RYS_NCOEF;
+  float2 t = __ldg(c + RYS_NCOEF - 1);
+  dfl v(t.x, t.y);
+#pragma unroll
+  for (int i = RYS_NCOEF - 2; i >= 0; --i) {
+    t = __ldg(c + i);
+    v = fma(v, s, dfl(t.x, t.y));
+  }
+  return v;
+}
+
 // FP64 kernels: the degree-7 FP64 tables.  FP32 kernels: the degree-4 tables,
-// evaluated in FP64 (default) or, with roots_f32, in FP32.
+// evaluated in FP64 (default) or, with roots_f32, in FP32.  Double-float
+// kernels: the degree-7 table in double-float.
 template <int N, typename T>
 __device__ __forceinline__ T rys_quantity(T X, int q, bool roots_f32 = false) {
-  if constexpr (sizeof(T) == 8) return rys_eval<N, RYS_NCOEF>(RYS_TABLE, X, q);
+  if constexpr (std::is_same<T, double>::value) return rys_eval<N, RYS_NCOEF>(RYS_TABLE, X, q);
+  else if constexpr (std::is_same<T, dfl>::value) return rys_eval_df<N>(X, q);
   else {
     if (roots_f32) return rys_eval_f32<N>(X, q);
     return (float)rys_eval<N, RYS_NCOEF_F32>(RYS_TABLE_F32, (double)X, q);
@@ -125,17 +161,21 @@ __host__ __device__ constexpr double pure_d(int m, int c) {
 template <typename T> struct PrimT;
 template <> struct PrimT<double> { using type = PrimPair; };
 template <> struct PrimT<float> { using type = PrimPairF; };
+template <> struct PrimT<dfl> { using type = PrimPairDF; };
 
 template <typename T> __device__ __forceinline__ const typename PrimT<T>::type* prims_of(const BuildArgs& a);
 template <> __device__ __forceinline__ const PrimPair* prims_of<double>(const BuildArgs& a) { return a.prims; }
 template <> __device__ __forceinline__ const PrimPairF* prims_of<float>(const BuildArgs& a) { return a.primsf; }
+template <> __device__ __forceinline__ const PrimPairDF* prims_of<dfl>(const BuildArgs& a) { return a.primsdf; }
 
 template <typename T> __device__ __forceinline__ const T* dj_of(const BuildArgs& a);
 template <> __device__ __forceinline__ const double* dj_of<double>(const BuildArgs& a) { return a.dj; }
 template <> __device__ __forceinline__ const float* dj_of<float>(const BuildArgs& a) { return a.djf; }
+template <> __device__ __forceinline__ const dfl* dj_of<dfl>(const BuildArgs& a) { return a.djdf; }
 template <typename T> __device__ __forceinline__ const T* dk_of(const BuildArgs& a);
 template <> __device__ __forceinline__ const double* dk_of<double>(const BuildArgs& a) { return a.dk; }
 template <> __device__ __forceinline__ const float* dk_of<float>(const BuildArgs& a) { return a.dkf; }
+template <> __device__ __forceinline__ const dfl* dk_of<dfl>(const BuildArgs& a) { return a.dkdf; }
 
 __device__ __forceinline__ void prim_load(const PrimPair* __restrict__ src, PrimPair& d) {
   const double2* s = reinterpret_cast<const double2*>(src);
@@ -153,10 +193,22 @@ __device__ __forceinline__ void prim_load(const PrimPairF* __restrict__ src, Pri
   d.sp = v4.x; d.pad = v4.y;
 }
 
+__device__ __forceinline__ void prim_load(const PrimPairDF* __restrict__ src, PrimPairDF& d) {
+  const float4* s = reinterpret_cast<const float4*>(src);
+  const float4 v0 = __ldg(s), v1 = __ldg(s + 1), v2 = __ldg(s + 2), v3 = __ldg(s + 3), v4 = __ldg(s + 4);
+  d.p = dfl(v0.x, v0.y); d.hp = dfl(v0.z, v0.w); d.px = dfl(v1.x, v1.y); d.py = dfl(v1.z, v1.w);
+  d.pz = dfl(v2.x, v2.y); d.ax = dfl(v2.z, v2.w); d.ay = dfl(v3.x, v3.y); d.az = dfl(v3.z, v3.w);
+  d.sp = dfl(v4.x, v4.y); d.spf = v4.z; d.pf = v4.w;
+}
+
 // FP32 screening data (K/p, p) of a primitive pair.
 __device__ __forceinline__ float2 prim_screen(const PrimPair* p) {
   const long long bits = __double_as_longlong(__ldg(reinterpret_cast<const double*>(p) + 9));
   return make_float2(__int_as_float((int)(bits & 0xffffffffll)), __int_as_float((int)(bits >> 32)));
+}
+__device__ __forceinline__ float2 prim_screen(const PrimPairDF* p) {
+  const float* f = reinterpret_cast<const float*>(p);
+  return make_float2(__ldg(f + 18), __ldg(f + 19));
 }
 __device__ __forceinline__ float2 prim_screen(const PrimPairF* p) {
   const float* f = reinterpret_cast<const float*>(p);
@@ -176,6 +228,16 @@ __device__ __forceinline__ bool screen_keep(const PrimPair* bp, float2 bs, const
   const double fqz = __ldg(b + 8) * __ldg(k + 8);
   return !(fqz * fqz < a.prim_cut2 * (__ldg(b) + __ldg(k)));
 }
+// Double-float pairs: the same band; inside it the test in double-float.
+__device__ __forceinline__ bool screen_keep(const PrimPairDF* bp, float2 bs, const PrimPairDF* kp, float2 ks,
+                                            const BuildArgs& a) {
+  const float r = fabsf(bs.x * ks.x) * rsqrtf(bs.y + ks.y);
+  if (r < a.prim_cut_lo) return false;
+  if (r > a.prim_cut_hi) return true;
+  const dfl fqz = df_ld(&bp->sp) * df_ld(&kp->sp);
+  const dfl lhs = fqz * fqz, rhs = dfl(a.prim_cut2) * (df_ld(&bp->p) + df_ld(&kp->p));
+  return !((lhs - rhs).hi < 0.0f);
+}
 __device__ __forceinline__ bool screen_keep(const PrimPairF*, float2 bs, const PrimPairF*, float2 ks,
                                             const BuildArgs& a) {
   const float r = fabsf(bs.x * ks.x) * rsqrtf(bs.y + ks.y);
@@ -191,6 +253,7 @@ struct PrimQuartet {
 
 __device__ __forceinline__ double rsqrt_t(double x) { return rsqrt64(x); }
 __device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+__device__ __forceinline__ dfl rsqrt_t(dfl x) { return df_rsqrt(x); }
 
 template <typename T, typename PP>
 __device__ __forceinline__ void prim_setup(const PP& bp, const PP& kp, PrimQuartet<T>& o) {
@@ -324,6 +387,13 @@ __device__ __constant__ const float SQRT3_POWF[5] = {1.0f, 1.7320508075688772f, 
 template <typename T> __device__ __forceinline__ T sqrt3_pow(int n);
 template <> __device__ __forceinline__ double sqrt3_pow<double>(int n) { return SQRT3_POW[n]; }
 template <> __device__ __forceinline__ float sqrt3_pow<float>(int n) { return SQRT3_POWF[n]; }
+// sqrt(3)^n as FP32 pairs (hi = round(v), lo = round(v - hi))
+__device__ __constant__ const float2 SQRT3_POW_DF[5] = {{1.0f, 0.0f},
+                                                       {1.7320507764816284f, 3.1087250107475484e-08f},
+                                                       {3.0f, 0.0f},
+                                                       {5.196152210235596f, 2.1247103632049402e-07f},
+                                                       {9.0f, 0.0f}};
+template <> __device__ __forceinline__ dfl sqrt3_pow<dfl>(int n) { return dfl(SQRT3_POW_DF[n].x, SQRT3_POW_DF[n].y); }
 
 // Element cutoff |v| < cut -> 0 (cut > 0), decided on the bit patterns: for
 // non-negative IEEE values the order of the magnitudes is the integer order of
@@ -697,7 +767,7 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
     }
   }
   constexpr int NEP = E::NEP;
-  if (SCH) {
+  if constexpr (SCH) {
     T m = 0;
     for (int e = lane; e < NEP; e += 32) m = fmax(m, fabs(V[e]));
 #pragma unroll
@@ -938,7 +1008,7 @@ __global__ void __launch_bounds__(128) k_prim_team(const BuildArgs a) {
         if (j < m) {
           const T keep = up ? acc[m + j] : acc[j];
           const T send = up ? acc[j] : acc[m + j];
-          acc[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+          acc[j] = keep + shfl_xor_t(send, off);
         }
       }
     }
@@ -947,6 +1017,76 @@ __global__ void __launch_bounds__(128) k_prim_team(const BuildArgs a) {
       if (KE * lane + j < NE) W[KE * lane + j] = acc[j];
     __syncwarp();
     team_epilogue<LA, LB, LC, LD, PURE, false, T>(a, qd, P, Q, W, lane);
+    __syncwarp();
+  }
+  if (a.counters && nprim) atomicAdd(a.counters, nprim);
+}
+
+// Double-float ("df") variants of the thread-per-quartet and primitive-
+// parallel kernels: the primitive loop (pair set-up, Rys roots and weights,
+// 2D integrals, accumulation) runs in double-float on the FP32 pipe; the
+// contracted block is converted to FP64 once per quartet and digested by the
+// FP64 epilogue.
+template <int LA, int LB, int LC, int LD, bool PURE>
+__global__ void __launch_bounds__(128) k_small_df(const BuildArgs a) {
+  constexpr int NE = Cls<LA, LB, LC, LD>::NE;
+  const int lane = threadIdx.x & 31;
+  const uint2* quartets;
+  long long nquartets;
+  work_range(a, quartets, nquartets);
+  unsigned long long nprim = 0;
+  const unsigned chunk = a.chunk >= 32 ? (unsigned)a.chunk : 32u;
+  for (;;) {
+    const long long base = grab(a.work, chunk, lane);
+    if (base >= nquartets) break;
+    const long long end = base + chunk < nquartets ? base + chunk : nquartets;
+    for (long long t = base + lane; t < end; t += 32) {
+      const uint2 qd = quartets[t];
+      PairDev P, Q;
+      dfl AB[3], CD[3];
+      quartet_geometry<dfl>(a, qd, P, Q, AB, CD);
+      dfl acc[NE];
+#pragma unroll
+      for (int e = 0; e < NE; ++e) acc[e] = dfl();
+      small_prims<LA, LB, LC, LD, dfl>(a, P, Q, AB, CD, 0, 1, acc, nprim);
+      double accd[NE];
+#pragma unroll
+      for (int e = 0; e < NE; ++e) accd[e] = df_to_double(acc[e]);
+      small_epilogue<LA, LB, LC, LD, PURE, false, double>(a, qd, P, Q, accd);
+    }
+  }
+  if (a.counters && nprim) atomicAdd(a.counters, nprim);
+}
+
+template <int LA, int LB, int LC, int LD, bool PURE>
+__global__ void __launch_bounds__(128) k_prim_df(const BuildArgs a) {
+  constexpr int NE = Cls<LA, LB, LC, LD>::NE;
+  const int lane = threadIdx.x & 31;
+  const uint2* quartets;
+  long long nquartets;
+  work_range(a, quartets, nquartets);
+  unsigned long long nprim = 0;
+  for (;;) {
+    const long long t = grab(a.work, 1u, lane);
+    if (t >= nquartets) break;
+    const uint2 qd = quartets[t];
+    PairDev P, Q;
+    dfl AB[3], CD[3];
+    quartet_geometry<dfl>(a, qd, P, Q, AB, CD);
+    dfl acc[NE];
+#pragma unroll
+    for (int e = 0; e < NE; ++e) acc[e] = dfl();
+    small_prims<LA, LB, LC, LD, dfl>(a, P, Q, AB, CD, lane, 32, acc, nprim);
+    double accd[NE];
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+      dfl v = acc[e];
+#pragma unroll
+      for (int s = 16; s > 0; s >>= 1)
+        v = v + dfl(__shfl_xor_sync(0xffffffffu, v.hi, s), __shfl_xor_sync(0xffffffffu, v.lo, s));
+      accd[e] = df_to_double(v);
+    }
+    if (lane == 0) small_epilogue<LA, LB, LC, LD, PURE, false, double>(a, qd, P, Q, accd);
     __syncwarp();
   }
   if (a.counters && nprim) atomicAdd(a.counters, nprim);

@@ -79,6 +79,14 @@ __global__ void k_to_f32(const double* __restrict__ x, long long n, float* y) {
     y[t] = (float)x[t];
 }
 
+__global__ void k_to_df(const double* __restrict__ x, long long n, dfl* y) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const double v = x[t];
+    const float h = (float)v;
+    y[t] = dfl(h, (float)(v - (double)h));
+  }
+}
+
 // shlden (OpenQP int2.F90:999-1047): max |D| over each shell-pair block and
 // over the densities; also each molecule's maximum (max_den).
 __global__ void k_dsh(const double* __restrict__ dp, int nfocks, const MolDev* __restrict__ mols,
@@ -630,6 +638,20 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
                       (float)q.ax, (float)q.ay, (float)q.az, (float)q.sp, 0.0f};
   }
   if ((rc = upload(c->d_primsf, pf, st))) return rc;
+  // double-float copy for the df mode: every FP64 field as an FP32 pair
+  std::vector<PrimPairDF> pd(fp.prims.size());
+  auto split = [](double v) {
+    const float h = (float)v;
+    return dfl(h, (float)(v - (double)h));
+  };
+  for (size_t i = 0; i < pd.size(); ++i) {
+    const PrimPair& q = fp.prims[i];
+    PrimPairDF& o = pd[i];
+    o.p = split(q.p); o.hp = split(q.hp); o.px = split(q.px); o.py = split(q.py); o.pz = split(q.pz);
+    o.ax = split(q.ax); o.ay = split(q.ay); o.az = split(q.az); o.sp = split(q.sp);
+    o.spf = q.spf; o.pf = q.pf;
+  }
+  if ((rc = upload(c->d_primsdf, pd, st))) return rc;
   if ((rc = upload(c->d_pair_ij, fp.ij, st))) return rc;
   if ((rc = upload(c->d_pair_type, fp.type, st))) return rc;
   if ((rc = upload(c->d_pair_mol, fp.mol, st))) return rc;
@@ -655,7 +677,7 @@ void ctx_free(oqpg_ctx* c) {
   if (!c) return;
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   DevBuf* bufs[] = {&c->d_shells, &c->d_pairs, &c->d_prims, &c->d_pair_ij, &c->d_pair_type, &c->d_q, &c->d_qf,
-                    &c->d_aoff, &c->d_naos, &c->d_mols, &c->d_pair_mol, &c->d_row_mol, &c->d_primsf,
+                    &c->d_aoff, &c->d_naos, &c->d_mols, &c->d_pair_mol, &c->d_row_mol, &c->d_primsf, &c->d_primsdf,
                     &c->d_sorted_idx, &c->d_sorted_q, &c->d_dp, &c->d_f, &c->d_fold, &c->d_gin, &c->d_gout,
                     &c->d_gpairs, &c->d_gprims, &c->d_galpha, &c->d_gprimsf, &c->d_galphaf, &c->d_coff,
                     &c->d_atom, &c->d_gmat, &c->d_gmatf, &c->d_dshg, &c->d_gcounts, &c->d_gwork, &c->d_de,
@@ -683,6 +705,10 @@ int ensure_bufs(oqpg_ctx* c, BuildBufs& B, int nk) {
   if (split_on(c)) {
     CK(B.djf.ensure(sizeof(float) * n2));
     if (nk == 2) CK(B.dkf.ensure(sizeof(float) * 2 * n2));
+  }
+  if (c->precision_mode == 3) {
+    CK(B.djdf.ensure(sizeof(dfl) * n2));
+    if (nk == 2) CK(B.dkdf.ensure(sizeof(dfl) * 2 * n2));
   }
   CK(B.gj.ensure(sizeof(double) * n2));
   CK(B.gk.ensure(sizeof(double) * nk * n2));
@@ -734,6 +760,15 @@ int issue_densities(oqpg_ctx* c, BuildBufs& B, const double* dp, int nfocks, cud
     if (nfocks == 2) {
       k_to_f32<<<(unsigned)std::min<long long>((2 * n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
           B.dk.as<double>(), (long long)(2 * n2), B.dkf.as<float>());
+      CK(cudaGetLastError());
+    }
+  }
+  if (c->precision_mode == 3) {
+    k_to_df<<<g, 256, 0, st>>>(B.dj.as<double>(), (long long)n2, B.djdf.as<dfl>());
+    CK(cudaGetLastError());
+    if (nfocks == 2) {
+      k_to_df<<<(unsigned)std::min<long long>((2 * n2 + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
+          B.dk.as<double>(), (long long)(2 * n2), B.dkdf.as<dfl>());
       CK(cudaGetLastError());
     }
   }
@@ -799,7 +834,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
   if (timing) CK(cudaEventRecord(c->ev[0], st));
   CK(cudaMemsetAsync(B.flag.p, 0, sizeof(unsigned), st));
   if ((rc = issue_densities(c, B, dp, nfocks, st))) return rc;
-  nlaunch += 2 + (split_on(c) ? (nk == 2 ? 2 : 1) : 0);
+  nlaunch += 2 + (split_on(c) || c->precision_mode == 3 ? (nk == 2 ? 2 : 1) : 0);
   ListArgs la = list_args(c, B);
   la.write = 1;
   CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * NLIST, st));
@@ -846,6 +881,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
   a.pairs = c->d_pairs.as<PairDev>();
   a.prims = c->d_prims.as<PrimPair>();
   a.primsf = c->d_primsf.as<PrimPairF>();
+  a.primsdf = c->d_primsdf.as<PrimPairDF>();
   a.nbf = c->stride;
   a.kstride = n2;
   a.nk = nk;
@@ -857,6 +893,8 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
   a.dk = (nk == 1) ? B.dj.as<double>() : B.dk.as<double>();
   a.djf = B.djf.as<float>();
   a.dkf = (nk == 1) ? B.djf.as<float>() : B.dkf.as<float>();
+  a.djdf = B.djdf.as<dfl>();
+  a.dkdf = (nk == 1) ? B.djdf.as<dfl>() : B.dkdf.as<dfl>();
   a.gj = B.gj.as<double>();
   a.gk = B.gk.as<double>();
   a.roots_f32 = c->precision_mode == 2 ? 1 : 0;
@@ -870,7 +908,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
     for (int prec = 0; prec < 2; ++prec) {
       const int li = cl + prec * NCLASS;
       if (!B.cap[li]) continue;
-      const int fl = prec ? MODE_F32 : 0;
+      const int fl = prec ? MODE_F32 : (c->precision_mode == 3 ? MODE_DF : 0);
       a.counters = B.primc.as<unsigned long long>() + li;
       a.quartets = B.slists[li].as<uint2>();
       a.nquartets = (long long)B.cap[li];
@@ -1230,10 +1268,10 @@ int oqpg_measure_fp64_peak(int iters, double* tflops) {
 
 int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold) {
   if (!ctx) return NOT_INIT;
-  if (mode < 0 || mode > 2) return UNSUPPORTED;
-  if (mode != 0 && !(threshold > 0.0)) return UNSUPPORTED;
+  if (mode < 0 || mode > 3) return UNSUPPORTED;
+  if ((mode == 1 || mode == 2) && !(threshold > 0.0)) return UNSUPPORTED;
   ctx->precision_mode = mode;
-  ctx->tau_f32 = mode != 0 ? threshold : 0.0;
+  ctx->tau_f32 = (mode == 1 || mode == 2) ? threshold : 0.0;
   ctx->hb.sized = false;  // the FP32 lists are sized by a fresh count pass
   return OK;
 }

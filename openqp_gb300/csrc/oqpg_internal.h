@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "oqpg_classes.h"
+#include "oqpg_df.cuh"
 
 namespace oqpg {
 
@@ -71,6 +72,7 @@ struct DevBuf {
 __global__ void k_unpack(const double* __restrict__ dp, int nfocks, const MolDev* __restrict__ mols,
                          const int* __restrict__ row_mol, int nrows, int stride, double* dj, double* dk);
 __global__ void k_to_f32(const double* __restrict__ x, long long n, float* y);
+__global__ void k_to_df(const double* __restrict__ x, long long n, dfl* y);
 __global__ void k_dsh(const double* __restrict__ dp, int nfocks, const MolDev* __restrict__ mols,
                       const int* __restrict__ pair_mol, const int2* __restrict__ pair_ij, int npair,
                       const int* __restrict__ aoff, const int* __restrict__ nao, double* dsh, float* dshf,
@@ -120,14 +122,15 @@ constexpr int NLIST = 2 * NCLASS;  // FP64 lists, then the FP32 lists of the pre
 // Per-build device buffers of one build pipeline (a context has one for its
 // direct builds and one owned by its captured graph).
 struct BuildBufs {
-  DevBuf dj, dk, djf, dkf, gj, gk, dsh, dshf, dmax, counts, primc, hist, cursor, work, ranges, caps, split, flag;
+  DevBuf dj, dk, djf, dkf, djdf, dkdf, gj, gk, dsh, dshf, dmax, counts, primc, hist, cursor, work, ranges, caps,
+      split, flag;
   DevBuf lists[NLIST], slists[NLIST], bins[NLIST];
   unsigned long long cap[NLIST] = {0};
   bool sized = false;
   unsigned long long* h_rb = nullptr;  // pinned readback: [0] flag, [1, 1+NLIST) counts, then primitive counts
   void release() {
-    DevBuf* b[] = {&dj, &dk, &djf, &dkf, &gj, &gk, &dsh, &dshf, &dmax, &counts, &primc, &hist, &cursor, &work,
-                   &ranges, &caps, &split, &flag};
+    DevBuf* b[] = {&dj, &dk, &djf, &dkf, &djdf, &dkdf, &gj, &gk, &dsh, &dshf, &dmax, &counts, &primc, &hist,
+                   &cursor, &work, &ranges, &caps, &split, &flag};
     for (DevBuf* x : b) x->release();
     for (auto& x : lists) x.release();
     for (auto& x : slists) x.release();
@@ -168,7 +171,7 @@ struct oqpg_ctx {
   int precision_mode = 0;
   double tau_f32 = 0.0;
   // device tables
-  oqpg::DevBuf d_shells, d_pairs, d_prims, d_primsf, d_pair_ij, d_pair_type, d_q, d_qf, d_aoff, d_naos, d_mols,
+  oqpg::DevBuf d_shells, d_pairs, d_prims, d_primsf, d_primsdf, d_pair_ij, d_pair_type, d_q, d_qf, d_aoff, d_naos, d_mols,
       d_pair_mol, d_row_mol;
   oqpg::DevBuf d_sorted_idx, d_sorted_q;
   // per-build buffers: direct builds, and the captured graph's own set

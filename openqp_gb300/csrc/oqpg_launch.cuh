@@ -65,9 +65,23 @@ cudaError_t launch_schwarz(const BuildArgs& a, int nsm, cudaStream_t st) {
 // mode: MODE_FOCK, MODE_SCHWARZ (diagonal classes only), MODE_PRIM (small
 // classes only: the heavily contracted head of a sorted list), each optionally
 // with MODE_F32 (FP32 quartets of the precision-split build; not Schwarz).
+template <int LA, int LB, int LC, int LD, bool PURE>
+cudaError_t launch_df(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
+  if constexpr (is_team<LA, LB, LC, LD>()) {
+    return launch_fock<LA, LB, LC, LD, PURE, dfl>(kind, a, nsm, st);
+  } else {
+    if (kind == MODE_PRIM) return launch_persistent(k_prim_df<LA, LB, LC, LD, PURE>, 0, 4, a, nsm, st);
+    return launch_persistent(k_small_df<LA, LB, LC, LD, PURE>, 0, 128, a, nsm, st);
+  }
+}
+
 template <int LA, int LB, int LC, int LD>
 cudaError_t launch_cls(bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
   const bool f32 = (mode & MODE_F32) != 0;
+  if (mode & MODE_DF) {
+    const int kind = mode & ~(MODE_DF | MODE_F32);
+    return pure ? launch_df<LA, LB, LC, LD, true>(kind, a, nsm, st) : launch_df<LA, LB, LC, LD, false>(kind, a, nsm, st);
+  }
   const int kind = mode & ~MODE_F32;
   if (kind == MODE_SCHWARZ) {
     if (f32) return cudaErrorInvalidValue;

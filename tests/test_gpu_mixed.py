@@ -72,3 +72,23 @@ def test_mixed_scf_energy_within_1e6(gpu, oracle_lib):
     mx = scf.run_scf(bas.nbf, S, H, enuc, 20, 20, fb.fock_jk, conv=1e-10, incremental=True)
     assert ref["converged"] and mx["converged"]
     assert abs(mx["energy"] - ref["energy"]) < 1e-6
+
+
+@pytest.mark.parametrize("basis,nw", [("6-31g(d)", 4), ("cc-pvdz", 3)])
+def test_double_float_mode_matches_fp64_and_oracle(gpu, oracle_lib, basis, nw):
+    """df mode: thread-per-quartet classes in double-float (FP32 pairs); the
+    plain-FP64 gate of 1e-10 against the oracle still holds, RHF and UHF."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(nw, workloads.cube_edge_like_c1(nw), seed=21, basis=basis)
+    fb = gpu.FockBuilder(bas)
+    d = workloads.density(bas, 5 * nw, 21)
+    f64 = fb.fock_jk(d)
+    fb.set_precision("df")
+    fdf = fb.fock_jk(d)
+    assert fb.stats()["f32_quartets"] == 0
+    assert np.abs(fdf - f64).max() < 1e-11
+    assert np.abs(fdf - oracle_lib.Oracle(bas).fock_jk(d)).max() < 1e-10
+    du = workloads.density_open(bas, 5 * nw + 1, 5 * nw - 1, 22)
+    fu = fb.fock_jk(du)
+    fb.set_precision("fp64")
+    assert np.abs(fu - fb.fock_jk(du)).max() < 1e-11
