@@ -288,6 +288,17 @@ def run_ours(args):
         mixed = {"mode": args.precision, "threshold": args.mixed_threshold, "fp64_builds_per_s": ws * args.steps / t64,
                  "speedup_vs_fp64": t64 / tsum, "max_abs_dF": float(np.abs(df).max()),
                  "dE2_Eh": de2, "f32_quartet_fraction": stats[-1]["f32_quartets"] / max(1, stats[-1]["quartets"])}
+    # the same build in double-float (FP32 pairs on the FP32 pipe), error against FP64
+    df_mode = None
+    if args.precision == "fp64" and not args.no_df:
+        tdf, _, fdf = timed("df")
+        ddf = (fdf - fval).cpu().numpy()[0]
+        from openqp_gb300.basis import unpack
+        df_mode = {"builds_per_s": ws * args.steps / tdf, "speedup_vs_fp64": tsum / tdf,
+                   "max_abs_dF_vs_fp64": float(np.abs(ddf).max()),
+                   "dE2_Eh": 0.5 * float(np.sum(unpack(d, bas.nbf) * unpack(ddf, bas.nbf))),
+                   "arithmetic": "double-float: unevaluated pairs of FP32 numbers (~44 bits), FP64 accumulators"}
+        fb.set_precision("fp64")
     # e2e through the seam with host buffers
     e2e_t = [float("nan")]
     if not args.no_e2e:
@@ -337,8 +348,11 @@ def run_ours(args):
                                         if s0["prim_per_class"][c]},
                 "list_ms": s0["list_ms"]}
         if mixed is not None:
-            line["dtype"] = "f32+f64"
+            line["dtype"] = {"df": "f32x2 (double-float)", "mixed-df": "f32 + f32x2 (double-float)"}.get(args.precision,
+                                                                                                        "f32+f64")
             line["precision_split"] = mixed
+        if df_mode is not None:
+            line["double_float_mode"] = df_mode
         if not args.no_cpu:
             cb, _ = cpu_baseline(bas, d, budget_s=args.cpu_budget)
             line["cpu_baseline"] = cb
@@ -585,6 +599,8 @@ def run_batch(args):
         return tsum, times, out.clone(), bb.stats(), bb.graph_info()
 
     t64, times64, f64, st64, gi64 = replay("fp64")
+    tdf, timesdf, fdf, _, _ = replay("df")
+    tmd, timesmd, fmd, stmd, _ = replay("mixed-df")
     prec = args.precision if args.precision != "fp64" else "mixed-fast"
     sampler = ClockSampler(local)
     sampler.start()
@@ -616,7 +632,8 @@ def run_batch(args):
                                           WORKLOAD["cutoff"])
         if rc != 0:
             raise RuntimeError("routec_fock_init_batch returned %d" % rc)
-        lib().routec_fock_set_precision({"mixed": 1, "mixed-fast": 2}[prec], args.mixed_threshold)
+        lib().routec_fock_set_precision({"mixed": 1, "mixed-fast": 2, "df": 3, "mixed-df": 4}[prec],
+                                        args.mixed_threshold)
         fh = np.zeros_like(dflat)
         info = ctypes.c_int(1)
         nm, nf = ctypes.c_int(nmol), ctypes.c_int(1)
@@ -663,6 +680,13 @@ def run_batch(args):
                                         "replay_ms_p99": pct(timesm, 99), "max_abs_dF_vs_fp64": df_max,
                                         "max_abs_dE2_Eh": de_max,
                                         "f32_quartet_fraction": stm["f32_quartets"] / max(1, stm["quartets"])},
+                "batched_double_float_graph": {"builds_per_s": ws * nmol * args.steps / tdf,
+                                               "replay_ms_p50": pct(timesdf, 50),
+                                               "max_abs_dF_vs_fp64": float(np.abs((fdf - f64).cpu().numpy()).max())},
+                "batched_mixed_df_graph": {"builds_per_s": ws * nmol * args.steps / tmd,
+                                           "replay_ms_p50": pct(timesmd, 50),
+                                           "max_abs_dF_vs_fp64": float(np.abs((fmd - f64).cpu().numpy()).max()),
+                                           "f32_quartet_fraction": stmd["f32_quartets"] / max(1, stmd["quartets"])},
                 "speedup_vs_plain_fp64": value / plain_rate,
                 "per_molecule_latency_ms": {"p50": pct(timesm, 50), "p99": pct(timesm, 99),
                                             "note": "every molecule of a batch completes with its graph replay"},
@@ -714,8 +738,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="water32_ccpvdz", choices=sorted(WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer seam timing (profiling runs)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed-fast", "df"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed-fast", "df", "mixed-df"])
     ap.add_argument("--mixed-threshold", type=float, default=1e-6)
+    ap.add_argument("--no-df", action="store_true", help="skip the double-float comparison of the default run")
     args = ap.parse_args()
     WORKLOAD.clear()
     WORKLOAD.update(WORKLOADS[args.workload])

@@ -184,7 +184,10 @@ int oqpg_schwarz(const oqpg_ctx* ctx, double* q);
  * (pairs of FP32 numbers, ~44 significant bits, on the FP32 pipe): the
  * thread-per-quartet classes digest in FP64, the warp-per-quartet classes in
  * double-float; all blocks are added into the FP64 accumulators (threshold
- * ignored).  No counterpart in the reference. */
+ * ignored).  mode 4 ("mixed-df"): the split of mode 2 with the quartets above
+ * the threshold in double-float instead of FP64.  The gradient follows modes
+ * 1, 2 and 4 with FP32 below the threshold and FP64 above it.  No counterpart
+ * in the reference. */
 int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold);
 
 /* Statistics of the last build, up to n (<= 73) doubles:

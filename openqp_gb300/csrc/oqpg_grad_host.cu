@@ -223,7 +223,7 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
       }
   cudaEvent_t e0 = c->ev[0], e1 = c->ev[3];
   GK(cudaEventRecord(e0, st));
-  const bool split = (c->precision_mode == 1 || c->precision_mode == 2) && c->tau_f32 > 0.0;
+  const bool split = (c->precision_mode == 1 || c->precision_mode == 2 || c->precision_mode == 4) && c->tau_f32 > 0.0;
   if ((rc = gupload(c->d_gmat, mats, st))) return rc;
   if (split) {
     std::vector<float> matsf(mats.size());
@@ -292,7 +292,7 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
     g.xsf = xs ? fm + 2 * n2 : nullptr;
     g.ysf = xs ? fm + 3 * n2 : nullptr;
   }
-  g.roots_f32 = c->precision_mode == 2 ? 1 : 0;
+  g.roots_f32 = (c->precision_mode == 2 || c->precision_mode == 4) ? 1 : 0;
   g.ncart = nc;
   g.coff = c->d_coff.as<int>();
   g.atom = c->d_atom.as<int>();

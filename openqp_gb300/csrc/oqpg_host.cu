@@ -241,12 +241,17 @@ __device__ __forceinline__ int prim_bin(const PairDev* pairs, uint2 q) {
 
 __device__ __forceinline__ int survivor_bin(const PairDev* pairs, const PrimPair* prims, uint2 q, float lo) {
   const PairDev P = pairs[q.x], Q = pairs[q.y];
+  // the heaviest quartets go to the primitive-parallel kernels whatever their
+  // exact count: bin them by the product and spare the scan
+  if (P.pcnt * Q.pcnt > 512) return work_bin(P.pcnt * Q.pcnt);
+  const float lo2 = lo * lo;
   int n = 0;
   for (int j = 0; j < Q.pcnt; ++j) {
     const float ks = __ldg(&prims[Q.poff + j].spf), kp = __ldg(&prims[Q.poff + j].pf);
     for (int i = 0; i < P.pcnt; ++i) {
-      const float r = fabsf(__ldg(&prims[P.poff + i].spf) * ks) * rsqrtf(__ldg(&prims[P.poff + i].pf) + kp);
-      n += r >= lo ? 1 : 0;
+      // |sp sq| / sqrt(p + q) >= lo, squared (FP32, no reciprocal square root)
+      const float t = __ldg(&prims[P.poff + i].spf) * ks;
+      n += t * t >= lo2 * (__ldg(&prims[P.poff + i].pf) + kp) ? 1 : 0;
     }
   }
   return work_bin(n);
@@ -695,7 +700,11 @@ void ctx_free(oqpg_ctx* c) {
   delete c;
 }
 
-bool split_on(const oqpg_ctx* c) { return (c->precision_mode == 1 || c->precision_mode == 2) && c->tau_f32 > 0.0; }
+bool split_on(const oqpg_ctx* c) {
+  return (c->precision_mode == 1 || c->precision_mode == 2 || c->precision_mode == 4) && c->tau_f32 > 0.0;
+}
+// double-float kernels for the quartets that are not FP32 (modes 3 and 4)
+bool df_on(const oqpg_ctx* c) { return c->precision_mode == 3 || c->precision_mode == 4; }
 
 // Buffers of one pipeline whose sizes follow from the batch alone.
 int ensure_bufs(oqpg_ctx* c, BuildBufs& B, int nk) {
@@ -706,7 +715,7 @@ int ensure_bufs(oqpg_ctx* c, BuildBufs& B, int nk) {
     CK(B.djf.ensure(sizeof(float) * n2));
     if (nk == 2) CK(B.dkf.ensure(sizeof(float) * 2 * n2));
   }
-  if (c->precision_mode == 3) {
+  if (df_on(c)) {
     CK(B.djdf.ensure(sizeof(dfl) * n2));
     if (nk == 2) CK(B.dkdf.ensure(sizeof(dfl) * 2 * n2));
   }
@@ -763,7 +772,7 @@ int issue_densities(oqpg_ctx* c, BuildBufs& B, const double* dp, int nfocks, cud
       CK(cudaGetLastError());
     }
   }
-  if (c->precision_mode == 3) {
+  if (df_on(c)) {
     k_to_df<<<g, 256, 0, st>>>(B.dj.as<double>(), (long long)n2, B.djdf.as<dfl>());
     CK(cudaGetLastError());
     if (nfocks == 2) {
@@ -834,7 +843,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
   if (timing) CK(cudaEventRecord(c->ev[0], st));
   CK(cudaMemsetAsync(B.flag.p, 0, sizeof(unsigned), st));
   if ((rc = issue_densities(c, B, dp, nfocks, st))) return rc;
-  nlaunch += 2 + (split_on(c) || c->precision_mode == 3 ? (nk == 2 ? 2 : 1) : 0);
+  nlaunch += 2 + (split_on(c) ? (nk == 2 ? 2 : 1) : 0) + (df_on(c) ? (nk == 2 ? 2 : 1) : 0);
   ListArgs la = list_args(c, B);
   la.write = 1;
   CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * NLIST, st));
@@ -897,7 +906,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
   a.dkdf = (nk == 1) ? B.djdf.as<dfl>() : B.dkdf.as<dfl>();
   a.gj = B.gj.as<double>();
   a.gk = B.gk.as<double>();
-  a.roots_f32 = c->precision_mode == 2 ? 1 : 0;
+  a.roots_f32 = (c->precision_mode == 2 || c->precision_mode == 4) ? 1 : 0;
   unsigned long long* ranges = B.ranges.as<unsigned long long>();
   // heaviest classes first
   for (int cl = NCLASS - 1; cl >= 0; --cl) {
@@ -908,7 +917,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
     for (int prec = 0; prec < 2; ++prec) {
       const int li = cl + prec * NCLASS;
       if (!B.cap[li]) continue;
-      const int fl = prec ? MODE_F32 : (c->precision_mode == 3 ? MODE_DF : 0);
+      const int fl = prec ? MODE_F32 : (df_on(c) ? MODE_DF : 0);
       a.counters = B.primc.as<unsigned long long>() + li;
       a.quartets = B.slists[li].as<uint2>();
       a.nquartets = (long long)B.cap[li];
@@ -1268,10 +1277,11 @@ int oqpg_measure_fp64_peak(int iters, double* tflops) {
 
 int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold) {
   if (!ctx) return NOT_INIT;
-  if (mode < 0 || mode > 3) return UNSUPPORTED;
-  if ((mode == 1 || mode == 2) && !(threshold > 0.0)) return UNSUPPORTED;
+  if (mode < 0 || mode > 4) return UNSUPPORTED;
+  const bool split = mode == 1 || mode == 2 || mode == 4;
+  if (split && !(threshold > 0.0)) return UNSUPPORTED;
   ctx->precision_mode = mode;
-  ctx->tau_f32 = (mode == 1 || mode == 2) ? threshold : 0.0;
+  ctx->tau_f32 = split ? threshold : 0.0;
   ctx->hb.sized = false;  // the FP32 lists are sized by a fresh count pass
   return OK;
 }

@@ -149,10 +149,11 @@ class FockBuilder:
         (Schwarz bound x shell density) is below threshold run in FP32 with their
         Rys roots/weights in FP64; "mixed-fast": the same with FP32 roots;
         "df": the thread-per-quartet classes in double-float arithmetic
-        (FP32 pairs, ~1e-13 relative) with FP64 digestion, no split.  The
+        (FP32 pairs, ~1e-13 relative) with FP64 digestion, no split;
+        "mixed-df": FP32 below the threshold (as mixed-fast), double-float above.  The
         gradient (grad2) splits the same way on the bound of its two-particle
         density."""
-        m = {"fp64": 0, "mixed": 1, "mixed-fast": 2, "df": 3}[mode]
+        m = {"fp64": 0, "mixed": 1, "mixed-fast": 2, "df": 3, "mixed-df": 4}[mode]
         rc = lib().oqpg_set_precision(self.h, m, float(threshold))
         if rc != 0:
             raise FockError(rc, "oqpg_set_precision")

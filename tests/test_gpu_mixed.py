@@ -92,3 +92,21 @@ def test_double_float_mode_matches_fp64_and_oracle(gpu, oracle_lib, basis, nw):
     fu = fb.fock_jk(du)
     fb.set_precision("fp64")
     assert np.abs(fu - fb.fock_jk(du)).max() < 1e-11
+
+
+def test_mixed_df_mode(gpu):
+    """mixed-df: FP32 below the threshold, double-float above; the error is the
+    FP32 part's (as mixed-fast), the double-float part adds nothing visible."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(5, workloads.cube_edge_like_c1(5), seed=23, basis="6-31g(d)")
+    fb = gpu.FockBuilder(bas)
+    d = workloads.density(bas, 25, 23)
+    f64 = fb.fock_jk(d)
+    fb.set_precision("mixed-fast", 1e-6)
+    fmf = fb.fock_jk(d)
+    fb.set_precision("mixed-df", 1e-6)
+    fmd = fb.fock_jk(d)
+    st = fb.stats()
+    assert st["f32_quartets"] > 0
+    assert np.abs(fmd - f64).max() < 1e-8
+    assert np.abs(fmd - fmf).max() < 1e-10
