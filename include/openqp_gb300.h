@@ -86,6 +86,33 @@ int routec_fock_set_precision(int mode, double threshold);
 void routec_grad2(const double* d, const double* xyz, double* de, const int* nbf, const int* natm,
                   const double* hfscale, const double* coulscale, int* info);
 
+/* Response-type builds on the process-global context (extensions: the
+ * reference has no seam for these digestions; a maintainer binds them in
+ * place of the int2_driver%run call of the consumer).
+ *
+ * routec_fock_td replaces int2_td_data_t (source/tdhf_lib.F90:140-224 and its
+ * parallel_stop :89-111), used by modules/tdhf_energy.F90:221,
+ * modules/cphf.F90:193 and modules/nmr_shielding.F90:454-487.
+ * d2(nbf, nbf, nvec) general square densities, apb / amb (nbf, nbf, nvec)
+ * OVERWRITTEN, all Fortran column-major; flags = OQPG_TD_* (the data type's
+ * int_apb, int_amb, tamm_dancoff, tamm_dancoff_coulomb); se / sc the
+ * scale_exchange / scale_coulomb of the data type.  Outputs that the flags
+ * do not ask for come back zero, as the reference's zero-initialised arrays.
+ *
+ * routec_fock_mrsf replaces the first pass of int2_mrsf_data_t (nmat = 7,
+ * source/tdhf_mrsf_lib.F90:218-333) or int2_umrsf_data_t (nmat = 11,
+ * :337-426) with tamm_dancoff = .true.; d3 / f3 (nvec, nmat, nbf, nbf)
+ * Fortran column-major, f3 OVERWRITTEN.  The CAM pass 2 is not built
+ * (info = 3 is never returned for it: the caller runs pass 2 natively). */
+#define OQPG_TD_APB 1
+#define OQPG_TD_AMB 2
+#define OQPG_TD_TDA 4
+#define OQPG_TD_TDA_COULOMB 8
+void routec_fock_td(const double* d2, double* apb, double* amb, const int* nbf, const int* nvec, const int* flags,
+                    const double* se, const double* sc, int* info);
+void routec_fock_mrsf(const double* d3, double* f3, const int* nbf, const int* nvec, const int* nmat,
+                      const double* se, const double* sc, int* info);
+
 /* Release the process-global context. */
 void routec_fock_finalize(void);
 
@@ -236,6 +263,21 @@ int oqpg_grad2_bilinear(oqpg_ctx* ctx, const double* x, const double* y, const d
  * bound of their two-particle density is below the threshold run in FP32 and
  * add into the FP64 gradient. */
 int oqpg_grad_stats(const oqpg_ctx* ctx, double* out, int n);
+
+/* Response-type builds (single-molecule contexts; see routec_fock_td and
+ * routec_fock_mrsf for the layouts and the reference routines).  Every
+ * density is screened, evaluated and digested in one pass over the quartets:
+ * the integrals are computed once for all nvec (x nmat) matrices.  The
+ * _device forms take device pointers and run on the given stream (null: the
+ * context's), synchronising before they return.  The context's precision
+ * mode applies. */
+int oqpg_fock_td(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, int nvec, int flags, double se,
+                 double sc);
+int oqpg_fock_td_device(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, int nvec, int flags, double se,
+                        double sc, void* stream);
+int oqpg_fock_mrsf(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, double se, double sc);
+int oqpg_fock_mrsf_device(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
+                          void* stream);
 
 /* Angular momenta (la, lb, lc, ld) of class c (0 <= c < 21). */
 int oqpg_class_l(int c, int* l4);

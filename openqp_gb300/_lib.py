@@ -68,6 +68,19 @@ def lib():
         L.routec_grad2.argtypes = [_d, _d, _d, _i, _i, _d, _d, _i]
         L.routec_grad2.restype = None
         L.oqpg_one_electron.argtypes = [ctypes.c_int, _i, _i, _i, _d, _d, _i, ctypes.c_int, _d, _d, ctypes.c_int, _d]
+        L.oqpg_fock_td.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_double]
+        L.oqpg_fock_td_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_void_p]
+        L.oqpg_fock_mrsf.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_double]
+        L.oqpg_fock_mrsf_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+        L.routec_fock_td.argtypes = [_d, _d, _d, _i, _i, _i, _d, _d, _i]
+        L.routec_fock_td.restype = None
+        L.routec_fock_mrsf.argtypes = [_d, _d, _i, _i, _i, _d, _d, _i]
+        L.routec_fock_mrsf.restype = None
         _lib = L
     return _lib
 

@@ -57,20 +57,21 @@ struct BuildArgs {
   long long nquartets;     // quartets (or, with range, the capacity that sizes the grid)
   const unsigned long long* range;  // optional device [begin, end) into quartets, read at kernel start
   int nbf;                 // row stride of the stacked matrices (largest nbf of the batch)
-  size_t kstride;          // elements between the exchange densities / accumulators of one batch
+  size_t kstride;          // elements between consecutive densities / accumulators (J or K)
+  int nj;                  // number of Coulomb densities (1 for the SCF builds)
   int nk;                  // number of exchange densities (1 RHF, 2 UHF/ROHF)
   double prim_cut;         // |K/p| pre-screen of a primitive pair
   double prim_cut2;        // (sp sq)^2 < prim_cut2 (p + q) skips a primitive quartet
   float prim_cut_lo;       // FP32 decision band of that test: |sp sq| / sqrt(p+q) below lo
   float prim_cut_hi;       // skips, above hi keeps, in between FP64 decides
   double elem_cut;         // element cutoff on |(ab|cd)|
-  const double* dj;        // full nbf x nbf density for Coulomb
+  const double* dj;        // nj full nbf x nbf densities for Coulomb
   const double* dk;        // nk full densities for exchange
   const float* djf;        // FP32 copies of dj / dk for the FP32 quartets
   const float* dkf;
   const struct dfl* djdf;  // double-float copies (df mode)
   const struct dfl* dkdf;
-  double* gj;              // nbf x nbf Coulomb accumulator
+  double* gj;              // nj x nbf x nbf Coulomb accumulators
   double* gk;              // nk x nbf x nbf exchange accumulators
   double* schwarz_out;     // Schwarz mode: per pair sqrt(max |(ab|ab)|)
   unsigned long long* counters;  // [0] primitive quartets evaluated by this launch

@@ -537,9 +537,10 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
   // columns within the molecule, rows in the stacked matrices
   const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
   const int ra = SA.mrow + oa, rb = SB.mrow + ob, rc = SC.mrow + oc;
-  const T* djt = dj_of<T>(a);
   // Coulomb: G_J[ab] += 2f sum_cd V D_cd ; G_J[cd] += 2f sum_ab V D_ab
-  {
+  for (int jj = 0; jj < a.nj; ++jj) {
+    const T* djt = dj_of<T>(a) + (size_t)jj * a.kstride;
+    double* gj = a.gj + (size_t)jj * a.kstride;
     T dab[E::A * E::B], dcd[E::C * E::D];
 #pragma unroll
     for (int i = 0; i < E::A; ++i)
@@ -566,11 +567,11 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
 #pragma unroll
     for (int i = 0; i < E::A; ++i)
 #pragma unroll
-      for (int j = 0; j < E::B; ++j) atomicAdd(a.gj + (size_t)(ra + i) * n + ob + j, f2 * (double)jab[i * E::B + j]);
+      for (int j = 0; j < E::B; ++j) atomicAdd(gj + (size_t)(ra + i) * n + ob + j, f2 * (double)jab[i * E::B + j]);
 #pragma unroll
     for (int i = 0; i < E::C; ++i)
 #pragma unroll
-      for (int j = 0; j < E::D; ++j) atomicAdd(a.gj + (size_t)(rc + i) * n + od + j, f2 * (double)jcd[i * E::D + j]);
+      for (int j = 0; j < E::D; ++j) atomicAdd(gj + (size_t)(rc + i) * n + od + j, f2 * (double)jcd[i * E::D + j]);
   }
   // Exchange: G_K[ac] += f sum V D_bd ; [ad] += f V D_bc ; [bc] += f V D_ad ; [bd] += f V D_ac
   for (int kk = 0; kk < a.nk; ++kk) {
@@ -778,92 +779,104 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
   }
   const T cut = (T)a.elem_cut;
   for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], cut);
-  // density blocks
+  // density blocks, one Coulomb and up to two exchange densities per pass
+  // (one pass for the SCF builds)
   const int n = a.nbf;
   const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
   const int ra = SA.mrow + oa, rb = SB.mrow + ob, rc = SC.mrow + oc;
-  const T* djt = dj_of<T>(a);
   T* Dab = W + NE;                 // after V (NE >= NEP)
   T* Dcd = Dab + E::A * E::B;
   T* Dk = Dcd + E::C * E::D;       // per k: ac, ad, bc, bd
   constexpr int DKS = SM::DK;
-  for (int i = lane; i < E::A * E::B; i += 32) Dab[i] = __ldg(djt + (size_t)(ra + i / E::B) * n + ob + i % E::B);
-  for (int i = lane; i < E::C * E::D; i += 32) Dcd[i] = __ldg(djt + (size_t)(rc + i / E::D) * n + od + i % E::D);
-  for (int kk = 0; kk < a.nk; ++kk) {
-    const T* dk = dk_of<T>(a) + (size_t)kk * a.kstride;
-    T* base = Dk + kk * DKS;
-    for (int i = lane; i < E::A * E::C; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::C) * n + oc + i % E::C);
-    base += E::A * E::C;
-    for (int i = lane; i < E::A * E::D; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::D) * n + od + i % E::D);
-    base += E::A * E::D;
-    for (int i = lane; i < E::B * E::C; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::C) * n + oc + i % E::C);
-    base += E::B * E::C;
-    for (int i = lane; i < E::B * E::D; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::D) * n + od + i % E::D);
-  }
-  __syncwarp();
   double f = 1.0;
   if (P.sha == P.shb) f *= 0.5;
   if (Q.sha == Q.shb) f *= 0.5;
   if (qd.x == qd.y) f *= 0.5;
   constexpr int NAB = E::A * E::B, NCD = E::C * E::D;
   constexpr int NAC = E::A * E::C, NAD = E::A * E::D, NBC = E::B * E::C, NBD = E::B * E::D;
-  const int ntarget = NAB + NCD + a.nk * (NAC + NAD + NBC + NBD);
-  // Every target element is a strided dot product of V with a density block:
-  //   s = sum_{u < n1, v < n2} V[vb + u s1 + v s2] Dv[u n2 + v].
-  // Only the (integer) descriptor depends on the target kind, so the lanes of
-  // a round share one FP64 instruction stream whatever kinds they hold.
   constexpr int BCD = E::B * E::C * E::D, CD_ = E::C * E::D;
-  for (int o = lane; o < ntarget; o += 32) {
-    int vb, s1, s2, n1, n2;
-    const T* dv;
-    double* dst;
-    double fac;
-    if (o < NAB) {          // J[a][b] += sum_cd V D[c][d]
-      const int i = o / E::B, j = o % E::B;
-      vb = o * NCD; s1 = 0; s2 = 1; n1 = 1; n2 = NCD; dv = Dcd;
-      dst = a.gj + (size_t)(ra + i) * n + ob + j;
-      fac = 2.0 * f;
-    } else if (o < NAB + NCD) {  // J[c][d] += sum_ab V D[a][b]
-      const int cd = o - NAB, k = cd / E::D, l = cd % E::D;
-      vb = cd; s1 = NCD; s2 = 0; n1 = NAB; n2 = 1; dv = Dab;
-      dst = a.gj + (size_t)(rc + k) * n + od + l;
-      fac = 2.0 * f;
-    } else {
-      int r = o - NAB - NCD;
-      const int kk = r / (NAC + NAD + NBC + NBD);
-      r -= kk * (NAC + NAD + NBC + NBD);
-      const T* dk = Dk + kk * DKS;
-      double* gk = a.gk + (size_t)kk * a.kstride;
-      fac = f;
-      if (r < NAC) {  // K[a][c] += sum_bd V[a b c d] D[b][d]
-        const int i = r / E::C, k = r % E::C;
-        vb = i * BCD + k * E::D; s1 = CD_; s2 = 1; n1 = E::B; n2 = E::D; dv = dk + NAC + NAD + NBC;
-        dst = gk + (size_t)(ra + i) * n + oc + k;
-      } else if (r < NAC + NAD) {  // K[a][d] += sum_bc V D[b][c]
-        r -= NAC;
-        const int i = r / E::D, l = r % E::D;
-        vb = i * BCD + l; s1 = CD_; s2 = E::D; n1 = E::B; n2 = E::C; dv = dk + NAC + NAD;
-        dst = gk + (size_t)(ra + i) * n + od + l;
-      } else if (r < NAC + NAD + NBC) {  // K[b][c] += sum_ad V D[a][d]
-        r -= NAC + NAD;
-        const int j = r / E::C, k = r % E::C;
-        vb = j * CD_ + k * E::D; s1 = BCD; s2 = 1; n1 = E::A; n2 = E::D; dv = dk + NAC;
-        dst = gk + (size_t)(rb + j) * n + oc + k;
-      } else {  // K[b][d] += sum_ac V D[a][c]
-        r -= NAC + NAD + NBC;
-        const int j = r / E::D, l = r % E::D;
-        vb = j * CD_ + l; s1 = BCD; s2 = E::D; n1 = E::A; n2 = E::C; dv = dk;
-        dst = gk + (size_t)(rb + j) * n + od + l;
+  const int npass = a.nj > (a.nk + 1) / 2 ? a.nj : (a.nk + 1) / 2;
+  for (int pass = 0; pass < npass; ++pass) {
+    const bool hasj = pass < a.nj;
+    const int k0 = 2 * pass;
+    const int nkp = a.nk - k0 >= 2 ? 2 : (a.nk - k0 > 0 ? a.nk - k0 : 0);
+    if (pass) __syncwarp();  // the previous pass has read its blocks
+    if (hasj) {
+      const T* djt = dj_of<T>(a) + (size_t)pass * a.kstride;
+      for (int i = lane; i < NAB; i += 32) Dab[i] = __ldg(djt + (size_t)(ra + i / E::B) * n + ob + i % E::B);
+      for (int i = lane; i < NCD; i += 32) Dcd[i] = __ldg(djt + (size_t)(rc + i / E::D) * n + od + i % E::D);
+    }
+    for (int kk = 0; kk < nkp; ++kk) {
+      const T* dk = dk_of<T>(a) + (size_t)(k0 + kk) * a.kstride;
+      T* base = Dk + kk * DKS;
+      for (int i = lane; i < NAC; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::C) * n + oc + i % E::C);
+      base += NAC;
+      for (int i = lane; i < NAD; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::D) * n + od + i % E::D);
+      base += NAD;
+      for (int i = lane; i < NBC; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::C) * n + oc + i % E::C);
+      base += NBC;
+      for (int i = lane; i < NBD; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::D) * n + od + i % E::D);
+    }
+    __syncwarp();
+    double* gj = a.gj + (size_t)pass * a.kstride;
+    const int nJ = hasj ? NAB + NCD : 0;
+    const int ntarget = nJ + nkp * (NAC + NAD + NBC + NBD);
+    // Every target element is a strided dot product of V with a density block:
+    //   s = sum_{u < n1, v < n2} V[vb + u s1 + v s2] Dv[u n2 + v].
+    // Only the (integer) descriptor depends on the target kind, so the lanes of
+    // a round share one FP64 instruction stream whatever kinds they hold.
+    for (int o = lane; o < ntarget; o += 32) {
+      int vb, s1, s2, n1, n2;
+      const T* dv;
+      double* dst;
+      double fac;
+      if (hasj && o < NAB) {  // J[a][b] += sum_cd V D[c][d]
+        const int i = o / E::B, j = o % E::B;
+        vb = o * NCD; s1 = 0; s2 = 1; n1 = 1; n2 = NCD; dv = Dcd;
+        dst = gj + (size_t)(ra + i) * n + ob + j;
+        fac = 2.0 * f;
+      } else if (o < nJ) {  // J[c][d] += sum_ab V D[a][b]
+        const int cd = o - NAB, k = cd / E::D, l = cd % E::D;
+        vb = cd; s1 = NCD; s2 = 0; n1 = NAB; n2 = 1; dv = Dab;
+        dst = gj + (size_t)(rc + k) * n + od + l;
+        fac = 2.0 * f;
+      } else {
+        int r = o - nJ;
+        const int kk = r / (NAC + NAD + NBC + NBD);
+        r -= kk * (NAC + NAD + NBC + NBD);
+        const T* dk = Dk + kk * DKS;
+        double* gk = a.gk + (size_t)(k0 + kk) * a.kstride;
+        fac = f;
+        if (r < NAC) {  // K[a][c] += sum_bd V[a b c d] D[b][d]
+          const int i = r / E::C, k = r % E::C;
+          vb = i * BCD + k * E::D; s1 = CD_; s2 = 1; n1 = E::B; n2 = E::D; dv = dk + NAC + NAD + NBC;
+          dst = gk + (size_t)(ra + i) * n + oc + k;
+        } else if (r < NAC + NAD) {  // K[a][d] += sum_bc V D[b][c]
+          r -= NAC;
+          const int i = r / E::D, l = r % E::D;
+          vb = i * BCD + l; s1 = CD_; s2 = E::D; n1 = E::B; n2 = E::C; dv = dk + NAC + NAD;
+          dst = gk + (size_t)(ra + i) * n + od + l;
+        } else if (r < NAC + NAD + NBC) {  // K[b][c] += sum_ad V D[a][d]
+          r -= NAC + NAD;
+          const int j = r / E::C, k = r % E::C;
+          vb = j * CD_ + k * E::D; s1 = BCD; s2 = 1; n1 = E::A; n2 = E::D; dv = dk + NAC;
+          dst = gk + (size_t)(rb + j) * n + oc + k;
+        } else {  // K[b][d] += sum_ac V D[a][c]
+          r -= NAC + NAD + NBC;
+          const int j = r / E::D, l = r % E::D;
+          vb = j * CD_ + l; s1 = BCD; s2 = E::D; n1 = E::A; n2 = E::C; dv = dk;
+          dst = gk + (size_t)(rb + j) * n + od + l;
+        }
       }
+      T s = 0;
+      const int nt = n1 * n2;
+      int u = 0, v = 0;
+      for (int t = 0; t < nt; ++t) {
+        s = fma(V[vb + u * s1 + v * s2], dv[t], s);
+        if (++v == n2) { v = 0; ++u; }
+      }
+      atomicAdd(dst, fac * (double)s);
     }
-    T s = 0;
-    const int nt = n1 * n2;
-    int u = 0, v = 0;
-    for (int t = 0; t < nt; ++t) {
-      s = fma(V[vb + u * s1 + v * s2], dv[t], s);
-      if (++v == n2) { v = 0; ++u; }
-    }
-    atomicAdd(dst, fac * (double)s);
   }
 }
 

@@ -700,26 +700,41 @@ void ctx_free(oqpg_ctx* c) {
   delete c;
 }
 
+}  // namespace
+
+namespace oqpg {
 bool split_on(const oqpg_ctx* c) {
   return (c->precision_mode == 1 || c->precision_mode == 2 || c->precision_mode == 4) && c->tau_f32 > 0.0;
 }
 // double-float kernels for the quartets that are not FP32 (modes 3 and 4)
 bool df_on(const oqpg_ctx* c) { return c->precision_mode == 3 || c->precision_mode == 4; }
+}  // namespace oqpg
 
-// Buffers of one pipeline whose sizes follow from the batch alone.
-int ensure_bufs(oqpg_ctx* c, BuildBufs& B, int nk) {
+namespace {
+
+// Buffers of one pipeline whose sizes follow from the batch and the job.  A
+// general job stages all its slices in dk (and its FP32 / double-float copies).
+int ensure_bufs(oqpg_ctx* c, BuildBufs& B, const Job& job) {
   const size_t n2 = (size_t)c->nbf * c->stride;
-  CK(B.dj.ensure(sizeof(double) * n2));
-  if (nk == 2) CK(B.dk.ensure(sizeof(double) * 2 * n2));
-  if (split_on(c)) {
-    CK(B.djf.ensure(sizeof(float) * n2));
-    if (nk == 2) CK(B.dkf.ensure(sizeof(float) * 2 * n2));
+  const size_t nj = (size_t)std::max(job.nj(), 1), nk = (size_t)std::max(job.nk(), 1);
+  if (job.gen) {
+    const size_t nsl = std::max<size_t>(job.gen->slices.size(), 1);
+    CK(B.dk.ensure(sizeof(double) * nsl * n2));
+    if (split_on(c)) CK(B.dkf.ensure(sizeof(float) * nsl * n2));
+    if (df_on(c)) CK(B.dkdf.ensure(sizeof(dfl) * nsl * n2));
+  } else {
+    CK(B.dj.ensure(sizeof(double) * n2));
+    if (nk == 2) CK(B.dk.ensure(sizeof(double) * 2 * n2));
+    if (split_on(c)) {
+      CK(B.djf.ensure(sizeof(float) * n2));
+      if (nk == 2) CK(B.dkf.ensure(sizeof(float) * 2 * n2));
+    }
+    if (df_on(c)) {
+      CK(B.djdf.ensure(sizeof(dfl) * n2));
+      if (nk == 2) CK(B.dkdf.ensure(sizeof(dfl) * 2 * n2));
+    }
   }
-  if (df_on(c)) {
-    CK(B.djdf.ensure(sizeof(dfl) * n2));
-    if (nk == 2) CK(B.dkdf.ensure(sizeof(dfl) * 2 * n2));
-  }
-  CK(B.gj.ensure(sizeof(double) * n2));
+  CK(B.gj.ensure(sizeof(double) * nj * n2));
   CK(B.gk.ensure(sizeof(double) * nk * n2));
   CK(B.dsh.ensure(sizeof(double) * std::max<long long>(c->dsh_elems, 1)));
   CK(B.dshf.ensure(sizeof(float) * std::max<long long>(c->dsh_elems, 1)));
@@ -757,7 +772,10 @@ ListArgs list_args(const oqpg_ctx* c, BuildBufs& B) {
 
 // Screening stage shared by the count pass and the build: unpacked densities
 // (and FP32 copies), shell densities and their per-molecule maxima.
-int issue_densities(oqpg_ctx* c, BuildBufs& B, const double* dp, int nfocks, cudaStream_t st) {
+int issue_densities(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st) {
+  if (job.gen) return gen_densities(c, B, *job.gen, st);
+  const double* dp = job.dp;
+  const int nfocks = job.nfocks;
   const size_t n2 = (size_t)c->nbf * c->stride;
   const unsigned g = (unsigned)std::min<long long>((n2 + 255) / 256, c->nsm * 8LL);
   k_unpack<<<g, 256, 0, st>>>(dp, nfocks, c->d_mols.as<MolDev>(), c->d_row_mol.as<int>(), c->nbf, c->stride,
@@ -816,10 +834,9 @@ int size_lists(oqpg_ctx* c, BuildBufs& B, const unsigned long long* counts, cuda
 }
 
 // Count pass: list lengths for the current density without writing the lists.
-int count_lists(oqpg_ctx* c, BuildBufs& B, const double* dp, int nfocks, cudaStream_t st,
-                unsigned long long* counts) {
+int count_lists(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, unsigned long long* counts) {
   int rc;
-  if ((rc = issue_densities(c, B, dp, nfocks, st))) return rc;
+  if ((rc = issue_densities(c, B, job, st))) return rc;
   ListArgs la = list_args(c, B);
   la.write = 0;
   CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * NLIST, st));
@@ -834,16 +851,16 @@ int count_lists(oqpg_ctx* c, BuildBufs& B, const double* dp, int nfocks, cudaStr
 // capacities; list lengths, sort cursors and work ranges stay on the device,
 // so the sequence can be captured into a CUDA graph.  A list longer than its
 // capacity sets the overflow flag; the finalize kernel then leaves f alone.
-int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* f_old, int nfocks, double se,
-                double sc, cudaStream_t st, bool timing, int* nlaunch_out) {
-  const int nk = nfocks;
+int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool timing, int* nlaunch_out) {
+  const int nj = job.nj(), nk = job.nk();
   const size_t n2 = (size_t)c->nbf * c->stride;
   int rc;
   int nlaunch = 0;
   if (timing) CK(cudaEventRecord(c->ev[0], st));
   CK(cudaMemsetAsync(B.flag.p, 0, sizeof(unsigned), st));
-  if ((rc = issue_densities(c, B, dp, nfocks, st))) return rc;
-  nlaunch += 2 + (split_on(c) ? (nk == 2 ? 2 : 1) : 0) + (df_on(c) ? (nk == 2 ? 2 : 1) : 0);
+  if ((rc = issue_densities(c, B, job, st))) return rc;
+  if (job.gen) nlaunch += 2 + (split_on(c) ? 1 : 0) + (df_on(c) ? 1 : 0);
+  else nlaunch += 2 + (split_on(c) ? (nk == 2 ? 2 : 1) : 0) + (df_on(c) ? (nk == 2 ? 2 : 1) : 0);
   ListArgs la = list_args(c, B);
   la.write = 1;
   CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * NLIST, st));
@@ -881,8 +898,8 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
   }
   if (timing) CK(cudaEventRecord(c->ev[1], st));
   // --- integrals + digestion
-  CK(cudaMemsetAsync(B.gj.p, 0, sizeof(double) * n2, st));
-  CK(cudaMemsetAsync(B.gk.p, 0, sizeof(double) * nk * n2, st));
+  if (nj) CK(cudaMemsetAsync(B.gj.p, 0, sizeof(double) * nj * n2, st));
+  if (nk) CK(cudaMemsetAsync(B.gk.p, 0, sizeof(double) * nk * n2, st));
   CK(cudaMemsetAsync(B.primc.p, 0, sizeof(unsigned long long) * NLIST, st));
   CK(cudaMemsetAsync(B.work.p, 0, sizeof(unsigned long long) * 2 * NLIST, st));
   BuildArgs a{};
@@ -893,17 +910,28 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
   a.primsdf = c->d_primsdf.as<PrimPairDF>();
   a.nbf = c->stride;
   a.kstride = n2;
+  a.nj = nj;
   a.nk = nk;
   a.prim_cut = 1e-4 * c->tau;
   a.prim_cut2 = a.prim_cut * a.prim_cut;
   set_band(a);
   a.elem_cut = c->tau;
-  a.dj = B.dj.as<double>();
-  a.dk = (nk == 1) ? B.dj.as<double>() : B.dk.as<double>();
-  a.djf = B.djf.as<float>();
-  a.dkf = (nk == 1) ? B.djf.as<float>() : B.dkf.as<float>();
-  a.djdf = B.djdf.as<dfl>();
-  a.dkdf = (nk == 1) ? B.djdf.as<dfl>() : B.dkdf.as<dfl>();
+  if (job.gen) {
+    const size_t k0 = (size_t)job.gen->k0 * n2;
+    a.dj = B.dk.as<double>();
+    a.dk = B.dk.as<double>() + k0;
+    a.djf = B.dkf.as<float>();
+    a.dkf = B.dkf.p ? B.dkf.as<float>() + k0 : nullptr;
+    a.djdf = B.dkdf.as<dfl>();
+    a.dkdf = B.dkdf.p ? B.dkdf.as<dfl>() + k0 : nullptr;
+  } else {
+    a.dj = B.dj.as<double>();
+    a.dk = (nk == 1) ? B.dj.as<double>() : B.dk.as<double>();
+    a.djf = B.djf.as<float>();
+    a.dkf = (nk == 1) ? B.djf.as<float>() : B.dkf.as<float>();
+    a.djdf = B.djdf.as<dfl>();
+    a.dkdf = (nk == 1) ? B.djdf.as<dfl>() : B.dkdf.as<dfl>();
+  }
   a.gj = B.gj.as<double>();
   a.gk = B.gk.as<double>();
   a.roots_f32 = (c->precision_mode == 2 || c->precision_mode == 4) ? 1 : 0;
@@ -937,11 +965,15 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const double* dp, double* f, double* 
     if (timing) CK(cudaEventRecord(c->evc[cl][1], st));
   }
   if (timing) CK(cudaEventRecord(c->ev[2], st));
-  const double ck = (nk == 1) ? 0.5 * se : se;
-  k_finalize<<<(unsigned)std::min<long long>((c->ntri + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
-      B.gj.as<double>(), B.gk.as<double>(), nk, c->d_mols.as<MolDev>(), c->nmol, c->ntri, c->stride, n2, sc, ck, f,
-      f_old, B.flag.as<unsigned>());
-  CK(cudaGetLastError());
+  if (job.gen) {
+    if ((rc = gen_finalize(c, B, *job.gen, st))) return rc;
+  } else {
+    const double ck = (nk == 1) ? 0.5 * job.se : job.se;
+    k_finalize<<<(unsigned)std::min<long long>((c->ntri + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
+        B.gj.as<double>(), B.gk.as<double>(), nk, c->d_mols.as<MolDev>(), c->nmol, c->ntri, c->stride, n2, job.sc,
+        ck, job.f, job.f_old, B.flag.as<unsigned>());
+    CK(cudaGetLastError());
+  }
   ++nlaunch;
   if (timing) CK(cudaEventRecord(c->ev[3], st));
   // readback of the flag, the list lengths and the primitive counts (pinned)
@@ -994,20 +1026,22 @@ void record_stats(oqpg_ctx* c, const BuildBufs& B, int nlaunch, bool timing) {
 // updated).  The first build of a context runs a count pass to size the
 // lists; a later build whose lists outgrow their capacities is redone with
 // larger ones (f and f_old untouched in between).
-int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfocks, double se, double sc,
-              cudaStream_t st) {
-  if (nfocks != 1 && nfocks != 2) return UNSUPPORTED;
+}  // namespace
+
+namespace oqpg {
+int ctx_build(oqpg_ctx* c, const Job& job, cudaStream_t st) {
+  if (!job.gen && job.nfocks != 1 && job.nfocks != 2) return UNSUPPORTED;
   BuildBufs& B = c->hb;
   int rc;
-  if ((rc = ensure_bufs(c, B, nfocks))) return rc;
+  if ((rc = ensure_bufs(c, B, job))) return rc;
   if (!B.sized) {
     unsigned long long counts[NLIST];
-    if ((rc = count_lists(c, B, dp, nfocks, st, counts))) return rc;
+    if ((rc = count_lists(c, B, job, st, counts))) return rc;
     if ((rc = size_lists(c, B, counts, st))) return rc;
   }
   for (int attempt = 0; attempt < 3; ++attempt) {
     int nlaunch = 0;
-    if ((rc = issue_build(c, B, dp, f, f_old, nfocks, se, sc, st, true, &nlaunch))) return rc;
+    if ((rc = issue_build(c, B, job, st, true, &nlaunch))) return rc;
     CK(cudaStreamSynchronize(st));
     const unsigned flag = (unsigned)(B.h_rb[0] & 0xffffffffu);
     if (flag == 0) {
@@ -1018,6 +1052,16 @@ int ctx_build(oqpg_ctx* c, const double* dp, double* f, double* f_old, int nfock
     if ((rc = size_lists(c, B, B.h_rb + 1, st))) return rc;
   }
   return DEV_ERR;  // quartet lists never fitted: nothing was written
+}
+}  // namespace oqpg
+
+namespace {
+
+// SCF job of packed densities
+Job packed_job(const double* dp, double* f, double* f_old, int nfocks, double se, double sc) {
+  Job j;
+  j.dp = dp; j.f = f; j.f_old = f_old; j.nfocks = nfocks; j.se = se; j.sc = sc;
+  return j;
 }
 
 int ctx_build_host(oqpg_ctx* c, const double* d, double* f, double* f_old, int nfocks, double se, double sc) {
@@ -1041,8 +1085,8 @@ int ctx_build_host(oqpg_ctx* c, const double* d, double* f, double* f_old, int n
     std::memcpy(c->h_out, f_old, bytes);
     CK(cudaMemcpyAsync(c->d_fold.p, c->h_out, bytes, cudaMemcpyHostToDevice, st));
   }
-  int rc = ctx_build(c, c->d_dp.as<double>(), c->d_f.as<double>(), f_old ? c->d_fold.as<double>() : nullptr, nfocks,
-                     se, sc, st);
+  int rc = ctx_build(c, packed_job(c->d_dp.as<double>(), c->d_f.as<double>(), f_old ? c->d_fold.as<double>() : nullptr,
+                                    nfocks, se, sc), st);
   if (rc) return rc;
   CK(cudaMemcpyAsync(c->h_out, c->d_f.p, bytes, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -1067,16 +1111,18 @@ int graph_capture(oqpg_ctx* c, const double* dp, int nfocks, double se, double s
   const size_t bytes = sizeof(double) * (size_t)c->ntri * nfocks;
   CK(c->d_gin.ensure(bytes));
   CK(c->d_gout.ensure(bytes));
-  if ((rc = ensure_bufs(c, B, nfocks))) return rc;
+  const Job cj = packed_job(dp, nullptr, nullptr, nfocks, se, sc);
+  if ((rc = ensure_bufs(c, B, cj))) return rc;
   unsigned long long counts[NLIST];
-  if ((rc = count_lists(c, B, dp, nfocks, gs, counts))) return rc;
+  if ((rc = count_lists(c, B, cj, gs, counts))) return rc;
   for (int k = 0; k < NLIST; ++k) counts[k] = std::max(counts[k], c->counts[k]);
   if ((rc = size_lists(c, B, counts, gs))) return rc;
   CK(cudaStreamSynchronize(gs));
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(gs, cudaStreamCaptureModeRelaxed));
   int nlaunch = 0;
-  rc = issue_build(c, B, c->d_gin.as<double>(), c->d_gout.as<double>(), nullptr, nfocks, se, sc, gs, false, &nlaunch);
+  rc = issue_build(c, B, packed_job(c->d_gin.as<double>(), c->d_gout.as<double>(), nullptr, nfocks, se, sc), gs,
+                   false, &nlaunch);
   cudaError_t e = cudaStreamEndCapture(gs, &g);
   if (rc) {
     if (g) cudaGraphDestroy(g);
@@ -1115,7 +1161,7 @@ int graph_build(oqpg_ctx* c, const double* d_device, double* f_device, int nfock
       return OK;
     }
   }
-  if ((rc = ctx_build(c, d_device, f_device, nullptr, nfocks, se, sc, st))) return rc;
+  if ((rc = ctx_build(c, packed_job(d_device, f_device, nullptr, nfocks, se, sc), st))) return rc;
   CK(cudaStreamSynchronize(st));
   return graph_capture(c, d_device, nfocks, se, sc);
 }
@@ -1171,7 +1217,7 @@ int oqpg_fock_jk_device(oqpg_ctx* ctx, const double* d_device, double* f_device,
                         void* stream) {
   if (!ctx) return NOT_INIT;
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-  return ctx_build(ctx, d_device, f_device, nullptr, nfocks, se, sc, st);
+  return ctx_build(ctx, packed_job(d_device, f_device, nullptr, nfocks, se, sc), st);
 }
 
 int oqpg_schwarz(const oqpg_ctx* ctx, double* q) {
@@ -1339,6 +1385,26 @@ int routec_fock_init_batch(int nmol, const int* nshell, const int* natom, const 
     g_ctx = nullptr;
   }
   return oqpg_create_batch(&g_ctx, nmol, nshell, natom, am, ncontr, origin, ex, cc, harmonic, xyz, cutoff);
+}
+
+void routec_fock_td(const double* d2, double* apb, double* amb, const int* nbf, const int* nvec, const int* flags,
+                    const double* se, const double* sc, int* info) {
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!d2 || !apb || !amb || !nbf || !nvec || !flags || !se || !sc) rc = UNSUPPORTED;
+  else if (*nbf != g_ctx->nbf) rc = NOT_INIT;
+  else rc = oqpg_fock_td(g_ctx, d2, apb, amb, *nvec, *flags, *se, *sc);
+  if (info) *info = rc;
+}
+
+void routec_fock_mrsf(const double* d3, double* f3, const int* nbf, const int* nvec, const int* nmat,
+                      const double* se, const double* sc, int* info) {
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!d3 || !f3 || !nbf || !nvec || !nmat || !se || !sc) rc = UNSUPPORTED;
+  else if (*nbf != g_ctx->nbf) rc = NOT_INIT;
+  else rc = oqpg_fock_mrsf(g_ctx, d3, f3, *nvec, *nmat, *se, *sc);
+  if (info) *info = rc;
 }
 
 void routec_fock_jk_batch(const double* d, double* f, const int* nmol, const int* nfocks, const double* se,

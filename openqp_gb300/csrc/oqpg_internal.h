@@ -97,6 +97,55 @@ __global__ void k_finalize(const double* __restrict__ gj, const double* __restri
                            const unsigned* __restrict__ flag);
 void set_band(BuildArgs& a);
 
+// --- general (square, not necessarily symmetric) densities -----------------
+// A response-type build (TDHF / CPHF A+B and A-B, MRSF sigma vectors) needs,
+// per input matrix X, J[X] and K[X] with the full permutational sums
+//   J[X]_ij = sum_kl (ij|kl) X_kl,   K[X]_ik = sum_jl (ij|kl) X_jl.
+// J only sees Xs = (X + X^T)/2; K[X] = K[Xs] + K[Xa] with Xa = (X - X^T)/2.
+// The kernels digest symmetric-storage densities: for a density S staged as a
+// full square matrix they accumulate G with J_full = G + G^T, and for K
+// K_full = G + G^T when S is symmetric, G - G^T when it is antisymmetric.
+// A job is a list of staged slices (Xs or Xa of one input), the Coulomb
+// slices [0, nj) and exchange slices [k0, k0 + nk) of that list, and per
+// output matrix a short sum of coef * (G + sign G^T) terms.
+struct GenSlice {
+  long long base;  // input matrix: element (r, c) at in[base + r in_rs + c in_cs]
+  int sign;        // +1: (X + X^T)/2, -1: (X - X^T)/2
+  int pad;
+};
+struct GenTerm {
+  double coef;
+  int kind;  // 0: Coulomb accumulator idx, 1: exchange accumulator idx
+  int idx;
+  int sign;  // +1 / -1: G + sign G^T
+  int pad;
+};
+struct GenOut {
+  double* dst;     // device: element (r, c) at dst[r out_rs + c out_cs]
+  int term0, nterm;
+};
+struct GenJob {
+  const double* in = nullptr;  // device
+  long long in_rs = 1, in_cs = 0, out_rs = 1, out_cs = 0;
+  std::vector<GenSlice> slices;
+  int nj = 0, k0 = 0, nk = 0;
+  std::vector<long long> screen;  // bases of the inputs that form the shell density
+  std::vector<GenOut> outs;
+  std::vector<GenTerm> terms;
+};
+
+// One build: packed SCF densities (gen == nullptr) or a general job.
+struct Job {
+  const double* dp = nullptr;
+  int nfocks = 0;
+  double* f = nullptr;
+  double* f_old = nullptr;
+  double se = 1.0, sc = 1.0;
+  const GenJob* gen = nullptr;
+  int nj() const { return gen ? gen->nj : 1; }
+  int nk() const { return gen ? gen->nk : nfocks; }
+};
+
 // Host-side primitive-pair tables of a context (oqpg_host.cu).
 struct HostPairs {
   std::vector<PairDev> pairs;
@@ -108,12 +157,19 @@ struct HostPairs {
 };
 
 struct GradArgs;
+struct BuildBufs;
 }  // namespace oqpg
 struct oqpg_ctx;
 namespace oqpg {
 void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vector<int>& ncontr,
                  const std::vector<int>& poff, const double* ex, const double* cc, double qcut, double ecut,
                  bool sp_screen, HostPairs& out);
+// general-job density staging / shell density and result assembly (oqpg_response.cu)
+int gen_densities(oqpg_ctx* c, BuildBufs& B, const GenJob& g, cudaStream_t st);
+int gen_finalize(oqpg_ctx* c, BuildBufs& B, const GenJob& g, cudaStream_t st);
+bool split_on(const oqpg_ctx* c);
+bool df_on(const oqpg_ctx* c);
+int ctx_build(oqpg_ctx* c, const Job& job, cudaStream_t st);
 cudaError_t launch_grad_a(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
 cudaError_t launch_grad_b(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
 
@@ -123,14 +179,14 @@ constexpr int NLIST = 2 * NCLASS;  // FP64 lists, then the FP32 lists of the pre
 // direct builds and one owned by its captured graph).
 struct BuildBufs {
   DevBuf dj, dk, djf, dkf, djdf, dkdf, gj, gk, dsh, dshf, dmax, counts, primc, hist, cursor, work, ranges, caps,
-      split, flag;
+      split, flag, gtab;
   DevBuf lists[NLIST], slists[NLIST], bins[NLIST];
   unsigned long long cap[NLIST] = {0};
   bool sized = false;
   unsigned long long* h_rb = nullptr;  // pinned readback: [0] flag, [1, 1+NLIST) counts, then primitive counts
   void release() {
     DevBuf* b[] = {&dj, &dk, &djf, &dkf, &djdf, &dkdf, &gj, &gk, &dsh, &dshf, &dmax, &counts, &primc, &hist,
-                   &cursor, &work, &ranges, &caps, &split, &flag};
+                   &cursor, &work, &ranges, &caps, &split, &flag, &gtab};
     for (DevBuf* x : b) x->release();
     for (auto& x : lists) x.release();
     for (auto& x : slists) x.release();

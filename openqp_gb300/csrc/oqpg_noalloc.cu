@@ -186,6 +186,7 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
   a.prims = c->d_prims.as<PrimPair>();
   a.nbf = n;
   a.kstride = n2;
+  a.nj = 1;
   a.nk = nk;
   a.prim_cut = 1e-4 * c->tau;
   a.prim_cut2 = a.prim_cut * a.prim_cut;

@@ -1,0 +1,348 @@
+// Response-type Fock builds on the same screened quartet pipeline: general
+// square (not necessarily symmetric) densities, many at once.
+//
+// Consumers in OpenQP (each replaced by one call here):
+//  * int2_td_data_t (tdhf_lib.F90:140-224, parallel_stop :89-111): TDHF / TDDFT
+//    A+B and A-B products, CPHF (modules/cphf.F90:193), NMR shielding
+//    (modules/nmr_shielding.F90:454-487);
+//  * int2_mrsf_data_t (tdhf_mrsf_lib.F90:218-333, pass 1) and
+//    int2_umrsf_data_t (tdhf_mrsf_lib.F90:337-426, pass 1): MRSF / UMRSF
+//    sigma vectors.
+// All of them are sums of J[X] and K[X] with full permutational sums over the
+// caller's matrices X; the GenJob recipe built here says which slices
+// (X + X^T)/2 or (X - X^T)/2 are staged, which accumulators they feed and how
+// each output matrix is assembled from the accumulators.
+#include <cstring>
+
+#include "oqpg_common.cuh"
+#include "oqpg_internal.h"
+#include "../../include/openqp_gb300.h"
+
+namespace oqpg {
+
+// Staged slice s: S[s][r][c] = (X(r, c) + sign X(c, r)) / 2 in the stacked
+// row-major layout (columns beyond nbf zeroed).
+__global__ void k_stage_gen(const double* __restrict__ in, long long rs, long long cs,
+                            const GenSlice* __restrict__ sl, int nsl, int n, int stride, double* out) {
+  const long long per = (long long)n * stride, tot = per * nsl;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int s = (int)(t / per);
+    const long long u = t - (long long)s * per;
+    const int r = (int)(u / stride), c = (int)(u % stride);
+    double v = 0.0;
+    if (c < n) {
+      const GenSlice S = sl[s];
+      const double x = in[S.base + r * rs + c * cs], y = in[S.base + c * rs + r * cs];
+      v = 0.5 * (x + (double)S.sign * y);
+    }
+    out[t] = v;
+  }
+}
+
+// shltd (tdhf_lib.F90:300-325) / shell_den_screen_mrsf (tdhf_mrsf_lib.F90:189-214):
+// for the pair (i >= j) the maximum |X(r, c)| over r in shell j, c in shell i
+// (that orientation of the block only) and over the screening inputs.
+__global__ void k_dsh_gen(const double* __restrict__ in, long long rs, long long cs,
+                          const long long* __restrict__ scr, int nscr, const int2* __restrict__ pair_ij, int npair,
+                          const int* __restrict__ aoff, const int* __restrict__ nao, int ns, double* dsh, float* dshf,
+                          unsigned long long* dmax_bits) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npair;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int2 ij = pair_ij[t];
+    const int hi = ij.x > ij.y ? ij.x : ij.y, lo = ij.x > ij.y ? ij.y : ij.x;
+    const int r0 = aoff[lo], r1 = r0 + nao[lo], c0 = aoff[hi], c1 = c0 + nao[hi];
+    double m = 0.0;
+    for (int q = 0; q < nscr; ++q) {
+      const double* x = in + scr[q];
+      for (int c = c0; c < c1; ++c)
+        for (int r = r0; r < r1; ++r) m = fmax(m, fabs(x[r * rs + c * cs]));
+    }
+    dsh[(long long)ij.x * ns + ij.y] = m;
+    dsh[(long long)ij.y * ns + ij.x] = m;
+    dshf[(long long)ij.x * ns + ij.y] = (float)m;
+    dshf[(long long)ij.y * ns + ij.x] = (float)m;
+    atomicMax(dmax_bits, (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+// out_o(r, c) = sum over the terms of o of coef (G[r][c] + sign G[c][r]),
+// G the term's Coulomb or exchange accumulator.  Nothing is written when a
+// quartet list overflowed (the build is then redone).
+__global__ void k_finalize_gen(const double* __restrict__ gj, const double* __restrict__ gk, size_t kstride,
+                               int stride, int n, const GenOut* __restrict__ outs, int nout,
+                               const GenTerm* __restrict__ terms, long long ors, long long ocs,
+                               const unsigned* __restrict__ flag) {
+  if (flag && *flag) return;
+  const long long per = (long long)n * n, tot = per * nout;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int o = (int)(t / per);
+    const long long u = t - (long long)o * per;
+    const int c = (int)(u / n), r = (int)(u % n);
+    const GenOut O = outs[o];
+    double v = 0.0;
+    for (int k = 0; k < O.nterm; ++k) {
+      const GenTerm T = terms[O.term0 + k];
+      const double* G = (T.kind ? gk : gj) + (size_t)T.idx * kstride;
+      v += T.coef * (G[(size_t)r * stride + c] + (double)T.sign * G[(size_t)c * stride + r]);
+    }
+    O.dst[r * ors + c * ocs] = v;
+  }
+}
+
+namespace {
+
+#define CKR(x)                                         \
+  do {                                                 \
+    cudaError_t e_ = (x);                              \
+    if (e_ != cudaSuccess) return e_ == cudaErrorMemoryAllocation ? NO_MEM : DEV_ERR; \
+  } while (0)
+
+size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+struct TabLayout {
+  size_t slices, screen, outs, terms, total;
+};
+
+TabLayout tab_layout(const GenJob& g) {
+  TabLayout L;
+  L.slices = 0;
+  L.screen = align16(L.slices + sizeof(GenSlice) * g.slices.size());
+  L.outs = align16(L.screen + sizeof(long long) * g.screen.size());
+  L.terms = align16(L.outs + sizeof(GenOut) * g.outs.size());
+  L.total = align16(L.terms + sizeof(GenTerm) * g.terms.size()) + 16;
+  return L;
+}
+
+unsigned grid_for(long long n, int nsm) { return (unsigned)std::min<long long>((n + 255) / 256, nsm * 8LL); }
+
+}  // namespace
+
+int gen_densities(oqpg_ctx* c, BuildBufs& B, const GenJob& g, cudaStream_t st) {
+  const TabLayout L = tab_layout(g);
+  CKR(B.gtab.ensure(L.total));
+  unsigned char* tab = B.gtab.as<unsigned char>();
+  if (!g.slices.empty())
+    CKR(cudaMemcpyAsync(tab + L.slices, g.slices.data(), sizeof(GenSlice) * g.slices.size(), cudaMemcpyHostToDevice,
+                        st));
+  if (!g.screen.empty())
+    CKR(cudaMemcpyAsync(tab + L.screen, g.screen.data(), sizeof(long long) * g.screen.size(),
+                        cudaMemcpyHostToDevice, st));
+  if (!g.outs.empty())
+    CKR(cudaMemcpyAsync(tab + L.outs, g.outs.data(), sizeof(GenOut) * g.outs.size(), cudaMemcpyHostToDevice, st));
+  if (!g.terms.empty())
+    CKR(cudaMemcpyAsync(tab + L.terms, g.terms.data(), sizeof(GenTerm) * g.terms.size(), cudaMemcpyHostToDevice,
+                        st));
+  const int nsl = (int)g.slices.size();
+  const long long n2 = (long long)c->nbf * c->stride;
+  if (nsl) {
+    k_stage_gen<<<grid_for(n2 * nsl, c->nsm), 256, 0, st>>>(g.in, g.in_rs, g.in_cs, (const GenSlice*)(tab + L.slices),
+                                                            nsl, c->nbf, c->stride, B.dk.as<double>());
+    CKR(cudaGetLastError());
+    if (split_on(c)) {
+      k_to_f32<<<grid_for(n2 * nsl, c->nsm), 256, 0, st>>>(B.dk.as<double>(), n2 * nsl, B.dkf.as<float>());
+      CKR(cudaGetLastError());
+    }
+    if (df_on(c)) {
+      k_to_df<<<grid_for(n2 * nsl, c->nsm), 256, 0, st>>>(B.dk.as<double>(), n2 * nsl, B.dkdf.as<dfl>());
+      CKR(cudaGetLastError());
+    }
+  }
+  CKR(cudaMemsetAsync(B.dmax.p, 0, sizeof(unsigned long long), st));
+  CKR(cudaMemsetAsync(B.dsh.p, 0, sizeof(double) * std::max<long long>(c->dsh_elems, 1), st));
+  k_dsh_gen<<<(unsigned)std::min<long long>((c->npair + 127) / 128, c->nsm * 8LL), 128, 0, st>>>(
+      g.in, g.in_rs, g.in_cs, (const long long*)(tab + L.screen), (int)g.screen.size(), c->d_pair_ij.as<int2>(),
+      c->npair, c->d_aoff.as<int>(), c->d_naos.as<int>(), c->nshell, B.dsh.as<double>(), B.dshf.as<float>(),
+      B.dmax.as<unsigned long long>());
+  CKR(cudaGetLastError());
+  return OK;
+}
+
+int gen_finalize(oqpg_ctx* c, BuildBufs& B, const GenJob& g, cudaStream_t st) {
+  const TabLayout L = tab_layout(g);
+  const unsigned char* tab = B.gtab.as<unsigned char>();
+  const long long n2 = (long long)c->nbf * c->nbf;
+  if (g.outs.empty()) return OK;
+  k_finalize_gen<<<grid_for(n2 * (long long)g.outs.size(), c->nsm), 256, 0, st>>>(
+      B.gj.as<double>(), B.gk.as<double>(), (size_t)c->nbf * c->stride, c->stride, c->nbf,
+      (const GenOut*)(tab + L.outs), (int)g.outs.size(), (const GenTerm*)(tab + L.terms), g.out_rs, g.out_cs,
+      B.flag.as<unsigned>());
+  CKR(cudaGetLastError());
+  return OK;
+}
+
+namespace {
+
+GenTerm term(double coef, int kind, int idx, int sign) {
+  GenTerm t;
+  t.coef = coef; t.kind = kind; t.idx = idx; t.sign = sign; t.pad = 0;
+  return t;
+}
+
+// int2_td_data_t recipe.  d2 (n, n, nvec) and apb / amb (n, n, nvec), Fortran
+// column-major; with the full sums J, K and D = d2(:, :, v):
+//   A+B (after the symmetrisation of parallel_stop): 4 sc J[D] - 2 se K[Ds]
+//   A-B:                                             -2 se K[Da]
+//   Tamm-Dancoff, into amb:                 2 sc J[D] (if Coulomb) - se K[D]
+void td_job(const oqpg_ctx* c, const double* d2, double* apb, double* amb, int nvec, int flags, double se,
+            double sc, GenJob& g) {
+  const long long n = c->nbf, nn = n * n;
+  const bool tda = flags & OQPG_TD_TDA;
+  const bool want_apb = !tda && (flags & OQPG_TD_APB), want_amb = !tda && (flags & OQPG_TD_AMB);
+  const bool need_j = want_apb || (tda && (flags & OQPG_TD_TDA_COULOMB));
+  const bool need_ks = want_apb || tda, need_ka = want_amb || tda;
+  g.in = d2;
+  g.in_rs = 1; g.in_cs = n;
+  g.out_rs = 1; g.out_cs = n;
+  const int nsym = need_ks ? nvec : 0;
+  for (int v = 0; v < nsym; ++v) g.slices.push_back(GenSlice{v * nn, +1, 0});
+  if (need_ka)
+    for (int v = 0; v < nvec; ++v) g.slices.push_back(GenSlice{v * nn, -1, 0});
+  g.nj = need_j ? nvec : 0;
+  g.k0 = 0;
+  g.nk = (int)g.slices.size();
+  for (int v = 0; v < nvec; ++v) g.screen.push_back(v * nn);
+  const int ka0 = nsym;
+  for (int v = 0; v < nvec; ++v) {
+    GenOut o{apb + v * nn, (int)g.terms.size(), 0};
+    if (want_apb) {
+      g.terms.push_back(term(4.0 * sc, 0, v, +1));
+      g.terms.push_back(term(-2.0 * se, 1, v, +1));
+    }
+    o.nterm = (int)g.terms.size() - o.term0;
+    g.outs.push_back(o);
+  }
+  for (int v = 0; v < nvec; ++v) {
+    GenOut o{amb + v * nn, (int)g.terms.size(), 0};
+    if (tda) {
+      if (need_j) g.terms.push_back(term(2.0 * sc, 0, v, +1));
+      g.terms.push_back(term(-se, 1, v, +1));
+      g.terms.push_back(term(-se, 1, ka0 + v, -1));
+    } else if (want_amb) {
+      g.terms.push_back(term(-2.0 * se, 1, ka0 + v, -1));
+    }
+    o.nterm = (int)g.terms.size() - o.term0;
+    g.outs.push_back(o);
+  }
+}
+
+// int2_mrsf_data_t (nmat 7) / int2_umrsf_data_t (nmat 11) recipe, pass 1.
+// d3 / f3 (nvec, nmat, n, n) Fortran column-major; with X = d3(v, m, :, :):
+//   MRSF:  m < 4: sc J[X] - se K[X];  m = 4..6: -se K[X]
+//   UMRSF: m < 8: sc J[X] - se K[X];  m = 8, 9: -se K[X^T];  m = 10: -se K[X]
+// Screening density: component nmat - 1 of every vector.
+void mrsf_job(const oqpg_ctx* c, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
+              GenJob& g) {
+  const long long n = c->nbf;
+  const bool um = nmat == 11;
+  const int ncoul = um ? 8 : 4;
+  g.in = d3;
+  g.in_rs = (long long)nmat * nvec; g.in_cs = n * nmat * nvec;
+  g.out_rs = g.in_rs; g.out_cs = g.in_cs;
+  auto base = [&](int m, int v) { return (long long)m * nvec + v; };
+  for (int m = 0; m < nmat; ++m)
+    for (int v = 0; v < nvec; ++v) g.slices.push_back(GenSlice{base(m, v), +1, 0});
+  for (int m = 0; m < nmat; ++m)
+    for (int v = 0; v < nvec; ++v) g.slices.push_back(GenSlice{base(m, v), -1, 0});
+  g.nj = ncoul * nvec;
+  g.k0 = 0;
+  g.nk = 2 * nmat * nvec;
+  for (int v = 0; v < nvec; ++v) g.screen.push_back(base(nmat - 1, v));
+  for (int m = 0; m < nmat; ++m)
+    for (int v = 0; v < nvec; ++v) {
+      const int s = m * nvec + v, a = nmat * nvec + s;
+      GenOut o{f3 + base(m, v), (int)g.terms.size(), 0};
+      if (m < ncoul) g.terms.push_back(term(sc, 0, s, +1));
+      const bool transposed = um && (m == 8 || m == 9);
+      g.terms.push_back(term(-se, 1, s, +1));
+      g.terms.push_back(term(transposed ? se : -se, 1, a, -1));
+      o.nterm = (int)g.terms.size() - o.term0;
+      g.outs.push_back(o);
+    }
+}
+
+int run_job(oqpg_ctx* c, const GenJob& g, cudaStream_t st) {
+  Job j;
+  j.gen = &g;
+  return ctx_build(c, j, st);
+}
+
+// host-buffer build: the input is copied to the context's d_dp, the job writes
+// its outputs into d_f (nout_buf consecutive blocks), which are copied back
+int host_job(oqpg_ctx* c, const double* in, size_t in_elems, double* const* host_out, const size_t* out_elems,
+             int nout_buf, const GenJob& g) {
+  cudaStream_t st = c->stream;
+  CKR(cudaMemcpyAsync(c->d_dp.p, in, sizeof(double) * in_elems, cudaMemcpyHostToDevice, st));
+  int rc = run_job(c, g, st);
+  if (rc) return rc;
+  size_t off = 0;
+  for (int b = 0; b < nout_buf; ++b) {
+    if (host_out[b])
+      CKR(cudaMemcpyAsync(host_out[b], c->d_f.as<double>() + off, sizeof(double) * out_elems[b],
+                          cudaMemcpyDeviceToHost, st));
+    off += out_elems[b];
+  }
+  CKR(cudaStreamSynchronize(st));
+  return OK;
+}
+
+bool td_args_ok(const oqpg_ctx* c, int nvec, int flags) {
+  return c && c->nmol == 1 && nvec >= 1 && (flags & ~(OQPG_TD_APB | OQPG_TD_AMB | OQPG_TD_TDA | OQPG_TD_TDA_COULOMB)) == 0;
+}
+
+}  // namespace
+}  // namespace oqpg
+
+using namespace oqpg;
+
+extern "C" {
+
+int oqpg_fock_td_device(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, int nvec, int flags, double se,
+                        double sc, void* stream) {
+  if (!td_args_ok(ctx, nvec, flags) || !d2 || !apb || !amb) return UNSUPPORTED;
+  GenJob g;
+  td_job(ctx, d2, apb, amb, nvec, flags, se, sc, g);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  int rc = run_job(ctx, g, st);
+  if (rc) return rc;
+  return cudaStreamSynchronize(st) == cudaSuccess ? OK : DEV_ERR;
+}
+
+int oqpg_fock_td(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, int nvec, int flags, double se,
+                 double sc) {
+  if (!td_args_ok(ctx, nvec, flags) || !d2) return UNSUPPORTED;
+  const size_t tot = (size_t)ctx->nbf * ctx->nbf * nvec;
+  if (ctx->d_dp.ensure(sizeof(double) * tot) != cudaSuccess) return NO_MEM;
+  if (ctx->d_f.ensure(sizeof(double) * 2 * tot) != cudaSuccess) return NO_MEM;
+  GenJob g;
+  td_job(ctx, ctx->d_dp.as<double>(), ctx->d_f.as<double>(), ctx->d_f.as<double>() + tot, nvec, flags, se, sc, g);
+  double* outs[2] = {apb, amb};
+  const size_t elems[2] = {tot, tot};
+  return host_job(ctx, d2, tot, outs, elems, 2, g);
+}
+
+int oqpg_fock_mrsf_device(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
+                          void* stream) {
+  if (!ctx || ctx->nmol != 1 || nvec < 1 || (nmat != 7 && nmat != 11) || !d3 || !f3) return UNSUPPORTED;
+  GenJob g;
+  mrsf_job(ctx, d3, f3, nvec, nmat, se, sc, g);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  int rc = run_job(ctx, g, st);
+  if (rc) return rc;
+  return cudaStreamSynchronize(st) == cudaSuccess ? OK : DEV_ERR;
+}
+
+int oqpg_fock_mrsf(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, double se, double sc) {
+  if (!ctx || ctx->nmol != 1 || nvec < 1 || (nmat != 7 && nmat != 11) || !d3) return UNSUPPORTED;
+  const size_t tot = (size_t)ctx->nbf * ctx->nbf * nmat * nvec;
+  if (ctx->d_dp.ensure(sizeof(double) * tot) != cudaSuccess) return NO_MEM;
+  if (ctx->d_f.ensure(sizeof(double) * tot) != cudaSuccess) return NO_MEM;
+  GenJob g;
+  mrsf_job(ctx, ctx->d_dp.as<double>(), ctx->d_f.as<double>(), nvec, nmat, se, sc, g);
+  double* outs[1] = {f3};
+  const size_t elems[1] = {tot};
+  return host_job(ctx, d3, tot, outs, elems, 1, g);
+}
+
+}  // extern "C"

@@ -125,6 +125,69 @@ class FockBuilder:
             raise FockError(rc, "oqpg_fock_jk_graph")
         return out
 
+    # ---- response-type builds (general square densities) ---------------------
+    def fock_td(self, x, apb=True, amb=False, tda=False, tda_coulomb=False, scale_exch=1.0, scale_coul=1.0):
+        """TDHF-type build of OpenQP's int2_td_data_t (tdhf_lib.F90:140-224).
+
+        x: (nvec, nbf, nbf) or (nbf, nbf) general square densities (host,
+        natural indexing x[v][r, c]).  Returns (apb, amb), each (nvec, nbf, nbf):
+          A+B: 4 sc J[X] - 2 se K[(X + X^T)/2]        (apb=True)
+          A-B: -2 se K[(X - X^T)/2]                    (amb=True)
+          TDA, into amb: 2 sc J[X] (tda_coulomb) - se K[X]
+        with J[X]_ij = sum (ij|kl) X_kl and K[X]_ik = sum (ij|kl) X_jl."""
+        x = np.asarray(x, dtype=np.float64)
+        squeeze = x.ndim == 2
+        x3 = x[None] if squeeze else x
+        nv, n = x3.shape[0], self.nbf
+        if x3.shape[1:] != (n, n):
+            raise ValueError("densities must be (nvec, %d, %d)" % (n, n))
+        fx = np.ascontiguousarray(x3.transpose(0, 2, 1))  # Fortran (nbf, nbf, nvec)
+        pa, ma = np.empty_like(fx), np.empty_like(fx)
+        rc = lib().oqpg_fock_td(self.h, ptr(fx), ptr(pa), ptr(ma), nv, td_flags(apb, amb, tda, tda_coulomb),
+                                float(scale_exch), float(scale_coul))
+        if rc != 0:
+            raise FockError(rc, "oqpg_fock_td")
+        pa, ma = pa.transpose(0, 2, 1), ma.transpose(0, 2, 1)
+        return (pa[0], ma[0]) if squeeze else (pa, ma)
+
+    def fock_td_device(self, x, apb=True, amb=False, tda=False, tda_coulomb=False, scale_exch=1.0,
+                       scale_coul=1.0, stream=None):
+        """fock_td on torch CUDA tensors: x (nvec, nbf, nbf) float64 -> (apb, amb)."""
+        import torch
+        if not (x.is_cuda and x.dtype == torch.float64):
+            raise ValueError("x must be a float64 CUDA tensor")
+        x3 = x if x.dim() == 3 else x.unsqueeze(0)
+        fx = x3.transpose(1, 2).contiguous()
+        pa, ma = torch.empty_like(fx), torch.empty_like(fx)
+        st = stream if stream is not None else torch.cuda.current_stream(x.device)
+        rc = lib().oqpg_fock_td_device(self.h, ctypes.c_void_p(fx.data_ptr()), ctypes.c_void_p(pa.data_ptr()),
+                                       ctypes.c_void_p(ma.data_ptr()), x3.shape[0],
+                                       td_flags(apb, amb, tda, tda_coulomb), float(scale_exch), float(scale_coul),
+                                       ctypes.c_void_p(st.cuda_stream))
+        if rc != 0:
+            raise FockError(rc, "oqpg_fock_td_device")
+        pa, ma = pa.transpose(1, 2), ma.transpose(1, 2)
+        return (pa[0], ma[0]) if x.dim() == 2 else (pa, ma)
+
+    def fock_mrsf(self, x, scale_exch=1.0, scale_coul=1.0):
+        """MRSF (nmat 7) / UMRSF (nmat 11) sigma-vector build of OpenQP's
+        int2_mrsf_data_t / int2_umrsf_data_t, first pass (tdhf_mrsf_lib.F90:218-426).
+
+        x: (nvec, nmat, nbf, nbf) host, natural indexing x[v, m][r, c].
+        Returns f of the same shape:
+          MRSF:  m < 4: sc J[X] - se K[X];  m >= 4: -se K[X]
+          UMRSF: m < 8: sc J[X] - se K[X];  m = 8, 9: -se K[X^T];  m = 10: -se K[X]."""
+        x = np.asarray(x, dtype=np.float64)
+        nv, nm, n = x.shape[0], x.shape[1], self.nbf
+        if x.shape[2:] != (n, n) or nm not in (7, 11):
+            raise ValueError("densities must be (nvec, 7 or 11, %d, %d)" % (n, n))
+        fx = np.ascontiguousarray(x.transpose(3, 2, 1, 0))  # Fortran (nvec, nmat, nbf, nbf)
+        out = np.empty_like(fx)
+        rc = lib().oqpg_fock_mrsf(self.h, ptr(fx), ptr(out), nv, nm, float(scale_exch), float(scale_coul))
+        if rc != 0:
+            raise FockError(rc, "oqpg_fock_mrsf")
+        return out.transpose(3, 2, 1, 0)
+
     def graph_info(self):
         c, r, k = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
         lib().oqpg_graph_info(self.h, ctypes.byref(c), ctypes.byref(r), ctypes.byref(k))
@@ -311,6 +374,37 @@ def routec_grad2(d, xyz, nbf, natom, hfscale=1.0, coulscale=1.0, de=None):
     lib().routec_grad2(ptr(d), ptr(x), ptr(de), ctypes.byref(n), ctypes.byref(na), ctypes.byref(hf), ctypes.byref(cs),
                        ctypes.byref(info))
     return de.reshape(-1, 3), info.value
+
+
+def td_flags(apb=True, amb=False, tda=False, tda_coulomb=False):
+    """OQPG_TD_* flags of the TD build (include/openqp_gb300.h)."""
+    return (1 if apb else 0) | (2 if amb else 0) | (4 if tda else 0) | (8 if tda_coulomb else 0)
+
+
+def routec_fock_td(d2, nbf, nvec, flags, se=1.0, sc=1.0):
+    """Calls routec_fock_td as a Fortran caller would: d2 the Fortran-ordered
+    (nbf, nbf, nvec) array as a flat buffer.  Returns (apb, amb, info), flat."""
+    d2 = np.ascontiguousarray(d2, dtype=np.float64).reshape(-1)
+    apb, amb = np.zeros_like(d2), np.zeros_like(d2)
+    n, nv, fl = ctypes.c_int(nbf), ctypes.c_int(nvec), ctypes.c_int(flags)
+    se_, sc_ = ctypes.c_double(se), ctypes.c_double(sc)
+    info = ctypes.c_int(1)
+    lib().routec_fock_td(ptr(d2), ptr(apb), ptr(amb), ctypes.byref(n), ctypes.byref(nv), ctypes.byref(fl),
+                         ctypes.byref(se_), ctypes.byref(sc_), ctypes.byref(info))
+    return apb, amb, info.value
+
+
+def routec_fock_mrsf(d3, nbf, nvec, nmat, se=1.0, sc=1.0):
+    """Calls routec_fock_mrsf with the Fortran-ordered (nvec, nmat, nbf, nbf)
+    array as a flat buffer.  Returns (f3, info), flat."""
+    d3 = np.ascontiguousarray(d3, dtype=np.float64).reshape(-1)
+    f3 = np.zeros_like(d3)
+    n, nv, nm = ctypes.c_int(nbf), ctypes.c_int(nvec), ctypes.c_int(nmat)
+    se_, sc_ = ctypes.c_double(se), ctypes.c_double(sc)
+    info = ctypes.c_int(1)
+    lib().routec_fock_mrsf(ptr(d3), ptr(f3), ctypes.byref(n), ctypes.byref(nv), ctypes.byref(nm),
+                           ctypes.byref(se_), ctypes.byref(sc_), ctypes.byref(info))
+    return f3, info.value
 
 
 def routec_finalize():

@@ -50,6 +50,10 @@ def lib():
         L.orc_grad2e.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                  ctypes.c_int, ctypes.c_int, ctypes.c_int, _d]
         L.orc_grad1e.argtypes = [ctypes.c_void_p, _d, _d, _d, _d]
+        L.orc_fock_td.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                  ctypes.c_double, ctypes.c_int]
+        L.orc_fock_mrsf.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -110,6 +114,26 @@ class Oracle:
                                  int(stride), int(offset), _p(st))
         return f, dict(t_init=st[0], t_schwarz=st[1], t_twoei=st[2], t_total=st[3], quartets=int(st[4]),
                        screened=int(st[5]), prim_quartets=int(st[6]), stored=int(st[7]))
+
+    def fock_td(self, x, flags, se=1.0, sc=1.0, nthreads=None):
+        """int2_td_data_t build: x (nvec, nbf, nbf) natural indexing -> (apb, amb)
+        in the same indexing (flags: 1 A+B, 2 A-B, 4 TDA, 8 TDA Coulomb)."""
+        x = np.asarray(x, dtype=np.float64)
+        fx = np.ascontiguousarray(x.transpose(0, 2, 1))
+        pa, ma = np.zeros_like(fx), np.zeros_like(fx)
+        lib().orc_fock_td(self.h, _p(fx), _p(pa), _p(ma), fx.shape[0], int(flags), se, sc, nthreads or os.cpu_count())
+        return pa.transpose(0, 2, 1), ma.transpose(0, 2, 1)
+
+    def fock_mrsf(self, x, se=1.0, sc=1.0, nthreads=None):
+        """int2_mrsf_data_t (nmat 7) / int2_umrsf_data_t (nmat 11) first pass:
+        x (nvec, nmat, nbf, nbf) natural indexing -> f3 in the same indexing."""
+        x = np.asarray(x, dtype=np.float64)
+        fx = np.ascontiguousarray(x.transpose(3, 2, 1, 0))
+        out = np.zeros_like(fx)
+        rc = lib().orc_fock_mrsf(self.h, _p(fx), _p(out), x.shape[0], x.shape[1], se, sc, nthreads or os.cpu_count())
+        if rc:
+            raise ValueError("nmat must be 7 or 11")
+        return out.transpose(3, 2, 1, 0)
 
     def schwarz(self, nthreads=None):
         ns = len(self.bas.am)

@@ -1,7 +1,8 @@
 // Oracle (test infrastructure only): the Fock-build driver of the CPU
 // restatement -- Schwarz bounds, shell density, the OpenMP quartet loop,
-// storeints and the RHF/UROHF digestion -- and the C entry points the tests
-// and the CPU-baseline leg of bench.py call through ctypes.
+// storeints, the RHF/UROHF digestion and the response (TDHF, MRSF, UMRSF)
+// digestions -- and the C entry points the tests and the CPU-baseline leg of
+// bench.py call through ctypes.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -159,8 +160,10 @@ static void update(Store& st, const double* d, double* f, int nfocks, size_t ntr
 }
 
 // int2_compute_data_t_storeints (int2.F90:1741-1865)
-static long storeints(const Basis& B, const int ids[4], const double* blk, double cutoff, Store& st, const double* d,
-                      double* f, int nfocks, size_t ntri, bool urohf, double se, double sc) {
+// flush(st) digests the buffered elements and empties the buffer (the
+// reference's update call when the 50 000-element buffer is full).
+template <class Flush>
+static long storeints(const Basis& B, const int ids[4], const double* blk, double cutoff, Store& st, Flush& flush) {
   const int n1 = B.sh[ids[0]].nao, n2 = B.sh[ids[1]].nao, n3 = B.sh[ids[2]].nao, n4 = B.sh[ids[3]].nao;
   const bool same = ids[0] == ids[2] && ids[1] == ids[3];
   const bool iandj = ids[0] == ids[1];
@@ -201,12 +204,72 @@ static long storeints(const Basis& B, const int ids[4], const double* blk, doubl
           int* p = &st.ids[4 * (size_t)st.n];
           p[0] = ii; p[1] = jj; p[2] = kk; p[3] = ll;
           st.val[st.n++] = val;
-          if (st.n == (int)st.val.size()) update(st, d, f, nfocks, ntri, urohf, se, sc);
+          if (st.n == (int)st.val.size()) flush(st);
         }
       }
     }
   }
   return nint;
+}
+
+struct TwoeiCounts {
+  long long nq = 0, nsk = 0, npq = 0, nst = 0;
+};
+
+// int2_twoei (int2.F90:589-923): the OpenMP loop over the cost-sorted bra
+// pairs with the pair screen Q_ij max_den < tau and the quartet screen
+// Q_ij Q_kl max(4 Dsh_ij, 4 Dsh_kl, Dsh_jl, Dsh_jk, Dsh_il, Dsh_ik) < tau
+// (int2.F90:963-986); every surviving quartet is evaluated and stored, and
+// make(tid) gives the digestion of thread tid (the data type's update).
+// stride/offset > 1 keep only the bra pairs p with p mod stride == offset.
+template <class MakeFlush>
+static TwoeiCounts twoei(const Basis& B, const PairStore& PS, const Cutoffs& cutoffs, double cut,
+                         const std::vector<double>& Q, const std::vector<double>& dsh, int nthreads, int stride,
+                         int offset, MakeFlush&& make) {
+  double max_den = 0;
+  for (double v : dsh) max_den = std::max(max_den, std::fabs(v));
+  std::vector<int> pi, pj;
+  pair_map(B, Q, pi, pj);
+  const int ns = B.nshell;
+  const int np = ns * (ns + 1) / 2;
+  long long nq = 0, nsk = 0, npq = 0, nst = 0;
+#pragma omp parallel num_threads(nthreads) reduction(+ : nq, nsk, npq, nst)
+  {
+    const int tid = omp_get_thread_num();
+    auto flush = make(tid);
+    QuartetWork W;
+    std::vector<double> blk(6 * 6 * 6 * 6);
+    Store st(50000);
+#pragma omp for schedule(dynamic, 1)
+    for (int p = 0; p < np; ++p) {
+      if (stride > 1 && p % stride != offset) continue;
+      const int i = pi[p], j = pj[p];
+      const double qij = Q[(size_t)i * ns + j];
+      if (qij * max_den < cut) { nsk += (long long)(i + 1) * i / 2 + j + 1; continue; }
+      for (int k = 0; k <= i; ++k) {
+        const int jork = (k == i) ? j : k;
+        for (int l = 0; l <= jork; ++l) {
+          double test = qij * Q[(size_t)k * ns + l];
+          const double* D = dsh.data();
+          test *= std::max({4 * D[(size_t)i * ns + j], 4 * D[(size_t)k * ns + l], D[(size_t)j * ns + l],
+                            D[(size_t)j * ns + k], D[(size_t)i * ns + l], D[(size_t)i * ns + k]});
+          if (test < cut) { ++nsk; continue; }
+          ++nq;
+          const int ids0[4] = {i, j, k, l};
+          int s[4], fl[4];
+          flip_quartet(B, ids0, s, fl);
+          const long pq = rys_quartet(B, PS, cutoffs, s, blk.data(), W);
+          if (pq == 0) continue;
+          npq += pq;
+          nst += storeints(B, s, blk.data(), cut, st, flush);
+        }
+      }
+    }
+    flush(st);
+  }
+  TwoeiCounts c;
+  c.nq = nq; c.nsk = nsk; c.npq = npq; c.nst = nst;
+  return c;
 }
 
 static double now() {
@@ -232,50 +295,13 @@ static int fock_jk(OrcHandle* H, const double* d, double* fout, int nfocks, doub
   const double t2 = now();
   std::vector<double> dsh;
   shlden(B, d, nfocks, dsh);
-  double max_den = 0;
-  for (double v : dsh) max_den = std::max(max_den, std::fabs(v));
-  std::vector<int> pi, pj;
-  pair_map(B, Q, pi, pj);
-  const int ns = B.nshell;
-  const int np = ns * (ns + 1) / 2;
   const size_t ntri = (size_t)B.nbf * (B.nbf + 1) / 2;
   const int nf = urohf ? 2 : nfocks;
   std::vector<double> facc((size_t)nthreads * nf * ntri, 0.0);
-  long long nq = 0, nsk = 0, npq = 0, nst = 0;
-#pragma omp parallel num_threads(nthreads) reduction(+ : nq, nsk, npq, nst)
-  {
-    const int tid = omp_get_thread_num();
+  const TwoeiCounts cnt = twoei(B, PS, cutoffs, cut, Q, dsh, nthreads, stride, offset, [&](int tid) {
     double* f = facc.data() + (size_t)tid * nf * ntri;
-    QuartetWork W;
-    std::vector<double> blk(6 * 6 * 6 * 6);
-    Store st(50000);
-#pragma omp for schedule(dynamic, 1)
-    for (int p = 0; p < np; ++p) {
-      if (stride > 1 && p % stride != offset) continue;
-      const int i = pi[p], j = pj[p];
-      const double qij = Q[(size_t)i * ns + j];
-      if (qij * max_den < cut) { nsk += (long long)(i + 1) * i / 2 + j + 1; continue; }
-      for (int k = 0; k <= i; ++k) {
-        const int jork = (k == i) ? j : k;
-        for (int l = 0; l <= jork; ++l) {
-          double test = qij * Q[(size_t)k * ns + l];
-          const double* D = dsh.data();
-          test *= std::max({4 * D[(size_t)i * ns + j], 4 * D[(size_t)k * ns + l], D[(size_t)j * ns + l],
-                            D[(size_t)j * ns + k], D[(size_t)i * ns + l], D[(size_t)i * ns + k]});
-          if (test < cut) { ++nsk; continue; }
-          ++nq;
-          const int ids0[4] = {i, j, k, l};
-          int s[4], fl[4];
-          flip_quartet(B, ids0, s, fl);
-          const long pq = rys_quartet(B, PS, cutoffs, s, blk.data(), W);
-          if (pq == 0) continue;
-          npq += pq;
-          nst += storeints(B, s, blk.data(), cut, st, d, f, nfocks, ntri, urohf, se, sc);
-        }
-      }
-    }
-    update(st, d, f, nfocks, ntri, urohf, se, sc);
-  }
+    return [=](Store& st) { update(st, d, f, nfocks, ntri, urohf, se, sc); };
+  });
   // parallel_stop: reduce the replicated copies
   for (int t = 1; t < nthreads; ++t)
     for (size_t e = 0; e < (size_t)nf * ntri; ++e) facc[e] += facc[(size_t)t * nf * ntri + e];
@@ -288,8 +314,236 @@ static int fock_jk(OrcHandle* H, const double* d, double* fout, int nfocks, doub
   const double t3 = now();
   if (stats) {
     stats->t_init = t1 - t0; stats->t_schwarz = t2 - t1; stats->t_twoei = t3 - t2; stats->t_total = t3 - t0;
-    stats->quartets = nq; stats->screened = nsk; stats->prim_quartets = npq; stats->stored = nst;
+    stats->quartets = cnt.nq; stats->screened = cnt.nsk; stats->prim_quartets = cnt.npq; stats->stored = cnt.nst;
   }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Response-type consumers of the same quartet loop (int2_td_data_t,
+// int2_mrsf_data_t, int2_umrsf_data_t): general square densities, one digestion
+// per data type.  Matrices are Fortran column-major; M(r, c) of an (n, n)
+// matrix is m[c * n + r].
+
+// shltd (tdhf_lib.F90:300-325) and shell_den_screen_mrsf
+// (tdhf_mrsf_lib.F90:189-214): for shells ish >= jsh, the maximum of |X(r, c)|
+// over r in jsh, c in ish (that one orientation of the block) and over the
+// matrices q at x + q mstep; element (r, c) of a matrix is at r rstep + c cstep.
+static void shell_den_general(const Basis& B, const double* x, int nmat, size_t mstep, size_t rstep, size_t cstep,
+                              std::vector<double>& dsh) {
+  const int ns = B.nshell;
+  dsh.assign((size_t)ns * ns, 0.0);
+  for (int si = 0; si < ns; ++si) {
+    const int mini = B.sh[si].aoff, maxi = mini + B.sh[si].nao;
+    for (int sj = 0; sj <= si; ++sj) {
+      const int minj = B.sh[sj].aoff, maxj = minj + B.sh[sj].nao;
+      double m = 0;
+      for (int q = 0; q < nmat; ++q)
+        for (int c = mini; c < maxi; ++c)
+          for (int r = minj; r < maxj; ++r) m = std::max(m, std::fabs(x[q * mstep + r * rstep + c * cstep]));
+      dsh[(size_t)si * ns + sj] = m;
+      dsh[(size_t)sj * ns + si] = m;
+    }
+  }
+}
+
+enum { TD_APB = 1, TD_AMB = 2, TD_TDA = 4, TD_TDA_COUL = 8 };
+
+// int2_td_data_t_update (tdhf_lib.F90:140-224)
+static void td_update(Store& st, const double* d2, double* apb, double* amb, int n, int nvec, int flags,
+                      double se, double sc) {
+  const size_t n2 = (size_t)n * n;
+  const double xval1 = se, cval2 = 2 * sc, cval4 = 4 * sc;
+  for (int v = 0; v < nvec; ++v) {
+    const double* d = d2 + v * n2;
+    double* P = apb + v * n2;
+    double* M = amb + v * n2;
+    auto D = [&](int r, int c) { return d[(size_t)c * n + r]; };
+    auto A = [&](double* m, int r, int c) -> double& { return m[(size_t)c * n + r]; };
+    for (int e = 0; e < st.n; ++e) {
+      const int i = st.ids[4 * e], j = st.ids[4 * e + 1], k = st.ids[4 * e + 2], l = st.ids[4 * e + 3];
+      const double val = st.val[e];
+      if (flags & TD_TDA) {
+        const double val1 = val * xval1, val2c = val * cval2;
+        A(M, i, k) -= val1 * D(j, l);
+        A(M, k, i) -= val1 * D(l, j);
+        A(M, i, l) -= val1 * D(j, k);
+        A(M, l, i) -= val1 * D(k, j);
+        A(M, j, k) -= val1 * D(i, l);
+        A(M, k, j) -= val1 * D(l, i);
+        A(M, j, l) -= val1 * D(i, k);
+        A(M, l, j) -= val1 * D(k, i);
+        if (flags & TD_TDA_COUL) {
+          A(M, i, j) += val2c * (D(k, l) + D(l, k));
+          A(M, j, i) += val2c * (D(k, l) + D(l, k));
+          A(M, k, l) += val2c * (D(i, j) + D(j, i));
+          A(M, l, k) += val2c * (D(i, j) + D(j, i));
+        }
+      } else {
+        const double val1 = val * xval1, val4c = val * cval4;
+        if (flags & TD_APB) {
+          A(P, i, j) += val4c * (D(k, l) + D(l, k));
+          A(P, k, l) += val4c * (D(i, j) + D(j, i));
+          A(P, i, k) -= val1 * (D(j, l) + D(l, j));
+          A(P, i, l) -= val1 * (D(j, k) + D(k, j));
+          A(P, j, k) -= val1 * (D(i, l) + D(l, i));
+          A(P, j, l) -= val1 * (D(i, k) + D(k, i));
+        }
+        if (flags & TD_AMB) {
+          A(M, i, k) += val1 * (D(l, j) - D(j, l));
+          A(M, i, l) += val1 * (D(k, j) - D(j, k));
+          A(M, j, k) += val1 * (D(l, i) - D(i, l));
+          A(M, j, l) += val1 * (D(k, i) - D(i, k));
+          A(M, k, i) -= val1 * (D(l, j) - D(j, l));
+          A(M, l, i) -= val1 * (D(k, j) - D(j, k));
+          A(M, k, j) -= val1 * (D(l, i) - D(i, l));
+          A(M, l, j) -= val1 * (D(k, i) - D(i, k));
+        }
+      }
+    }
+  }
+  st.n = 0;
+}
+
+// int2_mrsf_data_t_update (tdhf_mrsf_lib.F90:218-333, the FP64 pass-1 branch)
+// and int2_umrsf_data_t_update (tdhf_mrsf_lib.F90:337-426, pass 1).
+// d3 / f3 are (nvec, nmat, n, n): element (v, c, r, col) at ((col n + r) nmat + c) nvec + v.
+static void mrsf_update(Store& st, const double* d3, const double* ds, double* f3, int n, int nvec, int nmat,
+                        bool umrsf, double se, double sc) {
+  auto at = [&](int v, int c, int r, int col) { return (((size_t)col * n + r) * nmat + c) * nvec + v; };
+  for (int e = 0; e < st.n; ++e) {
+    const int i = st.ids[4 * e], j = st.ids[4 * e + 1], k = st.ids[4 * e + 2], l = st.ids[4 * e + 3];
+    const double val = st.val[e];
+    const double xval = val * se, cval = val * sc;
+    auto K8 = [&](int c, int v) {
+      f3[at(v, c, i, k)] -= xval * d3[at(v, c, j, l)];
+      f3[at(v, c, k, i)] -= xval * d3[at(v, c, l, j)];
+      f3[at(v, c, i, l)] -= xval * d3[at(v, c, j, k)];
+      f3[at(v, c, l, i)] -= xval * d3[at(v, c, k, j)];
+      f3[at(v, c, j, k)] -= xval * d3[at(v, c, i, l)];
+      f3[at(v, c, k, j)] -= xval * d3[at(v, c, l, i)];
+      f3[at(v, c, j, l)] -= xval * d3[at(v, c, i, k)];
+      f3[at(v, c, l, j)] -= xval * d3[at(v, c, k, i)];
+    };
+    if (!umrsf) {
+      for (int c = 0; c < 4; ++c)
+        for (int v = 0; v < nvec; ++v) {
+          const size_t dkl = (((size_t)l * n + k) * 4 + c) * nvec + v, dij = (((size_t)j * n + i) * 4 + c) * nvec + v;
+          f3[at(v, c, i, j)] += cval * ds[dkl];
+          f3[at(v, c, j, i)] += cval * ds[dkl];
+          f3[at(v, c, k, l)] += cval * ds[dij];
+          f3[at(v, c, l, k)] += cval * ds[dij];
+        }
+      for (int c = 0; c < 7; ++c)
+        for (int v = 0; v < nvec; ++v) K8(c, v);
+    } else {
+      for (int c = 0; c < 8; ++c)
+        for (int v = 0; v < nvec; ++v) {
+          f3[at(v, c, i, j)] += cval * d3[at(v, c, k, l)];
+          f3[at(v, c, k, l)] += cval * d3[at(v, c, i, j)];
+          f3[at(v, c, i, j)] += cval * d3[at(v, c, l, k)];
+          f3[at(v, c, l, k)] += cval * d3[at(v, c, i, j)];
+          f3[at(v, c, j, i)] += cval * d3[at(v, c, k, l)];
+          f3[at(v, c, k, l)] += cval * d3[at(v, c, j, i)];
+          f3[at(v, c, j, i)] += cval * d3[at(v, c, l, k)];
+          f3[at(v, c, l, k)] += cval * d3[at(v, c, j, i)];
+          K8(c, v);
+        }
+      for (int c = 8; c < 10; ++c)
+        for (int v = 0; v < nvec; ++v) {
+          f3[at(v, c, i, l)] -= xval * d3[at(v, c, k, j)];
+          f3[at(v, c, l, i)] -= xval * d3[at(v, c, j, k)];
+          f3[at(v, c, k, j)] -= xval * d3[at(v, c, i, l)];
+          f3[at(v, c, j, k)] -= xval * d3[at(v, c, l, i)];
+          f3[at(v, c, i, k)] -= xval * d3[at(v, c, l, j)];
+          f3[at(v, c, k, i)] -= xval * d3[at(v, c, j, l)];
+          f3[at(v, c, l, j)] -= xval * d3[at(v, c, i, k)];
+          f3[at(v, c, j, l)] -= xval * d3[at(v, c, k, i)];
+        }
+      for (int v = 0; v < nvec; ++v) K8(10, v);
+    }
+  }
+  st.n = 0;
+}
+
+struct Prepared {
+  PairStore PS;
+  Cutoffs cutoffs;
+  std::vector<double> Q;
+};
+
+static void prepare(OrcHandle* H, int nthreads, Prepared& P) {
+  const double cut = H->cutoff;
+  P.cutoffs = Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0));
+  P.PS.build(H->B, P.cutoffs);
+  schwarz(H->B, P.Q, nthreads);
+}
+
+// TDHF-type build: d2 (n, n, nvec) -> apb, amb (n, n, nvec), both overwritten;
+// int2_td_data_t_parallel_start/stop (tdhf_lib.F90:59-111): the replicated
+// copies are summed and every apb matrix symmetrised (mathlib.F90:134-143).
+static int fock_td(OrcHandle* H, const double* d2, double* apb, double* amb, int nvec, int flags, double se,
+                   double sc, int nthreads) {
+  const Basis& B = H->B;
+  const int n = B.nbf;
+  const size_t n2 = (size_t)n * n, tot = n2 * nvec;
+  Prepared P;
+  prepare(H, nthreads, P);
+  std::vector<double> dsh;
+  shell_den_general(B, d2, nvec, n2, 1, n, dsh);
+  std::vector<double> acc((size_t)nthreads * 2 * tot, 0.0);
+  twoei(B, P.PS, P.cutoffs, H->cutoff, P.Q, dsh, nthreads, 1, 0, [&](int tid) {
+    double* a = acc.data() + (size_t)tid * 2 * tot;
+    return [=](Store& st) { td_update(st, d2, a, a + tot, n, nvec, flags, se, sc); };
+  });
+  for (int t = 1; t < nthreads; ++t)
+    for (size_t e = 0; e < 2 * tot; ++e) acc[e] += acc[(size_t)t * 2 * tot + e];
+  for (int v = 0; v < nvec; ++v) {
+    double* a = acc.data() + v * n2;
+    for (int i = 0; i < n; ++i) {
+      for (int r = i; r < n; ++r) a[(size_t)i * n + r] += a[(size_t)r * n + i];
+      for (int r = 0; r < i; ++r) a[(size_t)i * n + r] = a[(size_t)r * n + i];
+    }
+  }
+  std::memcpy(apb, acc.data(), sizeof(double) * tot);
+  std::memcpy(amb, acc.data() + tot, sizeof(double) * tot);
+  return 0;
+}
+
+// MRSF (nmat = 7) / UMRSF (nmat = 11) response build: d3 -> f3 (overwritten),
+// int2_mrsf_data_t_parallel_start/stop (tdhf_mrsf_lib.F90:58-149); the
+// screening density is the last component (tdhf_mrsf_lib.F90:171-185).
+static int fock_mrsf(OrcHandle* H, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
+                     int nthreads) {
+  const Basis& B = H->B;
+  const int n = B.nbf;
+  const bool umrsf = nmat == 11;
+  if (nmat != 7 && nmat != 11) return 3;
+  const size_t tot = (size_t)n * n * nmat * nvec;
+  Prepared P;
+  prepare(H, nthreads, P);
+  std::vector<double> dsh;
+  shell_den_general(B, d3 + (size_t)(nmat - 1) * nvec, nvec, 1, (size_t)nmat * nvec, (size_t)n * nmat * nvec, dsh);
+  // symmetrised Coulomb components ds(v, c, r, col) = d3(v, c, r, col) + d3(v, c, col, r), c < 4
+  std::vector<double> ds;
+  if (!umrsf) {
+    ds.assign((size_t)n * n * 4 * nvec, 0.0);
+    for (int col = 0; col < n; ++col)
+      for (int r = 0; r < n; ++r)
+        for (int c = 0; c < 4; ++c)
+          for (int v = 0; v < nvec; ++v)
+            ds[(((size_t)col * n + r) * 4 + c) * nvec + v] =
+                d3[(((size_t)col * n + r) * nmat + c) * nvec + v] + d3[(((size_t)r * n + col) * nmat + c) * nvec + v];
+  }
+  std::vector<double> acc((size_t)nthreads * tot, 0.0);
+  const double* dsp = ds.data();
+  twoei(B, P.PS, P.cutoffs, H->cutoff, P.Q, dsh, nthreads, 1, 0, [&](int tid) {
+    double* a = acc.data() + (size_t)tid * tot;
+    return [=](Store& st) { mrsf_update(st, d3, dsp, a, n, nvec, nmat, umrsf, se, sc); };
+  });
+  for (int t = 1; t < nthreads; ++t)
+    for (size_t e = 0; e < tot; ++e) acc[e] += acc[(size_t)t * tot + e];
+  std::memcpy(f3, acc.data(), sizeof(double) * tot);
   return 0;
 }
 
@@ -348,6 +602,16 @@ int orc_fock_jk_sample(void* h, const double* d, double* f, int nfocks, double s
     stats6[7] = (double)st.stored;
   }
   return rc;
+}
+
+// flags: 1 A+B, 2 A-B, 4 Tamm-Dancoff, 8 Tamm-Dancoff with Coulomb terms.
+int orc_fock_td(void* h, const double* d2, double* apb, double* amb, int nvec, int flags, double se, double sc,
+                int nthreads) {
+  return fock_td((OrcHandle*)h, d2, apb, amb, nvec, flags, se, sc, nthreads);
+}
+
+int orc_fock_mrsf(void* h, const double* d3, double* f3, int nvec, int nmat, double se, double sc, int nthreads) {
+  return fock_mrsf((OrcHandle*)h, d3, f3, nvec, nmat, se, sc, nthreads);
 }
 
 void orc_schwarz(void* h, double* q, int nthreads) {

@@ -1,9 +1,9 @@
 """Extract OpenQP's own HF golden results into a small fixture.
 
 Reads the example inputs/outputs that OpenQP's ``--validate_examples`` checks
-(``examples/HF/*.json``, ``examples/NMR/*.json``): atoms, coordinates (Bohr,
-as stored in the JSON) and the reference total energy (and gradient where
-present).  Run once where the OpenQP checkout exists; the fixture is committed.
+(``examples/HF/*.json``, ``examples/NMR/*.json``, ``examples/TDHF/*.json``):
+atoms, coordinates (Bohr, as stored in the JSON) and the reference total
+energy (and gradient, and TDHF excitation energies, where present).  Run once where the OpenQP checkout exists; the fixture is committed.
 
 Usage: python make_golden.py <openqp checkout> > hf_golden.json
 """
@@ -21,6 +21,7 @@ CASES = [
     ("examples/NMR/H2O_RHF-NMR.json", "sto-3g", "rhf", 1),
     ("examples/NMR/CH3_UHF-GIAO-NMR.json", "sto-3g", "uhf", 2),
     ("examples/NMR/CH3_ROHF-GIAO-NMR.json", "sto-3g", "rohf", 2),
+    ("examples/TDHF/H2O_TDHF_ENERGY.json", "6-31g*", "rhf", 1),
 ]
 
 
@@ -33,6 +34,8 @@ def main(root):
                 "coord_bohr": d["coord"], "energy": d["energy"]}
         if "grad" in d:
             case["grad"] = d["grad"]
+        if d.get("td_energies") and any(d["td_energies"]):
+            case["td_energies"] = d["td_energies"]
         out.append(case)
     json.dump({"cases": out}, sys.stdout, indent=1)
 

@@ -7,7 +7,11 @@ Pins, in order of strength:
   * J/K semantics of the restated storeints + digestion + scaling against a
     dense ERI contraction;
   * Rys ERIs against an independent McMurchie-Davidson code;
-  * the Rys tables against 60-digit values.
+  * the Rys tables against 60-digit values;
+  * the response digestions (int2_td_data_t, int2_mrsf_data_t,
+    int2_umrsf_data_t) against dense J/K contractions of general matrices,
+    and OpenQP's golden TDHF excitation energies (examples/TDHF) from full
+    A+B / A-B matrices built with the restated int2_td_data_t.
 """
 import json
 import os
@@ -75,7 +79,8 @@ def test_one_electron_two_implementations_agree(oracle_lib):
         assert np.abs(o.one_electron("V") - onee.nuclear(bas)).max() < 1e-12
 
 
-@pytest.mark.parametrize("case", [c for c in GOLD if "GRADIENT" not in c["source"]], ids=lambda c: c["source"].split("/")[-1])
+@pytest.mark.parametrize("case", [c for c in GOLD if "GRADIENT" not in c["source"] and "TDHF" not in c["source"]],
+                         ids=lambda c: c["source"].split("/")[-1])
 def test_golden_hf_energy(oracle_lib, case):
     """OpenQP's own example energies; their CI gate is 4 decimals, we ask 1e-7."""
     from openqp_gb300 import onee, scf
@@ -156,3 +161,79 @@ def test_grad2e_matches_finite_difference_of_e2(oracle_lib):
         xm[at, x] -= h
         fd = (e2(xp) - e2(xm)) / (2 * h)
         assert abs(fd - g[at, x]) < 2e-7, (at, x, fd, g[at, x])
+
+
+def _dense_jk(o, n):
+    eri = o.eri_dense().reshape(n, n, n, n)
+    return (lambda D: np.einsum("ijkl,kl->ij", eri, D)), (lambda D: np.einsum("ijkl,jl->ik", eri, D))
+
+
+@pytest.mark.parametrize("flags", [1, 2, 3, 4, 12])
+def test_td_digestion_matches_dense_contraction(oracle_lib, flags):
+    """int2_td_data_t update + parallel_stop on general matrices X equals
+    A+B = 4 sc J[X] - 2 se K[Xs], A-B = -2 se K[Xa], TDA = 2 sc J[X] - se K[X]."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(1, workloads.cube_edge_like_c1(1), seed=3, basis="6-31g(d)")
+    o = oracle_lib.Oracle(bas, cutoff=1e-12)
+    n = o.nbf
+    J, K = _dense_jk(o, n)
+    x = np.random.default_rng(flags).standard_normal((3, n, n)) * 0.3
+    se, sc = 0.7, 1.3
+    pa, ma = o.fock_td(x, flags, se, sc)
+    for v in range(3):
+        D = x[v]
+        Ds, Da = 0.5 * (D + D.T), 0.5 * (D - D.T)
+        ep = np.zeros((n, n))
+        em = np.zeros((n, n))
+        if flags & 4:
+            em = -se * K(D) + (2 * sc * J(D) if flags & 8 else 0)
+        else:
+            if flags & 1:
+                ep = 4 * sc * J(D) - 2 * se * K(Ds)
+            if flags & 2:
+                em = -2 * se * K(Da)
+        assert np.abs(pa[v] - ep).max() < 1e-12
+        assert np.abs(ma[v] - em).max() < 1e-12
+
+
+@pytest.mark.parametrize("nmat", [7, 11])
+def test_mrsf_digestion_matches_dense_contraction(oracle_lib, nmat):
+    """int2_mrsf_data_t (7) / int2_umrsf_data_t (11) pass 1 equals
+    sc J[X] - se K[X] on the Coulomb components, -se K[X] (UMRSF 8, 9: K[X^T])
+    on the others."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(1, workloads.cube_edge_like_c1(1), seed=5, basis="6-31g(d)")
+    o = oracle_lib.Oracle(bas, cutoff=1e-12)
+    n = o.nbf
+    J, K = _dense_jk(o, n)
+    x = np.random.default_rng(nmat).standard_normal((2, nmat, n, n)) * 0.3
+    se, sc = 0.6, 1.2
+    f = o.fock_mrsf(x, se, sc)
+    ncoul = 4 if nmat == 7 else 8
+    for v in range(2):
+        for m in range(nmat):
+            D = x[v, m]
+            ref = -se * K(D.T if (nmat == 11 and m in (8, 9)) else D)
+            if m < ncoul:
+                ref = ref + sc * J(D)
+            assert np.abs(f[v, m] - ref).max() < 1e-12
+
+
+def test_golden_tdhf_excitation_energies(oracle_lib):
+    """OpenQP's examples/TDHF/H2O_TDHF_ENERGY: RHF energy and the three RPA
+    singlet excitation energies (their Davidson converges them to ~1e-7)."""
+    import rpa
+    from openqp_gb300 import onee, scf
+    from openqp_gb300.basis import build_basis
+    case = [c for c in GOLD if "TDHF" in c["source"]][0]
+    bas = build_basis(case["atoms"], np.array(case["coord_bohr"]).reshape(-1, 3), case["basis"])
+    o = oracle_lib.Oracle(bas, cutoff=1e-10)
+    S, T = onee.overlap_kinetic(bas)
+    H = T + onee.nuclear(bas)
+    r = scf.run_scf(o.nbf, S, H, onee.nuclear_repulsion(bas), 5, 5, lambda d: o.fock_jk(d), conv=1e-12,
+                    dconv=1e-10)
+    assert abs(r["energy"] - case["energy"]) < 1e-7
+    e, C = rpa.canonical_orbitals(S, r["Fock"][0])
+    w, apb, amb = rpa.rpa_energies(lambda x, fl: o.fock_td(x, fl), C, e, 5)
+    assert np.abs(apb - apb.T).max() < 1e-12 and np.abs(amb - amb.T).max() < 1e-12
+    assert np.abs(w[:3] - np.array(case["td_energies"])).max() < 5e-7
