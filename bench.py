@@ -60,6 +60,11 @@ WORKLOADS = {
     # the differentiation configuration: two-electron gradient of (H2O)16 6-31G(d)
     "grad_water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian RHF two-electron gradient (grd2)", nwater=16,
                                edge=9.52, seed=0, basis="6-31g(d)", cutoff=1e-10, grad=True),
+    # response-type (TDHF A+B and A-B) builds: 8 trial transition densities per build
+    "td_water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian TDHF A+B and A-B build, 8 trial vectors", nwater=16,
+                             edge=9.52, seed=0, basis="6-31g(d)", cutoff=1e-10, td=True, nvec=8),
+    "td_water32_ccpvdz": dict(name="(H2O)32 cc-pVDZ spherical TDHF A+B and A-B build, 8 trial vectors", nwater=32,
+                              edge=14.0, seed=0, basis="cc-pvdz", cutoff=1e-10, td=True, nvec=8),
     # (dd|dd) only: one Cartesian d shell (6-31G(d) carbon d, exponent 0.8) on each
     # point of a 4 x 4 x 4 cubic lattice of spacing 1.54 A, so that all 2080 pairs overlap
     "dd_only": dict(name="(dd|dd)-only: 64 Cartesian d shells (exponent 0.8) on a 4x4x4 lattice, 1.54 A spacing",
@@ -185,9 +190,141 @@ def cpu_baseline(bas, d, budget_s=20.0):
                        % (stride, stride, t_schwarz, st["quartets"])), dict(sample_s=st["t_twoei"], stride=stride)
 
 
+def td_workload(overlap="library"):
+    """Basis and the seeded (nvec, nbf, nbf) transition densities of a TD workload."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(WORKLOAD["nwater"], WORKLOAD["edge"], WORKLOAD["seed"], WORKLOAD["basis"])
+    if overlap == "library":
+        from openqp_gb300.onee import one_electron
+        S = one_electron(bas)[0]
+    else:
+        from oracle import oracle
+        oracle.build()
+        S = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"]).one_electron("S")
+    x = workloads.transition_densities(bas, workloads.nelectrons(bas) // 2, WORKLOAD["nvec"], WORKLOAD["seed"], S=S)
+    return bas, x
+
+
+def cpu_baseline_td(bas, x, budget_s):
+    """The oracle's int2_td_data_t restatement (all host cores) over 1/stride
+    of the bra shell pairs, scaled by stride, plus its full set-up."""
+    from oracle import oracle
+    oracle.build()
+    o = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"])
+    cores = os.cpu_count()
+    # the bra pairs are cost-sorted, so a sparse sample over-weights the
+    # heaviest pair: refine the stride until the sample fills about half the budget
+    stride = 997
+    for _ in range(4):
+        _, _, st = o.fock_td_sample(x, 3, stride, 0, nthreads=cores)
+        if stride == 1 or st["t_twoei"] >= 0.5 * budget_s:
+            break
+        stride = max(1, int(stride * st["t_twoei"] / budget_s))
+    t = st["t_twoei"] * stride + st["t_setup"]
+    return {"value": 1.0 / t, "unit": "TD builds/s", "cores": cores, "kind": "port",
+            "sample": "oracle int2_td_data_t restatement (A+B and A-B, %d vectors) over 1/%d of the cost-sorted bra "
+                      "shell pairs, x%d, plus the work outside the quartet loop (set-up, reduction; %.2f s); %d "
+                      "quartets in the sample"
+                      % (x.shape[0], stride, stride, st["t_setup"], st["quartets"])}
+
+
+def run_td(args):
+    """TD builds/s: A+B and A-B of nvec trial transition densities in one
+    pass over the quartets (OpenQP's int2_td_data_t with int_apb and int_amb),
+    densities resident on the device; e2e through the host-buffer entry."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    from openqp_gb300 import build as bld
+    bld.build()
+    from openqp_gb300.fock import FockBuilder, class_flops, class_labels, fp64_peak_tflops
+    bas, x = td_workload()
+    nvec = x.shape[0]
+    fb = FockBuilder(bas, cutoff=WORKLOAD["cutoff"])
+    fb.set_precision(args.precision, args.mixed_threshold)
+    xt = torch.from_numpy(x).cuda()
+    st = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        fb.fock_td_device(xt, apb=True, amb=True, stream=st)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    times, stats = [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        pa, ma = fb.fock_td_device(xt, apb=True, amb=True, stream=st)
+        e1.record(st)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        stats.append(fb.stats())
+    clocks = sampler.stop()
+    tsum = max_over_ranks(sum(times) / 1000.0)
+    value = ws * args.steps / tsum
+    e2e_t = []
+    if not args.no_e2e:
+        fb.fock_td(x, apb=True, amb=True)
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            hp, hm = fb.fock_td(x, apb=True, amb=True)
+            e2e_t.append(time.perf_counter() - t0)
+        assert np.abs(hp - pa.cpu().numpy()).max() < 1e-12
+    e2e = ws * args.steps / max_over_ranks(sum(e2e_t)) if e2e_t else float("nan")
+    labels = class_labels()
+    ms = np.mean([s["ms_per_class"] for s in stats], axis=0)
+    cdom = int(np.argmax(ms))
+    s0 = stats[-1]
+    pure = bool(bas.harmonic.any())
+    fl = [class_flops(c, s0["prim_per_class"][c], s0["per_class"][c], nk=2 * nvec, nj=nvec, pure=pure)
+          for c in range(21)]
+    achieved = fl[cdom] / (ms[cdom] * 1e-3) / 1e12
+    peak = fp64_peak_tflops()
+    nb = int(8 * nvec * bas.nbf * bas.nbf)
+    line = {"metric": "TDHF A+B / A-B builds/s (%d trial vectors per build)" % nvec, "value": value,
+            "unit": "TD builds/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * tsum / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else args.precision,
+            "data": "synthetic (seeded water cluster, seeded unit-norm transition densities C_occ Y C_vir^T)",
+            "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "nvec": nvec, "cutoff": WORKLOAD["cutoff"],
+                       "flags": "int_apb + int_amb", "l2": "flushed (256 MB write) before every timed step"},
+            "e2e": {"value": e2e, "unit": "TD builds/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": 2 * nb},
+            "roofline": {"bound": "fp64", "kernel": labels[cdom], "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                         "peak_source": "measured: FP64 FMA-chain probe on this device",
+                         "kernel_ms": float(ms[cdom]), "build_fp64_tflops": sum(fl) / (tsum / args.steps) / 1e12},
+            "quartets_per_s": s0["quartets"] / (tsum / args.steps),
+            "prim_quartets_per_s": s0["prim_quartets"] / (tsum / args.steps),
+            "gpu_launches": int(sum(s["launches"] for s in stats)), "clocks": clocks,
+            "class_ms": {labels[c]: round(float(ms[c]), 3) for c in range(21) if ms[c] > 0},
+            "list_ms": s0["list_ms"]}
+    if not args.no_cpu and rank == 0:
+        line["cpu_baseline"] = cpu_baseline_td(bas, x, args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
+        return
+    if WORKLOAD.get("td"):
+        bas, x = td_workload(overlap="oracle")
+        vals = [cpu_baseline_td(bas, x, args.cpu_budget)["value"] for _ in range(max(1, args.steps))]
+        cb = cpu_baseline_td(bas, x, args.cpu_budget)
+        v = statistics.median(vals)
+        cb["value"] = v
+        line = {"impl": "reference", "metric": "TDHF A+B / A-B builds/s (%d trial vectors per build)" % x.shape[0],
+                "value": v, "unit": "TD builds/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "nvec": x.shape[0],
+                           "cutoff": WORKLOAD["cutoff"]},
+                "cpu_baseline": cb, "e2e": {"value": v, "unit": "TD builds/s", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
         return
     if "batch" in WORKLOAD:
         from openqp_gb300 import workloads
@@ -750,6 +887,8 @@ def main():
         run_batch(args)
     elif WORKLOAD.get("grad"):
         run_grad(args)
+    elif WORKLOAD.get("td"):
+        run_td(args)
     elif WORKLOAD.get("scf"):
         run_scf_bench(args)
     else:

@@ -5,8 +5,8 @@
  * is host memory unless the name says _device.  All entry points return (or
  * store in *info) an OpenQP route-C status code:
  *   0 success, 1 not initialised, 2 out of memory, 3 unsupported input
- *   (angular momentum above d, mixed Cartesian/pure d shells, CAM), 4 device
- *   error.  A non-zero status means the caller's native path must run, which
+ *   (angular momentum above d, mixed Cartesian/pure d shells, CAM through an
+ *   entry without cam parameters), 4 device error.  A non-zero status means the caller's native path must run, which
  *   is exactly the contract of OpenQP's seam (source/modules/routec_bridge.F90:20-22).
  *
  * Two layers:
@@ -102,8 +102,8 @@ void routec_grad2(const double* d, const double* xyz, double* de, const int* nbf
  * routec_fock_mrsf replaces the first pass of int2_mrsf_data_t (nmat = 7,
  * source/tdhf_mrsf_lib.F90:218-333) or int2_umrsf_data_t (nmat = 11,
  * :337-426) with tamm_dancoff = .true.; d3 / f3 (nvec, nmat, nbf, nbf)
- * Fortran column-major, f3 OVERWRITTEN.  The CAM pass 2 is not built
- * (info = 3 is never returned for it: the caller runs pass 2 natively). */
+ * Fortran column-major, f3 OVERWRITTEN.  CAM builds: oqpg_fock_td_cam /
+ * oqpg_fock_mrsf_cam. */
 #define OQPG_TD_APB 1
 #define OQPG_TD_AMB 2
 #define OQPG_TD_TDA 4
@@ -112,6 +112,18 @@ void routec_fock_td(const double* d2, double* apb, double* amb, const int* nbf, 
                     const double* se, const double* sc, int* info);
 void routec_fock_mrsf(const double* d3, double* f3, const int* nbf, const int* nvec, const int* nmat,
                       const double* se, const double* sc, int* info);
+
+/* CAM (range-separated) build of routec_fock_jk's packed densities, the
+ * path the reference runs natively for CAM functionals
+ * (source/scf_addons.F90:1136-1167 skips the seam for them): int2_run_cam
+ * (source/integrals/int2.F90:538-584).  cam[5] = {alpha, beta, mu,
+ * alpha_coulomb, beta_coulomb}: pass 1 over 1/r with scale_exchange = alpha,
+ * scale_coulomb = alpha_coulomb (the reference's default 1); pass 2 over the
+ * erf(mu r)/r operator with its own Schwarz bounds, scale_exchange = beta,
+ * scale_coulomb = beta_coulomb (default 0); f = the sum, scaled as
+ * routec_fock_jk's. */
+void routec_fock_jk_cam(const double* d, double* f, const int* nbf, const int* nfocks, const double* cam,
+                        int* info);
 
 /* Release the process-global context. */
 void routec_fock_finalize(void);
@@ -278,6 +290,18 @@ int oqpg_fock_td_device(oqpg_ctx* ctx, const double* d2, double* apb, double* am
 int oqpg_fock_mrsf(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, double se, double sc);
 int oqpg_fock_mrsf_device(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
                           void* stream);
+
+/* CAM forms (see routec_fock_jk_cam for cam[5]).  The TD build's two passes
+ * accumulate before the A+B symmetrisation, as the reference's
+ * parallel_stop runs after the last pass; the MRSF pass 2 updates only the
+ * last component (tdhf_mrsf_lib.F90:314-328, 409-420).  Incremental (f_old)
+ * CAM builds are not offered. */
+int oqpg_fock_jk_cam(oqpg_ctx* ctx, const double* d, double* f, int nfocks, const double* cam);
+int oqpg_fock_jk_cam_device(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, const double* cam,
+                            void* stream);
+int oqpg_fock_td_cam(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, int nvec, int flags,
+                     const double* cam);
+int oqpg_fock_mrsf_cam(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, const double* cam);
 
 /* Angular momenta (la, lb, lc, ld) of class c (0 <= c < 21). */
 int oqpg_class_l(int c, int* l4);

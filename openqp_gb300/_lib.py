@@ -81,6 +81,13 @@ def lib():
         L.routec_fock_td.restype = None
         L.routec_fock_mrsf.argtypes = [_d, _d, _i, _i, _i, _d, _d, _i]
         L.routec_fock_mrsf.restype = None
+        L.oqpg_fock_jk_cam.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, _d]
+        L.oqpg_fock_jk_cam_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _d,
+                                              ctypes.c_void_p]
+        L.oqpg_fock_td_cam.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_int, ctypes.c_int, _d]
+        L.oqpg_fock_mrsf_cam.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d]
+        L.routec_fock_jk_cam.argtypes = [_d, _d, _i, _i, _d, _i]
+        L.routec_fock_jk_cam.restype = None
         _lib = L
     return _lib
 

@@ -65,6 +65,7 @@ struct BuildArgs {
   float prim_cut_lo;       // FP32 decision band of that test: |sp sq| / sqrt(p+q) below lo
   float prim_cut_hi;       // skips, above hi keeps, in between FP64 decides
   double elem_cut;         // element cutoff on |(ab|cd)|
+  double inv_mu2;          // 1/mu^2 of the erf(mu r)/r operator (CAM pass 2); 0: 1/r
   const double* dj;        // nj full nbf x nbf densities for Coulomb
   const double* dk;        // nk full densities for exchange
   const float* djf;        // FP32 copies of dj / dk for the FP32 quartets

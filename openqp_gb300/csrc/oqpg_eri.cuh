@@ -255,10 +255,16 @@ __device__ __forceinline__ double rsqrt_t(double x) { return rsqrt64(x); }
 __device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
 __device__ __forceinline__ dfl rsqrt_t(dfl x) { return df_rsqrt(x); }
 
+// att = 1/mu^2 > 0 evaluates the erf(mu r)/r operator of the CAM pass: p + q
+// becomes p + q + pq/mu^2 in rho, in the prefactor and in the recurrence
+// coefficients (int_rys.F90:225-240; int_rotaxis.F90:634-638 writes the same
+// as rho mu^2/(mu^2 + rho)).  The primitive screen keeps the plain p + q.
 template <typename T, typename PP>
-__device__ __forceinline__ void prim_setup(const PP& bp, const PP& kp, PrimQuartet<T>& o) {
+__device__ __forceinline__ void prim_setup(const PP& bp, const PP& kp, PrimQuartet<T>& o, bool has_att = false,
+                                           T att = T(0)) {
   const T fqz = bp.sp * kp.sp;
-  const T s = bp.p + kp.p;
+  T s = bp.p + kp.p;
+  if (has_att) s = fma(bp.p * kp.p, att, s);
   const T y = rsqrt_t(s);
   o.inv = y * y;
   o.qi = kp.p * o.inv;
@@ -473,7 +479,7 @@ __device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P
     prim_load(bpp + cb, bp);
     prim_load(kpp + cq, kp);
     PrimQuartet<T> pq;
-    prim_setup<T>(bp, kp, pq);
+    prim_setup<T>(bp, kp, pq, a.inv_mu2 != 0.0, (T)a.inv_mu2);
     ++nprim;
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
@@ -934,7 +940,7 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
         if (kb + 1 < P.pcnt) prim_load(bpp + kb + 1, bn);  // prefetch
         if (!screen_keep(bpp + kb, prim_screen(bpp + kb), kpp + kq, ks, a)) continue;
         PrimQuartet<T> pq;
-        prim_setup<T>(bp, kp, pq);
+        prim_setup<T>(bp, kp, pq, a.inv_mu2 != 0.0, (T)a.inv_mu2);
         ++nprim;
         if (lane < 2 * NR) {
           const T v = rys_quantity<NR, T>(pq.X, lane, a.roots_f32 != 0);

@@ -510,6 +510,76 @@ void default_tuning(oqpg_tuning& t) {
 // A batch of nmol molecules: nshell_m[m] shells on natom_m[m] atoms each, the
 // shell and atom arrays concatenated molecule by molecule (origin 1-based
 // within the molecule).  One molecule is the batch of one.
+// Schwarz bounds sqrt(max |(ab|ab)|) per pair (ints_exchange, int2.F90:1582-1737)
+// from pair tables built with the very tight cutoffs 1e-17 / 50; inv_mu2 > 0
+// gives the bounds of the erf-attenuated operator (int2.F90:675-681).
+// Needs the context's shells, AO offsets and molecules on the device.
+int schwarz_bounds(oqpg_ctx* c, double inv_mu2, std::vector<double>& out) {
+  cudaStream_t st = c->stream;
+  int rc;
+  HostPairs sp;
+  build_pairs(*c, c->h_am, c->h_ncontr, c->h_poff, c->h_ex.data(), c->h_cc.data(), 1e-17, 50.0, true, sp);
+  DevBuf d_pairs, d_prims, d_diag, d_q, d_w;
+  if ((rc = upload(d_pairs, sp.pairs, st))) return rc;
+  if ((rc = upload(d_prims, sp.prims, st))) return rc;
+  std::vector<std::vector<uint2>> diag(NCLASS);
+  for (int p = 0; p < c->npair; ++p) {
+    if (sp.pairs[p].pcnt == 0) continue;
+    diag[class_index(sp.type[p], sp.type[p])].push_back(make_uint2(p, p));
+  }
+  CK(d_q.ensure(sizeof(double) * c->npair));
+  CK(d_w.ensure(sizeof(unsigned long long)));
+  CK(cudaMemsetAsync(d_q.p, 0, sizeof(double) * c->npair, st));
+  for (int cl = 0; cl < NCLASS; ++cl) {
+    if (diag[cl].empty()) continue;
+    if ((rc = upload(d_diag, diag[cl], st))) return rc;
+    BuildArgs a{};
+    a.shells = c->d_shells.as<ShellDev>();
+    a.pairs = d_pairs.as<PairDev>();
+    a.prims = d_prims.as<PrimPair>();
+    a.quartets = d_diag.as<uint2>();
+    a.nquartets = (long long)diag[cl].size();
+    a.nbf = c->stride;
+    a.kstride = (size_t)c->nbf * c->stride;
+    a.prim_cut = 1e-17;
+    a.prim_cut2 = 1e-34;
+    a.inv_mu2 = inv_mu2;
+    set_band(a);
+    a.schwarz_out = d_q.as<double>();
+    CK(cudaMemsetAsync(d_w.p, 0, sizeof(unsigned long long), st));
+    a.work = d_w.as<unsigned long long>();
+    CK(launch_class(cl, c->pure, MODE_SCHWARZ, a, c->nsm, st));
+    CK(cudaStreamSynchronize(st));  // d_diag is reused by the next class
+  }
+  out.resize(c->npair);
+  CK(cudaMemcpyAsync(out.data(), d_q.p, sizeof(double) * c->npair, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return OK;
+}
+
+// Device screening tables of one set of Schwarz bounds: the bounds (FP64,
+// FP32) and each molecule's pairs by descending bound.
+int upload_schwarz(oqpg_ctx* c, const std::vector<double>& q, DevBuf& d_q, DevBuf& d_qf, DevBuf& d_sidx,
+                   DevBuf& d_sq) {
+  cudaStream_t st = c->stream;
+  int rc;
+  if ((rc = upload(d_q, q, st))) return rc;
+  std::vector<float> qf(c->npair);
+  for (int p = 0; p < c->npair; ++p) qf[p] = (float)q[p];
+  if ((rc = upload(d_qf, qf, st))) return rc;
+  std::vector<int> order(c->npair);
+  for (int p = 0; p < c->npair; ++p) order[p] = p;
+  for (const MolDev& M : c->mols)
+    std::stable_sort(order.begin() + M.pair0, order.begin() + M.pair0 + M.npair,
+                     [&](int x, int y) { return q[x] > q[y]; });
+  std::vector<double> sq(c->npair);
+  for (int p = 0; p < c->npair; ++p) sq[p] = q[order[p]];
+  if ((rc = upload(d_sidx, order, st))) return rc;
+  if ((rc = upload(d_sq, sq, st))) return rc;
+  CK(cudaStreamSynchronize(st));
+  return OK;
+}
+
 int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, const int* am_, const int* ncontr_,
              const int* origin, const double* ex, const double* cc, const int* harmonic, const double* xyz,
              double cutoff) {
@@ -591,45 +661,7 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
   if ((rc = upload(c->d_row_mol, row_mol, st))) return rc;
 
   // --- Schwarz bounds with OpenQP's very tight cutoffs (int2.F90:1600-1604)
-  HostPairs sp;
-  build_pairs(*c, am, ncontr, poff, ex, cc, 1e-17, 50.0, true, sp);
-  if ((rc = upload(c->d_pairs, sp.pairs, st))) return rc;
-  if ((rc = upload(c->d_prims, sp.prims, st))) return rc;
-  std::vector<std::vector<uint2>> diag(NCLASS);
-  for (int p = 0; p < c->npair; ++p) {
-    if (sp.pairs[p].pcnt == 0) continue;
-    diag[class_index(sp.type[p], sp.type[p])].push_back(make_uint2(p, p));
-  }
-  DevBuf d_diag, d_q, d_w;
-  CK(d_q.ensure(sizeof(double) * c->npair));
-  CK(d_w.ensure(sizeof(unsigned long long)));
-  CK(cudaMemsetAsync(d_q.p, 0, sizeof(double) * c->npair, st));
-  for (int cl = 0; cl < NCLASS; ++cl) {
-    if (diag[cl].empty()) continue;
-    if ((rc = upload(d_diag, diag[cl], st))) return rc;
-    BuildArgs a{};
-    a.shells = c->d_shells.as<ShellDev>();
-    a.pairs = c->d_pairs.as<PairDev>();
-    a.prims = c->d_prims.as<PrimPair>();
-    a.quartets = d_diag.as<uint2>();
-    a.nquartets = (long long)diag[cl].size();
-    a.nbf = c->stride;
-    a.kstride = (size_t)c->nbf * c->stride;
-    a.prim_cut = 1e-17;
-    a.prim_cut2 = 1e-34;
-    set_band(a);
-    a.schwarz_out = d_q.as<double>();
-    CK(cudaMemsetAsync(d_w.p, 0, sizeof(unsigned long long), st));
-    a.work = d_w.as<unsigned long long>();
-    CK(launch_class(cl, c->pure, MODE_SCHWARZ, a, c->nsm, st));
-    CK(cudaStreamSynchronize(st));  // d_diag is reused by the next class
-  }
-  c->schwarz_pair.resize(c->npair);
-  CK(cudaMemcpyAsync(c->schwarz_pair.data(), d_q.p, sizeof(double) * c->npair, cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  d_diag.release();
-  d_q.release();
-  d_w.release();
+  if ((rc = schwarz_bounds(c, 0.0, c->schwarz_pair))) return rc;
 
   // --- pair tables of the Fock build (cutoffs 1e-2 tau, 1e-4 tau, 25 ln 10; int2.F90:260-272)
   HostPairs fp;
@@ -660,23 +692,27 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
   if ((rc = upload(c->d_pair_ij, fp.ij, st))) return rc;
   if ((rc = upload(c->d_pair_type, fp.type, st))) return rc;
   if ((rc = upload(c->d_pair_mol, fp.mol, st))) return rc;
-  if ((rc = upload(c->d_q, c->schwarz_pair, st))) return rc;
-  std::vector<float> qf(c->npair);
-  for (int p = 0; p < c->npair; ++p) qf[p] = (float)c->schwarz_pair[p];
-  if ((rc = upload(c->d_qf, qf, st))) return rc;
-  // each molecule's pairs by descending Schwarz bound (global pair indices)
-  std::vector<int> order(c->npair);
-  for (int p = 0; p < c->npair; ++p) order[p] = p;
-  for (const MolDev& M : c->mols)
-    std::stable_sort(order.begin() + M.pair0, order.begin() + M.pair0 + M.npair,
-                     [&](int x, int y) { return c->schwarz_pair[x] > c->schwarz_pair[y]; });
-  std::vector<double> sq(c->npair);
-  for (int p = 0; p < c->npair; ++p) sq[p] = c->schwarz_pair[order[p]];
-  if ((rc = upload(c->d_sorted_idx, order, st))) return rc;
-  if ((rc = upload(c->d_sorted_q, sq, st))) return rc;
   CK(cudaStreamSynchronize(st));
+  return upload_schwarz(c, c->schwarz_pair, c->d_q, c->d_qf, c->d_sorted_idx, c->d_sorted_q);
+}
+
+}  // namespace
+
+// Screening tables of the erf-attenuated operator for mu (kept until mu changes).
+int oqpg::ensure_att(oqpg_ctx* c, double mu) {
+  if (!(mu > 0.0)) return UNSUPPORTED;
+  if (c->att_mu == mu) return OK;
+  c->att_mu = 0.0;
+  int rc;
+  if ((rc = schwarz_bounds(c, 1.0 / (mu * mu), c->schwarz_pair_att))) return rc;
+  if ((rc = upload_schwarz(c, c->schwarz_pair_att, c->d_q_att, c->d_qf_att, c->d_sorted_idx_att,
+                           c->d_sorted_q_att)))
+    return rc;
+  c->att_mu = mu;
   return OK;
 }
+
+namespace {
 
 void ctx_free(oqpg_ctx* c) {
   if (!c) return;
@@ -686,7 +722,7 @@ void ctx_free(oqpg_ctx* c) {
                     &c->d_sorted_idx, &c->d_sorted_q, &c->d_dp, &c->d_f, &c->d_fold, &c->d_gin, &c->d_gout,
                     &c->d_gpairs, &c->d_gprims, &c->d_galpha, &c->d_gprimsf, &c->d_galphaf, &c->d_coff,
                     &c->d_atom, &c->d_gmat, &c->d_gmatf, &c->d_dshg, &c->d_gcounts, &c->d_gwork, &c->d_de,
-                    &c->d_gcnt};
+                    &c->d_gcnt, &c->d_q_att, &c->d_qf_att, &c->d_sorted_idx_att, &c->d_sorted_q_att};
   for (DevBuf* b : bufs) b->release();
   c->hb.release();
   c->gb.release();
@@ -752,15 +788,18 @@ int ensure_bufs(oqpg_ctx* c, BuildBufs& B, const Job& job) {
   return OK;
 }
 
-ListArgs list_args(const oqpg_ctx* c, BuildBufs& B) {
+ListArgs list_args(const oqpg_ctx* c, BuildBufs& B, const Job& job) {
   ListArgs la{};
   la.npair = c->npair;
   la.mols = c->d_mols.as<MolDev>();
   la.pair_mol = c->d_pair_mol.as<int>();
   la.pair_ij = c->d_pair_ij.as<int2>();
   la.pair_type = c->d_pair_type.as<int>();
-  la.q = c->d_q.as<double>(); la.qf = c->d_qf.as<float>();
-  la.sorted_idx = c->d_sorted_idx.as<int>(); la.sorted_q = c->d_sorted_q.as<double>();
+  const bool att = job.inv_mu2 != 0.0;  // erf-attenuated pass: its own Schwarz bounds
+  la.q = (att ? c->d_q_att : c->d_q).as<double>();
+  la.qf = (att ? c->d_qf_att : c->d_qf).as<float>();
+  la.sorted_idx = (att ? c->d_sorted_idx_att : c->d_sorted_idx).as<int>();
+  la.sorted_q = (att ? c->d_sorted_q_att : c->d_sorted_q).as<double>();
   la.dsh = B.dsh.as<double>(); la.dshf = B.dshf.as<float>();
   la.dmax_bits = B.dmax.as<unsigned long long>();
   la.tau = c->tau;
@@ -837,7 +876,7 @@ int size_lists(oqpg_ctx* c, BuildBufs& B, const unsigned long long* counts, cuda
 int count_lists(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, unsigned long long* counts) {
   int rc;
   if ((rc = issue_densities(c, B, job, st))) return rc;
-  ListArgs la = list_args(c, B);
+  ListArgs la = list_args(c, B, job);
   la.write = 0;
   CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * NLIST, st));
   k_lists<<<c->npair, 256, 0, st>>>(la);
@@ -861,7 +900,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   if ((rc = issue_densities(c, B, job, st))) return rc;
   if (job.gen) nlaunch += 2 + (split_on(c) ? 1 : 0) + (df_on(c) ? 1 : 0);
   else nlaunch += 2 + (split_on(c) ? (nk == 2 ? 2 : 1) : 0) + (df_on(c) ? (nk == 2 ? 2 : 1) : 0);
-  ListArgs la = list_args(c, B);
+  ListArgs la = list_args(c, B, job);
   la.write = 1;
   CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * NLIST, st));
   k_lists<<<c->npair, 256, 0, st>>>(la);
@@ -916,6 +955,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   a.prim_cut2 = a.prim_cut * a.prim_cut;
   set_band(a);
   a.elem_cut = c->tau;
+  a.inv_mu2 = job.inv_mu2;
   if (job.gen) {
     const size_t k0 = (size_t)job.gen->k0 * n2;
     a.dj = B.dk.as<double>();
@@ -1064,7 +1104,23 @@ Job packed_job(const double* dp, double* f, double* f_old, int nfocks, double se
   return j;
 }
 
-int ctx_build_host(oqpg_ctx* c, const double* d, double* f, double* f_old, int nfocks, double se, double sc) {
+// CAM build (int2_run_cam, int2.F90:538-584) of packed densities on device
+// buffers: pass 1 over 1/r with cam = {alpha, beta, mu, alpha_c, beta_c}'s
+// (alpha, alpha_c) as (se, sc), pass 2 over erf(mu r)/r with (beta, beta_c)
+// added to f.
+int cam_build(oqpg_ctx* c, const double* dp, double* f, int nfocks, const double* cam, cudaStream_t st) {
+  if (!cam || !(cam[2] > 0.0)) return UNSUPPORTED;
+  int rc;
+  if ((rc = ensure_att(c, cam[2]))) return rc;
+  if ((rc = ctx_build(c, packed_job(dp, f, nullptr, nfocks, cam[0], cam[3]), st))) return rc;
+  Job j2 = packed_job(dp, f, f, nfocks, cam[1], cam[4]);
+  j2.inv_mu2 = 1.0 / (cam[2] * cam[2]);
+  return ctx_build(c, j2, st);
+}
+
+int ctx_build_host(oqpg_ctx* c, const double* d, double* f, double* f_old, int nfocks, double se, double sc,
+                   const double* cam = nullptr) {
+  if (cam && f_old) return UNSUPPORTED;
   const size_t bytes = sizeof(double) * (size_t)c->ntri * nfocks;
   if (bytes > c->h_bytes) {
     if (c->h_in) cudaFreeHost(c->h_in);
@@ -1085,8 +1141,9 @@ int ctx_build_host(oqpg_ctx* c, const double* d, double* f, double* f_old, int n
     std::memcpy(c->h_out, f_old, bytes);
     CK(cudaMemcpyAsync(c->d_fold.p, c->h_out, bytes, cudaMemcpyHostToDevice, st));
   }
-  int rc = ctx_build(c, packed_job(c->d_dp.as<double>(), c->d_f.as<double>(), f_old ? c->d_fold.as<double>() : nullptr,
-                                    nfocks, se, sc), st);
+  int rc = cam ? cam_build(c, c->d_dp.as<double>(), c->d_f.as<double>(), nfocks, cam, st)
+               : ctx_build(c, packed_job(c->d_dp.as<double>(), c->d_f.as<double>(),
+                                         f_old ? c->d_fold.as<double>() : nullptr, nfocks, se, sc), st);
   if (rc) return rc;
   CK(cudaMemcpyAsync(c->h_out, c->d_f.p, bytes, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -1385,6 +1442,29 @@ int routec_fock_init_batch(int nmol, const int* nshell, const int* natom, const 
     g_ctx = nullptr;
   }
   return oqpg_create_batch(&g_ctx, nmol, nshell, natom, am, ncontr, origin, ex, cc, harmonic, xyz, cutoff);
+}
+
+int oqpg_fock_jk_cam(oqpg_ctx* ctx, const double* d, double* f, int nfocks, const double* cam) {
+  if (!ctx || !d || !f) return UNSUPPORTED;
+  return ctx_build_host(ctx, d, f, nullptr, nfocks, 0.0, 0.0, cam);
+}
+
+int oqpg_fock_jk_cam_device(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, const double* cam,
+                            void* stream) {
+  if (!ctx || !d_device || !f_device) return UNSUPPORTED;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  int rc = cam_build(ctx, d_device, f_device, nfocks, cam, st);
+  if (rc) return rc;
+  return cudaStreamSynchronize(st) == cudaSuccess ? OK : DEV_ERR;
+}
+
+void routec_fock_jk_cam(const double* d, double* f, const int* nbf, const int* nfocks, const double* cam, int* info) {
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!d || !f || !nbf || !nfocks || !cam) rc = UNSUPPORTED;
+  else if (*nbf != g_ctx->nbf || g_ctx->nmol != 1) rc = NOT_INIT;
+  else rc = ctx_build_host(g_ctx, d, f, nullptr, *nfocks, 0.0, 0.0, cam);
+  if (info) *info = rc;
 }
 
 void routec_fock_td(const double* d2, double* apb, double* amb, const int* nbf, const int* nvec, const int* flags,

@@ -132,6 +132,7 @@ struct GenJob {
   std::vector<long long> screen;  // bases of the inputs that form the shell density
   std::vector<GenOut> outs;
   std::vector<GenTerm> terms;
+  bool accumulate = false;  // add into the outputs (second CAM pass) instead of overwriting
 };
 
 // One build: packed SCF densities (gen == nullptr) or a general job.
@@ -142,6 +143,7 @@ struct Job {
   double* f_old = nullptr;
   double se = 1.0, sc = 1.0;
   const GenJob* gen = nullptr;
+  double inv_mu2 = 0.0;  // erf(mu r)/r pass of a CAM build (needs ensure_att(mu) first)
   int nj() const { return gen ? gen->nj : 1; }
   int nk() const { return gen ? gen->nk : nfocks; }
 };
@@ -170,6 +172,7 @@ int gen_finalize(oqpg_ctx* c, BuildBufs& B, const GenJob& g, cudaStream_t st);
 bool split_on(const oqpg_ctx* c);
 bool df_on(const oqpg_ctx* c);
 int ctx_build(oqpg_ctx* c, const Job& job, cudaStream_t st);
+int ensure_att(oqpg_ctx* c, double mu);
 cudaError_t launch_grad_a(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
 cudaError_t launch_grad_b(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
 
@@ -230,6 +233,10 @@ struct oqpg_ctx {
   oqpg::DevBuf d_shells, d_pairs, d_prims, d_primsf, d_primsdf, d_pair_ij, d_pair_type, d_q, d_qf, d_aoff, d_naos, d_mols,
       d_pair_mol, d_row_mol;
   oqpg::DevBuf d_sorted_idx, d_sorted_q;
+  // screening tables of the erf-attenuated operator (CAM pass 2) for att_mu
+  double att_mu = 0.0;
+  std::vector<double> schwarz_pair_att;
+  oqpg::DevBuf d_q_att, d_qf_att, d_sorted_idx_att, d_sorted_q_att;
   // per-build buffers: direct builds, and the captured graph's own set
   oqpg::BuildBufs hb, gb;
   oqpg::DevBuf d_dp, d_f, d_fold;     // device copies of host-buffer builds

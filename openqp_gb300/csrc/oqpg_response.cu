@@ -67,11 +67,12 @@ __global__ void k_dsh_gen(const double* __restrict__ in, long long rs, long long
 }
 
 // out_o(r, c) = sum over the terms of o of coef (G[r][c] + sign G[c][r]),
-// G the term's Coulomb or exchange accumulator.  Nothing is written when a
-// quartet list overflowed (the build is then redone).
+// G the term's Coulomb or exchange accumulator (added to out_o with
+// accumulate).  Nothing is written when a quartet list overflowed (the build
+// is then redone).
 __global__ void k_finalize_gen(const double* __restrict__ gj, const double* __restrict__ gk, size_t kstride,
                                int stride, int n, const GenOut* __restrict__ outs, int nout,
-                               const GenTerm* __restrict__ terms, long long ors, long long ocs,
+                               const GenTerm* __restrict__ terms, long long ors, long long ocs, int accumulate,
                                const unsigned* __restrict__ flag) {
   if (flag && *flag) return;
   const long long per = (long long)n * n, tot = per * nout;
@@ -87,7 +88,8 @@ __global__ void k_finalize_gen(const double* __restrict__ gj, const double* __re
       const double* G = (T.kind ? gk : gj) + (size_t)T.idx * kstride;
       v += T.coef * (G[(size_t)r * stride + c] + (double)T.sign * G[(size_t)c * stride + r]);
     }
-    O.dst[r * ors + c * ocs] = v;
+    double* d = O.dst + (r * ors + c * ocs);
+    *d = accumulate ? *d + v : v;
   }
 }
 
@@ -167,7 +169,7 @@ int gen_finalize(oqpg_ctx* c, BuildBufs& B, const GenJob& g, cudaStream_t st) {
   k_finalize_gen<<<grid_for(n2 * (long long)g.outs.size(), c->nsm), 256, 0, st>>>(
       B.gj.as<double>(), B.gk.as<double>(), (size_t)c->nbf * c->stride, c->stride, c->nbf,
       (const GenOut*)(tab + L.outs), (int)g.outs.size(), (const GenTerm*)(tab + L.terms), g.out_rs, g.out_cs,
-      B.flag.as<unsigned>());
+      g.accumulate ? 1 : 0, B.flag.as<unsigned>());
   CKR(cudaGetLastError());
   return OK;
 }
@@ -262,20 +264,51 @@ void mrsf_job(const oqpg_ctx* c, const double* d3, double* f3, int nvec, int nma
     }
 }
 
-int run_job(oqpg_ctx* c, const GenJob& g, cudaStream_t st) {
+// Second (erf-attenuated) CAM pass of int2_mrsf_data_t / int2_umrsf_data_t
+// (tdhf_mrsf_lib.F90:314-328, 409-420): only the last component, -beta K[X],
+// added to f3.
+void mrsf_cam2_job(const oqpg_ctx* c, const double* d3, double* f3, int nvec, int nmat, double beta, GenJob& g) {
+  const long long n = c->nbf;
+  g.in = d3;
+  g.in_rs = (long long)nmat * nvec; g.in_cs = n * nmat * nvec;
+  g.out_rs = g.in_rs; g.out_cs = g.in_cs;
+  const int m = nmat - 1;
+  for (int v = 0; v < nvec; ++v) g.slices.push_back(GenSlice{(long long)m * nvec + v, +1, 0});
+  for (int v = 0; v < nvec; ++v) g.slices.push_back(GenSlice{(long long)m * nvec + v, -1, 0});
+  g.nj = 0;
+  g.k0 = 0;
+  g.nk = 2 * nvec;
+  for (int v = 0; v < nvec; ++v) g.screen.push_back((long long)m * nvec + v);
+  for (int v = 0; v < nvec; ++v) {
+    GenOut o{f3 + (long long)m * nvec + v, (int)g.terms.size(), 2};
+    g.terms.push_back(term(-beta, 1, v, +1));
+    g.terms.push_back(term(-beta, 1, nvec + v, -1));
+    g.outs.push_back(o);
+  }
+  g.accumulate = true;
+}
+
+int run_job(oqpg_ctx* c, const GenJob& g, cudaStream_t st, double inv_mu2 = 0.0) {
   Job j;
   j.gen = &g;
+  j.inv_mu2 = inv_mu2;
   return ctx_build(c, j, st);
 }
+
+// cam = {alpha, beta, mu, alpha_coulomb, beta_coulomb} (int2_run_cam,
+// int2.F90:538-584): pass 1 with scale_exchange alpha and scale_coulomb
+// alpha_coulomb over 1/r, pass 2 with beta and beta_coulomb over erf(mu r)/r.
+bool cam_ok(const double* cam) { return cam && cam[2] > 0.0; }
 
 // host-buffer build: the input is copied to the context's d_dp, the job writes
 // its outputs into d_f (nout_buf consecutive blocks), which are copied back
 int host_job(oqpg_ctx* c, const double* in, size_t in_elems, double* const* host_out, const size_t* out_elems,
-             int nout_buf, const GenJob& g) {
+             int nout_buf, const GenJob& g, const GenJob* g2 = nullptr, double inv_mu2 = 0.0) {
   cudaStream_t st = c->stream;
   CKR(cudaMemcpyAsync(c->d_dp.p, in, sizeof(double) * in_elems, cudaMemcpyHostToDevice, st));
   int rc = run_job(c, g, st);
   if (rc) return rc;
+  if (g2 && (rc = run_job(c, *g2, st, inv_mu2))) return rc;
   size_t off = 0;
   for (int b = 0; b < nout_buf; ++b) {
     if (host_out[b])
@@ -343,6 +376,39 @@ int oqpg_fock_mrsf(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nm
   double* outs[1] = {f3};
   const size_t elems[1] = {tot};
   return host_job(ctx, d3, tot, outs, elems, 1, g);
+}
+
+int oqpg_fock_td_cam(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, int nvec, int flags,
+                     const double* cam) {
+  if (!td_args_ok(ctx, nvec, flags) || !d2 || !cam_ok(cam)) return UNSUPPORTED;
+  int rc;
+  if ((rc = ensure_att(ctx, cam[2]))) return rc;
+  const size_t tot = (size_t)ctx->nbf * ctx->nbf * nvec;
+  if (ctx->d_dp.ensure(sizeof(double) * tot) != cudaSuccess) return NO_MEM;
+  if (ctx->d_f.ensure(sizeof(double) * 2 * tot) != cudaSuccess) return NO_MEM;
+  GenJob g1, g2;
+  double* pa = ctx->d_f.as<double>();
+  td_job(ctx, ctx->d_dp.as<double>(), pa, pa + tot, nvec, flags, cam[0], cam[3], g1);
+  td_job(ctx, ctx->d_dp.as<double>(), pa, pa + tot, nvec, flags, cam[1], cam[4], g2);
+  g2.accumulate = true;
+  double* outs[2] = {apb, amb};
+  const size_t elems[2] = {tot, tot};
+  return host_job(ctx, d2, tot, outs, elems, 2, g1, &g2, 1.0 / (cam[2] * cam[2]));
+}
+
+int oqpg_fock_mrsf_cam(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, const double* cam) {
+  if (!ctx || ctx->nmol != 1 || nvec < 1 || (nmat != 7 && nmat != 11) || !d3 || !cam_ok(cam)) return UNSUPPORTED;
+  int rc;
+  if ((rc = ensure_att(ctx, cam[2]))) return rc;
+  const size_t tot = (size_t)ctx->nbf * ctx->nbf * nmat * nvec;
+  if (ctx->d_dp.ensure(sizeof(double) * tot) != cudaSuccess) return NO_MEM;
+  if (ctx->d_f.ensure(sizeof(double) * tot) != cudaSuccess) return NO_MEM;
+  GenJob g1, g2;
+  mrsf_job(ctx, ctx->d_dp.as<double>(), ctx->d_f.as<double>(), nvec, nmat, cam[0], cam[3], g1);
+  mrsf_cam2_job(ctx, ctx->d_dp.as<double>(), ctx->d_f.as<double>(), nvec, nmat, cam[1], g2);
+  double* outs[1] = {f3};
+  const size_t elems[1] = {tot};
+  return host_job(ctx, d3, tot, outs, elems, 1, g1, &g2, 1.0 / (cam[2] * cam[2]));
 }
 
 }  // extern "C"

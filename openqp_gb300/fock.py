@@ -92,6 +92,20 @@ class FockBuilder:
             raise FockError(rc, "oqpg_fock_jk")
         return f
 
+    def fock_jk_cam(self, d, alpha, beta, mu, alpha_coul=1.0, beta_coul=0.0):
+        """CAM build (OpenQP's int2_run_cam, int2.F90:538-584) of packed
+        densities: sc = alpha_coul, se = alpha over 1/r plus sc = beta_coul,
+        se = beta over erf(mu r)/r; same packing and scaling as fock_jk."""
+        d = np.ascontiguousarray(np.atleast_2d(d), dtype=np.float64)
+        if d.shape[1] != self.ntri:
+            raise ValueError("density has %d packed elements, basis needs %d" % (d.shape[1], self.ntri))
+        f = np.empty_like(d)
+        rc = lib().oqpg_fock_jk_cam(self.h, ptr(d), ptr(f), d.shape[0], ptr(cam_array(alpha, beta, mu, alpha_coul,
+                                                                                      beta_coul)))
+        if rc != 0:
+            raise FockError(rc, "oqpg_fock_jk_cam")
+        return f
+
     def fock_jk_device(self, d, scale_exch=1.0, scale_coul=1.0, out=None, stream=None):
         """d: torch CUDA tensor (nfocks, ntri) float64 -> torch tensor, no host copies."""
         import torch
@@ -126,7 +140,8 @@ class FockBuilder:
         return out
 
     # ---- response-type builds (general square densities) ---------------------
-    def fock_td(self, x, apb=True, amb=False, tda=False, tda_coulomb=False, scale_exch=1.0, scale_coul=1.0):
+    def fock_td(self, x, apb=True, amb=False, tda=False, tda_coulomb=False, scale_exch=1.0, scale_coul=1.0,
+                cam=None):
         """TDHF-type build of OpenQP's int2_td_data_t (tdhf_lib.F90:140-224).
 
         x: (nvec, nbf, nbf) or (nbf, nbf) general square densities (host,
@@ -134,7 +149,9 @@ class FockBuilder:
           A+B: 4 sc J[X] - 2 se K[(X + X^T)/2]        (apb=True)
           A-B: -2 se K[(X - X^T)/2]                    (amb=True)
           TDA, into amb: 2 sc J[X] (tda_coulomb) - se K[X]
-        with J[X]_ij = sum (ij|kl) X_kl and K[X]_ik = sum (ij|kl) X_jl."""
+        with J[X]_ij = sum (ij|kl) X_kl and K[X]_ik = sum (ij|kl) X_jl.
+        cam = (alpha, beta, mu[, alpha_coul, beta_coul]): the two-pass CAM build
+        (scale_exch / scale_coul are then replaced by the pass scales)."""
         x = np.asarray(x, dtype=np.float64)
         squeeze = x.ndim == 2
         x3 = x[None] if squeeze else x
@@ -143,8 +160,11 @@ class FockBuilder:
             raise ValueError("densities must be (nvec, %d, %d)" % (n, n))
         fx = np.ascontiguousarray(x3.transpose(0, 2, 1))  # Fortran (nbf, nbf, nvec)
         pa, ma = np.empty_like(fx), np.empty_like(fx)
-        rc = lib().oqpg_fock_td(self.h, ptr(fx), ptr(pa), ptr(ma), nv, td_flags(apb, amb, tda, tda_coulomb),
-                                float(scale_exch), float(scale_coul))
+        fl = td_flags(apb, amb, tda, tda_coulomb)
+        if cam is not None:
+            rc = lib().oqpg_fock_td_cam(self.h, ptr(fx), ptr(pa), ptr(ma), nv, fl, ptr(cam_array(*cam)))
+        else:
+            rc = lib().oqpg_fock_td(self.h, ptr(fx), ptr(pa), ptr(ma), nv, fl, float(scale_exch), float(scale_coul))
         if rc != 0:
             raise FockError(rc, "oqpg_fock_td")
         pa, ma = pa.transpose(0, 2, 1), ma.transpose(0, 2, 1)
@@ -169,21 +189,26 @@ class FockBuilder:
         pa, ma = pa.transpose(1, 2), ma.transpose(1, 2)
         return (pa[0], ma[0]) if x.dim() == 2 else (pa, ma)
 
-    def fock_mrsf(self, x, scale_exch=1.0, scale_coul=1.0):
+    def fock_mrsf(self, x, scale_exch=1.0, scale_coul=1.0, cam=None):
         """MRSF (nmat 7) / UMRSF (nmat 11) sigma-vector build of OpenQP's
         int2_mrsf_data_t / int2_umrsf_data_t, first pass (tdhf_mrsf_lib.F90:218-426).
 
         x: (nvec, nmat, nbf, nbf) host, natural indexing x[v, m][r, c].
         Returns f of the same shape:
           MRSF:  m < 4: sc J[X] - se K[X];  m >= 4: -se K[X]
-          UMRSF: m < 8: sc J[X] - se K[X];  m = 8, 9: -se K[X^T];  m = 10: -se K[X]."""
+          UMRSF: m < 8: sc J[X] - se K[X];  m = 8, 9: -se K[X^T];  m = 10: -se K[X].
+        cam = (alpha, beta, mu[, alpha_coul, beta_coul]): pass 1 with (alpha,
+        alpha_coul), pass 2 over erf(mu r)/r adds -beta K[X] to the last component."""
         x = np.asarray(x, dtype=np.float64)
         nv, nm, n = x.shape[0], x.shape[1], self.nbf
         if x.shape[2:] != (n, n) or nm not in (7, 11):
             raise ValueError("densities must be (nvec, 7 or 11, %d, %d)" % (n, n))
         fx = np.ascontiguousarray(x.transpose(3, 2, 1, 0))  # Fortran (nvec, nmat, nbf, nbf)
         out = np.empty_like(fx)
-        rc = lib().oqpg_fock_mrsf(self.h, ptr(fx), ptr(out), nv, nm, float(scale_exch), float(scale_coul))
+        if cam is not None:
+            rc = lib().oqpg_fock_mrsf_cam(self.h, ptr(fx), ptr(out), nv, nm, ptr(cam_array(*cam)))
+        else:
+            rc = lib().oqpg_fock_mrsf(self.h, ptr(fx), ptr(out), nv, nm, float(scale_exch), float(scale_coul))
         if rc != 0:
             raise FockError(rc, "oqpg_fock_mrsf")
         return out.transpose(3, 2, 1, 0)
@@ -321,11 +346,11 @@ def fp64_peak_tflops(iters=20000):
     return v.value
 
 
-def class_flops(c, nprim, nquart, nk=1, pure=False):
+def class_flops(c, nprim, nquart, nk=1, pure=False, nj=1):
     """Algorithmic FP64 flops of class c: assembly 3 R N_c per primitive
     quartet (x*y, then FMA with z, per Rys root) plus digestion per
-    contracted quartet, 12 flops (6 FMA) per element for RHF, 2 + 4 nk FMA
-    per element for UHF/ROHF."""
+    contracted quartet, 2 FMA per element and Coulomb density plus 4 FMA per
+    element and exchange density (12 flops for RHF)."""
     l4 = (ctypes.c_int * 4)()
     lib().oqpg_class_l(c, l4)
     L = list(l4)
@@ -335,7 +360,7 @@ def class_flops(c, nprim, nquart, nk=1, pure=False):
     for l in L:
         nc *= (l + 1) * (l + 2) // 2
         nao *= (5 if (pure and l == 2) else (l + 1) * (l + 2) // 2)
-    dig = 12 if nk == 1 else 2 * (2 + 4 * nk)
+    dig = 2 * (2 * nj + 4 * nk)
     return 3.0 * R * nc * nprim + dig * nao * nquart
 
 
@@ -374,6 +399,24 @@ def routec_grad2(d, xyz, nbf, natom, hfscale=1.0, coulscale=1.0, de=None):
     lib().routec_grad2(ptr(d), ptr(x), ptr(de), ctypes.byref(n), ctypes.byref(na), ctypes.byref(hf), ctypes.byref(cs),
                        ctypes.byref(info))
     return de.reshape(-1, 3), info.value
+
+
+def cam_array(alpha, beta, mu, alpha_coul=1.0, beta_coul=0.0):
+    """The cam[5] argument of the C ABI (int2_run_cam's parameters)."""
+    if not mu > 0:
+        raise ValueError("CAM needs mu > 0")
+    return np.array([alpha, beta, mu, alpha_coul, beta_coul], dtype=np.float64)
+
+
+def routec_fock_jk_cam(d, nbf, nfocks, alpha, beta, mu, alpha_coul=1.0, beta_coul=0.0):
+    """Calls routec_fock_jk_cam with all arguments by reference. Returns (f, info)."""
+    d = np.ascontiguousarray(d, dtype=np.float64).reshape(-1)
+    f = np.zeros_like(d)
+    n, nf = ctypes.c_int(nbf), ctypes.c_int(nfocks)
+    info = ctypes.c_int(1)
+    lib().routec_fock_jk_cam(ptr(d), ptr(f), ctypes.byref(n), ctypes.byref(nf),
+                             ptr(cam_array(alpha, beta, mu, alpha_coul, beta_coul)), ctypes.byref(info))
+    return f.reshape(nfocks, -1), info.value
 
 
 def td_flags(apb=True, amb=False, tda=False, tda_coulomb=False):

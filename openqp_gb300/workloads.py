@@ -107,6 +107,25 @@ def density(bas, nocc, seed, S=None):
     return pack(2.0 * C @ C.T)
 
 
+def transition_densities(bas, nocc, nvec, seed, S=None):
+    """(nvec, nbf, nbf) AO transition densities X_v = C_occ Y_v C_vir^T of
+    seeded unit-norm occupied-virtual amplitudes Y_v, with C a full
+    Loewdin-orthonormal set of columns (the AO form of TDHF trial vectors,
+    tdhf_energy.F90:211-218)."""
+    if S is None:
+        S, _ = overlap_kinetic(bas)
+    rng = np.random.default_rng(seed)
+    n = S.shape[0]
+    C = loewdin_columns(S, n, rng)
+    Co, Cv = C[:, :nocc], C[:, nocc:]
+    out = np.empty((nvec, n, n))
+    for v in range(nvec):
+        Y = rng.standard_normal((nocc, n - nocc))
+        Y /= np.linalg.norm(Y)
+        out[v] = Co @ Y @ Cv.T
+    return out
+
+
 def density_open(bas, nalpha, nbeta, seed, S=None):
     """Packed (2, ntri) alpha/beta densities."""
     if S is None:

@@ -42,7 +42,10 @@ def lib():
         L.orc_shlden.argtypes = [ctypes.c_void_p, _d, ctypes.c_int, _d]
         L.orc_eri_quartet.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 4 + [_d]
         L.orc_md_quartet.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 4 + [_d]
+        L.orc_eri_quartet_att.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 4 + [ctypes.c_double, _d]
+        L.orc_md_quartet_att.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 4 + [ctypes.c_double, _d]
         L.orc_eri_dense.argtypes = [ctypes.c_void_p, _d]
+        L.orc_eri_dense_att.argtypes = [ctypes.c_void_p, ctypes.c_double, _d]
         L.orc_one_electron.argtypes = [ctypes.c_void_p, ctypes.c_int, _d, _d]
         L.orc_rys.argtypes = [ctypes.c_int, ctypes.c_double, _d, _d]
         L.orc_boys.argtypes = [ctypes.c_int, ctypes.c_double, _d]
@@ -54,6 +57,12 @@ def lib():
                                   ctypes.c_double, ctypes.c_int]
         L.orc_fock_mrsf.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_int]
+        L.orc_fock_jk_cam.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int]
+        L.orc_fock_td_cam.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int]
+        L.orc_fock_mrsf_cam.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int]
+        L.orc_schwarz_att.argtypes = [ctypes.c_void_p, _d, ctypes.c_int, ctypes.c_double]
+        L.orc_fock_td_sample.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d]
         _lib = L
     return _lib
 
@@ -124,6 +133,17 @@ class Oracle:
         lib().orc_fock_td(self.h, _p(fx), _p(pa), _p(ma), fx.shape[0], int(flags), se, sc, nthreads or os.cpu_count())
         return pa.transpose(0, 2, 1), ma.transpose(0, 2, 1)
 
+    def fock_td_sample(self, x, flags, stride, offset=0, se=1.0, sc=1.0, nthreads=None):
+        """fock_td over the bra pairs p (cost-sorted) with p % stride == offset.
+        Returns (apb, amb, stats) with set-up and loop seconds and the quartet count."""
+        x = np.asarray(x, dtype=np.float64)
+        fx = np.ascontiguousarray(x.transpose(0, 2, 1))
+        pa, ma = np.zeros_like(fx), np.zeros_like(fx)
+        st = np.zeros(3)
+        lib().orc_fock_td_sample(self.h, _p(fx), _p(pa), _p(ma), fx.shape[0], int(flags), se, sc,
+                                 nthreads or os.cpu_count(), int(stride), int(offset), _p(st))
+        return pa.transpose(0, 2, 1), ma.transpose(0, 2, 1), dict(t_setup=st[0], t_twoei=st[1], quartets=int(st[2]))
+
     def fock_mrsf(self, x, se=1.0, sc=1.0, nthreads=None):
         """int2_mrsf_data_t (nmat 7) / int2_umrsf_data_t (nmat 11) first pass:
         x (nvec, nmat, nbf, nbf) natural indexing -> f3 in the same indexing."""
@@ -134,6 +154,43 @@ class Oracle:
         if rc:
             raise ValueError("nmat must be 7 or 11")
         return out.transpose(3, 2, 1, 0)
+
+    # ---- CAM (int2_run_cam): regular pass + erf-attenuated pass ---------------
+    @staticmethod
+    def _cam(alpha, beta, mu, alpha_c, beta_c):
+        return np.array([alpha, beta, mu, alpha_c, beta_c], dtype=np.float64)
+
+    def fock_jk_cam(self, d, alpha, beta, mu, alpha_c=1.0, beta_c=0.0, urohf=None, nthreads=None):
+        d = np.ascontiguousarray(np.atleast_2d(d), dtype=np.float64)
+        if urohf is None:
+            urohf = d.shape[0] == 2
+        f = np.zeros_like(d)
+        c = self._cam(alpha, beta, mu, alpha_c, beta_c)
+        lib().orc_fock_jk_cam(self.h, _p(d), _p(f), d.shape[0], int(urohf), _p(c), nthreads or os.cpu_count())
+        return f
+
+    def fock_td_cam(self, x, flags, alpha, beta, mu, alpha_c=1.0, beta_c=0.0, nthreads=None):
+        x = np.asarray(x, dtype=np.float64)
+        fx = np.ascontiguousarray(x.transpose(0, 2, 1))
+        pa, ma = np.zeros_like(fx), np.zeros_like(fx)
+        c = self._cam(alpha, beta, mu, alpha_c, beta_c)
+        lib().orc_fock_td_cam(self.h, _p(fx), _p(pa), _p(ma), fx.shape[0], int(flags), _p(c),
+                              nthreads or os.cpu_count())
+        return pa.transpose(0, 2, 1), ma.transpose(0, 2, 1)
+
+    def fock_mrsf_cam(self, x, alpha, beta, mu, alpha_c=1.0, beta_c=0.0, nthreads=None):
+        x = np.asarray(x, dtype=np.float64)
+        fx = np.ascontiguousarray(x.transpose(3, 2, 1, 0))
+        out = np.zeros_like(fx)
+        c = self._cam(alpha, beta, mu, alpha_c, beta_c)
+        lib().orc_fock_mrsf_cam(self.h, _p(fx), _p(out), x.shape[0], x.shape[1], _p(c), nthreads or os.cpu_count())
+        return out.transpose(3, 2, 1, 0)
+
+    def schwarz_att(self, mu, nthreads=None):
+        ns = len(self.bas.am)
+        q = np.zeros(ns * ns)
+        lib().orc_schwarz_att(self.h, _p(q), nthreads or os.cpu_count(), float(mu))
+        return q.reshape(ns, ns)
 
     def schwarz(self, nthreads=None):
         ns = len(self.bas.am)
@@ -151,22 +208,25 @@ class Oracle:
     def _shape(self, i, j, k, l):
         return tuple(int(self.bas.naos[s]) for s in (i, j, k, l))
 
-    def eri_quartet(self, i, j, k, l):
+    def eri_quartet(self, i, j, k, l, mu=0.0):
+        """Rys block; mu > 0: the erf(mu r)/r operator."""
         sh = self._shape(i, j, k, l)
         out = np.zeros(int(np.prod(sh)))
-        lib().orc_eri_quartet(self.h, i, j, k, l, _p(out))
+        lib().orc_eri_quartet_att(self.h, i, j, k, l, float(mu), _p(out))
         return out.reshape(sh)
 
-    def md_quartet(self, i, j, k, l):
+    def md_quartet(self, i, j, k, l, mu=0.0):
+        """McMurchie-Davidson block; mu > 0: the erf(mu r)/r operator."""
         sh = self._shape(i, j, k, l)
         out = np.zeros(int(np.prod(sh)))
-        lib().orc_md_quartet(self.h, i, j, k, l, _p(out))
+        lib().orc_md_quartet_att(self.h, i, j, k, l, float(mu), _p(out))
         return out.reshape(sh)
 
-    def eri_dense(self):
+    def eri_dense(self, mu=0.0):
+        """Unscreened (nbf,)*4 tensor; mu > 0: the erf(mu r)/r operator."""
         n = self.nbf
         out = np.zeros(n ** 4)
-        lib().orc_eri_dense(self.h, _p(out))
+        lib().orc_eri_dense_att(self.h, float(mu), _p(out))
         return out.reshape(n, n, n, n)
 
     def one_electron(self, which, charges=None):

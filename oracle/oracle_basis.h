@@ -34,12 +34,16 @@ struct Basis {
 };
 
 // int2_cutoffs_t (source/integrals/int2_pairs.F90:27-35,285-294)
+// inv_mu2 = 1/mu^2 selects the erf-attenuated operator erf(mu r)/r of the
+// second CAM pass (int2.F90:538-584); 0 is the regular 1/r.
 struct Cutoffs {
   double integral, pair, quartet, exponent, pair2, quartet2;
-  static Cutoffs make(double cut, double pc, double qc, double ec) {
+  double inv_mu2 = 0.0;
+  static Cutoffs make(double cut, double pc, double qc, double ec, double inv_mu2 = 0.0) {
     Cutoffs c;
     c.integral = cut; c.pair = pc; c.quartet = qc; c.exponent = ec;
     c.pair2 = pc * pc; c.quartet2 = qc * qc;
+    c.inv_mu2 = inv_mu2;
     return c;
   }
 };

@@ -198,7 +198,9 @@ long rys_quartet(const Basis& B, const PairStore& PS, const Cutoffs& cut, const 
       const double x41 = pp + qq;
       if (fqz * fqz < cut.quartet2 * x41) continue;
       ++nprimq;
-      const double inv = 1.0 / x41;
+      // erf-attenuated: rho -> rho mu^2 / (mu^2 + rho), prefactor x sqrt(mu^2 / (mu^2 + rho))
+      // (int_rotaxis.F90:634-638), i.e. p + q -> p + q + p q / mu^2 (int_rys.F90:225-227)
+      const double inv = 1.0 / (cut.inv_mu2 != 0.0 ? x41 + pp * qq * cut.inv_mu2 : x41);
       const double rho = pp * qq * inv;
       const double P[3] = {PS.px[oP + p], PS.py[oP + p], PS.pz[oP + p]};
       const double PA[3] = {P[0] - S[0]->c[0], P[1] - S[0]->c[1], P[2] - S[0]->c[2]};

@@ -21,10 +21,19 @@ struct OrcStats {
   long long quartets, screened, prim_quartets, stored;
 };
 
+// int2_run_cam (int2.F90:538-584): pass 1 regular integrals with
+// scale_coulomb = alpha_c (1 by default), scale_exchange = alpha; pass 2
+// erf-attenuated integrals (own Schwarz bounds) with scale_coulomb = beta_c
+// (0 by default), scale_exchange = beta.
+struct Cam {
+  double alpha, beta, mu, alpha_c, beta_c;
+};
+
 // ints_exchange (int2.F90:1582-1737): Q(i,j) = sqrt(max |(ij|ij)|) with the
-// very tight cutoffs 1e-15 / 1e-17 / 1e-17 / 50.
-static void schwarz(const Basis& B, std::vector<double>& Q, int nthreads) {
-  const Cutoffs cut = Cutoffs::make(1e-15, 1e-17, 1e-17, 50.0);
+// very tight cutoffs 1e-15 / 1e-17 / 1e-17 / 50 (attenuated integrals when
+// inv_mu2 != 0, int2.F90:675-681).
+static void schwarz(const Basis& B, std::vector<double>& Q, int nthreads, double inv_mu2 = 0.0) {
+  const Cutoffs cut = Cutoffs::make(1e-15, 1e-17, 1e-17, 50.0, inv_mu2);
   PairStore PS;
   PS.build(B, cut);
   const int ns = B.nshell;
@@ -281,7 +290,8 @@ static double now() {
 // p mod stride == offset: the reference's own MPI work split
 // (int2.F90:759-761), used to time a bounded sample of a large build.
 static int fock_jk(OrcHandle* H, const double* d, double* fout, int nfocks, double se, double sc, int urohf,
-                   int nthreads, const double* qext, OrcStats* stats, int stride = 1, int offset = 0) {
+                   int nthreads, const double* qext, OrcStats* stats, int stride = 1, int offset = 0,
+                   const Cam* cam = nullptr) {
   const Basis& B = H->B;
   const double t0 = now();
   const double cut = H->cutoff;
@@ -298,10 +308,23 @@ static int fock_jk(OrcHandle* H, const double* d, double* fout, int nfocks, doub
   const size_t ntri = (size_t)B.nbf * (B.nbf + 1) / 2;
   const int nf = urohf ? 2 : nfocks;
   std::vector<double> facc((size_t)nthreads * nf * ntri, 0.0);
-  const TwoeiCounts cnt = twoei(B, PS, cutoffs, cut, Q, dsh, nthreads, stride, offset, [&](int tid) {
+  const double se1 = cam ? cam->alpha : se, sc1 = cam ? cam->alpha_c : sc;
+  TwoeiCounts cnt = twoei(B, PS, cutoffs, cut, Q, dsh, nthreads, stride, offset, [&](int tid) {
     double* f = facc.data() + (size_t)tid * nf * ntri;
-    return [=](Store& st) { update(st, d, f, nfocks, ntri, urohf, se, sc); };
+    return [=](Store& st) { update(st, d, f, nfocks, ntri, urohf, se1, sc1); };
   });
+  if (cam) {
+    const double inv_mu2 = 1.0 / (cam->mu * cam->mu);
+    const Cutoffs ca = Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0), inv_mu2);
+    std::vector<double> Qa;
+    schwarz(B, Qa, nthreads, inv_mu2);
+    const double se2 = cam->beta, sc2 = cam->beta_c;
+    const TwoeiCounts c2 = twoei(B, PS, ca, cut, Qa, dsh, nthreads, stride, offset, [&](int tid) {
+      double* f = facc.data() + (size_t)tid * nf * ntri;
+      return [=](Store& st) { update(st, d, f, nfocks, ntri, urohf, se2, sc2); };
+    });
+    cnt.nq += c2.nq; cnt.nsk += c2.nsk; cnt.npq += c2.npq; cnt.nst += c2.nst;
+  }
   // parallel_stop: reduce the replicated copies
   for (int t = 1; t < nthreads; ++t)
     for (size_t e = 0; e < (size_t)nf * ntri; ++e) facc[e] += facc[(size_t)t * nf * ntri + e];
@@ -466,6 +489,29 @@ static void mrsf_update(Store& st, const double* d3, const double* ds, double* f
   st.n = 0;
 }
 
+// int2_mrsf_data_t_update / int2_umrsf_data_t_update, pass 2 (CAM): only the
+// last component (agdlr), exchange with scale_exchange = beta
+// (tdhf_mrsf_lib.F90:314-328, 409-420).
+static void mrsf_update_pass2(Store& st, const double* d3, double* f3, int n, int nvec, int nmat, double se) {
+  auto at = [&](int v, int c, int r, int col) { return (((size_t)col * n + r) * nmat + c) * nvec + v; };
+  const int c = nmat - 1;
+  for (int e = 0; e < st.n; ++e) {
+    const int i = st.ids[4 * e], j = st.ids[4 * e + 1], k = st.ids[4 * e + 2], l = st.ids[4 * e + 3];
+    const double xval = st.val[e] * se;
+    for (int v = 0; v < nvec; ++v) {
+      f3[at(v, c, i, k)] -= xval * d3[at(v, c, j, l)];
+      f3[at(v, c, k, i)] -= xval * d3[at(v, c, l, j)];
+      f3[at(v, c, i, l)] -= xval * d3[at(v, c, j, k)];
+      f3[at(v, c, l, i)] -= xval * d3[at(v, c, k, j)];
+      f3[at(v, c, j, k)] -= xval * d3[at(v, c, i, l)];
+      f3[at(v, c, k, j)] -= xval * d3[at(v, c, l, i)];
+      f3[at(v, c, j, l)] -= xval * d3[at(v, c, i, k)];
+      f3[at(v, c, l, j)] -= xval * d3[at(v, c, k, i)];
+    }
+  }
+  st.n = 0;
+}
+
 struct Prepared {
   PairStore PS;
   Cutoffs cutoffs;
@@ -482,20 +528,40 @@ static void prepare(OrcHandle* H, int nthreads, Prepared& P) {
 // TDHF-type build: d2 (n, n, nvec) -> apb, amb (n, n, nvec), both overwritten;
 // int2_td_data_t_parallel_start/stop (tdhf_lib.F90:59-111): the replicated
 // copies are summed and every apb matrix symmetrised (mathlib.F90:134-143).
+// stride/offset > 1 restrict the bra pairs as in fock_jk (a timed sample);
+// stats: [0] seconds outside the quartet loop (pairs, Schwarz, shell
+// density, replicated copies and their reduction), [1] quartet-loop seconds,
+// [2] quartets evaluated.
 static int fock_td(OrcHandle* H, const double* d2, double* apb, double* amb, int nvec, int flags, double se,
-                   double sc, int nthreads) {
+                   double sc, int nthreads, int stride = 1, int offset = 0, double* stats = nullptr,
+                   const Cam* cam = nullptr) {
   const Basis& B = H->B;
   const int n = B.nbf;
   const size_t n2 = (size_t)n * n, tot = n2 * nvec;
+  const double t0 = now();
   Prepared P;
   prepare(H, nthreads, P);
   std::vector<double> dsh;
   shell_den_general(B, d2, nvec, n2, 1, n, dsh);
   std::vector<double> acc((size_t)nthreads * 2 * tot, 0.0);
-  twoei(B, P.PS, P.cutoffs, H->cutoff, P.Q, dsh, nthreads, 1, 0, [&](int tid) {
+  const double t1 = now();
+  const double se1 = cam ? cam->alpha : se, sc1 = cam ? cam->alpha_c : sc;
+  TwoeiCounts cnt = twoei(B, P.PS, P.cutoffs, H->cutoff, P.Q, dsh, nthreads, stride, offset, [&](int tid) {
     double* a = acc.data() + (size_t)tid * 2 * tot;
-    return [=](Store& st) { td_update(st, d2, a, a + tot, n, nvec, flags, se, sc); };
+    return [=](Store& st) { td_update(st, d2, a, a + tot, n, nvec, flags, se1, sc1); };
   });
+  if (cam) {
+    const double inv_mu2 = 1.0 / (cam->mu * cam->mu), cut = H->cutoff;
+    const Cutoffs ca = Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0), inv_mu2);
+    std::vector<double> Qa;
+    schwarz(B, Qa, nthreads, inv_mu2);
+    const double se2 = cam->beta, sc2 = cam->beta_c;
+    cnt.nq += twoei(B, P.PS, ca, cut, Qa, dsh, nthreads, stride, offset, [&](int tid) {
+      double* a = acc.data() + (size_t)tid * 2 * tot;
+      return [=](Store& st) { td_update(st, d2, a, a + tot, n, nvec, flags, se2, sc2); };
+    }).nq;
+  }
+  const double t2 = now();
   for (int t = 1; t < nthreads; ++t)
     for (size_t e = 0; e < 2 * tot; ++e) acc[e] += acc[(size_t)t * 2 * tot + e];
   for (int v = 0; v < nvec; ++v) {
@@ -507,6 +573,11 @@ static int fock_td(OrcHandle* H, const double* d2, double* apb, double* amb, int
   }
   std::memcpy(apb, acc.data(), sizeof(double) * tot);
   std::memcpy(amb, acc.data() + tot, sizeof(double) * tot);
+  if (stats) {
+    stats[0] = (t1 - t0) + (now() - t2);  // everything but the quartet loop
+    stats[1] = t2 - t1;
+    stats[2] = (double)cnt.nq;
+  }
   return 0;
 }
 
@@ -514,7 +585,7 @@ static int fock_td(OrcHandle* H, const double* d2, double* apb, double* amb, int
 // int2_mrsf_data_t_parallel_start/stop (tdhf_mrsf_lib.F90:58-149); the
 // screening density is the last component (tdhf_mrsf_lib.F90:171-185).
 static int fock_mrsf(OrcHandle* H, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
-                     int nthreads) {
+                     int nthreads, const Cam* cam = nullptr) {
   const Basis& B = H->B;
   const int n = B.nbf;
   const bool umrsf = nmat == 11;
@@ -537,10 +608,22 @@ static int fock_mrsf(OrcHandle* H, const double* d3, double* f3, int nvec, int n
   }
   std::vector<double> acc((size_t)nthreads * tot, 0.0);
   const double* dsp = ds.data();
+  const double se1 = cam ? cam->alpha : se, sc1 = cam ? cam->alpha_c : sc;
   twoei(B, P.PS, P.cutoffs, H->cutoff, P.Q, dsh, nthreads, 1, 0, [&](int tid) {
     double* a = acc.data() + (size_t)tid * tot;
-    return [=](Store& st) { mrsf_update(st, d3, dsp, a, n, nvec, nmat, umrsf, se, sc); };
+    return [=](Store& st) { mrsf_update(st, d3, dsp, a, n, nvec, nmat, umrsf, se1, sc1); };
   });
+  if (cam) {
+    const double inv_mu2 = 1.0 / (cam->mu * cam->mu), cut = H->cutoff;
+    const Cutoffs ca = Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0), inv_mu2);
+    std::vector<double> Qa;
+    schwarz(B, Qa, nthreads, inv_mu2);
+    const double se2 = cam->beta;
+    twoei(B, P.PS, ca, cut, Qa, dsh, nthreads, 1, 0, [&](int tid) {
+      double* a = acc.data() + (size_t)tid * tot;
+      return [=](Store& st) { mrsf_update_pass2(st, d3, a, n, nvec, nmat, se2); };
+    });
+  }
   for (int t = 1; t < nthreads; ++t)
     for (size_t e = 0; e < tot; ++e) acc[e] += acc[(size_t)t * tot + e];
   std::memcpy(f3, acc.data(), sizeof(double) * tot);
@@ -610,8 +693,36 @@ int orc_fock_td(void* h, const double* d2, double* apb, double* amb, int nvec, i
   return fock_td((OrcHandle*)h, d2, apb, amb, nvec, flags, se, sc, nthreads);
 }
 
+// The same build over the bra pairs p with p mod stride == offset; stats3 as fock_td.
+int orc_fock_td_sample(void* h, const double* d2, double* apb, double* amb, int nvec, int flags, double se,
+                       double sc, int nthreads, int stride, int offset, double* stats3) {
+  return fock_td((OrcHandle*)h, d2, apb, amb, nvec, flags, se, sc, nthreads, stride, offset, stats3);
+}
+
 int orc_fock_mrsf(void* h, const double* d3, double* f3, int nvec, int nmat, double se, double sc, int nthreads) {
   return fock_mrsf((OrcHandle*)h, d3, f3, nvec, nmat, se, sc, nthreads);
+}
+
+// CAM (two-pass) forms: cam5 = {alpha, beta, mu, alpha_coulomb, beta_coulomb}.
+int orc_fock_jk_cam(void* h, const double* d, double* f, int nfocks, int urohf, const double* cam5, int nthreads) {
+  const Cam cam{cam5[0], cam5[1], cam5[2], cam5[3], cam5[4]};
+  return fock_jk((OrcHandle*)h, d, f, nfocks, 0.0, 0.0, urohf, nthreads, nullptr, nullptr, 1, 0, &cam);
+}
+int orc_fock_td_cam(void* h, const double* d2, double* apb, double* amb, int nvec, int flags, const double* cam5,
+                    int nthreads) {
+  const Cam cam{cam5[0], cam5[1], cam5[2], cam5[3], cam5[4]};
+  return fock_td((OrcHandle*)h, d2, apb, amb, nvec, flags, 0.0, 0.0, nthreads, 1, 0, nullptr, &cam);
+}
+int orc_fock_mrsf_cam(void* h, const double* d3, double* f3, int nvec, int nmat, const double* cam5, int nthreads) {
+  const Cam cam{cam5[0], cam5[1], cam5[2], cam5[3], cam5[4]};
+  return fock_mrsf((OrcHandle*)h, d3, f3, nvec, nmat, 0.0, 0.0, nthreads, &cam);
+}
+
+// Schwarz bounds of the erf-attenuated operator (mu > 0).
+void orc_schwarz_att(void* h, double* q, int nthreads, double mu) {
+  std::vector<double> Q;
+  schwarz(((OrcHandle*)h)->B, Q, nthreads, 1.0 / (mu * mu));
+  std::memcpy(q, Q.data(), sizeof(double) * Q.size());
 }
 
 void orc_schwarz(void* h, double* q, int nthreads) {
@@ -628,10 +739,17 @@ void orc_shlden(void* h, const double* d, int nfocks, double* dsh) {
 
 // Normalised (pure) shell-quartet block in the caller's (i,j,k,l) order,
 // out[a][b][c][d]; screening cutoffs of a Fock build with the handle's cutoff.
+int orc_eri_quartet_att(void* h, int i, int j, int k, int l, double mu, double* out);
 int orc_eri_quartet(void* h, int i, int j, int k, int l, double* out) {
+  return orc_eri_quartet_att(h, i, j, k, l, 0.0, out);
+}
+
+// The same with the erf(mu r)/r operator (mu <= 0: regular 1/r).
+int orc_eri_quartet_att(void* h, int i, int j, int k, int l, double mu, double* out) {
   const Basis& B = ((OrcHandle*)h)->B;
   const double cut = ((OrcHandle*)h)->cutoff;
-  const Cutoffs cutoffs = Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0));
+  const Cutoffs cutoffs =
+      Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0), mu > 0 ? 1.0 / (mu * mu) : 0.0);
   PairStore PS;
   PS.build(B, cutoffs);
   const int ids[4] = {i, j, k, l};
@@ -660,10 +778,14 @@ int orc_eri_quartet(void* h, int i, int j, int k, int l, double* out) {
 
 // Dense (nbf^4) ERI tensor through the same engine without any screening
 // (tests of the J/K semantics on small systems).
-int orc_eri_dense(void* h, double* eri) {
+int orc_eri_dense_att(void* h, double mu, double* eri);
+int orc_eri_dense(void* h, double* eri) { return orc_eri_dense_att(h, 0.0, eri); }
+
+// mu > 0: the erf(mu r)/r operator.
+int orc_eri_dense_att(void* h, double mu, double* eri) {
   const Basis& B = ((OrcHandle*)h)->B;
   const int nb = B.nbf, ns = B.nshell;
-  const Cutoffs cutoffs = Cutoffs::make(0.0, 0.0, 0.0, 1e300);
+  const Cutoffs cutoffs = Cutoffs::make(0.0, 0.0, 0.0, 1e300, mu > 0 ? 1.0 / (mu * mu) : 0.0);
   PairStore PS;
   PS.build(B, cutoffs);
   QuartetWork W;

@@ -113,7 +113,15 @@ extern "C" {
 
 // Cartesian-normalised (pure-projected) ERI block in the caller's order, by
 // McMurchie-Davidson, no screening.
+int orc_md_quartet_att(void* h, int i, int j, int k, int l, double mu, double* out);
 int orc_md_quartet(void* h, int i, int j, int k, int l, double* out) {
+  return orc_md_quartet_att(h, i, j, k, l, 0.0, out);
+}
+
+// erf(mu r)/r (mu > 0): the operator's Fourier transform 4 pi k^-2 exp(-k^2 / 4 mu^2)
+// turns the Hermite Coulomb exponent alpha = pq/(p+q) into alpha mu^2 / (alpha + mu^2)
+// and scales the prefactor by sqrt(mu^2 / (alpha + mu^2)).
+int orc_md_quartet_att(void* h, int i, int j, int k, int l, double mu, double* out) {
   const Basis& B = ((OrcHandleView*)h)->B;
   const int sh[4] = {i, j, k, l};
   const Shell* S[4] = {&B.sh[i], &B.sh[j], &B.sh[k], &B.sh[l]};
@@ -149,10 +157,15 @@ int orc_md_quartet(void* h, int i, int j, int k, int l, double* out) {
           const double Kcd = B.cc[S[2]->poff + pc] * B.cc[S[3]->poff + pd] * std::exp(-c * dd / q * cd2);
           Herm1D Ecd[3];
           for (int d = 0; d < 3; ++d) Ecd[d].build(S[2]->am, S[3]->am, q, Q[d] - S[2]->c[d], Q[d] - S[3]->c[d]);
-          const double alpha = p * q / (p + q);
+          double alpha = p * q / (p + q);
+          double att = 1.0;
+          if (mu > 0) {
+            att = mu * mu / (alpha + mu * mu);
+            alpha *= att;
+          }
           HermR R;
           R.build(Lab + Lcd, alpha, P[0] - Q[0], P[1] - Q[1], P[2] - Q[2]);
-          const double pref = 2.0 * std::pow(PI, 2.5) / (p * q * std::sqrt(p + q)) * Kab * Kcd;
+          const double pref = 2.0 * std::pow(PI, 2.5) / (p * q * std::sqrt(p + q)) * std::sqrt(att) * Kab * Kcd;
           int idx = 0;
           for (int ia = 0; ia < n[0]; ++ia)
             for (int ib = 0; ib < n[1]; ++ib)

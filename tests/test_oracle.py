@@ -11,7 +11,10 @@ Pins, in order of strength:
   * the response digestions (int2_td_data_t, int2_mrsf_data_t,
     int2_umrsf_data_t) against dense J/K contractions of general matrices,
     and OpenQP's golden TDHF excitation energies (examples/TDHF) from full
-    A+B / A-B matrices built with the restated int2_td_data_t.
+    A+B / A-B matrices built with the restated int2_td_data_t;
+  * the erf-attenuated integrals of the CAM pass (Rys with p + q -> p + q +
+    pq/mu^2) against McMurchie-Davidson with the attenuated Hermite exponent,
+    and the two-pass CAM builds against dense contractions.
 """
 import json
 import os
@@ -237,3 +240,55 @@ def test_golden_tdhf_excitation_energies(oracle_lib):
     w, apb, amb = rpa.rpa_energies(lambda x, fl: o.fock_td(x, fl), C, e, 5)
     assert np.abs(apb - apb.T).max() < 1e-12 and np.abs(amb - amb.T).max() < 1e-12
     assert np.abs(w[:3] - np.array(case["td_energies"])).max() < 5e-7
+
+
+@pytest.mark.parametrize("basis", ["6-31g*", "cc-pvdz"])
+def test_attenuated_rys_matches_mcmurchie_davidson(oracle_lib, basis):
+    bas = h2o_basis(basis)
+    o = oracle_lib.Oracle(bas, cutoff=1e-14)
+    ns = len(bas.am)
+    rng = np.random.default_rng(1)
+    for _ in range(60):
+        i, j, k, l = (int(v) for v in rng.integers(0, ns, 4))
+        for mu in (0.2, 0.33, 1.0, 4.0):
+            a, b = o.eri_quartet(i, j, k, l, mu), o.md_quartet(i, j, k, l, mu)
+            assert np.abs(a - b).max() < 1e-14 * max(1.0, np.abs(b).max())
+
+
+def test_cam_builds_match_dense_contraction(oracle_lib):
+    """int2_run_cam: pass 1 (1/r) with alpha, alpha_c, pass 2 (erf(mu r)/r,
+    attenuated Schwarz) with beta, beta_c, for the RHF / UROHF Fock build, the
+    TD build and the MRSF build (pass 2: last component, exchange only)."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(1, workloads.cube_edge_like_c1(1), seed=2, basis="6-31g(d)")
+    o = oracle_lib.Oracle(bas, cutoff=1e-12)
+    n = o.nbf
+    e1, e2 = o.eri_dense(), o.eri_dense(mu=0.33)
+    J1, K1 = (lambda D: np.einsum("ijkl,kl->ij", e1, D)), (lambda D: np.einsum("ijkl,jl->ik", e1, D))
+    J2, K2 = (lambda D: np.einsum("ijkl,kl->ij", e2, D)), (lambda D: np.einsum("ijkl,jl->ik", e2, D))
+    from openqp_gb300.basis import pack, unpack
+    al, be, mu, ac, bc = 0.19, 0.46, 0.33, 1.0, 0.2
+    d = workloads.density(bas, 5, 0)
+    D = unpack(d, n)
+    f = o.fock_jk_cam(d, al, be, mu, ac, bc)[0]
+    ref = pack(ac * J1(D) - 0.5 * al * K1(D) + bc * J2(D) - 0.5 * be * K2(D))
+    assert np.abs(f - ref).max() < 1e-11
+    du = workloads.density_open(bas, 5, 4, 1)
+    Da, Db = unpack(du[0], n), unpack(du[1], n)
+    fu = o.fock_jk_cam(du, al, be, mu, ac, bc)
+    for s, Ds in enumerate((Da, Db)):
+        ref = pack(ac * J1(Da + Db) - al * K1(Ds) + bc * J2(Da + Db) - be * K2(Ds))
+        assert np.abs(fu[s] - ref).max() < 1e-11
+    x = np.random.default_rng(0).standard_normal((2, n, n)) * 0.3
+    pa, ma = o.fock_td_cam(x, 3, al, be, mu, ac, bc)
+    for v in range(2):
+        X = x[v]
+        Xs, Xa = 0.5 * (X + X.T), 0.5 * (X - X.T)
+        assert np.abs(pa[v] - (4 * ac * J1(X) - 2 * al * K1(Xs) + 4 * bc * J2(X) - 2 * be * K2(Xs))).max() < 1e-11
+        assert np.abs(ma[v] - (-2 * al * K1(Xa) - 2 * be * K2(Xa))).max() < 1e-11
+    x3 = np.random.default_rng(1).standard_normal((1, 7, n, n)) * 0.3
+    f3 = o.fock_mrsf_cam(x3, al, be, mu, ac, bc)
+    for m in range(7):
+        X = x3[0, m]
+        ref = -al * K1(X) + (ac * J1(X) if m < 4 else 0) - (be * K2(X) if m == 6 else 0)
+        assert np.abs(f3[0, m] - ref).max() < 1e-11
