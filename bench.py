@@ -20,6 +20,7 @@ screening threshold 1e-10.
 Multi-GPU runs are independent replicas (one molecule per rank, no collective).
 """
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -65,6 +66,10 @@ WORKLOADS = {
                              edge=9.52, seed=0, basis="6-31g(d)", cutoff=1e-10, td=True, nvec=8),
     "td_water32_ccpvdz": dict(name="(H2O)32 cc-pVDZ spherical TDHF A+B and A-B build, 8 trial vectors", nwater=32,
                               edge=14.0, seed=0, basis="cc-pvdz", cutoff=1e-10, td=True, nvec=8),
+    # CAM (range-separated) RHF build of the headline cluster: CAM-B3LYP's alpha, beta, mu
+    "cam_water32_ccpvdz": dict(name="(H2O)32 cc-pVDZ spherical RHF CAM J+K build (alpha 0.19, beta 0.46, mu 0.33)",
+                               nwater=32, edge=14.0, seed=0, basis="cc-pvdz", cutoff=1e-10,
+                               cam=(0.19, 0.46, 0.33, 1.0, 0.0)),
     # (dd|dd) only: one Cartesian d shell (6-31G(d) carbon d, exponent 0.8) on each
     # point of a 4 x 4 x 4 cubic lattice of spacing 1.54 A, so that all 2080 pairs overlap
     "dd_only": dict(name="(dd|dd)-only: 64 Cartesian d shells (exponent 0.8) on a 4x4x4 lattice, 1.54 A spacing",
@@ -306,9 +311,143 @@ def run_td(args):
         print(json.dumps(line), flush=True)
 
 
+def cpu_baseline_cam(bas, d, budget_s):
+    """The oracle's two-pass CAM build (all host cores) over 1/stride of the
+    cost-sorted bra pairs, scaled, plus the work outside the quartet loops."""
+    from oracle import oracle
+    oracle.build()
+    o = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"])
+    cores = os.cpu_count()
+    cam = WORKLOAD["cam"]
+    stride = 997
+    for _ in range(4):
+        _, st = o.fock_jk_cam_sample(d, *cam[:3], stride, 0, *cam[3:], nthreads=cores)
+        if stride == 1 or st["t_twoei"] >= 0.5 * budget_s:
+            break
+        stride = max(1, int(stride * st["t_twoei"] / budget_s))
+    t = st["t_twoei"] * stride + (st["t_total"] - st["t_twoei"])
+    return {"value": 1.0 / t, "unit": "builds/s", "cores": cores, "kind": "port",
+            "sample": "oracle two-pass CAM build (1/r and erf(mu r)/r, own Schwarz bounds) over 1/%d of the "
+                      "cost-sorted bra shell pairs, x%d, plus set-up; %d quartets in the sample"
+                      % (stride, stride, st["quartets"])}
+
+
+def run_cam(args):
+    """CAM builds/s: OpenQP's int2_run_cam (1/r pass, erf(mu r)/r pass with its
+    own Schwarz bounds) of the workload density, device-resident; e2e through
+    routec_fock_jk_cam with host buffers."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    from openqp_gb300 import build as bld
+    bld.build()
+    from openqp_gb300._lib import lib
+    from openqp_gb300.fock import FockBuilder, cam_array, class_flops, class_labels, fp64_peak_tflops, \
+        routec_fock_jk_cam, routec_init, ptr
+    bas, d = make_workload()
+    fb = FockBuilder(bas, cutoff=WORKLOAD["cutoff"])
+    fb.set_precision(args.precision, args.mixed_threshold)
+    cam = WORKLOAD["cam"]
+    ca = cam_array(*cam)
+    dt = torch.from_numpy(d[None]).cuda()
+    out = torch.empty_like(dt)
+    st = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def build():
+        rc = lib().oqpg_fock_jk_cam_device(fb.h, ctypes.c_void_p(dt.data_ptr()), ctypes.c_void_p(out.data_ptr()), 1,
+                                           ptr(ca), ctypes.c_void_p(st.cuda_stream))
+        if rc:
+            raise RuntimeError("oqpg_fock_jk_cam_device returned %d" % rc)
+
+    for _ in range(args.warmup):
+        build()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        build()
+        e1.record(st)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clocks = sampler.stop()
+    tsum = max_over_ranks(sum(times) / 1000.0)
+    value = ws * args.steps / tsum
+    # the plain (1/r only) build of the same density for comparison
+    tp = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fb.fock_jk_device(dt, out=out, stream=st)
+        e1.record(st)
+        e1.synchronize()
+        tp.append(e0.elapsed_time(e1))
+    stats = fb.stats()   # the last pass recorded: the plain build
+    e2e_t = []
+    if not args.no_e2e:
+        routec_init(bas, WORKLOAD["cutoff"])
+        routec_fock_jk_cam(d, bas.nbf, 1, *cam)
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            _, info = routec_fock_jk_cam(d, bas.nbf, 1, *cam)
+            e2e_t.append(time.perf_counter() - t0)
+            if info:
+                raise RuntimeError("routec_fock_jk_cam returned %d" % info)
+    e2e = ws * args.steps / max_over_ranks(sum(e2e_t)) if e2e_t else float("nan")
+    labels = class_labels()
+    ms = np.array(stats["ms_per_class"])
+    cdom = int(np.argmax(ms))
+    pure = bool(bas.harmonic.any())
+    achieved = class_flops(cdom, stats["prim_per_class"][cdom], stats["per_class"][cdom], pure=pure) / \
+        (ms[cdom] * 1e-3) / 1e12
+    peak = fp64_peak_tflops()
+    line = {"metric": "CAM J+K Fock builds/s", "value": value, "unit": "builds/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tsum / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else args.precision,
+            "data": "synthetic (seeded water cluster and Loewdin density)",
+            "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "cutoff": WORKLOAD["cutoff"],
+                       "cam": {"alpha": cam[0], "beta": cam[1], "mu": cam[2], "alpha_coulomb": cam[3],
+                               "beta_coulomb": cam[4]},
+                       "l2": "flushed (256 MB write) before every timed step"},
+            "e2e": {"value": e2e, "unit": "builds/s", "h2d_bytes_per_step": int(d.nbytes),
+                    "d2h_bytes_per_step": int(d.nbytes)},
+            "roofline": {"bound": "fp64", "kernel": labels[cdom] + " (1/r pass)", "achieved": achieved,
+                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                         "peak_source": "measured: FP64 FMA-chain probe on this device",
+                         "kernel_ms": float(ms[cdom])},
+            "plain_builds_per_s": args.steps / (sum(tp) / 1000.0), "clocks": clocks}
+    if not args.no_cpu and rank == 0:
+        line["cpu_baseline"] = cpu_baseline_cam(bas, d, args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
+        return
+    if WORKLOAD.get("cam"):
+        bas, d = make_workload(overlap="oracle")
+        vals = [cpu_baseline_cam(bas, d, args.cpu_budget)["value"] for _ in range(max(1, args.steps))]
+        cb = cpu_baseline_cam(bas, d, args.cpu_budget)
+        v = statistics.median(vals)
+        cb["value"] = v
+        line = {"impl": "reference", "metric": "CAM J+K Fock builds/s", "value": v, "unit": "builds/s",
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "cutoff": WORKLOAD["cutoff"]},
+                "cpu_baseline": cb, "e2e": {"value": v, "unit": "builds/s", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
         return
     if WORKLOAD.get("td"):
         bas, x = td_workload(overlap="oracle")
@@ -760,7 +899,6 @@ def run_batch(args):
     # e2e through the batch seam with host buffers (H2D + graph + D2H per step)
     e2e = None
     if not args.no_e2e:
-        import ctypes
         from openqp_gb300._lib import lib, ptr, _i
         from openqp_gb300.fock import _batch_arrays
         nsh, nat, k = _batch_arrays(bases)
@@ -889,6 +1027,8 @@ def main():
         run_grad(args)
     elif WORKLOAD.get("td"):
         run_td(args)
+    elif WORKLOAD.get("cam"):
+        run_cam(args)
     elif WORKLOAD.get("scf"):
         run_scf_bench(args)
     else:

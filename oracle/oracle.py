@@ -58,6 +58,8 @@ def lib():
         L.orc_fock_mrsf.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_int]
         L.orc_fock_jk_cam.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int]
+        L.orc_fock_jk_cam_sample.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, _d]
         L.orc_fock_td_cam.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int]
         L.orc_fock_mrsf_cam.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int]
         L.orc_schwarz_att.argtypes = [ctypes.c_void_p, _d, ctypes.c_int, ctypes.c_double]
@@ -168,6 +170,19 @@ class Oracle:
         c = self._cam(alpha, beta, mu, alpha_c, beta_c)
         lib().orc_fock_jk_cam(self.h, _p(d), _p(f), d.shape[0], int(urohf), _p(c), nthreads or os.cpu_count())
         return f
+
+    def fock_jk_cam_sample(self, d, alpha, beta, mu, stride, offset=0, alpha_c=1.0, beta_c=0.0, urohf=None,
+                           nthreads=None):
+        """fock_jk_cam over the bra pairs p with p % stride == offset (both passes). Returns (f, stats)."""
+        d = np.ascontiguousarray(np.atleast_2d(d), dtype=np.float64)
+        if urohf is None:
+            urohf = d.shape[0] == 2
+        f = np.zeros_like(d)
+        st = np.zeros(8)
+        c = self._cam(alpha, beta, mu, alpha_c, beta_c)
+        lib().orc_fock_jk_cam_sample(self.h, _p(d), _p(f), d.shape[0], int(urohf), _p(c), nthreads or os.cpu_count(),
+                                     int(stride), int(offset), _p(st))
+        return f, dict(t_init=st[0], t_schwarz=st[1], t_twoei=st[2], t_total=st[3], quartets=int(st[4]))
 
     def fock_td_cam(self, x, flags, alpha, beta, mu, alpha_c=1.0, beta_c=0.0, nthreads=None):
         x = np.asarray(x, dtype=np.float64)

@@ -708,6 +708,19 @@ int orc_fock_jk_cam(void* h, const double* d, double* f, int nfocks, int urohf, 
   const Cam cam{cam5[0], cam5[1], cam5[2], cam5[3], cam5[4]};
   return fock_jk((OrcHandle*)h, d, f, nfocks, 0.0, 0.0, urohf, nthreads, nullptr, nullptr, 1, 0, &cam);
 }
+// CAM build over the bra pairs p with p mod stride == offset (both passes); stats6 as orc_fock_jk.
+int orc_fock_jk_cam_sample(void* h, const double* d, double* f, int nfocks, int urohf, const double* cam5,
+                           int nthreads, int stride, int offset, double* stats6) {
+  const Cam cam{cam5[0], cam5[1], cam5[2], cam5[3], cam5[4]};
+  OrcStats st;
+  const int rc = fock_jk((OrcHandle*)h, d, f, nfocks, 0.0, 0.0, urohf, nthreads, nullptr, &st, stride, offset, &cam);
+  if (stats6) {
+    stats6[0] = st.t_init; stats6[1] = st.t_schwarz; stats6[2] = st.t_twoei; stats6[3] = st.t_total;
+    stats6[4] = (double)st.quartets; stats6[5] = (double)st.screened; stats6[6] = (double)st.prim_quartets;
+    stats6[7] = (double)st.stored;
+  }
+  return rc;
+}
 int orc_fock_td_cam(void* h, const double* d2, double* apb, double* amb, int nvec, int flags, const double* cam5,
                     int nthreads) {
   const Cam cam{cam5[0], cam5[1], cam5[2], cam5[3], cam5[4]};
