@@ -47,5 +47,9 @@ cudaError_t launch_group0(int c, bool pure, int mode, const BuildArgs& a, int ns
 cudaError_t launch_group1(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 cudaError_t launch_group2(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 cudaError_t launch_group3(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group4(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group5(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group6(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group7(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 
 }  // namespace oqpg

@@ -10,10 +10,6 @@ cudaError_t launch_group0(int c, bool pure, int mode, const BuildArgs& a, int ns
     case 1: return launch_cls<0, 0, 0, 1>(pure, mode, a, nsm, st);
     case 2: return launch_cls<0, 0, 0, 2>(pure, mode, a, nsm, st);
     case 3: return launch_cls<0, 0, 1, 1>(pure, mode, a, nsm, st);
-    case 4: return launch_cls<0, 0, 1, 2>(pure, mode, a, nsm, st);
-    case 6: return launch_cls<0, 1, 0, 1>(pure, mode, a, nsm, st);
-    case 7: return launch_cls<0, 1, 0, 2>(pure, mode, a, nsm, st);
-    case 8: return launch_cls<0, 1, 1, 1>(pure, mode, a, nsm, st);
     default: return cudaErrorInvalidValue;
   }
 }

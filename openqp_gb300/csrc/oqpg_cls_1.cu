@@ -6,12 +6,10 @@ namespace oqpg {
 
 cudaError_t launch_group1(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
   switch (c) {
-    case 5: return launch_cls<0, 0, 2, 2>(pure, mode, a, nsm, st);
-    case 9: return launch_cls<0, 1, 1, 2>(pure, mode, a, nsm, st);
-    case 10: return launch_cls<0, 1, 2, 2>(pure, mode, a, nsm, st);
-    case 11: return launch_cls<0, 2, 0, 2>(pure, mode, a, nsm, st);
-    case 12: return launch_cls<0, 2, 1, 1>(pure, mode, a, nsm, st);
-    case 15: return launch_cls<1, 1, 1, 1>(pure, mode, a, nsm, st);
+    case 4: return launch_cls<0, 0, 1, 2>(pure, mode, a, nsm, st);
+    case 6: return launch_cls<0, 1, 0, 1>(pure, mode, a, nsm, st);
+    case 7: return launch_cls<0, 1, 0, 2>(pure, mode, a, nsm, st);
+    case 8: return launch_cls<0, 1, 1, 1>(pure, mode, a, nsm, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -255,16 +255,15 @@ __device__ __forceinline__ double rsqrt_t(double x) { return rsqrt64(x); }
 __device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
 __device__ __forceinline__ dfl rsqrt_t(dfl x) { return df_rsqrt(x); }
 
-// att = 1/mu^2 > 0 evaluates the erf(mu r)/r operator of the CAM pass: p + q
+// ATT, att = 1/mu^2: the erf(mu r)/r operator of the CAM pass: p + q
 // becomes p + q + pq/mu^2 in rho, in the prefactor and in the recurrence
 // coefficients (int_rys.F90:225-240; int_rotaxis.F90:634-638 writes the same
 // as rho mu^2/(mu^2 + rho)).  The primitive screen keeps the plain p + q.
-template <typename T, typename PP>
-__device__ __forceinline__ void prim_setup(const PP& bp, const PP& kp, PrimQuartet<T>& o, bool has_att = false,
-                                           T att = T(0)) {
+template <typename T, bool ATT = false, typename PP>
+__device__ __forceinline__ void prim_setup(const PP& bp, const PP& kp, PrimQuartet<T>& o, T att = T(0)) {
   const T fqz = bp.sp * kp.sp;
   T s = bp.p + kp.p;
-  if (has_att) s = fma(bp.p * kp.p, att, s);
+  if constexpr (ATT) s = fma(bp.p * kp.p, att, s);
   const T y = rsqrt_t(s);
   o.inv = y * y;
   o.qi = kp.p * o.inv;
@@ -452,9 +451,10 @@ __device__ __forceinline__ void quartet_geometry(const BuildArgs& a, uint2 qd, P
 // (c = kq * nP + kb) of one contracted quartet.  Each iteration of the
 // arithmetic body computes one surviving candidate of this lane: the cheap
 // FP32 scan skips screened candidates without holding the warp in the body.
-template <int LA, int LB, int LC, int LD, typename T>
-__device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P, const PairDev& Q, const T AB[3],
-                                            const T CD[3], int first, int step, T* acc, unsigned long long& nprim) {
+template <int LA, int LB, int LC, int LD, typename T, bool ATT>
+__device__ __forceinline__ void small_prims_impl(const BuildArgs& a, const PairDev& P, const PairDev& Q,
+                                                 const T AB[3], const T CD[3], int first, int step, T* acc,
+                                                 unsigned long long& nprim) {
   using K = Cls<LA, LB, LC, LD>;
   using PP = typename PrimT<T>::type;
   constexpr int NE = K::NE, NR = K::NR, N2D = K::N2D;
@@ -479,7 +479,7 @@ __device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P
     prim_load(bpp + cb, bp);
     prim_load(kpp + cq, kp);
     PrimQuartet<T> pq;
-    prim_setup<T>(bp, kp, pq, a.inv_mu2 != 0.0, (T)a.inv_mu2);
+    prim_setup<T, ATT>(bp, kp, pq, (T)a.inv_mu2);
     ++nprim;
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
@@ -503,6 +503,15 @@ __device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P
         acc[e] = fma(I[0][K::off2d(e, 0)] * I[1][K::off2d(e, 1)], I[2][K::off2d(e, 2)], acc[e]);
     }
   }
+}
+
+// The attenuated (CAM) operator is a separate instance of the primitive
+// loop, chosen once per quartet, so the plain loop carries no extra work.
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P, const PairDev& Q, const T AB[3],
+                                            const T CD[3], int first, int step, T* acc, unsigned long long& nprim) {
+  if (a.inv_mu2 != 0.0) small_prims_impl<LA, LB, LC, LD, T, true>(a, P, Q, AB, CD, first, step, acc, nprim);
+  else small_prims_impl<LA, LB, LC, LD, T, false>(a, P, Q, AB, CD, first, step, acc, nprim);
 }
 
 // Normalisation, pure projection, element cutoff and digestion of one
@@ -708,7 +717,11 @@ template <int LA, int LB, int LC, int LD, bool PURE>
 struct TeamSmem {
   using K = Cls<LA, LB, LC, LD>;
   using E = Epi<LA, LB, LC, LD, PURE>;
-  static constexpr int PH1 = 2 * K::NR + K::NR * 3 * K::N2D;
+  // primitive quartets that k_team evaluates side by side: each takes 3 NR
+  // lanes in the 2D-table phase (one per root and dimension); the largest
+  // classes, whose element phase dominates, keep one
+  static constexpr int G = (K::NE > 400 || 32 / (3 * K::NR) < 1) ? 1 : 32 / (3 * K::NR);
+  static constexpr int PH1 = G * (2 * K::NR + K::NR * 3 * K::N2D);
   static constexpr int DJ = E::A * E::B + E::C * E::D;
   static constexpr int DK = E::A * E::C + E::A * E::D + E::B * E::C + E::B * E::D;
   // [0, NE): the quartet's accumulators (lane-owned elements), then the
@@ -733,7 +746,7 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
   const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
   // ---- epilogue: V = normalised block in smem, pure projection in place
   T* Tm = W + NE;
-#pragma unroll
+#pragma unroll (KE <= 8 ? KE : 4)
   for (int k = 0; k < KE; ++k) {
     const int e = lane + 32 * k;
     if (e < NE) {
@@ -900,9 +913,12 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
   T* smem = reinterpret_cast<T*>(smem_raw);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* W = smem + warp * SM::PER_WARP;
+  constexpr int G = SM::G;
   T* V = W;                // [NE] accumulators, then the normalised block
-  T* RT = W + NE;          // 2*NR: x_r, w_r * pref
-  T* I2 = RT + 2 * NR;     // [r][d][N2D]
+  T* RT = W + NE;          // [g][2 NR]: x_r, w_r * pref of group g
+  T* I2 = RT + G * 2 * NR; // [g][r][d][N2D]
+  // lane groups of 3 NR lanes, one primitive quartet each (lanes >= 3 NR G idle)
+  const int grp = lane / (3 * NR), gl = lane - grp * (3 * NR);
   for (int e = threadIdx.x; e < NE; e += blockDim.x) {
     const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
               id = e % K::ND;
@@ -925,31 +941,53 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
     PairDev P, Q;
     T AB[3], CD[3];
     quartet_geometry<T>(a, qd, P, Q, AB, CD);
-#pragma unroll
+#pragma unroll (KE <= 8 ? KE : 4)
     for (int k = 0; k < KE; ++k)
       if (lane + 32 * k < NE) V[lane + 32 * k] = 0;
     const PP* bpp = prims_of<T>(a) + P.poff;
     const PP* kpp = prims_of<T>(a) + Q.poff;
-    for (int kq = 0; kq < Q.pcnt; ++kq) {
-      PP kp, bn;
-      prim_load(kpp + kq, kp);
-      const float2 ks = prim_screen(kpp + kq);
-      if (P.pcnt > 0) prim_load(bpp, bn);
-      for (int kb = 0; kb < P.pcnt; ++kb) {
-        const PP bp = bn;
-        if (kb + 1 < P.pcnt) prim_load(bpp + kb + 1, bn);  // prefetch
-        if (!screen_keep(bpp + kb, prim_screen(bpp + kb), kpp + kq, ks, a)) continue;
+    const int nP = P.pcnt, total = P.pcnt * Q.pcnt;
+    // candidates c = kq nP + kb in windows of 32: each lane screens one, the
+    // survivors are dealt to the lane groups G at a time (one instance of
+    // the loop per operator: plain 1/r or the CAM pass's erf(mu r)/r)
+    auto prim_loop = [&](auto att_tag) {
+    constexpr bool ATT = decltype(att_tag)::value;
+    for (int c0 = 0; c0 < total; c0 += 32) {
+      bool keep = false;
+      {
+        const int c = c0 + lane;
+        if (c < total) {
+          const int kq = c / nP, kb = c - kq * nP;
+          keep = screen_keep(bpp + kb, prim_screen(bpp + kb), kpp + kq, prim_screen(kpp + kq), a);
+        }
+      }
+      unsigned mask = __ballot_sync(0xffffffffu, keep);
+      while (mask) {
+        const int avail = __popc(mask);
+        const int ng = avail < G ? avail : G;
+        // this group's candidate: the grp-th surviving one of the window
+        unsigned m = mask;
+        for (int i = 0; i < grp && i < ng; ++i) m &= m - 1;
+        const int myc = c0 + __ffs(m) - 1;
+        for (int i = 0; i < ng; ++i) mask &= mask - 1;
+        nprim += ng;
+        const bool active = grp < ng;
+        PP bp, kp;
         PrimQuartet<T> pq;
-        prim_setup<T>(bp, kp, pq, a.inv_mu2 != 0.0, (T)a.inv_mu2);
-        ++nprim;
-        if (lane < 2 * NR) {
-          const T v = rys_quantity<NR, T>(pq.X, lane, a.roots_f32 != 0);
-          RT[lane] = (lane & 1) ? v * pq.pref : v;
+        if (active) {
+          const int kq = myc / nP, kb = myc - kq * nP;
+          prim_load(bpp + kb, bp);
+          prim_load(kpp + kq, kp);
+          prim_setup<T, ATT>(bp, kp, pq, (T)a.inv_mu2);
+          if (gl < 2 * NR) {
+            const T v = rys_quantity<NR, T>(pq.X, gl, a.roots_f32 != 0);
+            RT[grp * 2 * NR + gl] = (gl & 1) ? v * pq.pref : v;
+          }
         }
         __syncwarp();
-        if (lane < 3 * NR) {
-          const int r = lane / 3, d = lane - 3 * r;
-          const T u = RT[2 * r], w = RT[2 * r + 1];
+        if (active) {
+          const int r = gl / 3, d = gl - 3 * r;
+          const T u = RT[grp * 2 * NR + 2 * r], w = RT[grp * 2 * NR + 2 * r + 1];
           const T uq = u * pq.qi, up = u * pq.pi;
           const T b00 = (T)0.5 * pq.inv * u;
           const T b10 = fma(-bp.hp, uq, bp.hp);
@@ -957,22 +995,24 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
           const T pqd = pick3(d, pq.PQ[0], pq.PQ[1], pq.PQ[2]);
           const T c00 = fma(-uq, pqd, pick3(d, bp.ax, bp.ay, bp.az));
           const T d00 = fma(up, pqd, pick3(d, kp.ax, kp.ay, kp.az));
-          T* dst = I2 + (r * 3 + d) * N2D;
+          T* dst = I2 + ((grp * NR + r) * 3 + d) * N2D;
           twod<LA, LB, LC, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01, pick3(d, AB[0], AB[1], AB[2]),
                                   pick3(d, CD[0], CD[1], CD[2]), [&](int i, T v) { dst[i] = v; });
         }
         __syncwarp();
-#pragma unroll
+#pragma unroll (KE <= 8 ? KE : 4)
         for (int k = 0; k < KE; ++k) {
           const int e = lane + 32 * k;
           if (e < NE) {
             const int o = s_offs[e];
             const int ox = o & 1023, oy = (o >> 10) & 1023, oz = o >> 20;
             T v = V[e];
+            for (int g = 0; g < ng; ++g) {
 #pragma unroll
-            for (int r = 0; r < NR; ++r) {
-              const T* g = I2 + r * 3 * N2D;
-              v = fma(g[ox] * g[N2D + oy], g[2 * N2D + oz], v);
+              for (int r = 0; r < NR; ++r) {
+                const T* gt = I2 + (g * NR + r) * 3 * N2D;
+                v = fma(gt[ox] * gt[N2D + oy], gt[2 * N2D + oz], v);
+              }
             }
             V[e] = v;
           }
@@ -980,6 +1020,9 @@ __global__ void __launch_bounds__(128) k_team(const BuildArgs a) {
         __syncwarp();
       }
     }
+    };
+    if (a.inv_mu2 != 0.0) prim_loop(std::true_type{});
+    else prim_loop(std::false_type{});
     team_epilogue<LA, LB, LC, LD, PURE, SCH, T>(a, qd, P, Q, W, lane);
     __syncwarp();
   }

@@ -285,7 +285,11 @@ struct GradTeamSmem {
   static constexpr int RT = 2 * G::NR;
   static constexpr int XT = 3 * G::NR * G::N2DX;
   static constexpr int TT = 3 * G::NR * 4 * G::N2D;   // per root x dim: I, dA, dB, dC
-  static constexpr int PER_WARP = RT + XT + TT;       // elements of the kernel's type
+  // classes with more than 16 elements per lane keep the two-particle density
+  // block in shared memory instead of registers (and loop over it unrolled by 4)
+  static constexpr bool BIG = (Cls<LA, LB, LC, LD>::NE + 31) / 32 > 16;
+  static constexpr int GM = BIG ? Cls<LA, LB, LC, LD>::NE : 0;
+  static constexpr int PER_WARP = RT + XT + TT + GM;  // elements of the kernel's type
 };
 
 template <int LA, int LB, int LC, int LD, typename T>
@@ -302,19 +306,24 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
   T* XT = W + SM::RT;
   T* TT = XT + SM::XT;
   const PP* prims = GAcc<T>::prims(g);
+  constexpr bool BIG = SM::BIG;
+  constexpr int KR = BIG ? 1 : KE;   // register-resident elements per lane
+  T* GM = TT + SM::TT;               // BIG: the density block
   // this lane's elements: packed offsets into the per-dim tables
-  int offs[KE];
+  int offs[KR];
+  if constexpr (!BIG) {
 #pragma unroll
-  for (int k = 0; k < KE; ++k) {
-    const int e = lane + 32 * k;
-    int o = 0;
-    if (e < NE) {
-      int ox[3];
+    for (int k = 0; k < KE; ++k) {
+      const int e = lane + 32 * k;
+      int o = 0;
+      if (e < NE) {
+        int ox[3];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) ox[d] = K::off2d(e, d);
-      o = ox[0] | (ox[1] << 10) | (ox[2] << 20);
+        for (int d = 0; d < 3; ++d) ox[d] = K::off2d(e, d);
+        o = ox[0] | (ox[1] << 10) | (ox[2] << 20);
+      }
+      offs[k] = o;
     }
-    offs[k] = o;
   }
   unsigned long long nprim = 0, nq = 0;
   for (;;) {
@@ -325,18 +334,29 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
     T AB[3], CD[3];
     int ro[4];
     quartet_setup<T>(g, qd, P, Q, AB, CD, ro);
-    T gam[KE];
+    T gam[KR];
     T dmx = 0;
-#pragma unroll
-    for (int k = 0; k < KE; ++k) {
-      const int e = lane + 32 * k;
-      gam[k] = 0;
-      if (e < NE) {
+    if constexpr (BIG) {
+#pragma unroll 4
+      for (int e = lane; e < NE; e += 32) {
         const T v = gamma_elem<T>(g, ro[0] + G::ia(e), ro[1] + G::ib(e), ro[2] + G::ic(e), ro[3] + G::id(e));
-        gam[k] = v;
+        GM[e] = v;
         const T nrm = (T)(cart_norm(LA, G::ia(e)) * cart_norm(LB, G::ib(e)) * cart_norm(LC, G::ic(e)) *
                           cart_norm(LD, G::id(e)));
         dmx = fmax(dmx, g.pure ? fabs(v) : fabs(v) / nrm);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < KE; ++k) {
+        const int e = lane + 32 * k;
+        gam[k] = 0;
+        if (e < NE) {
+          const T v = gamma_elem<T>(g, ro[0] + G::ia(e), ro[1] + G::ib(e), ro[2] + G::ic(e), ro[3] + G::id(e));
+          gam[k] = v;
+          const T nrm = (T)(cart_norm(LA, G::ia(e)) * cart_norm(LB, G::ib(e)) * cart_norm(LC, G::ic(e)) *
+                            cart_norm(LD, G::id(e)));
+          dmx = fmax(dmx, g.pure ? fabs(v) : fabs(v) / nrm);
+        }
       }
     }
     const T dabmax = warp_max(dmx);
@@ -398,29 +418,34 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
           Tb[3 * N2D + n] = vC;
         }
         __syncwarp();
+        auto contract = [&](int ox, int oy, int oz, T ge) {
 #pragma unroll
-        for (int k = 0; k < KE; ++k) {
-          if (lane + 32 * k < NE) {
-            const int ox = offs[k] & 1023, oy = (offs[k] >> 10) & 1023, oz = offs[k] >> 20;
-            const T ge = gam[k];
+          for (int r = 0; r < NR; ++r) {
+            const T* tx = TT + (r * 3 + 0) * 4 * N2D;
+            const T* ty = TT + (r * 3 + 1) * 4 * N2D;
+            const T* tz = TT + (r * 3 + 2) * 4 * N2D;
+            const T ix = tx[ox], iy = ty[oy], iz = tz[oz];
+            const T t1 = ge * iz;
+            const T yz = iy * t1, xz = ix * t1, xy = ix * iy * ge;
+            acc[0] = fma(tx[N2D + ox], yz, acc[0]);
+            acc[1] = fma(ty[N2D + oy], xz, acc[1]);
+            acc[2] = fma(tz[N2D + oz], xy, acc[2]);
+            acc[3] = fma(tx[2 * N2D + ox], yz, acc[3]);
+            acc[4] = fma(ty[2 * N2D + oy], xz, acc[4]);
+            acc[5] = fma(tz[2 * N2D + oz], xy, acc[5]);
+            acc[6] = fma(tx[3 * N2D + ox], yz, acc[6]);
+            acc[7] = fma(ty[3 * N2D + oy], xz, acc[7]);
+            acc[8] = fma(tz[3 * N2D + oz], xy, acc[8]);
+          }
+        };
+        if constexpr (BIG) {
+#pragma unroll 4
+          for (int e = lane; e < NE; e += 32) contract(K::off2d(e, 0), K::off2d(e, 1), K::off2d(e, 2), GM[e]);
+        } else {
 #pragma unroll
-            for (int r = 0; r < NR; ++r) {
-              const T* tx = TT + (r * 3 + 0) * 4 * N2D;
-              const T* ty = TT + (r * 3 + 1) * 4 * N2D;
-              const T* tz = TT + (r * 3 + 2) * 4 * N2D;
-              const T ix = tx[ox], iy = ty[oy], iz = tz[oz];
-              const T t1 = ge * iz;
-              const T yz = iy * t1, xz = ix * t1, xy = ix * iy * ge;
-              acc[0] = fma(tx[N2D + ox], yz, acc[0]);
-              acc[1] = fma(ty[N2D + oy], xz, acc[1]);
-              acc[2] = fma(tz[N2D + oz], xy, acc[2]);
-              acc[3] = fma(tx[2 * N2D + ox], yz, acc[3]);
-              acc[4] = fma(ty[2 * N2D + oy], xz, acc[4]);
-              acc[5] = fma(tz[2 * N2D + oz], xy, acc[5]);
-              acc[6] = fma(tx[3 * N2D + ox], yz, acc[6]);
-              acc[7] = fma(ty[3 * N2D + oy], xz, acc[7]);
-              acc[8] = fma(tz[3 * N2D + oz], xy, acc[8]);
-            }
+          for (int k = 0; k < KE; ++k) {
+            if (lane + 32 * k < NE)
+              contract(offs[k] & 1023, (offs[k] >> 10) & 1023, offs[k] >> 20, gam[k]);
           }
         }
         __syncwarp();

@@ -28,14 +28,24 @@ const ClassInfo& class_info(int c) { return kClasses[c]; }
 
 cudaError_t launch_class(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
   switch (c) {
-    case 0: case 1: case 2: case 3: case 4: case 6: case 7: case 8:
+    case 0: case 1: case 2: case 3:
       return launch_group0(c, pure, mode, a, nsm, st);
-    case 5: case 9: case 10: case 11: case 12: case 15:
+    case 4: case 6: case 7: case 8:
       return launch_group1(c, pure, mode, a, nsm, st);
-    case 13: case 14: case 16: case 17:
+    case 5: case 9: case 10:
       return launch_group2(c, pure, mode, a, nsm, st);
-    default:
+    case 11: case 12: case 15:
       return launch_group3(c, pure, mode, a, nsm, st);
+    case 13: case 14: case 16: case 17:
+      return launch_group4(c, pure, mode, a, nsm, st);
+    case 18:
+      return launch_group5(c, pure, mode, a, nsm, st);
+    case 19:
+      return launch_group6(c, pure, mode, a, nsm, st);
+    case 20:
+      return launch_group7(c, pure, mode, a, nsm, st);
+    default:
+      return cudaErrorInvalidValue;
   }
 }
 
