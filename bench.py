@@ -242,7 +242,7 @@ def run_td(args):
     torch.cuda.set_device(local)
     from openqp_gb300 import build as bld
     bld.build()
-    from openqp_gb300.fock import FockBuilder, class_flops, class_labels, fp64_peak_tflops
+    from openqp_gb300.fock import NCLASS, FockBuilder, class_flops, class_labels, fp64_peak_tflops
     bas, x = td_workload()
     nvec = x.shape[0]
     fb = FockBuilder(bas, cutoff=WORKLOAD["cutoff"])
@@ -284,7 +284,7 @@ def run_td(args):
     s0 = stats[-1]
     pure = bool(bas.harmonic.any())
     fl = [class_flops(c, s0["prim_per_class"][c], s0["per_class"][c], nk=2 * nvec, nj=nvec, pure=pure)
-          for c in range(21)]
+          for c in range(NCLASS)]
     achieved = fl[cdom] / (ms[cdom] * 1e-3) / 1e12
     peak = fp64_peak_tflops()
     nb = int(8 * nvec * bas.nbf * bas.nbf)
@@ -303,7 +303,7 @@ def run_td(args):
             "quartets_per_s": s0["quartets"] / (tsum / args.steps),
             "prim_quartets_per_s": s0["prim_quartets"] / (tsum / args.steps),
             "gpu_launches": int(sum(s["launches"] for s in stats)), "clocks": clocks,
-            "class_ms": {labels[c]: round(float(ms[c]), 3) for c in range(21) if ms[c] > 0},
+            "class_ms": {labels[c]: round(float(ms[c]), 3) for c in range(NCLASS) if ms[c] > 0},
             "list_ms": s0["list_ms"]}
     if not args.no_cpu and rank == 0:
         line["cpu_baseline"] = cpu_baseline_td(bas, x, args.cpu_budget)
@@ -512,7 +512,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     from openqp_gb300 import build as bld
     bld.build()
-    from openqp_gb300.fock import FockBuilder, class_flops, class_labels, fp64_peak_tflops, routec_init, \
+    from openqp_gb300.fock import NCLASS, FockBuilder, class_flops, class_labels, fp64_peak_tflops, routec_init, \
         routec_fock_jk
     bas, d = make_workload()
     fb = FockBuilder(bas, cutoff=WORKLOAD["cutoff"])
@@ -598,7 +598,7 @@ def run_ours(args):
     flops = class_flops(cdom, s0["prim_per_class"][cdom], s0["per_class"][cdom], nk=1, pure=bool(bas.harmonic.any()))
     achieved = flops / (ms[cdom] * 1e-3) / 1e12
     total_flops = sum(class_flops(c, s0["prim_per_class"][c], s0["per_class"][c], nk=1, pure=bool(bas.harmonic.any()))
-                      for c in range(21))
+                      for c in range(NCLASS))
     peak = fp64_peak_tflops()
     if rank == 0:
         line = {"metric": "J+K Fock builds/s", "value": value, "unit": "builds/s", "n_gpus": ws,
@@ -618,9 +618,9 @@ def run_ours(args):
                 "prim_quartets_per_s": s0["prim_quartets"] / (tsum / args.steps),
                 "gpu_launches": int(sum(s["launches"] for s in stats)),
                 "wall_s": wall, "clocks": clocks,
-                "class_ms": {labels[c]: round(float(ms[c]), 3) for c in range(21) if ms[c] > 0},
-                "class_quartets": {labels[c]: s0["per_class"][c] for c in range(21) if s0["per_class"][c]},
-                "class_prim_quartets": {labels[c]: s0["prim_per_class"][c] for c in range(21)
+                "class_ms": {labels[c]: round(float(ms[c]), 3) for c in range(NCLASS) if ms[c] > 0},
+                "class_quartets": {labels[c]: s0["per_class"][c] for c in range(NCLASS) if s0["per_class"][c]},
+                "class_prim_quartets": {labels[c]: s0["prim_per_class"][c] for c in range(NCLASS)
                                         if s0["prim_per_class"][c]},
                 "list_ms": s0["list_ms"]}
         if mixed is not None:
@@ -814,7 +814,7 @@ def run_batch(args):
     bld.build()
     from openqp_gb300 import autotune, workloads
     from openqp_gb300.basis import unpack
-    from openqp_gb300.fock import BatchFockBuilder, FockBuilder, class_flops, class_labels, fp64_peak_tflops
+    from openqp_gb300.fock import NCLASS, BatchFockBuilder, FockBuilder, class_flops, class_labels, fp64_peak_tflops
     sizes, bases, dens = workloads.water_batch(WORKLOAD["batch"], WORKLOAD["seed"] + rank, basis=WORKLOAD["basis"])
     nmol = len(bases)
     st = torch.cuda.current_stream()

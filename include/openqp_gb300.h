@@ -199,7 +199,7 @@ int oqpg_fock_jk_graph(oqpg_ctx* ctx, const double* d_device, double* f_device, 
 /* Graph captures and replays so far, and kernels in the captured graph. */
 int oqpg_graph_info(const oqpg_ctx* ctx, int* captures, int* replays, int* kernels);
 
-/* Per-class launch parameters, 21 entries each in the class order of
+/* Per-class launch parameters, 55 entries each in the class order of
  * oqpg_class_l (null: leave unchanged): split_log2 -- quartets of the <= 27
  * element classes with >= 2^split_log2 primitive quartets run one warp per
  * quartet (64: never); chunk -- quartets a warp takes per work grab in the
@@ -229,12 +229,12 @@ int oqpg_schwarz(const oqpg_ctx* ctx, double* q);
  * in the reference. */
 int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold);
 
-/* Statistics of the last build, up to n (<= 73) doubles:
+/* Statistics of the last build, up to n (<= 175) doubles:
  * [0] quartets computed, [1] primitive quartets, [2] list build ms,
  * [3] integral kernels ms, [4] total device ms, [5] nbf, [6] shell pairs,
- * [7 .. 28) quartets per class (la lb|lc ld) in the order of oqpg_class_l,
- * [28 .. 49) primitive quartets per class, [49 .. 70) kernel ms per class,
- * [70] kernels launched by the build, [71] FP32 quartets, [72] FP32
+ * [7 .. 62) quartets per class (la lb|lc ld) in the order of oqpg_class_l,
+ * [62 .. 117) primitive quartets per class, [117 .. 172) kernel ms per class,
+ * [172] kernels launched by the build, [173] FP32 quartets, [174] FP32
  * primitive quartets. */
 int oqpg_stats(const oqpg_ctx* ctx, double* out, int n);
 
@@ -303,7 +303,9 @@ int oqpg_fock_td_cam(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, 
                      const double* cam);
 int oqpg_fock_mrsf_cam(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, const double* cam);
 
-/* Angular momenta (la, lb, lc, ld) of class c (0 <= c < 21). */
+/* Angular momenta (la, lb, lc, ld) of class c (0 <= c < 55): classes 0-20 are
+ * the s-d ones, 21-54 those with an f shell (FP64 kernels only; the precision
+ * modes keep them in FP64). */
 int oqpg_class_l(int c, int* l4);
 
 /* FP64 FMA throughput of the current device (TFLOP/s, FMA = 2 flops) from an

@@ -27,7 +27,7 @@ import numpy as np
 
 _DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "basis_data")
 _ALIASES = {"6-31g*": "6-31g_d", "6-31g(d)": "6-31g_d", "6-31g_d": "6-31g_d", "6-31g": "6-31g",
-            "cc-pvdz": "cc-pvdz", "sto-3g": "sto-3g"}
+            "cc-pvdz": "cc-pvdz", "cc-pvtz": "cc-pvtz", "sto-3g": "sto-3g"}
 ANGSTROM = 1.0 / 0.52917721092   # Bohr per Angstrom (CODATA 2010, as in OpenQP's UNITS_ANGSTROM)
 
 

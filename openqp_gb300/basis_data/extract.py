@@ -26,6 +26,7 @@ SETS = {
     "6-31g": ("6-31g.basis", False),
     "6-31g(d)": ("6-31g(d).basis", False),
     "cc-pvdz": ("cc-pvdz.basis", True),
+    "cc-pvtz": ("cc-pvtz.basis", True),
 }
 
 

@@ -1,6 +1,6 @@
 """Generate the Rys quadrature tables used by the device kernels and the oracle.
 
-For n = 1..5 Rys roots, the quadrature
+For n = 1..7 Rys roots, the quadrature
     int_0^1 f(t^2) exp(-X t^2) dt  ~=  sum_i w_i(X) f(x_i(X)),   x_i = t_i^2,
 is exact for polynomials f of degree <= 2n-1.  Its nodes and weights are the
 Gauss nodes/weights of the measure exp(-X x) / (2 sqrt(x)) dx on [0, 1], whose
@@ -34,13 +34,13 @@ import mpmath as mp
 import numpy as np
 
 DPS = 60
-NMAX = 5
+NMAX = 7
 NCOEF = 8             # degree-7 interpolants
 NCOEF_F32 = 5         # degree-4 interpolants for the FP32 quartets
 X_SPLIT = 32          # quarter-unit intervals below, unit intervals above
 H_LO = 0.25
 W_HI = 1
-XMAX = {1: 40, 2: 48, 3: 56, 4: 64, 5: 72}
+XMAX = {1: 40, 2: 48, 3: 56, 4: 64, 5: 72, 6: 80, 7: 88}
 
 
 def boys_list(X, mmax):

@@ -1,4 +1,4 @@
-// The 21 (la lb | lc ld) classes of s-d quartets in kernel orientation and
+// The 55 (la lb | lc ld) classes of s-f quartets in kernel orientation and
 // the launchers of their kernels (one translation unit per group of classes).
 #pragma once
 #include <cuda_runtime.h>
@@ -7,16 +7,25 @@
 
 namespace oqpg {
 
-constexpr int NPAIRTYPE = 6;   // ss sp sd pp pd dd  (la <= lb)
-constexpr int NCLASS = 21;     // pair type of bra <= pair type of ket
-constexpr int PAIR_L[NPAIRTYPE][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+// Pair types (la <= lb): the six s-d ones, then the four with an f shell.
+constexpr int NPAIRTYPE = 10;  // ss sp sd pp pd dd | sf pf df ff
+constexpr int NPAIRTYPE_SD = 6;
+constexpr int NCLASS_SD = 21;  // classes of two s-d pair types
+constexpr int NCLASS = 55;     // pair type of bra <= pair type of ket
+constexpr int PAIR_L[NPAIRTYPE][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2},
+                                      {0, 3}, {1, 3}, {2, 3}, {3, 3}};
 
-inline int pair_type(int la, int lb) {  // la <= lb
-  return la == 0 ? lb : (la == 1 ? 2 + lb : 5);
+__host__ __device__ inline int pair_type(int la, int lb) {  // la <= lb
+  return lb == 3 ? 6 + la : (la == 0 ? lb : (la == 1 ? 2 + lb : 5));
 }
-inline int class_index(int tbra, int tket) {  // tbra <= tket
-  return tbra * NPAIRTYPE - tbra * (tbra - 1) / 2 + (tket - tbra);
+// Classes of two s-d pair types keep the indices 0..20; a class with an f
+// pair (ket type tk >= 6, bra type tb <= tk) follows at 21 + (tk(tk+1) - 42)/2 + tb.
+__host__ __device__ inline int class_index(int tbra, int tket) {  // tbra <= tket
+  if (tket < NPAIRTYPE_SD) return tbra * NPAIRTYPE_SD - tbra * (tbra - 1) / 2 + (tket - tbra);
+  return NCLASS_SD + (tket * (tket + 1) - 42) / 2 + tbra;
 }
+// classes 21.. involve an f shell: FP64 kernels only
+__host__ __device__ constexpr bool class_has_f(int c) { return c >= NCLASS_SD; }
 
 struct ClassInfo {
   int l[4];
@@ -51,5 +60,11 @@ cudaError_t launch_group4(int c, bool pure, int mode, const BuildArgs& a, int ns
 cudaError_t launch_group5(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 cudaError_t launch_group6(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 cudaError_t launch_group7(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group8(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group9(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group10(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group11(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group12(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group13(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 
 }  // namespace oqpg

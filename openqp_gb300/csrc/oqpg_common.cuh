@@ -85,18 +85,27 @@ struct BuildArgs {
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 
-// Cartesian exponents in OpenQP order: s; x y z; xx yy zz xy xz yz.
+// Cartesian exponents in OpenQP order (constants.F90:33-60): s; x y z;
+// xx yy zz xy xz yz; xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz.
+__host__ __device__ constexpr int cart_e3(int idx, int dim) {
+  // packed exponents (x | y << 2 | z << 4) of the ten f components
+  return ((idx == 0 ? 3 : idx == 1 ? 12 : idx == 2 ? 48 : idx == 3 ? 6 : idx == 4 ? 18 : idx == 5 ? 9
+           : idx == 6 ? 24 : idx == 7 ? 33 : idx == 8 ? 36 : 21) >> (2 * dim)) & 3;
+}
 __host__ __device__ constexpr int cart_e(int l, int idx, int dim) {
   return l == 0 ? 0
        : l == 1 ? (idx == dim ? 1 : 0)
+       : l == 3 ? cart_e3(idx, dim)
        : (idx < 3 ? (idx == dim ? 2 : 0)
           : idx == 3 ? (dim < 2 ? 1 : 0)
           : idx == 4 ? (dim != 1 ? 1 : 0)
                      : (dim > 0 ? 1 : 0));
 }
-// shells_pnrm2 for l <= 2 (individually normalised Cartesians)
+// shells_pnrm2 for l <= 3 (individually normalised Cartesians)
 __host__ __device__ constexpr double cart_norm(int l, int idx) {
-  return (l == 2 && idx >= 3) ? 1.7320508075688772 : 1.0;
+  return (l == 2 && idx >= 3) ? 1.7320508075688772
+       : (l == 3 && idx >= 3) ? (idx == 9 ? 3.8729833462074170 : 2.2360679774997897)
+                              : 1.0;
 }
 
 // FP64 reciprocal / reciprocal square root: hardware approximation refined by

@@ -144,7 +144,7 @@ __device__ __forceinline__ T rys_quantity(T X, int q, bool roots_f32 = false) {
   }
 }
 
-__host__ __device__ constexpr int naos(int l, bool pure) { return (pure && l == 2) ? 5 : ncart(l); }
+__host__ __device__ constexpr int naos(int l, bool pure) { return (pure && l >= 2) ? 2 * l + 1 : ncart(l); }
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 
 // Pure-d projection row m, Cartesian component c (m = -2..2: xy, yz, z^2, xz, x^2-y^2)
@@ -155,6 +155,24 @@ __host__ __device__ constexpr double pure_d(int m, int c) {
        : m == 3 ? (c == 4 ? 1.0 : 0.0)
                 : (c == 0 ? 0.86602540378443865 : (c == 1 ? -0.86602540378443865 : 0.0));
 }
+
+// Pure-f projection row m (m = -3..3), Cartesian component c of the normalised
+// Cartesians xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz: the real solid harmonics
+// (coefficients sqrt(10)/4, 3/(2 sqrt 2), sqrt(6)/4, sqrt(30)/20, sqrt(6/5),
+// 3/(2 sqrt 5), sqrt(3)/2; OpenQP int2_pure_generated.F90:134-149)
+__host__ __device__ constexpr double pure_f(int m, int c) {
+  constexpr double A = 0.79056941504209483, B = 1.0606601717798213, C = 0.61237243569579452,
+                   D = 0.27386127875258306, E = 1.0954451150103321, G = 0.67082039324993691,
+                   H = 0.86602540378443865;
+  return m == 0 ? (c == 1 ? -A : c == 3 ? B : 0.0)
+       : m == 1 ? (c == 9 ? 1.0 : 0.0)
+       : m == 2 ? (c == 1 ? -C : c == 3 ? -D : c == 8 ? E : 0.0)
+       : m == 3 ? (c == 2 ? 1.0 : (c == 4 || c == 6) ? -G : 0.0)
+       : m == 4 ? (c == 0 ? -C : c == 5 ? -D : c == 7 ? E : 0.0)
+       : m == 5 ? (c == 4 ? H : c == 6 ? -H : 0.0)
+                : (c == 0 ? A : c == 5 ? -B : 0.0);
+}
+__host__ __device__ constexpr double pure_coef(int l, int m, int c) { return l == 2 ? pure_d(m, c) : pure_f(m, c); }
 
 // ---------------------------------------------------------------------------
 // Primitive pairs in the arithmetic type of the kernel.
@@ -359,32 +377,35 @@ struct Epi {
   static constexpr int NEP = A * B * C * D;
 };
 
-// In-register pure projection of one index (compile-time dims); the Cartesian
-// norms of the d components are folded into the coefficients, so projected
-// indices need no separate normalisation.
-template <int D0, int D1, int D2, int D3, int POS, bool DO, typename T>
+// In-register pure projection of one index of angular momentum L (compile-time
+// dims; L < 2: copy); the Cartesian norms of the projected components are
+// folded into the coefficients, so projected indices need no separate
+// normalisation.
+template <int D0, int D1, int D2, int D3, int POS, int L, typename T>
 __device__ __forceinline__ void project_regs(const T* in, T* out) {
   constexpr int DIMS[4] = {D0, D1, D2, D3};
   constexpr int PRE = POS == 0 ? 1 : (POS == 1 ? D0 : (POS == 2 ? D0 * D1 : D0 * D1 * D2));
   constexpr int N = DIMS[POS];
   constexpr int POST = POS == 3 ? 1 : (POS == 2 ? D3 : (POS == 1 ? D2 * D3 : D1 * D2 * D3));
-  if (!DO) {
+  if constexpr (L < 2) {
 #pragma unroll
     for (int i = 0; i < PRE * N * POST; ++i) out[i] = in[i];
-    return;
+  } else {
+    constexpr int NP = 2 * L + 1;
+#pragma unroll
+    for (int a = 0; a < PRE; ++a)
+#pragma unroll
+      for (int m = 0; m < NP; ++m)
+#pragma unroll
+        for (int p = 0; p < POST; ++p) {
+          T v = 0;
+#pragma unroll
+          for (int c = 0; c < N; ++c)
+            if (pure_coef(L, m, c) != 0.0)
+              v = fma((T)(pure_coef(L, m, c) * cart_norm(L, c)), in[(a * N + c) * POST + p], v);
+          out[(a * NP + m) * POST + p] = v;
+        }
   }
-#pragma unroll
-  for (int a = 0; a < PRE; ++a)
-#pragma unroll
-    for (int m = 0; m < 5; ++m)
-#pragma unroll
-      for (int p = 0; p < POST; ++p) {
-        T v = 0;
-#pragma unroll
-        for (int c = 0; c < 6; ++c)
-          if (pure_d(m, c) != 0.0) v = fma((T)(pure_d(m, c) * cart_norm(2, c)), in[(a * N + c) * POST + p], v);
-        out[(a * 5 + m) * POST + p] = v;
-      }
 }
 
 __device__ __constant__ const double SQRT3_POW[5] = {1.0, 1.7320508075688772, 3.0, 5.196152422706632, 9.0};
@@ -529,10 +550,10 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
   for (int e = 0; e < NE; ++e) acc[e] *= (T)(PURE ? 1.0 : K::norm(e));
   constexpr int DA = K::NA, DB = K::NB, DC = K::NC, DD = K::ND;
   T t1[NE], t2[NE];
-  project_regs<DA, DB, DC, DD, 0, PURE && LA == 2>(acc, t1);
-  project_regs<E::A, DB, DC, DD, 1, PURE && LB == 2>(t1, t2);
-  project_regs<E::A, E::B, DC, DD, 2, PURE && LC == 2>(t2, t1);
-  project_regs<E::A, E::B, E::C, DD, 3, PURE && LD == 2>(t1, t2);
+  project_regs<DA, DB, DC, DD, 0, PURE ? LA : 0>(acc, t1);
+  project_regs<E::A, DB, DC, DD, 1, PURE ? LB : 0>(t1, t2);
+  project_regs<E::A, E::B, DC, DD, 2, PURE ? LC : 0>(t2, t1);
+  project_regs<E::A, E::B, E::C, DD, 3, PURE ? LD : 0>(t1, t2);
   T* V = t2;
   if (SCH) {
     T m = 0;
@@ -754,8 +775,12 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
                 id = e % K::ND;
       // product of the component norms: sqrt(3)^n for n off-diagonal d components,
       // looked up rather than multiplied out (one FP64 multiply per element)
-      const int n3 = (LA == 2 && ia >= 3) + (LB == 2 && ib >= 3) + (LC == 2 && ic >= 3) + (LD == 2 && id >= 3);
-      if (LA == 2 || LB == 2 || LC == 2 || LD == 2) V[e] *= sqrt3_pow<T>(n3);
+      if constexpr (LA == 3 || LB == 3 || LC == 3 || LD == 3) {
+        V[e] *= (T)(cart_norm(LA, ia) * cart_norm(LB, ib) * cart_norm(LC, ic) * cart_norm(LD, id));
+      } else {
+        const int n3 = (LA == 2 && ia >= 3) + (LB == 2 && ib >= 3) + (LC == 2 && ic >= 3) + (LD == 2 && id >= 3);
+        if (LA == 2 || LB == 2 || LC == 2 || LD == 2) V[e] *= sqrt3_pow<T>(n3);
+      }
     }
   }
   __syncwarp();
@@ -764,26 +789,45 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
     const int ls[4] = {LA, LB, LC, LD};
 #pragma unroll
     for (int pos = 0; pos < 4; ++pos) {
-      if (ls[pos] != 2) continue;
+      if (ls[pos] < 2) continue;
       int pre = 1, post = 1;
       for (int i = 0; i < pos; ++i) pre *= dims[i];
       for (int i = pos + 1; i < 4; ++i) post *= dims[i];
-      const int nout = pre * 5 * post;
-      for (int o = lane; o < nout; o += 32) {
-        const int p = o % post, m = (o / post) % 5, q = o / (5 * post);
-        const T* src = V + (size_t)q * 6 * post + p;
-        T v;
-        if (m == 0) v = src[3 * post];
-        else if (m == 1) v = src[5 * post];
-        else if (m == 2) v = src[2 * post] - (T)0.5 * (src[0] + src[post]);
-        else if (m == 3) v = src[4 * post];
-        else v = (T)0.86602540378443865 * (src[0] - src[post]);
-        Tm[o] = v;
+      if (ls[pos] == 2) {
+        const int nout = pre * 5 * post;
+        for (int o = lane; o < nout; o += 32) {
+          const int p = o % post, m = (o / post) % 5, q = o / (5 * post);
+          const T* src = V + (size_t)q * 6 * post + p;
+          T v;
+          if (m == 0) v = src[3 * post];
+          else if (m == 1) v = src[5 * post];
+          else if (m == 2) v = src[2 * post] - (T)0.5 * (src[0] + src[post]);
+          else if (m == 3) v = src[4 * post];
+          else v = (T)0.86602540378443865 * (src[0] - src[post]);
+          Tm[o] = v;
+        }
+        __syncwarp();
+        for (int o = lane; o < nout; o += 32) V[o] = Tm[o];
+        __syncwarp();
+        dims[pos] = 5;
+      } else {  // f: 10 normalised Cartesians -> 7
+        const int nout = pre * 7 * post;
+        for (int o = lane; o < nout; o += 32) {
+          const int p = o % post, m = (o / post) % 7, q = o / (7 * post);
+          const T* src = V + (size_t)q * 10 * post + p;
+          T v = 0;
+#pragma unroll
+          for (int c = 0; c < 10; ++c) {
+            const double w = pure_f(m, c);
+            if (w != 0.0) v = fma((T)w, src[c * post], v);
+          }
+          Tm[o] = v;
+        }
+        __syncwarp();
+        for (int o = lane; o < nout; o += 32) V[o] = Tm[o];
+        __syncwarp();
+        dims[pos] = 7;
       }
-      __syncwarp();
-      for (int o = lane; o < nout; o += 32) V[o] = Tm[o];
-      __syncwarp();
-      dims[pos] = 5;
     }
   }
   constexpr int NEP = E::NEP;

@@ -195,6 +195,7 @@ void cart_effective(const oqpg_ctx* c, const double* M, double* Mc) {
 // full AO matrices x, y (and the spin pair xs, ys, both null or both set).
 int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, const double* ys, double cj,
                double ckt, double cks, double cutoff, double* de) {
+  if (c->has_f) return UNSUPPORTED;  // derivative kernels are built for s-d shells only
   if (c->nmol != 1) return UNSUPPORTED;
   int rc;
   if ((rc = grad_init(c))) return rc;

@@ -22,8 +22,16 @@ static const ClassInfo kClasses[NCLASS] = {
     C_(1, 1, 1, 1), C_(1, 1, 1, 2), C_(1, 1, 2, 2),
     C_(1, 2, 1, 2), C_(1, 2, 2, 2),
     C_(2, 2, 2, 2),
+    // with an f pair (ket type sf, pf, df, ff; bra type <= ket type)
+    C_(0, 0, 0, 3), C_(0, 1, 0, 3), C_(0, 2, 0, 3), C_(1, 1, 0, 3), C_(1, 2, 0, 3), C_(2, 2, 0, 3),
+    C_(0, 3, 0, 3), C_(0, 0, 1, 3), C_(0, 1, 1, 3), C_(0, 2, 1, 3), C_(1, 1, 1, 3), C_(1, 2, 1, 3),
+    C_(2, 2, 1, 3), C_(0, 3, 1, 3), C_(1, 3, 1, 3), C_(0, 0, 2, 3), C_(0, 1, 2, 3), C_(0, 2, 2, 3),
+    C_(1, 1, 2, 3), C_(1, 2, 2, 3), C_(2, 2, 2, 3), C_(0, 3, 2, 3), C_(1, 3, 2, 3), C_(2, 3, 2, 3),
+    C_(0, 0, 3, 3), C_(0, 1, 3, 3), C_(0, 2, 3, 3), C_(1, 1, 3, 3), C_(1, 2, 3, 3), C_(2, 2, 3, 3),
+    C_(0, 3, 3, 3), C_(1, 3, 3, 3), C_(2, 3, 3, 3), C_(3, 3, 3, 3),
 #undef C_
 };
+static_assert(sizeof(kClasses) / sizeof(kClasses[0]) == NCLASS, "class table");
 const ClassInfo& class_info(int c) { return kClasses[c]; }
 
 cudaError_t launch_class(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
@@ -44,6 +52,18 @@ cudaError_t launch_class(int c, bool pure, int mode, const BuildArgs& a, int nsm
       return launch_group6(c, pure, mode, a, nsm, st);
     case 20:
       return launch_group7(c, pure, mode, a, nsm, st);
+    case 21: case 22: case 23: case 24: case 25: case 26: case 27:
+      return launch_group8(c, pure, mode, a, nsm, st);
+    case 28: case 29: case 30: case 31: case 32: case 33: case 34: case 35:
+      return launch_group9(c, pure, mode, a, nsm, st);
+    case 36: case 37: case 38: case 39: case 40:
+      return launch_group10(c, pure, mode, a, nsm, st);
+    case 41: case 42: case 43: case 44:
+      return launch_group11(c, pure, mode, a, nsm, st);
+    case 45: case 46: case 47: case 48: case 49:
+      return launch_group12(c, pure, mode, a, nsm, st);
+    case 50: case 51: case 52: case 53: case 54:
+      return launch_group13(c, pure, mode, a, nsm, st);
     default:
       return cudaErrorInvalidValue;
   }
@@ -52,7 +72,7 @@ cudaError_t launch_class(int c, bool pure, int mode, const BuildArgs& a, int nsm
 // ---------------------------------------------------------------------------
 // Small device kernels
 
-__device__ __forceinline__ int d_class_index(int tb, int tk) { return tb * 6 - tb * (tb - 1) / 2 + (tk - tb); }
+
 
 // Packed D -> full symmetric Coulomb density (Da + Db) and exchange densities,
 // every molecule of the batch into its rows of the stacked matrices (columns
@@ -212,9 +232,9 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
           }
         }
         const int tQ = a.pair_type[Q];
-        if (tP <= tQ) { c = d_class_index(tP, tQ); ent = make_uint2(P, Q); }
-        else { c = d_class_index(tQ, tP); ent = make_uint2(Q, P); }
-        if (f32) c += NCLASS;
+        if (tP <= tQ) { c = class_index(tP, tQ); ent = make_uint2(P, Q); }
+        else { c = class_index(tQ, tP); ent = make_uint2(Q, P); }
+        if (f32 && !class_has_f(c)) c += NCLASS;  // f classes have FP64 kernels only
         slot = atomicAdd(&cnt[c], 1u);
       }
     }
@@ -609,12 +629,13 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
     int s = 0;
     for (int m = 0; m < nmol; ++m)
       for (int k = 0; k < nshell_m[m]; ++k, ++s) {
-        if (am[s] < 0 || am[s] > 2 || ncontr[s] <= 0 || origin[s] < 1 || origin[s] > natom_m[m]) return UNSUPPORTED;
-        if (am[s] == 2) { ++nd; if (harmonic && harmonic[s]) ++npure; }
+        if (am[s] < 0 || am[s] > 3 || ncontr[s] <= 0 || origin[s] < 1 || origin[s] > natom_m[m]) return UNSUPPORTED;
+        if (am[s] >= 2) { ++nd; if (harmonic && harmonic[s]) ++npure; }
+        if (am[s] == 3) c->has_f = true;
         poff[s] = off; off += ncontr[s];
       }
   }
-  if (npure != 0 && npure != nd) return UNSUPPORTED;  // mixed Cartesian / pure d shells
+  if (npure != 0 && npure != nd) return UNSUPPORTED;  // mixed Cartesian / pure d, f shells
   c->pure = nd > 0 && npure == nd;
   int s = 0, atom0 = 0, row0 = 0, pair0 = 0, stride = 0;
   long long tri0 = 0, dsh0 = 0;
@@ -628,8 +649,8 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
       ShellDev& S = c->shells[s];
       const int at = atom0 + origin[s] - 1;
       S.x = xyz[3 * at]; S.y = xyz[3 * at + 1]; S.z = xyz[3 * at + 2];
-      S.am = am[s]; S.harm = (c->pure && am[s] == 2) ? 1 : 0;
-      S.nao = (S.harm ? 5 : ncart(am[s]));
+      S.am = am[s]; S.harm = (c->pure && am[s] >= 2) ? 1 : 0;
+      S.nao = (S.harm ? 2 * am[s] + 1 : ncart(am[s]));
       S.aoff = aoff;
       S.mrow = row0;
       c->aoff[s] = aoff; c->naos[s] = S.nao;
@@ -929,8 +950,8 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
     CK(cudaGetLastError());
     ++nlaunch;
   }
-  static_assert(NLIST <= 64, "k_bin_scan runs one thread per list in one 64-thread CTA");
-  k_bin_scan<<<1, 64, 0, st>>>(counts, B.caps.as<unsigned long long>(), B.split.as<int>(),
+  static_assert(NLIST <= 128, "k_bin_scan runs one thread per list in one 128-thread CTA");
+  k_bin_scan<<<1, 128, 0, st>>>(counts, B.caps.as<unsigned long long>(), B.split.as<int>(),
                                B.hist.as<unsigned long long>(), B.cursor.as<unsigned long long>(),
                                B.ranges.as<unsigned long long>(), B.flag.as<unsigned>());
   CK(cudaGetLastError());

@@ -217,6 +217,7 @@ struct oqpg_ctx {
   int nshell = 0, nbf = 0, natom = 0, npair = 0, nmol = 1, stride = 0;
   long long ntri = 0, dsh_elems = 0;  // packed elements per density, shell-density elements (whole batch)
   bool pure = false;
+  bool has_f = false;   // an f shell is registered (the gradient then declines)
   double tau = 1e-10;
   std::vector<oqpg::ShellDev> shells;
   std::vector<int> aoff, naos;

@@ -10,21 +10,30 @@ namespace oqpg {
 // pull work from a.work.
 template <typename Kern>
 cudaError_t launch_persistent(Kern kern, size_t smem, long long per_block_items, const BuildArgs& a, int nsm,
-                              cudaStream_t st) {
+                              cudaStream_t st, int threads = 128) {
   if (a.nquartets <= 0) return cudaSuccess;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
   if (a.ctas_per_sm > 0 && a.ctas_per_sm < per_sm) per_sm = a.ctas_per_sm;
   if (per_sm < 1) per_sm = 1;
   long long blocks = (a.nquartets + per_block_items - 1) / per_block_items;
   const long long cap = (long long)nsm * per_sm;
   if (blocks > cap) blocks = cap;
-  kern<<<(unsigned)blocks, 128, smem, st>>>(a);
+  kern<<<(unsigned)blocks, threads, smem, st>>>(a);
   return cudaGetLastError();
+}
+
+// Warps per CTA of a warp-per-quartet kernel: 4 unless the per-warp shared
+// memory of the class (the largest f classes) leaves room for fewer.
+template <int LA, int LB, int LC, int LD, bool PURE, typename T>
+constexpr int team_warps() {
+  constexpr size_t per_warp = sizeof(T) * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
+  constexpr size_t budget = 220 * 1024 - sizeof(int) * Cls<LA, LB, LC, LD>::NE;  // s_offs is static
+  return per_warp * 4 <= budget ? 4 : (per_warp * 2 <= budget ? 2 : 1);
 }
 
 // Classes with more than 27 Cartesian elements run one warp per quartet.
@@ -34,14 +43,15 @@ constexpr bool is_team() { return Cls<LA, LB, LC, LD>::NE > 27; }
 template <int LA, int LB, int LC, int LD, bool PURE, typename T>
 cudaError_t launch_fock(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
   if constexpr (is_team<LA, LB, LC, LD>()) {
-    const size_t smem = sizeof(T) * 4 * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
+    constexpr int W = team_warps<LA, LB, LC, LD, PURE, T>();
+    const size_t smem = sizeof(T) * W * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
     if (kind == MODE_PRIM) {
       if constexpr (prim_parallel(LA, LB, LC, LD))
-        return launch_persistent(k_prim_team<LA, LB, LC, LD, PURE, T>, smem, 4, a, nsm, st);
+        return launch_persistent(k_prim_team<LA, LB, LC, LD, PURE, T>, smem, W, a, nsm, st, 32 * W);
       else
         return cudaErrorInvalidValue;
     }
-    return launch_persistent(k_team<LA, LB, LC, LD, PURE, false, T>, smem, 4, a, nsm, st);
+    return launch_persistent(k_team<LA, LB, LC, LD, PURE, false, T>, smem, W, a, nsm, st, 32 * W);
   } else {
     if (kind == MODE_PRIM) return launch_persistent(k_prim<LA, LB, LC, LD, PURE, T>, 0, 4, a, nsm, st);
     return launch_persistent(k_small<LA, LB, LC, LD, PURE, false, T>, 0, 128, a, nsm, st);
@@ -52,8 +62,9 @@ template <int LA, int LB, int LC, int LD, bool PURE>
 cudaError_t launch_schwarz(const BuildArgs& a, int nsm, cudaStream_t st) {
   if constexpr (LA == LC && LB == LD) {
     if constexpr (is_team<LA, LB, LC, LD>()) {
-      const size_t smem = sizeof(double) * 4 * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
-      return launch_persistent(k_team<LA, LB, LC, LD, PURE, true, double>, smem, 4, a, nsm, st);
+      constexpr int W = team_warps<LA, LB, LC, LD, PURE, double>();
+      const size_t smem = sizeof(double) * W * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
+      return launch_persistent(k_team<LA, LB, LC, LD, PURE, true, double>, smem, W, a, nsm, st, 32 * W);
     } else {
       return launch_persistent(k_small<LA, LB, LC, LD, PURE, true, double>, 0, 128, a, nsm, st);
     }
@@ -77,6 +88,15 @@ cudaError_t launch_df(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
 
 template <int LA, int LB, int LC, int LD>
 cudaError_t launch_cls(bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
+  if constexpr (LA == 3 || LB == 3 || LC == 3 || LD == 3) {
+    // f classes: FP64 kernels only (never on the FP32 lists; FP64 in the df modes)
+    if (mode & MODE_F32) return cudaErrorInvalidValue;
+    const int kind = mode & ~MODE_DF;
+    if (kind == MODE_SCHWARZ)
+      return pure ? launch_schwarz<LA, LB, LC, LD, true>(a, nsm, st) : launch_schwarz<LA, LB, LC, LD, false>(a, nsm, st);
+    return pure ? launch_fock<LA, LB, LC, LD, true, double>(kind, a, nsm, st)
+                : launch_fock<LA, LB, LC, LD, false, double>(kind, a, nsm, st);
+  }
   const bool f32 = (mode & MODE_F32) != 0;
   if (mode & MODE_DF) {
     const int kind = mode & ~(MODE_DF | MODE_F32);

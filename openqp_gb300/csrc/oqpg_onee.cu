@@ -29,10 +29,14 @@ struct Sh {
 
 int ncart1(int l) { return (l + 1) * (l + 2) / 2; }
 
+// Cartesian exponents in OpenQP order (constants.F90:33-60): s; x y z;
+// xx yy zz xy xz yz; xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz.
 void exps_of(int l, int idx, int* e) {
-  static const int T[3][6][3] = {{{0, 0, 0}},
-                                 {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}},
-                                 {{2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}}};
+  static const int T[4][10][3] = {
+      {{0, 0, 0}},
+      {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}},
+      {{2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}},
+      {{3, 0, 0}, {0, 3, 0}, {0, 0, 3}, {2, 1, 0}, {2, 0, 1}, {1, 2, 0}, {0, 2, 1}, {1, 0, 2}, {0, 1, 2}, {1, 1, 1}}};
   e[0] = T[l][idx][0]; e[1] = T[l][idx][1]; e[2] = T[l][idx][2];
 }
 
@@ -55,9 +59,9 @@ void boys_f(int m, double T, double* F) {
   }
 }
 
-// Hermite expansion coefficients E[i][j][t], i <= 2, j <= 4, t <= 6
+// Hermite expansion coefficients E[i][j][t], i <= 3, j <= 5, t <= 8
 struct Herm {
-  double E[3][5][7];
+  double E[4][6][9];
   void build(int imax, int jmax, double p, double PA, double PB) {
     std::memset(E, 0, sizeof(E));
     E[0][0][0] = 1.0;
@@ -66,11 +70,11 @@ struct Herm {
       for (int j = 0; j <= jmax; ++j) {
         if (i == 0 && j == 0) continue;
         for (int t = 0; t <= i + j; ++t) {
-          const double(*src)[7] = (i > 0) ? E[i - 1] : E[i];
+          const double(*src)[9] = (i > 0) ? E[i - 1] : E[i];
           const int jj = (i > 0) ? j : j - 1;
           const double X = (i > 0) ? PA : PB;
           double v = X * src[jj][t];
-          if (t + 1 <= 6) v += (t + 1) * src[jj][t + 1];
+          if (t + 1 <= 8) v += (t + 1) * src[jj][t + 1];
           if (t > 0) v += o * src[jj][t - 1];
           E[i][j][t] = v;
         }
@@ -78,11 +82,11 @@ struct Herm {
   }
 };
 
-// Hermite Coulomb integrals R[t][u][v] for t+u+v <= L <= 4
-void hermite_r(int L, double alpha, double X, double Y, double Z, double R[5][5][5]) {
+// Hermite Coulomb integrals R[t][u][v] for t+u+v <= L <= 6
+void hermite_r(int L, double alpha, double X, double Y, double Z, double R[7][7][7]) {
   double F[9];
   boys_f(L, alpha * (X * X + Y * Y + Z * Z), F);
-  double Rn[5][5][5][5];  // [n][t][u][v]
+  double Rn[7][7][7][7];  // [n][t][u][v]
   double f = 1.0;
   for (int n = 0; n <= L; ++n) { Rn[n][0][0][0] = f * F[n]; f *= -2.0 * alpha; }
   for (int tot = 1; tot <= L; ++tot)
@@ -108,35 +112,57 @@ void hermite_r(int L, double alpha, double X, double Y, double Z, double R[5][5]
       for (int v = 0; v <= L - t - u; ++v) R[t][u][v] = Rn[0][t][u][v];
 }
 
-double cnorm(int l, int idx) { return (l == 2 && idx >= 3) ? 1.7320508075688772 : 1.0; }
+// shells_pnrm2 (constants.F90:110-140)
+double cnorm(int l, int idx) {
+  if (l == 2 && idx >= 3) return 1.7320508075688772;
+  if (l == 3 && idx >= 3) return idx == 9 ? 3.8729833462074170 : 2.2360679774997897;
+  return 1.0;
+}
+
+// pure d and f (m = -l .. l) from normalised Cartesians (int2_pure_generated.F90:119-149)
+const double* pure_row(int l, int m) {
+  static const double D[5][10] = {{0, 0, 0, 1, 0, 0}, {0, 0, 0, 0, 0, 1}, {-0.5, -0.5, 1, 0, 0, 0},
+                                  {0, 0, 0, 0, 1, 0}, {0.86602540378443865, -0.86602540378443865, 0, 0, 0, 0}};
+  static const double F[7][10] = {
+      {0, -0.79056941504209483, 0, 1.0606601717798213, 0, 0, 0, 0, 0, 0},
+      {0, 0, 0, 0, 0, 0, 0, 0, 0, 1},
+      {0, -0.61237243569579452, 0, -0.27386127875258306, 0, 0, 0, 0, 1.0954451150103321, 0},
+      {0, 0, 1, 0, -0.67082039324993691, 0, -0.67082039324993691, 0, 0, 0},
+      {-0.61237243569579452, 0, 0, 0, 0, -0.27386127875258306, 0, 1.0954451150103321, 0, 0},
+      {0, 0, 0, 0, 0.86602540378443865, 0, -0.86602540378443865, 0, 0, 0},
+      {0.79056941504209483, 0, 0, 0, 0, -1.0606601717798213, 0, 0, 0, 0}};
+  return l == 2 ? D[m] : F[m];
+}
 
 // normalise and pure-project a (na x nb) Cartesian block in place; returns dims
 void finish(double* blk, int la, int lb, int ha, int hb, int& da, int& db) {
   const int na = ncart1(la), nb = ncart1(lb);
   for (int i = 0; i < na; ++i)
     for (int j = 0; j < nb; ++j) blk[i * nb + j] *= cnorm(la, i) * cnorm(lb, j);
-  static const double T[5][6] = {{0, 0, 0, 1, 0, 0}, {0, 0, 0, 0, 0, 1}, {-0.5, -0.5, 1, 0, 0, 0},
-                                 {0, 0, 0, 0, 1, 0}, {0.86602540378443865, -0.86602540378443865, 0, 0, 0, 0}};
-  double tmp[36];
+  double tmp[100];
   da = na; db = nb;
-  if (ha && la == 2) {
-    for (int m = 0; m < 5; ++m)
+  if (ha && la >= 2) {
+    const int np = 2 * la + 1;
+    for (int m = 0; m < np; ++m)
       for (int j = 0; j < nb; ++j) {
+        const double* T = pure_row(la, m);
         double v = 0;
-        for (int c = 0; c < 6; ++c) v += T[m][c] * blk[c * nb + j];
+        for (int c = 0; c < na; ++c) v += T[c] * blk[c * nb + j];
         tmp[m * nb + j] = v;
       }
-    da = 5;
+    da = np;
     std::memcpy(blk, tmp, sizeof(double) * da * nb);
   }
-  if (hb && lb == 2) {
+  if (hb && lb >= 2) {
+    const int np = 2 * lb + 1;
     for (int i = 0; i < da; ++i)
-      for (int m = 0; m < 5; ++m) {
+      for (int m = 0; m < np; ++m) {
+        const double* T = pure_row(lb, m);
         double v = 0;
-        for (int c = 0; c < 6; ++c) v += T[m][c] * blk[i * nb + c];
-        tmp[i * 5 + m] = v;
+        for (int c = 0; c < nb; ++c) v += T[c] * blk[i * nb + c];
+        tmp[i * np + m] = v;
       }
-    db = 5;
+    db = np;
     std::memcpy(blk, tmp, sizeof(double) * da * db);
   }
 }
@@ -150,10 +176,10 @@ extern "C" int oqpg_one_electron(int nshell, const int* am, const int* ncontr, c
   std::vector<Sh> sh(nshell);
   int off = 0, aoff = 0;
   for (int s = 0; s < nshell; ++s) {
-    if (am[s] < 0 || am[s] > 2 || origin[s] < 1 || origin[s] > natom) return 3;
+    if (am[s] < 0 || am[s] > 3 || origin[s] < 1 || origin[s] > natom) return 3;
     Sh& S = sh[s];
     S.l = am[s]; S.n = ncontr[s]; S.off = off; S.harm = harmonic ? harmonic[s] : 0;
-    S.nao = (S.harm && S.l == 2) ? 5 : ncart1(S.l);
+    S.nao = (S.harm && S.l >= 2) ? 2 * S.l + 1 : ncart1(S.l);
     S.aoff = aoff;
     for (int d = 0; d < 3; ++d) S.c[d] = xyz[3 * (origin[s] - 1) + d];
     off += S.n; aoff += S.nao;
@@ -164,10 +190,10 @@ extern "C" int oqpg_one_electron(int nshell, const int* am, const int* ncontr, c
     const Sh& A = sh[si];
     const Sh& B = sh[sj];
     const int na = ncart1(A.l), nbb = ncart1(B.l);
-    int ea[6][3], eb[6][3];
+    int ea[10][3], eb[10][3];
     for (int i = 0; i < na; ++i) exps_of(A.l, i, ea[i]);
     for (int i = 0; i < nbb; ++i) exps_of(B.l, i, eb[i]);
-    double blk[36] = {0};
+    double blk[100] = {0};
     double ab2 = 0;
     for (int d = 0; d < 3; ++d) ab2 += (A.c[d] - B.c[d]) * (A.c[d] - B.c[d]);
     for (int p1 = 0; p1 < A.n; ++p1)
@@ -198,7 +224,7 @@ extern "C" int oqpg_one_electron(int nshell, const int* am, const int* ncontr, c
           for (int at = 0; at < natom; ++at) {
             const double Z = charges[at];
             if (Z == 0.0) continue;
-            double R[5][5][5];
+            double R[7][7][7];
             hermite_r(A.l + B.l, p, P[0] - xyz[3 * at], P[1] - xyz[3 * at + 1], P[2] - xyz[3 * at + 2], R);
             const double pref = -Z * 2.0 * kPi / p * K;
             for (int i = 0; i < na; ++i)

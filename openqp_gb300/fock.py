@@ -14,11 +14,11 @@ import numpy as np
 
 from ._lib import FockError, lib, ptr, _i
 
-NCLASS = 21
+NCLASS = 55
 
 
 def class_labels():
-    names = "spd"
+    names = "spdf"
     out = []
     for c in range(NCLASS):
         l4 = (ctypes.c_int * 4)()
@@ -359,7 +359,7 @@ def class_flops(c, nprim, nquart, nk=1, pure=False, nj=1):
     nao = 1
     for l in L:
         nc *= (l + 1) * (l + 2) // 2
-        nao *= (5 if (pure and l == 2) else (l + 1) * (l + 2) // 2)
+        nao *= (2 * l + 1 if (pure and l >= 2) else (l + 1) * (l + 2) // 2)
     dig = 2 * (2 * nj + 4 * nk)
     return 3.0 * R * nc * nprim + dig * nao * nquart
 

@@ -15,10 +15,24 @@ from scipy.special import gammainc, gamma
 from .basis import BasisArrays
 
 _CART = {0: [(0, 0, 0)], 1: [(1, 0, 0), (0, 1, 0), (0, 0, 1)],
-         2: [(2, 0, 0), (0, 2, 0), (0, 0, 2), (1, 1, 0), (1, 0, 1), (0, 1, 1)]}
-_NORM = {0: [1.0], 1: [1.0, 1.0, 1.0], 2: [1.0, 1.0, 1.0, math.sqrt(3), math.sqrt(3), math.sqrt(3)]}
+         2: [(2, 0, 0), (0, 2, 0), (0, 0, 2), (1, 1, 0), (1, 0, 1), (0, 1, 1)],
+         3: [(3, 0, 0), (0, 3, 0), (0, 0, 3), (2, 1, 0), (2, 0, 1), (1, 2, 0), (0, 2, 1), (1, 0, 2), (0, 1, 2),
+             (1, 1, 1)]}
+_NORM = {0: [1.0], 1: [1.0, 1.0, 1.0], 2: [1.0, 1.0, 1.0, math.sqrt(3), math.sqrt(3), math.sqrt(3)],
+         3: [1.0, 1.0, 1.0] + [math.sqrt(5)] * 6 + [math.sqrt(15)]}
 _PURE_D = np.array([[0, 0, 0, 1, 0, 0], [0, 0, 0, 0, 0, 1], [-0.5, -0.5, 1, 0, 0, 0],
                     [0, 0, 0, 0, 1, 0], [math.sqrt(3) / 2, -math.sqrt(3) / 2, 0, 0, 0, 0]])
+# pure f (m = -3 .. 3) from normalised Cartesians (int2_pure_generated.F90:134-149)
+_a, _b, _c, _d, _e = math.sqrt(10) / 4, 3 / (2 * math.sqrt(2)), math.sqrt(6) / 4, math.sqrt(30) / 20, math.sqrt(1.2)
+_g = 3 / (2 * math.sqrt(5))
+_PURE_F = np.array([[0, -_a, 0, _b, 0, 0, 0, 0, 0, 0],
+                    [0, 0, 0, 0, 0, 0, 0, 0, 0, 1],
+                    [0, -_c, 0, -_d, 0, 0, 0, 0, _e, 0],
+                    [0, 0, 1, 0, -_g, 0, -_g, 0, 0, 0],
+                    [-_c, 0, 0, 0, 0, -_d, 0, _e, 0, 0],
+                    [0, 0, 0, 0, math.sqrt(3) / 2, 0, -math.sqrt(3) / 2, 0, 0, 0],
+                    [_a, 0, 0, 0, 0, -_b, 0, 0, 0, 0]])
+_PURE = {2: _PURE_D, 3: _PURE_F}
 
 
 def _os_1d(imax, jmax, PA, PB, p):
@@ -46,10 +60,10 @@ def _os_1d(imax, jmax, PA, PB, p):
 
 def _finish(block, la, lb, ha, hb):
     block = block * np.array(_NORM[la])[:, None] * np.array(_NORM[lb])[None, :]
-    if ha and la == 2:
-        block = _PURE_D @ block
-    if hb and lb == 2:
-        block = block @ _PURE_D.T
+    if ha and la >= 2:
+        block = _PURE[la] @ block
+    if hb and lb >= 2:
+        block = block @ _PURE[lb].T
     return block
 
 

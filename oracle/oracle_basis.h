@@ -74,14 +74,15 @@ void boys(int m, double T, double* F);
 // Cartesian component exponents in OpenQP order (source/constants.F90:33-60):
 // s; x y z; xx yy zz xy xz yz.
 void cart_exps(int l, int idx, int* e);
-// shells_pnrm2 (source/constants.F90:110-140) for l <= 2
+// shells_pnrm2 (source/constants.F90:110-140) for l <= 3
 double cart_norm(int l, int idx);
-// Pure-d projection of normalised Cartesians (source/integrals/int2_pure_generated.F90:119-129)
+// Pure d / f projections of normalised Cartesians (source/integrals/int2_pure_generated.F90:119-149)
 extern const double PURE_D[5][6];
+extern const double PURE_F[7][10];
 
 struct QuartetWork {
-  double acc[6 * 6 * 6 * 6];
-  double tmp[6 * 6 * 6 * 6];
+  double acc[10 * 10 * 10 * 10];
+  double tmp[10 * 10 * 10 * 10];
 };
 
 // Normalised, pure-projected block of the flipped quartet s[]; returns the

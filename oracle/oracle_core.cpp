@@ -17,9 +17,9 @@
 //                           second), with the primitive screening of the
 //                           rotated-axis engine that OpenQP runs for s-d
 //                           quartets (source/integrals/int_rotaxis.F90:292-306,629)
-//   normalisation / pure d  source/integrals/int2.F90:1186-1208 (normalize_ints),
-//                           source/constants.F90:110-140,
-//                           source/integrals/int2_pure_generated.F90:119-129
+//   normalisation / pure    source/integrals/int2.F90:1186-1208 (normalize_ints),
+//                           source/constants.F90:33-60,110-140,
+//                           source/integrals/int2_pure_generated.F90:119-149 (d and f)
 // Rys nodes/weights come from our generated interpolation tables
 // (openqp_gb300/csrc/rys_tables.inc), not from OpenQP's rys.F90 fits.
 #include <algorithm>
@@ -40,16 +40,32 @@ const double PURE_D[5][6] = {
     {0.86602540378443865, -0.86602540378443865, 0, 0, 0, 0},  // x^2 - y^2
 };
 
+// Pure f (m = -3 .. 3) from the normalised Cartesians xxx yyy zzz xxy xxz xyy
+// yyz xzz yzz xyz: the real solid harmonics, e.g. m = 0: z^3 - 3/(2 sqrt 5)
+// (xxz + yyz) in normalised components.
+const double PURE_F[7][10] = {
+    {0, -0.79056941504209483, 0, 1.0606601717798213, 0, 0, 0, 0, 0, 0},   // y(3x^2 - y^2)
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 1},                                         // xyz
+    {0, -0.61237243569579452, 0, -0.27386127875258306, 0, 0, 0, 0, 1.0954451150103321, 0},  // y(4z^2 - r^2)
+    {0, 0, 1, 0, -0.67082039324993691, 0, -0.67082039324993691, 0, 0, 0},  // z(2z^2 - 3r^2)
+    {-0.61237243569579452, 0, 0, 0, 0, -0.27386127875258306, 0, 1.0954451150103321, 0, 0},  // x(4z^2 - r^2)
+    {0, 0, 0, 0, 0.86602540378443865, 0, -0.86602540378443865, 0, 0, 0},  // z(x^2 - y^2)
+    {0.79056941504209483, 0, 0, 0, 0, -1.0606601717798213, 0, 0, 0, 0},   // x(x^2 - 3y^2)
+};
+
 void cart_exps(int l, int idx, int* e) {
-  static const int T[3][6][3] = {
+  static const int T[4][10][3] = {
       {{0, 0, 0}},
       {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}},
-      {{2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}}};
+      {{2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}},
+      {{3, 0, 0}, {0, 3, 0}, {0, 0, 3}, {2, 1, 0}, {2, 0, 1}, {1, 2, 0}, {0, 2, 1}, {1, 0, 2}, {0, 1, 2},
+       {1, 1, 1}}};
   e[0] = T[l][idx][0]; e[1] = T[l][idx][1]; e[2] = T[l][idx][2];
 }
 
 double cart_norm(int l, int idx) {
   if (l == 2 && idx >= 3) return 1.7320508075688772;
+  if (l == 3 && idx >= 3) return idx == 9 ? 3.8729833462074170 : 2.2360679774997897;
   return 1.0;
 }
 
@@ -150,16 +166,17 @@ static void project_index(double* blk, int dims[4], int pos, int l, int harm, do
       if (f != 1.0)
         for (int p = 0; p < post; ++p) blk[(a * n + c) * post + p] *= f;
     }
-  if (!(harm && l == 2)) return;
+  if (!harm || l < 2) return;
+  const int nc = ncart(l), np = 2 * l + 1;
   for (int a = 0; a < pre; ++a)
-    for (int m = 0; m < 5; ++m)
+    for (int m = 0; m < np; ++m)
       for (int p = 0; p < post; ++p) {
         double v = 0;
-        for (int c = 0; c < 6; ++c) v += PURE_D[m][c] * blk[(a * 6 + c) * post + p];
-        tmp[(a * 5 + m) * post + p] = v;
+        for (int c = 0; c < nc; ++c) v += (l == 2 ? PURE_D[m][c] : PURE_F[m][c]) * blk[(a * nc + c) * post + p];
+        tmp[(a * np + m) * post + p] = v;
       }
-  dims[pos] = 5;
-  std::memcpy(blk, tmp, sizeof(double) * pre * 5 * post);
+  dims[pos] = np;
+  std::memcpy(blk, tmp, sizeof(double) * pre * np * post);
 }
 
 long rys_quartet(const Basis& B, const PairStore& PS, const Cutoffs& cut, const int s[4], double* out,
@@ -176,14 +193,14 @@ long rys_quartet(const Basis& B, const PairStore& PS, const Cutoffs& cut, const 
   long nprimq = 0;
   const double AB[3] = {S[0]->c[0] - S[1]->c[0], S[0]->c[1] - S[1]->c[1], S[0]->c[2] - S[1]->c[2]};
   const double CD[3] = {S[2]->c[0] - S[3]->c[0], S[2]->c[1] - S[3]->c[1], S[2]->c[2] - S[3]->c[2]};
-  int ea[6][3], eb[6][3], ec[6][3], ed[6][3];
+  int ea[10][3], eb[10][3], ec[10][3], ed[10][3];
   for (int i = 0; i < na; ++i) cart_exps(la, i, ea[i]);
   for (int i = 0; i < nb; ++i) cart_exps(lb, i, eb[i]);
   for (int i = 0; i < nc; ++i) cart_exps(lc, i, ec[i]);
   for (int i = 0; i < nd; ++i) cart_exps(ld, i, ed[i]);
   // 2D integrals I[root][dim][i][j][k][l], i<=la, j<=lb, k<=lc, l<=ld
-  static thread_local double I2[5][3][3][3][3][3];
-  double G[5][5];
+  static thread_local double I2[7][3][4][4][4][4];
+  double G[7][7];
   for (int q = 0; q < nQ; ++q) {
     const double sq = PS.k[oQ + q] * PS.ginv[oQ + q];
     if (std::fabs(sq) < cut.quartet) continue;
@@ -207,7 +224,7 @@ long rys_quartet(const Basis& B, const PairStore& PS, const Cutoffs& cut, const 
       const double PQ[3] = {P[0] - Q[0], P[1] - Q[1], P[2] - Q[2]};
       const double X = rho * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]);
       const double pref = fqz * std::sqrt(inv);
-      double rx[5], rw[5];
+      double rx[7], rw[7];
       rys_eval(nroots, X, rx, rw);
       for (int r = 0; r < nroots; ++r) {
         const double u = rx[r];
@@ -230,7 +247,7 @@ long rys_quartet(const Basis& B, const PairStore& PS, const Cutoffs& cut, const 
             }
           }
           // HRR bra then ket (int_rys.F90:619-661 in structure)
-          double H[5][3][5];  // H[i][j][m]
+          double H[7][4][7];  // H[i][j][m]
           for (int m = 0; m <= mmax; ++m) {
             for (int i = 0; i <= nmax; ++i) H[i][0][m] = G[i][m];
             for (int j = 1; j <= lb; ++j)
@@ -238,7 +255,7 @@ long rys_quartet(const Basis& B, const PairStore& PS, const Cutoffs& cut, const 
           }
           for (int i = 0; i <= la; ++i)
             for (int j = 0; j <= lb; ++j) {
-              double K2[5][3];
+              double K2[7][4];
               for (int k = 0; k <= mmax; ++k) K2[k][0] = H[i][j][k];
               for (int l = 1; l <= ld; ++l)
                 for (int k = 0; k <= mmax - l; ++k) K2[k][l] = K2[k + 1][l - 1] + CD[d] * K2[k][l - 1];

@@ -41,7 +41,7 @@ static void schwarz(const Basis& B, std::vector<double>& Q, int nthreads, double
 #pragma omp parallel num_threads(nthreads)
   {
     QuartetWork W;
-    std::vector<double> blk(6 * 6 * 6 * 6);
+    std::vector<double> blk(10 * 10 * 10 * 10);
 #pragma omp for schedule(dynamic, 4)
     for (int i = 0; i < ns; ++i) {
       for (int j = 0; j <= i; ++j) {
@@ -247,7 +247,7 @@ static TwoeiCounts twoei(const Basis& B, const PairStore& PS, const Cutoffs& cut
     const int tid = omp_get_thread_num();
     auto flush = make(tid);
     QuartetWork W;
-    std::vector<double> blk(6 * 6 * 6 * 6);
+    std::vector<double> blk(10 * 10 * 10 * 10);
     Store st(50000);
 #pragma omp for schedule(dynamic, 1)
     for (int p = 0; p < np; ++p) {
@@ -769,7 +769,7 @@ int orc_eri_quartet_att(void* h, int i, int j, int k, int l, double mu, double* 
   int s[4], fl[4];
   flip_quartet(B, ids, s, fl);
   QuartetWork W;
-  std::vector<double> blk(6 * 6 * 6 * 6, 0.0);
+  std::vector<double> blk(10 * 10 * 10 * 10, 0.0);
   rys_quartet(B, PS, cutoffs, s, blk.data(), W);
   int n[4], nf[4];
   for (int t = 0; t < 4; ++t) { n[t] = B.sh[ids[t]].nao; nf[t] = B.sh[s[t]].nao; }
@@ -802,7 +802,7 @@ int orc_eri_dense_att(void* h, double mu, double* eri) {
   PairStore PS;
   PS.build(B, cutoffs);
   QuartetWork W;
-  std::vector<double> blk(6 * 6 * 6 * 6, 0.0);
+  std::vector<double> blk(10 * 10 * 10 * 10, 0.0);
   for (int i = 0; i < ns; ++i)
     for (int j = 0; j < ns; ++j)
       for (int k = 0; k < ns; ++k)

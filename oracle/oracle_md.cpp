@@ -92,16 +92,18 @@ void finish_block(const Basis& B, const int* sh, int nidx, std::vector<double>& 
     for (int a = 0; a < pre; ++a)
       for (int c = 0; c < n; ++c)
         for (int p = 0; p < post; ++p) blk[((size_t)a * n + c) * post + p] *= cart_norm(l, c);
-    if (B.sh[sh[pos]].harm && l == 2) {
-      std::vector<double> t((size_t)pre * 5 * post);
+    if (B.sh[sh[pos]].harm && l >= 2) {
+      const int nc = ncart(l), np = 2 * l + 1;
+      std::vector<double> t((size_t)pre * np * post);
       for (int a = 0; a < pre; ++a)
-        for (int m = 0; m < 5; ++m)
+        for (int m = 0; m < np; ++m)
           for (int p = 0; p < post; ++p) {
             double v = 0;
-            for (int c = 0; c < 6; ++c) v += PURE_D[m][c] * blk[((size_t)a * 6 + c) * post + p];
-            t[((size_t)a * 5 + m) * post + p] = v;
+            for (int c = 0; c < nc; ++c)
+              v += (l == 2 ? PURE_D[m][c] : PURE_F[m][c]) * blk[((size_t)a * nc + c) * post + p];
+            t[((size_t)a * np + m) * post + p] = v;
           }
-      dims[pos] = 5;
+      dims[pos] = np;
       blk.swap(t);
     }
   }
@@ -125,7 +127,7 @@ int orc_md_quartet_att(void* h, int i, int j, int k, int l, double mu, double* o
   const Basis& B = ((OrcHandleView*)h)->B;
   const int sh[4] = {i, j, k, l};
   const Shell* S[4] = {&B.sh[i], &B.sh[j], &B.sh[k], &B.sh[l]};
-  int n[4], e[4][6][3];
+  int n[4], e[4][10][3];
   for (int t = 0; t < 4; ++t) {
     n[t] = ncart(S[t]->am);
     for (int c = 0; c < n[t]; ++c) cart_exps(S[t]->am, c, e[t][c]);
@@ -210,7 +212,7 @@ int orc_one_electron(void* h, int which, const double* zq, double* M) {
       const Shell& A = B.sh[si];
       const Shell& C = B.sh[sj];
       const int na = ncart(A.am), nc = ncart(C.am);
-      int ea[6][3], ec[6][3];
+      int ea[10][3], ec[10][3];
       for (int c = 0; c < na; ++c) cart_exps(A.am, c, ea[c]);
       for (int c = 0; c < nc; ++c) cart_exps(C.am, c, ec[c]);
       std::vector<double> blk((size_t)na * nc, 0.0);

@@ -34,7 +34,7 @@ def test_unsupported_angular_momentum_is_declined(libgpu):
     bas = build_basis([8], np.zeros((1, 3)), "6-31g*")
     k = _basis_arrays(bas)
     k[0] = k[0].copy()
-    k[0][-1] = 3   # an f shell
+    k[0][-1] = 4   # a g shell (s-f are supported)
     h = ctypes.c_void_p()
     rc = libgpu.oqpg_create(ctypes.byref(h), len(bas.am), ptr(k[0], _i), ptr(k[1], _i), ptr(k[2], _i), ptr(k[3]),
                             ptr(k[4]), ptr(k[5], _i), 1, ptr(k[6]), 1e-10)
@@ -50,4 +50,8 @@ def test_seam_without_init_declines(libgpu):
 def test_class_table(libgpu):
     from openqp_gb300.fock import class_labels
     lab = class_labels()
-    assert len(lab) == 21 and lab[0] == "(ss|ss)" and lab[-1] == "(dd|dd)"
+    assert len(lab) == 55 and lab[0] == "(ss|ss)" and lab[20] == "(dd|dd)" and lab[-1] == "(ff|ff)"
+    assert lab[21] == "(ss|sf)" and lab[27] == "(sf|sf)"
+    # class index of every (bra type <= ket type) pair: the s-d block first, then the f block
+    seen = set(lab)
+    assert len(seen) == 55

