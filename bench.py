@@ -61,6 +61,9 @@ WORKLOADS = {
     # the differentiation configuration: two-electron gradient of (H2O)16 6-31G(d)
     "grad_water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian RHF two-electron gradient (grd2)", nwater=16,
                                edge=9.52, seed=0, basis="6-31g(d)", cutoff=1e-10, grad=True),
+    # f shells: (H2O)16 cc-pVTZ spherical (one f shell per O, d on H; 928 bf)
+    "water16_ccpvtz": dict(name="(H2O)16 cc-pVTZ spherical RHF J+K Fock build (f shells)", nwater=16, edge=9.52,
+                           seed=0, basis="cc-pvtz", cutoff=1e-10),
     # response-type (TDHF A+B and A-B) builds: 8 trial transition densities per build
     "td_water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian TDHF A+B and A-B build, 8 trial vectors", nwater=16,
                              edge=9.52, seed=0, basis="6-31g(d)", cutoff=1e-10, td=True, nvec=8),
@@ -175,6 +178,23 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def sampled(run, budget_s):
+    """Bounded sample of a quartet loop over the cost-sorted bra pairs.
+    run(stride, offset) times the loop over the pairs p with p % stride ==
+    offset and returns (loop seconds, info).  The stride is refined until the
+    sample fills at least half the budget (or is the whole loop); the timed
+    sample takes the middle pair of every stride (offset stride // 2), since
+    the first pair of the cost-sorted order is the heaviest and offset 0
+    over-weights it.  Returns (estimated full loop seconds, stride, info)."""
+    stride = 997
+    for _ in range(6):
+        t, info = run(stride, stride // 2)
+        if stride == 1 or t >= 0.5 * budget_s:
+            break
+        stride = max(1, int(stride * max(t, 1e-3) / budget_s))
+    return t * stride, stride, info
+
+
 def cpu_baseline(bas, d, budget_s=20.0):
     """Oracle on a bounded sample; returns builds/s and a description."""
     from oracle import oracle
@@ -184,15 +204,18 @@ def cpu_baseline(bas, d, budget_s=20.0):
     t0 = time.perf_counter()
     q = o.schwarz(nthreads=cores)
     t_schwarz = time.perf_counter() - t0
-    _, st = o.fock_jk_sample(d, 997, 0, nthreads=cores, schwarz=q)
-    est_full = max(st["t_twoei"] * 997, 1e-3)
-    stride = max(1, int(math.ceil(est_full / budget_s)))
-    _, st = o.fock_jk_sample(d, stride, 0, nthreads=cores, schwarz=q)
-    t_build = st["t_twoei"] * stride + st["t_init"] + t_schwarz
+
+    def run(stride, offset):
+        _, st = o.fock_jk_sample(d, stride, offset, nthreads=cores, schwarz=q)
+        return st["t_twoei"], st
+
+    t_loop, stride, st = sampled(run, budget_s)
+    t_build = t_loop + st["t_init"] + t_schwarz
     return dict(value=1.0 / t_build, unit="builds/s", cores=cores, kind="port",
-                sample="oracle fock_jk over 1/%d of the cost-sorted shell pairs (offset 0), x%d, plus the full "
-                       "Schwarz set-up (%.2f s) the reference repeats per build; %d quartets in the sample"
-                       % (stride, stride, t_schwarz, st["quartets"])), dict(sample_s=st["t_twoei"], stride=stride)
+                sample="oracle fock_jk over 1/%d of the cost-sorted shell pairs (the middle pair of every %d), x%d, "
+                       "plus the full Schwarz set-up (%.2f s) the reference repeats per build; %d quartets in the sample"
+                       % (stride, stride, stride, t_schwarz, st["quartets"])), dict(sample_s=t_loop / stride,
+                                                                                   stride=stride)
 
 
 def td_workload(overlap="library"):
@@ -217,19 +240,17 @@ def cpu_baseline_td(bas, x, budget_s):
     oracle.build()
     o = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"])
     cores = os.cpu_count()
-    # the bra pairs are cost-sorted, so a sparse sample over-weights the
-    # heaviest pair: refine the stride until the sample fills about half the budget
-    stride = 997
-    for _ in range(4):
-        _, _, st = o.fock_td_sample(x, 3, stride, 0, nthreads=cores)
-        if stride == 1 or st["t_twoei"] >= 0.5 * budget_s:
-            break
-        stride = max(1, int(stride * st["t_twoei"] / budget_s))
-    t = st["t_twoei"] * stride + st["t_setup"]
+
+    def run(stride, offset):
+        _, _, st = o.fock_td_sample(x, 3, stride, offset, nthreads=cores)
+        return st["t_twoei"], st
+
+    t_loop, stride, st = sampled(run, budget_s)
+    t = t_loop + st["t_setup"]
     return {"value": 1.0 / t, "unit": "TD builds/s", "cores": cores, "kind": "port",
             "sample": "oracle int2_td_data_t restatement (A+B and A-B, %d vectors) over 1/%d of the cost-sorted bra "
-                      "shell pairs, x%d, plus the work outside the quartet loop (set-up, reduction; %.2f s); %d "
-                      "quartets in the sample"
+                      "shell pairs (the middle pair of every stride), x%d, plus the work outside the quartet loop "
+                      "(set-up, reduction; %.2f s); %d quartets in the sample"
                       % (x.shape[0], stride, stride, st["t_setup"], st["quartets"])}
 
 
@@ -319,16 +340,17 @@ def cpu_baseline_cam(bas, d, budget_s):
     o = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"])
     cores = os.cpu_count()
     cam = WORKLOAD["cam"]
-    stride = 997
-    for _ in range(4):
-        _, st = o.fock_jk_cam_sample(d, *cam[:3], stride, 0, *cam[3:], nthreads=cores)
-        if stride == 1 or st["t_twoei"] >= 0.5 * budget_s:
-            break
-        stride = max(1, int(stride * st["t_twoei"] / budget_s))
-    t = st["t_twoei"] * stride + (st["t_total"] - st["t_twoei"])
+
+    def run(stride, offset):
+        _, st = o.fock_jk_cam_sample(d, *cam[:3], stride, offset, *cam[3:], nthreads=cores)
+        return st["t_twoei"], st
+
+    t_loop, stride, st = sampled(run, budget_s)
+    t = t_loop + (st["t_total"] - st["t_twoei"])
     return {"value": 1.0 / t, "unit": "builds/s", "cores": cores, "kind": "port",
             "sample": "oracle two-pass CAM build (1/r and erf(mu r)/r, own Schwarz bounds) over 1/%d of the "
-                      "cost-sorted bra shell pairs, x%d, plus set-up; %d quartets in the sample"
+                      "cost-sorted bra shell pairs (the middle pair of every stride), x%d, plus set-up; %d quartets "
+                      "in the sample"
                       % (stride, stride, st["quartets"])}
 
 
@@ -785,16 +807,17 @@ def cpu_baseline_grad(bas, d, budget_s):
     o = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"])
     D = unpack(d, bas.nbf)
     cores = os.cpu_count()
-    t0 = time.perf_counter()
-    o.grad2e(D, nthreads=cores, stride=997, offset=0)
-    est = max((time.perf_counter() - t0) * 997, 1e-3)
-    stride = max(1, int(math.ceil(est / budget_s)))
-    t0 = time.perf_counter()
-    o.grad2e(D, nthreads=cores, stride=stride, offset=0)
-    t = (time.perf_counter() - t0) * stride
+
+    def run(stride, offset):
+        t0 = time.perf_counter()
+        o.grad2e(D, nthreads=cores, stride=stride, offset=offset)
+        return time.perf_counter() - t0, None
+
+    t, stride, _ = sampled(run, budget_s)
     return {"value": 1.0 / t, "unit": "grad evals/s", "cores": cores, "kind": "port",
             "sample": "oracle grd2 restatement (McMurchie-Davidson derivative integrals) over 1/%d of the bra shell "
-                      "pairs, x%d; %d quartets in the sample" % (stride, stride, o.last_grad2e_quartets)}
+                      "pairs (the middle pair of every %d), x%d; %d quartets in the sample"
+                      % (stride, stride, stride, o.last_grad2e_quartets)}
 
 
 def pct(v, q):
