@@ -5,8 +5,8 @@
  * is host memory unless the name says _device.  All entry points return (or
  * store in *info) an OpenQP route-C status code:
  *   0 success, 1 not initialised, 2 out of memory, 3 unsupported input
- *   (angular momentum above f, mixed Cartesian/pure d and f shells, gradients
- *   of bases with f shells), 4 device error.  A non-zero status means the caller's native path must run, which
+ *   (angular momentum above f, mixed Cartesian/pure d and f shells), 4 device
+ *   error.  A non-zero status means the caller's native path must run, which
  *   is exactly the contract of OpenQP's seam (source/modules/routec_bridge.F90:20-22).
  *
  * Two layers:

@@ -282,13 +282,18 @@ __global__ void __launch_bounds__(128) k_grad_lane(const GradArgs g) {
 template <int LA, int LB, int LC, int LD>
 struct GradTeamSmem {
   using G = GCls<LA, LB, LC, LD>;
-  static constexpr int RT = 2 * G::NR;
-  static constexpr int XT = 3 * G::NR * G::N2DX;
-  static constexpr int TT = 3 * G::NR * 4 * G::N2D;   // per root x dim: I, dA, dB, dC
   // classes with more than 16 elements per lane keep the two-particle density
   // block in shared memory instead of registers (and loop over it unrolled by 4)
   static constexpr bool BIG = (Cls<LA, LB, LC, LD>::NE + 31) / 32 > 16;
   static constexpr int GM = BIG ? Cls<LA, LB, LC, LD>::NE : 0;
+  // roots per pass of the table phases: all of them, or one at a time when
+  // the tables of every root would not fit one warp's shared memory (the
+  // largest f classes)
+  static constexpr bool PR = 8 * (2 * G::NR + 3 * G::NR * G::N2DX + 12 * G::NR * G::N2D + GM) > 200 * 1024;
+  static constexpr int RP = PR ? 1 : G::NR;
+  static constexpr int RT = 2 * G::NR;
+  static constexpr int XT = 3 * RP * G::N2DX;
+  static constexpr int TT = 3 * RP * 4 * G::N2D;      // per root x dim: I, dA, dB, dC
   static constexpr int PER_WARP = RT + XT + TT + GM;  // elements of the kernel's type
 };
 
@@ -383,8 +388,10 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
           RT[lane] = (lane & 1) ? v * pqd.pref : v;
         }
         __syncwarp();
-        if (lane < 3 * NR) {
-          const int r = lane / 3, d = lane - 3 * r;
+        constexpr int RP = SM::RP;
+        for (int r0 = 0; r0 < NR; r0 += RP) {
+        if (lane < 3 * RP) {
+          const int rl = lane / 3, d = lane - 3 * rl, r = r0 + rl;
           const T u = RT[2 * r], w = RT[2 * r + 1];
           const T uq = u * pqd.qi, up = u * pqd.pi;
           const T b00 = (T)0.5 * pqd.inv * u;
@@ -393,14 +400,14 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
           const T pqv = pick3(d, pqd.PQ[0], pqd.PQ[1], pqd.PQ[2]);
           const T c00 = fma(-uq, pqv, pick3(d, bp.ax, bp.ay, bp.az));
           const T d00 = fma(up, pqv, pick3(d, kp.ax, kp.ay, kp.az));
-          T* dst = XT + (r * 3 + d) * N2DX;
+          T* dst = XT + (rl * 3 + d) * N2DX;
           twod<LA + 1, LB, LC + 1, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01,
                                           pick3(d, AB[0], AB[1], AB[2]), pick3(d, CD[0], CD[1], CD[2]),
                                           [&](int i, T v) { dst[i] = v; });
         }
         __syncwarp();
         // derivative tables: per root x dim, I, dA, dB, dC over the unraised entries
-        for (int idx = lane; idx < 3 * NR * N2D; idx += 32) {
+        for (int idx = lane; idx < 3 * RP * N2D; idx += 32) {
           const int rd = idx / N2D, n = idx - rd * N2D, d = rd % 3;
           const int a = n / ((LB + 1) * (LC + 1) * (LD + 1)), b = (n / ((LC + 1) * (LD + 1))) % (LB + 1),
                     c = (n / (LD + 1)) % (LC + 1), dd = n % (LD + 1);
@@ -420,7 +427,7 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
         __syncwarp();
         auto contract = [&](int ox, int oy, int oz, T ge) {
 #pragma unroll
-          for (int r = 0; r < NR; ++r) {
+          for (int r = 0; r < RP; ++r) {
             const T* tx = TT + (r * 3 + 0) * 4 * N2D;
             const T* ty = TT + (r * 3 + 1) * 4 * N2D;
             const T* tz = TT + (r * 3 + 2) * 4 * N2D;
@@ -449,6 +456,7 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
           }
         }
         __syncwarp();
+        }
       }
     }
     grad_store<T>(g, P, Q, qd, acc, lane);

@@ -82,9 +82,9 @@ __global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
                            a.ck * (di[kl.x] * dj[kl.y] + di[kl.y] * dj[kl.x]);
       if (!(g < a.cutoff) && !same && !(g * bound < a.cutoff2)) {
         const int tQ = a.pair_type[Q];
-        if (tP <= tQ) { c = tP * 6 - tP * (tP - 1) / 2 + (tQ - tP); ent = make_uint2(P, Q); }
-        else { c = tQ * 6 - tQ * (tQ - 1) / 2 + (tP - tQ); ent = make_uint2(Q, P); }
-        if (g * bound < a.tau32) c += NCLASS;
+        if (tP <= tQ) { c = class_index(tP, tQ); ent = make_uint2(P, Q); }
+        else { c = class_index(tQ, tP); ent = make_uint2(Q, P); }
+        if (g * bound < a.tau32 && !class_has_f(c)) c += NCLASS;  // f classes: FP64 kernels only
         slot = atomicAdd(&cnt[c], 1u);
       }
     }
@@ -103,6 +103,21 @@ __global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
 }  // namespace oqpg
 
 using namespace oqpg;
+
+namespace oqpg {
+cudaError_t launch_grad_f0(int c, const GradArgs& g, int nsm, cudaStream_t st);
+cudaError_t launch_grad_f1(int c, const GradArgs& g, int nsm, cudaStream_t st);
+cudaError_t launch_grad_f2(int c, const GradArgs& g, int nsm, cudaStream_t st);
+cudaError_t launch_grad_f3(int c, const GradArgs& g, int nsm, cudaStream_t st);
+cudaError_t launch_grad_f4(int c, const GradArgs& g, int nsm, cudaStream_t st);
+cudaError_t launch_grad_f(int c, const GradArgs& g, int nsm, cudaStream_t st) {
+  if (c < 30) return launch_grad_f0(c, g, nsm, st);
+  if (c < 38) return launch_grad_f1(c, g, nsm, st);
+  if (c < 45) return launch_grad_f2(c, g, nsm, st);
+  if (c < 50) return launch_grad_f3(c, g, nsm, st);
+  return launch_grad_f4(c, g, nsm, st);
+}
+}  // namespace oqpg
 
 namespace {
 
@@ -176,12 +191,12 @@ void cart_effective(const oqpg_ctx* c, const double* M, double* Mc) {
       for (int x = 0; x < na; ++x)
         for (int y = 0; y < nbc; ++y) {
           double v = 0;
-          const int ma = pa ? 5 : na, mb = pb ? 5 : nbc;
+          const int ma = pa ? 2 * A.am + 1 : na, mb = pb ? 2 * B.am + 1 : nbc;
           for (int p = 0; p < ma; ++p) {
-            const double tp = pa ? pure_d(p, x) : (p == x ? 1.0 : 0.0);
+            const double tp = pa ? pure_coef(A.am, p, x) : (p == x ? 1.0 : 0.0);
             if (tp == 0.0) continue;
             for (int r = 0; r < mb; ++r) {
-              const double tr = pb ? pure_d(r, y) : (r == y ? 1.0 : 0.0);
+              const double tr = pb ? pure_coef(B.am, r, y) : (r == y ? 1.0 : 0.0);
               if (tr == 0.0) continue;
               v += tp * tr * M[(size_t)(A.aoff + p) * nb + B.aoff + r];
             }
@@ -195,7 +210,6 @@ void cart_effective(const oqpg_ctx* c, const double* M, double* Mc) {
 // full AO matrices x, y (and the spin pair xs, ys, both null or both set).
 int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, const double* ys, double cj,
                double ckt, double cks, double cutoff, double* de) {
-  if (c->has_f) return UNSUPPORTED;  // derivative kernels are built for s-d shells only
   if (c->nmol != 1) return UNSUPPORTED;
   int rc;
   if ((rc = grad_init(c))) return rc;
@@ -321,7 +335,8 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
     g.quartets = c->d_glists[li].as<uint2>();
     g.nquartets = (long long)counts[li];
     g.work = c->d_gwork.as<unsigned long long>() + li;
-    GK(cl < 15 ? launch_grad_a(cl, g, f32, c->nsm, st) : launch_grad_b(cl, g, f32, c->nsm, st));
+    GK(cl < 15 ? launch_grad_a(cl, g, f32, c->nsm, st)
+               : cl < NCLASS_SD ? launch_grad_b(cl, g, f32, c->nsm, st) : launch_grad_f(cl, g, c->nsm, st));
   }
   std::vector<double> h_de(3 * c->natom);
   unsigned long long h_cnt[2];

@@ -175,6 +175,7 @@ int ctx_build(oqpg_ctx* c, const Job& job, cudaStream_t st);
 int ensure_att(oqpg_ctx* c, double mu);
 cudaError_t launch_grad_a(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
 cudaError_t launch_grad_b(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
+cudaError_t launch_grad_f(int c, const GradArgs& g, int nsm, cudaStream_t st);  // classes with f, FP64
 
 constexpr int NLIST = 2 * NCLASS;  // FP64 lists, then the FP32 lists of the precision split
 
@@ -217,7 +218,7 @@ struct oqpg_ctx {
   int nshell = 0, nbf = 0, natom = 0, npair = 0, nmol = 1, stride = 0;
   long long ntri = 0, dsh_elems = 0;  // packed elements per density, shell-density elements (whole batch)
   bool pure = false;
-  bool has_f = false;   // an f shell is registered (the gradient then declines)
+  bool has_f = false;   // an f shell is registered
   double tau = 1e-10;
   std::vector<oqpg::ShellDev> shells;
   std::vector<int> aoff, naos;

@@ -35,21 +35,22 @@ extern "C" void orc_schwarz(void* h, double* q, int nthreads);
 
 namespace {
 
-// Cartesian components of l <= 3 in a fixed order; for l <= 2 it is OpenQP's
-// order (source/constants.F90:33-60), l = 3 is internal to this file.
+// Cartesian components of l <= 4 in a fixed order; for l <= 3 it is OpenQP's
+// order (source/constants.F90:33-60), l = 4 (raised f shells) is internal to
+// this file.
 struct CartList {
-  int n[4];
-  int e[4][10][3];
+  int n[5];
+  int e[5][15][3];
   CartList() {
-    for (int l = 0; l <= 3; ++l) {
+    for (int l = 0; l <= 4; ++l) {
       int k = 0;
-      if (l <= 2) {
+      if (l <= 3) {
         for (int c = 0; c < ncart(l); ++c) cart_exps(l, c, e[l][c]);
         k = ncart(l);
       } else {
-        for (int x = 3; x >= 0; --x)
-          for (int y = 3 - x; y >= 0; --y) {
-            e[l][k][0] = x; e[l][k][1] = y; e[l][k][2] = 3 - x - y;
+        for (int x = l; x >= 0; --x)
+          for (int y = l - x; y >= 0; --y) {
+            e[l][k][0] = x; e[l][k][1] = y; e[l][k][2] = l - x - y;
             ++k;
           }
       }
@@ -64,7 +65,7 @@ struct CartList {
 };
 const CartList CL;
 
-// 1D Hermite expansion coefficients E[i][j][t], i, j <= 4
+// 1D Hermite expansion coefficients E[i][j][t], i <= 4, j <= 6
 struct Herm {
   double E[5][7][12];
   void build(int imax, int jmax, double p, double PA, double PB) {
@@ -128,7 +129,7 @@ struct HermR {
   }
 };
 
-// Primitive ERI block over unnormalised Cartesian components (l <= 3 each),
+// Primitive ERI block over unnormalised Cartesian components (l <= 4 each),
 // out[((a*nb + b)*nc + c)*nd + d], without contraction coefficients.
 void prim_eri(const int l[4], const double* C[4], const double ex[4], std::vector<double>& out) {
   const double a = ex[0], b = ex[1], c = ex[2], d = ex[3];
@@ -180,7 +181,7 @@ void prim_eri(const int l[4], const double* C[4], const double ex[4], std::vecto
 }
 
 // Cartesian-effective density of one AO matrix: Dc = N T^T D T N per shell
-// block (T = pure-d projection for pure shells, N = Cartesian norms), in the
+// block (T = pure d / f projection for pure shells, N = Cartesian norms), in the
 // Cartesian layout of the basis (offsets coff).
 void cart_density(const Basis& B, const double* D, const std::vector<int>& coff, int ncart_tot,
                   std::vector<double>& Dc) {
@@ -193,13 +194,14 @@ void cart_density(const Basis& B, const double* D, const std::vector<int>& coff,
       for (int x = 0; x < na; ++x)
         for (int y = 0; y < nc; ++y) {
           double v = 0;
-          const bool pa = A.harm && A.am == 2, pc = C.harm && C.am == 2;
-          const int ma = pa ? 5 : na, mc = pc ? 5 : nc;
+          const bool pa = A.harm && A.am >= 2, pc = C.harm && C.am >= 2;
+          const int ma = pa ? 2 * A.am + 1 : na, mc = pc ? 2 * C.am + 1 : nc;
+          auto pure = [](int l, int m, int c) { return l == 2 ? PURE_D[m][c] : PURE_F[m][c]; };
           for (int p = 0; p < ma; ++p) {
-            const double tp = pa ? PURE_D[p][x] : (p == x ? 1.0 : 0.0);
+            const double tp = pa ? pure(A.am, p, x) : (p == x ? 1.0 : 0.0);
             if (tp == 0.0) continue;
             for (int r = 0; r < mc; ++r) {
-              const double tr = pc ? PURE_D[r][y] : (r == y ? 1.0 : 0.0);
+              const double tr = pc ? pure(C.am, r, y) : (r == y ? 1.0 : 0.0);
               if (tr == 0.0) continue;
               v += tp * tr * D[(size_t)(A.aoff + p) * B.nbf + C.aoff + r];
             }
@@ -243,7 +245,7 @@ long long orc_grad2e(void* h, const double* Dt, const double* Ds, double cj, dou
   for (int s = 0; s < ns; ++s) {
     coff[s] = nct;
     nct += ncart(B.sh[s].am);
-    if (B.sh[s].harm && B.sh[s].am == 2) pure = true;
+    if (B.sh[s].harm && B.sh[s].am >= 2) pure = true;
   }
   std::vector<double> Dtc, Dsc;
   cart_density(B, Dt, coff, nct, Dtc);

@@ -319,3 +319,30 @@ def test_f_shells_rys_matches_md_and_dense_fock(oracle_lib, spherical):
     ref = pack(np.einsum("ijkl,kl->ij", eri, D) - 0.5 * np.einsum("ijkl,jl->ik", eri, D))
     fk = oracle_lib.Oracle(bas, cutoff=1e-10).fock_jk(d)[0]
     assert np.abs(fk - ref).max() < 1e-10
+
+
+@pytest.mark.parametrize("spherical", [True, False])
+def test_grad2e_f_shells_matches_finite_difference(oracle_lib, spherical):
+    """cc-pVTZ water (f on O, d on H): the grd2 restatement with f shells
+    (raised g components) against central differences of E2 (h = 1e-4 Bohr)."""
+    from openqp_gb300 import workloads
+    from openqp_gb300.basis import unpack
+    bas = h2o_basis("cc-pvtz", spherical=spherical)
+    d = workloads.density(bas, 5, 4)
+    n = bas.nbf
+    D = unpack(d, n)
+    g = oracle_lib.Oracle(bas).grad2e(D)
+
+    def e2(xyz):
+        f = oracle_lib.Oracle(bas.with_geometry(xyz), cutoff=1e-12).fock_jk(d)[0]
+        return 0.5 * np.sum(D * unpack(f, n))
+
+    h = 1e-4
+    for at, x in ((0, 2), (1, 0), (2, 1)):
+        xp = bas.xyz.copy()
+        xp[at, x] += h
+        xm = bas.xyz.copy()
+        xm[at, x] -= h
+        fd = (e2(xp) - e2(xm)) / (2 * h)
+        assert abs(fd - g[at, x]) < 2e-7, (at, x, fd, g[at, x])
+    assert np.abs(g.sum(axis=0)).max() < 1e-9
