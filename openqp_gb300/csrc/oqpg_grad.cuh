@@ -291,10 +291,15 @@ struct GradTeamSmem {
   // largest f classes)
   static constexpr bool PR = 8 * (2 * G::NR + 3 * G::NR * G::N2DX + 12 * G::NR * G::N2D + GM) > 200 * 1024;
   static constexpr int RP = PR ? 1 : G::NR;
-  static constexpr int RT = 2 * G::NR;
-  static constexpr int XT = 3 * RP * G::N2DX;
-  static constexpr int TT = 3 * RP * 4 * G::N2D;      // per root x dim: I, dA, dB, dC
-  static constexpr int PER_WARP = RT + XT + TT + GM;  // elements of the kernel's type
+  // primitive quartets evaluated side by side (lane groups of 3 NR lanes in
+  // the table phases), as long as their tables stay small
+  static constexpr int NG0 = 32 / (3 * G::NR) > 0 ? 32 / (3 * G::NR) : 1;
+  static constexpr int NG = (PR || 8 * NG0 * (3 * G::NR * G::N2DX + 12 * G::NR * G::N2D) > 48 * 1024) ? 1 : NG0;
+  static constexpr int RTG = 2 * G::NR + 3;            // per group: x_r, w_r pref, then 2a, 2b, 2c
+  static constexpr int RT = NG * RTG;
+  static constexpr int XT = NG * 3 * RP * G::N2DX;
+  static constexpr int TT = NG * 3 * RP * 4 * G::N2D;  // per group, root x dim: I, dA, dB, dC
+  static constexpr int PER_WARP = RT + XT + TT + GM;   // elements of the kernel's type
 };
 
 template <int LA, int LB, int LC, int LD, typename T>
@@ -370,92 +375,123 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
     T acc[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) acc[k] = 0;
-    for (int kq = 0; kq < Q.pcnt; ++kq) {
-      PP kp;
-      prim_load(prims + Q.poff + kq, kp);
-      const T c2 = (T)2 * GAcc<T>::alpha(g, Q.poff + kq);
-      for (int kb = 0; kb < P.pcnt; ++kb) {
-        PP bp;
-        prim_load(prims + P.poff + kb, bp);
-        if (grad_prim_skip<T>(g, bp.sp * kp.sp, dabmax, bp.p + kp.p)) continue;
-        ++nprim;
+    // candidates c = kq nP + kb in windows of 32: each lane screens one, the
+    // survivors are dealt to the NG lane groups of 3 RP lanes
+    constexpr int NG = SM::NG, RP = SM::RP, RTG = SM::RTG;
+    const int grp = lane / (3 * RP), gl = lane - grp * (3 * RP);
+    const int nP = P.pcnt, total = P.pcnt * Q.pcnt;
+    for (int c0 = 0; c0 < total; c0 += 32) {
+      bool keep = false;
+      {
+        const int cand = c0 + lane;
+        if (cand < total) {
+          const int kq = cand / nP, kb = cand - kq * nP;
+          const PP* b = prims + P.poff + kb;
+          const PP* k = prims + Q.poff + kq;
+          keep = !grad_prim_skip<T>(g, __ldg(&b->sp) * __ldg(&k->sp), dabmax, __ldg(&b->p) + __ldg(&k->p));
+        }
+      }
+      unsigned mask = __ballot_sync(0xffffffffu, keep);
+      while (mask) {
+        const int avail = __popc(mask);
+        const int ng = avail < NG ? avail : NG;
+        unsigned m = mask;
+        for (int i = 0; i < grp && i < ng; ++i) m &= m - 1;
+        const int myc = c0 + __ffs(m) - 1;
+        for (int i = 0; i < ng; ++i) mask &= mask - 1;
+        nprim += ng;
+        const bool active = grp < ng;
+        PP bp, kp;
         PrimQuartet<T> pqd;
-        prim_setup<T>(bp, kp, pqd);
-        const T a2 = (T)2 * GAcc<T>::alpha(g, P.poff + kb);
-        const T b2 = (T)2 * bp.p - a2;
-        if (lane < 2 * NR) {
-          const T v = rys_quantity<NR, T>(pqd.X, lane, g.roots_f32 != 0);
-          RT[lane] = (lane & 1) ? v * pqd.pref : v;
+        T* RTg = RT + grp * RTG;
+        if (active) {
+          const int kq = myc / nP, kb = myc - kq * nP;
+          prim_load(prims + P.poff + kb, bp);
+          prim_load(prims + Q.poff + kq, kp);
+          prim_setup<T>(bp, kp, pqd);
+          for (int q = gl; q < 2 * NR; q += 3 * RP) {  // groups of 3 lanes (one root per pass) loop
+            const T v = rys_quantity<NR, T>(pqd.X, q, g.roots_f32 != 0);
+            RTg[q] = (q & 1) ? v * pqd.pref : v;
+          }
+          if (gl == 0) {
+            const T a2 = (T)2 * GAcc<T>::alpha(g, P.poff + kb);
+            RTg[2 * NR] = a2;
+            RTg[2 * NR + 1] = (T)2 * bp.p - a2;
+            RTg[2 * NR + 2] = (T)2 * GAcc<T>::alpha(g, Q.poff + kq);
+          }
         }
         __syncwarp();
-        constexpr int RP = SM::RP;
         for (int r0 = 0; r0 < NR; r0 += RP) {
-        if (lane < 3 * RP) {
-          const int rl = lane / 3, d = lane - 3 * rl, r = r0 + rl;
-          const T u = RT[2 * r], w = RT[2 * r + 1];
-          const T uq = u * pqd.qi, up = u * pqd.pi;
-          const T b00 = (T)0.5 * pqd.inv * u;
-          const T b10 = fma(-bp.hp, uq, bp.hp);
-          const T b01 = fma(-kp.hp, up, kp.hp);
-          const T pqv = pick3(d, pqd.PQ[0], pqd.PQ[1], pqd.PQ[2]);
-          const T c00 = fma(-uq, pqv, pick3(d, bp.ax, bp.ay, bp.az));
-          const T d00 = fma(up, pqv, pick3(d, kp.ax, kp.ay, kp.az));
-          T* dst = XT + (rl * 3 + d) * N2DX;
-          twod<LA + 1, LB, LC + 1, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01,
-                                          pick3(d, AB[0], AB[1], AB[2]), pick3(d, CD[0], CD[1], CD[2]),
-                                          [&](int i, T v) { dst[i] = v; });
-        }
-        __syncwarp();
-        // derivative tables: per root x dim, I, dA, dB, dC over the unraised entries
-        for (int idx = lane; idx < 3 * RP * N2D; idx += 32) {
-          const int rd = idx / N2D, n = idx - rd * N2D, d = rd % 3;
-          const int a = n / ((LB + 1) * (LC + 1) * (LD + 1)), b = (n / ((LC + 1) * (LD + 1))) % (LB + 1),
-                    c = (n / (LD + 1)) % (LC + 1), dd = n % (LD + 1);
-          const int o = ((a * (LB + 1) + b) * (LC + 2) + c) * (LD + 1) + dd;
-          const T* X = XT + rd * N2DX;
-          const T i0 = X[o], up1 = X[o + G::SA];
-          T vA = a2 * up1, vB = b2 * fma(pick3(d, AB[0], AB[1], AB[2]), i0, up1), vC = c2 * X[o + G::SC];
-          if (a > 0) vA = fma(-(T)a, X[o - G::SA], vA);
-          if (b > 0) vB = fma(-(T)b, X[o - G::SB], vB);
-          if (c > 0) vC = fma(-(T)c, X[o - G::SC], vC);
-          T* Tb = TT + rd * 4 * N2D;
-          Tb[n] = i0;
-          Tb[N2D + n] = vA;
-          Tb[2 * N2D + n] = vB;
-          Tb[3 * N2D + n] = vC;
-        }
-        __syncwarp();
-        auto contract = [&](int ox, int oy, int oz, T ge) {
-#pragma unroll
-          for (int r = 0; r < RP; ++r) {
-            const T* tx = TT + (r * 3 + 0) * 4 * N2D;
-            const T* ty = TT + (r * 3 + 1) * 4 * N2D;
-            const T* tz = TT + (r * 3 + 2) * 4 * N2D;
-            const T ix = tx[ox], iy = ty[oy], iz = tz[oz];
-            const T t1 = ge * iz;
-            const T yz = iy * t1, xz = ix * t1, xy = ix * iy * ge;
-            acc[0] = fma(tx[N2D + ox], yz, acc[0]);
-            acc[1] = fma(ty[N2D + oy], xz, acc[1]);
-            acc[2] = fma(tz[N2D + oz], xy, acc[2]);
-            acc[3] = fma(tx[2 * N2D + ox], yz, acc[3]);
-            acc[4] = fma(ty[2 * N2D + oy], xz, acc[4]);
-            acc[5] = fma(tz[2 * N2D + oz], xy, acc[5]);
-            acc[6] = fma(tx[3 * N2D + ox], yz, acc[6]);
-            acc[7] = fma(ty[3 * N2D + oy], xz, acc[7]);
-            acc[8] = fma(tz[3 * N2D + oz], xy, acc[8]);
+          if (active) {
+            const int rl = gl / 3, d = gl - 3 * rl, r = r0 + rl;
+            const T u = RTg[2 * r], w = RTg[2 * r + 1];
+            const T uq = u * pqd.qi, up = u * pqd.pi;
+            const T b00 = (T)0.5 * pqd.inv * u;
+            const T b10 = fma(-bp.hp, uq, bp.hp);
+            const T b01 = fma(-kp.hp, up, kp.hp);
+            const T pqv = pick3(d, pqd.PQ[0], pqd.PQ[1], pqd.PQ[2]);
+            const T c00 = fma(-uq, pqv, pick3(d, bp.ax, bp.ay, bp.az));
+            const T d00 = fma(up, pqv, pick3(d, kp.ax, kp.ay, kp.az));
+            T* dst = XT + ((grp * RP + rl) * 3 + d) * N2DX;
+            twod<LA + 1, LB, LC + 1, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01,
+                                            pick3(d, AB[0], AB[1], AB[2]), pick3(d, CD[0], CD[1], CD[2]),
+                                            [&](int i, T v) { dst[i] = v; });
           }
-        };
-        if constexpr (BIG) {
+          __syncwarp();
+          // derivative tables: per group, root x dim: I, dA, dB, dC over the unraised entries
+          for (int idx = lane; idx < ng * 3 * RP * N2D; idx += 32) {
+            const int grd = idx / N2D, n = idx - grd * N2D, d = grd % 3, gg = grd / (3 * RP);
+            const T* Rg = RT + gg * RTG;
+            const T a2 = Rg[2 * NR], b2 = Rg[2 * NR + 1], c2 = Rg[2 * NR + 2];
+            const int a = n / ((LB + 1) * (LC + 1) * (LD + 1)), b = (n / ((LC + 1) * (LD + 1))) % (LB + 1),
+                      c = (n / (LD + 1)) % (LC + 1), dd = n % (LD + 1);
+            const int o = ((a * (LB + 1) + b) * (LC + 2) + c) * (LD + 1) + dd;
+            const T* X = XT + grd * N2DX;
+            const T i0 = X[o], up1 = X[o + G::SA];
+            T vA = a2 * up1, vB = b2 * fma(pick3(d, AB[0], AB[1], AB[2]), i0, up1), vC = c2 * X[o + G::SC];
+            if (a > 0) vA = fma(-(T)a, X[o - G::SA], vA);
+            if (b > 0) vB = fma(-(T)b, X[o - G::SB], vB);
+            if (c > 0) vC = fma(-(T)c, X[o - G::SC], vC);
+            T* Tb = TT + grd * 4 * N2D;
+            Tb[n] = i0;
+            Tb[N2D + n] = vA;
+            Tb[2 * N2D + n] = vB;
+            Tb[3 * N2D + n] = vC;
+          }
+          __syncwarp();
+          auto contract = [&](int ox, int oy, int oz, T ge) {
+            for (int gg = 0; gg < ng; ++gg) {
+#pragma unroll
+              for (int r = 0; r < RP; ++r) {
+                const T* tx = TT + ((gg * RP + r) * 3 + 0) * 4 * N2D;
+                const T* ty = TT + ((gg * RP + r) * 3 + 1) * 4 * N2D;
+                const T* tz = TT + ((gg * RP + r) * 3 + 2) * 4 * N2D;
+                const T ix = tx[ox], iy = ty[oy], iz = tz[oz];
+                const T t1 = ge * iz;
+                const T yz = iy * t1, xz = ix * t1, xy = ix * iy * ge;
+                acc[0] = fma(tx[N2D + ox], yz, acc[0]);
+                acc[1] = fma(ty[N2D + oy], xz, acc[1]);
+                acc[2] = fma(tz[N2D + oz], xy, acc[2]);
+                acc[3] = fma(tx[2 * N2D + ox], yz, acc[3]);
+                acc[4] = fma(ty[2 * N2D + oy], xz, acc[4]);
+                acc[5] = fma(tz[2 * N2D + oz], xy, acc[5]);
+                acc[6] = fma(tx[3 * N2D + ox], yz, acc[6]);
+                acc[7] = fma(ty[3 * N2D + oy], xz, acc[7]);
+                acc[8] = fma(tz[3 * N2D + oz], xy, acc[8]);
+              }
+            }
+          };
+          if constexpr (BIG) {
 #pragma unroll 4
-          for (int e = lane; e < NE; e += 32) contract(K::off2d(e, 0), K::off2d(e, 1), K::off2d(e, 2), GM[e]);
-        } else {
+            for (int e = lane; e < NE; e += 32) contract(K::off2d(e, 0), K::off2d(e, 1), K::off2d(e, 2), GM[e]);
+          } else {
 #pragma unroll
-          for (int k = 0; k < KE; ++k) {
-            if (lane + 32 * k < NE)
-              contract(offs[k] & 1023, (offs[k] >> 10) & 1023, offs[k] >> 20, gam[k]);
+            for (int k = 0; k < KE; ++k) {
+              if (lane + 32 * k < NE)
+                contract(offs[k] & 1023, (offs[k] >> 10) & 1023, offs[k] >> 20, gam[k]);
+            }
           }
-        }
-        __syncwarp();
+          __syncwarp();
         }
       }
     }
