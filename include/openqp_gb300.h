@@ -113,6 +113,33 @@ void routec_fock_td(const double* d2, double* apb, double* amb, const int* nbf, 
 void routec_fock_mrsf(const double* d3, double* f3, const int* nbf, const int* nvec, const int* nmat,
                       const double* se, const double* sc, int* info);
 
+/* routec_fock_tdgrd replaces int2_tdgrd_data_t (source/tdhf_lib.F90:228-295,
+ * the int2_td_data_t parallel_stop :89-111), used by the SF / MRSF Z-vector
+ * solvers (modules/tdhf_sf_z_vector.F90:252,377,489,
+ * modules/tdhf_mrsf_z_vector.F90:1009,1737).  d2(nbf, nbf, 2) the alpha /
+ * beta densities, apb / amb (nbf, nbf, 2) OVERWRITTEN; flags OQPG_TD_APB /
+ * OQPG_TD_AMB; amb(:,:,2) comes back zero as in the reference.  cam = NULL
+ * for the plain build, else the five CAM values of routec_fock_jk_cam (the
+ * int2_run_cam two-pass build the callers request for CAM functionals).
+ *
+ * routec_fock_rpagrd replaces int2_rpagrd_data_t (source/tdhf_lib.F90:
+ * 1068-1322), used by the TDHF / TDDFT gradient
+ * (modules/tdhf_z_vector.F90:341,484).  xpy(nbf, nbf, ldp, np),
+ * xmy(nbf, nbf, ldm, nm), t(nbf, nbf, ldt, nt) (ld >= nspin; a count of 0
+ * leaves the pointer unread), hpp(nbf, nbf, nspin, np) = H+[X+Y],
+ * hpt(.., nt) = H+[T], hmm(.., nm) = H-[X-Y], OVERWRITTEN.  H+ is formed from
+ * the symmetric part of its operand (every reference caller passes symmetric
+ * matrices; for other operands the reference's own sum depends on its quartet
+ * order); H- fills spin component 1 only.  The screening density covers
+ * every ld component of xpy and xmy (both only when np > 0) and of t, as
+ * the reference's init_screen does. */
+void routec_fock_tdgrd(const double* d2, double* apb, double* amb, const int* nbf, const int* flags, const double* se,
+                       const double* sc, const double* cam, int* info);
+void routec_fock_rpagrd(const double* xpy, const int* ldp, const int* np, const double* xmy, const int* ldm,
+                        const int* nm, const double* t, const int* ldt, const int* nt, const int* nspin, const int* nbf,
+                        double* hpp, double* hpt, double* hmm, const double* se, const double* sc, const double* cam,
+                        int* info);
+
 /* CAM (range-separated) build of routec_fock_jk's packed densities, the
  * path the reference runs natively for CAM functionals
  * (source/scf_addons.F90:1136-1167 skips the seam for them): int2_run_cam
@@ -290,6 +317,20 @@ int oqpg_fock_td_device(oqpg_ctx* ctx, const double* d2, double* apb, double* am
 int oqpg_fock_mrsf(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, double se, double sc);
 int oqpg_fock_mrsf_device(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
                           void* stream);
+
+/* Gradient-side response builds (layouts in routec_fock_tdgrd /
+ * routec_fock_rpagrd); cam = NULL or the five CAM values.  The _device forms
+ * take device pointers and run on the given stream (null: the context's). */
+int oqpg_fock_tdgrd(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, int flags, double se, double sc,
+                    const double* cam);
+int oqpg_fock_tdgrd_device(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, int flags, double se,
+                           double sc, const double* cam, void* stream);
+int oqpg_fock_rpagrd(oqpg_ctx* ctx, const double* xpy, int ldp, int np, const double* xmy, int ldm, int nm,
+                     const double* t, int ldt, int nt, int nspin, double* hpp, double* hpt, double* hmm, double se,
+                     double sc, const double* cam);
+int oqpg_fock_rpagrd_device(oqpg_ctx* ctx, const double* xpy, int ldp, int np, const double* xmy, int ldm, int nm,
+                            const double* t, int ldt, int nt, int nspin, double* hpp, double* hpt, double* hmm,
+                            double se, double sc, const double* cam, void* stream);
 
 /* CAM forms (see routec_fock_jk_cam for cam[5]).  The TD build's two passes
  * accumulate before the A+B symmetrisation, as the reference's

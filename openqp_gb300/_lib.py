@@ -88,6 +88,18 @@ def lib():
         L.oqpg_fock_mrsf_cam.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d]
         L.routec_fock_jk_cam.argtypes = [_d, _d, _i, _i, _d, _i]
         L.routec_fock_jk_cam.restype = None
+        L.oqpg_fock_tdgrd.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double, _d]
+        L.oqpg_fock_tdgrd_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_int, ctypes.c_double, ctypes.c_double, _d, ctypes.c_void_p]
+        _rpa = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                ctypes.c_double, ctypes.c_double, _d]
+        L.oqpg_fock_rpagrd.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + _rpa
+        L.oqpg_fock_rpagrd_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + _rpa + [ctypes.c_void_p]
+        L.routec_fock_tdgrd.argtypes = [_d, _d, _d, _i, _i, _d, _d, _d, _i]
+        L.routec_fock_tdgrd.restype = None
+        L.routec_fock_rpagrd.argtypes = [_d, _i, _i, _d, _i, _i, _d, _i, _i, _i, _i, _d, _d, _d, _d, _d, _d, _i]
+        L.routec_fock_rpagrd.restype = None
         _lib = L
     return _lib
 

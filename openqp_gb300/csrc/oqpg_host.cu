@@ -1518,6 +1518,28 @@ void routec_fock_mrsf(const double* d3, double* f3, const int* nbf, const int* n
   if (info) *info = rc;
 }
 
+void routec_fock_tdgrd(const double* d2, double* apb, double* amb, const int* nbf, const int* flags, const double* se,
+                       const double* sc, const double* cam, int* info) {
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!d2 || !apb || !amb || !nbf || !flags || !se || !sc) rc = UNSUPPORTED;
+  else if (*nbf != g_ctx->nbf) rc = NOT_INIT;
+  else rc = oqpg_fock_tdgrd(g_ctx, d2, apb, amb, *flags, *se, *sc, cam);
+  if (info) *info = rc;
+}
+
+void routec_fock_rpagrd(const double* xpy, const int* ldp, const int* np, const double* xmy, const int* ldm,
+                        const int* nm, const double* t, const int* ldt, const int* nt, const int* nspin, const int* nbf,
+                        double* hpp, double* hpt, double* hmm, const double* se, const double* sc, const double* cam,
+                        int* info) {
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!ldp || !np || !ldm || !nm || !ldt || !nt || !nspin || !nbf || !se || !sc) rc = UNSUPPORTED;
+  else if (*nbf != g_ctx->nbf) rc = NOT_INIT;
+  else rc = oqpg_fock_rpagrd(g_ctx, xpy, *ldp, *np, xmy, *ldm, *nm, t, *ldt, *nt, *nspin, hpp, hpt, hmm, *se, *sc, cam);
+  if (info) *info = rc;
+}
+
 void routec_fock_jk_batch(const double* d, double* f, const int* nmol, const int* nfocks, const double* se,
                           const double* sc, int* info) {
   std::lock_guard<std::mutex> lk(g_mutex);

@@ -5,6 +5,11 @@
 //  * int2_td_data_t (tdhf_lib.F90:140-224, parallel_stop :89-111): TDHF / TDDFT
 //    A+B and A-B products, CPHF (modules/cphf.F90:193), NMR shielding
 //    (modules/nmr_shielding.F90:454-487);
+//  * int2_tdgrd_data_t (tdhf_lib.F90:228-295): the spin-adapted A+B / A-B of
+//    the SF and MRSF Z-vector equations (modules/tdhf_sf_z_vector.F90:252,
+//    modules/tdhf_mrsf_z_vector.F90:1009, 1737);
+//  * int2_rpagrd_data_t (tdhf_lib.F90:1068-1322): H+[X+Y], H+[T], H-[X-Y] of
+//    the TDHF / TDDFT gradient (modules/tdhf_z_vector.F90:341, 484);
 //  * int2_mrsf_data_t (tdhf_mrsf_lib.F90:218-333, pass 1) and
 //    int2_umrsf_data_t (tdhf_mrsf_lib.F90:337-426, pass 1): MRSF / UMRSF
 //    sigma vectors.
@@ -288,6 +293,110 @@ void mrsf_cam2_job(const oqpg_ctx* c, const double* d3, double* f3, int nvec, in
   g.accumulate = true;
 }
 
+// int2_tdgrd_data_t recipe (tdhf_lib.F90:228-295 with the int2_td_data_t
+// parallel_stop): d2 / apb / amb (n, n, 2) Fortran column-major, D1, D2 the two
+// spin densities:
+//   A+B, spin s (after the symmetrisation): 2 sc J[D1 + D2] - 2 se K[Ds_s]
+//   A-B, spin 1: -2 se K[D1a];  spin 2: zero
+void tdgrd_job(const oqpg_ctx* c, const double* d2, double* apb, double* amb, int flags, double se, double sc,
+               GenJob& g) {
+  const long long n = c->nbf, nn = n * n;
+  const bool want_apb = flags & OQPG_TD_APB, want_amb = flags & OQPG_TD_AMB;
+  g.in = d2;
+  g.in_rs = 1; g.in_cs = n;
+  g.out_rs = 1; g.out_cs = n;
+  if (want_apb)
+    for (int v = 0; v < 2; ++v) g.slices.push_back(GenSlice{v * nn, +1, 0});
+  const int ka = (int)g.slices.size();
+  if (want_amb) g.slices.push_back(GenSlice{0, -1, 0});
+  g.nj = want_apb ? 2 : 0;
+  g.k0 = 0;
+  g.nk = (int)g.slices.size();
+  for (int v = 0; v < 2; ++v) g.screen.push_back(v * nn);
+  for (int v = 0; v < 2; ++v) {
+    GenOut o{apb + v * nn, (int)g.terms.size(), 0};
+    if (want_apb) {
+      g.terms.push_back(term(2.0 * sc, 0, 0, +1));
+      g.terms.push_back(term(2.0 * sc, 0, 1, +1));
+      g.terms.push_back(term(-2.0 * se, 1, v, +1));
+    }
+    o.nterm = (int)g.terms.size() - o.term0;
+    g.outs.push_back(o);
+  }
+  for (int v = 0; v < 2; ++v) {
+    GenOut o{amb + v * nn, (int)g.terms.size(), 0};
+    if (want_amb && v == 0) g.terms.push_back(term(-2.0 * se, 1, ka, -1));
+    o.nterm = (int)g.terms.size() - o.term0;
+    g.outs.push_back(o);
+  }
+}
+
+// Operand layout of an int2_rpagrd_data_t build in one device block: xpy
+// (n, n, ldp, np), then xmy (n, n, ldm, nm), then t (n, n, ldt, nt); outputs
+// hpp (n, n, nspin, np), hpt (n, n, nspin, nt), hmm (n, n, nspin, nm).
+struct RpaDims {
+  int np, ldp, nm, ldm, nt, ldt, nspin;
+  long long xpy_off() const { return 0; }
+  long long xmy_off(long long nn) const { return nn * ldp * np; }
+  long long t_off(long long nn) const { return xmy_off(nn) + nn * ldm * nm; }
+  long long in_elems(long long nn) const { return t_off(nn) + nn * ldt * nt; }
+  long long out_elems(long long nn) const { return nn * nspin * (np + nt + nm); }
+};
+
+// int2_rpagrd_data_t recipe (tdhf_lib.F90:1177-1322 with parallel_stop
+// :1113-1145).  With V a vector of xpy or t and S = spin component:
+//   nspin 1: H+[V] = 4 sc J[V1] - 2 se K[V1]
+//   nspin 2: H+[V]_s = 2 sc J[V1 + V2] - 2 se K[V_s]
+//   H-[V]: spin 1 -2 se K[V1a], other spin zero
+// H+ is taken of the symmetric part of V: every caller passes symmetric
+// matrices (modules/tdhf_z_vector.F90:325-331, 439-447), and for a
+// non-symmetric V the reference's sum depends on its quartet ordering.  The
+// shell density is the maximum over every component of xpy and xmy (both
+// only when np > 0) and of t (init_screen, tdhf_lib.F90:1161-1173).
+void rpagrd_job(const oqpg_ctx* c, const double* in, const RpaDims& R, double* out, double se, double sc, GenJob& g) {
+  const long long n = c->nbf, nn = n * n;
+  g.in = in;
+  g.in_rs = 1; g.in_cs = n;
+  g.out_rs = 1; g.out_cs = n;
+  const int ns = R.nspin;
+  // symmetric slices of the H+ operands first (they feed J and K), then the
+  // antisymmetric ones of H-
+  auto plus_base = [&](int set, int v, int s) {
+    return set == 0 ? R.xpy_off() + nn * ((long long)v * R.ldp + s) : R.t_off(nn) + nn * ((long long)v * R.ldt + s);
+  };
+  const int nplus = R.np + R.nt;
+  for (int u = 0; u < nplus; ++u) {
+    const int set = u < R.np ? 0 : 1, v = u < R.np ? u : u - R.np;
+    for (int s = 0; s < ns; ++s) g.slices.push_back(GenSlice{plus_base(set, v, s), +1, 0});
+  }
+  const int km = (int)g.slices.size();
+  for (int v = 0; v < R.nm; ++v) g.slices.push_back(GenSlice{R.xmy_off(nn) + nn * (long long)v * R.ldm, -1, 0});
+  g.nj = km;
+  g.k0 = 0;
+  g.nk = (int)g.slices.size();
+  if (R.np > 0) {
+    for (long long q = 0; q < (long long)R.ldp * R.np; ++q) g.screen.push_back(R.xpy_off() + q * nn);
+    for (long long q = 0; q < (long long)R.ldm * R.nm; ++q) g.screen.push_back(R.xmy_off(nn) + q * nn);
+  }
+  for (long long q = 0; q < (long long)R.ldt * R.nt; ++q) g.screen.push_back(R.t_off(nn) + q * nn);
+  const double cj = ns == 1 ? 4.0 * sc : 2.0 * sc;
+  for (int u = 0; u < nplus; ++u)
+    for (int s = 0; s < ns; ++s) {
+      GenOut o{out + nn * ((long long)u * ns + s), (int)g.terms.size(), 0};
+      for (int s2 = 0; s2 < ns; ++s2) g.terms.push_back(term(cj, 0, u * ns + s2, +1));
+      g.terms.push_back(term(-2.0 * se, 1, u * ns + s, +1));
+      o.nterm = (int)g.terms.size() - o.term0;
+      g.outs.push_back(o);
+    }
+  for (int v = 0; v < R.nm; ++v)
+    for (int s = 0; s < ns; ++s) {
+      GenOut o{out + nn * ((long long)(nplus + v) * ns + s), (int)g.terms.size(), 0};
+      if (s == 0) g.terms.push_back(term(-2.0 * se, 1, km + v, -1));
+      o.nterm = (int)g.terms.size() - o.term0;
+      g.outs.push_back(o);
+    }
+}
+
 int run_job(oqpg_ctx* c, const GenJob& g, cudaStream_t st, double inv_mu2 = 0.0) {
   Job j;
   j.gen = &g;
@@ -318,6 +427,33 @@ int host_job(oqpg_ctx* c, const double* in, size_t in_elems, double* const* host
   }
   CKR(cudaStreamSynchronize(st));
   return OK;
+}
+
+// One build, or the two CAM passes (cam = {alpha, beta, mu, alpha_coulomb,
+// beta_coulomb}), of the recipe make(se, sc, job) on stream st.
+template <class Make>
+int run_scaled(oqpg_ctx* c, const double* cam, double se, double sc, cudaStream_t st, Make make) {
+  if (!cam) {
+    GenJob g;
+    make(se, sc, g);
+    return run_job(c, g, st);
+  }
+  int rc;
+  if ((rc = ensure_att(c, cam[2]))) return rc;
+  GenJob g1, g2;
+  make(cam[0], cam[3], g1);
+  make(cam[1], cam[4], g2);
+  g2.accumulate = true;
+  if ((rc = run_job(c, g1, st))) return rc;
+  return run_job(c, g2, st, 1.0 / (cam[2] * cam[2]));
+}
+
+bool rpa_dims_ok(const RpaDims& R, const double* xpy, const double* xmy, const double* t) {
+  if (R.nspin != 1 && R.nspin != 2) return false;
+  if (R.np < 0 || R.nm < 0 || R.nt < 0) return false;
+  if ((R.np && (!xpy || R.ldp < R.nspin)) || (R.nm && (!xmy || R.ldm < R.nspin)) || (R.nt && (!t || R.ldt < R.nspin)))
+    return false;
+  return true;
 }
 
 bool td_args_ok(const oqpg_ctx* c, int nvec, int flags) {
@@ -409,6 +545,82 @@ int oqpg_fock_mrsf_cam(oqpg_ctx* ctx, const double* d3, double* f3, int nvec, in
   double* outs[1] = {f3};
   const size_t elems[1] = {tot};
   return host_job(ctx, d3, tot, outs, elems, 1, g1, &g2, 1.0 / (cam[2] * cam[2]));
+}
+
+int oqpg_fock_tdgrd_device(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, int flags, double se,
+                           double sc, const double* cam, void* stream) {
+  if (!ctx || ctx->nmol != 1 || (flags & ~(OQPG_TD_APB | OQPG_TD_AMB)) || !d2 || !apb || !amb) return UNSUPPORTED;
+  if (cam && !cam_ok(cam)) return UNSUPPORTED;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  int rc = run_scaled(ctx, cam, se, sc, st, [&](double x, double y, GenJob& g) {
+    tdgrd_job(ctx, d2, apb, amb, flags, x, y, g);
+  });
+  if (rc) return rc;
+  return cudaStreamSynchronize(st) == cudaSuccess ? OK : DEV_ERR;
+}
+
+int oqpg_fock_tdgrd(oqpg_ctx* ctx, const double* d2, double* apb, double* amb, int flags, double se, double sc,
+                    const double* cam) {
+  if (!ctx || ctx->nmol != 1 || (flags & ~(OQPG_TD_APB | OQPG_TD_AMB)) || !d2 || !apb || !amb) return UNSUPPORTED;
+  if (cam && !cam_ok(cam)) return UNSUPPORTED;
+  const size_t tot = (size_t)ctx->nbf * ctx->nbf * 2;
+  if (ctx->d_dp.ensure(sizeof(double) * tot) != cudaSuccess) return NO_MEM;
+  if (ctx->d_f.ensure(sizeof(double) * 2 * tot) != cudaSuccess) return NO_MEM;
+  cudaStream_t st = ctx->stream;
+  double* dp = ctx->d_dp.as<double>();
+  double* f = ctx->d_f.as<double>();
+  CKR(cudaMemcpyAsync(dp, d2, sizeof(double) * tot, cudaMemcpyHostToDevice, st));
+  int rc = run_scaled(ctx, cam, se, sc, st, [&](double x, double y, GenJob& g) {
+    tdgrd_job(ctx, dp, f, f + tot, flags, x, y, g);
+  });
+  if (rc) return rc;
+  CKR(cudaMemcpyAsync(apb, f, sizeof(double) * tot, cudaMemcpyDeviceToHost, st));
+  CKR(cudaMemcpyAsync(amb, f + tot, sizeof(double) * tot, cudaMemcpyDeviceToHost, st));
+  CKR(cudaStreamSynchronize(st));
+  return OK;
+}
+
+// Shared body of the host and device RPA-gradient forms: the three operand
+// arrays are gathered into the context's d_dp (copy kind `kind`), the outputs
+// come back from d_f (to hpp / hpt / hmm with kind `back`).
+static int rpagrd_body(oqpg_ctx* ctx, const double* xpy, int ldp, int np, const double* xmy, int ldm, int nm,
+                       const double* t, int ldt, int nt, int nspin, double* hpp, double* hpt, double* hmm, double se,
+                       double sc, const double* cam, cudaStream_t st, cudaMemcpyKind kind, cudaMemcpyKind back) {
+  const RpaDims R{np, ldp, nm, ldm, nt, ldt, nspin};
+  if (!ctx || ctx->nmol != 1 || !rpa_dims_ok(R, xpy, xmy, t)) return UNSUPPORTED;
+  if ((np && !hpp) || (nt && !hpt) || (nm && !hmm)) return UNSUPPORTED;
+  if (cam && !cam_ok(cam)) return UNSUPPORTED;
+  const long long nn = (long long)ctx->nbf * ctx->nbf;
+  if (ctx->d_dp.ensure(sizeof(double) * std::max<long long>(R.in_elems(nn), 1)) != cudaSuccess) return NO_MEM;
+  if (ctx->d_f.ensure(sizeof(double) * std::max<long long>(R.out_elems(nn), 1)) != cudaSuccess) return NO_MEM;
+  double* dp = ctx->d_dp.as<double>();
+  double* f = ctx->d_f.as<double>();
+  if (np) CKR(cudaMemcpyAsync(dp + R.xpy_off(), xpy, sizeof(double) * nn * ldp * np, kind, st));
+  if (nm) CKR(cudaMemcpyAsync(dp + R.xmy_off(nn), xmy, sizeof(double) * nn * ldm * nm, kind, st));
+  if (nt) CKR(cudaMemcpyAsync(dp + R.t_off(nn), t, sizeof(double) * nn * ldt * nt, kind, st));
+  int rc = run_scaled(ctx, cam, se, sc, st, [&](double x, double y, GenJob& g) { rpagrd_job(ctx, dp, R, f, x, y, g); });
+  if (rc) return rc;
+  const long long blk = nn * nspin;
+  if (np) CKR(cudaMemcpyAsync(hpp, f, sizeof(double) * blk * np, back, st));
+  if (nt) CKR(cudaMemcpyAsync(hpt, f + blk * np, sizeof(double) * blk * nt, back, st));
+  if (nm) CKR(cudaMemcpyAsync(hmm, f + blk * (np + nt), sizeof(double) * blk * nm, back, st));
+  CKR(cudaStreamSynchronize(st));
+  return OK;
+}
+
+int oqpg_fock_rpagrd(oqpg_ctx* ctx, const double* xpy, int ldp, int np, const double* xmy, int ldm, int nm,
+                     const double* t, int ldt, int nt, int nspin, double* hpp, double* hpt, double* hmm, double se,
+                     double sc, const double* cam) {
+  return rpagrd_body(ctx, xpy, ldp, np, xmy, ldm, nm, t, ldt, nt, nspin, hpp, hpt, hmm, se, sc, cam,
+                     ctx ? ctx->stream : nullptr, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost);
+}
+
+int oqpg_fock_rpagrd_device(oqpg_ctx* ctx, const double* xpy, int ldp, int np, const double* xmy, int ldm, int nm,
+                            const double* t, int ldt, int nt, int nspin, double* hpp, double* hpt, double* hmm,
+                            double se, double sc, const double* cam, void* stream) {
+  cudaStream_t st = stream ? (cudaStream_t)stream : (ctx ? ctx->stream : nullptr);
+  return rpagrd_body(ctx, xpy, ldp, np, xmy, ldm, nm, t, ldt, nt, nspin, hpp, hpt, hmm, se, sc, cam, st,
+                     cudaMemcpyDeviceToDevice, cudaMemcpyDeviceToDevice);
 }
 
 }  // extern "C"

@@ -189,6 +189,61 @@ class FockBuilder:
         pa, ma = pa.transpose(1, 2), ma.transpose(1, 2)
         return (pa[0], ma[0]) if x.dim() == 2 else (pa, ma)
 
+    def fock_tdgrd(self, x, apb=True, amb=False, scale_exch=1.0, scale_coul=1.0, cam=None):
+        """Spin-adapted response build of OpenQP's int2_tdgrd_data_t
+        (tdhf_lib.F90:228-295), the operator of the SF / MRSF Z-vector solvers.
+
+        x: (2, nbf, nbf) alpha / beta densities (host, natural indexing).
+        Returns (apb, amb), each (2, nbf, nbf):
+          A+B, spin s: 2 sc J[X1 + X2] - 2 se K[(Xs + Xs^T)/2]      (apb=True)
+          A-B: spin 1 -2 se K[(X1 - X1^T)/2], spin 2 zero           (amb=True)
+        cam = (alpha, beta, mu[, alpha_coul, beta_coul]): the two-pass CAM build."""
+        x = np.asarray(x, dtype=np.float64)
+        n = self.nbf
+        if x.shape != (2, n, n):
+            raise ValueError("densities must be (2, %d, %d)" % (n, n))
+        fx = np.ascontiguousarray(x.transpose(0, 2, 1))
+        pa, ma = np.empty_like(fx), np.empty_like(fx)
+        fl = td_flags(apb, amb)
+        c = cam_array(*cam) if cam is not None else None
+        rc = lib().oqpg_fock_tdgrd(self.h, ptr(fx), ptr(pa), ptr(ma), fl, float(scale_exch), float(scale_coul),
+                                   ptr(c) if c is not None else None)
+        if rc != 0:
+            raise FockError(rc, "oqpg_fock_tdgrd")
+        return pa.transpose(0, 2, 1), ma.transpose(0, 2, 1)
+
+    def fock_rpagrd(self, xpy=None, xmy=None, t=None, nspin=1, scale_exch=1.0, scale_coul=1.0, cam=None):
+        """H+ / H- build of OpenQP's int2_rpagrd_data_t (tdhf_lib.F90:1068-1322),
+        used by the TDHF / TDDFT gradient.
+
+        xpy, xmy, t: (nvec, ld, nbf, nbf) host arrays (ld >= nspin) or None.
+        Returns (hpp, hpt, hmm), each (nvec, nspin, nbf, nbf) or None:
+          nspin 1: H+[V] = 4 sc J[V] - 2 se K[V]
+          nspin 2: H+[V]_s = 2 sc J[V1 + V2] - 2 se K[V_s]
+          H-[V]: spin 1 -2 se K[(V1 - V1^T)/2], other spin zero
+        (H+ of the symmetric part of V, the operand every reference caller
+        passes)."""
+        n = self.nbf
+
+        def fort(x):
+            if x is None:
+                return None, 1, 0
+            x = np.asarray(x, dtype=np.float64)
+            if x.ndim != 4 or x.shape[2:] != (n, n) or x.shape[1] < nspin:
+                raise ValueError("operands must be (nvec, ld >= nspin, %d, %d)" % (n, n))
+            return np.ascontiguousarray(x.transpose(0, 1, 3, 2)), x.shape[1], x.shape[0]
+
+        (fp, ldp, np_), (fm, ldm, nm), (ft, ldt, nt) = fort(xpy), fort(xmy), fort(t)
+        outs = [np.empty((k, nspin, n, n)) if k else None for k in (np_, nt, nm)]
+        vp = lambda a: a.ctypes.data if a is not None else None
+        c = cam_array(*cam) if cam is not None else None
+        rc = lib().oqpg_fock_rpagrd(self.h, vp(fp), ldp, np_, vp(fm), ldm, nm, vp(ft), ldt, nt, int(nspin),
+                                    vp(outs[0]), vp(outs[1]), vp(outs[2]), float(scale_exch), float(scale_coul),
+                                    ptr(c) if c is not None else None)
+        if rc != 0:
+            raise FockError(rc, "oqpg_fock_rpagrd")
+        return tuple(o.transpose(0, 1, 3, 2) if o is not None else None for o in outs)
+
     def fock_mrsf(self, x, scale_exch=1.0, scale_coul=1.0, cam=None):
         """MRSF (nmat 7) / UMRSF (nmat 11) sigma-vector build of OpenQP's
         int2_mrsf_data_t / int2_umrsf_data_t, first pass (tdhf_mrsf_lib.F90:218-426).
@@ -434,6 +489,20 @@ def routec_fock_td(d2, nbf, nvec, flags, se=1.0, sc=1.0):
     info = ctypes.c_int(1)
     lib().routec_fock_td(ptr(d2), ptr(apb), ptr(amb), ctypes.byref(n), ctypes.byref(nv), ctypes.byref(fl),
                          ctypes.byref(se_), ctypes.byref(sc_), ctypes.byref(info))
+    return apb, amb, info.value
+
+
+def routec_fock_tdgrd(d2, nbf, flags, se=1.0, sc=1.0, cam=None):
+    """Calls routec_fock_tdgrd with the Fortran-ordered (nbf, nbf, 2) array as a
+    flat buffer.  Returns (apb, amb, info), flat."""
+    d2 = np.ascontiguousarray(d2, dtype=np.float64).reshape(-1)
+    apb, amb = np.zeros_like(d2), np.zeros_like(d2)
+    n, fl = ctypes.c_int(nbf), ctypes.c_int(flags)
+    se_, sc_ = ctypes.c_double(se), ctypes.c_double(sc)
+    c = cam_array(*cam) if cam is not None else None
+    info = ctypes.c_int(1)
+    lib().routec_fock_tdgrd(ptr(d2), ptr(apb), ptr(amb), ctypes.byref(n), ctypes.byref(fl), ctypes.byref(se_),
+                            ctypes.byref(sc_), ptr(c) if c is not None else None, ctypes.byref(info))
     return apb, amb, info.value
 
 

@@ -57,6 +57,12 @@ def lib():
                                   ctypes.c_double, ctypes.c_int]
         L.orc_fock_mrsf.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_int]
+        L.orc_fock_tdgrd.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_int]
+        L.orc_fock_rpagrd.argtypes = [ctypes.c_void_p, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int,
+                                      _d, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _d, _d, ctypes.c_double,
+                                      ctypes.c_double, _d, ctypes.c_int]
+        L.orc_fock_tdgrd_cam.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_int, _d, ctypes.c_int]
         L.orc_fock_jk_cam.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int]
         L.orc_fock_jk_cam_sample.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, _d]
@@ -145,6 +151,44 @@ class Oracle:
         lib().orc_fock_td_sample(self.h, _p(fx), _p(pa), _p(ma), fx.shape[0], int(flags), se, sc,
                                  nthreads or os.cpu_count(), int(stride), int(offset), _p(st))
         return pa.transpose(0, 2, 1), ma.transpose(0, 2, 1), dict(t_setup=st[0], t_twoei=st[1], quartets=int(st[2]))
+
+    def fock_tdgrd(self, x, flags, se=1.0, sc=1.0, nthreads=None):
+        """int2_tdgrd_data_t build: x (2, nbf, nbf) spin densities, natural
+        indexing -> (apb, amb) (2, nbf, nbf) (flags: 1 A+B, 2 A-B)."""
+        x = np.asarray(x, dtype=np.float64)
+        fx = np.ascontiguousarray(x.transpose(0, 2, 1))
+        pa, ma = np.zeros_like(fx), np.zeros_like(fx)
+        lib().orc_fock_tdgrd(self.h, _p(fx), _p(pa), _p(ma), int(flags), se, sc, nthreads or os.cpu_count())
+        return pa.transpose(0, 2, 1), ma.transpose(0, 2, 1)
+
+    def fock_tdgrd_cam(self, x, flags, alpha, beta, mu, alpha_c=1.0, beta_c=0.0, nthreads=None):
+        x = np.asarray(x, dtype=np.float64)
+        fx = np.ascontiguousarray(x.transpose(0, 2, 1))
+        pa, ma = np.zeros_like(fx), np.zeros_like(fx)
+        c = self._cam(alpha, beta, mu, alpha_c, beta_c)
+        lib().orc_fock_tdgrd_cam(self.h, _p(fx), _p(pa), _p(ma), int(flags), _p(c), nthreads or os.cpu_count())
+        return pa.transpose(0, 2, 1), ma.transpose(0, 2, 1)
+
+    def fock_rpagrd(self, xpy, xmy, t, nspin, se=1.0, sc=1.0, cam=None, nthreads=None):
+        """int2_rpagrd_data_t build.  xpy / xmy / t: (nvec, ld, nbf, nbf)
+        natural indexing (or None), ld >= nspin -> (hpp, hpt, hmm), each
+        (nvec, nspin, nbf, nbf) or None.  cam = (alpha, beta, mu, alpha_c,
+        beta_c) runs the two-pass CAM form."""
+        n = self.nbf
+
+        def fort(x):
+            if x is None:
+                return np.zeros((0, 1, n, n)), 1, 0
+            x = np.asarray(x, dtype=np.float64)
+            return np.ascontiguousarray(x.transpose(0, 1, 3, 2)), x.shape[1], x.shape[0]
+
+        (fp, ldp, np_), (fm, ldm, nm), (ft, ldt, nt) = fort(xpy), fort(xmy), fort(t)
+        hp, ht, hm = (np.zeros((k, nspin, n, n)) for k in (np_, nt, nm))
+        c = self._cam(*cam) if cam is not None else None
+        lib().orc_fock_rpagrd(self.h, _p(fp), ldp, np_, _p(fm), ldm, nm, _p(ft), ldt, nt, int(nspin), _p(hp), _p(ht),
+                              _p(hm), se, sc, _p(c) if c is not None else None, nthreads or os.cpu_count())
+        out = [h.transpose(0, 1, 3, 2) if k else None for h, k in ((hp, np_), (ht, nt), (hm, nm))]
+        return tuple(out)
 
     def fock_mrsf(self, x, se=1.0, sc=1.0, nthreads=None):
         """int2_mrsf_data_t (nmat 7) / int2_umrsf_data_t (nmat 11) first pass:

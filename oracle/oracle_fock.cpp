@@ -428,6 +428,45 @@ static void td_update(Store& st, const double* d2, double* apb, double* amb, int
   st.n = 0;
 }
 
+// int2_tdgrd_data_t_update (tdhf_lib.F90:228-295): two spin densities,
+// Coulomb of their sum into both A+B matrices, exchange of each spin into its
+// own, A-B of the first only.
+static void tdgrd_update(Store& st, const double* d2, double* apb, double* amb, int n, int flags, double se,
+                         double sc) {
+  const size_t n2 = (size_t)n * n;
+  const double xval1 = se, xval2 = 2 * sc;
+  auto D = [&](int r, int c, int s) { return d2[s * n2 + (size_t)c * n + r]; };
+  auto A = [&](double* m, int r, int c, int s) -> double& { return m[s * n2 + (size_t)c * n + r]; };
+  for (int e = 0; e < st.n; ++e) {
+    const int i = st.ids[4 * e], j = st.ids[4 * e + 1], k = st.ids[4 * e + 2], l = st.ids[4 * e + 3];
+    const double val = st.val[e];
+    const double val1 = val * xval1, val2 = val * xval2;
+    if (flags & TD_APB) {
+      const double ckl = D(k, l, 0) + D(l, k, 0) + D(k, l, 1) + D(l, k, 1);
+      const double cij = D(i, j, 0) + D(j, i, 0) + D(i, j, 1) + D(j, i, 1);
+      for (int s = 0; s < 2; ++s) {
+        A(apb, i, j, s) += val2 * ckl;
+        A(apb, k, l, s) += val2 * cij;
+        A(apb, i, k, s) -= val1 * (D(j, l, s) + D(l, j, s));
+        A(apb, i, l, s) -= val1 * (D(j, k, s) + D(k, j, s));
+        A(apb, j, k, s) -= val1 * (D(i, l, s) + D(l, i, s));
+        A(apb, j, l, s) -= val1 * (D(i, k, s) + D(k, i, s));
+      }
+    }
+    if (flags & TD_AMB) {
+      A(amb, i, k, 0) += val1 * (D(l, j, 0) - D(j, l, 0));
+      A(amb, i, l, 0) += val1 * (D(k, j, 0) - D(j, k, 0));
+      A(amb, j, k, 0) += val1 * (D(l, i, 0) - D(i, l, 0));
+      A(amb, j, l, 0) += val1 * (D(k, i, 0) - D(i, k, 0));
+      A(amb, k, i, 0) -= val1 * (D(l, j, 0) - D(j, l, 0));
+      A(amb, l, i, 0) -= val1 * (D(k, j, 0) - D(j, k, 0));
+      A(amb, k, j, 0) -= val1 * (D(l, i, 0) - D(i, l, 0));
+      A(amb, l, j, 0) -= val1 * (D(k, i, 0) - D(i, k, 0));
+    }
+  }
+  st.n = 0;
+}
+
 // int2_mrsf_data_t_update (tdhf_mrsf_lib.F90:218-333, the FP64 pass-1 branch)
 // and int2_umrsf_data_t_update (tdhf_mrsf_lib.F90:337-426, pass 1).
 // d3 / f3 are (nvec, nmat, n, n): element (v, c, r, col) at ((col n + r) nmat + c) nvec + v.
@@ -581,6 +620,161 @@ static int fock_td(OrcHandle* H, const double* d2, double* apb, double* amb, int
   return 0;
 }
 
+// TD-gradient build of int2_tdgrd_data_t: d2 (n, n, 2) -> apb, amb (n, n, 2),
+// overwritten; parallel_stop of int2_td_data_t symmetrises both apb matrices.
+static int fock_tdgrd(OrcHandle* H, const double* d2, double* apb, double* amb, int flags, double se, double sc,
+                      int nthreads, const Cam* cam = nullptr) {
+  const Basis& B = H->B;
+  const int n = B.nbf;
+  const size_t n2 = (size_t)n * n, tot = 2 * n2;
+  Prepared P;
+  prepare(H, nthreads, P);
+  std::vector<double> dsh;
+  shell_den_general(B, d2, 2, n2, 1, n, dsh);
+  std::vector<double> acc((size_t)nthreads * 2 * tot, 0.0);
+  const double se1 = cam ? cam->alpha : se, sc1 = cam ? cam->alpha_c : sc;
+  twoei(B, P.PS, P.cutoffs, H->cutoff, P.Q, dsh, nthreads, 1, 0, [&](int tid) {
+    double* a = acc.data() + (size_t)tid * 2 * tot;
+    return [=](Store& st) { tdgrd_update(st, d2, a, a + tot, n, flags, se1, sc1); };
+  });
+  if (cam) {
+    const double inv_mu2 = 1.0 / (cam->mu * cam->mu), cut = H->cutoff;
+    const Cutoffs ca = Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0), inv_mu2);
+    std::vector<double> Qa;
+    schwarz(B, Qa, nthreads, inv_mu2);
+    const double se2 = cam->beta, sc2 = cam->beta_c;
+    twoei(B, P.PS, ca, cut, Qa, dsh, nthreads, 1, 0, [&](int tid) {
+      double* a = acc.data() + (size_t)tid * 2 * tot;
+      return [=](Store& st) { tdgrd_update(st, d2, a, a + tot, n, flags, se2, sc2); };
+    });
+  }
+  for (int t = 1; t < nthreads; ++t)
+    for (size_t e = 0; e < 2 * tot; ++e) acc[e] += acc[(size_t)t * 2 * tot + e];
+  for (int v = 0; v < 2; ++v) {
+    double* a = acc.data() + v * n2;
+    for (int i = 0; i < n; ++i) {
+      for (int r = i; r < n; ++r) a[(size_t)i * n + r] += a[(size_t)r * n + i];
+      for (int r = 0; r < i; ++r) a[(size_t)i * n + r] = a[(size_t)r * n + i];
+    }
+  }
+  std::memcpy(apb, acc.data(), sizeof(double) * tot);
+  std::memcpy(amb, acc.data() + tot, sizeof(double) * tot);
+  return 0;
+}
+
+// int2_rpagrd_data_t_update_hplus (tdhf_lib.F90:1208-1284): H+[V] of one
+// vector v (n, n, ld), spin components 0..nspin-1 of hp (n, n, nspin).
+static void rpagrd_hplus(const Store& st, const double* v, size_t ld_step, double* hp, int n, int nspin, double se,
+                         double sc) {
+  const size_t n2 = (size_t)n * n;
+  auto V = [&](int r, int c, int s) { return v[s * ld_step + (size_t)c * n + r]; };
+  auto H = [&](int r, int c, int s) -> double& { return hp[s * n2 + (size_t)c * n + r]; };
+  if (nspin == 1) {
+    const double xfact = 2 * se, cfact = 8 * sc;
+    for (int e = 0; e < st.n; ++e) {
+      const int i = st.ids[4 * e], j = st.ids[4 * e + 1], k = st.ids[4 * e + 2], l = st.ids[4 * e + 3];
+      const double xval = st.val[e] * xfact, cval = st.val[e] * cfact;
+      H(i, j, 0) += cval * V(l, k, 0);
+      H(k, l, 0) += cval * V(j, i, 0);
+      H(i, k, 0) -= xval * V(l, j, 0);
+      H(i, l, 0) -= xval * V(k, j, 0);
+      H(j, k, 0) -= xval * V(l, i, 0);
+      H(j, l, 0) -= xval * V(k, i, 0);
+    }
+  } else {
+    const double xfact = se, cfact = 2 * sc;
+    for (int e = 0; e < st.n; ++e) {
+      const int i = st.ids[4 * e], j = st.ids[4 * e + 1], k = st.ids[4 * e + 2], l = st.ids[4 * e + 3];
+      const double xval = st.val[e] * xfact, cval = st.val[e] * cfact;
+      const double ckl = V(k, l, 0) + V(l, k, 0) + V(k, l, 1) + V(l, k, 1);
+      const double cij = V(i, j, 0) + V(j, i, 0) + V(i, j, 1) + V(j, i, 1);
+      for (int s = 0; s < 2; ++s) {
+        H(i, j, s) += cval * ckl;
+        H(k, l, s) += cval * cij;
+        H(i, k, s) -= xval * (V(j, l, s) + V(l, j, s));
+        H(i, l, s) -= xval * (V(j, k, s) + V(k, j, s));
+        H(j, k, s) -= xval * (V(i, l, s) + V(l, i, s));
+        H(j, l, s) -= xval * (V(i, k, s) + V(k, i, s));
+      }
+    }
+  }
+}
+
+// int2_rpagrd_data_t_update_hminus (tdhf_lib.F90:1286-1322): spin component 0 only.
+static void rpagrd_hminus(const Store& st, const double* v, double* hm, int n, double se) {
+  auto V = [&](int r, int c) { return v[(size_t)c * n + r]; };
+  auto H = [&](int r, int c) -> double& { return hm[(size_t)c * n + r]; };
+  for (int e = 0; e < st.n; ++e) {
+    const int i = st.ids[4 * e], j = st.ids[4 * e + 1], k = st.ids[4 * e + 2], l = st.ids[4 * e + 3];
+    const double xval = st.val[e] * se;
+    H(i, k) += xval * (V(l, j) - V(j, l));
+    H(i, l) += xval * (V(k, j) - V(j, k));
+    H(j, k) += xval * (V(l, i) - V(i, l));
+    H(j, l) += xval * (V(k, i) - V(i, k));
+    H(k, i) -= xval * (V(l, j) - V(j, l));
+    H(l, i) -= xval * (V(k, j) - V(j, k));
+    H(k, j) -= xval * (V(l, i) - V(i, l));
+    H(l, j) -= xval * (V(k, i) - V(i, k));
+  }
+}
+
+// int2_rpagrd_data_t (tdhf_lib.F90:1068-1322): xpy (n, n, ldp, np), xmy
+// (n, n, ldm, nm), t (n, n, ldt, nt) -> hpp (n, n, nspin, np), hpt
+// (n, n, nspin, nt), hmm (n, n, nspin, nm), overwritten.  The shell density
+// is the maximum over every component of xpy and xmy (both only when np > 0)
+// and of t (init_screen, :1161-1173); parallel_stop symmetrises hpp and hpt.
+static int fock_rpagrd(OrcHandle* H, const double* xpy, int ldp, int np, const double* xmy, int ldm, int nm,
+                       const double* t, int ldt, int nt, int nspin, double* hpp, double* hpt, double* hmm, double se,
+                       double sc, int nthreads, const Cam* cam = nullptr) {
+  const Basis& B = H->B;
+  const int n = B.nbf;
+  const size_t n2 = (size_t)n * n, blk = n2 * nspin;
+  const size_t tp = blk * np, tt = blk * nt, tm = blk * nm, tot = tp + tt + tm;
+  Prepared P;
+  prepare(H, nthreads, P);
+  std::vector<double> dsh((size_t)B.nshell * B.nshell, 0.0), part;
+  auto screen = [&](const double* x, int nmat) {
+    shell_den_general(B, x, nmat, n2, 1, n, part);
+    for (size_t e = 0; e < dsh.size(); ++e) dsh[e] = std::max(dsh[e], part[e]);
+  };
+  if (np > 0) screen(xpy, ldp * np);
+  if (np > 0 && nm > 0) screen(xmy, ldm * nm);
+  if (nt > 0) screen(t, ldt * nt);
+  std::vector<double> acc((size_t)nthreads * tot, 0.0);
+  auto pass = [&](const Cutoffs& cuts, const std::vector<double>& Q, double sx, double scl) {
+    twoei(B, P.PS, cuts, H->cutoff, Q, dsh, nthreads, 1, 0, [&](int tid) {
+      double* a = acc.data() + (size_t)tid * tot;
+      return [=](Store& st) {
+        for (int v = 0; v < np; ++v) rpagrd_hplus(st, xpy + v * ldp * n2, n2, a + v * blk, n, nspin, sx, scl);
+        for (int v = 0; v < nt; ++v) rpagrd_hplus(st, t + v * ldt * n2, n2, a + tp + v * blk, n, nspin, sx, scl);
+        for (int v = 0; v < nm; ++v) rpagrd_hminus(st, xmy + v * ldm * n2, a + tp + tt + v * blk, n, sx);
+        st.n = 0;
+      };
+    });
+  };
+  pass(P.cutoffs, P.Q, cam ? cam->alpha : se, cam ? cam->alpha_c : sc);
+  if (cam) {
+    const double inv_mu2 = 1.0 / (cam->mu * cam->mu), cut = H->cutoff;
+    const Cutoffs ca = Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0), inv_mu2);
+    std::vector<double> Qa;
+    schwarz(B, Qa, nthreads, inv_mu2);
+    pass(ca, Qa, cam->beta, cam->beta_c);
+  }
+  for (int th = 1; th < nthreads; ++th)
+    for (size_t e = 0; e < tot; ++e) acc[e] += acc[(size_t)th * tot + e];
+  for (size_t v = 0; v < (size_t)(np + nt) * nspin; ++v) {
+    double* a = acc.data() + v * n2;
+    for (int i = 0; i < n; ++i) {
+      for (int r = i; r < n; ++r) a[(size_t)i * n + r] += a[(size_t)r * n + i];
+      for (int r = 0; r < i; ++r) a[(size_t)i * n + r] = a[(size_t)r * n + i];
+    }
+  }
+  if (np) std::memcpy(hpp, acc.data(), sizeof(double) * tp);
+  if (nt) std::memcpy(hpt, acc.data() + tp, sizeof(double) * tt);
+  if (nm) std::memcpy(hmm, acc.data() + tp + tt, sizeof(double) * tm);
+  return 0;
+}
+
 // MRSF (nmat = 7) / UMRSF (nmat = 11) response build: d3 -> f3 (overwritten),
 // int2_mrsf_data_t_parallel_start/stop (tdhf_mrsf_lib.F90:58-149); the
 // screening density is the last component (tdhf_mrsf_lib.F90:171-185).
@@ -701,6 +895,28 @@ int orc_fock_td_sample(void* h, const double* d2, double* apb, double* amb, int 
 
 int orc_fock_mrsf(void* h, const double* d3, double* f3, int nvec, int nmat, double se, double sc, int nthreads) {
   return fock_mrsf((OrcHandle*)h, d3, f3, nvec, nmat, se, sc, nthreads);
+}
+
+int orc_fock_tdgrd(void* h, const double* d2, double* apb, double* amb, int flags, double se, double sc,
+                   int nthreads) {
+  return fock_tdgrd((OrcHandle*)h, d2, apb, amb, flags, se, sc, nthreads);
+}
+
+int orc_fock_rpagrd(void* h, const double* xpy, int ldp, int np, const double* xmy, int ldm, int nm, const double* t,
+                    int ldt, int nt, int nspin, double* hpp, double* hpt, double* hmm, double se, double sc,
+                    const double* cam5, int nthreads) {
+  if (cam5) {
+    const Cam cam{cam5[0], cam5[1], cam5[2], cam5[3], cam5[4]};
+    return fock_rpagrd((OrcHandle*)h, xpy, ldp, np, xmy, ldm, nm, t, ldt, nt, nspin, hpp, hpt, hmm, se, sc,
+                       nthreads, &cam);
+  }
+  return fock_rpagrd((OrcHandle*)h, xpy, ldp, np, xmy, ldm, nm, t, ldt, nt, nspin, hpp, hpt, hmm, se, sc, nthreads);
+}
+
+int orc_fock_tdgrd_cam(void* h, const double* d2, double* apb, double* amb, int flags, const double* cam5,
+                       int nthreads) {
+  const Cam cam{cam5[0], cam5[1], cam5[2], cam5[3], cam5[4]};
+  return fock_tdgrd((OrcHandle*)h, d2, apb, amb, flags, 1.0, 1.0, nthreads, &cam);
 }
 
 // CAM (two-pass) forms: cam5 = {alpha, beta, mu, alpha_coulomb, beta_coulomb}.

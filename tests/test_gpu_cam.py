@@ -1,7 +1,8 @@
 """GPU parity of the CAM (range-separated) builds against the oracle's
 restatement of OpenQP's int2_run_cam: pass 1 over 1/r with (alpha,
 alpha_coulomb), pass 2 over erf(mu r)/r -- its own Schwarz bounds -- with
-(beta, beta_coulomb), for the SCF Fock build, the TD build and the MRSF build.
+(beta, beta_coulomb), for the SCF Fock build, the TD, TD-gradient and
+RPA-gradient builds and the MRSF build.
 
 Tolerance: 1e-10 max-abs (the plain-FP64 gate).
 """
@@ -69,6 +70,26 @@ def test_cam_td(gpu, oracle_lib):
                             tda_coulomb=bool(flags & 8), cam=CAM)
         rp, rm = o.fock_td_cam(x, flags, *CAM)
         assert np.abs(pa - rp).max() < TOL and np.abs(ma - rm).max() < TOL
+
+
+def test_cam_gradient_side_builds(gpu, oracle_lib):
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(4, 6.0, seed=2, basis="6-31g(d)")
+    n = bas.nbf
+    rng = np.random.default_rng(11)
+    fb = gpu.FockBuilder(bas)
+    o = oracle_lib.Oracle(bas)
+    x = rng.standard_normal((2, n, n)) * 0.2
+    pa, ma = fb.fock_tdgrd(x, apb=True, amb=True, cam=CAM)
+    rp, rm = o.fock_tdgrd_cam(x, 3, *CAM)
+    assert np.abs(pa - rp).max() < TOL and np.abs(ma - rm).max() < TOL
+    sym = lambda a: 0.5 * (a + a.swapaxes(-1, -2))
+    xpy = sym(rng.standard_normal((1, 2, n, n)) * 0.2)
+    xmy = rng.standard_normal((1, 1, n, n)) * 0.2
+    got = fb.fock_rpagrd(xpy, xmy, xpy[:, 1:2], 1, cam=CAM)
+    ref = o.fock_rpagrd(xpy, xmy, xpy[:, 1:2], 1, cam=CAM)
+    for g, r in zip(got, ref):
+        assert np.abs(g - r).max() < TOL
 
 
 @pytest.mark.parametrize("nmat", [7, 11])

@@ -1,6 +1,6 @@
 """GPU parity of the response-type builds (general square densities) against
-the oracle's restatement of OpenQP's int2_td_data_t / int2_mrsf_data_t /
-int2_umrsf_data_t digestions.
+the oracle's restatement of OpenQP's int2_td_data_t / int2_tdgrd_data_t /
+int2_rpagrd_data_t / int2_mrsf_data_t / int2_umrsf_data_t digestions.
 
 Tolerance: 1e-10 max-abs (the plain-FP64 gate) on every output matrix;
 the double-float mode is held to 1e-9.
@@ -168,3 +168,76 @@ def test_td_water16_properties(gpu):
         assert np.abs(m[:4] + m[4:8] - m[8:]).max() < 1e-8 * max(1.0, np.abs(m).max())
     assert np.abs(both[0] - both[0].transpose(0, 2, 1)).max() < 1e-12
     assert np.abs(both[1] + both[1].transpose(0, 2, 1)).max() < 1e-12
+
+
+@pytest.mark.parametrize("flags", [1, 2, 3])
+def test_tdgrd_water4(gpu, oracle_lib, flags):
+    """int2_tdgrd_data_t: two spin densities, (H2O)4 / cc-pVDZ; host form,
+    device form and the Fortran-style seam."""
+    import torch
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(4, 6.0, seed=7, basis="cc-pvdz")
+    n = bas.nbf
+    x = np.random.default_rng(20 + flags).standard_normal((2, n, n)) * 0.2
+    fb = gpu.FockBuilder(bas)
+    pa, ma = fb.fock_tdgrd(x, apb=bool(flags & 1), amb=bool(flags & 2), scale_exch=0.8, scale_coul=1.1)
+    rp, rm = oracle_lib.Oracle(bas).fock_tdgrd(x, flags, se=0.8, sc=1.1)
+    assert np.abs(pa - rp).max() < TOL and np.abs(ma - rm).max() < TOL
+    assert not ma[1].any()
+    from openqp_gb300._lib import lib
+    fx = torch.from_numpy(np.ascontiguousarray(x.transpose(0, 2, 1))).cuda()
+    tp, tm = torch.empty_like(fx), torch.empty_like(fx)
+    rc = lib().oqpg_fock_tdgrd_device(fb.h, fx.data_ptr(), tp.data_ptr(), tm.data_ptr(), flags, 0.8, 1.1, None,
+                                      torch.cuda.current_stream().cuda_stream)
+    assert rc == 0
+    assert np.abs(tp.cpu().numpy().transpose(0, 2, 1) - pa).max() < 1e-13
+    assert np.abs(tm.cpu().numpy().transpose(0, 2, 1) - ma).max() < 1e-13
+    assert gpu.routec_init(bas) == 0
+    try:
+        ap, am, info = gpu.routec_fock_tdgrd(np.ascontiguousarray(x.transpose(0, 2, 1)), n, flags, 0.8, 1.1)
+        assert info == 0
+        assert np.abs(ap.reshape(2, n, n).transpose(0, 2, 1) - pa).max() < 1e-13
+        assert np.abs(am.reshape(2, n, n).transpose(0, 2, 1) - ma).max() < 1e-13
+    finally:
+        gpu.routec_finalize()
+
+
+@pytest.mark.parametrize("nspin", [1, 2])
+def test_rpagrd_water4(gpu, oracle_lib, nspin):
+    """int2_rpagrd_data_t: H+[X+Y], H+[T], H-[X-Y] with symmetric H+
+    operands (as every reference caller passes) and a general X-Y; the
+    xpy2-style layout (an extra operand slot read only by the screening)."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(4, 6.0, seed=8, basis="6-31g(d)")
+    n = bas.nbf
+    rng = np.random.default_rng(nspin)
+    sym = lambda a: 0.5 * (a + a.swapaxes(-1, -2))
+    xpy = sym(rng.standard_normal((2, nspin + 1, n, n)) * 0.2)
+    t = sym(rng.standard_normal((1, nspin, n, n)) * 0.2)
+    xmy = rng.standard_normal((2, nspin, n, n)) * 0.2
+    fb = gpu.FockBuilder(bas)
+    o = oracle_lib.Oracle(bas)
+    got = fb.fock_rpagrd(xpy, xmy, t, nspin, scale_exch=0.6, scale_coul=1.2)
+    ref = o.fock_rpagrd(xpy, xmy, t, nspin, se=0.6, sc=1.2)
+    for g, r in zip(got, ref):
+        assert np.abs(g - r).max() < TOL
+    # the tdhf_z_vector.F90:341 call: t only
+    _, ht, _ = fb.fock_rpagrd(t=t, nspin=nspin)
+    assert np.abs(ht - o.fock_rpagrd(None, None, t, nspin)[1]).max() < TOL
+    # X-Y alone is not screened in (init_screen): zero, as the reference
+    _, _, hm = fb.fock_rpagrd(xmy=xmy, nspin=nspin)
+    assert not hm.any()
+
+
+def test_gradient_side_builds_reject_bad_input(gpu):
+    from openqp_gb300 import workloads
+    from openqp_gb300._lib import lib, ptr
+    bas = workloads.water_cluster_basis(1, workloads.cube_edge_like_c1(1), seed=0, basis="6-31g(d)")
+    fb = gpu.FockBuilder(bas)
+    x = np.zeros((2, bas.nbf, bas.nbf))
+    o1, o2 = np.zeros_like(x), np.zeros_like(x)
+    assert lib().oqpg_fock_tdgrd(fb.h, ptr(x), ptr(o1), ptr(o2), 4, 1.0, 1.0, None) == 3   # TDA not defined
+    v = x.ctypes.data
+    assert lib().oqpg_fock_rpagrd(fb.h, v, 1, 1, None, 1, 0, None, 1, 0, 3, v, None, None, 1.0, 1.0, None) == 3
+    assert lib().oqpg_fock_rpagrd(fb.h, v, 1, 1, None, 1, 0, None, 1, 0, 2, v, None, None, 1.0, 1.0, None) == 3
+    assert lib().oqpg_fock_rpagrd(fb.h, None, 1, 1, None, 1, 0, None, 1, 0, 1, v, None, None, 1.0, 1.0, None) == 3

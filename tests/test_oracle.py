@@ -225,6 +225,73 @@ def test_mrsf_digestion_matches_dense_contraction(oracle_lib, nmat):
             assert np.abs(f[v, m] - ref).max() < 1e-12
 
 
+@pytest.mark.parametrize("flags", [1, 2, 3])
+def test_tdgrd_digestion_matches_dense_contraction(oracle_lib, flags):
+    """int2_tdgrd_data_t update + the int2_td_data_t parallel_stop on two
+    general spin densities equals A+B_s = 2 sc J[X1 + X2] - 2 se K[Xs_s],
+    A-B_1 = -2 se K[X1a], A-B_2 = 0."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(1, workloads.cube_edge_like_c1(1), seed=3, basis="6-31g(d)")
+    o = oracle_lib.Oracle(bas, cutoff=1e-12)
+    n = o.nbf
+    J, K = _dense_jk(o, n)
+    x = np.random.default_rng(10 + flags).standard_normal((2, n, n)) * 0.3
+    se, sc = 0.7, 1.3
+    pa, ma = o.fock_tdgrd(x, flags, se, sc)
+    for s in range(2):
+        ep = 2 * sc * J(x[0] + x[1]) - 2 * se * K(0.5 * (x[s] + x[s].T)) if flags & 1 else 0 * x[s]
+        assert np.abs(pa[s] - ep).max() < 1e-12
+    em = -2 * se * K(0.5 * (x[0] - x[0].T)) if flags & 2 else 0 * x[0]
+    assert np.abs(ma[0] - em).max() < 1e-12
+    assert not ma[1].any()
+
+
+@pytest.mark.parametrize("nspin", [1, 2])
+def test_rpagrd_digestion_matches_dense_contraction(oracle_lib, nspin):
+    """int2_rpagrd_data_t hplus / hminus + parallel_stop: for symmetric V,
+    H+[V] = 4 sc J[V] - 2 se K[V] (nspin 1) or 2 sc J[V1 + V2] - 2 se K[V_s]
+    (nspin 2); H-[V] = -2 se K[V1a] in spin 1, zero in spin 2.  A third
+    operand slot beyond nspin (the reference's xpy2(:,:,2,:)) is read only by
+    the screening."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(1, workloads.cube_edge_like_c1(1), seed=3, basis="6-31g(d)")
+    o = oracle_lib.Oracle(bas, cutoff=1e-12)
+    n = o.nbf
+    J, K = _dense_jk(o, n)
+    rng = np.random.default_rng(nspin)
+    sym = lambda a: 0.5 * (a + a.swapaxes(-1, -2))
+    xpy = sym(rng.standard_normal((2, nspin + 1, n, n)) * 0.3)
+    t = sym(rng.standard_normal((1, nspin, n, n)) * 0.3)
+    xmy = rng.standard_normal((2, nspin, n, n)) * 0.3
+    se, sc = 0.7, 1.3
+    hp, ht, hm = o.fock_rpagrd(xpy, xmy, t, nspin, se, sc)
+
+    def hplus(v, s):
+        if nspin == 1:
+            return 4 * sc * J(v[0]) - 2 * se * K(v[0])
+        return 2 * sc * J(v[0] + v[1]) - 2 * se * K(v[s])
+
+    for i in range(2):
+        for s in range(nspin):
+            assert np.abs(hp[i, s] - hplus(xpy[i], s)).max() < 1e-11
+        assert np.abs(hm[i, 0] + 2 * se * K(0.5 * (xmy[i, 0] - xmy[i, 0].T))).max() < 1e-12
+        if nspin == 2:
+            assert not hm[i, 1].any()
+    for s in range(nspin):
+        assert np.abs(ht[0, s] - hplus(t[0], s)).max() < 1e-11
+
+
+def test_rpagrd_screens_xmy_only_with_xpy(oracle_lib):
+    """The reference's init_screen adds X-Y to the shell density only when
+    X+Y is present: with X-Y alone every quartet is screened out."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(1, workloads.cube_edge_like_c1(1), seed=3, basis="6-31g(d)")
+    o = oracle_lib.Oracle(bas, cutoff=1e-12)
+    xmy = np.random.default_rng(0).standard_normal((1, 1, o.nbf, o.nbf))
+    _, _, hm = o.fock_rpagrd(None, xmy, None, 1)
+    assert not hm.any()
+
+
 def test_golden_tdhf_excitation_energies(oracle_lib):
     """OpenQP's examples/TDHF/H2O_TDHF_ENERGY: RHF energy and the three RPA
     singlet excitation energies (their Davidson converges them to ~1e-7)."""
