@@ -140,6 +140,30 @@ void routec_fock_rpagrd(const double* xpy, const int* ldp, const int* np, const 
                         double* hpp, double* hpt, double* hmm, const double* se, const double* sc, const double* cam,
                         int* info);
 
+/* MRSF Davidson sigma session: the reference's routec_sig seam
+ * (source/modules/routec_sig.F90:1-140, driven by
+ * modules/tdhf_mrsf_energy.F90:638-690), on the routec_fock_init context.
+ *
+ * routec_sig_init uploads the MO coefficients mo_a / mo_b and the MO Fock
+ * matrices fmo_a / fmo_b (C^T F C, unpacked), all (nbf, nbf) Fortran
+ * column-major, for nocca / noccb occupied alpha / beta orbitals (MRSF:
+ * nocca = noccb + 2) and kind 1 (singlet) or 3 (triplet); returns 0 when the
+ * session is ready (1: no context or another basis, 3: unsupported input).
+ * routec_sig_set_scale sets the HF exchange scale (scale_exchange =
+ * scale_coulomb of the int2_mrsf_data_t build; 1 by default).
+ * routec_sig_iter maps bvec_mo(ntrial, nv_new) to sigma_mo(ntrial, nv_new) =
+ * (A-B) X, ntrial = nocca (nbf - noccb), the native mrsfcbc -> int2 ->
+ * mrsfmntoia + mrsfesum product (info 0 on success; any other value tells
+ * the caller to fall back to its native path).  routec_sig_free ends the
+ * session (routec_fock_init / routec_fock_finalize end it too).  The
+ * integrals use the context's cutoff; the reference's native response
+ * screens at max(SCF cutoff, 1e-8) (tdhf_mrsf_energy.F90:511-514). */
+int routec_sig_init(const int* nbf, const double* mo_a, const double* mo_b, const double* fmo_a, const double* fmo_b,
+                    const int* nocca, const int* noccb, const int* kind);
+void routec_sig_set_scale(const double* s);
+void routec_sig_iter(const double* bvec_mo, const int* nv_new, double* sigma_mo, int* info);
+void routec_sig_free(void);
+
 /* CAM (range-separated) build of routec_fock_jk's packed densities, the
  * path the reference runs natively for CAM functionals
  * (source/scf_addons.F90:1136-1167 skips the seam for them): int2_run_cam

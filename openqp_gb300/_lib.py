@@ -100,6 +100,13 @@ def lib():
         L.routec_fock_tdgrd.restype = None
         L.routec_fock_rpagrd.argtypes = [_d, _i, _i, _d, _i, _i, _d, _i, _i, _i, _i, _d, _d, _d, _d, _d, _d, _i]
         L.routec_fock_rpagrd.restype = None
+        L.routec_sig_init.argtypes = [_i, _d, _d, _d, _d, _i, _i, _i]
+        L.routec_sig_set_scale.argtypes = [_d]
+        L.routec_sig_set_scale.restype = None
+        L.routec_sig_iter.argtypes = [_d, _i, _d, _i]
+        L.routec_sig_iter.restype = None
+        L.routec_sig_free.argtypes = []
+        L.routec_sig_free.restype = None
         _lib = L
     return _lib
 

@@ -434,6 +434,12 @@ namespace {
 std::mutex g_mutex;
 oqpg_ctx* g_ctx = nullptr;
 
+}  // namespace
+
+oqpg_ctx* oqpg::routec_context() { return g_ctx; }
+
+namespace {
+
 int to_status(cudaError_t e) {
   if (e == cudaSuccess) return OK;
   if (e == cudaErrorMemoryAllocation) return NO_MEM;
@@ -1435,6 +1441,7 @@ int oqpg_class_l(int c, int* l4) {
 int routec_fock_init(int nshell, const int* am, const int* ncontr, const int* origin, const double* ex,
                      const double* cc, const int* harmonic, int natom, const double* xyz, double cutoff) {
   std::lock_guard<std::mutex> lk(g_mutex);
+  sig_release();
   if (g_ctx) {
     ctx_free(g_ctx);
     g_ctx = nullptr;
@@ -1468,6 +1475,7 @@ int routec_fock_init_batch(int nmol, const int* nshell, const int* natom, const 
                            const int* origin, const double* ex, const double* cc, const int* harmonic,
                            const double* xyz, double cutoff) {
   std::lock_guard<std::mutex> lk(g_mutex);
+  sig_release();
   if (g_ctx) {
     ctx_free(g_ctx);
     g_ctx = nullptr;
@@ -1601,6 +1609,7 @@ void routec_grad2(const double* d, const double* xyz, double* de, const int* nbf
 
 void routec_fock_finalize(void) {
   std::lock_guard<std::mutex> lk(g_mutex);
+  sig_release();
   ctx_free(g_ctx);
   g_ctx = nullptr;
 }

@@ -173,6 +173,18 @@ bool split_on(const oqpg_ctx* c);
 bool df_on(const oqpg_ctx* c);
 int ctx_build(oqpg_ctx* c, const Job& job, cudaStream_t st);
 int ensure_att(oqpg_ctx* c, double mu);
+
+// Layout of an MRSF-type operand: component m of vector v, element (r, c) at
+// m sm + v sv + r rs + c cs.
+struct MrsfLayout {
+  long long rs, cs, sm, sv;
+};
+void mrsf_job_layout(const oqpg_ctx* c, const double* in, double* out, int nvec, int nmat, double se, double sc,
+                     const MrsfLayout& L, bool neg_lead, GenJob& g);
+// The process-global context of the routec_* seam (null before routec_fock_init)
+// and the end of the MRSF sigma session bound to it.
+oqpg_ctx* routec_context();
+void sig_release();
 cudaError_t launch_grad_a(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
 cudaError_t launch_grad_b(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
 cudaError_t launch_grad_f(int c, const GradArgs& g, int nsm, cudaStream_t st);  // classes with f, FP64

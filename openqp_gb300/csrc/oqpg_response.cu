@@ -234,20 +234,24 @@ void td_job(const oqpg_ctx* c, const double* d2, double* apb, double* amb, int n
   }
 }
 
+}  // namespace
+
 // int2_mrsf_data_t (nmat 7) / int2_umrsf_data_t (nmat 11) recipe, pass 1.
-// d3 / f3 (nvec, nmat, n, n) Fortran column-major; with X = d3(v, m, :, :):
+// Component m of vector v: element (r, c) at base + r rs + c cs with
+// base = m sm + v sv (MrsfLayout); with X that matrix:
 //   MRSF:  m < 4: sc J[X] - se K[X];  m = 4..6: -se K[X]
 //   UMRSF: m < 8: sc J[X] - se K[X];  m = 8, 9: -se K[X^T];  m = 10: -se K[X]
-// Screening density: component nmat - 1 of every vector.
-void mrsf_job(const oqpg_ctx* c, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
-              GenJob& g) {
-  const long long n = c->nbf;
+// neg_lead negates the outputs of components 0..5 (the MRSF triplet sign of
+// tdhf_mrsf_energy.F90:762-766).  Screening density: component nmat - 1 of
+// every vector.
+void mrsf_job_layout(const oqpg_ctx* c, const double* in, double* out, int nvec, int nmat, double se, double sc,
+                     const MrsfLayout& L, bool neg_lead, GenJob& g) {
   const bool um = nmat == 11;
   const int ncoul = um ? 8 : 4;
-  g.in = d3;
-  g.in_rs = (long long)nmat * nvec; g.in_cs = n * nmat * nvec;
-  g.out_rs = g.in_rs; g.out_cs = g.in_cs;
-  auto base = [&](int m, int v) { return (long long)m * nvec + v; };
+  g.in = in;
+  g.in_rs = L.rs; g.in_cs = L.cs;
+  g.out_rs = L.rs; g.out_cs = L.cs;
+  auto base = [&](int m, int v) { return (long long)m * L.sm + (long long)v * L.sv; };
   for (int m = 0; m < nmat; ++m)
     for (int v = 0; v < nvec; ++v) g.slices.push_back(GenSlice{base(m, v), +1, 0});
   for (int m = 0; m < nmat; ++m)
@@ -259,14 +263,28 @@ void mrsf_job(const oqpg_ctx* c, const double* d3, double* f3, int nvec, int nma
   for (int m = 0; m < nmat; ++m)
     for (int v = 0; v < nvec; ++v) {
       const int s = m * nvec + v, a = nmat * nvec + s;
-      GenOut o{f3 + base(m, v), (int)g.terms.size(), 0};
-      if (m < ncoul) g.terms.push_back(term(sc, 0, s, +1));
+      const double sg = neg_lead && m < 6 ? -1.0 : 1.0;
+      GenOut o{out + base(m, v), (int)g.terms.size(), 0};
+      if (m < ncoul) g.terms.push_back(term(sg * sc, 0, s, +1));
       const bool transposed = um && (m == 8 || m == 9);
-      g.terms.push_back(term(-se, 1, s, +1));
-      g.terms.push_back(term(transposed ? se : -se, 1, a, -1));
+      g.terms.push_back(term(-sg * se, 1, s, +1));
+      g.terms.push_back(term(sg * (transposed ? se : -se), 1, a, -1));
       o.nterm = (int)g.terms.size() - o.term0;
       g.outs.push_back(o);
     }
+}
+
+namespace {
+
+// d3 / f3 (nvec, nmat, n, n) Fortran column-major, the data types' layout.
+MrsfLayout fortran_mrsf(const oqpg_ctx* c, int nvec, int nmat) {
+  const long long n = c->nbf;
+  return MrsfLayout{(long long)nmat * nvec, n * nmat * nvec, nvec, 1};
+}
+
+void mrsf_job(const oqpg_ctx* c, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
+              GenJob& g) {
+  mrsf_job_layout(c, d3, f3, nvec, nmat, se, sc, fortran_mrsf(c, nvec, nmat), false, g);
 }
 
 // Second (erf-attenuated) CAM pass of int2_mrsf_data_t / int2_umrsf_data_t

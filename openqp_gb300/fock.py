@@ -506,6 +506,40 @@ def routec_fock_tdgrd(d2, nbf, flags, se=1.0, sc=1.0, cam=None):
     return apb, amb, info.value
 
 
+def routec_sig_init(mo_a, mo_b, fmo_a, fmo_b, nocca, noccb, kind):
+    """Begins the MRSF sigma session as routec_sig_begin does
+    (modules/routec_sig.F90): (nbf, nbf) natural-indexed host matrices, kind 1
+    singlet / 3 triplet.  Returns the status (0: ready)."""
+    mats = [np.asfortranarray(np.asarray(m, dtype=np.float64)) for m in (mo_a, mo_b, fmo_a, fmo_b)]
+    n = ctypes.c_int(mats[0].shape[0])
+    na, nb, k = ctypes.c_int(nocca), ctypes.c_int(noccb), ctypes.c_int(kind)
+    flat = [np.ascontiguousarray(m.T).reshape(-1) for m in mats]   # column-major buffers
+    return lib().routec_sig_init(ctypes.byref(n), *[ptr(f) for f in flat], ctypes.byref(na), ctypes.byref(nb),
+                                 ctypes.byref(k))
+
+
+def routec_sig_set_scale(s):
+    v = ctypes.c_double(s)
+    lib().routec_sig_set_scale(ctypes.byref(v))
+
+
+def routec_sig_iter(bvec):
+    """bvec (ntrial, nv) -> (sigma (ntrial, nv), info): the Fortran
+    bvec_mo(:, ist:iend) slice as a column-major buffer."""
+    b = np.asarray(bvec, dtype=np.float64)
+    if b.ndim == 1:
+        b = b[:, None]
+    fb = np.ascontiguousarray(b.T)           # column v contiguous
+    out = np.zeros_like(fb)
+    nv, info = ctypes.c_int(b.shape[1]), ctypes.c_int(1)
+    lib().routec_sig_iter(ptr(fb), ctypes.byref(nv), ptr(out), ctypes.byref(info))
+    return out.T, info.value
+
+
+def routec_sig_free():
+    lib().routec_sig_free()
+
+
 def routec_fock_mrsf(d3, nbf, nvec, nmat, se=1.0, sc=1.0):
     """Calls routec_fock_mrsf with the Fortran-ordered (nvec, nmat, nbf, nbf)
     array as a flat buffer.  Returns (f3, info), flat."""

@@ -45,6 +45,11 @@ def test_seam_without_init_declines(libgpu):
     from openqp_gb300 import fock
     f, info = fock.routec_fock_jk(np.zeros(3), 2, 1)
     assert info == 1
+    eye = np.eye(4)
+    assert fock.routec_sig_init(eye, eye, eye, eye, 3, 1, 1) == 1
+    _, info = fock.routec_sig_iter(np.zeros((9, 1)))
+    assert info == 1
+    fock.routec_sig_free()
 
 
 def test_class_table(libgpu):

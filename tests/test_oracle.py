@@ -292,6 +292,24 @@ def test_rpagrd_screens_xmy_only_with_xpy(oracle_lib):
     assert not hm.any()
 
 
+@pytest.mark.parametrize("which", [0, 1], ids=["singlet", "triplet"])
+def test_golden_mrsf_excitation_energies(oracle_lib, which):
+    """OpenQP's h2o_rohf_mrsf-{s,t}_6-31g_hf: ROHF triplet energy and the six
+    MRSF-TDHF excitation energies from the oracle's restatement of the native
+    sigma triple (mrsfcbc -> int2_mrsf_data_t -> mrsfmntoia + mrsfesum) over
+    the full active trial space (their Davidson converges them to ~1e-9)."""
+    import mrsf
+    from oracle import mrsf_sigma as ms
+    from openqp_gb300.basis import build_basis
+    case = json.load(open(os.path.join(ROOT, "tests", "golden", "mrsf_golden.json")))["cases"][which]
+    o = oracle_lib.Oracle(build_basis(case["atoms"], np.array(case["coord_bohr"]).reshape(-1, 3), case["basis"]))
+    bas, r, C, fa, fb, na, nb = mrsf.rohf_reference(case, o.fock_jk)
+    assert abs(r["energy"] - case["energy"]) < 1e-8
+    mrst = case["mrsf_multiplicity"]
+    w = mrsf.mrsf_energies(lambda E: ms.sigma(o.fock_mrsf, E, C, C, fa, fb, na, nb, mrst), bas.nbf, na, nb, mrst, 6)
+    assert np.abs(w - np.array(case["td_energies"])).max() < 1e-7
+
+
 def test_golden_tdhf_excitation_energies(oracle_lib):
     """OpenQP's examples/TDHF/H2O_TDHF_ENERGY: RHF energy and the three RPA
     singlet excitation energies (their Davidson converges them to ~1e-7)."""
