@@ -69,6 +69,11 @@ WORKLOADS = {
                              edge=9.52, seed=0, basis="6-31g(d)", cutoff=1e-10, td=True, nvec=8),
     "td_water32_ccpvdz": dict(name="(H2O)32 cc-pVDZ spherical TDHF A+B and A-B build, 8 trial vectors", nwater=32,
                               edge=14.0, seed=0, basis="cc-pvdz", cutoff=1e-10, td=True, nvec=8),
+    # the MRSF Davidson sigma session (routec_sig_iter): 8 new trial vectors of a triplet-reference
+    # (nocca = noccb + 2) singlet MRSF, MO transforms + one nmat-7 integral pass
+    "mrsf_water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian MRSF singlet sigma session, 8 trial vectors "
+                                    "(nocca 81, noccb 79)", nwater=16, edge=9.52, seed=0, basis="6-31g(d)",
+                               cutoff=1e-10, sigma=True, nvec=8, mrst=1),
     # CAM (range-separated) RHF build of the headline cluster: CAM-B3LYP's alpha, beta, mu
     "cam_water32_ccpvdz": dict(name="(H2O)32 cc-pVDZ spherical RHF CAM J+K build (alpha 0.19, beta 0.46, mu 0.33)",
                                nwater=32, edge=14.0, seed=0, basis="cc-pvdz", cutoff=1e-10,
@@ -332,6 +337,160 @@ def run_td(args):
         print(json.dumps(line), flush=True)
 
 
+def sigma_workload(overlap="library"):
+    """Basis, occupations and the seeded session inputs of the sigma workload."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(WORKLOAD["nwater"], WORKLOAD["edge"], WORKLOAD["seed"], WORKLOAD["basis"])
+    if overlap == "library":
+        from openqp_gb300.onee import one_electron
+        S = one_electron(bas)[0]
+    else:
+        from oracle import oracle
+        oracle.build()
+        S = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"]).one_electron("S")
+    nel = workloads.nelectrons(bas)
+    na, nb = nel // 2 + 1, nel // 2 - 1
+    C, fa, fb, b = workloads.mrsf_session_inputs(bas, na, nb, WORKLOAD["nvec"], WORKLOAD["seed"], S=S)
+    return bas, na, nb, C, fa, fb, b
+
+
+def cpu_baseline_sigma(bas, na, nb, C, fa, fb, b, budget_s):
+    """The oracle's restatement of the native sigma triple: the NumPy MO
+    transforms (mrsfcbc, mrsfmntoia, mrsfesum) timed whole, the nmat-7
+    int2_mrsf_data_t build (all host cores) over 1/stride of the cost-sorted
+    bra pairs, scaled, plus its set-up."""
+    from oracle import oracle
+    from oracle import mrsf_sigma as ms
+    oracle.build()
+    o = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"])
+    cores = os.cpu_count()
+    mrst = WORKLOAD["mrst"]
+    n = bas.nbf
+    t0 = time.perf_counter()
+    xs = [ms.iatogen(b[:, v], n, na, nb) for v in range(b.shape[1])]
+    d3 = np.stack([ms.mrsfcbc(C, C, x, na, nb, mrst) for x in xs])
+    t_cbc = time.perf_counter() - t0
+
+    def run(stride, offset):
+        f3, st = o.fock_mrsf_sample(d3, stride, offset, nthreads=cores)
+        return st["t_twoei"], (st, f3)
+
+    t_loop, stride, (st, f3) = sampled(run, budget_s)
+    t0 = time.perf_counter()
+    for v in range(b.shape[1]):
+        ms.mrsfmntoia(f3[v], C, C, na, nb, mrst) + ms.mrsfesum(xs[v], fa, fb, na, nb, mrst)
+    t_back = time.perf_counter() - t0
+    t = t_loop + st["t_setup"] + t_cbc + t_back
+    return {"value": 1.0 / t, "unit": "sigma calls/s", "cores": cores, "kind": "port",
+            "sample": "oracle restatement of the native MRSF sigma triple for %d vectors: NumPy mrsfcbc / "
+                      "mrsfmntoia / mrsfesum timed whole (%.2f s), the int2_mrsf_data_t quartet loop over 1/%d of the "
+                      "cost-sorted bra shell pairs (the middle pair of every stride), x%d, plus its set-up (%.2f s); "
+                      "%d quartets in the sample"
+                      % (b.shape[1], t_cbc + t_back, stride, stride, st["t_setup"], st["quartets"])}
+
+
+def run_sigma(args):
+    """MRSF sigma calls/s: one routec_sig_iter product (A-B) X of nvec new trial
+    vectors (MO -> AO, one nmat-7 integral pass, AO -> MO), device buffers
+    for value, the host-buffer seam itself for e2e."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    from openqp_gb300 import build as bld
+    bld.build()
+    from openqp_gb300._lib import lib
+    from openqp_gb300.fock import (NCLASS, FockBuilder, class_flops, class_labels, fp64_peak_tflops, routec_finalize,
+                                   routec_init, routec_sig_init, routec_sig_iter, routec_sig_set_scale)
+    bas, na, nb, C, fa, fb, b = sigma_workload()
+    nvec, mrst = b.shape[1], WORKLOAD["mrst"]
+    if routec_init(bas, WORKLOAD["cutoff"]) != 0:
+        raise RuntimeError("routec_fock_init failed")
+    rc = routec_sig_init(C, C, fa, fb, na, nb, mrst)
+    if rc:
+        raise RuntimeError("routec_sig_init returned %d" % rc)
+    routec_sig_set_scale(1.0)
+    bt = torch.from_numpy(np.ascontiguousarray(b.T)).cuda()      # column v contiguous = Fortran (ntrial, nv)
+    out = torch.empty_like(bt)
+    st = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def call():
+        rc = lib().oqpg_sig_iter_device(ctypes.c_void_p(bt.data_ptr()), nvec, ctypes.c_void_p(out.data_ptr()),
+                                        ctypes.c_void_p(st.cuda_stream))
+        if rc:
+            raise RuntimeError("oqpg_sig_iter_device returned %d" % rc)
+
+    for _ in range(args.warmup):
+        call()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        call()
+        e1.record(st)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clocks = sampler.stop()
+    tsum = max_over_ranks(sum(times) / 1000.0)
+    value = ws * args.steps / tsum
+    e2e_t = []
+    if not args.no_e2e:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            sg, info = routec_sig_iter(b)
+            e2e_t.append(time.perf_counter() - t0)
+            if info:
+                raise RuntimeError("routec_sig_iter returned %d" % info)
+        assert np.abs(sg - out.cpu().numpy().T).max() < 1e-12 * max(1.0, np.abs(sg).max())
+    e2e = ws * args.steps / max_over_ranks(sum(e2e_t)) if e2e_t else float("nan")
+    # the integral pass alone (same seven densities per vector) for the class times and the roofline
+    fbld = FockBuilder(bas, cutoff=WORKLOAD["cutoff"])
+    from oracle import mrsf_sigma as ms
+    d3 = np.stack([ms.mrsfcbc(C, C, ms.iatogen(b[:, v], bas.nbf, na, nb), na, nb, mrst) for v in range(nvec)])
+    fbld.fock_mrsf(d3)
+    fbld.fock_mrsf(d3)
+    s0 = fbld.stats()
+    labels = class_labels()
+    ms_c = np.array(s0["ms_per_class"])
+    cdom = int(np.argmax(ms_c))
+    pure = bool(bas.harmonic.any())
+    nk, nj = 2 * 7 * nvec, 4 * nvec
+    fl = [class_flops(c, s0["prim_per_class"][c], s0["per_class"][c], nk=nk, nj=nj, pure=pure) for c in range(NCLASS)]
+    achieved = fl[cdom] / (ms_c[cdom] * 1e-3) / 1e12
+    peak = fp64_peak_tflops()
+    routec_finalize()
+    nbytes = int(8 * b.size)
+    line = {"metric": "MRSF sigma calls/s (%d trial vectors per call)" % nvec, "value": value,
+            "unit": "sigma calls/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * tsum / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded water cluster, Loewdin MO set, orbital-energy ladder MO Fock, seeded unit "
+                    "trial vectors)",
+            "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "nvec": nvec, "nocca": na, "noccb": nb,
+                       "kind": "singlet" if mrst == 1 else "triplet", "cutoff": WORKLOAD["cutoff"],
+                       "l2": "flushed (256 MB write) before every timed step"},
+            "e2e": {"value": e2e, "unit": "sigma calls/s", "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes},
+            "roofline": {"bound": "fp64", "kernel": labels[cdom] + " (the call's integral pass)",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": "measured: FP64 FMA-chain probe on this device",
+                         "kernel_ms": float(ms_c[cdom]), "integral_pass_ms": float(s0["total_ms"])
+                         if "total_ms" in s0 else None},
+            # per call: the integral pass's launches (as counted by the same job on a FockBuilder) plus the
+            # session's four elementwise kernels; the cuBLAS DGEMMs are library kernels and not counted
+            "gpu_launches": int(args.steps * (s0["launches"] + 4)), "clocks": clocks,
+            "class_ms": {labels[c]: round(float(ms_c[c]), 3) for c in range(NCLASS) if ms_c[c] > 0}}
+    if not args.no_cpu and rank == 0:
+        line["cpu_baseline"] = cpu_baseline_sigma(bas, na, nb, C, fa, fb, b, args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def cpu_baseline_cam(bas, d, budget_s):
     """The oracle's two-pass CAM build (all host cores) over 1/stride of the
     cost-sorted bra pairs, scaled, plus the work outside the quartet loops."""
@@ -468,6 +627,23 @@ def run_reference(args):
                 "data": "synthetic (seeded)",
                 "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "cutoff": WORKLOAD["cutoff"]},
                 "cpu_baseline": cb, "e2e": {"value": v, "unit": "builds/s", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    if WORKLOAD.get("sigma"):
+        bas, na, nb, C, fa, fb, b = sigma_workload(overlap="oracle")
+        vals = [cpu_baseline_sigma(bas, na, nb, C, fa, fb, b, args.cpu_budget)["value"]
+                for _ in range(max(1, args.steps))]
+        cb = cpu_baseline_sigma(bas, na, nb, C, fa, fb, b, args.cpu_budget)
+        v = statistics.median(vals)
+        cb["value"] = v
+        line = {"impl": "reference", "metric": "MRSF sigma calls/s (%d trial vectors per call)" % b.shape[1],
+                "value": v, "unit": "sigma calls/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "nvec": b.shape[1], "nocca": na,
+                           "noccb": nb, "cutoff": WORKLOAD["cutoff"]},
+                "cpu_baseline": cb, "e2e": {"value": v, "unit": "sigma calls/s", "h2d_bytes_per_step": 0,
                                             "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -1048,6 +1224,8 @@ def main():
         run_batch(args)
     elif WORKLOAD.get("grad"):
         run_grad(args)
+    elif WORKLOAD.get("sigma"):
+        run_sigma(args)
     elif WORKLOAD.get("td"):
         run_td(args)
     elif WORKLOAD.get("cam"):

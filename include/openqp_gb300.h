@@ -163,6 +163,10 @@ int routec_sig_init(const int* nbf, const double* mo_a, const double* mo_b, cons
 void routec_sig_set_scale(const double* s);
 void routec_sig_iter(const double* bvec_mo, const int* nv_new, double* sigma_mo, int* info);
 void routec_sig_free(void);
+/* routec_sig_iter on device buffers (bvec(ntrial, nv), sigma(ntrial, nv)) and
+ * the given stream (null: the context's); synchronises before it returns.
+ * Returns the status routec_sig_iter puts in info. */
+int oqpg_sig_iter_device(const double* bvec, int nv, double* sigma, void* stream);
 
 /* CAM (range-separated) build of routec_fock_jk's packed densities, the
  * path the reference runs natively for CAM functionals

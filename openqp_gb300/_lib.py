@@ -105,6 +105,7 @@ def lib():
         L.routec_sig_set_scale.restype = None
         L.routec_sig_iter.argtypes = [_d, _i, _d, _i]
         L.routec_sig_iter.restype = None
+        L.oqpg_sig_iter_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.routec_sig_free.argtypes = []
         L.routec_sig_free.restype = None
         _lib = L

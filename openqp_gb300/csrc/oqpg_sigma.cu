@@ -170,9 +170,10 @@ cublasStatus_t gemm(cublasHandle_t h, bool ta, bool tb, int m, int n, int k, dou
                                    A, lda, sa, B, ldb, sb, &beta, C, ldc, sc, nv);
 }
 
-int sig_run(SigSession& S, const double* bvec_host, int nv, double* sigma_host) {
+// bvec / sigma are host buffers, or device buffers with device_io (then st
+// is the caller's stream).
+int sig_run(SigSession& S, const double* bvec_in, int nv, double* sigma_out, bool device_io, cudaStream_t st) {
   oqpg_ctx* c = S.ctx;
-  cudaStream_t st = c->stream;
   const int n = S.n, na = S.na, nb = S.nb, nvir = n - na, nvb = n - nb, lr1 = na - 2, lr2 = na - 1;
   const long long nn = (long long)n * n, ntrial = (long long)na * nvb;
   const size_t D = sizeof(double);
@@ -188,14 +189,16 @@ int sig_run(SigSession& S, const double* bvec_host, int nv, double* sigma_host) 
   CKS(S.sc.ensure(D * nn * nv));
   CKS(S.e.ensure(D * nn * nv));
   CKS(S.tv.ensure(D * 4 * n * nv));
-  double *bv = S.bv.as<double>(), *x = S.x.as<double>(), *d3 = S.d3.as<double>(), *f3 = S.f3.as<double>();
+  const double* bv = device_io ? bvec_in : S.bv.as<double>();
+  double *x = S.x.as<double>(), *d3 = S.d3.as<double>(), *f3 = S.f3.as<double>();
   double *t12 = S.t12.as<double>(), *c12 = S.c12.as<double>(), *y = S.y.as<double>(), *w = S.w.as<double>();
-  double *scr = S.sc.as<double>(), *e = S.e.as<double>(), *tv = S.tv.as<double>(), *sig = S.sig.as<double>();
+  double *scr = S.sc.as<double>(), *e = S.e.as<double>(), *tv = S.tv.as<double>();
+  double* sig = device_io ? sigma_out : S.sig.as<double>();
   const double *va = S.va.as<double>(), *vb = S.vb.as<double>(), *fa = S.fa.as<double>(), *fb = S.fb.as<double>();
   cublasHandle_t h = S.blas;
   CKB(cublasSetStream(h, st));
 
-  CKS(cudaMemcpyAsync(bv, bvec_host, D * ntrial * nv, cudaMemcpyHostToDevice, st));
+  if (!device_io) CKS(cudaMemcpyAsync(S.bv.p, bvec_in, D * ntrial * nv, cudaMemcpyHostToDevice, st));
   k_sig_unpack<<<grid_of(nn * nv, c->nsm), 256, 0, st>>>(bv, nv, n, na, nb, x);
   CKS(cudaGetLastError());
   // mrsfcbc
@@ -259,7 +262,7 @@ int sig_run(SigSession& S, const double* bvec_host, int nv, double* sigma_host) 
            nn, nv));
   k_sig_final<<<nv, 256, 0, st>>>(bv, x, scr, e, fa, fb, n, na, nb, S.mrst, sig);
   CKS(cudaGetLastError());
-  CKS(cudaMemcpyAsync(sigma_host, sig, D * ntrial * nv, cudaMemcpyDeviceToHost, st));
+  if (!device_io) CKS(cudaMemcpyAsync(sigma_out, sig, D * ntrial * nv, cudaMemcpyDeviceToHost, st));
   CKS(cudaStreamSynchronize(st));
   return OK;
 }
@@ -334,8 +337,16 @@ void routec_sig_iter(const double* bvec_mo, const int* nv_new, double* sigma_mo,
   if (!g_sig || g_sig->ctx != routec_context()) rc = NOT_INIT;
   else if (!bvec_mo || !nv_new || !sigma_mo || *nv_new < 0) rc = UNSUPPORTED;
   else if (*nv_new == 0) rc = OK;
-  else rc = sig_run(*g_sig, bvec_mo, *nv_new, sigma_mo);
+  else rc = sig_run(*g_sig, bvec_mo, *nv_new, sigma_mo, false, g_sig->ctx->stream);
   if (info) *info = rc;
+}
+
+int oqpg_sig_iter_device(const double* bvec, int nv, double* sigma, void* stream) {
+  std::lock_guard<std::mutex> lk(g_sig_mutex);
+  if (!g_sig || g_sig->ctx != routec_context()) return NOT_INIT;
+  if (!bvec || !sigma || nv < 0) return UNSUPPORTED;
+  if (nv == 0) return OK;
+  return sig_run(*g_sig, bvec, nv, sigma, true, stream ? (cudaStream_t)stream : g_sig->ctx->stream);
 }
 
 void routec_sig_free(void) { sig_release(); }

@@ -126,6 +126,26 @@ def transition_densities(bas, nocc, nvec, seed, S=None):
     return out
 
 
+def mrsf_session_inputs(bas, nocca, noccb, nvec, seed, S=None):
+    """Inputs of an MRSF sigma session: a full Loewdin-orthonormal MO set C
+    (alpha = beta, as for an ROHF reference), MO Fock matrices with an
+    ascending orbital-energy ladder plus a small symmetric coupling, and nvec
+    seeded unit-norm trial vectors (nocca (nbf - noccb), nvec)."""
+    if S is None:
+        S, _ = overlap_kinetic(bas)
+    rng = np.random.default_rng(seed)
+    n = S.shape[0]
+    C = loewdin_columns(S, n, rng)
+    eps = np.linspace(-1.5, 2.5, n)
+    fmo = []
+    for _ in range(2):
+        w = rng.standard_normal((n, n)) * 0.01
+        fmo.append(np.diag(eps) + 0.5 * (w + w.T))
+    b = rng.standard_normal((nocca * (n - noccb), nvec))
+    b /= np.linalg.norm(b, axis=0)
+    return C, fmo[0], fmo[1], b
+
+
 def density_open(bas, nalpha, nbeta, seed, S=None):
     """Packed (2, ntri) alpha/beta densities."""
     if S is None:

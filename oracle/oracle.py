@@ -62,6 +62,8 @@ def lib():
         L.orc_fock_rpagrd.argtypes = [ctypes.c_void_p, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int,
                                       _d, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _d, _d, ctypes.c_double,
                                       ctypes.c_double, _d, ctypes.c_int]
+        L.orc_fock_mrsf_sample.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d]
         L.orc_fock_tdgrd_cam.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_int, _d, ctypes.c_int]
         L.orc_fock_jk_cam.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int]
         L.orc_fock_jk_cam_sample.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_int, ctypes.c_int, _d, ctypes.c_int,
@@ -200,6 +202,17 @@ class Oracle:
         if rc:
             raise ValueError("nmat must be 7 or 11")
         return out.transpose(3, 2, 1, 0)
+
+    def fock_mrsf_sample(self, x, stride, offset=0, se=1.0, sc=1.0, nthreads=None):
+        """fock_mrsf over the bra pairs p (cost-sorted) with p % stride == offset.
+        Returns (f3, stats) with set-up and loop seconds and the quartet count."""
+        x = np.asarray(x, dtype=np.float64)
+        fx = np.ascontiguousarray(x.transpose(3, 2, 1, 0))
+        out = np.zeros_like(fx)
+        st = np.zeros(3)
+        lib().orc_fock_mrsf_sample(self.h, _p(fx), _p(out), x.shape[0], x.shape[1], se, sc,
+                                   nthreads or os.cpu_count(), int(stride), int(offset), _p(st))
+        return out.transpose(3, 2, 1, 0), dict(t_setup=st[0], t_twoei=st[1], quartets=int(st[2]))
 
     # ---- CAM (int2_run_cam): regular pass + erf-attenuated pass ---------------
     @staticmethod

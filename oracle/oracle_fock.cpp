@@ -779,7 +779,9 @@ static int fock_rpagrd(OrcHandle* H, const double* xpy, int ldp, int np, const d
 // int2_mrsf_data_t_parallel_start/stop (tdhf_mrsf_lib.F90:58-149); the
 // screening density is the last component (tdhf_mrsf_lib.F90:171-185).
 static int fock_mrsf(OrcHandle* H, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
-                     int nthreads, const Cam* cam = nullptr) {
+                     int nthreads, const Cam* cam = nullptr, int stride = 1, int offset = 0,
+                     double* stats = nullptr) {
+  const double t0 = now();
   const Basis& B = H->B;
   const int n = B.nbf;
   const bool umrsf = nmat == 11;
@@ -803,10 +805,12 @@ static int fock_mrsf(OrcHandle* H, const double* d3, double* f3, int nvec, int n
   std::vector<double> acc((size_t)nthreads * tot, 0.0);
   const double* dsp = ds.data();
   const double se1 = cam ? cam->alpha : se, sc1 = cam ? cam->alpha_c : sc;
-  twoei(B, P.PS, P.cutoffs, H->cutoff, P.Q, dsh, nthreads, 1, 0, [&](int tid) {
+  const double t1 = now();
+  const TwoeiCounts cnt = twoei(B, P.PS, P.cutoffs, H->cutoff, P.Q, dsh, nthreads, stride, offset, [&](int tid) {
     double* a = acc.data() + (size_t)tid * tot;
     return [=](Store& st) { mrsf_update(st, d3, dsp, a, n, nvec, nmat, umrsf, se1, sc1); };
   });
+  const double t2 = now();
   if (cam) {
     const double inv_mu2 = 1.0 / (cam->mu * cam->mu), cut = H->cutoff;
     const Cutoffs ca = Cutoffs::make(cut, 1e-2 * cut, 1e-4 * cut, 25.0 * std::log(10.0), inv_mu2);
@@ -821,6 +825,11 @@ static int fock_mrsf(OrcHandle* H, const double* d3, double* f3, int nvec, int n
   for (int t = 1; t < nthreads; ++t)
     for (size_t e = 0; e < tot; ++e) acc[e] += acc[(size_t)t * tot + e];
   std::memcpy(f3, acc.data(), sizeof(double) * tot);
+  if (stats) {
+    stats[0] = (t1 - t0) + (now() - t2);  // everything but the (first) quartet loop
+    stats[1] = t2 - t1;
+    stats[2] = (double)cnt.nq;
+  }
   return 0;
 }
 
@@ -895,6 +904,13 @@ int orc_fock_td_sample(void* h, const double* d2, double* apb, double* amb, int 
 
 int orc_fock_mrsf(void* h, const double* d3, double* f3, int nvec, int nmat, double se, double sc, int nthreads) {
   return fock_mrsf((OrcHandle*)h, d3, f3, nvec, nmat, se, sc, nthreads);
+}
+
+// fock_mrsf over the bra pairs p (cost-sorted) with p % stride == offset;
+// stats3 = {seconds outside the quartet loop, loop seconds, quartets}.
+int orc_fock_mrsf_sample(void* h, const double* d3, double* f3, int nvec, int nmat, double se, double sc,
+                         int nthreads, int stride, int offset, double* stats3) {
+  return fock_mrsf((OrcHandle*)h, d3, f3, nvec, nmat, se, sc, nthreads, nullptr, stride, offset, stats3);
 }
 
 int orc_fock_tdgrd(void* h, const double* d2, double* apb, double* amb, int flags, double se, double sc,
