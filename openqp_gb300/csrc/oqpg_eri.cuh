@@ -146,6 +146,7 @@ __device__ __forceinline__ T rys_quantity(T X, int q, bool roots_f32 = false) {
 
 __host__ __device__ constexpr int naos(int l, bool pure) { return (pure && l >= 2) ? 2 * l + 1 : ncart(l); }
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 
 // Pure-d projection row m, Cartesian component c (m = -2..2: xy, yz, z^2, xz, x^2-y^2)
 __host__ __device__ constexpr double pure_d(int m, int c) {
@@ -734,6 +735,22 @@ __global__ void __launch_bounds__(128) k_prim(const BuildArgs a) {
 
 // ===========================================================================
 // Large classes: one warp per quartet.
+// Order of the six digestion target kinds by decreasing dot-product length
+// (stable: equal lengths keep their index order).
+struct KindOrder {
+  int k[6];
+};
+__host__ __device__ constexpr KindOrder kind_order(const int (&nt)[6]) {
+  KindOrder o{{0, 1, 2, 3, 4, 5}};
+  for (int i = 1; i < 6; ++i)
+    for (int j = i; j > 0 && nt[o.k[j]] > nt[o.k[j - 1]]; --j) {
+      const int t = o.k[j];
+      o.k[j] = o.k[j - 1];
+      o.k[j - 1] = t;
+    }
+  return o;
+}
+
 template <int LA, int LB, int LC, int LD, bool PURE>
 struct TeamSmem {
   using K = Cls<LA, LB, LC, LD>;
@@ -750,6 +767,10 @@ struct TeamSmem {
   // projection (NE) and the digestion (density blocks)
   static constexpr int REST = cmax(PH1, cmax(K::NE, DJ + 2 * DK));
   static constexpr int PER_WARP = K::NE + REST;   // elements of the kernel's type
+  // exchange / Coulomb densities digested per pass: as many as the shared
+  // region holds (at least 2 and 1), at most 8 each
+  static constexpr int PK = cmin(8, (REST - DJ) / DK);
+  static constexpr int PJ = cmax(1, cmin(8, (REST - PK * DK) / DJ));
 };
 
 // Epilogue of a warp-owned contracted quartet whose raw Cartesian block is in
@@ -842,15 +863,14 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
   }
   const T cut = (T)a.elem_cut;
   for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], cut);
-  // density blocks, one Coulomb and up to two exchange densities per pass
-  // (one pass for the SCF builds)
+  // density blocks: up to PJ Coulomb and PK exchange densities per pass (one
+  // pass for the SCF builds)
   const int n = a.nbf;
   const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
   const int ra = SA.mrow + oa, rb = SB.mrow + ob, rc = SC.mrow + oc;
-  T* Dab = W + NE;                 // after V (NE >= NEP)
-  T* Dcd = Dab + E::A * E::B;
-  T* Dk = Dcd + E::C * E::D;       // per k: ac, ad, bc, bd
-  constexpr int DKS = SM::DK;
+  constexpr int PJ = SM::PJ, PK = SM::PK, DJS = SM::DJ, DKS = SM::DK;
+  T* Dj = W + NE;                  // after V (NE >= NEP); per Coulomb density: ab, cd
+  T* Dk = Dj + PJ * DJS;           // per exchange density: ac, ad, bc, bd
   double f = 1.0;
   if (P.sha == P.shb) f *= 0.5;
   if (Q.sha == Q.shb) f *= 0.5;
@@ -858,18 +878,27 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
   constexpr int NAB = E::A * E::B, NCD = E::C * E::D;
   constexpr int NAC = E::A * E::C, NAD = E::A * E::D, NBC = E::B * E::C, NBD = E::B * E::D;
   constexpr int BCD = E::B * E::C * E::D, CD_ = E::C * E::D;
-  const int npass = a.nj > (a.nk + 1) / 2 ? a.nj : (a.nk + 1) / 2;
+  // target kinds 0..5 = J[ab], J[cd], K[ac], K[ad], K[bc], K[bd]; targets per
+  // density and dot-product lengths
+  constexpr int CNT[6] = {NAB, NCD, NAC, NAD, NBC, NBD};
+  constexpr int NT[6] = {NCD, NAB, NBD, NBC, NAD, NAC};
+  // kinds in order of decreasing dot length, so that the long dot products
+  // share rounds of 32 lanes with each other rather than with short ones
+  constexpr auto ORD = kind_order(NT);
+  const int npj = (a.nj + PJ - 1) / PJ, npk = (a.nk + PK - 1) / PK;
+  const int npass = npj > npk ? npj : npk;
   for (int pass = 0; pass < npass; ++pass) {
-    const bool hasj = pass < a.nj;
-    const int k0 = 2 * pass;
-    const int nkp = a.nk - k0 >= 2 ? 2 : (a.nk - k0 > 0 ? a.nk - k0 : 0);
+    const int j0 = pass * PJ, k0 = pass * PK;
+    const int pj = a.nj - j0 >= PJ ? PJ : (a.nj - j0 > 0 ? a.nj - j0 : 0);
+    const int pk = a.nk - k0 >= PK ? PK : (a.nk - k0 > 0 ? a.nk - k0 : 0);
     if (pass) __syncwarp();  // the previous pass has read its blocks
-    if (hasj) {
-      const T* djt = dj_of<T>(a) + (size_t)pass * a.kstride;
-      for (int i = lane; i < NAB; i += 32) Dab[i] = __ldg(djt + (size_t)(ra + i / E::B) * n + ob + i % E::B);
-      for (int i = lane; i < NCD; i += 32) Dcd[i] = __ldg(djt + (size_t)(rc + i / E::D) * n + od + i % E::D);
+    for (int jj = 0; jj < pj; ++jj) {
+      const T* djt = dj_of<T>(a) + (size_t)(j0 + jj) * a.kstride;
+      T* dab = Dj + jj * DJS;
+      for (int i = lane; i < NAB; i += 32) dab[i] = __ldg(djt + (size_t)(ra + i / E::B) * n + ob + i % E::B);
+      for (int i = lane; i < NCD; i += 32) dab[NAB + i] = __ldg(djt + (size_t)(rc + i / E::D) * n + od + i % E::D);
     }
-    for (int kk = 0; kk < nkp; ++kk) {
+    for (int kk = 0; kk < pk; ++kk) {
       const T* dk = dk_of<T>(a) + (size_t)(k0 + kk) * a.kstride;
       T* base = Dk + kk * DKS;
       for (int i = lane; i < NAC; i += 32) base[i] = __ldg(dk + (size_t)(ra + i / E::C) * n + oc + i % E::C);
@@ -881,52 +910,53 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
       for (int i = lane; i < NBD; i += 32) base[i] = __ldg(dk + (size_t)(rb + i / E::D) * n + od + i % E::D);
     }
     __syncwarp();
-    double* gj = a.gj + (size_t)pass * a.kstride;
-    const int nJ = hasj ? NAB + NCD : 0;
-    const int ntarget = nJ + nkp * (NAC + NAD + NBC + NBD);
+    const int ntarget = (NAB + NCD) * pj + (NAC + NAD + NBC + NBD) * pk;
     // Every target element is a strided dot product of V with a density block:
     //   s = sum_{u < n1, v < n2} V[vb + u s1 + v s2] Dv[u n2 + v].
     // Only the (integer) descriptor depends on the target kind, so the lanes of
     // a round share one FP64 instruction stream whatever kinds they hold.
     for (int o = lane; o < ntarget; o += 32) {
+      int r = o, kind = 0;
+#pragma unroll
+      for (int q = 0, found = 0; q < 6; ++q) {
+        const int kd = ORD.k[q];
+        const int cnt = CNT[kd] * (kd < 2 ? pj : pk);
+        if (!found) {
+          if (r < cnt) { kind = kd; found = 1; } else { r -= cnt; }
+        }
+      }
+      const int di = r / CNT[kind], e = r - di * CNT[kind];
       int vb, s1, s2, n1, n2;
       const T* dv;
       double* dst;
-      double fac;
-      if (hasj && o < NAB) {  // J[a][b] += sum_cd V D[c][d]
-        const int i = o / E::B, j = o % E::B;
-        vb = o * NCD; s1 = 0; s2 = 1; n1 = 1; n2 = NCD; dv = Dcd;
-        dst = gj + (size_t)(ra + i) * n + ob + j;
+      double fac = f;
+      if (kind == 0) {  // J[a][b] += sum_cd V D[c][d]
+        const int i = e / E::B, j = e % E::B;
+        vb = e * NCD; s1 = 0; s2 = 1; n1 = 1; n2 = NCD; dv = Dj + di * DJS + NAB;
+        dst = a.gj + (size_t)(j0 + di) * a.kstride + (size_t)(ra + i) * n + ob + j;
         fac = 2.0 * f;
-      } else if (o < nJ) {  // J[c][d] += sum_ab V D[a][b]
-        const int cd = o - NAB, k = cd / E::D, l = cd % E::D;
-        vb = cd; s1 = NCD; s2 = 0; n1 = NAB; n2 = 1; dv = Dab;
-        dst = gj + (size_t)(rc + k) * n + od + l;
+      } else if (kind == 1) {  // J[c][d] += sum_ab V D[a][b]
+        const int k = e / E::D, l = e % E::D;
+        vb = e; s1 = NCD; s2 = 0; n1 = NAB; n2 = 1; dv = Dj + di * DJS;
+        dst = a.gj + (size_t)(j0 + di) * a.kstride + (size_t)(rc + k) * n + od + l;
         fac = 2.0 * f;
       } else {
-        int r = o - nJ;
-        const int kk = r / (NAC + NAD + NBC + NBD);
-        r -= kk * (NAC + NAD + NBC + NBD);
-        const T* dk = Dk + kk * DKS;
-        double* gk = a.gk + (size_t)(k0 + kk) * a.kstride;
-        fac = f;
-        if (r < NAC) {  // K[a][c] += sum_bd V[a b c d] D[b][d]
-          const int i = r / E::C, k = r % E::C;
+        const T* dk = Dk + di * DKS;
+        double* gk = a.gk + (size_t)(k0 + di) * a.kstride;
+        if (kind == 2) {  // K[a][c] += sum_bd V[a b c d] D[b][d]
+          const int i = e / E::C, k = e % E::C;
           vb = i * BCD + k * E::D; s1 = CD_; s2 = 1; n1 = E::B; n2 = E::D; dv = dk + NAC + NAD + NBC;
           dst = gk + (size_t)(ra + i) * n + oc + k;
-        } else if (r < NAC + NAD) {  // K[a][d] += sum_bc V D[b][c]
-          r -= NAC;
-          const int i = r / E::D, l = r % E::D;
+        } else if (kind == 3) {  // K[a][d] += sum_bc V D[b][c]
+          const int i = e / E::D, l = e % E::D;
           vb = i * BCD + l; s1 = CD_; s2 = E::D; n1 = E::B; n2 = E::C; dv = dk + NAC + NAD;
           dst = gk + (size_t)(ra + i) * n + od + l;
-        } else if (r < NAC + NAD + NBC) {  // K[b][c] += sum_ad V D[a][d]
-          r -= NAC + NAD;
-          const int j = r / E::C, k = r % E::C;
+        } else if (kind == 4) {  // K[b][c] += sum_ad V D[a][d]
+          const int j = e / E::C, k = e % E::C;
           vb = j * CD_ + k * E::D; s1 = BCD; s2 = 1; n1 = E::A; n2 = E::D; dv = dk + NAC;
           dst = gk + (size_t)(rb + j) * n + oc + k;
         } else {  // K[b][d] += sum_ac V D[a][c]
-          r -= NAC + NAD + NBC;
-          const int j = r / E::D, l = r % E::D;
+          const int j = e / E::D, l = e % E::D;
           vb = j * CD_ + l; s1 = BCD; s2 = E::D; n1 = E::A; n2 = E::C; dv = dk;
           dst = gk + (size_t)(rb + j) * n + od + l;
         }
