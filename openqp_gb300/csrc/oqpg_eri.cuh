@@ -564,12 +564,15 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
     return;
   }
   const T cut = (T)a.elem_cut;
-#pragma unroll
-  for (int e = 0; e < E::NEP; ++e) V[e] = cut_elem(V[e], cut);
+  // the shell-identity factor f (a power of two) scales the block once, not
+  // every digested target: exact, and NEP multiplies instead of one per atomic
   double f = 1.0;
   if (P.sha == P.shb) f *= 0.5;
   if (Q.sha == Q.shb) f *= 0.5;
   if (qd.x == qd.y) f *= 0.5;
+  const T fT = (T)f;
+#pragma unroll
+  for (int e = 0; e < E::NEP; ++e) V[e] = cut_elem(V[e], cut) * fT;
   const int n = a.nbf;
   // columns within the molecule, rows in the stacked matrices
   const int oa = SA.aoff, ob = SB.aoff, oc = SC.aoff, od = SD.aoff;
@@ -600,15 +603,16 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
         jab[ab] = fma(v, dcd[cd], jab[ab]);
         jcd[cd] = fma(v, dab[ab], jcd[cd]);
       }
-    const double f2 = 2.0 * f;
 #pragma unroll
     for (int i = 0; i < E::A; ++i)
 #pragma unroll
-      for (int j = 0; j < E::B; ++j) atomicAdd(gj + (size_t)(ra + i) * n + ob + j, f2 * (double)jab[i * E::B + j]);
+      for (int j = 0; j < E::B; ++j)
+        atomicAdd(gj + (size_t)(ra + i) * n + ob + j, (double)(jab[i * E::B + j] + jab[i * E::B + j]));
 #pragma unroll
     for (int i = 0; i < E::C; ++i)
 #pragma unroll
-      for (int j = 0; j < E::D; ++j) atomicAdd(gj + (size_t)(rc + i) * n + od + j, f2 * (double)jcd[i * E::D + j]);
+      for (int j = 0; j < E::D; ++j)
+        atomicAdd(gj + (size_t)(rc + i) * n + od + j, (double)(jcd[i * E::D + j] + jcd[i * E::D + j]));
   }
   // Exchange: G_K[ac] += f sum V D_bd ; [ad] += f V D_bc ; [bc] += f V D_ad ; [bd] += f V D_ac
   for (int kk = 0; kk < a.nk; ++kk) {
@@ -655,16 +659,16 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
 #pragma unroll
     for (int i = 0; i < E::A; ++i) {
 #pragma unroll
-      for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(ra + i) * n + oc + j, f * (double)kac[i * E::C + j]);
+      for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(ra + i) * n + oc + j, (double)kac[i * E::C + j]);
 #pragma unroll
-      for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(ra + i) * n + od + j, f * (double)kad[i * E::D + j]);
+      for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(ra + i) * n + od + j, (double)kad[i * E::D + j]);
     }
 #pragma unroll
     for (int i = 0; i < E::B; ++i) {
 #pragma unroll
-      for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(rb + i) * n + oc + j, f * (double)kbc[i * E::C + j]);
+      for (int j = 0; j < E::C; ++j) atomicAdd(gk + (size_t)(rb + i) * n + oc + j, (double)kbc[i * E::C + j]);
 #pragma unroll
-      for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(rb + i) * n + od + j, f * (double)kbd[i * E::D + j]);
+      for (int j = 0; j < E::D; ++j) atomicAdd(gk + (size_t)(rb + i) * n + od + j, (double)kbd[i * E::D + j]);
     }
   }
 }
@@ -862,7 +866,13 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
     return;
   }
   const T cut = (T)a.elem_cut;
-  for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], cut);
+  // the shell-identity factor (a power of two) scales the block once
+  double f = 1.0;
+  if (P.sha == P.shb) f *= 0.5;
+  if (Q.sha == Q.shb) f *= 0.5;
+  if (qd.x == qd.y) f *= 0.5;
+  const T fT = (T)f;
+  for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], cut) * fT;
   // density blocks: up to PJ Coulomb and PK exchange densities per pass (one
   // pass for the SCF builds)
   const int n = a.nbf;
@@ -871,10 +881,6 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
   constexpr int PJ = SM::PJ, PK = SM::PK, DJS = SM::DJ, DKS = SM::DK;
   T* Dj = W + NE;                  // after V (NE >= NEP); per Coulomb density: ab, cd
   T* Dk = Dj + PJ * DJS;           // per exchange density: ac, ad, bc, bd
-  double f = 1.0;
-  if (P.sha == P.shb) f *= 0.5;
-  if (Q.sha == Q.shb) f *= 0.5;
-  if (qd.x == qd.y) f *= 0.5;
   constexpr int NAB = E::A * E::B, NCD = E::C * E::D;
   constexpr int NAC = E::A * E::C, NAD = E::A * E::D, NBC = E::B * E::C, NBD = E::B * E::D;
   constexpr int BCD = E::B * E::C * E::D, CD_ = E::C * E::D;
@@ -929,17 +935,14 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
       int vb, s1, s2, n1, n2;
       const T* dv;
       double* dst;
-      double fac = f;
       if (kind == 0) {  // J[a][b] += sum_cd V D[c][d]
         const int i = e / E::B, j = e % E::B;
         vb = e * NCD; s1 = 0; s2 = 1; n1 = 1; n2 = NCD; dv = Dj + di * DJS + NAB;
         dst = a.gj + (size_t)(j0 + di) * a.kstride + (size_t)(ra + i) * n + ob + j;
-        fac = 2.0 * f;
       } else if (kind == 1) {  // J[c][d] += sum_ab V D[a][b]
         const int k = e / E::D, l = e % E::D;
         vb = e; s1 = NCD; s2 = 0; n1 = NAB; n2 = 1; dv = Dj + di * DJS;
         dst = a.gj + (size_t)(j0 + di) * a.kstride + (size_t)(rc + k) * n + od + l;
-        fac = 2.0 * f;
       } else {
         const T* dk = Dk + di * DKS;
         double* gk = a.gk + (size_t)(k0 + di) * a.kstride;
@@ -968,7 +971,7 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
         s = fma(V[vb + u * s1 + v * s2], dv[t], s);
         if (++v == n2) { v = 0; ++u; }
       }
-      atomicAdd(dst, fac * (double)s);
+      atomicAdd(dst, (double)(kind < 2 ? s + s : s));   // Coulomb targets carry the factor 2
     }
   }
 }
