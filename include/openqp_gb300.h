@@ -86,6 +86,15 @@ int routec_fock_set_precision(int mode, double threshold);
 void routec_grad2(const double* d, const double* xyz, double* de, const int* nbf, const int* natm,
                   const double* hfscale, const double* coulscale, int* info);
 
+/* routec_grad2_mrsf: the reference's MRSF gradient seam
+ * (source/modules/routec_bridge.F90:65-76, called from
+ * modules/tdhf_mrsf_gradient.F90:274-297 for non-CAM runs): oqpg_grad2_mrsf
+ * on the routec_fock_init context, de(3, natm) accumulated; declines
+ * (info = 1) for another basis or geometry. */
+void routec_grad2_mrsf(const double* d, const double* p, const double* spc, const double* xyz, double* de,
+                       const int* nbf, const int* natm, const double* hfscale, const double* hfscale2,
+                       const double* coulscale, const double* spcscale, const int* mrst, int* info);
+
 /* Response-type builds on the process-global context (extensions: the
  * reference has no seam for these digestions; a maintainer binds them in
  * place of the int2_driver%run call of the consumer).
@@ -330,6 +339,17 @@ int oqpg_grad2_bilinear(oqpg_ctx* ctx, const double* x, const double* y, const d
  * bound of their two-particle density is below the threshold run in FP32 and
  * add into the FP64 gradient. */
 int oqpg_grad_stats(const oqpg_ctx* ctx, double* out, int n);
+
+/* Two-electron MRSF gradient, accumulated into de(3, natom): grd2 with the
+ * two-particle density of grd2_mrsf_compute_data_t (source/modules/
+ * tdhf_mrsf_gradient.F90:341-355, 404-601).  d, p (nbf, nbf, 2): the RAW alpha
+ * / beta SCF and relaxed difference densities (the sum / difference of its
+ * init is formed here); spc (7, nbf, nbf): the response densities bo2v,
+ * bo1v, bco1, bco2, o21v, co12, ball (general, not symmetric), all Fortran
+ * column-major; spcscale = {spc_coco, spc_ovov, spc_coov}; mrst 1 or 3.
+ * FP64 whatever the precision mode. */
+int oqpg_grad2_mrsf(oqpg_ctx* ctx, const double* d, const double* p, const double* spc, double hfscale,
+                    double hfscale2, double coulscale, const double* spcscale, int mrst, double* de);
 
 /* Response-type builds (single-molecule contexts; see routec_fock_td and
  * routec_fock_mrsf for the layouts and the reference routines).  Every

@@ -64,6 +64,10 @@ def lib():
         L.oqpg_grad2.argtypes = [ctypes.c_void_p, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double, _d]
         L.oqpg_grad2_bilinear.argtypes = [ctypes.c_void_p, _d, _d, _d, _d, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_double, _d]
+        L.oqpg_grad2_mrsf.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      _d, ctypes.c_int, _d]
+        L.routec_grad2_mrsf.argtypes = [_d, _d, _d, _d, _d, _i, _i, _d, _d, _d, _d, _i, _i]
+        L.routec_grad2_mrsf.restype = None
         L.oqpg_grad_stats.argtypes = [ctypes.c_void_p, _d, ctypes.c_int]
         L.routec_grad2.argtypes = [_d, _d, _d, _i, _i, _d, _d, _i]
         L.routec_grad2.restype = None

@@ -61,6 +61,12 @@ struct GradArgs {
   double cutoff2;           // quartet skipped if dabmax Q_P Q_Q < cutoff / 2
   double dtol2;             // (sp sq)^2 < dtol2 (p + q): primitive quartet skipped
   double dabcut2;           // (sp sq)^2 dabmax^2 < dabcut2 (p + q): skipped
+  // MRSF form (mrsf != 0): eleven Cartesian-effective matrices d2a, d2b, p2a,
+  // p2b, ball, bo2v, bo1v, bco1, bco2, o21v, co12 at mm + m ncart^2 and the
+  // coefficients of grd2_mrsf_compute_data_t_get_density (mq with sgnk)
+  int mrsf;
+  const double* mm;
+  double mcoul, mx, mx2, mq1, mq2, mq3;
   double* de;               // 3 x natom, accumulated
   unsigned long long* counters;  // [0] primitive quartets evaluated, [1] quartets evaluated
   int ctas_per_sm;
@@ -102,10 +108,52 @@ struct GCls {
   }
 };
 
+// MRSF two-particle density of grd2_mrsf_compute_data_t_get_density
+// (modules/tdhf_mrsf_gradient.F90:404-601) at Cartesian-effective indices
+// (i, j, k, l).  The reference's eight-term sums are regrouped: the
+// co12 / o21v sums are twice four products, and its dc / dd sums pair up as
+// dc(X, Y) = dc(Y, X), dd(X, Y) = dd(Y, X).
+static __device__ __noinline__ double gamma_mrsf(const GradArgs& g, int i, int j, int k, int l) {
+  const size_t n = (size_t)g.ncart, n2 = n * n;
+  auto X = [&](int m, int r, int c) { return __ldg(g.mm + m * n2 + (size_t)r * n + c); };
+  enum { A = 0, B = 1, P = 2, Q = 3, L = 4, V2 = 5, V1 = 6, K1 = 7, K2 = 8, O = 9, C = 10 };
+  const double aij = X(A, i, j), pij = X(P, i, j);
+  double df1 = g.mcoul * ((aij + pij) * X(A, k, l) + aij * X(P, k, l));
+  if (g.mx != 0.0 || g.mx2 != 0.0) {
+    const double aik = X(A, i, k), ail = X(A, i, l), bik = X(B, i, k), bil = X(B, i, l);
+    const double dq1 = (aik + X(P, i, k)) * X(A, j, l) + aik * X(P, j, l) + (ail + X(P, i, l)) * X(A, j, k) +
+                       ail * X(P, j, k) + (bik + X(Q, i, k)) * X(B, j, l) + bik * X(Q, j, l) +
+                       (bil + X(Q, i, l)) * X(B, j, k) + bil * X(Q, j, k);
+    const double dt2 = X(L, i, k) * X(L, j, l) + X(L, k, i) * X(L, l, j) + X(L, i, l) * X(L, j, k) +
+                       X(L, l, i) * X(L, k, j);
+    df1 -= g.mx * dq1 + 2.0 * g.mx2 * dt2;
+  }
+  auto four = [&](int m) {
+    return X(m, i, k) * X(m, l, j) + X(m, i, l) * X(m, k, j) + X(m, j, k) * X(m, l, i) + X(m, j, l) * X(m, k, i);
+  };
+  if (g.mq1 != 0.0) df1 += 2.0 * g.mq1 * four(C);
+  if (g.mq2 != 0.0) df1 += 2.0 * g.mq2 * four(O);
+  if (g.mq3 != 0.0) {
+    auto dc = [&](int x, int y) {
+      return X(x, i, k) * X(y, j, l) + X(x, i, l) * X(y, j, k) + X(x, j, k) * X(y, i, l) + X(x, j, l) * X(y, i, k) +
+             X(x, l, j) * X(y, k, i) + X(x, k, j) * X(y, l, i) + X(x, l, i) * X(y, k, j) + X(x, k, i) * X(y, l, j);
+    };
+    auto dd = [&](int x, int y) {
+      return (X(x, i, j) + X(x, j, i)) * (X(y, k, l) + X(y, l, k)) +
+             (X(x, k, l) + X(x, l, k)) * (X(y, i, j) + X(y, j, i));
+    };
+    df1 += 2.0 * g.mq3 * (dd(K1, V2) + dd(K2, V1) - dc(K1, V2) - dc(K2, V1));
+  }
+  return df1;
+}
+
 // Two-particle density of Cartesian element (ra, rb, rc, rd) (matrix rows /
 // columns in the Cartesian layout).
 template <typename T>
 __device__ __forceinline__ T gamma_elem(const GradArgs& g, int ra, int rb, int rc, int rd) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (g.mrsf) return gamma_mrsf(g, ra, rb, rc, rd);
+  }
   const int n = g.ncart;
   const T* xt = GAcc<T>::xt(g);
   const T* yt = GAcc<T>::yt(g);

@@ -206,6 +206,19 @@ void cart_effective(const oqpg_ctx* c, const double* M, double* Mc) {
     }
 }
 
+// Two-particle density of a gradient run: the bilinear HF form over
+// mats = x, y[, xs, ys], or (mrsf) the MRSF form over the eleven matrices of
+// grd2_mrsf_compute_data_t.  cjb / ckb bound |Gamma| by the shell maxima
+// for the quartet lists: cjb d_ab d_cd + ckb (d_ac d_bd + d_ad d_bc).
+struct GammaSpec {
+  bool spin = false, mrsf = false;
+  double cj = 0, ckt = 0, cks = 0;
+  double mcoul = 0, mx = 0, mx2 = 0, mq[3] = {0, 0, 0};
+  double cjb = 0, ckb = 0;
+};
+
+int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& gs, double cutoff, double* de);
+
 // dE/dR (accumulated into de[3 natom]) for the two-particle density of the
 // full AO matrices x, y (and the spin pair xs, ys, both null or both set).
 int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, const double* ys, double cj,
@@ -213,13 +226,26 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
   if (c->nmol != 1) return UNSUPPORTED;
   int rc;
   if ((rc = grad_init(c))) return rc;
-  cudaStream_t st = c->stream;
-  const int nc = c->ncart, ns = c->nshell;
+  const int nc = c->ncart;
   const size_t n2 = (size_t)nc * nc;
   const int nmat = xs ? 4 : 2;
   std::vector<double> mats(n2 * nmat);
   const double* src[4] = {x, y, xs, ys};
   for (int k = 0; k < nmat; ++k) cart_effective(c, src[k], mats.data() + k * n2);
+  GammaSpec gs;
+  gs.spin = xs != nullptr;
+  gs.cj = cj; gs.ckt = ckt; gs.cks = cks;
+  gs.cjb = std::fabs(cj);
+  gs.ckb = std::fabs(ckt) + std::fabs(cks);
+  return grad_run(c, mats, nmat, gs, cutoff, de);
+}
+
+int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& gs, double cutoff, double* de) {
+  int rc;
+  cudaStream_t st = c->stream;
+  const int nc = c->ncart, ns = c->nshell;
+  const size_t n2 = (size_t)nc * nc;
+  const bool xs = gs.spin;
   // shell maxima of the screening matrices
   std::vector<double> dsh((size_t)ns * ns, 0.0);
   for (int k = 0; k < nmat; ++k)
@@ -236,9 +262,17 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
         double& d = dsh[(size_t)si * ns + sj];
         d = std::max(d, m);
       }
+  if (gs.mrsf)   // the response matrices are not symmetric and enter transposed too
+    for (int si = 0; si < ns; ++si)
+      for (int sj = 0; sj < si; ++sj) {
+        const double m = std::max(dsh[(size_t)si * ns + sj], dsh[(size_t)sj * ns + si]);
+        dsh[(size_t)si * ns + sj] = dsh[(size_t)sj * ns + si] = m;
+      }
   cudaEvent_t e0 = c->ev[0], e1 = c->ev[3];
   GK(cudaEventRecord(e0, st));
-  const bool split = (c->precision_mode == 1 || c->precision_mode == 2 || c->precision_mode == 4) && c->tau_f32 > 0.0;
+  // the MRSF form runs in FP64 only (no FP32 copies of its eleven matrices)
+  const bool split = !gs.mrsf && (c->precision_mode == 1 || c->precision_mode == 2 || c->precision_mode == 4) &&
+                     c->tau_f32 > 0.0;
   if ((rc = gupload(c->d_gmat, mats, st))) return rc;
   if (split) {
     std::vector<float> matsf(mats.size());
@@ -261,8 +295,8 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
   la.sorted_q = c->d_sorted_q.as<double>();
   la.dsh = c->d_dshg.as<double>();
   la.atom = c->d_atom.as<int>();
-  la.cj = std::fabs(cj);
-  la.ck = std::fabs(ckt) + std::fabs(cks);
+  la.cj = gs.cjb;
+  la.ck = gs.ckb;
   la.cutoff = cutoff;
   la.cutoff2 = 0.5 * cutoff;
   la.tau32 = split ? c->tau_f32 : 0.0;
@@ -298,9 +332,18 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
   g.primsf = c->d_gprimsf.as<PrimPairF>();
   g.alphaf = c->d_galphaf.as<float>();
   const double* dm = c->d_gmat.as<double>();
-  g.xt = dm; g.yt = dm + n2;
-  g.xs = xs ? dm + 2 * n2 : nullptr;
-  g.ys = xs ? dm + 3 * n2 : nullptr;
+  if (gs.mrsf) {
+    g.xt = g.yt = dm;
+    g.xs = g.ys = nullptr;
+    g.mm = dm;
+    g.mrsf = 1;
+    g.mcoul = gs.mcoul; g.mx = gs.mx; g.mx2 = gs.mx2;
+    g.mq1 = gs.mq[0]; g.mq2 = gs.mq[1]; g.mq3 = gs.mq[2];
+  } else {
+    g.xt = dm; g.yt = dm + n2;
+    g.xs = xs ? dm + 2 * n2 : nullptr;
+    g.ys = xs ? dm + 3 * n2 : nullptr;
+  }
   if (split) {
     const float* fm = c->d_gmatf.as<float>();
     g.xtf = fm; g.ytf = fm + n2;
@@ -311,7 +354,7 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
   g.ncart = nc;
   g.coff = c->d_coff.as<int>();
   g.atom = c->d_atom.as<int>();
-  g.cj = cj; g.ckt = ckt; g.cks = cks;
+  g.cj = gs.cj; g.ckt = gs.ckt; g.cks = gs.cks;
   g.pure = c->pure ? 1 : 0;
   g.q = c->d_q.as<double>();
   g.cutoff2 = 0.5 * cutoff;
@@ -379,6 +422,46 @@ int grad_packed(oqpg_ctx* c, const double* d, int nfocks, double hfscale, double
   return grad_build(c, Dt.data(), Dt.data(), ds, ds, 4.0 * coulscale, hfscale, hfscale, c->tau, de);
 }
 
+// grd2 with the MRSF two-particle density (modules/tdhf_mrsf_gradient.F90:
+// 341-355 init, :404-601 get_density): d, p (n, n, 2) raw alpha / beta,
+// spc (7, n, n), Fortran column-major.
+int grad_mrsf(oqpg_ctx* c, const double* d, const double* p, const double* spc, double hfscale, double hfscale2,
+              double coulscale, const double* spcscale, int mrst, double* de) {
+  if (c->nmol != 1) return UNSUPPORTED;
+  if (mrst != 1 && mrst != 3) return UNSUPPORTED;
+  int rc;
+  if ((rc = grad_init(c))) return rc;
+  const int n = c->nbf, nc = c->ncart;
+  const size_t nn = (size_t)n * n, n2 = (size_t)nc * nc;
+  std::vector<double> raw(nn), mats(11 * n2);
+  auto make = [&](int m, auto elem) {
+    for (int r = 0; r < n; ++r)
+      for (int q = 0; q < n; ++q) raw[(size_t)r * n + q] = elem((size_t)r, (size_t)q);
+    cart_effective(c, raw.data(), mats.data() + m * n2);
+  };
+  auto F = [&](const double* M, size_t r, size_t q) { return M[r + n * q]; };
+  make(0, [&](size_t r, size_t q) { return F(d, r, q) + F(d + nn, r, q); });
+  make(1, [&](size_t r, size_t q) { return F(d, r, q) - F(d + nn, r, q); });
+  make(2, [&](size_t r, size_t q) { return F(p, r, q) + F(p + nn, r, q); });
+  make(3, [&](size_t r, size_t q) { return F(p, r, q) - F(p + nn, r, q); });
+  // spc(1..7) = bo2v, bo1v, bco1, bco2, o21v, co12, ball; kept as ball, bo2v, ..., co12
+  const int comp[7] = {6, 0, 1, 2, 3, 4, 5};
+  for (int k = 0; k < 7; ++k) make(4 + k, [&](size_t r, size_t q) { return spc[comp[k] + 7 * (r + n * q)]; });
+  const double sgnk = mrst == 3 ? -1.0 : 1.0;
+  GammaSpec gs;
+  gs.mrsf = true;
+  gs.mcoul = 4.0 * coulscale;
+  gs.mx = hfscale;
+  gs.mx2 = hfscale2;
+  for (int k = 0; k < 3; ++k) gs.mq[k] = sgnk * spcscale[k];
+  // |Gamma| <= cjb d_ab d_cd + ckb (d_ac d_bd + d_ad d_bc) over the shell maxima
+  // of all eleven matrices (term counts of the reference's sums)
+  gs.cjb = 3.0 * std::fabs(gs.mcoul) + 32.0 * std::fabs(spcscale[2]);
+  gs.ckb = 6.0 * std::fabs(hfscale) + 4.0 * std::fabs(hfscale2) + 4.0 * std::fabs(spcscale[0]) +
+           4.0 * std::fabs(spcscale[1]) + 16.0 * std::fabs(spcscale[2]);
+  return grad_run(c, mats, 11, gs, c->tau, de);
+}
+
 }  // namespace
 
 extern "C" {
@@ -394,6 +477,13 @@ int oqpg_grad2_bilinear(oqpg_ctx* ctx, const double* x, const double* y, const d
   if (!ctx) return NOT_INIT;
   if (!x || !y || !de || (!xs) != (!ys)) return UNSUPPORTED;
   return grad_build(ctx, x, y, xs, ys, cj, ckt, cks, ctx->tau, de);
+}
+
+int oqpg_grad2_mrsf(oqpg_ctx* ctx, const double* d, const double* p, const double* spc, double hfscale,
+                    double hfscale2, double coulscale, const double* spcscale, int mrst, double* de) {
+  if (!ctx) return NOT_INIT;
+  if (!d || !p || !spc || !spcscale || !de) return UNSUPPORTED;
+  return grad_mrsf(ctx, d, p, spc, hfscale, hfscale2, coulscale, spcscale, mrst, de);
 }
 
 int oqpg_grad_stats(const oqpg_ctx* ctx, double* out, int n) {

@@ -1607,6 +1607,30 @@ void routec_grad2(const double* d, const double* xyz, double* de, const int* nbf
   if (info) *info = rc;
 }
 
+void routec_grad2_mrsf(const double* d, const double* p, const double* spc, const double* xyz, double* de,
+                       const int* nbf, const int* natm, const double* hfscale, const double* hfscale2,
+                       const double* coulscale, const double* spcscale, const int* mrst, int* info) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!d || !p || !spc || !xyz || !de || !nbf || !natm || !hfscale || !hfscale2 || !coulscale || !spcscale ||
+           !mrst)
+    rc = UNSUPPORTED;
+  else if (*nbf != g_ctx->nbf || *natm != g_ctx->natom || g_ctx->nmol != 1) rc = NOT_INIT;
+  else {
+    rc = OK;
+    for (int s = 0; s < g_ctx->nshell && rc == OK; ++s) {
+      const int at = g_ctx->shell_atom[s];
+      const ShellDev& S = g_ctx->shells[s];
+      if (std::fabs(S.x - xyz[3 * at]) > 1e-10 || std::fabs(S.y - xyz[3 * at + 1]) > 1e-10 ||
+          std::fabs(S.z - xyz[3 * at + 2]) > 1e-10)
+        rc = NOT_INIT;
+    }
+    if (rc == OK) rc = oqpg_grad2_mrsf(g_ctx, d, p, spc, *hfscale, *hfscale2, *coulscale, spcscale, *mrst, de);
+  }
+  if (info) *info = rc;
+}
+
 void routec_fock_finalize(void) {
   std::lock_guard<std::mutex> lk(g_mutex);
   sig_release();

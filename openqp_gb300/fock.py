@@ -323,6 +323,25 @@ class FockBuilder:
             raise FockError(rc, "oqpg_grad2_bilinear")
         return de.reshape(-1, 3)
 
+    def grad2_mrsf(self, d, p, spc, hfscale, hfscale2, coulscale=1.0, spcscale=(1.0, 1.0, 1.0), mrst=1):
+        """MRSF two-electron gradient (natom, 3) of OpenQP's
+        grd2_mrsf_compute_data_t (modules/tdhf_mrsf_gradient.F90:341-601).
+        d, p: (2, nbf, nbf) raw alpha / beta SCF and relaxed difference
+        densities; spc: (7, nbf, nbf) response densities (bo2v, bo1v, bco1,
+        bco2, o21v, co12, ball), natural indexing; spcscale = (spc_coco,
+        spc_ovov, spc_coov)."""
+        n = self.nbf
+        fd, fp = (np.ascontiguousarray(np.asarray(m, dtype=np.float64).reshape(2, n, n).transpose(0, 2, 1))
+                  for m in (d, p))
+        fs = np.ascontiguousarray(np.asarray(spc, dtype=np.float64).reshape(7, n, n).transpose(2, 1, 0))
+        sc = np.asarray(spcscale, dtype=np.float64)
+        de = np.zeros(3 * self.bas.natom)
+        rc = lib().oqpg_grad2_mrsf(self.h, ptr(fd), ptr(fp), ptr(fs), float(hfscale), float(hfscale2),
+                                   float(coulscale), ptr(sc), int(mrst), ptr(de))
+        if rc != 0:
+            raise FockError(rc, "oqpg_grad2_mrsf")
+        return de.reshape(-1, 3)
+
     def grad_stats(self):
         s = np.zeros(5)
         lib().oqpg_grad_stats(self.h, ptr(s), 5)
@@ -453,6 +472,22 @@ def routec_grad2(d, xyz, nbf, natom, hfscale=1.0, coulscale=1.0, de=None):
     info = ctypes.c_int(1)
     lib().routec_grad2(ptr(d), ptr(x), ptr(de), ctypes.byref(n), ctypes.byref(na), ctypes.byref(hf), ctypes.byref(cs),
                        ctypes.byref(info))
+    return de.reshape(-1, 3), info.value
+
+
+def routec_grad2_mrsf(d, p, spc, xyz, nbf, natom, hfscale, hfscale2, coulscale=1.0, spcscale=(1.0, 1.0, 1.0), mrst=1,
+                      de=None):
+    """Calls routec_grad2_mrsf as OpenQP's bridge does: d, p the Fortran
+    (nbf, nbf, 2) arrays and spc the Fortran (7, nbf, nbf) array as flat
+    buffers; de (natom, 3) is accumulated.  Returns (de, info)."""
+    bufs = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in (d, p, spc, xyz)]
+    de = np.zeros(3 * natom) if de is None else np.ascontiguousarray(de, dtype=np.float64).reshape(-1)
+    sc = np.asarray(spcscale, dtype=np.float64)
+    n, na, ms = ctypes.c_int(nbf), ctypes.c_int(natom), ctypes.c_int(mrst)
+    hf, hf2, cs = ctypes.c_double(hfscale), ctypes.c_double(hfscale2), ctypes.c_double(coulscale)
+    info = ctypes.c_int(1)
+    lib().routec_grad2_mrsf(*[ptr(b) for b in bufs], ptr(de), ctypes.byref(n), ctypes.byref(na), ctypes.byref(hf),
+                            ctypes.byref(hf2), ctypes.byref(cs), ptr(sc), ctypes.byref(ms), ctypes.byref(info))
     return de.reshape(-1, 3), info.value
 
 

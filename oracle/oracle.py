@@ -49,6 +49,9 @@ def lib():
         L.orc_one_electron.argtypes = [ctypes.c_void_p, ctypes.c_int, _d, _d]
         L.orc_rys.argtypes = [ctypes.c_int, ctypes.c_double, _d, _d]
         L.orc_boys.argtypes = [ctypes.c_int, ctypes.c_double, _d]
+        L.orc_grad2e_mrsf.restype = ctypes.c_longlong
+        L.orc_grad2e_mrsf.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      _d, ctypes.c_int, ctypes.c_double, ctypes.c_int, _d]
         L.orc_grad2e.restype = ctypes.c_longlong
         L.orc_grad2e.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                  ctypes.c_int, ctypes.c_int, ctypes.c_int, _d]
@@ -320,6 +323,23 @@ class Oracle:
         nt = nthreads or os.cpu_count()
         nq = lib().orc_grad2e(self.h, _p(dt), None if dsp is None else _p(dsp), 4.0 * coulscale, hfscale, cutoff,
                               nt, int(stride), int(offset), _p(de))
+        self.last_grad2e_quartets = int(nq)
+        return de.reshape(-1, 3)
+
+    def grad2e_mrsf(self, d, p, spc, hfscale, hfscale2, coulscale=1.0, spcscale=(1.0, 1.0, 1.0), mrst=1,
+                    cutoff=1e-10, nthreads=None):
+        """MRSF two-electron gradient (natom, 3) of grd2 with the two-particle
+        density of grd2_mrsf_compute_data_t: d, p (2, nbf, nbf) raw alpha / beta
+        SCF and relaxed difference densities, spc (7, nbf, nbf) the response
+        densities (bo2v, bo1v, bco1, bco2, o21v, co12, ball), natural indexing."""
+        n = self.nbf
+        fd = np.ascontiguousarray(np.asarray(d, dtype=np.float64).transpose(0, 2, 1))
+        fp = np.ascontiguousarray(np.asarray(p, dtype=np.float64).transpose(0, 2, 1))
+        fs = np.ascontiguousarray(np.asarray(spc, dtype=np.float64).transpose(2, 1, 0))   # Fortran (7, n, n)
+        sc = np.asarray(spcscale, dtype=np.float64)
+        de = np.zeros(3 * self.bas.natom)
+        nq = lib().orc_grad2e_mrsf(self.h, _p(fd), _p(fp), _p(fs), hfscale, hfscale2, coulscale, _p(sc), int(mrst),
+                                   cutoff, nthreads or os.cpu_count(), _p(de))
         self.last_grad2e_quartets = int(nq)
         return de.reshape(-1, 3)
 

@@ -222,8 +222,29 @@ extern "C" {
 // ck = hfscale.  stride > 1 evaluates only the bra pairs ij with
 // ij % stride == offset (a bounded sample for timing).  Returns the number of
 // shell quartets evaluated.
-long long orc_grad2e(void* h, const double* Dt, const double* Ds, double cj, double ck, double cutoff, int nthreads,
-                     int stride, int offset, double* de) {
+}  // extern "C"
+
+namespace {
+
+// Cartesian layout of the basis: offset of every shell, total count, pure flag.
+struct CartLayout {
+  std::vector<int> coff;
+  int nct = 0;
+  bool pure = false;
+  explicit CartLayout(const Basis& B) : coff(B.nshell) {
+    for (int s = 0; s < B.nshell; ++s) {
+      coff[s] = nct;
+      nct += ncart(B.sh[s].am);
+      if (B.sh[s].harm && B.sh[s].am >= 2) pure = true;
+    }
+  }
+};
+
+// grd2_driver_gen over the canonical shell quartets with the two-particle
+// density gamma_fn(ra, rb, rc, rd) of Cartesian-effective indices.
+template <class GammaFn>
+long long grad2e_impl(void* h, const CartLayout& CLy, GammaFn gamma_fn, double cutoff, int nthreads, int stride,
+                      int offset, double* de) {
   const Basis& B = ((Handle*)h)->B;
   const int ns = B.nshell;
   // grd2 pair cutoffs (grd2.F90:238-260): dabcut, 10^-20, 10^-20, 20 ln 10
@@ -238,18 +259,8 @@ long long orc_grad2e(void* h, const double* Dt, const double* Ds, double cj, dou
   PS.build(B, cut);
   std::vector<double> Q((size_t)ns * ns);
   orc_schwarz(h, Q.data(), nthreads);
-  // Cartesian layout and Cartesian-effective densities
-  std::vector<int> coff(ns);
-  int nct = 0;
-  bool pure = false;
-  for (int s = 0; s < ns; ++s) {
-    coff[s] = nct;
-    nct += ncart(B.sh[s].am);
-    if (B.sh[s].harm && B.sh[s].am >= 2) pure = true;
-  }
-  std::vector<double> Dtc, Dsc;
-  cart_density(B, Dt, coff, nct, Dtc);
-  if (Ds) cart_density(B, Ds, coff, nct, Dsc);
+  const std::vector<int>& coff = CLy.coff;
+  const bool pure = CLy.pure;
   const double dtol2 = dtol * dtol;
   const double cutoff2 = cutoff / 2.0;
   long long numint = 0;
@@ -286,11 +297,7 @@ long long orc_grad2e(void* h, const double* Dt, const double* Ds, double cj, dou
                 for (int c = 0; c < n[2]; ++c)
                   for (int d = 0; d < n[3]; ++d, ++e) {
                     const size_t ra = coff[i] + a, rb = coff[j] + b, rc = coff[k] + c, rd = coff[l] + d;
-                    auto M = [&](const std::vector<double>& X, size_t r, size_t s) { return X[r * nct + s]; };
-                    double g = cj * M(Dtc, ra, rb) * M(Dtc, rc, rd) -
-                               ck * (M(Dtc, ra, rc) * M(Dtc, rb, rd) + M(Dtc, ra, rd) * M(Dtc, rb, rc));
-                    if (Ds)
-                      g -= ck * (M(Dsc, ra, rc) * M(Dsc, rb, rd) + M(Dsc, ra, rd) * M(Dsc, rb, rc));
+                    const double g = gamma_fn(ra, rb, rc, rd);
                     gam[e] = g;
                     const double nrm = pure ? 1.0
                                             : cart_norm(lv[0], a) * cart_norm(lv[1], b) * cart_norm(lv[2], c) *
@@ -374,6 +381,116 @@ long long orc_grad2e(void* h, const double* Dt, const double* Ds, double cj, dou
   for (int t = 0; t < nthreads; ++t)
     for (int x = 0; x < 3 * natom; ++x) de[x] += de_all[(size_t)t * 3 * natom + x];
   return numint;
+}
+
+// The MRSF two-particle density of grd2_mrsf_compute_data_t_get_density
+// (modules/tdhf_mrsf_gradient.F90:404-601), literally, over the
+// Cartesian-effective matrices M[0..10] = d2a, d2b, p2a, p2b (after the init
+// sum / difference, :341-355), ball, bo2v, bo1v, bco1, bco2, o21v, co12.
+struct MrsfGamma {
+  const std::vector<double>* M;
+  int n;
+  double coulfact, xcfact, xcfact2, q1, q2, q3, sgnk;
+  double operator()(size_t i1, size_t j1, size_t k1, size_t l1) const {
+    auto E = [&](int m, size_t r, size_t c) { return M[m][r * n + c]; };
+    auto d2a = [&](size_t r, size_t c) { return E(0, r, c); };
+    auto d2b = [&](size_t r, size_t c) { return E(1, r, c); };
+    auto p2a = [&](size_t r, size_t c) { return E(2, r, c); };
+    auto p2b = [&](size_t r, size_t c) { return E(3, r, c); };
+    auto ball = [&](size_t r, size_t c) { return E(4, r, c); };
+    auto bo2v = [&](size_t r, size_t c) { return E(5, r, c); };
+    auto bo1v = [&](size_t r, size_t c) { return E(6, r, c); };
+    auto bco1 = [&](size_t r, size_t c) { return E(7, r, c); };
+    auto bco2 = [&](size_t r, size_t c) { return E(8, r, c); };
+    auto o21v = [&](size_t r, size_t c) { return E(9, r, c); };
+    auto co12 = [&](size_t r, size_t c) { return E(10, r, c); };
+    double df1 = (d2a(i1, j1) + p2a(i1, j1)) * d2a(k1, l1) + d2a(i1, j1) * p2a(k1, l1);
+    df1 = df1 * coulfact;
+    if (xcfact != 0.0 || xcfact2 != 0.0) {
+      const double dq1 = (d2a(i1, k1) + p2a(i1, k1)) * d2a(j1, l1) + d2a(i1, k1) * p2a(j1, l1) +
+                         (d2a(i1, l1) + p2a(i1, l1)) * d2a(j1, k1) + d2a(i1, l1) * p2a(j1, k1) +
+                         (d2b(i1, k1) + p2b(i1, k1)) * d2b(j1, l1) + d2b(i1, k1) * p2b(j1, l1) +
+                         (d2b(i1, l1) + p2b(i1, l1)) * d2b(j1, k1) + d2b(i1, l1) * p2b(j1, k1);
+      const double dt2 = ball(i1, k1) * ball(j1, l1) + ball(k1, i1) * ball(l1, j1) + ball(i1, l1) * ball(j1, k1) +
+                         ball(l1, i1) * ball(k1, j1);
+      df1 = df1 - xcfact * dq1 - xcfact2 * 2.0 * dt2;
+    }
+    auto eight = [&](auto X) {   // db1 / db2 pattern
+      return X(i1, k1) * X(l1, j1) + X(i1, l1) * X(k1, j1) + X(j1, k1) * X(l1, i1) + X(j1, l1) * X(k1, i1) +
+             X(l1, j1) * X(i1, k1) + X(k1, j1) * X(i1, l1) + X(l1, i1) * X(j1, k1) + X(k1, i1) * X(j1, l1);
+    };
+    if (q1 != 0.0) df1 = df1 + sgnk * q1 * eight(co12);
+    if (q2 != 0.0) df1 = df1 + sgnk * q2 * eight(o21v);
+    if (q3 != 0.0) {
+      auto dc = [&](auto X, auto Y) {
+        return X(i1, k1) * Y(j1, l1) + X(i1, l1) * Y(j1, k1) + X(j1, k1) * Y(i1, l1) + X(j1, l1) * Y(i1, k1) +
+               X(l1, j1) * Y(k1, i1) + X(k1, j1) * Y(l1, i1) + X(l1, i1) * Y(k1, j1) + X(k1, i1) * Y(l1, j1);
+      };
+      auto dd = [&](auto X, auto Y) {
+        return X(i1, j1) * Y(l1, k1) + X(i1, j1) * Y(k1, l1) + X(j1, i1) * Y(l1, k1) + X(j1, i1) * Y(k1, l1) +
+               X(l1, k1) * Y(i1, j1) + X(k1, l1) * Y(i1, j1) + X(l1, k1) * Y(j1, i1) + X(k1, l1) * Y(j1, i1);
+      };
+      const double dc1 = dc(bco1, bo2v), dc2 = dc(bco2, bo1v), dc3 = dc(bo2v, bco1), dc4 = dc(bo1v, bco2);
+      const double dd1 = dd(bco1, bo2v), dd2 = dd(bco2, bo1v), dd3 = dd(bo2v, bco1), dd4 = dd(bo1v, bco2);
+      df1 = df1 + sgnk * q3 * (-dc1 - dc2 - dc3 - dc4 + dd1 + dd2 + dd3 + dd4);
+    }
+    return df1;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+long long orc_grad2e(void* h, const double* Dt, const double* Ds, double cj, double ck, double cutoff, int nthreads,
+                     int stride, int offset, double* de) {
+  const Basis& B = ((Handle*)h)->B;
+  const CartLayout CLy(B);
+  const int nct = CLy.nct;
+  std::vector<double> Dtc, Dsc;
+  cart_density(B, Dt, CLy.coff, nct, Dtc);
+  if (Ds) cart_density(B, Ds, CLy.coff, nct, Dsc);
+  const bool spin = Ds != nullptr;
+  auto gam = [&](size_t ra, size_t rb, size_t rc, size_t rd) {
+    auto M = [&](const std::vector<double>& X, size_t r, size_t s) { return X[r * nct + s]; };
+    double g = cj * M(Dtc, ra, rb) * M(Dtc, rc, rd) -
+               ck * (M(Dtc, ra, rc) * M(Dtc, rb, rd) + M(Dtc, ra, rd) * M(Dtc, rb, rc));
+    if (spin) g -= ck * (M(Dsc, ra, rc) * M(Dsc, rb, rd) + M(Dsc, ra, rd) * M(Dsc, rb, rc));
+    return g;
+  };
+  return grad2e_impl(h, CLy, gam, cutoff, nthreads, stride, offset, de);
+}
+
+// MRSF two-electron gradient (accumulated into de[3*natom]): d, p (nbf, nbf, 2)
+// the raw alpha / beta SCF and relaxed difference densities, spc (7, nbf, nbf)
+// the response densities, all Fortran column-major (the routec_grad2_mrsf
+// layout); spcscale = {spc_coco, spc_ovov, spc_coov}; mrst 1 or 3.
+long long orc_grad2e_mrsf(void* h, const double* d, const double* p, const double* spc, double hfscale,
+                          double hfscale2, double coulscale, const double* spcscale, int mrst, double cutoff,
+                          int nthreads, double* de) {
+  const Basis& B = ((Handle*)h)->B;
+  const int n = B.nbf;
+  const size_t n2 = (size_t)n * n;
+  const CartLayout CLy(B);
+  std::vector<double> raw(n2);
+  std::vector<double> M[11];
+  auto fort = [&](const double* F, size_t r, size_t c) { return F[r + n * c]; };
+  auto make = [&](int m, auto elem) {
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < n; ++c) raw[(size_t)r * n + c] = elem(r, c);
+    cart_density(B, raw.data(), CLy.coff, CLy.nct, M[m]);
+  };
+  make(0, [&](int r, int c) { return fort(d, r, c) + fort(d + n2, r, c); });
+  make(1, [&](int r, int c) { return fort(d, r, c) - fort(d + n2, r, c); });
+  make(2, [&](int r, int c) { return fort(p, r, c) + fort(p + n2, r, c); });
+  make(3, [&](int r, int c) { return fort(p, r, c) - fort(p + n2, r, c); });
+  // spc(7, nbf, nbf): ball is component 7, then bo2v, bo1v, bco1, bco2, o21v, co12 = 1..6
+  const int comp[7] = {6, 0, 1, 2, 3, 4, 5};
+  for (int q = 0; q < 7; ++q)
+    make(4 + q, [&](int r, int c) { return spc[comp[q] + 7 * ((size_t)r + (size_t)n * c)]; });
+  MrsfGamma G{M, CLy.nct, 4.0 * coulscale, hfscale, hfscale2, spcscale[0], spcscale[1], spcscale[2],
+              mrst == 3 ? -1.0 : 1.0};
+  return grad2e_impl(h, CLy, G, cutoff, nthreads, 1, 0, de);
 }
 
 // One-electron gradient (accumulated into de[3*natom]): sum_uv D_uv dH_uv/dR

@@ -205,3 +205,67 @@ def test_grad2_precision_split(gpu, mode):
     assert np.abs(g32 - g64).max() < 1e-7
     fb.set_precision(mode, 1e-3)
     assert np.abs(fb.grad2(d) - g64).max() < 1e-5
+
+
+def _mrsf_inputs(bas, seed):
+    from openqp_gb300 import workloads
+    n = bas.nbf
+    nel = workloads.nelectrons(bas)
+    du = workloads.density_open(bas, nel // 2 + 1, nel // 2 - 1, seed)
+    d = np.stack([_full(du[0], n), _full(du[1], n)])
+    rng = np.random.default_rng(seed)
+    p = rng.standard_normal((2, n, n)) * 0.05
+    p = 0.5 * (p + p.transpose(0, 2, 1))
+    spc = rng.standard_normal((7, n, n)) * 0.05
+    return d, p, spc
+
+
+@pytest.mark.parametrize("mrst", [1, 3])
+@pytest.mark.parametrize("nw,basis", [(2, "6-31g(d)"), (2, "cc-pvdz")])
+def test_grad2_mrsf_matches_oracle(gpu, oracle_lib, mrst, nw, basis):
+    """grd2 with the MRSF two-particle density of grd2_mrsf_compute_data_t
+    (non-symmetric response densities, spin-pair scales apart from HFscale)."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(nw, workloads.cube_edge_like_c1(nw), seed=6, basis=basis)
+    d, p, spc = _mrsf_inputs(bas, mrst)
+    fb = gpu.FockBuilder(bas)
+    o = oracle_lib.Oracle(bas)
+    args = (0.5, 0.45, 1.0, (0.4, 0.3, 0.2), mrst)
+    g = fb.grad2_mrsf(d, p, spc, *args)
+    ref = o.grad2e_mrsf(d, p, spc, *args)
+    assert np.abs(g - ref).max() < 1e-9 * max(1.0, np.abs(ref).max())
+    assert np.abs(g.sum(axis=0)).max() < 1e-9 * max(1.0, np.abs(ref).max())
+    # Coulomb only (every exchange-type branch off)
+    g0 = fb.grad2_mrsf(d, p, spc, 0.0, 0.0, 1.0, (0.0, 0.0, 0.0), mrst)
+    r0 = o.grad2e_mrsf(d, p, spc, 0.0, 0.0, 1.0, (0.0, 0.0, 0.0), mrst)
+    assert np.abs(g0 - r0).max() < 1e-9 * max(1.0, np.abs(r0).max())
+
+
+def test_grad2_mrsf_seam_and_precision(gpu):
+    """routec_grad2_mrsf with the Fortran buffers of tdhf_mrsf_gradient (de
+    accumulated, another geometry declined); the MRSF form stays FP64 when the
+    context runs the precision split."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(2, workloads.cube_edge_like_c1(2), seed=1, basis="6-31g(d)")
+    n = bas.nbf
+    d, p, spc = _mrsf_inputs(bas, 5)
+    fb = gpu.FockBuilder(bas)
+    ref = fb.grad2_mrsf(d, p, spc, 0.5, 0.5, 1.0, (0.5, 0.5, 0.5), 1)
+    fb.set_precision("mixed", 1e-6)
+    assert np.abs(fb.grad2_mrsf(d, p, spc, 0.5, 0.5, 1.0, (0.5, 0.5, 0.5), 1) - ref).max() < 1e-12
+    fd = np.ascontiguousarray(d.transpose(0, 2, 1))          # Fortran (nbf, nbf, 2)
+    fp = np.ascontiguousarray(p.transpose(0, 2, 1))
+    fs = np.ascontiguousarray(spc.transpose(2, 1, 0))        # Fortran (7, nbf, nbf)
+    assert gpu.routec_init(bas, 1e-10) == 0
+    try:
+        de0 = np.ones((bas.natom, 3))
+        de, info = gpu.routec_grad2_mrsf(fd, fp, fs, bas.xyz, n, bas.natom, 0.5, 0.5, 1.0, (0.5, 0.5, 0.5), 1,
+                                         de=de0)
+        assert info == 0
+        assert np.abs(de - (1.0 + ref)).max() < 1e-10 * max(1.0, np.abs(ref).max())
+        moved = bas.xyz.copy()
+        moved[1, 2] += 0.01
+        _, info = gpu.routec_grad2_mrsf(fd, fp, fs, moved, n, bas.natom, 0.5, 0.5, 1.0, (0.5, 0.5, 0.5), 1)
+        assert info == 1
+    finally:
+        gpu.routec_finalize()

@@ -169,6 +169,75 @@ def test_grad2e_matches_finite_difference_of_e2(oracle_lib):
         assert abs(fd - g[at, x]) < 2e-7, (at, x, fd, g[at, x])
 
 
+def mrsf_gamma(d, p, spc, coul, x, x2, q, sgnk):
+    """Dense AO two-particle density of grd2_mrsf_compute_data_t_get_density
+    (modules/tdhf_mrsf_gradient.F90:404-601) in compact form: the eight-term
+    sums of the reference regrouped by index pairing."""
+    A, B = d[0] + d[1], d[0] - d[1]
+    P, Q = p[0] + p[1], p[0] - p[1]
+    bo2v, bo1v, bco1, bco2, o21v, co12, ball = spc
+    e = np.einsum
+    g = coul * (e("ij,kl->ijkl", A + P, A) + e("ij,kl->ijkl", A, P))
+
+    def ex(X, Y):   # X_ik Y_jl + X_il Y_jk
+        return e("ik,jl->ijkl", X, Y) + e("il,jk->ijkl", X, Y)
+
+    g -= x * (ex(A + P, A) + ex(A, P) + ex(B + Q, B) + ex(B, Q))
+    g -= 2 * x2 * (ex(ball, ball) + ex(ball.T, ball.T))
+
+    def eight(X):
+        return 2 * (e("ik,lj->ijkl", X, X) + e("il,kj->ijkl", X, X) + e("jk,li->ijkl", X, X) + e("jl,ki->ijkl", X, X))
+
+    g += sgnk * (q[0] * eight(co12) + q[1] * eight(o21v))
+
+    def dc(X, Y):
+        return (e("ik,jl->ijkl", X, Y) + e("il,jk->ijkl", X, Y) + e("jk,il->ijkl", X, Y) + e("jl,ik->ijkl", X, Y)
+                + e("lj,ki->ijkl", X, Y) + e("kj,li->ijkl", X, Y) + e("li,kj->ijkl", X, Y) + e("ki,lj->ijkl", X, Y))
+
+    def dd(X, Y):
+        return e("ij,kl->ijkl", X + X.T, Y + Y.T) + e("kl,ij->ijkl", X + X.T, Y + Y.T)
+
+    g += sgnk * q[2] * (-dc(bco1, bo2v) - dc(bco2, bo1v) - dc(bo2v, bco1) - dc(bo1v, bco2)
+                        + dd(bco1, bo2v) + dd(bco2, bo1v) + dd(bo2v, bco1) + dd(bo1v, bco2))
+    return g
+
+
+@pytest.mark.parametrize("mrst", [1, 3])
+def test_grad2e_mrsf_matches_finite_difference(oracle_lib, mrst):
+    """The MRSF two-electron gradient (grd2 with the MRSF two-particle density,
+    general non-symmetric response densities) equals central differences
+    (h = 1e-4 Bohr) of E2 = 1/8 sum_ijkl Gamma_ijkl (ij|kl) at fixed AO
+    densities; Gamma (compact restatement) has the eightfold symmetry."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(1, workloads.cube_edge_like_c1(1), seed=2, basis="6-31g(d)")
+    n = bas.nbf
+    rng = np.random.default_rng(mrst)
+    sym = lambda a: 0.5 * (a + a.swapaxes(-1, -2))
+    d, p = sym(rng.standard_normal((2, n, n)) * 0.3), sym(rng.standard_normal((2, n, n)) * 0.3)
+    spc = rng.standard_normal((7, n, n)) * 0.3
+    x, x2, q = 0.5, 0.45, (0.4, 0.3, 0.2)
+    sgnk = -1.0 if mrst == 3 else 1.0
+    G = mrsf_gamma(d, p, spc, 4.0, x, x2, q, sgnk)
+    for perm in ((1, 0, 2, 3), (0, 1, 3, 2), (2, 3, 0, 1)):
+        assert np.abs(G - G.transpose(perm)).max() < 1e-12 * np.abs(G).max()
+    o = oracle_lib.Oracle(bas)
+    g = o.grad2e_mrsf(d, p, spc, x, x2, 1.0, q, mrst)
+
+    def e2(xyz):
+        eri = oracle_lib.Oracle(bas.with_geometry(xyz)).eri_dense().reshape(n, n, n, n)
+        return np.sum(G * eri) / 8.0
+
+    h = 1e-4
+    for at, c in ((0, 2), (1, 0), (2, 1)):
+        xp = bas.xyz.copy()
+        xp[at, c] += h
+        xm = bas.xyz.copy()
+        xm[at, c] -= h
+        fd = (e2(xp) - e2(xm)) / (2 * h)
+        assert abs(fd - g[at, c]) < 2e-7 * max(1.0, abs(fd)), (at, c, fd, g[at, c])
+    assert np.abs(g.sum(axis=0)).max() < 1e-9
+
+
 def _dense_jk(o, n):
     eri = o.eri_dense().reshape(n, n, n, n)
     return (lambda D: np.einsum("ijkl,kl->ij", eri, D)), (lambda D: np.einsum("ijkl,jl->ik", eri, D))
