@@ -61,6 +61,10 @@ WORKLOADS = {
     # the differentiation configuration: two-electron gradient of (H2O)16 6-31G(d)
     "grad_water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian RHF two-electron gradient (grd2)", nwater=16,
                                edge=9.52, seed=0, basis="6-31g(d)", cutoff=1e-10, grad=True),
+    # the MRSF two-electron gradient (routec_grad2_mrsf): grd2 with the eleven-matrix MRSF density
+    "grad_mrsf_water16_631gd": dict(name="(H2O)16 6-31G(d) Cartesian MRSF two-electron gradient (grd2 with the "
+                                         "grd2_mrsf_compute_data_t density)", nwater=16, edge=9.52, seed=0,
+                                    basis="6-31g(d)", cutoff=1e-10, grad=True, mrsf_grad=True),
     # f shells: (H2O)16 cc-pVTZ spherical (one f shell per O, d on H; 928 bf)
     "water16_ccpvtz": dict(name="(H2O)16 cc-pVTZ spherical RHF J+K Fock build (f shells)", nwater=16, edge=9.52,
                            seed=0, basis="cc-pvtz", cutoff=1e-10),
@@ -615,6 +619,32 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
+    if WORKLOAD.get("grad"):
+        bas, d = make_workload(overlap="oracle")
+        if WORKLOAD.get("mrsf_grad"):
+            from openqp_gb300 import workloads
+            from oracle import oracle
+            oracle.build()
+            S = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"]).one_electron("S")
+            dm, pm, spc = workloads.mrsf_gradient_inputs(bas, WORKLOAD["seed"], S=S)
+            one = lambda: cpu_baseline_grad_mrsf(bas, dm, pm, spc, args.cpu_budget)
+            metric = "MRSF two-electron gradient evaluations/s"
+        else:
+            one = lambda: cpu_baseline_grad(bas, d, args.cpu_budget)
+            metric = "two-electron gradient evaluations/s"
+        vals = [one()["value"] for _ in range(max(1, args.steps))]
+        cb = one()
+        v = statistics.median(vals)
+        cb["value"] = v
+        line = {"impl": "reference", "metric": metric, "value": v, "unit": "grad evals/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "natom": bas.natom,
+                           "cutoff": WORKLOAD["cutoff"]},
+                "cpu_baseline": cb, "e2e": {"value": v, "unit": "grad evals/s", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     if WORKLOAD.get("cam"):
         bas, d = make_workload(overlap="oracle")
         vals = [cpu_baseline_cam(bas, d, args.cpu_budget)["value"] for _ in range(max(1, args.steps))]
@@ -923,6 +953,8 @@ def run_grad(args):
     from openqp_gb300.fock import FockBuilder, fp64_peak_tflops
     bas, d = make_workload()
     fb = FockBuilder(bas, cutoff=WORKLOAD["cutoff"])
+    if WORKLOAD.get("mrsf_grad"):
+        return run_grad_mrsf(args, bas, fb)
     for _ in range(args.warmup):
         fb.grad2(d)
     torch.cuda.synchronize()
@@ -972,6 +1004,84 @@ def run_grad(args):
         line["cpu_baseline"] = cpu_baseline_grad(bas, d, args.cpu_budget)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+MRSF_GRAD_ARGS = (0.5, 0.5, 1.0, (0.5, 0.5, 0.5), 1)   # hfscale, hfscale2, coulscale, spc scales, singlet
+
+
+def run_grad_mrsf(args, bas, fb):
+    """MRSF two-electron gradient evaluations/s through FockBuilder.grad2_mrsf
+    (host matrices in, dE/dR out: the seam's own data flow, so value and e2e
+    coincide), with the plain RHF-form gradient of the same total density for
+    comparison."""
+    import torch
+    ws, rank, local = dist_env()
+    from openqp_gb300 import workloads
+    from openqp_gb300.basis import pack
+    from openqp_gb300.fock import fp64_peak_tflops
+    d, p, spc = workloads.mrsf_gradient_inputs(bas, WORKLOAD["seed"])
+    for _ in range(args.warmup):
+        fb.grad2_mrsf(d, p, spc, *MRSF_GRAD_ARGS)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    sampler = ClockSampler(local)
+    sampler.start()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g = fb.grad2_mrsf(d, p, spc, *MRSF_GRAD_ARGS)
+        times.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    st = fb.grad_stats()
+    value = ws * args.steps / max_over_ranks(sum(times))
+    dt = pack(d[0] + d[1])
+    fb.grad2(dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fb.grad2(dt)
+    t_plain = (time.perf_counter() - t0) / args.steps
+    nb = int(8 * (d.size + p.size + spc.size))
+    line = {"metric": "MRSF two-electron gradient evaluations/s", "value": value, "unit": "grad evals/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded water cluster, triplet-reference densities, seeded response densities)",
+            "config": {"workload": WORKLOAD["name"], "nbf": bas.nbf, "natom": bas.natom, "cutoff": WORKLOAD["cutoff"],
+                       "hfscale": MRSF_GRAD_ARGS[0], "hfscale2": MRSF_GRAD_ARGS[1],
+                       "spcscale": list(MRSF_GRAD_ARGS[3]), "kind": "singlet",
+                       "l2": "flushed (256 MB write) before every timed step"},
+            "e2e": {"value": value, "unit": "grad evals/s", "h2d_bytes_per_step": nb,
+                    "d2h_bytes_per_step": int(8 * 3 * bas.natom)},
+            "grad_stats": st, "quartets_per_s": st["quartets"] / (sum(times) / args.steps),
+            "prim_quartets_per_s": st["prim_quartets"] / (sum(times) / args.steps),
+            "plain_rhf_form_grad_evals_per_s": 1.0 / t_plain,
+            "fp64_peak_tflops": fp64_peak_tflops(), "clocks": clocks,
+            "max_abs_grad": float(np.abs(g).max()), "sum_grad": float(np.abs(g.sum(axis=0)).max())}
+    if not args.no_cpu and rank == 0:
+        line["cpu_baseline"] = cpu_baseline_grad_mrsf(bas, d, p, spc, args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_grad_mrsf(bas, d, p, spc, budget_s):
+    """The oracle's grd2 restatement with the MRSF density (all host cores) on
+    1/stride of the bra shell pairs, scaled by stride."""
+    from oracle import oracle
+    oracle.build()
+    o = oracle.Oracle(bas, cutoff=WORKLOAD["cutoff"])
+    cores = os.cpu_count()
+
+    def run(stride, offset):
+        t0 = time.perf_counter()
+        o.grad2e_mrsf(d, p, spc, *MRSF_GRAD_ARGS, nthreads=cores, stride=stride, offset=offset)
+        return time.perf_counter() - t0, None
+
+    t, stride, _ = sampled(run, budget_s)
+    return {"value": 1.0 / t, "unit": "grad evals/s", "cores": cores, "kind": "port",
+            "sample": "oracle grd2 restatement with the MRSF two-particle density over 1/%d of the bra shell pairs "
+                      "(the middle pair of every %d), x%d; %d quartets in the sample"
+                      % (stride, stride, stride, o.last_grad2e_quartets)}
 
 
 def cpu_baseline_grad(bas, d, budget_s):

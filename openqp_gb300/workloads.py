@@ -146,6 +146,27 @@ def mrsf_session_inputs(bas, nocca, noccb, nvec, seed, S=None):
     return C, fmo[0], fmo[1], b
 
 
+def mrsf_gradient_inputs(bas, seed, S=None):
+    """Inputs of an MRSF two-electron gradient: raw alpha / beta densities of
+    a triplet reference (nocca = noccb + 2, Loewdin-orthonormal columns), a
+    symmetric relaxed difference density pair and seven general response
+    densities of the same scale (seeded); (2, n, n), (2, n, n), (7, n, n)."""
+    from .basis import unpack
+    n = bas.nbf
+    nel = nelectrons(bas)
+    du = density_open(bas, nel // 2 + 1, nel // 2 - 1, seed, S=S)
+    d = np.stack([unpack(du[0], n), unpack(du[1], n)])
+    if S is None:
+        S, _ = overlap_kinetic(bas)
+    rng = np.random.default_rng(seed + 1)
+    C = loewdin_columns(S, 2 * (nel // 2 + 1), rng)
+    h = C.shape[1] // 2
+    p = np.stack([0.1 * (C[:, :h] @ C[:, h:].T + C[:, h:] @ C[:, :h].T)] * 2)
+    spc = np.stack([0.1 * C[:, (k % h):(k % h) + 1] @ C[:, h + (k % h):h + (k % h) + 1].T for k in range(6)]
+                   + [0.1 * C[:, :h] @ C[:, h:].T])
+    return d, p, spc
+
+
 def density_open(bas, nalpha, nbeta, seed, S=None):
     """Packed (2, ntri) alpha/beta densities."""
     if S is None:

@@ -51,7 +51,8 @@ def lib():
         L.orc_boys.argtypes = [ctypes.c_int, ctypes.c_double, _d]
         L.orc_grad2e_mrsf.restype = ctypes.c_longlong
         L.orc_grad2e_mrsf.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
-                                      _d, ctypes.c_int, ctypes.c_double, ctypes.c_int, _d]
+                                      _d, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      _d]
         L.orc_grad2e.restype = ctypes.c_longlong
         L.orc_grad2e.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                  ctypes.c_int, ctypes.c_int, ctypes.c_int, _d]
@@ -327,7 +328,7 @@ class Oracle:
         return de.reshape(-1, 3)
 
     def grad2e_mrsf(self, d, p, spc, hfscale, hfscale2, coulscale=1.0, spcscale=(1.0, 1.0, 1.0), mrst=1,
-                    cutoff=1e-10, nthreads=None):
+                    cutoff=1e-10, nthreads=None, stride=1, offset=0):
         """MRSF two-electron gradient (natom, 3) of grd2 with the two-particle
         density of grd2_mrsf_compute_data_t: d, p (2, nbf, nbf) raw alpha / beta
         SCF and relaxed difference densities, spc (7, nbf, nbf) the response
@@ -339,7 +340,7 @@ class Oracle:
         sc = np.asarray(spcscale, dtype=np.float64)
         de = np.zeros(3 * self.bas.natom)
         nq = lib().orc_grad2e_mrsf(self.h, _p(fd), _p(fp), _p(fs), hfscale, hfscale2, coulscale, _p(sc), int(mrst),
-                                   cutoff, nthreads or os.cpu_count(), _p(de))
+                                   cutoff, nthreads or os.cpu_count(), int(stride), int(offset), _p(de))
         self.last_grad2e_quartets = int(nq)
         return de.reshape(-1, 3)
 

@@ -464,10 +464,11 @@ long long orc_grad2e(void* h, const double* Dt, const double* Ds, double cj, dou
 // MRSF two-electron gradient (accumulated into de[3*natom]): d, p (nbf, nbf, 2)
 // the raw alpha / beta SCF and relaxed difference densities, spc (7, nbf, nbf)
 // the response densities, all Fortran column-major (the routec_grad2_mrsf
-// layout); spcscale = {spc_coco, spc_ovov, spc_coov}; mrst 1 or 3.
+// layout); spcscale = {spc_coco, spc_ovov, spc_coov}; mrst 1 or 3; stride /
+// offset as in orc_grad2e.
 long long orc_grad2e_mrsf(void* h, const double* d, const double* p, const double* spc, double hfscale,
                           double hfscale2, double coulscale, const double* spcscale, int mrst, double cutoff,
-                          int nthreads, double* de) {
+                          int nthreads, int stride, int offset, double* de) {
   const Basis& B = ((Handle*)h)->B;
   const int n = B.nbf;
   const size_t n2 = (size_t)n * n;
@@ -490,7 +491,7 @@ long long orc_grad2e_mrsf(void* h, const double* d, const double* p, const doubl
     make(4 + q, [&](int r, int c) { return spc[comp[q] + 7 * ((size_t)r + (size_t)n * c)]; });
   MrsfGamma G{M, CLy.nct, 4.0 * coulscale, hfscale, hfscale2, spcscale[0], spcscale[1], spcscale[2],
               mrst == 3 ? -1.0 : 1.0};
-  return grad2e_impl(h, CLy, G, cutoff, nthreads, 1, 0, de);
+  return grad2e_impl(h, CLy, G, cutoff, nthreads, stride, offset, de);
 }
 
 // One-electron gradient (accumulated into de[3*natom]): sum_uv D_uv dH_uv/dR
