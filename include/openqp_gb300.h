@@ -351,6 +351,15 @@ int oqpg_grad_stats(const oqpg_ctx* ctx, double* out, int n);
 int oqpg_grad2_mrsf(oqpg_ctx* ctx, const double* d, const double* p, const double* spc, double hfscale,
                     double hfscale2, double coulscale, const double* spcscale, int mrst, double* de);
 
+/* Two-electron SF-TDDFT gradient of grd2_sf_compute_data_t
+ * (source/modules/tdhf_sf_gradient.F90:277-502; the reference has no seam
+ * for it, a maintainer replaces the grd2_driver call of sf_2e_grad): d, p as
+ * in oqpg_grad2_mrsf, v (nbf, nbf) the spin-flip transition density (Fortran
+ * column-major, general); de(3, natom) accumulated.  The density is the MRSF
+ * one with ball = v and the spin-pair coupling terms off. */
+int oqpg_grad2_sf(oqpg_ctx* ctx, const double* d, const double* p, const double* v, double hfscale, double hfscale2,
+                  double coulscale, double* de);
+
 /* Response-type builds (single-molecule contexts; see routec_fock_td and
  * routec_fock_mrsf for the layouts and the reference routines).  Every
  * density is screened, evaluated and digested in one pass over the quartets:

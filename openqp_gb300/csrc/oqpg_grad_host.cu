@@ -486,6 +486,19 @@ int oqpg_grad2_mrsf(oqpg_ctx* ctx, const double* d, const double* p, const doubl
   return grad_mrsf(ctx, d, p, spc, hfscale, hfscale2, coulscale, spcscale, mrst, de);
 }
 
+int oqpg_grad2_sf(oqpg_ctx* ctx, const double* d, const double* p, const double* v, double hfscale, double hfscale2,
+                  double coulscale, double* de) {
+  if (!ctx) return NOT_INIT;
+  if (!d || !p || !v || !de) return UNSUPPORTED;
+  // grd2_sf_compute_data_t's density is the MRSF one with ball = v and every
+  // spin-pair coupling term off (modules/tdhf_sf_gradient.F90:423-502)
+  const size_t n = (size_t)ctx->nbf;
+  std::vector<double> spc(7 * n * n, 0.0);
+  for (size_t q = 0; q < n * n; ++q) spc[6 + 7 * q] = v[q];
+  const double zero[3] = {0.0, 0.0, 0.0};
+  return grad_mrsf(ctx, d, p, spc.data(), hfscale, hfscale2, coulscale, zero, 1, de);
+}
+
 int oqpg_grad_stats(const oqpg_ctx* ctx, double* out, int n) {
   if (!ctx) return NOT_INIT;
   for (int i = 0; i < n && i < 5; ++i) out[i] = ctx->grad_stats[i];

@@ -342,6 +342,22 @@ class FockBuilder:
             raise FockError(rc, "oqpg_grad2_mrsf")
         return de.reshape(-1, 3)
 
+    def grad2_sf(self, d, p, v, hfscale, hfscale2, coulscale=1.0):
+        """SF-TDDFT two-electron gradient (natom, 3) of OpenQP's
+        grd2_sf_compute_data_t (modules/tdhf_sf_gradient.F90:277-502): d, p
+        (2, nbf, nbf) raw alpha / beta densities, v (nbf, nbf) the transition
+        density, natural indexing."""
+        n = self.nbf
+        fd, fp = (np.ascontiguousarray(np.asarray(m, dtype=np.float64).reshape(2, n, n).transpose(0, 2, 1))
+                  for m in (d, p))
+        fv = np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(n, n).T)
+        de = np.zeros(3 * self.bas.natom)
+        rc = lib().oqpg_grad2_sf(self.h, ptr(fd), ptr(fp), ptr(fv), float(hfscale), float(hfscale2), float(coulscale),
+                                 ptr(de))
+        if rc != 0:
+            raise FockError(rc, "oqpg_grad2_sf")
+        return de.reshape(-1, 3)
+
     def grad_stats(self):
         s = np.zeros(5)
         lib().oqpg_grad_stats(self.h, ptr(s), 5)

@@ -269,3 +269,18 @@ def test_grad2_mrsf_seam_and_precision(gpu):
         assert info == 1
     finally:
         gpu.routec_finalize()
+
+
+def test_grad2_sf_matches_oracle(gpu, oracle_lib):
+    """grd2_sf_compute_data_t: the MRSF density with ball = v and no spin-pair
+    coupling terms (the oracle's literal MRSF restatement with those inputs is
+    the SF get_density term for term)."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(2, workloads.cube_edge_like_c1(2), seed=9, basis="cc-pvdz")
+    d, p, spc = _mrsf_inputs(bas, 7)
+    v = spc[0]
+    g = gpu.FockBuilder(bas).grad2_sf(d, p, v, 0.5, 0.45)
+    sp = np.zeros_like(spc)
+    sp[6] = v
+    ref = oracle_lib.Oracle(bas).grad2e_mrsf(d, p, sp, 0.5, 0.45, 1.0, (0.0, 0.0, 0.0), 1)
+    assert np.abs(g - ref).max() < 1e-9 * max(1.0, np.abs(ref).max())
