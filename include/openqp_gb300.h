@@ -351,6 +351,20 @@ int oqpg_grad_stats(const oqpg_ctx* ctx, double* out, int n);
 int oqpg_grad2_mrsf(oqpg_ctx* ctx, const double* d, const double* p, const double* spc, double hfscale,
                     double hfscale2, double coulscale, const double* spcscale, int mrst, double* de);
 
+/* CAM two-electron gradients: grd2_driver's CAM branch
+ * (source/integrals/grd2.F90:104-128).  Pass 1 uses the regular integrals
+ * with coulscale 1 and the alpha exchange scales.  Pass 2 uses erf(mu r)/r
+ * with coulscale 0, the beta scales, its own Schwarz bounds
+ * (grd2.F90:247-248) and the attenuated primitive screens
+ * (grd2_rys.F90:368-373).  de is accumulated.
+ * oqpg_grad2_cam: packed SCF densities as in oqpg_grad2 (nfocks 1 or 2).
+ * oqpg_grad2_mrsf_cam: the MRSF form with cam5 = {reference alpha,
+ * reference beta, response alpha, response beta, mu}; the spin-pair terms
+ * enter both passes, as in the reference. */
+int oqpg_grad2_cam(oqpg_ctx* ctx, const double* d, int nfocks, double alpha, double beta, double mu, double* de);
+int oqpg_grad2_mrsf_cam(oqpg_ctx* ctx, const double* d, const double* p, const double* spc, const double* cam5,
+                        const double* spcscale, int mrst, double* de);
+
 /* Two-electron SF-TDDFT gradient of grd2_sf_compute_data_t
  * (source/modules/tdhf_sf_gradient.F90:277-502; the reference has no seam
  * for it, a maintainer replaces the grd2_driver call of sf_2e_grad): d, p as

@@ -66,6 +66,9 @@ def lib():
                                           ctypes.c_double, _d]
         L.oqpg_grad2_mrsf.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                       _d, ctypes.c_int, _d]
+        L.oqpg_grad2_cam.argtypes = [ctypes.c_void_p, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, _d]
+        L.oqpg_grad2_mrsf_cam.argtypes = [ctypes.c_void_p, _d, _d, _d, _d, _d, ctypes.c_int, _d]
         L.oqpg_grad2_sf.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                     _d]
         L.routec_grad2_mrsf.argtypes = [_d, _d, _d, _d, _d, _i, _i, _d, _d, _d, _d, _i, _i]

@@ -67,6 +67,7 @@ struct GradArgs {
   int mrsf;
   const double* mm;
   double mcoul, mx, mx2, mq1, mq2, mq3;
+  double inv_mu2;           // erf(mu r)/r pass of the CAM gradient: 1/mu^2 (0: 1/r)
   double* de;               // 3 x natom, accumulated
   unsigned long long* counters;  // [0] primitive quartets evaluated, [1] quartets evaluated
   int ctas_per_sm;
@@ -219,8 +220,9 @@ __device__ __forceinline__ void quartet_setup(const GradArgs& g, uint2 qd, PairD
 }
 
 // Primitive-quartet screens of grd2_rys_compute (grd2_rys.F90:361-372),
-// (sp sq)^2 < dtol2 (p + q) and (sp sq)^2 dabmax^2 < dabcut2 (p + q), written
-// without the squares so that FP32 quartets do not underflow.
+// (sp sq)^2 < dtol2 s and (sp sq)^2 dabmax^2 < dabcut2 s with s = p + q (+ pq /
+// mu^2 in the attenuated pass), written without the squares so that FP32
+// quartets do not underflow.
 template <typename T>
 __device__ __forceinline__ bool grad_prim_skip(const GradArgs& g, T pfac, T dabmax, T s) {
   const T a = fabs(pfac), rs = sqrt(s);
@@ -268,10 +270,10 @@ __global__ void __launch_bounds__(128) k_grad_lane(const GradArgs g) {
       PP bp, kp;
       prim_load(prims + P.poff + kb, bp);
       prim_load(prims + Q.poff + kq, kp);
-      if (grad_prim_skip<T>(g, bp.sp * kp.sp, dabmax, bp.p + kp.p)) continue;
+      if (grad_prim_skip<T>(g, bp.sp * kp.sp, dabmax, fma(bp.p * kp.p, (T)g.inv_mu2, bp.p + kp.p))) continue;
       ++nprim;
       PrimQuartet<T> pqd;
-      prim_setup<T>(bp, kp, pqd);
+      prim_setup<T, true>(bp, kp, pqd, (T)g.inv_mu2);
       const T a2 = (T)2 * GAcc<T>::alpha(g, P.poff + kb);
       const T b2 = (T)2 * bp.p - a2;
       const T c2 = (T)2 * GAcc<T>::alpha(g, Q.poff + kq);
@@ -436,7 +438,8 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
           const int kq = cand / nP, kb = cand - kq * nP;
           const PP* b = prims + P.poff + kb;
           const PP* k = prims + Q.poff + kq;
-          keep = !grad_prim_skip<T>(g, __ldg(&b->sp) * __ldg(&k->sp), dabmax, __ldg(&b->p) + __ldg(&k->p));
+          const T pb = __ldg(&b->p), pk = __ldg(&k->p);
+          keep = !grad_prim_skip<T>(g, __ldg(&b->sp) * __ldg(&k->sp), dabmax, fma(pb * pk, (T)g.inv_mu2, pb + pk));
         }
       }
       unsigned mask = __ballot_sync(0xffffffffu, keep);
@@ -456,7 +459,7 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
           const int kq = myc / nP, kb = myc - kq * nP;
           prim_load(prims + P.poff + kb, bp);
           prim_load(prims + Q.poff + kq, kp);
-          prim_setup<T>(bp, kp, pqd);
+          prim_setup<T, true>(bp, kp, pqd, (T)g.inv_mu2);
           for (int q = gl; q < 2 * NR; q += 3 * RP) {  // groups of 3 lanes (one root per pass) loop
             const T v = rys_quantity<NR, T>(pqd.X, q, g.roots_f32 != 0);
             RTg[q] = (q & 1) ? v * pqd.pref : v;

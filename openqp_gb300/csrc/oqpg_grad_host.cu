@@ -217,12 +217,13 @@ struct GammaSpec {
   double cjb = 0, ckb = 0;
 };
 
-int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& gs, double cutoff, double* de);
+int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& gs, double cutoff, double* de,
+             double inv_mu2 = 0.0);
 
 // dE/dR (accumulated into de[3 natom]) for the two-particle density of the
 // full AO matrices x, y (and the spin pair xs, ys, both null or both set).
 int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, const double* ys, double cj,
-               double ckt, double cks, double cutoff, double* de) {
+               double ckt, double cks, double cutoff, double* de, double inv_mu2 = 0.0) {
   if (c->nmol != 1) return UNSUPPORTED;
   int rc;
   if ((rc = grad_init(c))) return rc;
@@ -237,10 +238,13 @@ int grad_build(oqpg_ctx* c, const double* x, const double* y, const double* xs, 
   gs.cj = cj; gs.ckt = ckt; gs.cks = cks;
   gs.cjb = std::fabs(cj);
   gs.ckb = std::fabs(ckt) + std::fabs(cks);
-  return grad_run(c, mats, nmat, gs, cutoff, de);
+  return grad_run(c, mats, nmat, gs, cutoff, de, inv_mu2);
 }
 
-int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& gs, double cutoff, double* de) {
+// inv_mu2 != 0: the erf-attenuated pass (its Schwarz bounds must be current:
+// ensure_att).
+int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& gs, double cutoff, double* de,
+             double inv_mu2) {
   int rc;
   cudaStream_t st = c->stream;
   const int nc = c->ncart, ns = c->nshell;
@@ -290,9 +294,10 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
   la.pair_ij = c->d_pair_ij.as<int2>();
   la.pair_type = c->d_pair_type.as<int>();
   la.gpairs = c->d_gpairs.as<PairDev>();
-  la.q = c->d_q.as<double>();
-  la.sorted_idx = c->d_sorted_idx.as<int>();
-  la.sorted_q = c->d_sorted_q.as<double>();
+  const bool att = inv_mu2 != 0.0;
+  la.q = (att ? c->d_q_att : c->d_q).as<double>();
+  la.sorted_idx = (att ? c->d_sorted_idx_att : c->d_sorted_idx).as<int>();
+  la.sorted_q = (att ? c->d_sorted_q_att : c->d_sorted_q).as<double>();
   la.dsh = c->d_dshg.as<double>();
   la.atom = c->d_atom.as<int>();
   la.cj = gs.cjb;
@@ -356,7 +361,8 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
   g.atom = c->d_atom.as<int>();
   g.cj = gs.cj; g.ckt = gs.ckt; g.cks = gs.cks;
   g.pure = c->pure ? 1 : 0;
-  g.q = c->d_q.as<double>();
+  g.q = (att ? c->d_q_att : c->d_q).as<double>();
+  g.inv_mu2 = inv_mu2;
   g.cutoff2 = 0.5 * cutoff;
   // grd2: dtol = 10^-20 and dabcut = 1e-11 (smaller for very tight exponents), both squared
   double zbig = 0;
@@ -426,7 +432,7 @@ int grad_packed(oqpg_ctx* c, const double* d, int nfocks, double hfscale, double
 // 341-355 init, :404-601 get_density): d, p (n, n, 2) raw alpha / beta,
 // spc (7, n, n), Fortran column-major.
 int grad_mrsf(oqpg_ctx* c, const double* d, const double* p, const double* spc, double hfscale, double hfscale2,
-              double coulscale, const double* spcscale, int mrst, double* de) {
+              double coulscale, const double* spcscale, int mrst, double* de, const double* cam5 = nullptr) {
   if (c->nmol != 1) return UNSUPPORTED;
   if (mrst != 1 && mrst != 3) return UNSUPPORTED;
   int rc;
@@ -459,7 +465,48 @@ int grad_mrsf(oqpg_ctx* c, const double* d, const double* p, const double* spc, 
   gs.cjb = 3.0 * std::fabs(gs.mcoul) + 32.0 * std::fabs(spcscale[2]);
   gs.ckb = 6.0 * std::fabs(hfscale) + 4.0 * std::fabs(hfscale2) + 4.0 * std::fabs(spcscale[0]) +
            4.0 * std::fabs(spcscale[1]) + 16.0 * std::fabs(spcscale[2]);
-  return grad_run(c, mats, 11, gs, c->tau, de);
+  if (!cam5) return grad_run(c, mats, 11, gs, c->tau, de);
+  // grd2_driver's CAM branch (grd2.F90:104-128): regular pass with the alphas,
+  // then the attenuated pass with the betas and no Coulomb; the spin-pair
+  // coupling terms enter both passes
+  if ((rc = ensure_att(c, cam5[4]))) return rc;
+  for (int pass = 0; pass < 2; ++pass) {
+    GammaSpec gp = gs;
+    gp.mcoul = pass ? 0.0 : 4.0;
+    gp.mx = pass ? cam5[1] : cam5[0];
+    gp.mx2 = pass ? cam5[3] : cam5[2];
+    gp.cjb = 3.0 * std::fabs(gp.mcoul) + 32.0 * std::fabs(spcscale[2]);
+    gp.ckb = 6.0 * std::fabs(gp.mx) + 4.0 * std::fabs(gp.mx2) + 4.0 * std::fabs(spcscale[0]) +
+             4.0 * std::fabs(spcscale[1]) + 16.0 * std::fabs(spcscale[2]);
+    if ((rc = grad_run(c, mats, 11, gp, c->tau, de, pass ? 1.0 / (cam5[4] * cam5[4]) : 0.0))) return rc;
+  }
+  return OK;
+}
+
+// grd2_driver's CAM branch for the SCF densities (packed, nfocks 1 or 2):
+// regular pass with coulscale 1 and hfscale alpha, erf(mu r)/r pass with
+// coulscale 0 and hfscale beta.
+int grad_cam(oqpg_ctx* c, const double* d, int nfocks, double alpha, double beta, double mu, double* de) {
+  if (nfocks != 1 && nfocks != 2) return UNSUPPORTED;
+  if (!(mu > 0.0)) return UNSUPPORTED;
+  int rc;
+  if ((rc = ensure_att(c, mu))) return rc;
+  const int n = c->nbf;
+  const size_t n2 = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
+  std::vector<double> Dt(n2), Ds;
+  unpack_full(d, n, Dt.data());
+  if (nfocks == 2) {
+    std::vector<double> Db(n2);
+    unpack_full(d + ntri, n, Db.data());
+    Ds.resize(n2);
+    for (size_t k = 0; k < n2; ++k) {
+      Ds[k] = Dt[k] - Db[k];
+      Dt[k] += Db[k];
+    }
+  }
+  const double* ds = nfocks == 2 ? Ds.data() : nullptr;
+  if ((rc = grad_build(c, Dt.data(), Dt.data(), ds, ds, 4.0, alpha, alpha, c->tau, de))) return rc;
+  return grad_build(c, Dt.data(), Dt.data(), ds, ds, 0.0, beta, beta, c->tau, de, 1.0 / (mu * mu));
 }
 
 }  // namespace
@@ -484,6 +531,19 @@ int oqpg_grad2_mrsf(oqpg_ctx* ctx, const double* d, const double* p, const doubl
   if (!ctx) return NOT_INIT;
   if (!d || !p || !spc || !spcscale || !de) return UNSUPPORTED;
   return grad_mrsf(ctx, d, p, spc, hfscale, hfscale2, coulscale, spcscale, mrst, de);
+}
+
+int oqpg_grad2_cam(oqpg_ctx* ctx, const double* d, int nfocks, double alpha, double beta, double mu, double* de) {
+  if (!ctx) return NOT_INIT;
+  if (!d || !de) return UNSUPPORTED;
+  return grad_cam(ctx, d, nfocks, alpha, beta, mu, de);
+}
+
+int oqpg_grad2_mrsf_cam(oqpg_ctx* ctx, const double* d, const double* p, const double* spc, const double* cam5,
+                        const double* spcscale, int mrst, double* de) {
+  if (!ctx) return NOT_INIT;
+  if (!d || !p || !spc || !cam5 || !spcscale || !de || !(cam5[4] > 0.0)) return UNSUPPORTED;
+  return grad_mrsf(ctx, d, p, spc, cam5[0], cam5[2], 1.0, spcscale, mrst, de, cam5);
 }
 
 int oqpg_grad2_sf(oqpg_ctx* ctx, const double* d, const double* p, const double* v, double hfscale, double hfscale2,

@@ -323,7 +323,18 @@ class FockBuilder:
             raise FockError(rc, "oqpg_grad2_bilinear")
         return de.reshape(-1, 3)
 
-    def grad2_mrsf(self, d, p, spc, hfscale, hfscale2, coulscale=1.0, spcscale=(1.0, 1.0, 1.0), mrst=1):
+    def grad2_cam(self, d, alpha, beta, mu):
+        """CAM two-electron gradient (natom, 3) of grd2_driver's CAM branch:
+        1/r pass with hfscale alpha, erf(mu r)/r pass with hfscale beta and no
+        Coulomb.  d as in grad2."""
+        d = np.ascontiguousarray(np.atleast_2d(d), dtype=np.float64)
+        de = np.zeros(3 * self.bas.natom)
+        rc = lib().oqpg_grad2_cam(self.h, ptr(d), d.shape[0], float(alpha), float(beta), float(mu), ptr(de))
+        if rc != 0:
+            raise FockError(rc, "oqpg_grad2_cam")
+        return de.reshape(-1, 3)
+
+    def grad2_mrsf(self, d, p, spc, hfscale, hfscale2, coulscale=1.0, spcscale=(1.0, 1.0, 1.0), mrst=1, cam=None):
         """MRSF two-electron gradient (natom, 3) of OpenQP's
         grd2_mrsf_compute_data_t (modules/tdhf_mrsf_gradient.F90:341-601).
         d, p: (2, nbf, nbf) raw alpha / beta SCF and relaxed difference
@@ -336,8 +347,12 @@ class FockBuilder:
         fs = np.ascontiguousarray(np.asarray(spc, dtype=np.float64).reshape(7, n, n).transpose(2, 1, 0))
         sc = np.asarray(spcscale, dtype=np.float64)
         de = np.zeros(3 * self.bas.natom)
-        rc = lib().oqpg_grad2_mrsf(self.h, ptr(fd), ptr(fp), ptr(fs), float(hfscale), float(hfscale2),
-                                   float(coulscale), ptr(sc), int(mrst), ptr(de))
+        if cam is not None:   # (reference alpha, reference beta, response alpha, response beta, mu)
+            c5 = np.asarray(cam, dtype=np.float64)
+            rc = lib().oqpg_grad2_mrsf_cam(self.h, ptr(fd), ptr(fp), ptr(fs), ptr(c5), ptr(sc), int(mrst), ptr(de))
+        else:
+            rc = lib().oqpg_grad2_mrsf(self.h, ptr(fd), ptr(fp), ptr(fs), float(hfscale), float(hfscale2),
+                                       float(coulscale), ptr(sc), int(mrst), ptr(de))
         if rc != 0:
             raise FockError(rc, "oqpg_grad2_mrsf")
         return de.reshape(-1, 3)

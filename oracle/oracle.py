@@ -52,7 +52,10 @@ def lib():
         L.orc_grad2e_mrsf.restype = ctypes.c_longlong
         L.orc_grad2e_mrsf.argtypes = [ctypes.c_void_p, _d, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                       _d, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                      _d]
+                                      _d, _d]
+        L.orc_grad2e_cam.restype = ctypes.c_longlong
+        L.orc_grad2e_cam.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_int, _d]
         L.orc_grad2e.restype = ctypes.c_longlong
         L.orc_grad2e.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                  ctypes.c_int, ctypes.c_int, ctypes.c_int, _d]
@@ -327,8 +330,19 @@ class Oracle:
         self.last_grad2e_quartets = int(nq)
         return de.reshape(-1, 3)
 
+    def grad2e_cam(self, dt, ds, alpha, beta, mu, cutoff=1e-10, nthreads=None):
+        """CAM two-electron gradient (natom, 3) of grd2_driver: regular pass with
+        hfscale alpha, erf(mu r)/r pass with hfscale beta and no Coulomb."""
+        n = self.nbf
+        dt = np.ascontiguousarray(dt, dtype=np.float64).reshape(n, n)
+        dsp = None if ds is None else np.ascontiguousarray(ds, dtype=np.float64).reshape(n, n)
+        de = np.zeros(3 * self.bas.natom)
+        lib().orc_grad2e_cam(self.h, _p(dt), None if dsp is None else _p(dsp), alpha, beta, mu, cutoff,
+                             nthreads or os.cpu_count(), _p(de))
+        return de.reshape(-1, 3)
+
     def grad2e_mrsf(self, d, p, spc, hfscale, hfscale2, coulscale=1.0, spcscale=(1.0, 1.0, 1.0), mrst=1,
-                    cutoff=1e-10, nthreads=None, stride=1, offset=0):
+                    cutoff=1e-10, nthreads=None, stride=1, offset=0, cam=None):
         """MRSF two-electron gradient (natom, 3) of grd2 with the two-particle
         density of grd2_mrsf_compute_data_t: d, p (2, nbf, nbf) raw alpha / beta
         SCF and relaxed difference densities, spc (7, nbf, nbf) the response
@@ -340,7 +354,8 @@ class Oracle:
         sc = np.asarray(spcscale, dtype=np.float64)
         de = np.zeros(3 * self.bas.natom)
         nq = lib().orc_grad2e_mrsf(self.h, _p(fd), _p(fp), _p(fs), hfscale, hfscale2, coulscale, _p(sc), int(mrst),
-                                   cutoff, nthreads or os.cpu_count(), int(stride), int(offset), _p(de))
+                                   cutoff, nthreads or os.cpu_count(), int(stride), int(offset), _p(de),
+                                   None if cam is None else _p(np.asarray(cam, dtype=np.float64)))
         self.last_grad2e_quartets = int(nq)
         return de.reshape(-1, 3)
 

@@ -32,6 +32,7 @@
 using namespace orc;
 
 extern "C" void orc_schwarz(void* h, double* q, int nthreads);
+extern "C" void orc_schwarz_att(void* h, double* q, int nthreads, double mu);
 
 namespace {
 
@@ -131,7 +132,10 @@ struct HermR {
 
 // Primitive ERI block over unnormalised Cartesian components (l <= 4 each),
 // out[((a*nb + b)*nc + c)*nd + d], without contraction coefficients.
-void prim_eri(const int l[4], const double* C[4], const double ex[4], std::vector<double>& out) {
+// inv_mu2 > 0: the erf(mu r)/r operator (Hermite exponent alpha -> alpha mu^2 /
+// (alpha + mu^2), prefactor x sqrt(mu^2 / (alpha + mu^2))).
+void prim_eri(const int l[4], const double* C[4], const double ex[4], std::vector<double>& out,
+              double inv_mu2 = 0.0) {
   const double a = ex[0], b = ex[1], c = ex[2], d = ex[3];
   const double p = a + b, q = c + d;
   double P[3], Q[3], ab2 = 0, cd2 = 0;
@@ -147,9 +151,14 @@ void prim_eri(const int l[4], const double* C[4], const double ex[4], std::vecto
     Ecd[k].build(l[2], l[3], q, Q[k] - C[2][k], Q[k] - C[3][k]);
   }
   HermR R;
-  R.build(l[0] + l[1] + l[2] + l[3], p * q / (p + q), P[0] - Q[0], P[1] - Q[1], P[2] - Q[2]);
-  const double pref = 2.0 * std::pow(PI, 2.5) / (p * q * std::sqrt(p + q)) * std::exp(-a * b / p * ab2) *
-                      std::exp(-c * d / q * cd2);
+  double alpha = p * q / (p + q), att = 1.0;
+  if (inv_mu2 > 0.0) {
+    att = 1.0 / (1.0 + alpha * inv_mu2);   // mu^2 / (alpha + mu^2)
+    alpha *= att;
+  }
+  R.build(l[0] + l[1] + l[2] + l[3], alpha, P[0] - Q[0], P[1] - Q[1], P[2] - Q[2]);
+  const double pref = 2.0 * std::pow(PI, 2.5) / (p * q * std::sqrt(p + q)) * std::sqrt(att) *
+                      std::exp(-a * b / p * ab2) * std::exp(-c * d / q * cd2);
   const int n[4] = {CL.n[l[0]], CL.n[l[1]], CL.n[l[2]], CL.n[l[3]]};
   out.assign((size_t)n[0] * n[1] * n[2] * n[3], 0.0);
   size_t idx = 0;
@@ -242,9 +251,12 @@ struct CartLayout {
 
 // grd2_driver_gen over the canonical shell quartets with the two-particle
 // density gamma_fn(ra, rb, rc, rd) of Cartesian-effective indices.
+// inv_mu2 > 0: the erf-attenuated pass of grd2_driver's CAM branch
+// (grd2.F90:117-128): attenuated Schwarz bounds (grd2.F90:247-248) and
+// ab = p + q + pq / mu^2 in the primitive screens (grd2_rys.F90:368-373).
 template <class GammaFn>
 long long grad2e_impl(void* h, const CartLayout& CLy, GammaFn gamma_fn, double cutoff, int nthreads, int stride,
-                      int offset, double* de) {
+                      int offset, double* de, double inv_mu2 = 0.0) {
   const Basis& B = ((Handle*)h)->B;
   const int ns = B.nshell;
   // grd2 pair cutoffs (grd2.F90:238-260): dabcut, 10^-20, 10^-20, 20 ln 10
@@ -258,7 +270,8 @@ long long grad2e_impl(void* h, const CartLayout& CLy, GammaFn gamma_fn, double c
   PairStore PS;
   PS.build(B, cut);
   std::vector<double> Q((size_t)ns * ns);
-  orc_schwarz(h, Q.data(), nthreads);
+  if (inv_mu2 > 0.0) orc_schwarz_att(h, Q.data(), nthreads, 1.0 / std::sqrt(inv_mu2));
+  else orc_schwarz(h, Q.data(), nthreads);
   const std::vector<int>& coff = CLy.coff;
   const bool pure = CLy.pure;
   const double dtol2 = dtol * dtol;
@@ -314,7 +327,7 @@ long long grad2e_impl(void* h, const CartLayout& CLy, GammaFn gamma_fn, double c
               for (int v = 0; v < PS.cnt[ij]; ++v) {
                 const double da = PS.k[pij + v] * PS.ginv[pij + v], db = PS.k[pkl + u] * PS.ginv[pkl + u];
                 const double aa = PS.g[pij + v], bb = PS.g[pkl + u];
-                const double pfac = da * db, test = pfac * pfac, s = aa + bb;
+                const double pfac = da * db, test = pfac * pfac, s = aa + bb + aa * bb * inv_mu2;
                 if (test < dtol2 * s) continue;
                 if (test * dabmax * dabmax < dabcut * dabcut * s) continue;  // gdat_init squares dabcut
                 // exponents of the four primitives, per caller shell (the pair store
@@ -337,8 +350,8 @@ long long grad2e_impl(void* h, const CartLayout& CLy, GammaFn gamma_fn, double c
                   int lp[4] = {lv[0], lv[1], lv[2], lv[3]}, lm[4] = {lv[0], lv[1], lv[2], lv[3]};
                   lp[ctr] += 1;
                   lm[ctr] -= 1;
-                  prim_eri(lp, Cn, xe, bp);
-                  if (lm[ctr] >= 0) prim_eri(lm, Cn, xe, bm);
+                  prim_eri(lp, Cn, xe, bp, inv_mu2);
+                  if (lm[ctr] >= 0) prim_eri(lm, Cn, xe, bm, inv_mu2);
                   int np[4] = {CL.n[lp[0]], CL.n[lp[1]], CL.n[lp[2]], CL.n[lp[3]]};
                   int nm[4] = {lm[0] >= 0 ? CL.n[lm[0]] : 0, lm[1] >= 0 ? CL.n[lm[1]] : 0,
                                lm[2] >= 0 ? CL.n[lm[2]] : 0, lm[3] >= 0 ? CL.n[lm[3]] : 0};
@@ -461,14 +474,43 @@ long long orc_grad2e(void* h, const double* Dt, const double* Ds, double cj, dou
   return grad2e_impl(h, CLy, gam, cutoff, nthreads, stride, offset, de);
 }
 
+// CAM form of orc_grad2e (grd2_driver, grd2.F90:104-128): pass 1 regular
+// integrals with coulscale 1 and hfscale alpha, pass 2 erf(mu r)/r with
+// coulscale 0 and hfscale beta, accumulated into de.
+long long orc_grad2e_cam(void* h, const double* Dt, const double* Ds, double alpha, double beta, double mu,
+                         double cutoff, int nthreads, double* de) {
+  const Basis& B = ((Handle*)h)->B;
+  const CartLayout CLy(B);
+  const int nct = CLy.nct;
+  std::vector<double> Dtc, Dsc;
+  cart_density(B, Dt, CLy.coff, nct, Dtc);
+  if (Ds) cart_density(B, Ds, CLy.coff, nct, Dsc);
+  const bool spin = Ds != nullptr;
+  long long nq = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    const double cj = pass ? 0.0 : 4.0, ck = pass ? beta : alpha;
+    auto gam = [&](size_t ra, size_t rb, size_t rc, size_t rd) {
+      auto M = [&](const std::vector<double>& X, size_t r, size_t s) { return X[r * nct + s]; };
+      double g = cj * M(Dtc, ra, rb) * M(Dtc, rc, rd) -
+                 ck * (M(Dtc, ra, rc) * M(Dtc, rb, rd) + M(Dtc, ra, rd) * M(Dtc, rb, rc));
+      if (spin) g -= ck * (M(Dsc, ra, rc) * M(Dsc, rb, rd) + M(Dsc, ra, rd) * M(Dsc, rb, rc));
+      return g;
+    };
+    nq += grad2e_impl(h, CLy, gam, cutoff, nthreads, 1, 0, de, pass ? 1.0 / (mu * mu) : 0.0);
+  }
+  return nq;
+}
+
 // MRSF two-electron gradient (accumulated into de[3*natom]): d, p (nbf, nbf, 2)
 // the raw alpha / beta SCF and relaxed difference densities, spc (7, nbf, nbf)
 // the response densities, all Fortran column-major (the routec_grad2_mrsf
 // layout); spcscale = {spc_coco, spc_ovov, spc_coov}; mrst 1 or 3; stride /
-// offset as in orc_grad2e.
+// offset as in orc_grad2e.  cam5 (or null) = {reference alpha, reference beta,
+// response alpha, response beta, mu}: the two passes of grd2_driver's CAM
+// branch (the hfscale / hfscale2 / coulscale arguments are then unused).
 long long orc_grad2e_mrsf(void* h, const double* d, const double* p, const double* spc, double hfscale,
                           double hfscale2, double coulscale, const double* spcscale, int mrst, double cutoff,
-                          int nthreads, int stride, int offset, double* de) {
+                          int nthreads, int stride, int offset, double* de, const double* cam5) {
   const Basis& B = ((Handle*)h)->B;
   const int n = B.nbf;
   const size_t n2 = (size_t)n * n;
@@ -491,6 +533,16 @@ long long orc_grad2e_mrsf(void* h, const double* d, const double* p, const doubl
     make(4 + q, [&](int r, int c) { return spc[comp[q] + 7 * ((size_t)r + (size_t)n * c)]; });
   MrsfGamma G{M, CLy.nct, 4.0 * coulscale, hfscale, hfscale2, spcscale[0], spcscale[1], spcscale[2],
               mrst == 3 ? -1.0 : 1.0};
+  if (cam5) {   // grd2_driver's CAM branch: pass 1 with the alphas, pass 2 attenuated with the betas
+    G.coulfact = 4.0;
+    G.xcfact = cam5[0];
+    G.xcfact2 = cam5[2];
+    long long nq = grad2e_impl(h, CLy, G, cutoff, nthreads, stride, offset, de);
+    G.coulfact = 0.0;
+    G.xcfact = cam5[1];
+    G.xcfact2 = cam5[3];
+    return nq + grad2e_impl(h, CLy, G, cutoff, nthreads, stride, offset, de, 1.0 / (cam5[4] * cam5[4]));
+  }
   return grad2e_impl(h, CLy, G, cutoff, nthreads, stride, offset, de);
 }
 

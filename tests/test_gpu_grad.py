@@ -284,3 +284,31 @@ def test_grad2_sf_matches_oracle(gpu, oracle_lib):
     sp[6] = v
     ref = oracle_lib.Oracle(bas).grad2e_mrsf(d, p, sp, 0.5, 0.45, 1.0, (0.0, 0.0, 0.0), 1)
     assert np.abs(g - ref).max() < 1e-9 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("nw,basis", [(2, "6-31g(d)"), (2, "cc-pvdz")])
+def test_grad2_cam_matches_oracle(gpu, oracle_lib, nw, basis):
+    """grd2_driver's CAM branch: 1/r pass (alpha) + erf(mu r)/r pass (beta, no
+    Coulomb) with its own Schwarz bounds, RHF and UHF; then the MRSF CAM form;
+    a plain gradient on the same context afterwards is unaffected."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(nw, workloads.cube_edge_like_c1(nw), seed=11, basis=basis)
+    n = bas.nbf
+    fb = gpu.FockBuilder(bas)
+    o = oracle_lib.Oracle(bas)
+    cam = (0.19, 0.46, 0.33)
+    d = workloads.density(bas, 5 * nw, 1)
+    g = fb.grad2_cam(d, *cam)
+    ref = o.grad2e_cam(_full(d, n), None, *cam)
+    assert np.abs(g - ref).max() < 1e-9 * max(1.0, np.abs(ref).max())
+    du = workloads.density_open(bas, 5 * nw + 1, 5 * nw - 1, 2)
+    Da, Db = _full(du[0], n), _full(du[1], n)
+    g = fb.grad2_cam(du, *cam)
+    ref = o.grad2e_cam(Da + Db, Da - Db, *cam)
+    assert np.abs(g - ref).max() < 1e-9 * max(1.0, np.abs(ref).max())
+    dm, p, spc = _mrsf_inputs(bas, 3)
+    c5 = (0.19, 0.46, 0.25, 0.5, 0.33)
+    g = fb.grad2_mrsf(dm, p, spc, 0.0, 0.0, spcscale=(0.4, 0.3, 0.2), mrst=1, cam=c5)
+    ref = o.grad2e_mrsf(dm, p, spc, 0.0, 0.0, 1.0, (0.4, 0.3, 0.2), 1, cam=c5)
+    assert np.abs(g - ref).max() < 1e-9 * max(1.0, np.abs(ref).max())
+    assert np.abs(fb.grad2(d) - o.grad2e(_full(d, n))).max() < 1e-9

@@ -238,6 +238,34 @@ def test_grad2e_mrsf_matches_finite_difference(oracle_lib, mrst):
     assert np.abs(g.sum(axis=0)).max() < 1e-9
 
 
+def test_grad2e_cam_matches_finite_difference(oracle_lib):
+    """grd2_driver's CAM branch (regular pass with hfscale alpha, erf(mu r)/r
+    pass with hfscale beta and no Coulomb, its own Schwarz bounds and the
+    attenuated primitive screens) against central differences of E2 =
+    1/2 Tr D G_CAM(D) from the pinned CAM Fock build."""
+    from openqp_gb300 import workloads
+    from openqp_gb300.basis import unpack
+    bas = workloads.water_cluster_basis(2, 4.0, seed=3, basis="6-31g*")
+    d = workloads.density(bas, 10, 3)
+    n = bas.nbf
+    D = unpack(d, n)
+    cam = (0.19, 0.46, 0.33)
+    g = oracle_lib.Oracle(bas).grad2e_cam(D, None, *cam)
+
+    def e2(xyz):
+        f = oracle_lib.Oracle(bas.with_geometry(xyz)).fock_jk_cam(d, *cam)[0]
+        return 0.5 * np.sum(D * unpack(f, n))
+
+    h = 1e-4
+    for at, x in ((0, 2), (1, 0), (4, 1)):
+        xp = bas.xyz.copy()
+        xp[at, x] += h
+        xm = bas.xyz.copy()
+        xm[at, x] -= h
+        fd = (e2(xp) - e2(xm)) / (2 * h)
+        assert abs(fd - g[at, x]) < 2e-7, (at, x, fd, g[at, x])
+
+
 def _dense_jk(o, n):
     eri = o.eri_dense().reshape(n, n, n, n)
     return (lambda D: np.einsum("ijkl,kl->ij", eri, D)), (lambda D: np.einsum("ijkl,jl->ik", eri, D))
