@@ -988,6 +988,16 @@ def run_grad(args):
              "speedup_vs_fp64": sum(times) / sum(tm), "max_abs_grad_error_Eh_bohr": float(np.abs(gm - g).max()),
              "f32_quartet_fraction": stm["f32_quartets_listed"] / max(1, stm["quartets_listed"])}
     fb.set_precision("fp64")
+    # the CAM gradient (grd2_driver's two-pass branch, CAM-B3LYP's alpha, beta, mu) of the same density
+    fb.grad2_cam(d, 0.19, 0.46, 0.33)
+    tc = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fb.grad2_cam(d, 0.19, 0.46, 0.33)
+        tc.append(time.perf_counter() - t0)
+    cam_line = {"alpha": 0.19, "beta": 0.46, "mu": 0.33, "grad_evals_per_s": args.steps / sum(tc)}
     line = {"metric": "two-electron gradient evaluations/s", "value": value, "unit": "grad evals/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(times) / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -998,7 +1008,7 @@ def run_grad(args):
                     "d2h_bytes_per_step": int(8 * 3 * bas.natom)},
             "grad_stats": st, "quartets_per_s": st["quartets"] / (sum(times) / args.steps),
             "prim_quartets_per_s": st["prim_quartets"] / (sum(times) / args.steps),
-            "fp64_peak_tflops": fp64_peak_tflops(), "clocks": clocks, "precision_split": split,
+            "fp64_peak_tflops": fp64_peak_tflops(), "clocks": clocks, "precision_split": split, "cam": cam_line,
             "max_abs_grad": float(np.abs(g).max()), "sum_grad": float(np.abs(g.sum(axis=0)).max())}
     if not args.no_cpu and rank == 0:
         line["cpu_baseline"] = cpu_baseline_grad(bas, d, args.cpu_budget)
