@@ -36,8 +36,11 @@ sys.path.insert(0, ROOT)
 
 WORKLOADS = {
     # the headline workload (the metric's configuration)
+    # traffic: DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per build of a class's
+    # launches (k_prim head + k_small), from one-pass ncu captures of this workload's bench command
     "water32_ccpvdz": dict(name="(H2O)32 cc-pVDZ spherical RHF J+K Fock build", nwater=32, edge=14.0, seed=0,
-                           basis="cc-pvdz", cutoff=1e-10),
+                           basis="cc-pvdz", cutoff=1e-10,
+                           traffic={"(ss|sp)": 300.9e6, "(ss|ss)": 171.8e6, "(sp|sp)": 139.7e6}),
     # the plain-FP64 parity configuration
     "water4_631gd": dict(name="(H2O)4 6-31G(d) Cartesian RHF J+K Fock build", nwater=4, edge=6.0, seed=0,
                          basis="6-31g(d)", cutoff=1e-10),
@@ -839,7 +842,9 @@ def run_ours(args):
                 "e2e": {"value": e2e, "unit": "builds/s", "h2d_bytes_per_step": int(8 * ntri),
                         "d2h_bytes_per_step": int(8 * ntri)},
                 "roofline": {"bound": "fp64", "kernel": labels[cdom], "achieved": achieved, "peak": peak,
-                             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                             "unit": "TFLOP/s", "frac": achieved / peak,
+                             "traffic": WORKLOAD.get("traffic", {}).get(labels[cdom]),
+                             "traffic_unit": "DRAM bytes per build of the class (ncu)",
                              "peak_source": "measured: FP64 FMA-chain probe on this device",
                              "kernel_ms": float(ms[cdom]), "build_fp64_tflops": total_flops / (tsum / args.steps) / 1e12},
                 "quartets_per_s": s0["quartets"] / (tsum / args.steps),
