@@ -76,6 +76,41 @@ __device__ __forceinline__ double rys_eval(const double* table, double X, int q)
   return v;
 }
 
+// Node u and weight w of root r together (FP64): one range test for both, and
+// above the table both come from one reciprocal square root y = X^-1/2
+// (u = R2_r y^2, w = W_r y) instead of a reciprocal and a reciprocal square root.
+template <int N, int NCOEF>
+__device__ __forceinline__ void rys_eval_uw(const double* table, double X, int r, double& u, double& w) {
+  const long long xb = __double_as_longlong(X);
+  if (xb >= __double_as_longlong((double)rys_xmax(N))) {
+    const int i = (N * (N - 1)) / 2 + r;
+    const double y = rsqrt64(X);
+    u = RYS_HERM_R2[i] * (y * y);
+    w = RYS_HERM_W[i] * y;
+    return;
+  }
+  int k;
+  double s;
+  if (xb < __double_as_longlong((double)RYS_X_SPLIT)) {
+    k = __double2int_rz(X * (double)RYS_LO_PER_UNIT);
+    s = fma(2.0 * RYS_LO_PER_UNIT, X, -(double)(2 * k + 1));
+  } else {
+    const int f = __double2int_rz(X);
+    k = RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
+    s = fma(2.0, X, -(double)(2 * f + 1));
+  }
+  // node coefficients at c, weight coefficients at c + NCOEF
+  const double* c = table + rys_offset(N, NCOEF) + (k * 2 * N + 2 * r) * NCOEF;
+  double vu = __ldg(c + NCOEF - 1), vw = __ldg(c + 2 * NCOEF - 1);
+#pragma unroll
+  for (int i = NCOEF - 2; i >= 0; --i) {
+    vu = fma(vu, s, __ldg(c + i));
+    vw = fma(vw, s, __ldg(c + NCOEF + i));
+  }
+  u = vu;
+  w = vw;
+}
+
 // FP32 variant of the same evaluation (the degree-4 table rounded to FP32),
 // for the FP32 quartets when the split is asked to keep no FP64 at all.
 template <int N>
@@ -141,6 +176,17 @@ __device__ __forceinline__ T rys_quantity(T X, int q, bool roots_f32 = false) {
   else {
     if (roots_f32) return rys_eval_f32<N>(X, q);
     return (float)rys_eval<N, RYS_NCOEF_F32>(RYS_TABLE_F32, (double)X, q);
+  }
+}
+
+// Node and weight of root r (the pair that a thread-per-quartet loop needs).
+template <int N, typename T>
+__device__ __forceinline__ void rys_node_weight(T X, int r, bool roots_f32, T& u, T& w) {
+  if constexpr (std::is_same<T, double>::value) {
+    rys_eval_uw<N, RYS_NCOEF>(RYS_TABLE, X, r, u, w);
+  } else {
+    u = rys_quantity<N, T>(X, 2 * r, roots_f32);
+    w = rys_quantity<N, T>(X, 2 * r + 1, roots_f32);
   }
 }
 
@@ -505,8 +551,9 @@ __device__ __forceinline__ void small_prims_impl(const BuildArgs& a, const PairD
     ++nprim;
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
-      const T u = rys_quantity<NR, T>(pq.X, 2 * r, a.roots_f32 != 0);
-      const T w = rys_quantity<NR, T>(pq.X, 2 * r + 1, a.roots_f32 != 0) * pq.pref;
+      T u, w;
+      rys_node_weight<NR, T>(pq.X, r, a.roots_f32 != 0, u, w);
+      w *= pq.pref;
       const T uq = u * pq.qi, up = u * pq.pi;
       const T b00 = (T)0.5 * pq.inv * u;
       const T b10 = fma(-bp.hp, uq, bp.hp);

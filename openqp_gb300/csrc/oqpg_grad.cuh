@@ -279,8 +279,9 @@ __global__ void __launch_bounds__(128) k_grad_lane(const GradArgs g) {
       const T c2 = (T)2 * GAcc<T>::alpha(g, Q.poff + kq);
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
-        const T u = rys_quantity<NR, T>(pqd.X, 2 * r, g.roots_f32 != 0);
-        const T w = rys_quantity<NR, T>(pqd.X, 2 * r + 1, g.roots_f32 != 0) * pqd.pref;
+        T u, w;
+        rys_node_weight<NR, T>(pqd.X, r, g.roots_f32 != 0, u, w);
+        w *= pqd.pref;
         const T uq = u * pqd.qi, up = u * pqd.pi;
         const T b00 = (T)0.5 * pqd.inv * u;
         const T b10 = fma(-bp.hp, uq, bp.hp);
