@@ -56,8 +56,11 @@ template <int N, int NCOEF>
 __device__ __forceinline__ double rys_eval(const double* table, double X, int q) {
   const long long xb = __double_as_longlong(X);
   if (xb >= __double_as_longlong((double)rys_xmax(N))) {
+    // nodes R2 / X and weights W / sqrt(X) from one reciprocal square root, so
+    // lanes that evaluate nodes and lanes that evaluate weights take one path
     const int r = (N * (N - 1)) / 2 + (q >> 1);
-    return (q & 1) ? RYS_HERM_W[r] * rsqrt64(X) : RYS_HERM_R2[r] * rcp64(X);
+    const double y = rsqrt64(X);
+    return (q & 1) ? RYS_HERM_W[r] * y : RYS_HERM_R2[r] * (y * y);
   }
   int k;
   double s;
