@@ -146,7 +146,9 @@ __device__ __forceinline__ dfl rys_eval_df(dfl X, int q) {
   if (X.hi >= (float)rys_xmax(N)) {
     const int r = (N * (N - 1)) / 2 + (q >> 1);
     const float2 c = RYS_HERM_W_DF[r], c2 = RYS_HERM_R2_DF[r];
-    return (q & 1) ? dfl(c.x, c.y) * df_rsqrt(X) : dfl(c2.x, c2.y) * df_rcp(X);
+    // one reciprocal square root for nodes and weights (one path for all lanes)
+    const dfl y = df_rsqrt(X);
+    return (q & 1) ? dfl(c.x, c.y) * y : dfl(c2.x, c2.y) * (y * y);
   }
   int k;
   dfl s;
@@ -169,6 +171,42 @@ __device__ __forceinline__ dfl rys_eval_df(dfl X, int q) {
   return v;
 }
 
+// Node u and weight w of root r together in double-float (the FP64 joint
+// evaluation's structure: one range test, one reciprocal square root above the table).
+template <int N>
+__device__ __forceinline__ void rys_eval_uw_df(dfl X, int r, dfl& u, dfl& w) {
+  if (X.hi >= (float)rys_xmax(N)) {
+    const int i = (N * (N - 1)) / 2 + r;
+    const float2 c = RYS_HERM_W_DF[i], c2 = RYS_HERM_R2_DF[i];
+    const dfl y = df_rsqrt(X);
+    u = dfl(c2.x, c2.y) * (y * y);
+    w = dfl(c.x, c.y) * y;
+    return;
+  }
+  int k;
+  dfl s;
+  if (X.hi < (float)RYS_X_SPLIT) {
+    k = min(__float2int_rz(X.hi * (float)RYS_LO_PER_UNIT), RYS_X_SPLIT * RYS_LO_PER_UNIT - 1);
+    s = dfl(X.hi * (2.0f * RYS_LO_PER_UNIT), X.lo * (2.0f * RYS_LO_PER_UNIT)) + dfl(-(2 * k + 1));
+  } else {
+    const int f = min(__float2int_rz(X.hi), rys_xmax(N) - 1);
+    k = RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
+    s = dfl(X.hi * 2.0f, X.lo * 2.0f) + dfl(-(2 * f + 1));
+  }
+  const float2* c = RYS_TABLE_DF + rys_offset(N, RYS_NCOEF) + (k * 2 * N + 2 * r) * RYS_NCOEF;
+  float2 tu = __ldg(c + RYS_NCOEF - 1), tw = __ldg(c + 2 * RYS_NCOEF - 1);
+  dfl vu(tu.x, tu.y), vw(tw.x, tw.y);
+#pragma unroll
+  for (int i = RYS_NCOEF - 2; i >= 0; --i) {
+    tu = __ldg(c + i);
+    tw = __ldg(c + RYS_NCOEF + i);
+    vu = fma(vu, s, dfl(tu.x, tu.y));
+    vw = fma(vw, s, dfl(tw.x, tw.y));
+  }
+  u = vu;
+  w = vw;
+}
+
 // FP64 kernels: the degree-7 FP64 tables.  FP32 kernels: the degree-4 tables,
 // evaluated in FP64 (default) or, with roots_f32, in FP32.  Double-float
 // kernels: the degree-7 table in double-float.
@@ -187,6 +225,8 @@ template <int N, typename T>
 __device__ __forceinline__ void rys_node_weight(T X, int r, bool roots_f32, T& u, T& w) {
   if constexpr (std::is_same<T, double>::value) {
     rys_eval_uw<N, RYS_NCOEF>(RYS_TABLE, X, r, u, w);
+  } else if constexpr (std::is_same<T, dfl>::value) {
+    rys_eval_uw_df<N>(X, r, u, w);
   } else {
     u = rys_quantity<N, T>(X, 2 * r, roots_f32);
     w = rys_quantity<N, T>(X, 2 * r + 1, roots_f32);
