@@ -77,6 +77,15 @@ void routec_fock_jk_batch(const double* d, double* f, const int* nmol, const int
  * (see oqpg_set_precision).  No counterpart in the reference seam. */
 int routec_fock_set_precision(int mode, double threshold);
 
+/* Run-time two-electron cutoff of the following builds on the process-global
+ * context (oqpg_set_cutoff).  Replaces int2_compute_t_set_cutoff
+ * (source/integrals/int2.F90:480-496): the progressive-screening SCF changes
+ * infos%control%int2e_cutoff before every build (source/scf.F90:721-734) and
+ * fock_jk re-reads it (int2.F90:271).  *cutoff > 0; *info = 0, 1 (not
+ * initialised) or 3 (not a positive finite cutoff).  By reference, Fortran
+ * style. */
+void routec_fock_set_cutoff(const double* cutoff, int* info);
+
 /* The reference's 2e-gradient seam (source/modules/routec_bridge.F90:51-61,
  * 241, 292-310; caller source/modules/hf_gradient.F90:270-289): d is the
  * packed total RHF density, xyz(3, natm) in Bohr must be the geometry
@@ -231,19 +240,31 @@ int oqpg_fock_jk(oqpg_ctx* ctx, const double* d, double* f, int nfocks, double s
 int oqpg_fock_jk_device(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, double se,
                         double sc, void* stream);
 
-/* The same build as oqpg_fock_jk_device for callers that cannot allocate
- * device memory while they build Fock matrices (a host whose own pool
- * allocator owns all device memory, or a loop that cannot take the device
- * synchronisation of cudaMalloc/cudaFree).  It calls no cudaMalloc, cudaFree
- * or other allocating routine: every per-build buffer lives in one static
- * 24 MiB device array that each GPU loading the library holds until exit.
- * Limits: nbf <= 128, nshell <= 128, at most ~1.5 million screened quartets;
- * larger inputs return 5 before any kernel runs.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) with that device
- * current, so make that first call before any stream capture.  All calls share
- * the array and each clears what must start at zero; calls that overlap on the
- * GPU race on it.  The context itself (read-only tables) comes from
- * oqpg_create.  There is no counterpart of this entry point in the reference. */
+/* A plain-FP64 build of the packed densities on device buffers (as
+ * oqpg_fock_jk_device in precision mode 0 with the built-in launch defaults)
+ * for callers that cannot allocate device memory while they build Fock
+ * matrices (a host whose own pool allocator owns all device memory, or a loop
+ * that cannot take the device synchronisation of cudaMalloc/cudaFree).  It
+ * calls no cudaMalloc, cudaFree or other allocating routine: every per-build
+ * buffer lives in one static 24 MiB device array that each GPU loading the
+ * library holds until exit.  It follows the context's cutoff
+ * (oqpg_set_cutoff) but ignores its precision split and tuning
+ * (oqpg_set_precision, oqpg_set_tuning): it always builds in FP64.
+ * Limits: nbf <= 128 and nshell <= 128 (checked before any kernel runs), and
+ * as many screened quartets as the rest of the array holds (two 8-byte
+ * entries each, about 1.5 million at nbf = 128), which is known only after
+ * the screening pass: those two limits return 5 with f_device untouched.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; under lazy module loading
+ * (CUDA_MODULE_LOADING=LAZY, the default) that lookup may also load the
+ * module and reserve the static array at that moment, so make the first call
+ * before any stream capture and before a pool allocator claims the remaining
+ * device memory.  All calls share the array and each clears what must start at
+ * zero; calls that overlap on the GPU race on it.  A failing launch or copy
+ * waits for the work already queued on the stream before it returns 4, so no
+ * kernel of the failed call still uses the array.  The context itself
+ * (read-only tables) comes from oqpg_create.  There is no counterpart of this
+ * entry point in the reference. */
 int oqpg_fock_jk_noalloc(oqpg_ctx* ctx, const double* d_device, double* f_device, int nfocks, double se,
                          double sc, void* stream);
 
@@ -292,6 +313,18 @@ int oqpg_schwarz(const oqpg_ctx* ctx, double* q);
  * 1, 2 and 4 with FP32 below the threshold and FP64 above it.  No counterpart
  * in the reference. */
 int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold);
+
+/* Cutoff tau of the following Fock-type builds: the quartet screen (tau), the
+ * primitive-quartet screen (1e-4 tau squared against p + q), the primitive
+ * pair screen (1e-4 tau) and the element cutoff (tau), as
+ * int2_compute_t_set_cutoff (source/integrals/int2.F90:480-496) sets them; the
+ * exponent cutoff (25 ln 10) and the Schwarz bounds do not change.  A cutoff
+ * at or above the one the context was created with only shortens the
+ * primitive-pair ranges; a tighter one rebuilds the pair tables.  Returns 0, 1
+ * (null context) or 3 (not a positive finite cutoff).  oqpg_get_cutoff returns
+ * the current cutoff (-1 for a null context). */
+int oqpg_set_cutoff(oqpg_ctx* ctx, double cutoff);
+double oqpg_get_cutoff(const oqpg_ctx* ctx);
 
 /* Statistics of the last build, up to n (<= 175) doubles:
  * [0] quartets computed, [1] primitive quartets, [2] list build ms,
@@ -423,6 +456,14 @@ int oqpg_class_l(int c, int* l4);
 /* FP64 FMA throughput of the current device (TFLOP/s, FMA = 2 flops) from an
  * FMA-chain probe kernel; the denominator of the kernels' FP64 roofline. */
 int oqpg_measure_fp64_peak(int iters, double* tflops);
+
+/* Accuracy check of the kernels' own arithmetic: for n FP64 arguments
+ * x_device[i] (device memory; the kernels' range, positive normal numbers
+ * with 2^-126 <= x < 2^128) writes out_device[6 i + 0 .. 5] = the library's
+ * FP64 1/sqrt(x), CUDA's rsqrt(x), the library's FP64 1/x, IEEE 1.0 / x, and
+ * the double-float 1/sqrt(x) and 1/x of the df precision mode (as FP64).
+ * Synchronises the device.  No counterpart in the reference. */
+int oqpg_math_check(const double* x_device, double* out_device, long long n);
 
 #ifdef __cplusplus
 }

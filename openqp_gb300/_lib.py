@@ -42,8 +42,14 @@ def lib():
         L.oqpg_stats.argtypes = [ctypes.c_void_p, _d, ctypes.c_int]
         L.oqpg_class_l.argtypes = [ctypes.c_int, _i]
         L.oqpg_measure_fp64_peak.argtypes = [ctypes.c_int, _d]
+        L.oqpg_math_check.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]
         L.oqpg_set_precision.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
         L.routec_fock_set_precision.argtypes = [ctypes.c_int, ctypes.c_double]
+        L.oqpg_set_cutoff.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.oqpg_get_cutoff.argtypes = [ctypes.c_void_p]
+        L.oqpg_get_cutoff.restype = ctypes.c_double
+        L.routec_fock_set_cutoff.argtypes = [_d, _i]
+        L.routec_fock_set_cutoff.restype = None
         L.routec_fock_init.argtypes = [ctypes.c_int, _i, _i, _i, _d, _d, _i, ctypes.c_int, _d, ctypes.c_double]
         L.routec_fock_jk.argtypes = [_d, _d, _i, _i, _d, _d, _i]
         L.routec_fock_jk.restype = None

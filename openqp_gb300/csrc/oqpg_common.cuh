@@ -24,7 +24,8 @@ struct PrimPair {
   double p;      // exponent sum
   double hp;     // 0.5 / p
   double px, py, pz;     // Gaussian product centre
-  double ax, ay, az;     // P - A (A: first shell of the pair in kernel orientation)
+  double ax, ay, az;     // P - A (A: first shell of the pair in kernel orientation); in the
+                         // Fock tables P - B when A is an s shell (the recursion then runs on B)
   double sp;     // K / p with K = sqrt(2) pi^(5/4) c_a c_b exp(-a b |AB|^2 / p)
   float spf, pf; // FP32 copies of sp and p for the primitive-quartet pre-screen
 };
@@ -108,8 +109,9 @@ __host__ __device__ constexpr double cart_norm(int l, int idx) {
                               : 1.0;
 }
 
-// FP64 reciprocal / reciprocal square root: hardware approximation refined by
-// two Newton steps (4 FP64 FMA for 1/x, 6 for 1/sqrt(x)); exact to ~1 ulp.
+// FP64 reciprocal: the hardware approximation rcp.approx.ftz.f64 refined by
+// two Newton-Raphson steps for f(r) = 1/r - x (r <- r + r (1 - x r)), each
+// doubling the correct bits; 4 FP64 FMA, about 1 ulp.
 __device__ __forceinline__ double rcp64(double x) {
   double r;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
@@ -118,14 +120,31 @@ __device__ __forceinline__ double rcp64(double x) {
   e = fma(-x, r, 1.0);
   return fma(r, e, r);
 }
+
+// FP64 1/sqrt(x) for a positive normal x with 2^-126 <= x < 2^128 (every
+// argument of the integral kernels: exponent sums p + q and Rys arguments X).
+// Seed: y0 = rsqrtf(x'), x' = x truncated to FP32 (same exponent, leading 23
+// mantissa bits), so y0 is within 2^-21 of 1/sqrt(x) (rsqrtf: at most 2 ulp).
+// One third-order step of the binomial series
+//   1/sqrt(x) = y0 (1 - t)^(-1/2) = y0 (1 + t/2 + 3 t^2 / 8 + 5 t^3 / 16 + ...),
+//   t = 1 - x y0^2
+// (Householder's method of order 3 for x^(-1/2)), truncated after t^2: the
+// dropped terms are below 2^-60 relative, so the result is within about one
+// ulp.  The FP64 <-> FP32 conversions are integer bit operations, so the
+// whole evaluation costs 5 FP64 instructions (2 DMUL, 3 DFMA).
 __device__ __forceinline__ double rsqrt64(double x) {
-  double y;
-  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  const double hx = 0.5 * x;
-  double t = fma(-hx * y, y, 0.5);
-  y = fma(y, t, y);
-  t = fma(-hx * y, y, 0.5);
-  return fma(y, t, y);
+  const int hi = __double2hiint(x);
+  const unsigned lo = (unsigned)__double2loint(x);
+  // FP32 bits: exponent rebased by 1023 - 127 = 896, mantissa truncated
+  const float xf = __uint_as_float(((unsigned)(hi - (896 << 20)) << 3) | (lo >> 29));
+  const unsigned yb = __float_as_uint(rsqrtf(xf));
+  // back to FP64 bits (y0 is a positive normal FP32 number)
+  const double y0 = __hiloint2double((int)((((yb >> 23) + 896u) << 20) | ((yb & 0x7fffffu) >> 3)),
+                                     (int)((yb & 7u) << 29));
+  const double xy = x * y0;
+  const double t = fma(-xy, y0, 1.0);
+  const double a = fma(t, 0.375, 0.5);
+  return fma(t * y0, a, y0);
 }
 
 }  // namespace oqpg

@@ -48,10 +48,30 @@ __host__ __device__ constexpr int rys_offset(int n, int ncoef) {  // start of th
   return n <= 1 ? 0 : rys_offset(n - 1, ncoef) + rys_nint(n - 1) * 2 * (n - 1) * ncoef;
 }
 
+// Interval k of the table at X >= 0 and the Chebyshev variable s in [-1, 1]:
+// width 1/4 below 32 (k = floor(4X), s = 8X - (2k+1)), unit width above
+// (f = floor(X), k = 128 + f - 32, s = 2X - (2f+1)).  The floors and the
+// constant 2k+1 come from the bits of X with integer instructions, so the
+// only FP64 instruction is the FMA that forms s.
+static_assert(RYS_LO_PER_UNIT == 4, "interval arithmetic below assumes quarter-unit intervals under the split");
+__device__ __forceinline__ int rys_interval(long long xb, double X, double& s) {
+  const bool lo = xb < __double_as_longlong((double)RYS_X_SPLIT);
+  // floor(X 2^a), a = 2 below the split, 0 above (X < 2^30)
+  const int e = (int)(xb >> 52) - 1023 + (lo ? 2 : 0);
+  const long long m = (xb & 0xfffffffffffffll) | 0x10000000000000ll;
+  const int f = (int)(m >> (e < 0 ? 63 : 52 - e));
+  // -(2f + 1) as a double: odd integer v < 2^21, exponent from its leading bit
+  const unsigned v = 2u * (unsigned)f + 1u;
+  const int ev = 31 - __clz(v);
+  const double c = __longlong_as_double((long long)((1ull << 63) | ((unsigned long long)(1023 + ev) << 52) |
+                                                    (((unsigned long long)v << (52 - ev)) & 0xfffffffffffffull)));
+  s = fma(lo ? 2.0 * RYS_LO_PER_UNIT : 2.0, X, c);
+  return lo ? f : RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
+}
+
 // Quantity q of the N-root rule at X (FP64): q even -> node x_{q/2}, q odd ->
-// weight w_{q/2}.  Interval k: width 1/4 below 32 (s = 8X - (2k+1)), unit
-// width above (s = 2X - (2 floor(X) + 1)).  X >= 0, so the range tests compare
-// bit patterns as integers (no FP64 instruction).
+// weight w_{q/2}.  X >= 0, so the range tests compare bit patterns as
+// integers (no FP64 instruction).
 template <int N, int NCOEF>
 __device__ __forceinline__ double rys_eval(const double* table, double X, int q) {
   const long long xb = __double_as_longlong(X);
@@ -62,16 +82,8 @@ __device__ __forceinline__ double rys_eval(const double* table, double X, int q)
     const double y = rsqrt64(X);
     return (q & 1) ? RYS_HERM_W[r] * y : RYS_HERM_R2[r] * (y * y);
   }
-  int k;
   double s;
-  if (xb < __double_as_longlong((double)RYS_X_SPLIT)) {
-    k = __double2int_rz(X * (double)RYS_LO_PER_UNIT);
-    s = fma(2.0 * RYS_LO_PER_UNIT, X, -(double)(2 * k + 1));
-  } else {
-    const int f = __double2int_rz(X);
-    k = RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
-    s = fma(2.0, X, -(double)(2 * f + 1));
-  }
+  const int k = rys_interval(xb, X, s);
   const double* c = table + rys_offset(N, NCOEF) + (k * 2 * N + q) * NCOEF;
   double v = __ldg(c + NCOEF - 1);
 #pragma unroll
@@ -92,16 +104,8 @@ __device__ __forceinline__ void rys_eval_uw(const double* table, double X, int r
     w = RYS_HERM_W[i] * y;
     return;
   }
-  int k;
   double s;
-  if (xb < __double_as_longlong((double)RYS_X_SPLIT)) {
-    k = __double2int_rz(X * (double)RYS_LO_PER_UNIT);
-    s = fma(2.0 * RYS_LO_PER_UNIT, X, -(double)(2 * k + 1));
-  } else {
-    const int f = __double2int_rz(X);
-    k = RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
-    s = fma(2.0, X, -(double)(2 * f + 1));
-  }
+  const int k = rys_interval(xb, X, s);
   // node coefficients at c, weight coefficients at c + NCOEF
   const double* c = table + rys_offset(N, NCOEF) + (k * 2 * N + 2 * r) * NCOEF;
   double vu = __ldg(c + NCOEF - 1), vw = __ldg(c + 2 * NCOEF - 1);
@@ -386,6 +390,9 @@ __device__ __forceinline__ void prim_setup(const PP& bp, const PP& kp, PrimQuart
 
 // 2D integrals of one root and one Cartesian dimension:
 // out[((i*(LB+1)+j)*(LC+1)+k)*(LD+1)+l], i<=LA, j<=LB, k<=LC, l<=LD.
+// A pair whose first shell is an s shell (LA = 0, LC = 0) runs the recursion
+// on its second centre and needs no transfer: the caller's c00 (d00) is then
+// formed from P - B (Q - D), which the Fock pair tables store for such pairs.
 template <int LA, int LB, int LC, int LD, typename T, typename Out>
 __device__ __forceinline__ void twod(T g00, T c00, T d00, T b00, T b10, T b01, T ab, T cd, Out&& out) {
   constexpr int NMAX = LA + LB, MMAX = LC + LD;
@@ -408,17 +415,22 @@ __device__ __forceinline__ void twod(T g00, T c00, T d00, T b00, T b10, T b01, T
   T H[LA + 1][LB + 1][MMAX + 1];
 #pragma unroll
   for (int m = 0; m <= MMAX; ++m) {
-    T col[NMAX + 1];
+    if constexpr (LA == 0) {
 #pragma unroll
-    for (int i = 0; i <= NMAX; ++i) col[i] = G[i][m];
+      for (int j = 0; j <= LB; ++j) H[0][j][m] = G[j][m];
+    } else {
+      T col[NMAX + 1];
 #pragma unroll
-    for (int i = 0; i <= LA; ++i) H[i][0][m] = col[i];
+      for (int i = 0; i <= NMAX; ++i) col[i] = G[i][m];
 #pragma unroll
-    for (int j = 1; j <= LB; ++j) {
+      for (int i = 0; i <= LA; ++i) H[i][0][m] = col[i];
 #pragma unroll
-      for (int i = 0; i <= NMAX - j; ++i) col[i] = fma(ab, col[i], col[i + 1]);
+      for (int j = 1; j <= LB; ++j) {
 #pragma unroll
-      for (int i = 0; i <= LA; ++i) H[i][j][m] = col[i];
+        for (int i = 0; i <= NMAX - j; ++i) col[i] = fma(ab, col[i], col[i + 1]);
+#pragma unroll
+        for (int i = 0; i <= LA; ++i) H[i][j][m] = col[i];
+      }
     }
   }
   // ket transfer
@@ -426,17 +438,22 @@ __device__ __forceinline__ void twod(T g00, T c00, T d00, T b00, T b10, T b01, T
   for (int i = 0; i <= LA; ++i)
 #pragma unroll
     for (int j = 0; j <= LB; ++j) {
-      T col[MMAX + 1];
+      if constexpr (LC == 0) {
 #pragma unroll
-      for (int k = 0; k <= MMAX; ++k) col[k] = H[i][j][k];
+        for (int l = 0; l <= LD; ++l) out((i * (LB + 1) + j) * (LD + 1) + l, H[i][j][l]);
+      } else {
+        T col[MMAX + 1];
 #pragma unroll
-      for (int k = 0; k <= LC; ++k) out(((i * (LB + 1) + j) * (LC + 1) + k) * (LD + 1) + 0, col[k]);
+        for (int k = 0; k <= MMAX; ++k) col[k] = H[i][j][k];
 #pragma unroll
-      for (int l = 1; l <= LD; ++l) {
+        for (int k = 0; k <= LC; ++k) out(((i * (LB + 1) + j) * (LC + 1) + k) * (LD + 1) + 0, col[k]);
 #pragma unroll
-        for (int k = 0; k <= MMAX - l; ++k) col[k] = fma(cd, col[k], col[k + 1]);
+        for (int l = 1; l <= LD; ++l) {
 #pragma unroll
-        for (int k = 0; k <= LC; ++k) out(((i * (LB + 1) + j) * (LC + 1) + k) * (LD + 1) + l, col[k]);
+          for (int k = 0; k <= MMAX - l; ++k) col[k] = fma(cd, col[k], col[k + 1]);
+#pragma unroll
+          for (int k = 0; k <= LC; ++k) out(((i * (LB + 1) + j) * (LC + 1) + k) * (LD + 1) + l, col[k]);
+        }
       }
     }
 }

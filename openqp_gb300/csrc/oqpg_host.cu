@@ -250,9 +250,9 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
   }
 }
 
-// Counting sort of a class list by primitive-quartet work (descending, in
-// quarter-octave bins), so that the lanes of a warp run loops of similar
-// length.  The work of a quartet is the number of its primitive quartets that
+// Counting sort of a class list by primitive-quartet work (descending; exact
+// counts below BIN_EXACT, quarter-octave bins above), so that the lanes of a
+// warp run loops of equal or similar length.  The work of a quartet is the number of its primitive quartets that
 // pass the FP32 pre-screen |sp sq| / sqrt(p + q) >= lo, the loop trip count of
 // the FP64 body (without prims: the product of the pair primitive counts).
 // k_bin_hist: per-bin counts (and each entry's bin); k_bin_scatter:
@@ -260,9 +260,16 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
 // cursors.
 
 __device__ __forceinline__ int work_bin(int n) {
-  if (n <= 1) return NBIN - 1;
-  const int k = (int)(4.0f * __log2f((float)n));
-  return NBIN - 1 - (k < NBIN - 1 ? k : NBIN - 1);
+  int b;
+  if (n < BIN_EXACT) {
+    b = n < 1 ? 0 : n - 1;
+  } else {
+    // quarter octaves from the leading bit: n = 2^e r, r in [1, 2)
+    const int e = 31 - __clz(n);
+    const float r = (float)n * __int_as_float((127 - e) << 23);
+    b = 4 * e + BIN_EXACT - 25 + (r >= 1.18920712f) + (r >= 1.41421356f) + (r >= 1.68179283f);
+  }
+  return NBIN - 1 - (b < NBIN - 1 ? b : NBIN - 1);
 }
 
 __device__ __forceinline__ int prim_bin(const PairDev* pairs, uint2 q) {
@@ -462,11 +469,19 @@ int to_status(cudaError_t e) {
 // the rotated-axis pre-screen |K/p| >= quartet cutoff (int_rotaxis.F90:292-306),
 // applied once (the Fock build; the gradient's Rys path has no such screen).
 // Pairs are numbered molecule by molecule, canonical (i >= j) within each.
+// With sp_screen a primitive pair is kept iff min(|K|, |K/p|) >= qcut; with
+// key_order each shell pair's primitive pairs are stored in decreasing order
+// of that key, so the pairs a looser cutoff keeps are a prefix of the range
+// (the run-time cutoff of oqpg_set_cutoff only shortens the counts).  With
+// s_on_b (the tables of the Fock-type kernels) a pair whose first shell is an
+// s shell stores P - B in place of P - A: those kernels run the recursion on
+// the second centre and skip the horizontal transfer.
 void oqpg::build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vector<int>& ncontr,
                        const std::vector<int>& poff, const double* ex, const double* cc, double qcut, double ecut,
-                       bool sp_screen, HostPairs& out) {
+                       bool sp_screen, HostPairs& out, bool key_order, bool s_on_b) {
   const double sqrtpito52 = std::sqrt(2.0) * std::pow(3.14159265358979323846, 1.25);
   out.pairs.clear(); out.prims.clear(); out.ij.clear(); out.type.clear(); out.mol.clear(); out.alpha.clear();
+  out.key.clear();
   for (int m = 0; m < c.nmol; ++m) {
     const MolDev& M = c.mols[m];
     for (int li = 0; li < M.ns; ++li)
@@ -478,6 +493,7 @@ void oqpg::build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std:
         const double ab2 = (A.x - B.x) * (A.x - B.x) + (A.y - B.y) * (A.y - B.y) + (A.z - B.z) * (A.z - B.z);
         PairDev pd;
         pd.sha = sa; pd.shb = sb; pd.poff = (int)out.prims.size();
+        const size_t first = out.prims.size();
         for (int p1 = 0; p1 < ncontr[sa]; ++p1)
           for (int p2 = 0; p2 < ncontr[sb]; ++p2) {
             const double a1 = ex[poff[sa] + p1], a2 = ex[poff[sb] + p2];
@@ -495,11 +511,31 @@ void oqpg::build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std:
             pp.px = (a1 * A.x + a2 * B.x) * gi;
             pp.py = (a1 * A.y + a2 * B.y) * gi;
             pp.pz = (a1 * A.z + a2 * B.z) * gi;
-            pp.ax = pp.px - A.x; pp.ay = pp.py - A.y; pp.az = pp.pz - A.z;
+            // the recursion's centre: A, or B when A is an s shell (no transfer then)
+            const ShellDev& R = (s_on_b && A.am == 0) ? B : A;
+            pp.ax = pp.px - R.x; pp.ay = pp.py - R.y; pp.az = pp.pz - R.z;
             pp.sp = sp; pp.spf = (float)sp; pp.pf = (float)g;
             out.prims.push_back(pp);
             out.alpha.push_back(a1);
+            out.key.push_back(sp_screen ? std::min(std::fabs(k1), std::fabs(sp)) : std::fabs(k1));
           }
+        if (key_order) {
+          const size_t n = out.prims.size() - first;
+          std::vector<int> ord(n);
+          for (size_t i = 0; i < n; ++i) ord[i] = (int)i;
+          std::stable_sort(ord.begin(), ord.end(),
+                           [&](int x, int y) { return out.key[first + x] > out.key[first + y]; });
+          std::vector<PrimPair> pp(n);
+          std::vector<double> al(n), ky(n);
+          for (size_t i = 0; i < n; ++i) {
+            pp[i] = out.prims[first + ord[i]];
+            al[i] = out.alpha[first + ord[i]];
+            ky[i] = out.key[first + ord[i]];
+          }
+          std::copy(pp.begin(), pp.end(), out.prims.begin() + first);
+          std::copy(al.begin(), al.end(), out.alpha.begin() + first);
+          std::copy(ky.begin(), ky.end(), out.key.begin() + first);
+        }
         pd.pcnt = (int)out.prims.size() - pd.poff;
         out.pairs.push_back(pd);
         out.ij.push_back(make_int2(li, lj));
@@ -554,7 +590,8 @@ int schwarz_bounds(oqpg_ctx* c, double inv_mu2, std::vector<double>& out) {
   cudaStream_t st = c->stream;
   int rc;
   HostPairs sp;
-  build_pairs(*c, c->h_am, c->h_ncontr, c->h_poff, c->h_ex.data(), c->h_cc.data(), 1e-17, 50.0, true, sp);
+  build_pairs(*c, c->h_am, c->h_ncontr, c->h_poff, c->h_ex.data(), c->h_cc.data(), 1e-17, 50.0, true, sp, false,
+              true);
   DevBuf d_pairs, d_prims, d_diag, d_q, d_w;
   if ((rc = upload(d_pairs, sp.pairs, st))) return rc;
   if ((rc = upload(d_prims, sp.prims, st))) return rc;
@@ -613,6 +650,48 @@ int upload_schwarz(oqpg_ctx* c, const std::vector<double>& q, DevBuf& d_q, DevBu
   if ((rc = upload(d_sidx, order, st))) return rc;
   if ((rc = upload(d_sq, sq, st))) return rc;
   CK(cudaStreamSynchronize(st));
+  return OK;
+}
+
+// Pair tables of the Fock-type builds at cutoff (primitive cutoffs 1e-4 tau and
+// 25 ln 10, int2.F90:260-272; int2_prepare_pair), key-ordered so that a looser
+// run-time cutoff is a prefix of every shell pair's range.
+int fock_tables(oqpg_ctx* c, double cutoff) {
+  cudaStream_t st = c->stream;
+  int rc;
+  HostPairs fp;
+  build_pairs(*c, c->h_am, c->h_ncontr, c->h_poff, c->h_ex.data(), c->h_cc.data(), 1e-4 * cutoff,
+              25.0 * std::log(10.0), true, fp, true, true);
+  if ((rc = upload(c->d_pairs, fp.pairs, st))) return rc;
+  if ((rc = upload(c->d_prims, fp.prims, st))) return rc;
+  std::vector<PrimPairF> pf(fp.prims.size());
+  for (size_t i = 0; i < pf.size(); ++i) {
+    const PrimPair& q = fp.prims[i];
+    pf[i] = PrimPairF{(float)q.p, (float)q.hp, (float)q.px, (float)q.py, (float)q.pz,
+                      (float)q.ax, (float)q.ay, (float)q.az, (float)q.sp, 0.0f};
+  }
+  if ((rc = upload(c->d_primsf, pf, st))) return rc;
+  // double-float copy for the df mode: every FP64 field as an FP32 pair
+  std::vector<PrimPairDF> pd(fp.prims.size());
+  auto split = [](double v) {
+    const float h = (float)v;
+    return dfl(h, (float)(v - (double)h));
+  };
+  for (size_t i = 0; i < pd.size(); ++i) {
+    const PrimPair& q = fp.prims[i];
+    PrimPairDF& o = pd[i];
+    o.p = split(q.p); o.hp = split(q.hp); o.px = split(q.px); o.py = split(q.py); o.pz = split(q.pz);
+    o.ax = split(q.ax); o.ay = split(q.ay); o.az = split(q.az); o.sp = split(q.sp);
+    o.spf = q.spf; o.pf = q.pf;
+  }
+  if ((rc = upload(c->d_primsdf, pd, st))) return rc;
+  if ((rc = upload(c->d_pair_ij, fp.ij, st))) return rc;
+  if ((rc = upload(c->d_pair_type, fp.type, st))) return rc;
+  if ((rc = upload(c->d_pair_mol, fp.mol, st))) return rc;
+  CK(cudaStreamSynchronize(st));
+  c->h_fpairs = fp.pairs;
+  c->h_fkey = fp.key;
+  c->tau_built = cutoff;
   return OK;
 }
 
@@ -700,35 +779,8 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
   // --- Schwarz bounds with OpenQP's very tight cutoffs (int2.F90:1600-1604)
   if ((rc = schwarz_bounds(c, 0.0, c->schwarz_pair))) return rc;
 
-  // --- pair tables of the Fock build (cutoffs 1e-2 tau, 1e-4 tau, 25 ln 10; int2.F90:260-272)
-  HostPairs fp;
-  build_pairs(*c, am, ncontr, poff, ex, cc, 1e-4 * cutoff, 25.0 * std::log(10.0), true, fp);
-  if ((rc = upload(c->d_pairs, fp.pairs, st))) return rc;
-  if ((rc = upload(c->d_prims, fp.prims, st))) return rc;
-  std::vector<PrimPairF> pf(fp.prims.size());
-  for (size_t i = 0; i < pf.size(); ++i) {
-    const PrimPair& q = fp.prims[i];
-    pf[i] = PrimPairF{(float)q.p, (float)q.hp, (float)q.px, (float)q.py, (float)q.pz,
-                      (float)q.ax, (float)q.ay, (float)q.az, (float)q.sp, 0.0f};
-  }
-  if ((rc = upload(c->d_primsf, pf, st))) return rc;
-  // double-float copy for the df mode: every FP64 field as an FP32 pair
-  std::vector<PrimPairDF> pd(fp.prims.size());
-  auto split = [](double v) {
-    const float h = (float)v;
-    return dfl(h, (float)(v - (double)h));
-  };
-  for (size_t i = 0; i < pd.size(); ++i) {
-    const PrimPair& q = fp.prims[i];
-    PrimPairDF& o = pd[i];
-    o.p = split(q.p); o.hp = split(q.hp); o.px = split(q.px); o.py = split(q.py); o.pz = split(q.pz);
-    o.ax = split(q.ax); o.ay = split(q.ay); o.az = split(q.az); o.sp = split(q.sp);
-    o.spf = q.spf; o.pf = q.pf;
-  }
-  if ((rc = upload(c->d_primsdf, pd, st))) return rc;
-  if ((rc = upload(c->d_pair_ij, fp.ij, st))) return rc;
-  if ((rc = upload(c->d_pair_type, fp.type, st))) return rc;
-  if ((rc = upload(c->d_pair_mol, fp.mol, st))) return rc;
+  // --- pair tables of the Fock build
+  if ((rc = fock_tables(c, cutoff))) return rc;
   CK(cudaStreamSynchronize(st));
   return upload_schwarz(c, c->schwarz_pair, c->d_q, c->d_qf, c->d_sorted_idx, c->d_sorted_q);
 }
@@ -901,7 +953,7 @@ int size_lists(oqpg_ctx* c, BuildBufs& B, const unsigned long long* counts, cuda
   int split[NLIST];
   for (int k = 0; k < NLIST; ++k) {
     const int cl = k % NCLASS;
-    split[k] = class_info(cl).prim ? std::max(0, NBIN - 4 * c->tune.split_log2[cl]) : 0;
+    split[k] = class_info(cl).prim ? head_bins(c->tune.split_log2[cl]) : 0;
   }
   CK(cudaMemcpyAsync(B.split.p, split, sizeof(split), cudaMemcpyHostToDevice, st));
   CK(cudaStreamSynchronize(st));  // the host arrays above are stack memory
@@ -1227,6 +1279,7 @@ int graph_capture(oqpg_ctx* c, const double* dp, int nfocks, double se, double s
   cudaGraphDestroy(g);
   CK(e);
   c->g_nfocks = nfocks; c->g_se = se; c->g_sc = sc; c->g_mode = c->precision_mode; c->g_tau32 = c->tau_f32;
+  c->g_tau = c->tau;
   c->g_nlaunch = nlaunch;
   ++c->graph_captures;
   return OK;
@@ -1242,7 +1295,7 @@ int graph_build(oqpg_ctx* c, const double* d_device, double* f_device, int nfock
   if (nfocks != 1 && nfocks != 2) return UNSUPPORTED;
   const size_t bytes = sizeof(double) * (size_t)c->ntri * nfocks;
   const bool fresh = c->gexec && c->g_nfocks == nfocks && c->g_se == se && c->g_sc == sc &&
-                     c->g_mode == c->precision_mode && c->g_tau32 == c->tau_f32;
+                     c->g_mode == c->precision_mode && c->g_tau32 == c->tau_f32 && c->g_tau == c->tau;
   int rc;
   if (fresh) {
     CK(cudaMemcpyAsync(c->d_gin.p, d_device, bytes, cudaMemcpyDeviceToDevice, st));
@@ -1415,6 +1468,32 @@ int oqpg_measure_fp64_peak(int iters, double* tflops) {
   return OK;
 }
 
+// The library's reciprocal and reciprocal square root (FP64 and double-float)
+// beside CUDA's rsqrt() and IEEE division, one argument per thread.
+__global__ void k_math_check(const double* __restrict__ x, double* __restrict__ out, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = x[i];
+  double* o = out + 6 * i;
+  o[0] = oqpg::rsqrt64(v);
+  o[1] = rsqrt(v);
+  o[2] = oqpg::rcp64(v);
+  o[3] = 1.0 / v;
+  const float h = (float)v;
+  const oqpg::dfl d(h, (float)(v - (double)h));
+  o[4] = (double)oqpg::df_rsqrt(d);
+  o[5] = (double)oqpg::df_rcp(d);
+}
+
+int oqpg_math_check(const double* x_device, double* out_device, long long n) {
+  if (!x_device || !out_device || n < 0) return UNSUPPORTED;
+  if (n == 0) return OK;
+  k_math_check<<<(unsigned)((n + 255) / 256), 256>>>(x_device, out_device, n);
+  CK(cudaGetLastError());
+  CK(cudaDeviceSynchronize());
+  return OK;
+}
+
 int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold) {
   if (!ctx) return NOT_INIT;
   if (mode < 0 || mode > 4) return UNSUPPORTED;
@@ -1430,6 +1509,46 @@ int routec_fock_set_precision(int mode, double threshold) {
   std::lock_guard<std::mutex> lk(g_mutex);
   if (!g_ctx) return NOT_INIT;
   return oqpg_set_precision(g_ctx, mode, threshold);
+}
+
+// int2_compute_t_set_cutoff (int2.F90:480-496): tau, 1e-2 tau and 1e-4 tau of
+// the following builds; the exponent cutoff and the Schwarz bounds stay.  At
+// or above the cutoff the pair tables were built at, only the primitive counts
+// of the shell pairs shrink (the tables are key-ordered, so the pairs the
+// reference's tables at this cutoff hold are a prefix); below it the tables
+// are rebuilt at the new cutoff.
+int oqpg_set_cutoff(oqpg_ctx* ctx, double cutoff) {
+  if (!ctx) return NOT_INIT;
+  if (!(cutoff > 0.0) || !std::isfinite(cutoff)) return UNSUPPORTED;
+  if (cutoff == ctx->tau) return OK;
+  int rc;
+  if (cutoff < ctx->tau_built) {
+    if ((rc = fock_tables(ctx, cutoff))) return rc;
+  } else {
+    const double qcut = 1e-4 * cutoff;
+    std::vector<PairDev> pr = ctx->h_fpairs;
+    for (PairDev& p : pr) {
+      int n = 0;
+      while (n < p.pcnt && !(ctx->h_fkey[p.poff + n] < qcut)) ++n;
+      p.pcnt = n;
+    }
+    if ((rc = upload(ctx->d_pairs, pr, ctx->stream))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  ctx->tau = cutoff;
+  ctx->hb.sized = false;  // the lists are sized by a fresh count pass
+  return OK;
+}
+
+double oqpg_get_cutoff(const oqpg_ctx* ctx) { return ctx ? ctx->tau : -1.0; }
+
+void routec_fock_set_cutoff(const double* cutoff, int* info) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!cutoff) rc = UNSUPPORTED;
+  else rc = oqpg_set_cutoff(g_ctx, *cutoff);
+  if (info) *info = rc;
 }
 
 int oqpg_class_l(int c, int* l4) {

@@ -13,7 +13,19 @@ namespace oqpg {
 
 enum Status { OK = 0, NOT_INIT = 1, NO_MEM = 2, UNSUPPORTED = 3, DEV_ERR = 4 };
 
-constexpr int NBIN = 64;            // primitive-count bins of the class-list sort
+// Primitive-count bins of the class-list sort, heaviest first: a quartet with
+// n surviving primitive quartets goes to bin NBIN - 1 - b(n), b(n) = n - 1 for
+// n < BIN_EXACT (exact counts, so the lanes of a warp run equal trip counts)
+// and 4 log2(n) + BIN_EXACT - 25 above (quarter octaves).
+constexpr int NBIN = 128;
+constexpr int BIN_EXACT = 64;
+// Bins 0 .. head_bins(s) - 1 hold the quartets with at least 2^s primitive quartets.
+inline int head_bins(int s) {
+  if (s < 0) return NBIN;
+  if (s > 30) return 0;
+  const int b = (1 << s) < BIN_EXACT ? (1 << s) - 1 : 4 * s + BIN_EXACT - 25;
+  return b > NBIN - 1 ? 0 : NBIN - b;
+}
 constexpr int PRIM_SPLIT_LOG2 = 8;  // >= 256 primitive quartets: warp per quartet
 
 // One molecule of a context (a context holds a batch of one or more).  Its
@@ -153,6 +165,10 @@ struct HostPairs {
   std::vector<PairDev> pairs;
   std::vector<PrimPair> prims;
   std::vector<double> alpha;  // exponent of the pair's first shell, per primitive pair
+  // screening key min(|K|, |K/p|) of each primitive pair (pre-screened tables:
+  // a shell pair's primitive pairs are in decreasing key order, so the pairs
+  // that a looser cutoff keeps are a prefix of its range)
+  std::vector<double> key;
   std::vector<int2> ij;       // molecule-local shells of each pair
   std::vector<int> type;
   std::vector<int> mol;
@@ -165,7 +181,7 @@ struct oqpg_ctx;
 namespace oqpg {
 void build_pairs(const oqpg_ctx& c, const std::vector<int>& am, const std::vector<int>& ncontr,
                  const std::vector<int>& poff, const double* ex, const double* cc, double qcut, double ecut,
-                 bool sp_screen, HostPairs& out);
+                 bool sp_screen, HostPairs& out, bool key_order = false, bool s_on_b = false);
 // general-job density staging / shell density and result assembly (oqpg_response.cu)
 int gen_densities(oqpg_ctx* c, BuildBufs& B, const GenJob& g, cudaStream_t st);
 int gen_finalize(oqpg_ctx* c, BuildBufs& B, const GenJob& g, cudaStream_t st);
@@ -231,7 +247,10 @@ struct oqpg_ctx {
   long long ntri = 0, dsh_elems = 0;  // packed elements per density, shell-density elements (whole batch)
   bool pure = false;
   bool has_f = false;   // an f shell is registered
-  double tau = 1e-10;
+  double tau = 1e-10;      // run-time cutoff of the Fock-type builds (oqpg_set_cutoff)
+  double tau_built = 1e-10;  // cutoff the Fock pair tables were built at (tau >= tau_built)
+  std::vector<oqpg::PairDev> h_fpairs;  // those tables' shell pairs with their full primitive counts
+  std::vector<double> h_fkey;           // and the screening key of every primitive pair
   std::vector<oqpg::ShellDev> shells;
   std::vector<int> aoff, naos;
   std::vector<oqpg::MolDev> mols;
@@ -263,7 +282,7 @@ struct oqpg_ctx {
   cudaGraphExec_t gexec = nullptr;
   cudaStream_t gstream = nullptr;
   int g_nfocks = 0, g_mode = -1;
-  double g_se = 0, g_sc = 0, g_tau32 = 0;
+  double g_se = 0, g_sc = 0, g_tau32 = 0, g_tau = 0;
   oqpg::DevBuf d_gin, d_gout;        // the graph's packed input / output
   int graph_replays = 0, graph_captures = 0, g_nlaunch = 0;
   // two-electron gradient: pair tables with the gradient cutoffs (built on first use)

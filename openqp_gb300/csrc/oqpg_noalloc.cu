@@ -6,16 +6,20 @@
 // out-of-memory or fragmentation from allocations made behind its back, and a
 // latency-critical SCF loop cannot afford the device-wide synchronisation a
 // cudaMalloc/cudaFree pair may cause.  For them oqpg_fock_jk_noalloc runs the
-// same build as oqpg_fock_jk_device, with every per-build buffer (densities,
-// J/K accumulators, shell densities, quartet lists, counters) carved out of
-// one file-scope device array of fixed size, so it calls no cudaMalloc,
-// cudaFree or allocating library routine.  The read-only tables of the
-// molecule (shells, primitive pairs, Schwarz bounds) are the context's, made
-// once by oqpg_create.
+// plain-FP64 build of oqpg_fock_jk_device (precision mode 0, the built-in
+// launch defaults, whatever the context's precision split and tuning say;
+// the context's cutoff applies), with every per-build buffer (densities, J/K
+// accumulators, shell densities, quartet lists, counters) carved out of one
+// file-scope device array of fixed size, so it calls no cudaMalloc, cudaFree
+// or allocating library routine.  The read-only tables of the molecule
+// (shells, primitive pairs, Schwarz bounds) are the context's, made once by
+// oqpg_create.
 //
-// Limits: nbf <= 128, nshell <= 128 and at most NOALLOC_MAX_QUARTETS screened
-// quartets over all classes; larger inputs are rejected with status
-// OQPG_NOALLOC_TOO_LARGE (5) before any kernel runs.
+// Limits: nbf <= 128 and nshell <= 128, checked before any kernel runs; the
+// screened quartets of all classes must fit the rest of the array (an
+// unsorted and a sorted 8-byte entry each: about 1.5 million at nbf = 128),
+// which the screening pass finds out.  Either limit returns status 5 with
+// the caller's output untouched (only the scratch array has been written).
 #include <cstring>
 #include <mutex>
 
@@ -42,6 +46,10 @@ void* g_scratch_addr[MAX_DEVICES] = {nullptr};
 // Device address of g_noalloc_scratch on the current device.  In host code
 // the array's name is a host-side stand-in, not a device address, so the
 // address is looked up once per device (with that device current) and cached.
+// Under lazy module loading the first lookup may load the module and reserve
+// the array's device memory at that moment, so the first call on a device
+// should come before any stream capture and before a pool allocator takes
+// the rest of the device memory.
 int scratch_address(void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return oqpg::DEV_ERR;
@@ -96,15 +104,22 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
   unsigned long long* primc = cv.take<unsigned long long>(NCLASS);
   unsigned long long* work = cv.take<unsigned long long>(2 * NCLASS);
   cv.used = (cv.used + 255) & ~size_t(255);
-  const size_t qcap = (NOALLOC_BYTES - cv.used) / (2 * sizeof(uint2));  // unsorted + sorted copies
+  // unsorted + sorted copies; a multiple of 32 entries (256 bytes), so the
+  // second copy starts aligned and both end inside the array
+  const size_t qcap = ((NOALLOC_BYTES - cv.used) / (2 * sizeof(uint2))) & ~size_t(31);
   uint2* lists = cv.take<uint2>(qcap);
   uint2* slists = cv.take<uint2>(qcap);
   if (cv.used > NOALLOC_BYTES) return DEV_ERR;
 
+// A failed launch or copy waits for the work already queued on the stream
+// (it uses the shared array) before the call returns.
 #define NK(x)                                      \
   do {                                             \
     cudaError_t e_ = (x);                          \
-    if (e_ != cudaSuccess) return DEV_ERR;         \
+    if (e_ != cudaSuccess) {                       \
+      cudaStreamSynchronize(st);                   \
+      return DEV_ERR;                              \
+    }                                              \
   } while (0)
 
   NK(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), st));
@@ -201,7 +216,7 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
     a.counters = primc + cl;
     long long head = 0;
     if (class_info(cl).prim && !class_info(cl).team) {
-      for (int b = 0; b <= NBIN - 1 - 4 * PRIM_SPLIT_LOG2; ++b) head += (long long)h_hist[cl * NBIN + b];
+      for (int b = 0; b < head_bins(PRIM_SPLIT_LOG2); ++b) head += (long long)h_hist[cl * NBIN + b];
       if (head > 0) {
         a.quartets = slists + off[cl];
         a.nquartets = head;

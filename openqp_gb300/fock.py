@@ -301,6 +301,19 @@ class FockBuilder:
         if rc != 0:
             raise FockError(rc, "oqpg_set_precision")
 
+    def set_cutoff(self, cutoff):
+        """Two-electron cutoff of the following builds, as OpenQP's
+        int2_compute_t_set_cutoff (the progressive-screening SCF changes it per
+        build)."""
+        rc = lib().oqpg_set_cutoff(self.h, float(cutoff))
+        if rc != 0:
+            raise FockError(rc, "oqpg_set_cutoff")
+        self.cutoff = float(cutoff)
+
+    def get_cutoff(self):
+        """The cutoff the library applies to the next build."""
+        return lib().oqpg_get_cutoff(self.h)
+
     def grad2(self, d, hfscale=1.0, coulscale=1.0):
         """Two-electron gradient (natom, 3) for packed densities d ((ntri,) or
         (nfocks, ntri): total RHF density, or alpha and beta)."""
@@ -491,6 +504,31 @@ def routec_fock_jk(d, nbf, nfocks, se=1.0, sc=1.0):
     lib().routec_fock_jk(ptr(d), ptr(f), ctypes.byref(n), ctypes.byref(nf), ctypes.byref(se_), ctypes.byref(sc_),
                          ctypes.byref(info))
     return f.reshape(nfocks, -1), info.value
+
+
+def routec_fock_jk_inc(dd, f_old, nbf, nfocks, se=1.0, sc=1.0):
+    """Calls routec_fock_jk_inc (all by reference): F = F_old + G(dD) with
+    F_old overwritten by F, as fock_jk's f_old branch.  f_old is updated in
+    place (a float64 C-contiguous array).  Returns (f, info)."""
+    dd = np.ascontiguousarray(dd, dtype=np.float64).reshape(-1)
+    if not (isinstance(f_old, np.ndarray) and f_old.dtype == np.float64 and f_old.flags.c_contiguous
+            and f_old.size == dd.size):
+        raise ValueError("f_old must be a C-contiguous float64 array of the density's size")
+    f = np.zeros_like(dd)
+    n, nf = ctypes.c_int(nbf), ctypes.c_int(nfocks)
+    se_, sc_ = ctypes.c_double(se), ctypes.c_double(sc)
+    info = ctypes.c_int(1)
+    lib().routec_fock_jk_inc(ptr(dd), ptr(f), ptr(f_old), ctypes.byref(n), ctypes.byref(nf), ctypes.byref(se_),
+                             ctypes.byref(sc_), ctypes.byref(info))
+    return f.reshape(nfocks, -1), info.value
+
+
+def routec_fock_set_cutoff(cutoff):
+    """Calls routec_fock_set_cutoff by reference; returns info."""
+    c = ctypes.c_double(cutoff)
+    info = ctypes.c_int(1)
+    lib().routec_fock_set_cutoff(ctypes.byref(c), ctypes.byref(info))
+    return info.value
 
 
 def routec_grad2(d, xyz, nbf, natom, hfscale=1.0, coulscale=1.0, de=None):

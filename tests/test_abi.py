@@ -21,7 +21,7 @@ def libgpu():
 
 def test_exports_every_declared_symbol(libgpu):
     hdr = open(os.path.join(ROOT, "include", "openqp_gb300.h")).read()
-    names = set(re.findall(r"^\s*(?:int|void)\s+\**\s*(\w+)\s*\(", hdr, re.M))
+    names = set(re.findall(r"^\s*(?:int|void|double)\s+\**\s*(\w+)\s*\(", hdr, re.M))
     assert {"routec_fock_jk", "routec_fock_init", "oqpg_create"} <= names
     for n in names:
         assert hasattr(libgpu, n), n
@@ -44,6 +44,9 @@ def test_unsupported_angular_momentum_is_declined(libgpu):
 def test_seam_without_init_declines(libgpu):
     from openqp_gb300 import fock
     f, info = fock.routec_fock_jk(np.zeros(3), 2, 1)
+    assert info == 1
+    assert fock.routec_fock_set_cutoff(1e-8) == 1
+    f, info = fock.routec_fock_jk_inc(np.zeros(3), np.zeros(3), 2, 1)
     assert info == 1
     eye = np.eye(4)
     assert fock.routec_sig_init(eye, eye, eye, eye, 3, 1, 1) == 1

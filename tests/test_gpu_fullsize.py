@@ -8,7 +8,13 @@ compares the CUDA result with a complete oracle run on all host cores (about
   scf_addons.F90:1063-1214 through int2.F90:589-923), and the same build in
   the double-float precision mode;
 * C40H82 6-31G(d) Cartesian, 764 bf, one RHF build and one UHF build;
-* (H2O)16 6-31G(d), 304 bf, the two-electron gradient (grd2.F90:145-391).
+* (H2O)16 6-31G(d), 304 bf, the two-electron gradient (grd2.F90:145-391);
+* C40H82 6-31G(d): the whole RHF SCF with the precision split and incremental
+  dD builds (form (b), scf.F90:758-773), energy within 1e-6 Eh of the
+  plain-FP64 SCF on the same input;
+* the 256-cluster batch (1-16 waters each, 6-31G) built from one captured
+  CUDA graph: a seeded sample of its molecules against the oracle, FP64 and
+  with the precision split.
 
 Tolerances are the plain-FP64 gates of the small cases: 1e-10 max-abs on the
 packed Fock matrix, 1e-9 Eh/Bohr on the gradient.
@@ -78,3 +84,57 @@ def test_water16_631gd_full_gradient(gpu, oracle_lib):
     assert np.abs(g - ref).max() < GTOL
     # translational invariance of the two-electron gradient
     assert np.abs(g.sum(axis=0)).max() < GTOL
+
+
+def test_alkane40_mixed_incremental_scf(gpu):
+    """C40H82 6-31G(d) RHF SCF: FP32 below the bound 1e-6 (roots and weights
+    in FP64: mode "mixed"; and mode "mixed-df", double-float above the bound)
+    with incremental dD builds, against the plain-FP64 SCF of the same GPU
+    builder (pinned to the oracle at this size by the build test above)."""
+    from openqp_gb300 import onee, scf, workloads
+    from openqp_gb300.basis import build_basis
+    z, xyz = workloads.alkane(40, 0)
+    bas = build_basis(z, xyz, "6-31g(d)")
+    S, T, V = onee.one_electron(bas)
+    H = T + V
+    enuc = onee.nuclear_repulsion(bas)
+    nocc = workloads.nelectrons(bas) // 2
+    fb = gpu.FockBuilder(bas)
+    ref = scf.run_scf(bas.nbf, S, H, enuc, nocc, nocc, fb.fock_jk, conv=1e-9, maxit=60)
+    assert ref["converged"]
+    for mode in ("mixed", "mixed-df"):
+        fb.set_precision(mode, 1e-6)
+        r = scf.run_scf(bas.nbf, S, H, enuc, nocc, nocc, fb.fock_jk, conv=1e-9, maxit=60, incremental=True)
+        assert r["converged"], mode
+        assert abs(r["energy"] - ref["energy"]) < 1e-6, mode
+    fb.set_precision("fp64")
+
+
+def test_batch256_graph_sample_against_oracle(gpu, oracle_lib):
+    """The 256-cluster batch built from one captured graph (capture, then a
+    replay): 12 seeded molecules plus the largest one against the oracle at
+    1e-10; with the precision split (mode "mixed", bound 1e-6) the two-electron
+    energy 1/2 Tr(D dF) of each sampled molecule within 1e-6 Eh of the
+    oracle's."""
+    import torch
+    from openqp_gb300 import workloads
+    from openqp_gb300.basis import unpack
+    sizes, bases, dens = workloads.water_batch(256, 0, basis="6-31g")
+    bb = gpu.BatchFockBuilder(bases)
+    d = torch.from_numpy(bb.pack(dens)[None]).cuda()
+    bb.fock_jk_graph(d)
+    f64 = bb.unpack(bb.fock_jk_graph(d).cpu().numpy()[0])
+    assert bb.graph_info()["replays"] >= 1
+    sample = sorted(set(np.random.default_rng(0).choice(256, 12, replace=False).tolist()) |
+                    {int(np.argmax(sizes))})
+    refs = {m: oracle_lib.Oracle(bases[m]).fock_jk(dens[m]).reshape(-1) for m in sample}
+    for m in sample:
+        assert np.abs(f64[m][0] - refs[m]).max() < TOL, m
+    bb.set_precision("mixed", 1e-6)
+    bb.fock_jk_graph(d)
+    fmx = bb.unpack(bb.fock_jk_graph(d).cpu().numpy()[0])
+    assert bb.stats()["f32_quartets"] > 0
+    for m in sample:
+        n = bases[m].nbf
+        de2 = 0.5 * float(np.sum(unpack(dens[m], n) * unpack(fmx[m][0] - refs[m], n)))
+        assert abs(de2) < 1e-6, m
