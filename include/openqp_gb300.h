@@ -326,13 +326,14 @@ int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold);
 int oqpg_set_cutoff(oqpg_ctx* ctx, double cutoff);
 double oqpg_get_cutoff(const oqpg_ctx* ctx);
 
-/* Statistics of the last build, up to n (<= 175) doubles:
+/* Statistics of the last build, up to n (<= 230) doubles:
  * [0] quartets computed, [1] primitive quartets, [2] list build ms,
  * [3] integral kernels ms, [4] total device ms, [5] nbf, [6] shell pairs,
  * [7 .. 62) quartets per class (la lb|lc ld) in the order of oqpg_class_l,
  * [62 .. 117) primitive quartets per class, [117 .. 172) kernel ms per class,
  * [172] kernels launched by the build, [173] FP32 quartets, [174] FP32
- * primitive quartets. */
+ * primitive quartets, [175 .. 230) the part of each class's kernel ms spent
+ * in its FP32 launches (precision split). */
 int oqpg_stats(const oqpg_ctx* ctx, double* out, int n);
 
 /* One-electron integrals on the host for the SCF around the Fock build

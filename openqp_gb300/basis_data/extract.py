@@ -74,4 +74,6 @@ def main(src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/basis_sets")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python extract.py <openqp checkout>/basis_sets")
+    main(sys.argv[1])

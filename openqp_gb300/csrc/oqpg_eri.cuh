@@ -69,25 +69,46 @@ __device__ __forceinline__ int rys_interval(long long xb, double X, double& s) {
   return lo ? f : RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
 }
 
+// Above the table (X >= 32 + 8N) the nodes and weights are R2/X and W/sqrt(X):
+// polynomials of degree 2 and 1 in y = X^-1/2 (y from one reciprocal square
+// root).  A warp whose lanes all lie above the table evaluates them directly;
+// a warp whose lanes all lie in the table runs the interpolant; a warp with
+// lanes on both sides runs ONE Horner chain, in the interval variable s for
+// table lanes and in y for the others with the coefficients (0, 0, R2, 0, ...)
+// and (0, W, 0, ...), so the two kinds of lanes share every FMA of the chain
+// (a divergent branch would issue both evaluations for the whole warp).  The
+// zero coefficients make the chain exact: R2 y y and W y.
+
 // Quantity q of the N-root rule at X (FP64): q even -> node x_{q/2}, q odd ->
 // weight w_{q/2}.  X >= 0, so the range tests compare bit patterns as
 // integers (no FP64 instruction).
 template <int N, int NCOEF>
 __device__ __forceinline__ double rys_eval(const double* table, double X, int q) {
   const long long xb = __double_as_longlong(X);
-  if (xb >= __double_as_longlong((double)rys_xmax(N))) {
+  const bool asym = xb >= __double_as_longlong((double)rys_xmax(N));
+  const unsigned act = __activemask();
+  const unsigned ba = __ballot_sync(act, asym);
+  const int r = (N * (N - 1)) / 2 + (q >> 1);
+  if (ba == act) {
     // nodes R2 / X and weights W / sqrt(X) from one reciprocal square root, so
     // lanes that evaluate nodes and lanes that evaluate weights take one path
-    const int r = (N * (N - 1)) / 2 + (q >> 1);
     const double y = rsqrt64(X);
     return (q & 1) ? RYS_HERM_W[r] * y : RYS_HERM_R2[r] * (y * y);
   }
-  double s;
-  const int k = rys_interval(xb, X, s);
-  const double* c = table + rys_offset(N, NCOEF) + (k * 2 * N + q) * NCOEF;
-  double v = __ldg(c + NCOEF - 1);
+  double s, a = 0.0;
+  const double* c = table;
+  if (asym) {
+    s = rsqrt64(X);
+    a = (q & 1) ? RYS_HERM_W[r] : RYS_HERM_R2[r];
+  } else {
+    const int k = rys_interval(xb, X, s);
+    c = table + rys_offset(N, NCOEF) + (k * 2 * N + q) * NCOEF;
+  }
+  // the single nonzero coefficient of the large-X form: degree 1 (weight) or 2 (node)
+  const int ia = (q & 1) ? 1 : 2;
+  double v = asym ? 0.0 : __ldg(c + NCOEF - 1);
 #pragma unroll
-  for (int i = NCOEF - 2; i >= 0; --i) v = fma(v, s, __ldg(c + i));
+  for (int i = NCOEF - 2; i >= 0; --i) v = fma(v, s, asym ? (i == ia ? a : 0.0) : __ldg(c + i));
   return v;
 }
 
@@ -97,22 +118,32 @@ __device__ __forceinline__ double rys_eval(const double* table, double X, int q)
 template <int N, int NCOEF>
 __device__ __forceinline__ void rys_eval_uw(const double* table, double X, int r, double& u, double& w) {
   const long long xb = __double_as_longlong(X);
-  if (xb >= __double_as_longlong((double)rys_xmax(N))) {
-    const int i = (N * (N - 1)) / 2 + r;
+  const bool asym = xb >= __double_as_longlong((double)rys_xmax(N));
+  const unsigned act = __activemask();
+  const unsigned ba = __ballot_sync(act, asym);
+  const int i0 = (N * (N - 1)) / 2 + r;
+  if (ba == act) {
     const double y = rsqrt64(X);
-    u = RYS_HERM_R2[i] * (y * y);
-    w = RYS_HERM_W[i] * y;
+    u = RYS_HERM_R2[i0] * (y * y);
+    w = RYS_HERM_W[i0] * y;
     return;
   }
-  double s;
-  const int k = rys_interval(xb, X, s);
-  // node coefficients at c, weight coefficients at c + NCOEF
-  const double* c = table + rys_offset(N, NCOEF) + (k * 2 * N + 2 * r) * NCOEF;
-  double vu = __ldg(c + NCOEF - 1), vw = __ldg(c + 2 * NCOEF - 1);
+  double s, r2 = 0.0, wh = 0.0;
+  const double* c = table;
+  if (asym) {
+    s = rsqrt64(X);
+    r2 = RYS_HERM_R2[i0];
+    wh = RYS_HERM_W[i0];
+  } else {
+    const int k = rys_interval(xb, X, s);
+    // node coefficients at c, weight coefficients at c + NCOEF
+    c = table + rys_offset(N, NCOEF) + (k * 2 * N + 2 * r) * NCOEF;
+  }
+  double vu = asym ? 0.0 : __ldg(c + NCOEF - 1), vw = asym ? 0.0 : __ldg(c + 2 * NCOEF - 1);
 #pragma unroll
   for (int i = NCOEF - 2; i >= 0; --i) {
-    vu = fma(vu, s, __ldg(c + i));
-    vw = fma(vw, s, __ldg(c + NCOEF + i));
+    vu = fma(vu, s, asym ? (i == 2 ? r2 : 0.0) : __ldg(c + i));
+    vw = fma(vw, s, asym ? (i == 1 ? wh : 0.0) : __ldg(c + NCOEF + i));
   }
   u = vu;
   w = vw;
@@ -371,7 +402,9 @@ __device__ __forceinline__ dfl rsqrt_t(dfl x) { return df_rsqrt(x); }
 // becomes p + q + pq/mu^2 in rho, in the prefactor and in the recurrence
 // coefficients (int_rys.F90:225-240; int_rotaxis.F90:634-638 writes the same
 // as rho mu^2/(mu^2 + rho)).  The primitive screen keeps the plain p + q.
-template <typename T, bool ATT = false, typename PP>
+// XPI: X = q (p/s) |PQ|^2 instead of p (q/s) |PQ|^2 (same value), for callers
+// that never use q/s (a bra pair of two s shells): one multiply fewer.
+template <typename T, bool ATT = false, bool XPI = false, typename PP>
 __device__ __forceinline__ void prim_setup(const PP& bp, const PP& kp, PrimQuartet<T>& o, T att = T(0)) {
   const T fqz = bp.sp * kp.sp;
   T s = bp.p + kp.p;
@@ -384,7 +417,7 @@ __device__ __forceinline__ void prim_setup(const PP& bp, const PP& kp, PrimQuart
   o.PQ[1] = bp.py - kp.py;
   o.PQ[2] = bp.pz - kp.pz;
   const T r2 = fma(o.PQ[0], o.PQ[0], fma(o.PQ[1], o.PQ[1], o.PQ[2] * o.PQ[2]));
-  o.X = bp.p * o.qi * r2;
+  o.X = XPI ? kp.p * o.pi * r2 : bp.p * o.qi * r2;
   o.pref = fqz * y;
 }
 
@@ -528,6 +561,28 @@ __device__ __constant__ const float2 SQRT3_POW_DF[5] = {{1.0f, 0.0f},
                                                        {9.0f, 0.0f}};
 template <> __device__ __forceinline__ dfl sqrt3_pow<dfl>(int n) { return dfl(SQRT3_POW_DF[n].x, SQRT3_POW_DF[n].y); }
 
+// sqrt(3)^n / 2^k, n <= 4, k <= 3: the component norms of a Cartesian element
+// times the shell-identity factor 2^-k.  FP64: a select of the constant and an
+// integer subtraction from its exponent (exact), so the element pays one FP64
+// multiply for both factors.
+template <typename T> __device__ __forceinline__ T norm_pow(int n, int k) {
+  return sqrt3_pow<T>(n) * (T)(k == 0 ? 1.0f : k == 1 ? 0.5f : k == 2 ? 0.25f : 0.125f);
+}
+template <> __device__ __forceinline__ double norm_pow<double>(int n, int k) {
+  const double c = n == 0 ? 1.0 : n == 1 ? 1.7320508075688772 : n == 2 ? 3.0 : n == 3 ? 5.196152422706632 : 9.0;
+  return __longlong_as_double(__double_as_longlong(c) - ((long long)k << 52));
+}
+// sqrt(5)^n, n <= 4
+template <typename T> __device__ __forceinline__ T sqrt5_pow(int n) {
+  return (T)(n == 0 ? 1.0f : n == 1 ? 2.23606798f : n == 2 ? 5.0f : n == 3 ? 11.1803399f : 25.0f);
+}
+template <> __device__ __forceinline__ double sqrt5_pow<double>(int n) {
+  return n == 0 ? 1.0 : n == 1 ? 2.2360679774997897 : n == 2 ? 5.0 : n == 3 ? 11.180339887498949 : 25.0;
+}
+template <> __device__ __forceinline__ dfl sqrt5_pow<dfl>(int n) {
+  return dfl(n == 0 ? 1.0 : n == 1 ? 2.2360679774997897 : n == 2 ? 5.0 : n == 3 ? 11.180339887498949 : 25.0);
+}
+
 // Element cutoff |v| < cut -> 0 (cut > 0), decided on the bit patterns: for
 // non-negative IEEE values the order of the magnitudes is the integer order of
 // their bits, so no FP64 compare is spent.
@@ -607,7 +662,7 @@ __device__ __forceinline__ void small_prims_impl(const BuildArgs& a, const PairD
     prim_load(bpp + cb, bp);
     prim_load(kpp + cq, kp);
     PrimQuartet<T> pq;
-    prim_setup<T, ATT>(bp, kp, pq, (T)a.inv_mu2);
+    prim_setup<T, ATT, LA + LB == 0>(bp, kp, pq, (T)a.inv_mu2);
     ++nprim;
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
@@ -897,21 +952,43 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
   constexpr int NE = K::NE, KE = (NE + 31) / 32;
   T* V = W;
   const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
+  // the shell-identity factor f = 1/2^k of the digestion (a power of two).  A
+  // Cartesian block takes it in the same multiply as the component norms,
+  // which is exact (V N f == (V N) f bit for bit), and its element cutoff
+  // |V N| < tau becomes |V N f| < tau f; a block without norms is scaled only
+  // when f != 1 (uniform over the warp).  Pure blocks are scaled after the
+  // projection, the Schwarz pass not at all.
+  const int kf = (P.sha == P.shb) + (Q.sha == Q.shb) + (qd.x == qd.y);   // f = 2^-kf
+  const double f = kf == 0 ? 1.0 : kf == 1 ? 0.5 : kf == 2 ? 0.25 : 0.125;
+  const T fT = (T)f;
+  const int kn = (PURE || SCH) ? 0 : kf;   // the halvings the norm multiply carries
+  constexpr bool NORMS = LA >= 2 || LB >= 2 || LC >= 2 || LD >= 2;
   // ---- epilogue: V = normalised block in smem, pure projection in place
   T* Tm = W + NE;
+  if (NORMS || (!PURE && !SCH && f != 1.0)) {
 #pragma unroll (KE <= 8 ? KE : 4)
-  for (int k = 0; k < KE; ++k) {
-    const int e = lane + 32 * k;
-    if (e < NE) {
-      const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
-                id = e % K::ND;
-      // product of the component norms: sqrt(3)^n for n off-diagonal d components,
-      // looked up rather than multiplied out (one FP64 multiply per element)
-      if constexpr (LA == 3 || LB == 3 || LC == 3 || LD == 3) {
-        V[e] *= (T)(cart_norm(LA, ia) * cart_norm(LB, ib) * cart_norm(LC, ic) * cart_norm(LD, id));
-      } else {
-        const int n3 = (LA == 2 && ia >= 3) + (LB == 2 && ib >= 3) + (LC == 2 && ic >= 3) + (LD == 2 && id >= 3);
-        if (LA == 2 || LB == 2 || LC == 2 || LD == 2) V[e] *= sqrt3_pow<T>(n3);
+    for (int k = 0; k < KE; ++k) {
+      const int e = lane + 32 * k;
+      if (e < NE) {
+        const int ia = e / (K::NB * K::NC * K::ND), ib = (e / (K::NC * K::ND)) % K::NB, ic = (e / K::ND) % K::NC,
+                  id = e % K::ND;
+        // product of the component norms: sqrt(3)^n for n off-diagonal d components,
+        // looked up rather than multiplied out (one FP64 multiply per element)
+        if constexpr (NORMS) {
+          // sqrt(3) per off-diagonal d component, sqrt(5) per f component xxy..yzz,
+          // sqrt(15) = sqrt(3) sqrt(5) for xyz (shells_pnrm2)
+          auto c3 = [](int l, int i) { return (l == 2 && i >= 3) || (l == 3 && i == 9); };
+          auto c5 = [](int l, int i) { return l == 3 && i >= 3; };
+          const int n3 = c3(LA, ia) + c3(LB, ib) + c3(LC, ic) + c3(LD, id);
+          if constexpr (LA == 3 || LB == 3 || LC == 3 || LD == 3) {
+            const int n5 = c5(LA, ia) + c5(LB, ib) + c5(LC, ic) + c5(LD, id);
+            V[e] *= norm_pow<T>(n3, kn) * sqrt5_pow<T>(n5);
+          } else {
+            V[e] *= norm_pow<T>(n3, kn);
+          }
+        } else {
+          V[e] *= fT;
+        }
       }
     }
   }
@@ -973,13 +1050,12 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
     return;
   }
   const T cut = (T)a.elem_cut;
-  // the shell-identity factor (a power of two) scales the block once
-  double f = 1.0;
-  if (P.sha == P.shb) f *= 0.5;
-  if (Q.sha == Q.shb) f *= 0.5;
-  if (qd.x == qd.y) f *= 0.5;
-  const T fT = (T)f;
-  for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], cut) * fT;
+  if constexpr (PURE) {
+    for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], cut) * fT;
+  } else {
+    const T cutf = cut * fT;   // the block already carries f (exact)
+    for (int e = lane; e < NEP; e += 32) V[e] = cut_elem(V[e], cutf);
+  }
   // density blocks: up to PJ Coulomb and PK exchange densities per pass (one
   // pass for the SCF builds)
   const int n = a.nbf;

@@ -1073,6 +1073,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
     a.ctas_per_sm = c->tune.ctas_per_sm[cl];
     for (int prec = 0; prec < 2; ++prec) {
       const int li = cl + prec * NCLASS;
+      if (timing && prec == 1) CK(cudaEventRecord(c->evc[cl][2], st));   // FP64 launches done
       if (!B.cap[li]) continue;
       const int fl = prec ? MODE_F32 : (df_on(c) ? MODE_DF : 0);
       a.counters = B.primc.as<unsigned long long>() + li;
@@ -1134,9 +1135,13 @@ void record_stats(oqpg_ctx* c, const BuildBufs& B, int nlaunch, bool timing) {
     S[7 + NCLASS + k] = (double)nprim[k] + (double)nprim[NCLASS + k];
     q32 += (double)cnt[NCLASS + k];
     p32 += (double)nprim[NCLASS + k];
-    float tk = 0;
-    if (timing && (B.cap[k] || B.cap[NCLASS + k])) cudaEventElapsedTime(&tk, c->evc[k][0], c->evc[k][1]);
+    float tk = 0, t32 = 0;
+    if (timing && (B.cap[k] || B.cap[NCLASS + k])) {
+      cudaEventElapsedTime(&tk, c->evc[k][0], c->evc[k][1]);
+      cudaEventElapsedTime(&t32, c->evc[k][2], c->evc[k][1]);
+    }
     S[7 + 2 * NCLASS + k] = tk;
+    S[10 + 3 * NCLASS + k] = t32;
     S[1] += S[7 + NCLASS + k];
   }
   S[0] = nq;
@@ -1428,7 +1433,7 @@ int oqpg_get_tuning(const oqpg_ctx* ctx, int* split_log2, int* chunk, int* ctas_
 
 int oqpg_stats(const oqpg_ctx* ctx, double* out, int n) {
   if (!ctx) return NOT_INIT;
-  for (int i = 0; i < n && i < 10 + 3 * NCLASS; ++i) out[i] = ctx->last_stats[i];
+  for (int i = 0; i < n && i < 10 + 4 * NCLASS; ++i) out[i] = ctx->last_stats[i];
   return OK;
 }
 

@@ -295,6 +295,6 @@ struct oqpg_ctx {
   unsigned long long gcaps[oqpg::NLIST] = {0};
   double grad_stats[5] = {0, 0, 0, 0, 0};  // quartets listed, evaluated, primitive quartets, ms, FP32 listed
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  cudaEvent_t evc[oqpg::NCLASS][2] = {};
-  double last_stats[10 + 3 * oqpg::NCLASS] = {0};
+  cudaEvent_t evc[oqpg::NCLASS][3] = {};   // class start, after its FP64 launches, end
+  double last_stats[10 + 4 * oqpg::NCLASS] = {0};
 };

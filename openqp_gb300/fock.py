@@ -401,14 +401,15 @@ class FockBuilder:
         return q.reshape(ns, ns)
 
     def stats(self):
-        s = np.zeros(10 + 3 * NCLASS)
+        s = np.zeros(10 + 4 * NCLASS)
         lib().oqpg_stats(self.h, ptr(s), len(s))
         return dict(quartets=int(s[0]), prim_quartets=int(s[1]), list_ms=s[2], eri_ms=s[3], total_ms=s[4],
                     nbf=int(s[5]), npair=int(s[6]), per_class=[int(v) for v in s[7:7 + NCLASS]],
                     prim_per_class=[int(v) for v in s[7 + NCLASS:7 + 2 * NCLASS]],
                     ms_per_class=[float(v) for v in s[7 + 2 * NCLASS:7 + 3 * NCLASS]],
                     launches=int(s[7 + 3 * NCLASS]), f32_quartets=int(s[8 + 3 * NCLASS]),
-                    f32_prim_quartets=int(s[9 + 3 * NCLASS]))
+                    f32_prim_quartets=int(s[9 + 3 * NCLASS]),
+                    ms_per_class_f32=[float(v) for v in s[10 + 3 * NCLASS:10 + 4 * NCLASS]])
 
 
 class BatchFockBuilder(FockBuilder):

@@ -30,4 +30,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_mrsf_golden.py <openqp checkout> > mrsf_golden.json")
+    main(sys.argv[1])
