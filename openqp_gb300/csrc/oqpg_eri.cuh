@@ -10,7 +10,7 @@
 // their digested blocks into the same FP64 accumulators.
 //
 //   k_small : one thread per quartet, everything in registers (classes with at
-//             most 27 Cartesian elements).
+//             most 54 Cartesian elements, 27 with an f shell).
 //   k_prim  : heavily contracted small-class quartets, one warp per quartet,
 //             lanes split the primitive loop.
 //   k_team  : one warp per quartet.  Lanes share the primitive loop: Rys
@@ -628,19 +628,56 @@ __device__ __forceinline__ void quartet_geometry(const BuildArgs& a, uint2 qd, P
 }
 
 // ===========================================================================
-// Small classes (at most 27 Cartesian elements): everything in registers.
+// Small classes (at most 54 Cartesian elements, 27 with an f shell):
+// everything in registers.
 //
 // small_prims accumulates the primitive quartets c = first, first + step, ...
 // (c = kq * nP + kb) of one contracted quartet.  Each iteration of the
 // arithmetic body computes one surviving candidate of this lane: the cheap
 // FP32 scan skips screened candidates without holding the warp in the body.
+// The arithmetic body: primitive quartet (bra pair cb, ket pair cq) of one
+// contracted quartet added into acc.
+template <int LA, int LB, int LC, int LD, typename T, bool ATT>
+__device__ __forceinline__ void prim_body(const BuildArgs& a, const typename PrimT<T>::type* bpp,
+                                          const typename PrimT<T>::type* kpp, int cb, int cq, const T AB[3],
+                                          const T CD[3], T* acc) {
+  using K = Cls<LA, LB, LC, LD>;
+  using PP = typename PrimT<T>::type;
+  constexpr int NE = K::NE, NR = K::NR, N2D = K::N2D;
+  PP bp, kp;
+  prim_load(bpp + cb, bp);
+  prim_load(kpp + cq, kp);
+  PrimQuartet<T> pq;
+  prim_setup<T, ATT, LA + LB == 0>(bp, kp, pq, (T)a.inv_mu2);
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    T u, w;
+    rys_node_weight<NR, T>(pq.X, r, a.roots_f32 != 0, u, w);
+    w *= pq.pref;
+    const T uq = u * pq.qi, up = u * pq.pi;
+    const T b00 = (T)0.5 * pq.inv * u;
+    const T b10 = fma(-bp.hp, uq, bp.hp);
+    const T b01 = fma(-kp.hp, up, kp.hp);
+    T I[3][N2D];
+    const T PA[3] = {bp.ax, bp.ay, bp.az}, QC[3] = {kp.ax, kp.ay, kp.az};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const T c00 = fma(-uq, pq.PQ[d], PA[d]);
+      const T d00 = fma(up, pq.PQ[d], QC[d]);
+      twod<LA, LB, LC, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01, AB[d], CD[d],
+                              [&](int i, T v) { I[d][i] = v; });
+    }
+#pragma unroll
+    for (int e = 0; e < NE; ++e)
+      acc[e] = fma(I[0][K::off2d(e, 0)] * I[1][K::off2d(e, 1)], I[2][K::off2d(e, 2)], acc[e]);
+  }
+}
+
 template <int LA, int LB, int LC, int LD, typename T, bool ATT>
 __device__ __forceinline__ void small_prims_impl(const BuildArgs& a, const PairDev& P, const PairDev& Q,
                                                  const T AB[3], const T CD[3], int first, int step, T* acc,
                                                  unsigned long long& nprim) {
-  using K = Cls<LA, LB, LC, LD>;
   using PP = typename PrimT<T>::type;
-  constexpr int NE = K::NE, NR = K::NR, N2D = K::N2D;
   const PP* bpp = prims_of<T>(a) + P.poff;
   const PP* kpp = prims_of<T>(a) + Q.poff;
   const int nP = P.pcnt, nQ = Q.pcnt;
@@ -658,34 +695,8 @@ __device__ __forceinline__ void small_prims_impl(const BuildArgs& a, const PairD
       if (screen_keep(bpp + b, prim_screen(bpp + b), kpp + q, ks, a)) { cb = b; cq = q; break; }
     }
     if (cb < 0) break;
-    PP bp, kp;
-    prim_load(bpp + cb, bp);
-    prim_load(kpp + cq, kp);
-    PrimQuartet<T> pq;
-    prim_setup<T, ATT, LA + LB == 0>(bp, kp, pq, (T)a.inv_mu2);
     ++nprim;
-#pragma unroll
-    for (int r = 0; r < NR; ++r) {
-      T u, w;
-      rys_node_weight<NR, T>(pq.X, r, a.roots_f32 != 0, u, w);
-      w *= pq.pref;
-      const T uq = u * pq.qi, up = u * pq.pi;
-      const T b00 = (T)0.5 * pq.inv * u;
-      const T b10 = fma(-bp.hp, uq, bp.hp);
-      const T b01 = fma(-kp.hp, up, kp.hp);
-      T I[3][N2D];
-      const T PA[3] = {bp.ax, bp.ay, bp.az}, QC[3] = {kp.ax, kp.ay, kp.az};
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const T c00 = fma(-uq, pq.PQ[d], PA[d]);
-        const T d00 = fma(up, pq.PQ[d], QC[d]);
-        twod<LA, LB, LC, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01, AB[d], CD[d],
-                                [&](int i, T v) { I[d][i] = v; });
-      }
-#pragma unroll
-      for (int e = 0; e < NE; ++e)
-        acc[e] = fma(I[0][K::off2d(e, 0)] * I[1][K::off2d(e, 1)], I[2][K::off2d(e, 2)], acc[e]);
-    }
+    prim_body<LA, LB, LC, LD, T, ATT>(a, bpp, kpp, cb, cq, AB, CD, acc);
   }
 }
 
@@ -696,6 +707,67 @@ __device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P
                                             const T CD[3], int first, int step, T* acc, unsigned long long& nprim) {
   if (a.inv_mu2 != 0.0) small_prims_impl<LA, LB, LC, LD, T, true>(a, P, Q, AB, CD, first, step, acc, nprim);
   else small_prims_impl<LA, LB, LC, LD, T, false>(a, P, Q, AB, CD, first, step, acc, nprim);
+}
+
+// All 32 lanes of a warp on the primitive quartets of ONE contracted quartet
+// (the primitive-parallel kernels).  The lanes screen a window of 32
+// candidates (one each, FP32), and the survivors are dealt to the lanes that
+// hold none, in order; the arithmetic body runs only when every lane holds a
+// survivor (or the candidates are exhausted), so its FP64 instructions issue
+// on 32 lanes instead of on the lanes whose stride-32 slice happened to keep
+// a candidate.  Each lane accumulates its survivors into its own acc; the
+// caller reduces over the warp.
+template <int LA, int LB, int LC, int LD, typename T, bool ATT>
+__device__ __forceinline__ void warp_prims_impl(const BuildArgs& a, const PairDev& P, const PairDev& Q,
+                                                const T AB[3], const T CD[3], int lane, T* acc,
+                                                unsigned long long& nprim) {
+  using PP = typename PrimT<T>::type;
+  const PP* bpp = prims_of<T>(a) + P.poff;
+  const PP* kpp = prims_of<T>(a) + Q.poff;
+  const int nP = P.pcnt, nQ = Q.pcnt;
+  const int total = nP * nQ;
+  int hb = 0, hq = 0;   // the survivor this lane holds
+  int held = 0;         // lanes [0, held) hold one (uniform over the warp)
+  for (int w = 0; w < total; w += 32) {
+    const int c = w + lane;
+    bool keep = false;
+    int cb = 0, cq = 0;
+    if (c < total) {
+      cq = c / nP;
+      cb = c - cq * nP;
+      keep = screen_keep(bpp + cb, prim_screen(bpp + cb), kpp + cq, prim_screen(kpp + cq), a);
+    }
+    unsigned m = __ballot_sync(0xffffffffu, keep);
+    while (m) {
+      const int s = __popc(m);
+      const int take = s < 32 - held ? s : 32 - held;
+      // lane held + j receives the (j+1)-th surviving candidate of the window
+      const int j = lane - held;
+      const bool mine = j >= 0 && j < take;
+      const int src = mine ? (int)__fns(m, 0, j + 1) : 0;
+      const int sb = __shfl_sync(0xffffffffu, cb, src), sq = __shfl_sync(0xffffffffu, cq, src);
+      if (mine) { hb = sb; hq = sq; }
+      const unsigned last = __fns(m, 0, take);   // position of the last survivor taken
+      m = last >= 31u ? 0u : (m & ~((2u << last) - 1u));
+      held += take;
+      if (held == 32) {
+        nprim += 1;
+        prim_body<LA, LB, LC, LD, T, ATT>(a, bpp, kpp, hb, hq, AB, CD, acc);
+        held = 0;
+      }
+    }
+  }
+  if (lane < held) {
+    nprim += 1;
+    prim_body<LA, LB, LC, LD, T, ATT>(a, bpp, kpp, hb, hq, AB, CD, acc);
+  }
+}
+
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void warp_prims(const BuildArgs& a, const PairDev& P, const PairDev& Q, const T AB[3],
+                                           const T CD[3], int lane, T* acc, unsigned long long& nprim) {
+  if (a.inv_mu2 != 0.0) warp_prims_impl<LA, LB, LC, LD, T, true>(a, P, Q, AB, CD, lane, acc, nprim);
+  else warp_prims_impl<LA, LB, LC, LD, T, false>(a, P, Q, AB, CD, lane, acc, nprim);
 }
 
 // Normalisation, pure projection, element cutoff and digestion of one
@@ -885,7 +957,7 @@ __global__ void __launch_bounds__(128) k_prim(const BuildArgs a) {
     T acc[NE];
 #pragma unroll
     for (int e = 0; e < NE; ++e) acc[e] = 0;
-    small_prims<LA, LB, LC, LD, T>(a, P, Q, AB, CD, lane, 32, acc, nprim);
+    warp_prims<LA, LB, LC, LD, T>(a, P, Q, AB, CD, lane, acc, nprim);
 #pragma unroll
     for (int e = 0; e < NE; ++e) {
       T v = acc[e];
@@ -1317,7 +1389,7 @@ __global__ void __launch_bounds__(128) k_prim_team(const BuildArgs a) {
     T acc[MP];
 #pragma unroll
     for (int e = 0; e < MP; ++e) acc[e] = 0;
-    small_prims<LA, LB, LC, LD, T>(a, P, Q, AB, CD, lane, 32, acc, nprim);
+    warp_prims<LA, LB, LC, LD, T>(a, P, Q, AB, CD, lane, acc, nprim);
     // reduce-scatter over the 32 lanes: at each level keep the half selected
     // by the lane bit, add the partner's copy of it
 #pragma unroll
@@ -1398,7 +1470,7 @@ __global__ void __launch_bounds__(128) k_prim_df(const BuildArgs a) {
     dfl acc[NE];
 #pragma unroll
     for (int e = 0; e < NE; ++e) acc[e] = dfl();
-    small_prims<LA, LB, LC, LD, dfl>(a, P, Q, AB, CD, lane, 32, acc, nprim);
+    warp_prims<LA, LB, LC, LD, dfl>(a, P, Q, AB, CD, lane, acc, nprim);
     double accd[NE];
 #pragma unroll
     for (int e = 0; e < NE; ++e) {

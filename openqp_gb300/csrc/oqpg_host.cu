@@ -15,7 +15,7 @@
 namespace oqpg {
 
 static const ClassInfo kClasses[NCLASS] = {
-#define C_(a, b, c, d) {{a, b, c, d}, (ncart(a) * ncart(b) * ncart(c) * ncart(d) > 27), prim_parallel(a, b, c, d)}
+#define C_(a, b, c, d) {{a, b, c, d}, team_class(a, b, c, d), prim_parallel(a, b, c, d)}
     C_(0, 0, 0, 0), C_(0, 0, 0, 1), C_(0, 0, 0, 2), C_(0, 0, 1, 1), C_(0, 0, 1, 2), C_(0, 0, 2, 2),
     C_(0, 1, 0, 1), C_(0, 1, 0, 2), C_(0, 1, 1, 1), C_(0, 1, 1, 2), C_(0, 1, 2, 2),
     C_(0, 2, 0, 2), C_(0, 2, 1, 1), C_(0, 2, 1, 2), C_(0, 2, 2, 2),

@@ -36,9 +36,10 @@ constexpr int team_warps() {
   return per_warp * 4 <= budget ? 4 : (per_warp * 2 <= budget ? 2 : 1);
 }
 
-// Classes with more than 27 Cartesian elements run one warp per quartet.
+// Classes with more than 54 Cartesian elements (27 with an f shell) run one
+// warp per quartet.
 template <int LA, int LB, int LC, int LD>
-constexpr bool is_team() { return Cls<LA, LB, LC, LD>::NE > 27; }
+constexpr bool is_team() { return team_class(LA, LB, LC, LD); }
 
 template <int LA, int LB, int LC, int LD, bool PURE, typename T>
 cudaError_t launch_fock(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
