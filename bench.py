@@ -36,11 +36,12 @@ sys.path.insert(0, ROOT)
 
 WORKLOADS = {
     # the headline workload (the metric's configuration)
-    # traffic: DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per build of a class's
-    # launches (k_prim head + k_small), from one-pass ncu captures of this workload's bench command
+    # traffic: DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per build of the
+    # dominant class, scaled by quartets from a one-launch ncu capture of the same kernel on
+    # (H2O)16 6-31G(d): 15.02 MB for 1 648 969 (ss|sp) quartets, 9.11 bytes each (the 8-byte list
+    # entry; pairs and densities stay in L2), x 34 830 594 quartets here
     "water32_ccpvdz": dict(name="(H2O)32 cc-pVDZ spherical RHF J+K Fock build", nwater=32, edge=14.0, seed=0,
-                           basis="cc-pvdz", cutoff=1e-10,
-                           traffic={"(ss|sp)": 300.9e6, "(ss|ss)": 171.8e6, "(sp|sp)": 139.7e6}),
+                           basis="cc-pvdz", cutoff=1e-10, traffic={"(ss|sp)": 317.2e6}),
     # the plain-FP64 parity configuration
     "water4_631gd": dict(name="(H2O)4 6-31G(d) Cartesian RHF J+K Fock build", nwater=4, edge=6.0, seed=0,
                          basis="6-31g(d)", cutoff=1e-10),
@@ -882,7 +883,7 @@ def run_ours(args):
                 "roofline": {"bound": "fp64", "kernel": labels[cdom], "achieved": achieved, "peak": peak,
                              "unit": "TFLOP/s", "frac": achieved / peak,
                              "traffic": WORKLOAD.get("traffic", {}).get(labels[cdom]),
-                             "traffic_unit": "DRAM bytes per build of the class (ncu)",
+                             "traffic_unit": "DRAM bytes per build of the class (ncu, scaled from a small case)",
                              "peak_source": "measured: FP64 FMA-chain probe on this device",
                              "kernel_ms": float(ms[cdom]), "build_fp64_tflops": total_flops / (tsum / args.steps) / 1e12},
                 "quartets_per_s": s0["quartets"] / (tsum / args.steps),
