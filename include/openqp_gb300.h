@@ -86,6 +86,20 @@ int routec_fock_set_precision(int mode, double threshold);
  * style. */
 void routec_fock_set_cutoff(const double* cutoff, int* info);
 
+/* Petite list of the process-global context (oqpg_set_symmetry) from
+ * OpenQP's own symmetry arrays, as pyoqp stages them for
+ * int2_compute_t_enable_petite and symmetrize_skeleton_signed
+ * (source/integrals/int2.F90:312-365, source/scf_addons.F90:1563-1615):
+ * shell_map[(op-1)*nshell + s] and ao_target[(op-1)*nbf + mu] the 1-based
+ * images of shell s and AO mu under operation op (integer(8), tagarrays
+ * OQP_sym_shell_map, OQP_sym_ao_target), ao_sign[(op-1)*nbf + mu] = +-1
+ * (OQP_sym_ao_sign).  *nops <= 1 switches the reduction off.  The seam still
+ * returns the complete Fock matrix.  *info = 0, 1 (not initialised) or 3
+ * (not an abelian group of signed AO permutations of this basis).  All
+ * arguments by reference, Fortran style. */
+void routec_fock_set_symmetry(const int* nops, const long long* shell_map, const long long* ao_target,
+                              const double* ao_sign, int* info);
+
 /* The reference's 2e-gradient seam (source/modules/routec_bridge.F90:51-61,
  * 241, 292-310; caller source/modules/hf_gradient.F90:270-289): d is the
  * packed total RHF density, xyz(3, natm) in Bohr must be the geometry
@@ -325,6 +339,27 @@ int oqpg_set_precision(oqpg_ctx* ctx, int mode, double threshold);
  * the current cutoff (-1 for a null context). */
 int oqpg_set_cutoff(oqpg_ctx* ctx, double cutoff);
 double oqpg_get_cutoff(const oqpg_ctx* ctx);
+
+/* Petite list (symmetry reduction) of the following SCF builds of a
+ * single-molecule context: the petite-list path of OpenQP's int2_twoei
+ * (source/integrals/int2.F90:411-469, 781-795) with the skeleton
+ * symmetrisation of fock_jk (source/scf_addons.F90:1205, 1563-1615), abelian
+ * groups.  nops (2, 4 or 8) operations, each a signed permutation of the AOs:
+ * shell_map[op*nshell + s] = the shell that op maps shell s onto (same angular
+ * momentum), ao_target[op*nbf + mu] = AO i of that shell for AO i of shell s,
+ * ao_sign[op*nbf + mu] = +-1; 0-based.  The operations must form a group.  A
+ * build computes one quartet per orbit, weighted by the orbit size, and
+ * returns the projection of the skeleton matrix onto the totally symmetric
+ * component: the complete Fock matrix.  Each build checks on the device that
+ * its densities are invariant (max |P(D) - D| <= 1e-6 max |D|, as
+ * petite_density_asymmetry, scf_addons.F90:1250-1274) and builds every
+ * quartet otherwise.  Response, CAM, gradient and no-alloc builds ignore it.
+ * nops <= 1 switches it off.  Returns 0, 1 (null context) or 3 (a batch
+ * context, or maps that are not a group of signed AO permutations).
+ * oqpg_symmetry_info: the group order (1 without) and whether the last direct
+ * build used the reduction. */
+int oqpg_set_symmetry(oqpg_ctx* ctx, int nops, const int* shell_map, const int* ao_target, const double* ao_sign);
+int oqpg_symmetry_info(const oqpg_ctx* ctx, int* nops, int* reduced);
 
 /* Statistics of the last build, up to n (<= 230) doubles:
  * [0] quartets computed, [1] primitive quartets, [2] list build ms,

@@ -50,6 +50,11 @@ def lib():
         L.oqpg_get_cutoff.restype = ctypes.c_double
         L.routec_fock_set_cutoff.argtypes = [_d, _i]
         L.routec_fock_set_cutoff.restype = None
+        L.oqpg_set_symmetry.argtypes = [ctypes.c_void_p, ctypes.c_int, _i, _i, _d]
+        L.oqpg_symmetry_info.argtypes = [ctypes.c_void_p, _i, _i]
+        _ll = ctypes.POINTER(ctypes.c_longlong)
+        L.routec_fock_set_symmetry.argtypes = [_i, _ll, _ll, _d, _i]
+        L.routec_fock_set_symmetry.restype = None
         L.routec_fock_init.argtypes = [ctypes.c_int, _i, _i, _i, _d, _d, _i, ctypes.c_int, _d, ctypes.c_double]
         L.routec_fock_jk.argtypes = [_d, _d, _i, _i, _d, _d, _i]
         L.routec_fock_jk.restype = None

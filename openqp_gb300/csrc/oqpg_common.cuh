@@ -46,6 +46,13 @@ struct PairDev {
   int poff, pcnt;  // primitive-pair range
 };
 
+// A quartet-list entry is (bra pair, ket pair).  With the petite list the two
+// top bits of the bra pair index carry log2 of the quartet's orbit weight
+// (1, 2, 4 or 8 symmetry-equivalent quartets); pair indices stay below 2^30.
+constexpr unsigned PAIR_MASK = 0x3fffffffu;
+__host__ __device__ inline unsigned entry_pair(unsigned x) { return x & PAIR_MASK; }
+__host__ __device__ inline int entry_wlog2(unsigned x) { return (int)(x >> 30); }
+
 // Parameters of one Fock build (or Schwarz pass) shared by the class kernels.
 struct BuildArgs {
   const ShellDev* shells;

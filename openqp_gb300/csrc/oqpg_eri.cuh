@@ -561,12 +561,12 @@ __device__ __constant__ const float2 SQRT3_POW_DF[5] = {{1.0f, 0.0f},
                                                        {9.0f, 0.0f}};
 template <> __device__ __forceinline__ dfl sqrt3_pow<dfl>(int n) { return dfl(SQRT3_POW_DF[n].x, SQRT3_POW_DF[n].y); }
 
-// sqrt(3)^n / 2^k, n <= 4, k <= 3: the component norms of a Cartesian element
-// times the shell-identity factor 2^-k.  FP64: a select of the constant and an
+// sqrt(3)^n / 2^k, n <= 4, |k| <= 3: the component norms of a Cartesian element
+// times the shell-identity factor and the petite-list weight, 2^-k.  FP64: a select of the constant and an
 // integer subtraction from its exponent (exact), so the element pays one FP64
 // multiply for both factors.
 template <typename T> __device__ __forceinline__ T norm_pow(int n, int k) {
-  return sqrt3_pow<T>(n) * (T)(k == 0 ? 1.0f : k == 1 ? 0.5f : k == 2 ? 0.25f : 0.125f);
+  return sqrt3_pow<T>(n) * (T)__int_as_float((127 - k) << 23);   // 2^-k, |k| <= 3
 }
 template <> __device__ __forceinline__ double norm_pow<double>(int n, int k) {
   const double c = n == 0 ? 1.0 : n == 1 ? 1.7320508075688772 : n == 2 ? 3.0 : n == 3 ? 5.196152422706632 : 9.0;
@@ -620,7 +620,7 @@ __device__ __forceinline__ void work_range(const BuildArgs& a, const uint2*& q, 
 template <typename T>
 __device__ __forceinline__ void quartet_geometry(const BuildArgs& a, uint2 qd, PairDev& P, PairDev& Q, T AB[3],
                                                  T CD[3]) {
-  P = a.pairs[qd.x];
+  P = a.pairs[entry_pair(qd.x)];
   Q = a.pairs[qd.y];
   const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
   AB[0] = (T)(SA.x - SB.x); AB[1] = (T)(SA.y - SB.y); AB[2] = (T)(SA.z - SB.z);
@@ -800,10 +800,9 @@ __device__ __forceinline__ void small_epilogue(const BuildArgs& a, uint2 qd, con
   const T cut = (T)a.elem_cut;
   // the shell-identity factor f (a power of two) scales the block once, not
   // every digested target: exact, and NEP multiplies instead of one per atomic
-  double f = 1.0;
-  if (P.sha == P.shb) f *= 0.5;
-  if (Q.sha == Q.shb) f *= 0.5;
-  if (qd.x == qd.y) f *= 0.5;
+  // times the petite-list orbit weight 2^w (w = 0 without symmetry)
+  const int kf = (P.sha == P.shb) + (Q.sha == Q.shb) + (entry_pair(qd.x) == qd.y) - entry_wlog2(qd.x);
+  const double f = __longlong_as_double((long long)(1023 - kf) << 52);   // 2^-kf, exact
   const T fT = (T)f;
 #pragma unroll
   for (int e = 0; e < E::NEP; ++e) V[e] = cut_elem(V[e], cut) * fT;
@@ -1030,8 +1029,9 @@ __device__ __forceinline__ void team_epilogue(const BuildArgs& a, uint2 qd, cons
   // |V N| < tau becomes |V N f| < tau f; a block without norms is scaled only
   // when f != 1 (uniform over the warp).  Pure blocks are scaled after the
   // projection, the Schwarz pass not at all.
-  const int kf = (P.sha == P.shb) + (Q.sha == Q.shb) + (qd.x == qd.y);   // f = 2^-kf
-  const double f = kf == 0 ? 1.0 : kf == 1 ? 0.5 : kf == 2 ? 0.25 : 0.125;
+  // f = 2^-kf; the petite-list orbit weight 2^w of the entry enters as -w (w = 0 without symmetry)
+  const int kf = (P.sha == P.shb) + (Q.sha == Q.shb) + (entry_pair(qd.x) == qd.y) - entry_wlog2(qd.x);
+  const double f = __longlong_as_double((long long)(1023 - kf) << 52);   // 2^-kf, exact
   const T fT = (T)f;
   const int kn = (PURE || SCH) ? 0 : kf;   // the halvings the norm multiply carries
   constexpr bool NORMS = LA >= 2 || LB >= 2 || LC >= 2 || LD >= 2;

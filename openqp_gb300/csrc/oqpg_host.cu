@@ -148,6 +148,31 @@ __global__ void k_dsh(const double* __restrict__ dp, int nfocks, const MolDev* _
 }
 
 
+// Petite-list weight of the canonical quartet (i, j, k, l) (i >= j, k >= l,
+// (i, j) >= (k, l); molecule-local shells) under an abelian group given by the
+// shell images map[op ns + s] (petite_quartet_weight, int2.F90:411-469): -1
+// when some operation maps it onto a lexicographically larger canonical
+// quartet (it is skipped), else log2 of the orbit size nops / |stabiliser|.
+__device__ int petite_wlog2(const int* __restrict__ map, int nops, int ns, int i, int j, int k, int l) {
+  int nstab = 0;
+  for (int op = 0; op < nops; ++op) {
+    const int* m = map + op * ns;
+    int a1 = __ldg(m + i), a2 = __ldg(m + j), b1 = __ldg(m + k), b2 = __ldg(m + l);
+    if (a1 < a2) { const int t = a1; a1 = a2; a2 = t; }
+    if (b1 < b2) { const int t = b1; b1 = b2; b2 = t; }
+    if (a1 < b1 || (a1 == b1 && a2 < b2)) {
+      int t = a1; a1 = b1; b1 = t;
+      t = a2; a2 = b2; b2 = t;
+    }
+    if (a1 != i) { if (a1 > i) return -1; }
+    else if (a2 != j) { if (a2 > j) return -1; }
+    else if (b1 != k) { if (b1 > k) return -1; }
+    else if (b2 != l) { if (b2 > l) return -1; }
+    else ++nstab;
+  }
+  return __ffs(nops / nstab) - 1;   // nops is a power of two, so is the orbit size
+}
+
 // Screened quartet lists, one CTA per bra pair P (the larger pair index of the
 // canonical quartet, int2.F90:755-805): pair screen Q_P Dmax >= tau, then for
 // every Q <= P the quartet screen Q_P Q_Q max(4D_ij, 4D_kl, D_jl, D_jk, D_il, D_ik)
@@ -193,6 +218,13 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
   const float dij4 = 4.0f * di[ij.y];
   const float tlo = (float)(a.tau * (1.0 - 1e-5)), thi = (float)(a.tau * (1.0 + 1e-5));
   const float mlo = (float)(a.tau_f32 * (1.0 - 1e-5)), mhi = (float)(a.tau_f32 * (1.0 + 1e-5));
+  // the petite list applies when the density is invariant under the group
+  bool petite = false;
+  if (a.sym_nops > 1) {
+    const double resid = __longlong_as_double((long long)a.sym_bits[0]);
+    const double scale = __longlong_as_double((long long)a.sym_bits[1]);
+    petite = resid <= 1e-6 * scale;
+  }
   for (int s0 = 0; s0 < len; s0 += blockDim.x) {
     if (threadIdx.x < 2 * NCLASS) cnt[threadIdx.x] = 0;
     __syncthreads();
@@ -222,6 +254,11 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
         t = exact();
         pass = !(t < a.tau);
       }
+      int wl = 0;
+      if (pass && petite) {
+        wl = petite_wlog2(a.sym_map, a.sym_nops, a.sym_ns, ij.x, ij.y, kl.x, kl.y);
+        pass = wl >= 0;
+      }
       if (pass) {
         bool f32 = false;
         if (a.tau_f32 > 0.0) {
@@ -234,6 +271,7 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
         const int tQ = a.pair_type[Q];
         if (tP <= tQ) { c = class_index(tP, tQ); ent = make_uint2(P, Q); }
         else { c = class_index(tQ, tP); ent = make_uint2(Q, P); }
+        ent.x |= (unsigned)wl << 30;   // orbit weight 2^wl (petite list)
         if (f32 && !class_has_f(c)) c += NCLASS;  // f classes have FP64 kernels only
         slot = atomicAdd(&cnt[c], 1u);
       }
@@ -273,11 +311,11 @@ __device__ __forceinline__ int work_bin(int n) {
 }
 
 __device__ __forceinline__ int prim_bin(const PairDev* pairs, uint2 q) {
-  return work_bin(pairs[q.x].pcnt * pairs[q.y].pcnt);
+  return work_bin(pairs[entry_pair(q.x)].pcnt * pairs[q.y].pcnt);
 }
 
 __device__ __forceinline__ int survivor_bin(const PairDev* pairs, const PrimPair* prims, uint2 q, float lo) {
-  const PairDev P = pairs[q.x], Q = pairs[q.y];
+  const PairDev P = pairs[entry_pair(q.x)], Q = pairs[q.y];
   // the heaviest quartets go to the primitive-parallel kernels whatever their
   // exact count: bin them by the product and spare the scan
   if (P.pcnt * Q.pcnt > 512) return work_bin(P.pcnt * Q.pcnt);
@@ -753,6 +791,7 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
     stride = std::max(stride, M.nbf);
   }
   c->nbf = row0; c->stride = stride; c->ntri = tri0; c->dsh_elems = dsh0; c->npair = pair0;
+  if ((unsigned)pair0 > PAIR_MASK) return UNSUPPORTED;   // quartet entries keep two bits of the pair index
   c->h_am = am; c->h_ncontr = ncontr; c->h_poff = poff;
   c->h_ex.assign(ex, ex + off); c->h_cc.assign(cc, cc + off);
   c->shell_atom.resize(nshell);
@@ -873,6 +912,10 @@ int ensure_bufs(oqpg_ctx* c, BuildBufs& B, const Job& job) {
   CK(B.caps.ensure(sizeof(unsigned long long) * NLIST));
   CK(B.split.ensure(sizeof(int) * NLIST));
   CK(B.flag.ensure(sizeof(unsigned)));
+  if (petite_on(c, job)) {
+    CK(B.sym.ensure(sizeof(unsigned long long) * 2));
+    CK(B.fsk.ensure(sizeof(double) * (size_t)c->ntri * std::max(job.nfocks, 1)));
+  }
   if (!B.h_rb) CK(cudaMallocHost(&B.h_rb, sizeof(unsigned long long) * (1 + 2 * NLIST)));
   return OK;
 }
@@ -895,6 +938,12 @@ ListArgs list_args(const oqpg_ctx* c, BuildBufs& B, const Job& job) {
   la.tau_f32 = split_on(c) ? c->tau_f32 : 0.0;
   la.counts = B.counts.as<unsigned long long>();
   for (int k = 0; k < NLIST; ++k) { la.lists[k] = B.lists[k].as<uint2>(); la.caps[k] = B.cap[k]; }
+  if (petite_on(c, job)) {
+    la.sym_map = c->d_sym_map.as<int>();
+    la.sym_nops = c->sym_nops;
+    la.sym_ns = c->nshell;
+    la.sym_bits = B.sym.as<unsigned long long>();
+  }
   return la;
 }
 
@@ -933,6 +982,7 @@ int issue_densities(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st) 
       c->d_aoff.as<int>(), c->d_naos.as<int>(), B.dsh.as<double>(), B.dshf.as<float>(),
       B.dmax.as<unsigned long long>());
   CK(cudaGetLastError());
+  if (petite_on(c, job)) return petite_check(c, B, job, st);
   return OK;
 }
 
@@ -1097,6 +1147,8 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   if (timing) CK(cudaEventRecord(c->ev[2], st));
   if (job.gen) {
     if ((rc = gen_finalize(c, B, *job.gen, st))) return rc;
+  } else if (petite_on(c, job)) {
+    if ((rc = petite_finalize(c, B, job, (nk == 1) ? 0.5 * job.se : job.se, st))) return rc;
   } else {
     const double ck = (nk == 1) ? 0.5 * job.se : job.se;
     k_finalize<<<(unsigned)std::min<long long>((c->ntri + 255) / 256, c->nsm * 8LL), 256, 0, st>>>(
@@ -1206,9 +1258,12 @@ int cam_build(oqpg_ctx* c, const double* dp, double* f, int nfocks, const double
   if (!cam || !(cam[2] > 0.0)) return UNSUPPORTED;
   int rc;
   if ((rc = ensure_att(c, cam[2]))) return rc;
-  if ((rc = ctx_build(c, packed_job(dp, f, nullptr, nfocks, cam[0], cam[3]), st))) return rc;
+  Job j1 = packed_job(dp, f, nullptr, nfocks, cam[0], cam[3]);
+  j1.petite = false;   // the petite list serves plain SCF builds only
+  if ((rc = ctx_build(c, j1, st))) return rc;
   Job j2 = packed_job(dp, f, f, nfocks, cam[1], cam[4]);
   j2.inv_mu2 = 1.0 / (cam[2] * cam[2]);
+  j2.petite = false;
   return ctx_build(c, j2, st);
 }
 
@@ -1546,6 +1601,27 @@ int oqpg_set_cutoff(oqpg_ctx* ctx, double cutoff) {
 }
 
 double oqpg_get_cutoff(const oqpg_ctx* ctx) { return ctx ? ctx->tau : -1.0; }
+
+// OpenQP's symmetry data (tagarrays OQP_sym_shell_map, OQP_sym_ao_target,
+// OQP_sym_ao_sign: 1-based images, the shell or AO index fastest) for the
+// process-global context.
+void routec_fock_set_symmetry(const int* nops, const long long* shell_map, const long long* ao_target,
+                              const double* ao_sign, int* info) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  int rc;
+  if (!g_ctx) rc = NOT_INIT;
+  else if (!nops) rc = UNSUPPORTED;
+  else if (*nops <= 1) rc = oqpg_set_symmetry(g_ctx, 0, nullptr, nullptr, nullptr);
+  else if (!shell_map || !ao_target || !ao_sign || *nops > 8) rc = UNSUPPORTED;
+  else {
+    const int k = *nops, ns = g_ctx->nshell, n = g_ctx->nbf;
+    std::vector<int> sm((size_t)k * ns), at((size_t)k * n);
+    for (size_t i = 0; i < sm.size(); ++i) sm[i] = (int)shell_map[i] - 1;
+    for (size_t i = 0; i < at.size(); ++i) at[i] = (int)ao_target[i] - 1;
+    rc = oqpg_set_symmetry(g_ctx, k, sm.data(), at.data(), ao_sign);
+  }
+  if (info) *info = rc;
+}
 
 void routec_fock_set_cutoff(const double* cutoff, int* info) {
   std::lock_guard<std::mutex> lk(g_mutex);

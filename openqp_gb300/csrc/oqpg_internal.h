@@ -58,6 +58,13 @@ struct ListArgs {
   uint2* lists[2 * NCLASS];
   unsigned long long caps[2 * NCLASS];
   int write;
+  // petite list (one molecule): shell images of the symmetry operations,
+  // map[op ns + s]; sym_bits = (density asymmetry, density scale) as FP64 bits,
+  // the reduction applies when asymmetry <= 1e-6 scale
+  const int* sym_map;
+  int sym_nops;
+  int sym_ns;
+  const unsigned long long* sym_bits;
 };
 
 struct DevBuf {
@@ -156,6 +163,7 @@ struct Job {
   double se = 1.0, sc = 1.0;
   const GenJob* gen = nullptr;
   double inv_mu2 = 0.0;  // erf(mu r)/r pass of a CAM build (needs ensure_att(mu) first)
+  bool petite = true;    // the context's petite list may apply (plain SCF builds of packed densities)
   int nj() const { return gen ? gen->nj : 1; }
   int nk() const { return gen ? gen->nk : nfocks; }
 };
@@ -188,6 +196,12 @@ int gen_finalize(oqpg_ctx* c, BuildBufs& B, const GenJob& g, cudaStream_t st);
 bool split_on(const oqpg_ctx* c);
 bool df_on(const oqpg_ctx* c);
 int ctx_build(oqpg_ctx* c, const Job& job, cudaStream_t st);
+// petite list (oqpg_petite.cu): whether it applies to a job, the density
+// invariance check (before the lists) and the symmetrisation of the skeleton
+// Fock matrix (in place of the plain finalize)
+bool petite_on(const oqpg_ctx* c, const Job& job);
+int petite_check(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st);
+int petite_finalize(oqpg_ctx* c, BuildBufs& B, const Job& job, double ck, cudaStream_t st);
 int ensure_att(oqpg_ctx* c, double mu);
 
 // Layout of an MRSF-type operand: component m of vector v, element (r, c) at
@@ -211,14 +225,14 @@ constexpr int NLIST = 2 * NCLASS;  // FP64 lists, then the FP32 lists of the pre
 // direct builds and one owned by its captured graph).
 struct BuildBufs {
   DevBuf dj, dk, djf, dkf, djdf, dkdf, gj, gk, dsh, dshf, dmax, counts, primc, hist, cursor, work, ranges, caps,
-      split, flag, gtab;
+      split, flag, gtab, sym, fsk;
   DevBuf lists[NLIST], slists[NLIST], bins[NLIST];
   unsigned long long cap[NLIST] = {0};
   bool sized = false;
   unsigned long long* h_rb = nullptr;  // pinned readback: [0] flag, [1, 1+NLIST) counts, then primitive counts
   void release() {
     DevBuf* b[] = {&dj, &dk, &djf, &dkf, &djdf, &dkdf, &gj, &gk, &dsh, &dshf, &dmax, &counts, &primc, &hist,
-                   &cursor, &work, &ranges, &caps, &split, &flag, &gtab};
+                   &cursor, &work, &ranges, &caps, &split, &flag, &gtab, &sym, &fsk};
     for (DevBuf* x : b) x->release();
     for (auto& x : lists) x.release();
     for (auto& x : slists) x.release();
@@ -259,6 +273,9 @@ struct oqpg_ctx {
   std::vector<int> h_am, h_ncontr, h_poff, shell_atom;
   std::vector<double> h_ex, h_cc;
   oqpg_tuning tune;
+  // petite list: nops >= 2 symmetry operations (abelian: signed AO permutations)
+  int sym_nops = 0;
+  oqpg::DevBuf d_sym_map, d_sym_inv, d_sym_sgn;   // shell images; AO preimages and their signs
   // precision split: 0 = every quartet in FP64, 1 = bound < tau_f32 in FP32
   int precision_mode = 0;
   double tau_f32 = 0.0;

@@ -310,6 +310,30 @@ class FockBuilder:
             raise FockError(rc, "oqpg_set_cutoff")
         self.cutoff = float(cutoff)
 
+    def set_symmetry(self, sym=None):
+        """Petite list of the following SCF builds: sym = (nops, shell_map,
+        ao_target, ao_sign) as openqp_gb300.symmetry.abelian_symmetry returns
+        (0-based); None or nops <= 1 switches it off.  The builds still return
+        the complete Fock matrix."""
+        if sym is None or int(sym[0]) <= 1:
+            rc = lib().oqpg_set_symmetry(self.h, 0, None, None, None)
+        else:
+            nops, sm, at, sg = sym
+            self._sym = (np.ascontiguousarray(sm, dtype=np.int32), np.ascontiguousarray(at, dtype=np.int32),
+                         np.ascontiguousarray(sg, dtype=np.float64))
+            rc = lib().oqpg_set_symmetry(self.h, int(nops), ptr(self._sym[0], _i), ptr(self._sym[1], _i),
+                                         ptr(self._sym[2]))
+        if rc != 0:
+            raise FockError(rc, "oqpg_set_symmetry")
+
+    def symmetry_info(self):
+        """(group order, whether the last direct build used the reduction)"""
+        n, r = ctypes.c_int(0), ctypes.c_int(0)
+        rc = lib().oqpg_symmetry_info(self.h, ctypes.byref(n), ctypes.byref(r))
+        if rc != 0:
+            raise FockError(rc, "oqpg_symmetry_info")
+        return n.value, bool(r.value)
+
     def get_cutoff(self):
         """The cutoff the library applies to the next build."""
         return lib().oqpg_get_cutoff(self.h)
@@ -529,6 +553,24 @@ def routec_fock_set_cutoff(cutoff):
     c = ctypes.c_double(cutoff)
     info = ctypes.c_int(1)
     lib().routec_fock_set_cutoff(ctypes.byref(c), ctypes.byref(info))
+    return info.value
+
+
+def routec_fock_set_symmetry(nops, shell_map=None, ao_target=None, ao_sign=None):
+    """Calls routec_fock_set_symmetry with OpenQP's staged layout: 1-based
+    integer(8) images, shell or AO index fastest.  Takes the 0-based arrays of
+    openqp_gb300.symmetry.abelian_symmetry.  Returns info."""
+    n = ctypes.c_int(int(nops))
+    info = ctypes.c_int(1)
+    if int(nops) <= 1:
+        lib().routec_fock_set_symmetry(ctypes.byref(n), None, None, None, ctypes.byref(info))
+        return info.value
+    sm = np.ascontiguousarray(np.asarray(shell_map).reshape(-1) + 1, dtype=np.int64)
+    at = np.ascontiguousarray(np.asarray(ao_target).reshape(-1) + 1, dtype=np.int64)
+    sg = np.ascontiguousarray(np.asarray(ao_sign).reshape(-1), dtype=np.float64)
+    ll = ctypes.POINTER(ctypes.c_longlong)
+    lib().routec_fock_set_symmetry(ctypes.byref(n), sm.ctypes.data_as(ll), at.ctypes.data_as(ll), ptr(sg),
+                                   ctypes.byref(info))
     return info.value
 
 
