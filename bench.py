@@ -1546,7 +1546,7 @@ def run_batch(args):
                              "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
                              "peak_source": "measured: FP64 FMA-chain probe on this device",
                              "kernel_ms": float(ms[cdom])},
-                "autotune": {"split_log2": tune["split_log2"], "chunk": tune["chunk"],
+                "autotune": {"family": tune.get("family"), "split_log2": tune["split_log2"], "chunk": tune["chunk"],
                              "ctas_per_sm": tune["ctas_per_sm"], "class_ms_sum_tuned": float(sum(tune["class_ms"])),
                              "class_ms_sum_default": float(sum(tune.get("default_class_ms", tune["class_ms"])))},
                 "gpu_launches": int(gim["kernels"]) * args.steps,

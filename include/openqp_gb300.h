@@ -299,14 +299,27 @@ int oqpg_fock_jk_graph(oqpg_ctx* ctx, const double* d_device, double* f_device, 
 int oqpg_graph_info(const oqpg_ctx* ctx, int* captures, int* replays, int* kernels);
 
 /* Per-class launch parameters, 55 entries each in the class order of
- * oqpg_class_l (null: leave unchanged): split_log2 -- quartets of the <= 27
- * element classes with >= 2^split_log2 primitive quartets run one warp per
- * quartet (64: never); chunk -- quartets a warp takes per work grab in the
- * thread-per-quartet kernels (multiple of 32); ctas_per_sm -- grid cap per SM
- * (0: as many as fit).  The autotuner of the Python front end picks them.
- * No counterpart in the reference. */
+ * oqpg_class_l (null: leave unchanged): split_log2 -- quartets with
+ * >= 2^split_log2 surviving primitive quartets run the primitive-parallel
+ * kernel, one warp per quartet with the lanes on its primitives (64: never;
+ * -1, the default: 8 for thread-per-quartet lists, 4 for warp-per-quartet
+ * ones); chunk -- quartets a warp takes per work grab in the thread-per-quartet
+ * kernels (multiple of 32); ctas_per_sm -- grid cap per SM (0: as many as
+ * fit).  The autotuner of the Python front end picks them.  No counterpart in
+ * the reference. */
 int oqpg_set_tuning(oqpg_ctx* ctx, const int* split_log2, const int* chunk, const int* ctas_per_sm);
 int oqpg_get_tuning(const oqpg_ctx* ctx, int* split_log2, int* chunk, int* ctas_per_sm);
+
+/* Kernel family per class (55 entries): the classes with 28..108 Cartesian
+ * elements and no f shell have both a thread-per-quartet kernel (the block in
+ * registers) and a warp-per-quartet one.  family[c] = 0 (default): thread
+ * per quartet when the class's list holds at least 1024 quartets per SM
+ * (enough to fill the GPU), else warp per quartet; 1: thread per quartet; 2:
+ * warp per quartet.  Ignored for classes with one family.  available[c] (get)
+ * = 1 thread per quartet, 2 warp per quartet, 3 both.  The autotuner searches
+ * it.  No counterpart in the reference. */
+int oqpg_set_kernel_family(oqpg_ctx* ctx, const int* family);
+int oqpg_get_kernel_family(const oqpg_ctx* ctx, int* family, int* available);
 
 /* Schwarz bounds sqrt(max |(ab|ab)|) per shell pair, nshell x nshell (host);
  * single-molecule contexts only. */

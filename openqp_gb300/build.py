@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libopenqp_gb300.so")
-SOURCES = ["oqpg_cls_%d.cu" % g for g in (13, 12, 11, 10, 9, 8, 7, 6, 5, 3, 2, 1, 4, 0)] + \
+SOURCES = ["oqpg_cls_%d.cu" % g for g in (17, 15, 14, 16, 2, 3, 4, 18, 13, 12, 11, 10, 9, 8, 7, 6, 5, 1, 0)] + \
     ["oqpg_grad_cls_f%d.cu" % g for g in range(5)] + \
     ["oqpg_grad_cls_a.cu", "oqpg_grad_cls_b.cu", "oqpg_host.cu", "oqpg_noalloc.cu", "oqpg_onee.cu", "oqpg_grad_host.cu",
      "oqpg_response.cu", "oqpg_sigma.cu", "oqpg_petite.cu"]

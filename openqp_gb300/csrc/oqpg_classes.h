@@ -29,7 +29,8 @@ __host__ __device__ constexpr bool class_has_f(int c) { return c >= NCLASS_SD; }
 
 struct ClassInfo {
   int l[4];
-  int team;        // 1: one warp per quartet, 0: one thread per quartet
+  int small;       // 1: has the thread-per-quartet kernels (k_small, k_prim)
+  int team;        // 1: has the warp-per-quartet kernels (k_team, k_prim_team)
   int prim;        // 1: has the primitive-parallel kernel for its heavily contracted quartets
 };
 
@@ -40,13 +41,25 @@ __host__ __device__ constexpr bool prim_parallel(int la, int lb, int lc, int ld)
          ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) + 3 * (la + 1) * (lb + 1) * (lc + 1) * (ld + 1) <= 100;
 }
 const ClassInfo& class_info(int c);
-// One warp per quartet above 54 Cartesian elements (27 for the classes with an f
-// shell); below, one thread per quartet keeps the whole block in registers.
-// The (sp|pd), (sd|pp), (sd|sd) and (ss|dd) classes measured 2.2x faster
-// thread per quartet than warp per quartet on (H2O)32 cc-pVDZ.
-__host__ __device__ constexpr bool team_class(int la, int lb, int lc, int ld) {
-  return ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) > ((la == 3 || lb == 3 || lc == 3 || ld == 3) ? 27 : 54);
+// Kernel families of a class.  Thread per quartet keeps the whole block in
+// registers (up to 108 Cartesian elements, 27 with an f shell; beyond 54 with
+// some spilling, cheap next to the FP64 work); warp per quartet shares one
+// quartet among 32 lanes (above 27 elements).  A class with both (28-108
+// elements, no f shell) picks per list at launch: thread per quartet needs
+// enough quartets to fill the GPU.  Measured on (H2O)32 cc-pVDZ, thread per
+// quartet ran (sp|pd) 2.3x, (sd|pd) 2.2x, (sp|dd) 1.8x, (pp|pp) 1.2x faster;
+// on (H2O)16 6-31G(d), with ~1e4-1e5 quartets per list, warp per quartet ran
+// (sp|pd) 1.5x, (sd|pp) 2.3x, (pp|pp) 5x faster.
+__host__ __device__ constexpr bool has_small(int la, int lb, int lc, int ld) {
+  return ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) <= ((la == 3 || lb == 3 || lc == 3 || ld == 3) ? 27 : 108);
 }
+__host__ __device__ constexpr bool has_team(int la, int lb, int lc, int ld) {
+  return ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) > 27;
+}
+// Thread per quartet by default from this many quartets per SM in a list
+// (four waves of 128-thread CTAs at two CTAs per SM, the occupancy at 255
+// registers per thread).
+constexpr long long SMALL_MIN_PER_SM = 4 * 256;
 
 // Kernel variants of a class.
 constexpr int MODE_FOCK = 0;     // Fock build
@@ -73,5 +86,10 @@ cudaError_t launch_group10(int c, bool pure, int mode, const BuildArgs& a, int n
 cudaError_t launch_group11(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 cudaError_t launch_group12(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 cudaError_t launch_group13(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group14(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group15(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group16(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group17(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_group18(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st);
 
 }  // namespace oqpg

@@ -7,8 +7,6 @@ namespace oqpg {
 cudaError_t launch_group2(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
   switch (c) {
     case 5: return launch_cls<0, 0, 2, 2>(pure, mode, a, nsm, st);
-    case 9: return launch_cls<0, 1, 1, 2>(pure, mode, a, nsm, st);
-    case 10: return launch_cls<0, 1, 2, 2>(pure, mode, a, nsm, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -7,8 +7,6 @@ namespace oqpg {
 cudaError_t launch_group3(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
   switch (c) {
     case 11: return launch_cls<0, 2, 0, 2>(pure, mode, a, nsm, st);
-    case 12: return launch_cls<0, 2, 1, 1>(pure, mode, a, nsm, st);
-    case 15: return launch_cls<1, 1, 1, 1>(pure, mode, a, nsm, st);
     default: return cudaErrorInvalidValue;
   }
 }

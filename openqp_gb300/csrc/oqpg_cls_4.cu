@@ -7,9 +7,6 @@ namespace oqpg {
 cudaError_t launch_group4(int c, bool pure, int mode, const BuildArgs& a, int nsm, cudaStream_t st) {
   switch (c) {
     case 13: return launch_cls<0, 2, 1, 2>(pure, mode, a, nsm, st);
-    case 14: return launch_cls<0, 2, 2, 2>(pure, mode, a, nsm, st);
-    case 16: return launch_cls<1, 1, 1, 2>(pure, mode, a, nsm, st);
-    case 17: return launch_cls<1, 1, 2, 2>(pure, mode, a, nsm, st);
     default: return cudaErrorInvalidValue;
   }
 }

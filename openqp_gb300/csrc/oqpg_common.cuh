@@ -87,6 +87,7 @@ struct BuildArgs {
   unsigned long long* work;      // work-distribution counter of this launch (zeroed before it)
   int roots_f32;                 // FP32 quartets: evaluate Rys roots/weights in FP32 too
   int chunk;                     // thread-per-quartet kernels: quartets per warp grab (multiple of 32)
+  int team;                      // a class with both kernel families: 1 = warp per quartet
   int ctas_per_sm;               // launch: grid cap per SM (0: as many as fit)
 };
 

@@ -15,7 +15,7 @@
 namespace oqpg {
 
 static const ClassInfo kClasses[NCLASS] = {
-#define C_(a, b, c, d) {{a, b, c, d}, team_class(a, b, c, d), prim_parallel(a, b, c, d)}
+#define C_(a, b, c, d) {{a, b, c, d}, has_small(a, b, c, d), has_team(a, b, c, d), prim_parallel(a, b, c, d)}
     C_(0, 0, 0, 0), C_(0, 0, 0, 1), C_(0, 0, 0, 2), C_(0, 0, 1, 1), C_(0, 0, 1, 2), C_(0, 0, 2, 2),
     C_(0, 1, 0, 1), C_(0, 1, 0, 2), C_(0, 1, 1, 1), C_(0, 1, 1, 2), C_(0, 1, 2, 2),
     C_(0, 2, 0, 2), C_(0, 2, 1, 1), C_(0, 2, 1, 2), C_(0, 2, 2, 2),
@@ -40,12 +40,22 @@ cudaError_t launch_class(int c, bool pure, int mode, const BuildArgs& a, int nsm
       return launch_group0(c, pure, mode, a, nsm, st);
     case 4: case 6: case 7: case 8:
       return launch_group1(c, pure, mode, a, nsm, st);
-    case 5: case 9: case 10:
+    case 5:
       return launch_group2(c, pure, mode, a, nsm, st);
-    case 11: case 12: case 15:
+    case 9:
+      return launch_group14(c, pure, mode, a, nsm, st);
+    case 10:
+      return launch_group15(c, pure, mode, a, nsm, st);
+    case 11:
       return launch_group3(c, pure, mode, a, nsm, st);
-    case 13: case 14: case 16: case 17:
+    case 12:
+      return launch_group16(c, pure, mode, a, nsm, st);
+    case 15:
+      return launch_group17(c, pure, mode, a, nsm, st);
+    case 13:
       return launch_group4(c, pure, mode, a, nsm, st);
+    case 14: case 16: case 17:
+      return launch_group18(c, pure, mode, a, nsm, st);
     case 18:
       return launch_group5(c, pure, mode, a, nsm, st);
     case 19:
@@ -608,10 +618,8 @@ int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
 
 void default_tuning(oqpg_tuning& t) {
   for (int k = 0; k < NCLASS; ++k) {
-    // thread-per-quartet classes hand quartets of >= 256 surviving primitive
-    // quartets to the primitive-parallel kernel; warp-per-quartet classes
-    // already at 16, where 32 lanes on the primitives beat the team's 2D phase
-    t.split_log2[k] = class_info(k).team ? 4 : PRIM_SPLIT_LOG2;
+    t.split_log2[k] = -1;   // by the family the list runs (eff_split)
+    t.family[k] = 0;        // by list size (list_team)
     t.chunk[k] = 32;
     t.ctas_per_sm[k] = 0;
   }
@@ -986,6 +994,26 @@ int issue_densities(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st) 
   return OK;
 }
 
+// Whether a list of class cl with capacity cap runs the warp-per-quartet
+// kernels: the only family of the class, the tuned one, or by default warp per
+// quartet while the list is too short to fill the GPU thread per quartet.
+bool list_team(const oqpg_ctx* c, int cl, unsigned long long cap) {
+  const ClassInfo& ci = class_info(cl);
+  if (!ci.small) return true;
+  if (!ci.team) return false;
+  if (c->tune.family[cl] == 1) return false;
+  if (c->tune.family[cl] == 2) return true;
+  return (long long)cap < SMALL_MIN_PER_SM * c->nsm;
+}
+// The primitive-count split of a list: thread-per-quartet lists hand quartets
+// of >= 256 surviving primitive quartets to the primitive-parallel kernel,
+// warp-per-quartet lists already those of >= 16, where 32 lanes on the
+// primitives beat the team's 2D phase; or the tuned value.
+int eff_split(const oqpg_ctx* c, int cl, bool team) {
+  const int s = c->tune.split_log2[cl];
+  return s >= 0 ? s : (team ? 4 : PRIM_SPLIT_LOG2);
+}
+
 // (Re)size the lists of a pipeline for the given per-list counts, with headroom
 // for the screening of later densities.
 int size_lists(oqpg_ctx* c, BuildBufs& B, const unsigned long long* counts, cudaStream_t st) {
@@ -1003,7 +1031,8 @@ int size_lists(oqpg_ctx* c, BuildBufs& B, const unsigned long long* counts, cuda
   int split[NLIST];
   for (int k = 0; k < NLIST; ++k) {
     const int cl = k % NCLASS;
-    split[k] = class_info(cl).prim ? head_bins(c->tune.split_log2[cl]) : 0;
+    B.team[k] = list_team(c, cl, B.cap[k]) ? 1 : 0;
+    split[k] = class_info(cl).prim ? head_bins(eff_split(c, cl, B.team[k] != 0)) : 0;
   }
   CK(cudaMemcpyAsync(B.split.p, split, sizeof(split), cudaMemcpyHostToDevice, st));
   CK(cudaStreamSynchronize(st));  // the host arrays above are stack memory
@@ -1129,7 +1158,8 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
       a.counters = B.primc.as<unsigned long long>() + li;
       a.quartets = B.slists[li].as<uint2>();
       a.nquartets = (long long)B.cap[li];
-      if (class_info(cl).prim && c->tune.split_log2[cl] < 64) {
+      a.team = B.team[li];
+      if (class_info(cl).prim && eff_split(c, cl, B.team[li] != 0) < 64) {
         // quartets with >= 2^split primitive quartets (a prefix of the sorted
         // list) go to the warp-per-quartet primitive-parallel kernel
         a.range = ranges + 4 * li;
@@ -1457,7 +1487,7 @@ int oqpg_graph_info(const oqpg_ctx* ctx, int* captures, int* replays, int* kerne
 int oqpg_set_tuning(oqpg_ctx* ctx, const int* split_log2, const int* chunk, const int* ctas_per_sm) {
   if (!ctx) return NOT_INIT;
   for (int k = 0; k < NCLASS; ++k) {
-    if (split_log2 && (split_log2[k] < 0 || split_log2[k] > 64)) return UNSUPPORTED;
+    if (split_log2 && (split_log2[k] < -1 || split_log2[k] > 64)) return UNSUPPORTED;
     if (chunk && (chunk[k] < 32 || chunk[k] > 4096 || chunk[k] % 32)) return UNSUPPORTED;
     if (ctas_per_sm && (ctas_per_sm[k] < 0 || ctas_per_sm[k] > 64)) return UNSUPPORTED;
   }
@@ -1472,6 +1502,30 @@ int oqpg_set_tuning(oqpg_ctx* ctx, const int* split_log2, const int* chunk, cons
   if (ctx->gexec) {
     cudaGraphExecDestroy(ctx->gexec);
     ctx->gexec = nullptr;
+  }
+  return OK;
+}
+
+int oqpg_set_kernel_family(oqpg_ctx* ctx, const int* family) {
+  if (!ctx) return NOT_INIT;
+  if (!family) return UNSUPPORTED;
+  for (int k = 0; k < NCLASS; ++k)
+    if (family[k] < 0 || family[k] > 2) return UNSUPPORTED;
+  for (int k = 0; k < NCLASS; ++k) ctx->tune.family[k] = family[k];
+  ctx->hb.sized = false;
+  ctx->gb.sized = false;
+  if (ctx->gexec) {
+    cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
+  }
+  return OK;
+}
+
+int oqpg_get_kernel_family(const oqpg_ctx* ctx, int* family, int* available) {
+  if (!ctx) return NOT_INIT;
+  for (int k = 0; k < NCLASS; ++k) {
+    if (family) family[k] = ctx->tune.family[k];
+    if (available) available[k] = (class_info(k).small ? 1 : 0) | (class_info(k).team ? 2 : 0);
   }
   return OK;
 }

@@ -228,6 +228,7 @@ struct BuildBufs {
       split, flag, gtab, sym, fsk;
   DevBuf lists[NLIST], slists[NLIST], bins[NLIST];
   unsigned long long cap[NLIST] = {0};
+  unsigned char team[NLIST] = {0};     // list runs the warp-per-quartet kernels (set with the sizes)
   bool sized = false;
   unsigned long long* h_rb = nullptr;  // pinned readback: [0] flag, [1, 1+NLIST) counts, then primitive counts
   void release() {
@@ -241,6 +242,7 @@ struct BuildBufs {
     h_rb = nullptr;
     sized = false;
     for (auto& x : cap) x = 0;
+    for (auto& x : team) x = 0;
   }
 };
 
@@ -248,7 +250,8 @@ struct BuildBufs {
 
 // Per-class launch parameters picked by the autotuner.
 struct oqpg_tuning {
-  int split_log2[oqpg::NCLASS];  // small classes: quartets with >= 2^k primitive quartets run warp-per-quartet
+  int split_log2[oqpg::NCLASS];  // quartets with >= 2^k primitive quartets run primitive-parallel (-1: 8, 4 warp per quartet)
+  int family[oqpg::NCLASS];      // classes with both kernel families: 0 by list size, 1 thread, 2 warp per quartet
   int chunk[oqpg::NCLASS];       // small classes: quartets a warp takes per grab (multiple of 32)
   int ctas_per_sm[oqpg::NCLASS]; // grid cap per SM (0: as many as fit)
 };

@@ -36,14 +36,14 @@ constexpr int team_warps() {
   return per_warp * 4 <= budget ? 4 : (per_warp * 2 <= budget ? 2 : 1);
 }
 
-// Classes with more than 54 Cartesian elements (27 with an f shell) run one
-// warp per quartet.
+// The kernel family a launch uses: a class with both runs warp per quartet
+// when a.team is set (the host decides per list), thread per quartet otherwise.
 template <int LA, int LB, int LC, int LD>
-constexpr bool is_team() { return team_class(LA, LB, LC, LD); }
+__host__ __device__ constexpr bool only_team() { return !has_small(LA, LB, LC, LD); }
 
 template <int LA, int LB, int LC, int LD, bool PURE, typename T>
-cudaError_t launch_fock(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
-  if constexpr (is_team<LA, LB, LC, LD>()) {
+cudaError_t launch_team(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
+  if constexpr (has_team(LA, LB, LC, LD)) {
     constexpr int W = team_warps<LA, LB, LC, LD, PURE, T>();
     const size_t smem = sizeof(T) * W * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
     if (kind == MODE_PRIM) {
@@ -54,15 +54,29 @@ cudaError_t launch_fock(int kind, const BuildArgs& a, int nsm, cudaStream_t st) 
     }
     return launch_persistent(k_team<LA, LB, LC, LD, PURE, false, T>, smem, W, a, nsm, st, 32 * W);
   } else {
+    return cudaErrorInvalidValue;
+  }
+}
+
+template <int LA, int LB, int LC, int LD, bool PURE, typename T>
+cudaError_t launch_fock(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
+  if constexpr (only_team<LA, LB, LC, LD>()) {
+    return launch_team<LA, LB, LC, LD, PURE, T>(kind, a, nsm, st);
+  } else {
+    if constexpr (has_team(LA, LB, LC, LD)) {
+      if (a.team) return launch_team<LA, LB, LC, LD, PURE, T>(kind, a, nsm, st);
+    }
     if (kind == MODE_PRIM) return launch_persistent(k_prim<LA, LB, LC, LD, PURE, T>, 0, 4, a, nsm, st);
     return launch_persistent(k_small<LA, LB, LC, LD, PURE, false, T>, 0, 128, a, nsm, st);
   }
 }
 
+// Schwarz bounds of the diagonal quartets: thread per quartet where the class
+// has it.
 template <int LA, int LB, int LC, int LD, bool PURE>
 cudaError_t launch_schwarz(const BuildArgs& a, int nsm, cudaStream_t st) {
   if constexpr (LA == LC && LB == LD) {
-    if constexpr (is_team<LA, LB, LC, LD>()) {
+    if constexpr (only_team<LA, LB, LC, LD>()) {
       constexpr int W = team_warps<LA, LB, LC, LD, PURE, double>();
       const size_t smem = sizeof(double) * W * TeamSmem<LA, LB, LC, LD, PURE>::PER_WARP;
       return launch_persistent(k_team<LA, LB, LC, LD, PURE, true, double>, smem, W, a, nsm, st, 32 * W);
@@ -74,14 +88,17 @@ cudaError_t launch_schwarz(const BuildArgs& a, int nsm, cudaStream_t st) {
   }
 }
 
-// mode: MODE_FOCK, MODE_SCHWARZ (diagonal classes only), MODE_PRIM (small
-// classes only: the heavily contracted head of a sorted list), each optionally
-// with MODE_F32 (FP32 quartets of the precision-split build; not Schwarz).
+// mode: MODE_FOCK, MODE_SCHWARZ (diagonal classes only), MODE_PRIM (the
+// heavily contracted head of a sorted list), each optionally with MODE_F32
+// (FP32 quartets of the precision-split build; not Schwarz).
 template <int LA, int LB, int LC, int LD, bool PURE>
 cudaError_t launch_df(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
-  if constexpr (is_team<LA, LB, LC, LD>()) {
+  if constexpr (only_team<LA, LB, LC, LD>()) {
     return launch_fock<LA, LB, LC, LD, PURE, dfl>(kind, a, nsm, st);
   } else {
+    if constexpr (has_team(LA, LB, LC, LD)) {
+      if (a.team) return launch_team<LA, LB, LC, LD, PURE, dfl>(kind, a, nsm, st);
+    }
     if (kind == MODE_PRIM) return launch_persistent(k_prim_df<LA, LB, LC, LD, PURE>, 0, 4, a, nsm, st);
     return launch_persistent(k_small_df<LA, LB, LC, LD, PURE>, 0, 128, a, nsm, st);
   }

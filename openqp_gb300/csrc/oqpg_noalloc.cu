@@ -215,7 +215,7 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
     if (!h_counts[cl]) continue;
     a.counters = primc + cl;
     long long head = 0;
-    if (class_info(cl).prim && !class_info(cl).team) {
+    if (class_info(cl).prim && class_info(cl).small) {   // thread per quartet where the class has it
       for (int b = 0; b < head_bins(PRIM_SPLIT_LOG2); ++b) head += (long long)h_hist[cl * NBIN + b];
       if (head > 0) {
         a.quartets = slists + off[cl];

@@ -287,6 +287,22 @@ class FockBuilder:
         lib().oqpg_get_tuning(self.h, *[ptr(a, _i) for a in arrs])
         return dict(split_log2=arrs[0].tolist(), chunk=arrs[1].tolist(), ctas_per_sm=arrs[2].tolist())
 
+    def set_kernel_family(self, family):
+        """Per class: 0 by list size (default), 1 thread per quartet, 2 warp
+        per quartet (classes with both kernels; ignored elsewhere)."""
+        a = np.ascontiguousarray(family, dtype=np.int32)
+        if a.shape != (NCLASS,):
+            raise ValueError("one entry per class (%d)" % NCLASS)
+        rc = lib().oqpg_set_kernel_family(self.h, ptr(a, _i))
+        if rc != 0:
+            raise FockError(rc, "oqpg_set_kernel_family")
+
+    def get_kernel_family(self):
+        """(family per class, available families per class: 1 thread, 2 warp, 3 both)"""
+        f, av = np.zeros(NCLASS, dtype=np.int32), np.zeros(NCLASS, dtype=np.int32)
+        lib().oqpg_get_kernel_family(self.h, ptr(f, _i), ptr(av, _i))
+        return f.tolist(), av.tolist()
+
     def set_precision(self, mode, threshold=1e-6):
         """mode "fp64": plain path; mode "mixed": quartets whose screening value
         (Schwarz bound x shell density) is below threshold run in FP32 with their

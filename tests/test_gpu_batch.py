@@ -190,6 +190,15 @@ def test_tuning_changes_launches_not_results(gpu):
         assert np.abs(fb.fock_jk(d) - ref).max() < 1e-12
     with pytest.raises(gpu.FockError):
         fb.set_tuning(chunk=[33] * nc)
+    # the kernel family of the classes that have both (28-108 elements): thread
+    # per quartet, warp per quartet, by list size -- the same matrices
+    fam, avail = fb.get_kernel_family()
+    assert fam == [0] * nc and 3 in avail and avail[0] == 1 and avail[20] == 2
+    for f in (1, 2, 0):
+        fb.set_kernel_family([f] * nc)
+        assert np.abs(fb.fock_jk(d) - ref).max() < 1e-12
+    with pytest.raises(gpu.FockError):
+        fb.set_kernel_family([3] * nc)
 
 
 def test_autotune_picks_and_persists(gpu, tmp_path):
