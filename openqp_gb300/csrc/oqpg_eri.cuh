@@ -40,6 +40,7 @@ namespace oqpg {
 #define RYS_STORAGE static __device__ const
 #include "rys_tables.inc"
 #include "rys_tables_df.inc"
+#include "rys_tables_fine.inc"
 #undef RYS_STORAGE
 
 __host__ __device__ constexpr int rys_xmax(int n) { return 32 + 8 * n; }
@@ -47,17 +48,27 @@ __host__ __device__ constexpr int rys_nint(int n) { return RYS_X_SPLIT * RYS_LO_
 __host__ __device__ constexpr int rys_offset(int n, int ncoef) {  // start of the n-root table
   return n <= 1 ? 0 : rys_offset(n - 1, ncoef) + rys_nint(n - 1) * 2 * (n - 1) * ncoef;
 }
+// The finer grid of the one- and two-root FP64 tables (rys_tables_fine.inc)
+__host__ __device__ constexpr int rys_nint_fine(int n) {
+  return RYS_X_SPLIT * RYS_FINE_LO_PER_UNIT + (rys_xmax(n) - RYS_X_SPLIT) * RYS_FINE_HI_PER_UNIT;
+}
+__host__ __device__ constexpr int rys_offset_fine(int n) {
+  return n <= 1 ? 0 : rys_offset_fine(n - 1) + rys_nint_fine(n - 1) * 2 * (n - 1) * RYS_FINE_NCOEF;
+}
+static_assert(rys_offset_fine(RYS_FINE_NMAX + 1) == RYS_TABLE_FINE_SIZE, "fine Rys table layout");
 
-// Interval k of the table at X >= 0 and the Chebyshev variable s in [-1, 1]:
-// width 1/4 below 32 (k = floor(4X), s = 8X - (2k+1)), unit width above
-// (f = floor(X), k = 128 + f - 32, s = 2X - (2f+1)).  The floors and the
-// constant 2k+1 come from the bits of X with integer instructions, so the
-// only FP64 instruction is the FMA that forms s.
-static_assert(RYS_LO_PER_UNIT == 4, "interval arithmetic below assumes quarter-unit intervals under the split");
+// Interval k of a table at X >= 0 and the Chebyshev variable s in [-1, 1],
+// for intervals of width 2^-LL below 32 and 2^-LH from 32 up: with
+// f = floor(X 2^L) (L = LL or LH), k = f below 32 and
+// 32 2^LL + (f - 32 2^LH) above, s = 2^(L+1) X - (2f+1).  The floors and the
+// constant 2f+1 come from the bits of X with integer instructions, so the
+// only FP64 instruction is the FMA that forms s.  The standard tables use
+// LL = 2, LH = 0; the fine one- and two-root tables LL = 3, LH = 1.
+template <int LL, int LH>
 __device__ __forceinline__ int rys_interval(long long xb, double X, double& s) {
   const bool lo = xb < __double_as_longlong((double)RYS_X_SPLIT);
-  // floor(X 2^a), a = 2 below the split, 0 above (X < 2^30)
-  const int e = (int)(xb >> 52) - 1023 + (lo ? 2 : 0);
+  // floor(X 2^L) (X < 2^30)
+  const int e = (int)(xb >> 52) - 1023 + (lo ? LL : LH);
   const long long m = (xb & 0xfffffffffffffll) | 0x10000000000000ll;
   const int f = (int)(m >> (e < 0 ? 63 : 52 - e));
   // -(2f + 1) as a double: odd integer v < 2^21, exponent from its leading bit
@@ -65,9 +76,11 @@ __device__ __forceinline__ int rys_interval(long long xb, double X, double& s) {
   const int ev = 31 - __clz(v);
   const double c = __longlong_as_double((long long)((1ull << 63) | ((unsigned long long)(1023 + ev) << 52) |
                                                     (((unsigned long long)v << (52 - ev)) & 0xfffffffffffffull)));
-  s = fma(lo ? 2.0 * RYS_LO_PER_UNIT : 2.0, X, c);
-  return lo ? f : RYS_X_SPLIT * RYS_LO_PER_UNIT + (f - RYS_X_SPLIT);
+  s = fma(lo ? (double)(2 << LL) : (double)(2 << LH), X, c);
+  return lo ? f : (RYS_X_SPLIT << LL) + (f - (RYS_X_SPLIT << LH));
 }
+static_assert(RYS_LO_PER_UNIT == 4 && RYS_FINE_LO_PER_UNIT == 8 && RYS_FINE_HI_PER_UNIT == 2,
+              "rys_interval grids: 1/4 and 1 (standard), 1/8 and 1/2 (fine)");
 
 // Above the table (X >= 32 + 8N) the nodes and weights are R2/X and W/sqrt(X):
 // polynomials of degree 2 and 1 in y = X^-1/2 (y from one reciprocal square
@@ -82,7 +95,7 @@ __device__ __forceinline__ int rys_interval(long long xb, double X, double& s) {
 // Quantity q of the N-root rule at X (FP64): q even -> node x_{q/2}, q odd ->
 // weight w_{q/2}.  X >= 0, so the range tests compare bit patterns as
 // integers (no FP64 instruction).
-template <int N, int NCOEF>
+template <int N, int NCOEF, bool FINE = false>
 __device__ __forceinline__ double rys_eval(const double* table, double X, int q) {
   const long long xb = __double_as_longlong(X);
   const bool asym = xb >= __double_as_longlong((double)rys_xmax(N));
@@ -101,8 +114,8 @@ __device__ __forceinline__ double rys_eval(const double* table, double X, int q)
     s = rsqrt64(X);
     a = (q & 1) ? RYS_HERM_W[r] : RYS_HERM_R2[r];
   } else {
-    const int k = rys_interval(xb, X, s);
-    c = table + rys_offset(N, NCOEF) + (k * 2 * N + q) * NCOEF;
+    const int k = FINE ? rys_interval<3, 1>(xb, X, s) : rys_interval<2, 0>(xb, X, s);
+    c = table + (FINE ? rys_offset_fine(N) : rys_offset(N, NCOEF)) + (k * 2 * N + q) * NCOEF;
   }
   // the single nonzero coefficient of the large-X form: degree 1 (weight) or 2 (node)
   const int ia = (q & 1) ? 1 : 2;
@@ -115,7 +128,8 @@ __device__ __forceinline__ double rys_eval(const double* table, double X, int q)
 // Node u and weight w of root r together (FP64): one range test for both, and
 // above the table both come from one reciprocal square root y = X^-1/2
 // (u = R2_r y^2, w = W_r y) instead of a reciprocal and a reciprocal square root.
-template <int N, int NCOEF>
+// FINE: the one- and two-root fine tables (degree 6, rys_tables_fine.inc).
+template <int N, int NCOEF, bool FINE = false>
 __device__ __forceinline__ void rys_eval_uw(const double* table, double X, int r, double& u, double& w) {
   const long long xb = __double_as_longlong(X);
   const bool asym = xb >= __double_as_longlong((double)rys_xmax(N));
@@ -135,9 +149,9 @@ __device__ __forceinline__ void rys_eval_uw(const double* table, double X, int r
     r2 = RYS_HERM_R2[i0];
     wh = RYS_HERM_W[i0];
   } else {
-    const int k = rys_interval(xb, X, s);
+    const int k = FINE ? rys_interval<3, 1>(xb, X, s) : rys_interval<2, 0>(xb, X, s);
     // node coefficients at c, weight coefficients at c + NCOEF
-    c = table + rys_offset(N, NCOEF) + (k * 2 * N + 2 * r) * NCOEF;
+    c = table + (FINE ? rys_offset_fine(N) : rys_offset(N, NCOEF)) + (k * 2 * N + 2 * r) * NCOEF;
   }
   double vu = asym ? 0.0 : __ldg(c + NCOEF - 1), vw = asym ? 0.0 : __ldg(c + 2 * NCOEF - 1);
 #pragma unroll
@@ -176,6 +190,13 @@ __device__ __forceinline__ float rys_eval_f32(float X, int q) {
 
 // Double-float evaluation of the degree-7 FP64 table (coefficients as FP32
 // pairs), interval selection on the leading FP32 word.
+// Double-float Horner chains start in plain FP32: the interpolants'
+// coefficients of degree >= 5 are below 2e-7 of the leading one (all root
+// counts, every interval), so the FP32 rounding of c7 s^2 + c6 s + c5 stays
+// below 2e-14 of the result, under the double-float resolution; degrees 4..0
+// run in double-float (5 of the 7 FMAs of the chain).
+constexpr int RYS_DF_TAIL = 5;
+
 template <int N>
 __device__ __forceinline__ dfl rys_eval_df(dfl X, int q) {
   if (X.hi >= (float)rys_xmax(N)) {
@@ -196,11 +217,14 @@ __device__ __forceinline__ dfl rys_eval_df(dfl X, int q) {
     s = dfl(X.hi * 2.0f, X.lo * 2.0f) + dfl(-(2 * f + 1));
   }
   const float2* c = RYS_TABLE_DF + rys_offset(N, RYS_NCOEF) + (k * 2 * N + q) * RYS_NCOEF;
-  float2 t = __ldg(c + RYS_NCOEF - 1);
-  dfl v(t.x, t.y);
+  // the top of the chain in FP32 (see RYS_DF_TAIL), the rest in double-float
+  float f = __ldg(c + RYS_NCOEF - 1).x;
 #pragma unroll
-  for (int i = RYS_NCOEF - 2; i >= 0; --i) {
-    t = __ldg(c + i);
+  for (int i = RYS_NCOEF - 2; i >= RYS_DF_TAIL; --i) f = fmaf(f, s.hi, __ldg(c + i).x);
+  dfl v(f, 0.0f);
+#pragma unroll
+  for (int i = RYS_DF_TAIL - 1; i >= 0; --i) {
+    const float2 t = __ldg(c + i);
     v = fma(v, s, dfl(t.x, t.y));
   }
   return v;
@@ -229,12 +253,16 @@ __device__ __forceinline__ void rys_eval_uw_df(dfl X, int r, dfl& u, dfl& w) {
     s = dfl(X.hi * 2.0f, X.lo * 2.0f) + dfl(-(2 * f + 1));
   }
   const float2* c = RYS_TABLE_DF + rys_offset(N, RYS_NCOEF) + (k * 2 * N + 2 * r) * RYS_NCOEF;
-  float2 tu = __ldg(c + RYS_NCOEF - 1), tw = __ldg(c + 2 * RYS_NCOEF - 1);
-  dfl vu(tu.x, tu.y), vw(tw.x, tw.y);
+  float fu = __ldg(c + RYS_NCOEF - 1).x, fw = __ldg(c + 2 * RYS_NCOEF - 1).x;
 #pragma unroll
-  for (int i = RYS_NCOEF - 2; i >= 0; --i) {
-    tu = __ldg(c + i);
-    tw = __ldg(c + RYS_NCOEF + i);
+  for (int i = RYS_NCOEF - 2; i >= RYS_DF_TAIL; --i) {
+    fu = fmaf(fu, s.hi, __ldg(c + i).x);
+    fw = fmaf(fw, s.hi, __ldg(c + RYS_NCOEF + i).x);
+  }
+  dfl vu(fu, 0.0f), vw(fw, 0.0f);
+#pragma unroll
+  for (int i = RYS_DF_TAIL - 1; i >= 0; --i) {
+    const float2 tu = __ldg(c + i), tw = __ldg(c + RYS_NCOEF + i);
     vu = fma(vu, s, dfl(tu.x, tu.y));
     vw = fma(vw, s, dfl(tw.x, tw.y));
   }
@@ -242,12 +270,16 @@ __device__ __forceinline__ void rys_eval_uw_df(dfl X, int r, dfl& u, dfl& w) {
   w = vw;
 }
 
-// FP64 kernels: the degree-7 FP64 tables.  FP32 kernels: the degree-4 tables,
-// evaluated in FP64 (default) or, with roots_f32, in FP32.  Double-float
-// kernels: the degree-7 table in double-float.
+// FP64 kernels: the degree-7 FP64 tables (degree 6 on the finer grid for one
+// and two roots).  FP32 kernels: the degree-4 tables, evaluated in FP64
+// (default) or, with roots_f32, in FP32.  Double-float kernels: the degree-7
+// table in double-float.
 template <int N, typename T>
 __device__ __forceinline__ T rys_quantity(T X, int q, bool roots_f32 = false) {
-  if constexpr (std::is_same<T, double>::value) return rys_eval<N, RYS_NCOEF>(RYS_TABLE, X, q);
+  if constexpr (std::is_same<T, double>::value) {
+    if constexpr (N <= RYS_FINE_NMAX) return rys_eval<N, RYS_FINE_NCOEF, true>(RYS_TABLE_FINE, X, q);
+    else return rys_eval<N, RYS_NCOEF>(RYS_TABLE, X, q);
+  }
   else if constexpr (std::is_same<T, dfl>::value) return rys_eval_df<N>(X, q);
   else {
     if (roots_f32) return rys_eval_f32<N>(X, q);
@@ -259,7 +291,8 @@ __device__ __forceinline__ T rys_quantity(T X, int q, bool roots_f32 = false) {
 template <int N, typename T>
 __device__ __forceinline__ void rys_node_weight(T X, int r, bool roots_f32, T& u, T& w) {
   if constexpr (std::is_same<T, double>::value) {
-    rys_eval_uw<N, RYS_NCOEF>(RYS_TABLE, X, r, u, w);
+    if constexpr (N <= RYS_FINE_NMAX) rys_eval_uw<N, RYS_FINE_NCOEF, true>(RYS_TABLE_FINE, X, r, u, w);
+    else rys_eval_uw<N, RYS_NCOEF>(RYS_TABLE, X, r, u, w);
   } else if constexpr (std::is_same<T, dfl>::value) {
     rys_eval_uw_df<N>(X, r, u, w);
   } else {
