@@ -321,6 +321,20 @@ int oqpg_get_tuning(const oqpg_ctx* ctx, int* split_log2, int* chunk, int* ctas_
 int oqpg_set_kernel_family(oqpg_ctx* ctx, const int* family);
 int oqpg_get_kernel_family(const oqpg_ctx* ctx, int* family, int* available);
 
+/* Shell families (on by default): s shells of one atom with the same
+ * primitive exponents (the generally contracted shells of cc-pVXZ sets, which
+ * OpenQP stores as separate segmented shells) share their primitive
+ * integrals in the (ss|ss), (ss|sp), (ss|sd), (ss|pp) and (sp|sp) classes of
+ * plain FP64 SCF builds: one primitive integral per family quartet, added to
+ * every member shell quartet with its own contraction factors, primitive
+ * screens, quartet screen, element cutoff and digestion, so the result is the
+ * reference's shell-by-shell sum.  on = 0 evaluates every shell quartet on
+ * its own.  info: on, and the family pairs with more than one member shell
+ * pair (0: the basis has no shared primitives).  No counterpart in the
+ * reference (int2.F90 loops over shell quartets). */
+int oqpg_set_shell_families(oqpg_ctx* ctx, int on);
+int oqpg_shell_families_info(const oqpg_ctx* ctx, int* on, int* nshared);
+
 /* Schwarz bounds sqrt(max |(ab|ab)|) per shell pair, nshell x nshell (host);
  * single-molecule contexts only. */
 int oqpg_schwarz(const oqpg_ctx* ctx, double* q);

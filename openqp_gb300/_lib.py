@@ -71,6 +71,8 @@ def lib():
         L.oqpg_get_tuning.argtypes = [ctypes.c_void_p, _i, _i, _i]
         L.oqpg_set_kernel_family.argtypes = [ctypes.c_void_p, _i]
         L.oqpg_get_kernel_family.argtypes = [ctypes.c_void_p, _i, _i]
+        L.oqpg_set_shell_families.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.oqpg_shell_families_info.argtypes = [ctypes.c_void_p, _i, _i]
         L.routec_fock_init_batch.argtypes = [ctypes.c_int, _i, _i, _i, _i, _i, _d, _d, _i, _d, ctypes.c_double]
         L.routec_fock_jk_batch.argtypes = [_d, _d, _i, _i, _d, _d, _i]
         L.routec_fock_jk_batch.restype = None

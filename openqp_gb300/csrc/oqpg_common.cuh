@@ -53,6 +53,34 @@ constexpr unsigned PAIR_MASK = 0x3fffffffu;
 __host__ __device__ inline unsigned entry_pair(unsigned x) { return x & PAIR_MASK; }
 __host__ __device__ inline int entry_wlog2(unsigned x) { return (int)(x >> 30); }
 
+// Shell families: s shells on one atom whose primitives have the same
+// exponents (the generally contracted shells of correlation-consistent sets,
+// e.g. the 1s and 2s of O in cc-pVDZ), at most two per family.  A family pair
+// (two families, or a family and another shell) has up to FAM_MAX member
+// shell pairs that share every primitive pair's geometry and differ only in
+// the contraction coefficients, so one primitive integral serves them all.
+// Its primitive pairs are the union of the members' (PrimPair, with sp the
+// largest member |K/p|, for the screens); FamCoef holds each member's own K/p,
+// zero where the member's primitive-pair screen drops the pair.
+constexpr int FAM_MAX = 4;
+struct FamMem {
+  int n;             // member shell pairs (1..FAM_MAX)
+  int m[FAM_MAX];    // their indices in the canonical pair table
+};
+struct FamCoef {
+  double sp[FAM_MAX];
+  float spf[FAM_MAX];
+};
+// Family-quartet list entries: family pair indices in the low 24 bits of x
+// and y, and the member combinations (m of x, n of y) that pass the quartet
+// screen as bit 4m + n of a 16-bit mask, bits 0-7 in the top byte of x and
+// bits 8-15 in the top byte of y.
+constexpr unsigned FAM_IDX_MASK = 0xffffffu;
+__host__ __device__ inline uint2 fam_entry(unsigned fx, unsigned fy, unsigned mask) {
+  return make_uint2(fx | ((mask & 0xffu) << 24), fy | ((mask >> 8) << 24));
+}
+__host__ __device__ inline unsigned fam_mask(uint2 e) { return (e.x >> 24) | ((e.y >> 24) << 8); }
+
 // Parameters of one Fock build (or Schwarz pass) shared by the class kernels.
 struct BuildArgs {
   const ShellDev* shells;
@@ -89,6 +117,12 @@ struct BuildArgs {
   int chunk;                     // thread-per-quartet kernels: quartets per warp grab (multiple of 32)
   int team;                      // a class with both kernel families: 1 = warp per quartet
   int ctas_per_sm;               // launch: grid cap per SM (0: as many as fit)
+  // shell-family builds (quartets are family quartets; pairs stays the
+  // canonical pair table, for the members' digestion)
+  const PairDev* fpairs;         // family pairs: representative shells, union primitive range
+  const FamMem* fmem;
+  const PrimPair* fprims;        // union primitive pairs
+  const FamCoef* fcoef;          // per union primitive pair: the members' K/p
 };
 
 // ---------------------------------------------------------------------------

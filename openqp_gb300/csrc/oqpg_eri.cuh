@@ -661,7 +661,7 @@ __device__ __forceinline__ void quartet_geometry(const BuildArgs& a, uint2 qd, P
 }
 
 // ===========================================================================
-// Small classes (at most 54 Cartesian elements, 27 with an f shell):
+// Small classes (at most 108 Cartesian elements, 27 with an f shell):
 // everything in registers.
 //
 // small_prims accumulates the primitive quartets c = first, first + step, ...
@@ -669,8 +669,9 @@ __device__ __forceinline__ void quartet_geometry(const BuildArgs& a, uint2 qd, P
 // arithmetic body computes one surviving candidate of this lane: the cheap
 // FP32 scan skips screened candidates without holding the warp in the body.
 // The arithmetic body: primitive quartet (bra pair cb, ket pair cq) of one
-// contracted quartet added into acc.
-template <int LA, int LB, int LC, int LD, typename T, bool ATT>
+// contracted quartet added into acc.  UNIT: with unit pair factors K/p (the
+// shell-family kernels apply each member's factors afterwards).
+template <int LA, int LB, int LC, int LD, typename T, bool ATT, bool UNIT = false>
 __device__ __forceinline__ void prim_body(const BuildArgs& a, const typename PrimT<T>::type* bpp,
                                           const typename PrimT<T>::type* kpp, int cb, int cq, const T AB[3],
                                           const T CD[3], T* acc) {
@@ -680,6 +681,10 @@ __device__ __forceinline__ void prim_body(const BuildArgs& a, const typename Pri
   PP bp, kp;
   prim_load(bpp + cb, bp);
   prim_load(kpp + cq, kp);
+  if constexpr (UNIT) {
+    bp.sp = (T)1;
+    kp.sp = (T)1;
+  }
   PrimQuartet<T> pq;
   prim_setup<T, ATT, LA + LB == 0>(bp, kp, pq, (T)a.inv_mu2);
 #pragma unroll
@@ -706,14 +711,11 @@ __device__ __forceinline__ void prim_body(const BuildArgs& a, const typename Pri
   }
 }
 
-template <int LA, int LB, int LC, int LD, typename T, bool ATT>
-__device__ __forceinline__ void small_prims_impl(const BuildArgs& a, const PairDev& P, const PairDev& Q,
-                                                 const T AB[3], const T CD[3], int first, int step, T* acc,
-                                                 unsigned long long& nprim) {
-  using PP = typename PrimT<T>::type;
-  const PP* bpp = prims_of<T>(a) + P.poff;
-  const PP* kpp = prims_of<T>(a) + Q.poff;
-  const int nP = P.pcnt, nQ = Q.pcnt;
+// The screened primitive quartets c = first, first + step, ... (c = kq nP + kb)
+// of one contracted quartet: body(kb, kq) for each that passes the screen.
+template <typename PP, typename Body>
+__device__ __forceinline__ void prim_loop_lane(const BuildArgs& a, const PP* bpp, const PP* kpp, int nP, int nQ,
+                                               int first, int step, unsigned long long& nprim, Body&& body) {
   if (nP == 0 || nQ == 0) return;
   int kq = first / nP, kb = first - kq * nP;
   int kq_loaded = -1;
@@ -729,8 +731,19 @@ __device__ __forceinline__ void small_prims_impl(const BuildArgs& a, const PairD
     }
     if (cb < 0) break;
     ++nprim;
-    prim_body<LA, LB, LC, LD, T, ATT>(a, bpp, kpp, cb, cq, AB, CD, acc);
+    body(cb, cq);
   }
+}
+
+template <int LA, int LB, int LC, int LD, typename T, bool ATT>
+__device__ __forceinline__ void small_prims_impl(const BuildArgs& a, const PairDev& P, const PairDev& Q,
+                                                 const T AB[3], const T CD[3], int first, int step, T* acc,
+                                                 unsigned long long& nprim) {
+  using PP = typename PrimT<T>::type;
+  const PP* bpp = prims_of<T>(a) + P.poff;
+  const PP* kpp = prims_of<T>(a) + Q.poff;
+  prim_loop_lane(a, bpp, kpp, P.pcnt, Q.pcnt, first, step, nprim,
+                 [&](int cb, int cq) { prim_body<LA, LB, LC, LD, T, ATT>(a, bpp, kpp, cb, cq, AB, CD, acc); });
 }
 
 // The attenuated (CAM) operator is a separate instance of the primitive
@@ -750,14 +763,9 @@ __device__ __forceinline__ void small_prims(const BuildArgs& a, const PairDev& P
 // on 32 lanes instead of on the lanes whose stride-32 slice happened to keep
 // a candidate.  Each lane accumulates its survivors into its own acc; the
 // caller reduces over the warp.
-template <int LA, int LB, int LC, int LD, typename T, bool ATT>
-__device__ __forceinline__ void warp_prims_impl(const BuildArgs& a, const PairDev& P, const PairDev& Q,
-                                                const T AB[3], const T CD[3], int lane, T* acc,
-                                                unsigned long long& nprim) {
-  using PP = typename PrimT<T>::type;
-  const PP* bpp = prims_of<T>(a) + P.poff;
-  const PP* kpp = prims_of<T>(a) + Q.poff;
-  const int nP = P.pcnt, nQ = Q.pcnt;
+template <typename PP, typename Body>
+__device__ __forceinline__ void prim_loop_warp(const BuildArgs& a, const PP* bpp, const PP* kpp, int nP, int nQ,
+                                               int lane, unsigned long long& nprim, Body&& body) {
   const int total = nP * nQ;
   int hb = 0, hq = 0;   // the survivor this lane holds
   int held = 0;         // lanes [0, held) hold one (uniform over the warp)
@@ -785,15 +793,26 @@ __device__ __forceinline__ void warp_prims_impl(const BuildArgs& a, const PairDe
       held += take;
       if (held == 32) {
         nprim += 1;
-        prim_body<LA, LB, LC, LD, T, ATT>(a, bpp, kpp, hb, hq, AB, CD, acc);
+        body(hb, hq);
         held = 0;
       }
     }
   }
   if (lane < held) {
     nprim += 1;
-    prim_body<LA, LB, LC, LD, T, ATT>(a, bpp, kpp, hb, hq, AB, CD, acc);
+    body(hb, hq);
   }
+}
+
+template <int LA, int LB, int LC, int LD, typename T, bool ATT>
+__device__ __forceinline__ void warp_prims_impl(const BuildArgs& a, const PairDev& P, const PairDev& Q,
+                                                const T AB[3], const T CD[3], int lane, T* acc,
+                                                unsigned long long& nprim) {
+  using PP = typename PrimT<T>::type;
+  const PP* bpp = prims_of<T>(a) + P.poff;
+  const PP* kpp = prims_of<T>(a) + Q.poff;
+  prim_loop_warp(a, bpp, kpp, P.pcnt, Q.pcnt, lane, nprim,
+                 [&](int cb, int cq) { prim_body<LA, LB, LC, LD, T, ATT>(a, bpp, kpp, cb, cq, AB, CD, acc); });
 }
 
 template <int LA, int LB, int LC, int LD, typename T>

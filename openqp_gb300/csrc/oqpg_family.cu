@@ -1,0 +1,553 @@
+// Shell families: one primitive integral for every shell pair that shares
+// its primitives.
+//
+// Correlation-consistent basis sets contract several s shells of an atom from
+// the same primitives (cc-pVDZ oxygen: the 1s and 2s both from nine
+// exponents).  OpenQP stores them as separate shells (segmented form) and its
+// Fock build (int2.F90:755-805, the shell-quartet loop) evaluates every shell
+// quartet on its own, so a quartet of such shells repeats the same primitive
+// integrals with other contraction coefficients.  Here the s shells of one
+// atom with identical exponents form a family (two shells at most), the
+// family pairs (two families, or a family and another shell) carry the union
+// of their members' primitive pairs, and a family quartet evaluates each
+// union primitive quartet once, with unit pair factors, and adds it to every
+// member combination with that combination's own factors K_ab/p K_cd/q.
+//
+// The result is the reference's sum term by term: each member keeps its own
+// primitive-pair screen (a dropped pair has factor 0), its own primitive-
+// quartet screen (|K/p K/q| / sqrt(p + q) against 1e-4 tau, decided per
+// combination), its own quartet screen (the mask k_lists_fam stores per
+// combination) and its own element cutoff and digestion (small_epilogue with
+// the member's shells).  Only the classes whose members x elements block fits
+// in registers are built this way ((ss|ss), (ss|sp), (ss|sd), (ss|pp),
+// (sp|sp): fam_class); the other quartets of family shells stay shell
+// quartets.  Plain FP64 SCF builds only (fam_on).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/openqp_gb300.h"
+#include "oqpg_internal.h"
+#include "oqpg_launch.cuh"
+
+namespace oqpg {
+
+// ---------------------------------------------------------------------------
+// Family-quartet lists: one CTA per family pair FP, walking the family pairs
+// FQ <= FP of its molecule in order of descending bound (the prefix that can
+// pass, as k_lists does for shell pairs).  Each member combination (P, Q) is
+// screened exactly as k_lists screens the shell quartet: the pair screen on
+// the larger of the two pair indices, then the quartet screen; a family
+// quartet is listed when some combination passes, with the passing ones in
+// its mask.  For FP == FQ the combinations with Q > P are the same quartets
+// as (Q, P) and are skipped.
+__device__ __forceinline__ unsigned fam_mask_transpose(unsigned m) {
+  unsigned t = 0;
+#pragma unroll
+  for (int i = 0; i < FAM_MAX; ++i)
+#pragma unroll
+    for (int j = 0; j < FAM_MAX; ++j) t |= ((m >> (4 * i + j)) & 1u) << (4 * j + i);
+  return t;
+}
+
+__global__ void __launch_bounds__(256) k_lists_fam(const ListArgs a) {
+  __shared__ unsigned cnt[NCLASS_SD], mcnt[NCLASS_SD];
+  __shared__ unsigned long long base[NCLASS_SD];
+  __shared__ int s_len;
+  const int FP = blockIdx.x;
+  const int mi = a.fpair_mol[FP];
+  const MolDev M = a.mols[mi];
+  const double dmax = __longlong_as_double((long long)a.dmax_bits[mi]);
+  const double qFP = a.fq[FP];
+  if (qFP * dmax < a.tau) return;
+  const int f0 = a.fmol0[mi];
+  if (threadIdx.x == 0) {
+    const double thr = a.tau / (4.0 * qFP * dmax) * (1.0 - 1e-9);
+    const double* sq = a.fsorted_q + f0;
+    int lo = 0, hi = a.fmoln[mi];
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (sq[mid] >= thr) lo = mid + 1;
+      else hi = mid;
+    }
+    s_len = lo;
+  }
+  __syncthreads();
+  const int len = s_len;
+  const int ns = M.ns;
+  const float* dshf = a.dshf + M.dsh0;
+  const double* dshd = a.dsh + M.dsh0;
+  const FamMem mp = a.fmem[FP];
+  const int tFP = a.fpair_type[FP];
+  const float tlo = (float)(a.tau * (1.0 - 1e-5)), thi = (float)(a.tau * (1.0 + 1e-5));
+  for (int s0 = 0; s0 < len; s0 += blockDim.x) {
+    if (threadIdx.x < NCLASS_SD) cnt[threadIdx.x] = mcnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int s = s0 + threadIdx.x;
+    const int FQ = s < len ? a.fsorted_idx[f0 + s] : 0x7fffffff;
+    int cl = -1;
+    unsigned slot = 0;
+    uint2 ent = make_uint2(0u, 0u);
+    if (FQ <= FP) {
+      const FamMem mq = a.fmem[FQ];
+      const int tFQ = a.fpair_type[FQ];
+      const int c = tFP <= tFQ ? class_index(tFP, tFQ) : class_index(tFQ, tFP);
+      if ((mp.n > 1 || mq.n > 1) && fam_class(c)) {
+        unsigned mask = 0;
+#pragma unroll
+        for (int m = 0; m < FAM_MAX; ++m) {
+          if (m >= mp.n) break;
+          const int P = mp.m[m];
+          const int2 ij = a.pair_ij[P];
+          const float* di = dshf + (long long)ij.x * ns;
+          const float* dj = dshf + (long long)ij.y * ns;
+          const float dij4 = 4.0f * di[ij.y];
+          const double qP = a.q[P];
+          const float qPf = a.qf[P];
+#pragma unroll
+          for (int n = 0; n < FAM_MAX; ++n) {
+            if (n >= mq.n) break;
+            const int Q = mq.m[n];
+            if (FQ == FP && Q > P) continue;
+            if (a.q[P > Q ? P : Q] * dmax < a.tau) continue;   // pair screen of the larger pair index
+            const int2 kl = a.pair_ij[Q];
+            const float tf = quartet_value_f32(a, ns, dshf, di, dj, dij4, qPf, Q, kl);
+            bool pass;
+            if (tf < tlo) pass = false;
+            else if (tf > thi) pass = true;
+            else pass = !(quartet_value(a, ns, dshd, ij, qP, Q, kl) < a.tau);
+            if (pass) mask |= 1u << (4 * m + n);
+          }
+        }
+        if (mask) {
+          cl = c;
+          ent = tFP <= tFQ ? fam_entry(FP, FQ, mask) : fam_entry(FQ, FP, fam_mask_transpose(mask));
+          slot = atomicAdd(&cnt[c], 1u);
+          atomicAdd(&mcnt[c], (unsigned)__popc(mask));
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < NCLASS_SD && cnt[threadIdx.x]) {
+      base[threadIdx.x] = atomicAdd(&a.counts[NCLASS + threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
+      atomicAdd(&a.fam_members[threadIdx.x], (unsigned long long)mcnt[threadIdx.x]);
+    }
+    __syncthreads();
+    if (cl >= 0 && a.write) {
+      const unsigned long long pos = base[cl] + slot;
+      if (pos < a.caps[NCLASS + cl]) a.lists[NCLASS + cl][pos] = ent;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Family-quartet integrals.
+template <int LA, int LB, int LC, int LD>
+struct FamCls {
+  static constexpr int MB = fam_members_max(LA, LB), MK = fam_members_max(LC, LD);
+  static constexpr int NE = Cls<LA, LB, LC, LD>::NE;
+  static constexpr int NACC = MB * MK * NE;   // member combination (m, n), element e at (m MK + n) NE + e
+};
+
+// The primitive-quartet screen of member combination (m, n):
+// (K_m/p K_n/q)^2 < prim_cut2 (p + q) drops it (int_rotaxis.F90:629), in FP32
+// outside the narrow band around the cutoff, else in FP64.
+__device__ __forceinline__ bool fam_keep(const BuildArgs& a, float r, double spm, double sqn, const PrimPair* bp,
+                                         const PrimPair* kp) {
+  if (r < a.prim_cut_lo) return false;
+  if (r > a.prim_cut_hi) return true;
+  const double f = spm * sqn;
+  return !(f * f < a.prim_cut2 * (__ldg(&bp->p) + __ldg(&kp->p)));
+}
+
+// One union primitive quartet (bra cb, ket cq): the block with unit pair
+// factors, then each member combination's share.  nb, nk: members of the two
+// family pairs (absent members have factor 0 as well).
+template <int LA, int LB, int LC, int LD>
+__device__ __forceinline__ void fam_body(const BuildArgs& a, const PrimPair* bpp, const PrimPair* kpp,
+                                         const FamCoef* bco, const FamCoef* kco, int cb, int cq, const double AB[3],
+                                         const double CD[3], int nb, int nk, double* acc) {
+  using F = FamCls<LA, LB, LC, LD>;
+  constexpr int NE = F::NE, MB = F::MB, MK = F::MK;
+  double v[NE];
+#pragma unroll
+  for (int e = 0; e < NE; ++e) v[e] = 0.0;
+  prim_body<LA, LB, LC, LD, double, false, true>(a, bpp, kpp, cb, cq, AB, CD, v);
+  const float2 bs = prim_screen(bpp + cb), ks = prim_screen(kpp + cq);
+  const float rs = rsqrtf(bs.y + ks.y);
+  double sq[MK];
+  float sqf[MK];
+#pragma unroll
+  for (int n = 0; n < MK; ++n) {
+    sq[n] = __ldg(&kco[cq].sp[n]);
+    sqf[n] = __ldg(&kco[cq].spf[n]);
+  }
+#pragma unroll
+  for (int m = 0; m < MB; ++m) {
+    if (m >= nb) break;
+    const double spm = __ldg(&bco[cb].sp[m]);
+    const float spmf = fabsf(__ldg(&bco[cb].spf[m]));
+    if constexpr (NE == 1) {
+      const double t = spm * v[0];
+#pragma unroll
+      for (int n = 0; n < MK; ++n) {
+        if (n >= nk) break;
+        const bool keep = fam_keep(a, spmf * fabsf(sqf[n]) * rs, spm, sq[n], bpp + cb, kpp + cq);
+        acc[m * MK + n] = fma(keep ? sq[n] : 0.0, t, acc[m * MK + n]);
+      }
+    } else {
+#pragma unroll
+      for (int n = 0; n < MK; ++n) {
+        if (n >= nk) break;
+        const bool keep = fam_keep(a, spmf * fabsf(sqf[n]) * rs, spm, sq[n], bpp + cb, kpp + cq);
+        const double f = keep ? spm * sq[n] : 0.0;
+#pragma unroll
+        for (int e = 0; e < NE; ++e) acc[(m * MK + n) * NE + e] = fma(f, v[e], acc[(m * MK + n) * NE + e]);
+      }
+    }
+  }
+}
+
+// Family quartet geometry: representative shells of the two family pairs.
+__device__ __forceinline__ void fam_geometry(const BuildArgs& a, const PairDev& P, const PairDev& Q, double AB[3],
+                                             double CD[3]) {
+  const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
+  AB[0] = SA.x - SB.x; AB[1] = SA.y - SB.y; AB[2] = SA.z - SB.z;
+  CD[0] = SC.x - SD.x; CD[1] = SC.y - SD.y; CD[2] = SC.z - SD.z;
+}
+
+// Member combination k = m MK + n of a family quartet digested as the shell
+// quartet (member m of the bra family pair | member n of the ket's): its
+// block is copied out of acc by compile-time selects (one epilogue instance).
+template <int LA, int LB, int LC, int LD, bool PURE>
+__device__ __forceinline__ void fam_digest(const BuildArgs& a, const FamMem& mb, const FamMem& mk, int k,
+                                           const double* acc) {
+  using F = FamCls<LA, LB, LC, LD>;
+  constexpr int NE = F::NE, MB = F::MB, MK = F::MK;
+  double blk[NE];
+  int P = 0, Q = 0;
+#pragma unroll
+  for (int e = 0; e < NE; ++e) blk[e] = 0.0;
+#pragma unroll
+  for (int kk = 0; kk < MB * MK; ++kk)
+    if (kk == k) {
+#pragma unroll
+      for (int e = 0; e < NE; ++e) blk[e] = acc[kk * NE + e];
+      P = mb.m[kk / MK];
+      Q = mk.m[kk % MK];
+    }
+  small_epilogue<LA, LB, LC, LD, PURE, false, double>(a, make_uint2((unsigned)P, (unsigned)Q), a.pairs[P], a.pairs[Q],
+                                                     blk);
+}
+
+// Thread per family quartet (the light ones): warps take chunks of the list
+// sorted by union primitive quartets, like k_small.
+template <int LA, int LB, int LC, int LD, bool PURE>
+__global__ void __launch_bounds__(128) k_fam_small(const BuildArgs a) {
+  using F = FamCls<LA, LB, LC, LD>;
+  constexpr int MB = F::MB, MK = F::MK;
+  const int lane = threadIdx.x & 31;
+  const uint2* quartets;
+  long long nquartets;
+  work_range(a, quartets, nquartets);
+  unsigned long long nprim = 0;
+  const unsigned chunk = a.chunk >= 32 ? (unsigned)a.chunk : 32u;
+  for (;;) {
+    const long long base = grab(a.work, chunk, lane);
+    if (base >= nquartets) break;
+    const long long end = base + chunk < nquartets ? base + chunk : nquartets;
+    for (long long t = base + lane; t < end; t += 32) {
+      const uint2 e = quartets[t];
+      const unsigned mask = fam_mask(e);
+      const PairDev P = a.fpairs[e.x & FAM_IDX_MASK], Q = a.fpairs[e.y & FAM_IDX_MASK];
+      const FamMem mb = a.fmem[e.x & FAM_IDX_MASK], mk = a.fmem[e.y & FAM_IDX_MASK];
+      double AB[3], CD[3];
+      fam_geometry(a, P, Q, AB, CD);
+      double acc[F::NACC];
+#pragma unroll
+      for (int i = 0; i < F::NACC; ++i) acc[i] = 0.0;
+      const PrimPair* bpp = a.fprims + P.poff;
+      const PrimPair* kpp = a.fprims + Q.poff;
+      const FamCoef* bco = a.fcoef + P.poff;
+      const FamCoef* kco = a.fcoef + Q.poff;
+      prim_loop_lane(a, bpp, kpp, P.pcnt, Q.pcnt, 0, 1, nprim, [&](int cb, int cq) {
+        fam_body<LA, LB, LC, LD>(a, bpp, kpp, bco, kco, cb, cq, AB, CD, mb.n, mk.n, acc);
+      });
+#pragma unroll 1
+      for (int k = 0; k < MB * MK; ++k)
+        if ((mask >> (4 * (k / MK) + k % MK)) & 1u) fam_digest<LA, LB, LC, LD, PURE>(a, mb, mk, k, acc);
+    }
+  }
+  if (a.counters && nprim) atomicAdd(a.counters, nprim);
+}
+
+// One warp per heavy family quartet: the lanes share its union primitive
+// quartets (dealt as in k_prim), the member blocks are summed over the warp,
+// and lane k digests member combination k.
+template <int LA, int LB, int LC, int LD, bool PURE>
+__global__ void __launch_bounds__(128) k_fam_warp(const BuildArgs a) {
+  using F = FamCls<LA, LB, LC, LD>;
+  constexpr int NE = F::NE, MB = F::MB, MK = F::MK;
+  const int lane = threadIdx.x & 31;
+  const uint2* quartets;
+  long long nquartets;
+  work_range(a, quartets, nquartets);
+  unsigned long long nprim = 0;
+  for (;;) {
+    const long long t = grab(a.work, 1u, lane);
+    if (t >= nquartets) break;
+    const uint2 e = quartets[t];
+    const unsigned mask = fam_mask(e);
+    const PairDev P = a.fpairs[e.x & FAM_IDX_MASK], Q = a.fpairs[e.y & FAM_IDX_MASK];
+    const FamMem mb = a.fmem[e.x & FAM_IDX_MASK], mk = a.fmem[e.y & FAM_IDX_MASK];
+    double AB[3], CD[3];
+    fam_geometry(a, P, Q, AB, CD);
+    double acc[F::NACC];
+#pragma unroll
+    for (int i = 0; i < F::NACC; ++i) acc[i] = 0.0;
+    const PrimPair* bpp = a.fprims + P.poff;
+    const PrimPair* kpp = a.fprims + Q.poff;
+    const FamCoef* bco = a.fcoef + P.poff;
+    const FamCoef* kco = a.fcoef + Q.poff;
+    prim_loop_warp(a, bpp, kpp, P.pcnt, Q.pcnt, lane, nprim, [&](int cb, int cq) {
+      fam_body<LA, LB, LC, LD>(a, bpp, kpp, bco, kco, cb, cq, AB, CD, mb.n, mk.n, acc);
+    });
+    // warp sums of the listed combinations (the mask is uniform over the warp)
+#pragma unroll
+    for (int k = 0; k < MB * MK; ++k) {
+      if (!((mask >> (4 * (k / MK) + k % MK)) & 1u)) continue;
+#pragma unroll
+      for (int i = 0; i < NE; ++i) {
+        double v = acc[k * NE + i];
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+        acc[k * NE + i] = v;
+      }
+    }
+    static_assert(MB * MK <= 32, "one lane per member combination");
+    if (lane < MB * MK && ((mask >> (4 * (lane / MK) + lane % MK)) & 1u))
+      fam_digest<LA, LB, LC, LD, PURE>(a, mb, mk, lane, acc);
+  }
+  if (a.counters && nprim) atomicAdd(a.counters, nprim);
+}
+
+template <int LA, int LB, int LC, int LD, bool PURE>
+cudaError_t launch_fam_cls(bool warp, const BuildArgs& a, int nsm, cudaStream_t st) {
+  if (warp) return launch_persistent(k_fam_warp<LA, LB, LC, LD, PURE>, 0, 4, a, nsm, st);
+  return launch_persistent(k_fam_small<LA, LB, LC, LD, PURE>, 0, 128, a, nsm, st);
+}
+
+cudaError_t launch_family(int c, bool pure, bool warp, const BuildArgs& a, int nsm, cudaStream_t st) {
+  switch (c) {
+    case 0: return launch_fam_cls<0, 0, 0, 0, false>(warp, a, nsm, st);
+    case 1: return launch_fam_cls<0, 0, 0, 1, false>(warp, a, nsm, st);
+    case 2: return pure ? launch_fam_cls<0, 0, 0, 2, true>(warp, a, nsm, st)
+                        : launch_fam_cls<0, 0, 0, 2, false>(warp, a, nsm, st);
+    case 3: return launch_fam_cls<0, 0, 1, 1, false>(warp, a, nsm, st);
+    case 6: return launch_fam_cls<0, 1, 0, 1, false>(warp, a, nsm, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host: the family tables.
+
+bool fam_on(const oqpg_ctx* c, const Job& job) {
+  return c->fam_enabled && c->nfpair > 0 && !split_on(c) && !df_on(c) && !job.gen && job.inv_mu2 == 0.0 &&
+         !petite_on(c, job);
+}
+
+namespace {
+
+template <typename T>
+cudaError_t upload_vec(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
+  cudaError_t e = b.ensure(std::max<size_t>(sizeof(T) * v.size(), 16));
+  if (e != cudaSuccess || v.empty()) return e;
+  return cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st);
+}
+
+}  // namespace
+
+// Families of each molecule (s shells on one atom with bitwise-equal exponent
+// lists, in shell order, two at most), and the family pairs of the family
+// classes' pair types, molecule by molecule (FA >= FB in family order; the
+// representative shells in kernel orientation, the side-A family holding the
+// first shell).  Member (x, y), x of side A, y of side B, is the canonical
+// shell pair of x and y; its factor on union primitive pair (i, j) is
+// K/p = sqrt(2) pi^(5/4) c_x,i c_y,j exp(-a_i a_j |AB|^2 / p) / p with the
+// reference's pair screens (int2_pairs.F90:179-266 and the rotated-axis
+// pre-screen |K|, |K/p| >= 1e-4 tau), evaluated with build_pairs's operation
+// order, so each member's nonzero factors are bitwise its own pair table's.
+int family_tables(oqpg_ctx* c, double cutoff) {
+  c->nfpair = 0;
+  c->nfam_multi = 0;
+  const double qcut = 1e-4 * cutoff, ecut = 25.0 * std::log(10.0);
+  const double sqrtpito52 = std::sqrt(2.0) * std::pow(3.14159265358979323846, 1.25);
+  const std::vector<int>& am = c->h_am;
+  const std::vector<int>& nc = c->h_ncontr;
+  const std::vector<int>& po = c->h_poff;
+  const double* ex = c->h_ex.data();
+  const double* cc = c->h_cc.data();
+  std::vector<PairDev> fpairs;
+  std::vector<FamMem> fmem;
+  std::vector<PrimPair> fprims;
+  std::vector<FamCoef> fcoef;
+  std::vector<int> fmol, ftype, fmol0(c->nmol), fmoln(c->nmol);
+  std::vector<double> fq;
+  std::vector<unsigned char> multi(c->npair, 0);
+  for (int mi = 0; mi < c->nmol; ++mi) {
+    const MolDev& M = c->mols[mi];
+    std::vector<std::vector<int>> fam;
+    for (int s = M.shell0; s < M.shell0 + M.ns; ++s) {
+      bool placed = false;
+      if (am[s] == 0)
+        for (auto& f : fam) {
+          const int r = f[0];
+          if (f.size() < 2 && am[r] == 0 && c->shell_atom[r] == c->shell_atom[s] && nc[r] == nc[s] &&
+              std::memcmp(ex + po[r], ex + po[s], sizeof(double) * nc[s]) == 0) {
+            f.push_back(s);
+            placed = true;
+            break;
+          }
+        }
+      if (!placed) fam.push_back({s});
+    }
+    fmol0[mi] = (int)fpairs.size();
+    for (size_t fa = 0; fa < fam.size(); ++fa)
+      for (size_t fb = 0; fb <= fa; ++fb) {
+        int sa = fam[fa][0], sb = fam[fb][0];
+        const bool swap = am[sa] > am[sb];
+        if (swap) std::swap(sa, sb);
+        const int t = pair_type(am[sa], am[sb]);
+        if (!fam_pair_type(t)) continue;
+        const std::vector<int>& FA = swap ? fam[fb] : fam[fa];
+        const std::vector<int>& FB = swap ? fam[fa] : fam[fb];
+        std::vector<std::pair<int, int>> ms;
+        if (fa == fb) {
+          for (size_t i = 0; i < FA.size(); ++i)
+            for (size_t j = 0; j <= i; ++j) ms.push_back({FA[i], FA[j]});
+        } else {
+          for (int x : FA)
+            for (int y : FB) ms.push_back({x, y});
+        }
+        FamMem fm{};
+        fm.n = (int)ms.size();
+        double q = 0.0;
+        for (int k = 0; k < FAM_MAX; ++k) fm.m[k] = -1;
+        for (size_t k = 0; k < ms.size(); ++k) {
+          int li = ms[k].first - M.shell0, lj = ms[k].second - M.shell0;
+          if (li < lj) std::swap(li, lj);
+          fm.m[k] = M.pair0 + li * (li + 1) / 2 + lj;
+          q = std::max(q, c->schwarz_pair[fm.m[k]]);
+        }
+        const ShellDev& A = c->shells[sa];
+        const ShellDev& B = c->shells[sb];
+        const double ab2 = (A.x - B.x) * (A.x - B.x) + (A.y - B.y) * (A.y - B.y) + (A.z - B.z) * (A.z - B.z);
+        PairDev pd;
+        pd.sha = sa;
+        pd.shb = sb;
+        pd.poff = (int)fprims.size();
+        for (int i = 0; i < nc[sa]; ++i)
+          for (int j = 0; j < nc[sb]; ++j) {
+            const double a1 = ex[po[sa] + i], a2 = ex[po[sb] + j];
+            const double g = a1 + a2;
+            double e12 = a1 * a2 * ab2;
+            if (e12 > g * ecut) continue;
+            const double gi = 1.0 / g;
+            e12 *= gi;
+            const double eab = std::exp(-e12);
+            FamCoef fc{};
+            double mx = 0.0;
+            for (size_t k = 0; k < ms.size(); ++k) {
+              const double k1 = cc[po[ms[k].first] + i] * cc[po[ms[k].second] + j] * eab;
+              if (std::fabs(k1) < qcut) continue;
+              const double sp = sqrtpito52 * k1 * gi;
+              if (std::fabs(sp) < qcut) continue;
+              fc.sp[k] = sp;
+              fc.spf[k] = (float)sp;
+              mx = std::max(mx, std::fabs(sp));
+            }
+            if (mx == 0.0) continue;
+            PrimPair pp;
+            pp.p = g;
+            pp.hp = 0.5 * gi;
+            pp.px = (a1 * A.x + a2 * B.x) * gi;
+            pp.py = (a1 * A.y + a2 * B.y) * gi;
+            pp.pz = (a1 * A.z + a2 * B.z) * gi;
+            const ShellDev& R = A.am == 0 ? B : A;   // the recursion runs on B when A is an s shell
+            pp.ax = pp.px - R.x;
+            pp.ay = pp.py - R.y;
+            pp.az = pp.pz - R.z;
+            pp.sp = mx;
+            pp.spf = (float)mx;
+            pp.pf = (float)g;
+            fprims.push_back(pp);
+            fcoef.push_back(fc);
+          }
+        pd.pcnt = (int)fprims.size() - pd.poff;
+        if (ms.size() > 1) {
+          ++c->nfam_multi;
+          for (size_t k = 0; k < ms.size(); ++k) multi[fm.m[k]] = 1;
+        }
+        fpairs.push_back(pd);
+        fmem.push_back(fm);
+        fmol.push_back(mi);
+        ftype.push_back(t);
+        fq.push_back(q);
+      }
+    fmoln[mi] = (int)fpairs.size() - fmol0[mi];
+  }
+  if (c->nfam_multi == 0 || fpairs.size() > FAM_IDX_MASK) {
+    c->nfam_multi = 0;
+    return OK;   // nothing to share (or too many family pairs for the list entries)
+  }
+  std::vector<int> order(fpairs.size());
+  for (size_t p = 0; p < order.size(); ++p) order[p] = (int)p;
+  for (int mi = 0; mi < c->nmol; ++mi)
+    std::stable_sort(order.begin() + fmol0[mi], order.begin() + fmol0[mi] + fmoln[mi],
+                     [&](int x, int y) { return fq[x] > fq[y]; });
+  std::vector<double> sq(order.size());
+  for (size_t p = 0; p < order.size(); ++p) sq[p] = fq[order[p]];
+  cudaStream_t st = c->stream;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = upload_vec(c->d_fpairs, fpairs, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fmem, fmem, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fprims, fprims, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fcoef, fcoef, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fpair_mol, fmol, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fpair_type, ftype, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fq, fq, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fsorted_idx, order, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fsorted_q, sq, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fmol0, fmol0, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fmoln, fmoln, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_pair_fam_multi, multi, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? NO_MEM : DEV_ERR;
+  c->nfpair = (int)fpairs.size();
+  return OK;
+}
+
+}  // namespace oqpg
+
+using namespace oqpg;
+
+extern "C" int oqpg_set_shell_families(oqpg_ctx* c, int on) {
+  if (!c) return NOT_INIT;
+  if (c->gexec) {   // a captured build holds the previous lists
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  c->fam_enabled = on != 0;
+  c->hb.sized = false;
+  return OK;
+}
+
+extern "C" int oqpg_shell_families_info(const oqpg_ctx* c, int* on, int* nshared) {
+  if (!c) return NOT_INIT;
+  if (on) *on = c->fam_enabled ? 1 : 0;
+  if (nshared) *nshared = c->nfpair > 0 ? c->nfam_multi : 0;
+  return OK;
+}

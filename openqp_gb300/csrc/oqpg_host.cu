@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
   const float dij4 = 4.0f * di[ij.y];
   const float tlo = (float)(a.tau * (1.0 - 1e-5)), thi = (float)(a.tau * (1.0 + 1e-5));
   const float mlo = (float)(a.tau_f32 * (1.0 - 1e-5)), mhi = (float)(a.tau_f32 * (1.0 + 1e-5));
+  const bool famP = a.fam && a.pair_fam_multi[P];
   // the petite list applies when the density is invariant under the group
   bool petite = false;
   if (a.sym_nops > 1) {
@@ -243,20 +244,15 @@ __global__ void __launch_bounds__(256) k_lists(const ListArgs a) {
     int c = -1;
     unsigned slot = 0;
     uint2 ent;
-    if (Q <= P) {
+    // quartets of a family class with a member-sharing pair are k_lists_fam's
+    const bool fam_skip = Q <= P && a.fam && (famP || a.pair_fam_multi[Q]) &&
+                          fam_class(tP <= a.pair_type[Q] ? class_index(tP, a.pair_type[Q])
+                                                         : class_index(a.pair_type[Q], tP));
+    if (Q <= P && !fam_skip) {
       const int2 kl = a.pair_ij[Q];
-      const float m = fmaxf(fmaxf(fmaxf(dij4, 4.0f * dshf[(long long)kl.x * ns + kl.y]), fmaxf(dj[kl.y], dj[kl.x])),
-                            fmaxf(di[kl.y], di[kl.x]));
-      const float tf = qPf * a.qf[Q] * m;
+      const float tf = quartet_value_f32(a, ns, dshf, di, dj, dij4, qPf, Q, kl);
       double t = -1.0;  // exact test value, computed only near a threshold
-      auto exact = [&]() {
-        const double* Di = dshd + (long long)ij.x * ns;
-        const double* Dj = dshd + (long long)ij.y * ns;
-        double v = qP * a.q[Q];
-        v *= fmax(fmax(fmax(4.0 * Di[ij.y], 4.0 * dshd[(long long)kl.x * ns + kl.y]), fmax(Dj[kl.y], Dj[kl.x])),
-                  fmax(Di[kl.y], Di[kl.x]));
-        return v;
-      };
+      auto exact = [&]() { return quartet_value(a, ns, dshd, ij, qP, Q, kl); };
       bool pass;
       if (tf < tlo) pass = false;
       else if (tf > thi) pass = true;
@@ -320,12 +316,13 @@ __device__ __forceinline__ int work_bin(int n) {
   return NBIN - 1 - (b < NBIN - 1 ? b : NBIN - 1);
 }
 
-__device__ __forceinline__ int prim_bin(const PairDev* pairs, uint2 q) {
-  return work_bin(pairs[entry_pair(q.x)].pcnt * pairs[q.y].pcnt);
+__device__ __forceinline__ int prim_bin(const PairDev* pairs, uint2 q, unsigned xmask, unsigned ymask) {
+  return work_bin(pairs[q.x & xmask].pcnt * pairs[q.y & ymask].pcnt);
 }
 
-__device__ __forceinline__ int survivor_bin(const PairDev* pairs, const PrimPair* prims, uint2 q, float lo) {
-  const PairDev P = pairs[entry_pair(q.x)], Q = pairs[q.y];
+__device__ __forceinline__ int survivor_bin(const PairDev* pairs, const PrimPair* prims, uint2 q, float lo,
+                                            unsigned xmask, unsigned ymask) {
+  const PairDev P = pairs[q.x & xmask], Q = pairs[q.y & ymask];
   // the heaviest quartets go to the primitive-parallel kernels whatever their
   // exact count: bin them by the product and spare the scan
   if (P.pcnt * Q.pcnt > 512) return work_bin(P.pcnt * Q.pcnt);
@@ -350,13 +347,13 @@ __device__ __forceinline__ long long list_len(long long n, const unsigned long l
 
 __global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const unsigned long long* n_dev,
                            const PairDev* __restrict__ pairs, const PrimPair* __restrict__ prims, float lo,
-                           unsigned char* bins, unsigned long long* hist) {
+                           unsigned xmask, unsigned ymask, unsigned char* bins, unsigned long long* hist) {
   __shared__ unsigned h[NBIN];
   n = list_len(n, n_dev);
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x) h[i] = 0;
   __syncthreads();
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int b = prims ? survivor_bin(pairs, prims, list[t], lo) : prim_bin(pairs, list[t]);
+    const int b = prims ? survivor_bin(pairs, prims, list[t], lo, xmask, ymask) : prim_bin(pairs, list[t], xmask, ymask);
     if (bins) bins[t] = (unsigned char)b;
     atomicAdd(&h[b], 1u);
   }
@@ -370,8 +367,8 @@ __global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const un
 // the primitive counts).
 __global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ list, long long n,
                                                      const unsigned long long* n_dev,
-                                                     const PairDev* __restrict__ pairs,
-                                                     const unsigned char* __restrict__ bins,
+                                                     const PairDev* __restrict__ pairs, unsigned xmask,
+                                                     unsigned ymask, const unsigned char* __restrict__ bins,
                                                      unsigned long long* cursors, uint2* out, long long chunk,
                                                      const unsigned* flag) {
   __shared__ unsigned h[NBIN];
@@ -384,7 +381,7 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ l
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x) h[i] = 0;
   __syncthreads();
   for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x)
-    atomicAdd(&h[bins ? bins[t] : prim_bin(pairs, list[t])], 1u);
+    atomicAdd(&h[bins ? bins[t] : prim_bin(pairs, list[t], xmask, ymask)], 1u);
   __syncthreads();
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x) {
     b[i] = h[i] ? atomicAdd(&cursors[i], (unsigned long long)h[i]) : 0ull;
@@ -393,7 +390,7 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ l
   __syncthreads();
   for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
     const uint2 q = list[t];
-    const int bin = bins ? bins[t] : prim_bin(pairs, q);
+    const int bin = bins ? bins[t] : prim_bin(pairs, q, xmask, ymask);
     const unsigned r = atomicAdd(&h[bin], 1u);
     out[b[bin] + r] = q;
   }
@@ -829,7 +826,9 @@ int ctx_init(oqpg_ctx* c, int nmol, const int* nshell_m, const int* natom_m, con
   // --- pair tables of the Fock build
   if ((rc = fock_tables(c, cutoff))) return rc;
   CK(cudaStreamSynchronize(st));
-  return upload_schwarz(c, c->schwarz_pair, c->d_q, c->d_qf, c->d_sorted_idx, c->d_sorted_q);
+  if ((rc = upload_schwarz(c, c->schwarz_pair, c->d_q, c->d_qf, c->d_sorted_idx, c->d_sorted_q))) return rc;
+  // --- shell families (shared primitives of generally contracted s shells)
+  return family_tables(c, cutoff);
 }
 
 }  // namespace
@@ -858,7 +857,10 @@ void ctx_free(oqpg_ctx* c) {
                     &c->d_sorted_idx, &c->d_sorted_q, &c->d_dp, &c->d_f, &c->d_fold, &c->d_gin, &c->d_gout,
                     &c->d_gpairs, &c->d_gprims, &c->d_galpha, &c->d_gprimsf, &c->d_galphaf, &c->d_coff,
                     &c->d_atom, &c->d_gmat, &c->d_gmatf, &c->d_dshg, &c->d_gcounts, &c->d_gwork, &c->d_de,
-                    &c->d_gcnt, &c->d_q_att, &c->d_qf_att, &c->d_sorted_idx_att, &c->d_sorted_q_att};
+                    &c->d_gcnt, &c->d_q_att, &c->d_qf_att, &c->d_sorted_idx_att, &c->d_sorted_q_att,
+                    &c->d_fpairs, &c->d_fmem, &c->d_fprims, &c->d_fcoef, &c->d_fpair_mol, &c->d_fpair_type,
+                    &c->d_fq, &c->d_fsorted_idx, &c->d_fsorted_q, &c->d_fmol0, &c->d_fmoln,
+                    &c->d_pair_fam_multi};
   for (DevBuf* b : bufs) b->release();
   c->hb.release();
   c->gb.release();
@@ -911,7 +913,7 @@ int ensure_bufs(oqpg_ctx* c, BuildBufs& B, const Job& job) {
   CK(B.dsh.ensure(sizeof(double) * std::max<long long>(c->dsh_elems, 1)));
   CK(B.dshf.ensure(sizeof(float) * std::max<long long>(c->dsh_elems, 1)));
   CK(B.dmax.ensure(sizeof(unsigned long long) * c->nmol));
-  CK(B.counts.ensure(sizeof(unsigned long long) * NLIST));
+  CK(B.counts.ensure(sizeof(unsigned long long) * (NLIST + NCLASS)));   // + family member quartets
   CK(B.primc.ensure(sizeof(unsigned long long) * NLIST));
   CK(B.hist.ensure(sizeof(unsigned long long) * NLIST * NBIN));
   CK(B.cursor.ensure(sizeof(unsigned long long) * NLIST * NBIN));
@@ -924,7 +926,7 @@ int ensure_bufs(oqpg_ctx* c, BuildBufs& B, const Job& job) {
     CK(B.sym.ensure(sizeof(unsigned long long) * 2));
     CK(B.fsk.ensure(sizeof(double) * (size_t)c->ntri * std::max(job.nfocks, 1)));
   }
-  if (!B.h_rb) CK(cudaMallocHost(&B.h_rb, sizeof(unsigned long long) * (1 + 2 * NLIST)));
+  if (!B.h_rb) CK(cudaMallocHost(&B.h_rb, sizeof(unsigned long long) * (1 + 2 * NLIST + NCLASS)));
   return OK;
 }
 
@@ -946,6 +948,21 @@ ListArgs list_args(const oqpg_ctx* c, BuildBufs& B, const Job& job) {
   la.tau_f32 = split_on(c) ? c->tau_f32 : 0.0;
   la.counts = B.counts.as<unsigned long long>();
   for (int k = 0; k < NLIST; ++k) { la.lists[k] = B.lists[k].as<uint2>(); la.caps[k] = B.cap[k]; }
+  if (fam_on(c, job)) {
+    la.fam = 1;
+    la.pair_fam_multi = c->d_pair_fam_multi.as<unsigned char>();
+    la.nfpair = c->nfpair;
+    la.fpairs = c->d_fpairs.as<PairDev>();
+    la.fmem = c->d_fmem.as<FamMem>();
+    la.fpair_mol = c->d_fpair_mol.as<int>();
+    la.fpair_type = c->d_fpair_type.as<int>();
+    la.fq = c->d_fq.as<double>();
+    la.fsorted_idx = c->d_fsorted_idx.as<int>();
+    la.fsorted_q = c->d_fsorted_q.as<double>();
+    la.fmol0 = c->d_fmol0.as<int>();
+    la.fmoln = c->d_fmoln.as<int>();
+    la.fam_members = B.counts.as<unsigned long long>() + NLIST;
+  }
   if (petite_on(c, job)) {
     la.sym_map = c->d_sym_map.as<int>();
     la.sym_nops = c->sym_nops;
@@ -1046,9 +1063,13 @@ int count_lists(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, unsi
   if ((rc = issue_densities(c, B, job, st))) return rc;
   ListArgs la = list_args(c, B, job);
   la.write = 0;
-  CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * NLIST, st));
+  CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * (NLIST + NCLASS), st));
   k_lists<<<c->npair, 256, 0, st>>>(la);
   CK(cudaGetLastError());
+  if (la.fam) {
+    k_lists_fam<<<c->nfpair, 256, 0, st>>>(la);
+    CK(cudaGetLastError());
+  }
   CK(cudaMemcpyAsync(counts, B.counts.p, sizeof(unsigned long long) * NLIST, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   return OK;
@@ -1070,20 +1091,30 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   else nlaunch += 2 + (split_on(c) ? (nk == 2 ? 2 : 1) : 0) + (df_on(c) ? (nk == 2 ? 2 : 1) : 0);
   ListArgs la = list_args(c, B, job);
   la.write = 1;
-  CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * NLIST, st));
+  B.fam = la.fam != 0;
+  CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * (NLIST + NCLASS), st));
   k_lists<<<c->npair, 256, 0, st>>>(la);
   CK(cudaGetLastError());
   ++nlaunch;
+  if (la.fam) {
+    k_lists_fam<<<c->nfpair, 256, 0, st>>>(la);
+    CK(cudaGetLastError());
+    ++nlaunch;
+  }
   // order every list by surviving primitive quartets (counting sort, device-side scan)
   CK(cudaMemsetAsync(B.hist.p, 0, sizeof(unsigned long long) * NLIST * NBIN, st));
   const float lo = (float)(1e-4 * c->tau * (1.0 - 1e-4));
   unsigned long long* counts = B.counts.as<unsigned long long>();
+  // the second list of a family class holds family quartets in family builds
+  auto fam_list = [&](int k) { return B.fam && k >= NCLASS && fam_class(k - NCLASS); };
   for (int k = 0; k < NLIST; ++k) {
     if (!B.cap[k]) continue;
     const long long cap = (long long)B.cap[k];
+    const bool fl = fam_list(k);
     k_bin_hist<<<(unsigned)std::min<long long>((cap + 255) / 256, c->nsm * 4LL), 256, 0, st>>>(
-        B.lists[k].as<uint2>(), cap, counts + k, c->d_pairs.as<PairDev>(), c->d_prims.as<PrimPair>(), lo,
-        B.bins[k].as<unsigned char>(), B.hist.as<unsigned long long>() + k * NBIN);
+        B.lists[k].as<uint2>(), cap, counts + k, (fl ? c->d_fpairs : c->d_pairs).as<PairDev>(),
+        (fl ? c->d_fprims : c->d_prims).as<PrimPair>(), lo, fl ? FAM_IDX_MASK : PAIR_MASK,
+        fl ? FAM_IDX_MASK : 0xffffffffu, B.bins[k].as<unsigned char>(), B.hist.as<unsigned long long>() + k * NBIN);
     CK(cudaGetLastError());
     ++nlaunch;
   }
@@ -1097,8 +1128,10 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   for (int k = 0; k < NLIST; ++k) {
     if (!B.cap[k]) continue;
     const long long cap = (long long)B.cap[k];
+    const bool fl = fam_list(k);
     k_bin_scatter<<<(unsigned)((cap + chunk - 1) / chunk), 256, 0, st>>>(
-        B.lists[k].as<uint2>(), cap, counts + k, c->d_pairs.as<PairDev>(), B.bins[k].as<unsigned char>(),
+        B.lists[k].as<uint2>(), cap, counts + k, (fl ? c->d_fpairs : c->d_pairs).as<PairDev>(),
+        fl ? FAM_IDX_MASK : PAIR_MASK, fl ? FAM_IDX_MASK : 0xffffffffu, B.bins[k].as<unsigned char>(),
         B.cursor.as<unsigned long long>() + k * NBIN, B.slists[k].as<uint2>(), chunk, B.flag.as<unsigned>());
     CK(cudaGetLastError());
     ++nlaunch;
@@ -1143,6 +1176,10 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   a.gj = B.gj.as<double>();
   a.gk = B.gk.as<double>();
   a.roots_f32 = (c->precision_mode == 2 || c->precision_mode == 4) ? 1 : 0;
+  a.fpairs = c->d_fpairs.as<PairDev>();
+  a.fmem = c->d_fmem.as<FamMem>();
+  a.fprims = c->d_fprims.as<PrimPair>();
+  a.fcoef = c->d_fcoef.as<FamCoef>();
   unsigned long long* ranges = B.ranges.as<unsigned long long>();
   // heaviest classes first
   for (int cl = NCLASS - 1; cl >= 0; --cl) {
@@ -1159,6 +1196,17 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
       a.quartets = B.slists[li].as<uint2>();
       a.nquartets = (long long)B.cap[li];
       a.team = B.team[li];
+      if (prec == 1 && B.fam && fam_class(cl)) {
+        // family quartets: the heavy head warp per quartet, the rest thread per quartet
+        a.range = ranges + 4 * li;
+        a.work = B.work.as<unsigned long long>() + NLIST + li;
+        CK(launch_family(cl, c->pure, true, a, c->nsm, st));
+        a.range = ranges + 4 * li + 2;
+        a.work = B.work.as<unsigned long long>() + li;
+        CK(launch_family(cl, c->pure, false, a, c->nsm, st));
+        nlaunch += 2;
+        continue;
+      }
       if (class_info(cl).prim && eff_split(c, cl, B.team[li] != 0) < 64) {
         // quartets with >= 2^split primitive quartets (a prefix of the sorted
         // list) go to the warp-per-quartet primitive-parallel kernel
@@ -1193,6 +1241,8 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   CK(cudaMemcpyAsync(B.h_rb + 1, B.counts.p, sizeof(unsigned long long) * NLIST, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(B.h_rb + 1 + NLIST, B.primc.p, sizeof(unsigned long long) * NLIST, cudaMemcpyDeviceToHost,
                      st));
+  CK(cudaMemcpyAsync(B.h_rb + 1 + 2 * NLIST, B.counts.as<unsigned long long>() + NLIST,
+                     sizeof(unsigned long long) * NCLASS, cudaMemcpyDeviceToHost, st));
   if (nlaunch_out) *nlaunch_out = nlaunch;
   return OK;
 }
@@ -1210,13 +1260,18 @@ void record_stats(oqpg_ctx* c, const BuildBufs& B, int nlaunch, bool timing) {
   double* S = c->last_stats;
   S[1] = 0;
   double nq = 0, q32 = 0, p32 = 0;
+  const unsigned long long* fmq = B.h_rb + 1 + 2 * NLIST;   // member quartets of the family lists
   for (int k = 0; k < NCLASS; ++k) {
-    const unsigned long long q = cnt[k] + cnt[NCLASS + k];
+    // quartets: the shell quartets evaluated (a family quartet counts its members)
+    const bool fl = B.fam && fam_class(k);
+    const unsigned long long q = cnt[k] + (fl ? fmq[k] : cnt[NCLASS + k]);
     nq += (double)q;
     S[7 + k] = (double)q;
     S[7 + NCLASS + k] = (double)nprim[k] + (double)nprim[NCLASS + k];
-    q32 += (double)cnt[NCLASS + k];
-    p32 += (double)nprim[NCLASS + k];
+    if (!fl) {
+      q32 += (double)cnt[NCLASS + k];
+      p32 += (double)nprim[NCLASS + k];
+    }
     float tk = 0, t32 = 0;
     if (timing && (B.cap[k] || B.cap[NCLASS + k])) {
       cudaEventElapsedTime(&tk, c->evc[k][0], c->evc[k][1]);
@@ -1648,6 +1703,11 @@ int oqpg_set_cutoff(oqpg_ctx* ctx, double cutoff) {
     }
     if ((rc = upload(ctx->d_pairs, pr, ctx->stream))) return rc;
     CK(cudaStreamSynchronize(ctx->stream));
+  }
+  if ((rc = family_tables(ctx, cutoff))) return rc;
+  if (ctx->gexec) {   // a captured build holds the previous tables
+    cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
   }
   ctx->tau = cutoff;
   ctx->hb.sized = false;  // the lists are sized by a fresh count pass

@@ -65,7 +65,43 @@ struct ListArgs {
   int sym_nops;
   int sym_ns;
   const unsigned long long* sym_bits;
+  // shell families: k_lists leaves the quartets of the family classes with a
+  // member-sharing side (pair_fam_multi) to k_lists_fam, which lists family
+  // quartets into the second list of those classes
+  int fam;
+  const unsigned char* pair_fam_multi;   // per pair: its family pair has more than one member
+  int nfpair;
+  const PairDev* fpairs;
+  const FamMem* fmem;
+  const int* fpair_mol;
+  const int* fpair_type;
+  const double* fq;                      // family Schwarz bound: the largest member bound
+  const int* fsorted_idx;                // per molecule: its family pairs by descending bound
+  const double* fsorted_q;
+  const int* fmol0;                      // first family pair of each molecule
+  const int* fmoln;                      // and their number
+  unsigned long long* fam_members;       // per class: member quartets listed (statistics)
 };
+
+// The quartet screen of k_lists (int2.F90:975-986) for bra pair (shells ij,
+// bound qP) and ket pair Q (shells kl): the FP32 test value
+// Q_P Q_Q max(4D_ij, 4D_kl, D_jl, D_jk, D_il, D_ik) and, with the reference's
+// operation order, the FP64 one.  di, dj: the shell-density rows of i and j.
+__device__ __forceinline__ float quartet_value_f32(const ListArgs& a, int ns, const float* dshf, const float* di,
+                                                   const float* dj, float dij4, float qPf, int Q, int2 kl) {
+  const float m = fmaxf(fmaxf(fmaxf(dij4, 4.0f * dshf[(long long)kl.x * ns + kl.y]), fmaxf(dj[kl.y], dj[kl.x])),
+                        fmaxf(di[kl.y], di[kl.x]));
+  return qPf * a.qf[Q] * m;
+}
+__device__ __forceinline__ double quartet_value(const ListArgs& a, int ns, const double* dshd, int2 ij, double qP,
+                                                int Q, int2 kl) {
+  const double* Di = dshd + (long long)ij.x * ns;
+  const double* Dj = dshd + (long long)ij.y * ns;
+  double v = qP * a.q[Q];
+  v *= fmax(fmax(fmax(4.0 * Di[ij.y], 4.0 * dshd[(long long)kl.x * ns + kl.y]), fmax(Dj[kl.y], Dj[kl.x])),
+            fmax(Di[kl.y], Di[kl.x]));
+  return v;
+}
 
 struct DevBuf {
   void* p = nullptr;
@@ -97,15 +133,19 @@ __global__ void k_dsh(const double* __restrict__ dp, int nfocks, const MolDev* _
                       const int* __restrict__ aoff, const int* __restrict__ nao, double* dsh, float* dshf,
                       unsigned long long* dmax_bits);
 __global__ void k_lists(const ListArgs a);
+// family quartets (oqpg_family.cu), one CTA per family pair
+__global__ void k_lists_fam(const ListArgs a);
 // n entries, or with n_dev the device count min(*n_dev, n) (n is then the capacity)
 // prims null: bins by the product of the pair primitive counts; else by the
 // primitive quartets passing the FP32 pre-screen at lo (bins[t] stores each bin)
+// (xmask, ymask: the bits of an entry's x and y that hold the pair indices)
 __global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const unsigned long long* n_dev,
                            const PairDev* __restrict__ pairs, const PrimPair* __restrict__ prims, float lo,
-                           unsigned char* bins, unsigned long long* hist);
+                           unsigned xmask, unsigned ymask, unsigned char* bins, unsigned long long* hist);
 __global__ void k_bin_scatter(const uint2* __restrict__ list, long long n, const unsigned long long* n_dev,
-                              const PairDev* __restrict__ pairs, const unsigned char* __restrict__ bins,
-                              unsigned long long* cursors, uint2* out, long long chunk, const unsigned* flag);
+                              const PairDev* __restrict__ pairs, unsigned xmask, unsigned ymask,
+                              const unsigned char* __restrict__ bins, unsigned long long* cursors, uint2* out,
+                              long long chunk, const unsigned* flag);
 __global__ void k_bin_scan(const unsigned long long* counts, const unsigned long long* caps, const int* split_bins,
                            const unsigned long long* hist, unsigned long long* cursors, unsigned long long* ranges,
                            unsigned* overflow);
@@ -203,6 +243,10 @@ bool petite_on(const oqpg_ctx* c, const Job& job);
 int petite_check(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st);
 int petite_finalize(oqpg_ctx* c, BuildBufs& B, const Job& job, double ck, cudaStream_t st);
 int ensure_att(oqpg_ctx* c, double mu);
+// shell families (oqpg_family.cu): the family tables at a cutoff (after the
+// Schwarz bounds), and whether a job's build lists family quartets
+int family_tables(oqpg_ctx* c, double cutoff);
+bool fam_on(const oqpg_ctx* c, const Job& job);
 
 // Layout of an MRSF-type operand: component m of vector v, element (r, c) at
 // m sm + v sv + r rs + c cs.
@@ -230,7 +274,10 @@ struct BuildBufs {
   unsigned long long cap[NLIST] = {0};
   unsigned char team[NLIST] = {0};     // list runs the warp-per-quartet kernels (set with the sizes)
   bool sized = false;
-  unsigned long long* h_rb = nullptr;  // pinned readback: [0] flag, [1, 1+NLIST) counts, then primitive counts
+  bool fam = false;                    // the last build issued listed family quartets
+  // pinned readback: [0] flag, [1, 1+NLIST) counts, then NLIST primitive
+  // counts, then NCLASS member quartets of the family lists
+  unsigned long long* h_rb = nullptr;
   void release() {
     DevBuf* b[] = {&dj, &dk, &djf, &dkf, &djdf, &dkdf, &gj, &gk, &dsh, &dshf, &dmax, &counts, &primc, &hist,
                    &cursor, &work, &ranges, &caps, &split, &flag, &gtab, &sym, &fsk};
@@ -279,6 +326,11 @@ struct oqpg_ctx {
   // petite list: nops >= 2 symmetry operations (abelian: signed AO permutations)
   int sym_nops = 0;
   oqpg::DevBuf d_sym_map, d_sym_inv, d_sym_sgn;   // shell images; AO preimages and their signs
+  // shell families (oqpg_family.cu): on by default; tables at the current cutoff
+  bool fam_enabled = true;
+  int nfpair = 0, nfam_multi = 0;   // family pairs; those with more than one member
+  oqpg::DevBuf d_fpairs, d_fmem, d_fprims, d_fcoef, d_fpair_mol, d_fpair_type, d_fq, d_fsorted_idx, d_fsorted_q,
+      d_fmol0, d_fmoln, d_pair_fam_multi;
   // precision split: 0 = every quartet in FP64, 1 = bound < tau_f32 in FP32
   int precision_mode = 0;
   double tau_f32 = 0.0;

@@ -170,7 +170,8 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
     if (!h_counts[k]) continue;
     k_bin_hist<<<(unsigned)((h_counts[k] + 255) / 256), 256, 0, st>>>(lists + off[k], (long long)h_counts[k], nullptr,
                                                                       c->d_pairs.as<PairDev>(), nullptr, 0.0f,
-                                                                      nullptr, hist + k * NBIN);
+                                                                      PAIR_MASK, 0xffffffffu, nullptr,
+                                                                      hist + k * NBIN);
     NK(cudaGetLastError());
   }
   unsigned long long h_hist[NCLASS * NBIN], h_cur[NCLASS * NBIN];
@@ -186,8 +187,8 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
     if (!h_counts[k]) continue;
     const long long chunk = 4096;
     k_bin_scatter<<<(unsigned)((h_counts[k] + chunk - 1) / chunk), 256, 0, st>>>(
-        lists + off[k], (long long)h_counts[k], nullptr, c->d_pairs.as<PairDev>(), nullptr, cursor + k * NBIN,
-        slists + off[k], chunk, nullptr);
+        lists + off[k], (long long)h_counts[k], nullptr, c->d_pairs.as<PairDev>(), PAIR_MASK, 0xffffffffu, nullptr,
+        cursor + k * NBIN, slists + off[k], chunk, nullptr);
     NK(cudaGetLastError());
   }
   // integrals and digestion

@@ -303,6 +303,21 @@ class FockBuilder:
         lib().oqpg_get_kernel_family(self.h, ptr(f, _i), ptr(av, _i))
         return f.tolist(), av.tolist()
 
+    def set_shell_families(self, on):
+        """Share the primitive integrals of s shells with equal exponents on
+        one atom (cc-pVXZ's generally contracted shells) in the (ss|ss),
+        (ss|sp), (ss|sd), (ss|pp), (sp|sp) classes of plain FP64 SCF builds
+        (default on); off: every shell quartet on its own."""
+        rc = lib().oqpg_set_shell_families(self.h, 1 if on else 0)
+        if rc != 0:
+            raise FockError(rc, "oqpg_set_shell_families")
+
+    def shell_families_info(self):
+        """(on, family pairs with more than one member shell pair)"""
+        on, n = ctypes.c_int(0), ctypes.c_int(0)
+        lib().oqpg_shell_families_info(self.h, ctypes.byref(on), ctypes.byref(n))
+        return bool(on.value), n.value
+
     def set_precision(self, mode, threshold=1e-6):
         """mode "fp64": plain path; mode "mixed": quartets whose screening value
         (Schwarz bound x shell density) is below threshold run in FP32 with their
