@@ -324,14 +324,15 @@ int oqpg_get_kernel_family(const oqpg_ctx* ctx, int* family, int* available);
 /* Shell families (on by default): s shells of one atom with the same
  * primitive exponents (the generally contracted shells of cc-pVXZ sets, which
  * OpenQP stores as separate segmented shells) share their primitive
- * integrals in the (ss|ss), (ss|sp), (ss|sd), (ss|pp) and (sp|sp) classes of
- * plain FP64 SCF builds: one primitive integral per family quartet, added to
- * every member shell quartet with its own contraction factors, primitive
- * screens, quartet screen, element cutoff and digestion, so the result is the
- * reference's shell-by-shell sum.  on = 0 evaluates every shell quartet on
- * its own.  info: on, and the family pairs with more than one member shell
- * pair (0: the basis has no shared primitives).  No counterpart in the
- * reference (int2.F90 loops over shell quartets). */
+ * integrals in the (ss|ss), (ss|sp), (ss|sd), (ss|pp), (ss|pd), (sp|sp),
+ * (sp|sd) and (sp|pp) classes of plain FP64 SCF builds: one primitive
+ * integral per family quartet, added to every member shell quartet with its
+ * own contraction factors, primitive screens, quartet screen, element cutoff
+ * and digestion, so the result is the reference's shell-by-shell sum.
+ * on = 0 evaluates every shell quartet on its own.  info: on, and the family
+ * pairs with more than one member shell pair (0: the basis has no shared
+ * primitives).  No counterpart in the reference (int2.F90 loops over shell
+ * quartets). */
 int oqpg_set_shell_families(oqpg_ctx* ctx, int on);
 int oqpg_shell_families_info(const oqpg_ctx* ctx, int* on, int* nshared);
 

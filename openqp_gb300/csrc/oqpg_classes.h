@@ -60,27 +60,27 @@ __host__ __device__ constexpr bool has_team(int la, int lb, int lc, int ld) {
 // type (la <= lb) can have (families are s shells, two at most), and the
 // classes built as family quartets: members on some side, and a block of
 // members x elements small enough for registers ((ss|ss), (ss|sp), (ss|sd),
-// (ss|pp), (sp|sp)).
+// (ss|pp), (ss|pd), (sp|sp), (sp|sd), (sp|pp)).
 __host__ __device__ constexpr int fam_members_max(int la, int lb) {
   return la == 0 ? (lb == 0 ? 4 : 2) : 1;
 }
 __host__ __device__ constexpr bool fam_class_l(int la, int lb, int lc, int ld) {
   return la <= 2 && lb <= 2 && lc <= 2 && ld <= 2 && fam_members_max(la, lb) * fam_members_max(lc, ld) > 1 &&
-         ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) * fam_members_max(la, lb) * fam_members_max(lc, ld) <= 48;
+         ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) * fam_members_max(la, lb) * fam_members_max(lc, ld) <= 72;
 }
-__host__ __device__ inline bool fam_class(int c) { return c == 0 || c == 1 || c == 2 || c == 3 || c == 6; }
+__host__ __device__ inline bool fam_class(int c) { return c <= 4 || (c >= 6 && c <= 8); }
 constexpr bool fam_class_table_ok() {   // the list above is fam_class_l over the s-d classes
   for (int tb = 0; tb < NPAIRTYPE_SD; ++tb)
     for (int tk = tb; tk < NPAIRTYPE_SD; ++tk) {
       const int c = tb * NPAIRTYPE_SD - tb * (tb - 1) / 2 + (tk - tb);
-      const bool listed = c == 0 || c == 1 || c == 2 || c == 3 || c == 6;
+      const bool listed = c <= 4 || (c >= 6 && c <= 8);
       if (listed != fam_class_l(PAIR_L[tb][0], PAIR_L[tb][1], PAIR_L[tk][0], PAIR_L[tk][1])) return false;
     }
   return true;
 }
-static_assert(fam_class_table_ok(), "family classes: (ss|ss) 0, (ss|sp) 1, (ss|sd) 2, (ss|pp) 3, (sp|sp) 6");
-// Family-pair types: the pair types of the family classes (ss, sp, sd, pp).
-__host__ __device__ inline bool fam_pair_type(int t) { return t <= 3; }
+static_assert(fam_class_table_ok(), "family classes: 0-4 (ss|ss..pd), 6-8 (sp|sp), (sp|sd), (sp|pp)");
+// Family-pair types: the pair types of the family classes (ss, sp, sd, pp, pd).
+__host__ __device__ inline bool fam_pair_type(int t) { return t <= 4; }
 cudaError_t launch_family(int c, bool pure, bool warp, const BuildArgs& a, int nsm, cudaStream_t st);
 
 // Thread per quartet by default from this many quartets per SM in a list

@@ -20,8 +20,8 @@
 // combination) and its own element cutoff and digestion (small_epilogue with
 // the member's shells).  Only the classes whose members x elements block fits
 // in registers are built this way ((ss|ss), (ss|sp), (ss|sd), (ss|pp),
-// (sp|sp): fam_class); the other quartets of family shells stay shell
-// quartets.  Plain FP64 SCF builds only (fam_on).
+// (ss|pd), (sp|sp), (sp|sd), (sp|pp): fam_class); the other quartets of
+// family shells stay shell quartets.  Plain FP64 SCF builds only (fam_on).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -36,7 +36,9 @@ namespace oqpg {
 // ---------------------------------------------------------------------------
 // Family-quartet lists: one CTA per family pair FP, walking the family pairs
 // FQ <= FP of its molecule in order of descending bound (the prefix that can
-// pass, as k_lists does for shell pairs).  Each member combination (P, Q) is
+// pass, as k_lists does for shell pairs); a one-member FP walks only the
+// family pairs with several members (quartets of two one-member pairs are
+// k_lists's).  Each member combination (P, Q) is
 // screened exactly as k_lists screens the shell quartet: the pair screen on
 // the larger of the two pair indices, then the quartet screen; a family
 // quartet is listed when some combination passes, with the passing ones in
@@ -61,11 +63,14 @@ __global__ void __launch_bounds__(256) k_lists_fam(const ListArgs a) {
   const double dmax = __longlong_as_double((long long)a.dmax_bits[mi]);
   const double qFP = a.fq[FP];
   if (qFP * dmax < a.tau) return;
-  const int f0 = a.fmol0[mi];
+  const FamMem mp = a.fmem[FP];
+  const bool single = mp.n == 1;
+  const int f0 = single ? a.fmmol0[mi] : a.fmol0[mi];
+  const int* sorted_idx = single ? a.fmsorted_idx : a.fsorted_idx;
   if (threadIdx.x == 0) {
     const double thr = a.tau / (4.0 * qFP * dmax) * (1.0 - 1e-9);
-    const double* sq = a.fsorted_q + f0;
-    int lo = 0, hi = a.fmoln[mi];
+    const double* sq = (single ? a.fmsorted_q : a.fsorted_q) + f0;
+    int lo = 0, hi = single ? a.fmmoln[mi] : a.fmoln[mi];
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
       if (sq[mid] >= thr) lo = mid + 1;
@@ -78,14 +83,13 @@ __global__ void __launch_bounds__(256) k_lists_fam(const ListArgs a) {
   const int ns = M.ns;
   const float* dshf = a.dshf + M.dsh0;
   const double* dshd = a.dsh + M.dsh0;
-  const FamMem mp = a.fmem[FP];
   const int tFP = a.fpair_type[FP];
   const float tlo = (float)(a.tau * (1.0 - 1e-5)), thi = (float)(a.tau * (1.0 + 1e-5));
   for (int s0 = 0; s0 < len; s0 += blockDim.x) {
     if (threadIdx.x < NCLASS_SD) cnt[threadIdx.x] = mcnt[threadIdx.x] = 0;
     __syncthreads();
     const int s = s0 + threadIdx.x;
-    const int FQ = s < len ? a.fsorted_idx[f0 + s] : 0x7fffffff;
+    const int FQ = s < len ? sorted_idx[f0 + s] : 0x7fffffff;
     int cl = -1;
     unsigned slot = 0;
     uint2 ent = make_uint2(0u, 0u);
@@ -162,28 +166,51 @@ __device__ __forceinline__ bool fam_keep(const BuildArgs& a, float r, double spm
   return !(f * f < a.prim_cut2 * (__ldg(&bp->p) + __ldg(&kp->p)));
 }
 
+// Accumulators of one family quartet in one lane, with the ket factors of
+// the current ket primitive (the union primitive quartets arrive in
+// increasing c = kq nP + kb, so they are loaded once per ket primitive).
+template <int LA, int LB, int LC, int LD>
+struct FamAcc {
+  using F = FamCls<LA, LB, LC, LD>;
+  double acc[F::NACC];
+  double sq[F::MK];
+  float sqf[F::MK];
+  int kq = -1;
+};
+
+template <int LA, int LB, int LC, int LD>
+__device__ __forceinline__ void fam_acc_init(FamAcc<LA, LB, LC, LD>& s) {
+  using F = FamCls<LA, LB, LC, LD>;
+#pragma unroll
+  for (int i = 0; i < F::NACC; ++i) s.acc[i] = 0.0;
+  s.kq = -1;
+}
+
 // One union primitive quartet (bra cb, ket cq): the block with unit pair
-// factors, then each member combination's share.  nb, nk: members of the two
-// family pairs (absent members have factor 0 as well).
+// factors, then each member combination's share, K_m/p K_n/q, or nothing
+// where the combination's own primitive-quartet screen drops the quartet.
+// nb, nk: members of the two family pairs.  (Taking the ket factors out of
+// each ket-primitive row instead, NE x nb FMAs per quartet plus a flush per
+// row, measured slower: after screening the rows are short.)
 template <int LA, int LB, int LC, int LD>
 __device__ __forceinline__ void fam_body(const BuildArgs& a, const PrimPair* bpp, const PrimPair* kpp,
                                          const FamCoef* bco, const FamCoef* kco, int cb, int cq, const double AB[3],
-                                         const double CD[3], int nb, int nk, double* acc) {
+                                         const double CD[3], int nb, int nk, FamAcc<LA, LB, LC, LD>& s) {
   using F = FamCls<LA, LB, LC, LD>;
   constexpr int NE = F::NE, MB = F::MB, MK = F::MK;
+  if (cq != s.kq) {
+    s.kq = cq;
+#pragma unroll
+    for (int n = 0; n < MK; ++n) {
+      s.sq[n] = __ldg(&kco[cq].sp[n]);
+      s.sqf[n] = fabsf(__ldg(&kco[cq].spf[n]));
+    }
+  }
   double v[NE];
 #pragma unroll
   for (int e = 0; e < NE; ++e) v[e] = 0.0;
   prim_body<LA, LB, LC, LD, double, false, true>(a, bpp, kpp, cb, cq, AB, CD, v);
-  const float2 bs = prim_screen(bpp + cb), ks = prim_screen(kpp + cq);
-  const float rs = rsqrtf(bs.y + ks.y);
-  double sq[MK];
-  float sqf[MK];
-#pragma unroll
-  for (int n = 0; n < MK; ++n) {
-    sq[n] = __ldg(&kco[cq].sp[n]);
-    sqf[n] = __ldg(&kco[cq].spf[n]);
-  }
+  const float rs = rsqrtf(prim_screen(bpp + cb).y + prim_screen(kpp + cq).y);
 #pragma unroll
   for (int m = 0; m < MB; ++m) {
     if (m >= nb) break;
@@ -194,17 +221,17 @@ __device__ __forceinline__ void fam_body(const BuildArgs& a, const PrimPair* bpp
 #pragma unroll
       for (int n = 0; n < MK; ++n) {
         if (n >= nk) break;
-        const bool keep = fam_keep(a, spmf * fabsf(sqf[n]) * rs, spm, sq[n], bpp + cb, kpp + cq);
-        acc[m * MK + n] = fma(keep ? sq[n] : 0.0, t, acc[m * MK + n]);
+        const bool keep = fam_keep(a, spmf * s.sqf[n] * rs, spm, s.sq[n], bpp + cb, kpp + cq);
+        s.acc[m * MK + n] = fma(keep ? s.sq[n] : 0.0, t, s.acc[m * MK + n]);
       }
     } else {
 #pragma unroll
       for (int n = 0; n < MK; ++n) {
         if (n >= nk) break;
-        const bool keep = fam_keep(a, spmf * fabsf(sqf[n]) * rs, spm, sq[n], bpp + cb, kpp + cq);
-        const double f = keep ? spm * sq[n] : 0.0;
+        const bool keep = fam_keep(a, spmf * s.sqf[n] * rs, spm, s.sq[n], bpp + cb, kpp + cq);
+        const double f = keep ? spm * s.sq[n] : 0.0;
 #pragma unroll
-        for (int e = 0; e < NE; ++e) acc[(m * MK + n) * NE + e] = fma(f, v[e], acc[(m * MK + n) * NE + e]);
+        for (int e = 0; e < NE; ++e) s.acc[(m * MK + n) * NE + e] = fma(f, v[e], s.acc[(m * MK + n) * NE + e]);
       }
     }
   }
@@ -265,19 +292,18 @@ __global__ void __launch_bounds__(128) k_fam_small(const BuildArgs a) {
       const FamMem mb = a.fmem[e.x & FAM_IDX_MASK], mk = a.fmem[e.y & FAM_IDX_MASK];
       double AB[3], CD[3];
       fam_geometry(a, P, Q, AB, CD);
-      double acc[F::NACC];
-#pragma unroll
-      for (int i = 0; i < F::NACC; ++i) acc[i] = 0.0;
+      FamAcc<LA, LB, LC, LD> s;
+      fam_acc_init(s);
       const PrimPair* bpp = a.fprims + P.poff;
       const PrimPair* kpp = a.fprims + Q.poff;
       const FamCoef* bco = a.fcoef + P.poff;
       const FamCoef* kco = a.fcoef + Q.poff;
       prim_loop_lane(a, bpp, kpp, P.pcnt, Q.pcnt, 0, 1, nprim, [&](int cb, int cq) {
-        fam_body<LA, LB, LC, LD>(a, bpp, kpp, bco, kco, cb, cq, AB, CD, mb.n, mk.n, acc);
+        fam_body<LA, LB, LC, LD>(a, bpp, kpp, bco, kco, cb, cq, AB, CD, mb.n, mk.n, s);
       });
 #pragma unroll 1
       for (int k = 0; k < MB * MK; ++k)
-        if ((mask >> (4 * (k / MK) + k % MK)) & 1u) fam_digest<LA, LB, LC, LD, PURE>(a, mb, mk, k, acc);
+        if ((mask >> (4 * (k / MK) + k % MK)) & 1u) fam_digest<LA, LB, LC, LD, PURE>(a, mb, mk, k, s.acc);
     }
   }
   if (a.counters && nprim) atomicAdd(a.counters, nprim);
@@ -304,16 +330,16 @@ __global__ void __launch_bounds__(128) k_fam_warp(const BuildArgs a) {
     const FamMem mb = a.fmem[e.x & FAM_IDX_MASK], mk = a.fmem[e.y & FAM_IDX_MASK];
     double AB[3], CD[3];
     fam_geometry(a, P, Q, AB, CD);
-    double acc[F::NACC];
-#pragma unroll
-    for (int i = 0; i < F::NACC; ++i) acc[i] = 0.0;
+    FamAcc<LA, LB, LC, LD> s;
+    fam_acc_init(s);
     const PrimPair* bpp = a.fprims + P.poff;
     const PrimPair* kpp = a.fprims + Q.poff;
     const FamCoef* bco = a.fcoef + P.poff;
     const FamCoef* kco = a.fcoef + Q.poff;
     prim_loop_warp(a, bpp, kpp, P.pcnt, Q.pcnt, lane, nprim, [&](int cb, int cq) {
-      fam_body<LA, LB, LC, LD>(a, bpp, kpp, bco, kco, cb, cq, AB, CD, mb.n, mk.n, acc);
+      fam_body<LA, LB, LC, LD>(a, bpp, kpp, bco, kco, cb, cq, AB, CD, mb.n, mk.n, s);
     });
+    double* acc = s.acc;
     // warp sums of the listed combinations (the mask is uniform over the warp)
 #pragma unroll
     for (int k = 0; k < MB * MK; ++k) {
@@ -346,7 +372,12 @@ cudaError_t launch_family(int c, bool pure, bool warp, const BuildArgs& a, int n
     case 2: return pure ? launch_fam_cls<0, 0, 0, 2, true>(warp, a, nsm, st)
                         : launch_fam_cls<0, 0, 0, 2, false>(warp, a, nsm, st);
     case 3: return launch_fam_cls<0, 0, 1, 1, false>(warp, a, nsm, st);
+    case 4: return pure ? launch_fam_cls<0, 0, 1, 2, true>(warp, a, nsm, st)
+                        : launch_fam_cls<0, 0, 1, 2, false>(warp, a, nsm, st);
     case 6: return launch_fam_cls<0, 1, 0, 1, false>(warp, a, nsm, st);
+    case 7: return pure ? launch_fam_cls<0, 1, 0, 2, true>(warp, a, nsm, st)
+                        : launch_fam_cls<0, 1, 0, 2, false>(warp, a, nsm, st);
+    case 8: return launch_fam_cls<0, 1, 1, 1, false>(warp, a, nsm, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -510,6 +541,18 @@ int family_tables(oqpg_ctx* c, double cutoff) {
                      [&](int x, int y) { return fq[x] > fq[y]; });
   std::vector<double> sq(order.size());
   for (size_t p = 0; p < order.size(); ++p) sq[p] = fq[order[p]];
+  // the same order restricted to the family pairs with several members
+  std::vector<int> morder, fmmol0(c->nmol), fmmoln(c->nmol);
+  std::vector<double> msq;
+  for (int mi = 0; mi < c->nmol; ++mi) {
+    fmmol0[mi] = (int)morder.size();
+    for (int k = fmol0[mi]; k < fmol0[mi] + fmoln[mi]; ++k)
+      if (fmem[order[k]].n > 1) {
+        morder.push_back(order[k]);
+        msq.push_back(fq[order[k]]);
+      }
+    fmmoln[mi] = (int)morder.size() - fmmol0[mi];
+  }
   cudaStream_t st = c->stream;
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = upload_vec(c->d_fpairs, fpairs, st);
@@ -524,6 +567,10 @@ int family_tables(oqpg_ctx* c, double cutoff) {
   if (e == cudaSuccess) e = upload_vec(c->d_fmol0, fmol0, st);
   if (e == cudaSuccess) e = upload_vec(c->d_fmoln, fmoln, st);
   if (e == cudaSuccess) e = upload_vec(c->d_pair_fam_multi, multi, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fmsorted_idx, morder, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fmsorted_q, msq, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fmmol0, fmmol0, st);
+  if (e == cudaSuccess) e = upload_vec(c->d_fmmoln, fmmoln, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? NO_MEM : DEV_ERR;
   c->nfpair = (int)fpairs.size();

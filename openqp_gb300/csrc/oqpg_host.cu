@@ -860,7 +860,7 @@ void ctx_free(oqpg_ctx* c) {
                     &c->d_gcnt, &c->d_q_att, &c->d_qf_att, &c->d_sorted_idx_att, &c->d_sorted_q_att,
                     &c->d_fpairs, &c->d_fmem, &c->d_fprims, &c->d_fcoef, &c->d_fpair_mol, &c->d_fpair_type,
                     &c->d_fq, &c->d_fsorted_idx, &c->d_fsorted_q, &c->d_fmol0, &c->d_fmoln,
-                    &c->d_pair_fam_multi};
+                    &c->d_pair_fam_multi, &c->d_fmsorted_idx, &c->d_fmsorted_q, &c->d_fmmol0, &c->d_fmmoln};
   for (DevBuf* b : bufs) b->release();
   c->hb.release();
   c->gb.release();
@@ -961,6 +961,10 @@ ListArgs list_args(const oqpg_ctx* c, BuildBufs& B, const Job& job) {
     la.fsorted_q = c->d_fsorted_q.as<double>();
     la.fmol0 = c->d_fmol0.as<int>();
     la.fmoln = c->d_fmoln.as<int>();
+    la.fmsorted_idx = c->d_fmsorted_idx.as<int>();
+    la.fmsorted_q = c->d_fmsorted_q.as<double>();
+    la.fmmol0 = c->d_fmmol0.as<int>();
+    la.fmmoln = c->d_fmmoln.as<int>();
     la.fam_members = B.counts.as<unsigned long long>() + NLIST;
   }
   if (petite_on(c, job)) {

@@ -80,6 +80,10 @@ struct ListArgs {
   const double* fsorted_q;
   const int* fmol0;                      // first family pair of each molecule
   const int* fmoln;                      // and their number
+  const int* fmsorted_idx;               // per molecule: the family pairs with more than one member,
+  const double* fmsorted_q;              // by descending bound (segment at fmmol0, fmmoln entries)
+  const int* fmmol0;
+  const int* fmmoln;
   unsigned long long* fam_members;       // per class: member quartets listed (statistics)
 };
 
@@ -330,7 +334,7 @@ struct oqpg_ctx {
   bool fam_enabled = true;
   int nfpair = 0, nfam_multi = 0;   // family pairs; those with more than one member
   oqpg::DevBuf d_fpairs, d_fmem, d_fprims, d_fcoef, d_fpair_mol, d_fpair_type, d_fq, d_fsorted_idx, d_fsorted_q,
-      d_fmol0, d_fmoln, d_pair_fam_multi;
+      d_fmol0, d_fmoln, d_pair_fam_multi, d_fmsorted_idx, d_fmsorted_q, d_fmmol0, d_fmmoln;
   // precision split: 0 = every quartet in FP64, 1 = bound < tau_f32 in FP32
   int precision_mode = 0;
   double tau_f32 = 0.0;

@@ -1,8 +1,9 @@
 """Shell families on the GPU: the generally contracted s shells of cc-pVXZ
 sets (OpenQP stores them as separate segmented shells and int2.F90 evaluates
 every shell quartet on its own) share their primitive integrals in the
-(ss|ss), (ss|sp), (ss|sd), (ss|pp), (sp|sp) classes.  The result must be the
-shell-by-shell sum: against the oracle at the plain-FP64 gate (1e-10), and
+(ss|ss), (ss|sp), (ss|sd), (ss|pp), (ss|pd), (sp|sp), (sp|sd), (sp|pp)
+classes.  The result must be the shell-by-shell sum: against the oracle at
+the plain-FP64 gate (1e-10), and
 against the same context with families off to 1e-12 (only the order of the
 additions differs); the number of shell quartets evaluated must not change.
 """
