@@ -321,9 +321,10 @@ int oqpg_get_tuning(const oqpg_ctx* ctx, int* split_log2, int* chunk, int* ctas_
 int oqpg_set_kernel_family(oqpg_ctx* ctx, const int* family);
 int oqpg_get_kernel_family(const oqpg_ctx* ctx, int* family, int* available);
 
-/* Shell families (on by default): s shells of one atom with the same
- * primitive exponents (the generally contracted shells of cc-pVXZ sets, which
- * OpenQP stores as separate segmented shells) share their primitive
+/* Shell families (on by default): two s shells of one atom whose primitive
+ * exponents are the same, or one's among the other's (the generally
+ * contracted shells of cc-pVXZ sets, which OpenQP stores as separate
+ * segmented shells) share their primitive
  * integrals in the (ss|ss), (ss|sp), (ss|sd), (ss|pp), (ss|pd), (sp|sp),
  * (sp|sd) and (sp|pp) classes of plain FP64 SCF builds: one primitive
  * integral per family quartet, added to every member shell quartet with its

@@ -6,8 +6,10 @@
 // exponents).  OpenQP stores them as separate shells (segmented form) and its
 // Fock build (int2.F90:755-805, the shell-quartet loop) evaluates every shell
 // quartet on its own, so a quartet of such shells repeats the same primitive
-// integrals with other contraction coefficients.  Here the s shells of one
-// atom with identical exponents form a family (two shells at most), the
+// integrals with other contraction coefficients.  Here two s shells of one
+// atom form a family when one's exponents are all among the other's (equal
+// lists, as oxygen's 1s and 2s; or a subset, as hydrogen's uncontracted 2s
+// within its 1s contraction in cc-pVDZ), the
 // family pairs (two families, or a family and another shell) carry the union
 // of their members' primitive pairs, and a family quartet evaluates each
 // union primitive quartet once, with unit pair factors, and adds it to every
@@ -392,6 +394,19 @@ bool fam_on(const oqpg_ctx* c, const Job& job) {
 
 namespace {
 
+// The primitive of shell s with exponent a (bitwise), or -1.
+int prim_index(const double* ex, const std::vector<int>& po, const std::vector<int>& nc, int s, double a) {
+  for (int i = 0; i < nc[s]; ++i)
+    if (std::memcmp(ex + po[s] + i, &a, sizeof(double)) == 0) return i;
+  return -1;
+}
+// Every exponent of shell s is one of shell r's.
+bool exps_within(const double* ex, const std::vector<int>& po, const std::vector<int>& nc, int s, int r) {
+  for (int i = 0; i < nc[s]; ++i)
+    if (prim_index(ex, po, nc, r, ex[po[s] + i]) < 0) return false;
+  return true;
+}
+
 template <typename T>
 cudaError_t upload_vec(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
   cudaError_t e = b.ensure(std::max<size_t>(sizeof(T) * v.size(), 16));
@@ -401,12 +416,15 @@ cudaError_t upload_vec(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
 
 }  // namespace
 
-// Families of each molecule (s shells on one atom with bitwise-equal exponent
-// lists, in shell order, two at most), and the family pairs of the family
+// Families of each molecule (two s shells on one atom, one's exponents all
+// among the other's, bitwise; the representative holds every exponent; in
+// shell order), and the family pairs of the family
 // classes' pair types, molecule by molecule (FA >= FB in family order; the
 // representative shells in kernel orientation, the side-A family holding the
 // first shell).  Member (x, y), x of side A, y of side B, is the canonical
-// shell pair of x and y; its factor on union primitive pair (i, j) is
+// shell pair of x and y; its factor on union primitive pair (i, j) (the
+// representatives' exponents a_i, a_j; x's and y's primitives with those
+// exponents, or factor 0) is
 // K/p = sqrt(2) pi^(5/4) c_x,i c_y,j exp(-a_i a_j |AB|^2 / p) / p with the
 // reference's pair screens (int2_pairs.F90:179-266 and the rotated-axis
 // pre-screen |K|, |K/p| >= 1e-4 tau), evaluated with build_pairs's operation
@@ -436,9 +454,10 @@ int family_tables(oqpg_ctx* c, double cutoff) {
       if (am[s] == 0)
         for (auto& f : fam) {
           const int r = f[0];
-          if (f.size() < 2 && am[r] == 0 && c->shell_atom[r] == c->shell_atom[s] && nc[r] == nc[s] &&
-              std::memcmp(ex + po[r], ex + po[s], sizeof(double) * nc[s]) == 0) {
+          if (f.size() < 2 && am[r] == 0 && c->shell_atom[r] == c->shell_atom[s] &&
+              (exps_within(ex, po, nc, s, r) || exps_within(ex, po, nc, r, s))) {
             f.push_back(s);
+            if (nc[s] > nc[r]) std::swap(f[0], f[1]);   // the representative holds every exponent
             placed = true;
             break;
           }
@@ -492,7 +511,9 @@ int family_tables(oqpg_ctx* c, double cutoff) {
             FamCoef fc{};
             double mx = 0.0;
             for (size_t k = 0; k < ms.size(); ++k) {
-              const double k1 = cc[po[ms[k].first] + i] * cc[po[ms[k].second] + j] * eab;
+              const int ix = prim_index(ex, po, nc, ms[k].first, a1), iy = prim_index(ex, po, nc, ms[k].second, a2);
+              if (ix < 0 || iy < 0) continue;   // the member has no such primitive pair
+              const double k1 = cc[po[ms[k].first] + ix] * cc[po[ms[k].second] + iy] * eab;
               if (std::fabs(k1) < qcut) continue;
               const double sp = sqrtpito52 * k1 * gi;
               if (std::fabs(sp) < qcut) continue;

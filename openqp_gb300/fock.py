@@ -304,8 +304,9 @@ class FockBuilder:
         return f.tolist(), av.tolist()
 
     def set_shell_families(self, on):
-        """Share the primitive integrals of s shells with equal exponents on
-        one atom (cc-pVXZ's generally contracted shells) in the s-rich classes
+        """Share the primitive integrals of two s shells on one atom whose
+        exponents are equal or nested (cc-pVXZ's generally contracted shells)
+        in the s-rich classes
         ((ss|ss) .. (ss|pd), (sp|sp), (sp|sd), (sp|pp)) of plain FP64 SCF builds
         (default on); off: every shell quartet on its own."""
         rc = lib().oqpg_set_shell_families(self.h, 1 if on else 0)
