@@ -79,6 +79,10 @@ constexpr bool fam_class_table_ok() {   // the list above is fam_class_l over th
   return true;
 }
 static_assert(fam_class_table_ok(), "family classes: 0-4 (ss|ss..pd), 6-8 (sp|sp), (sp|sd), (sp|pp)");
+// The family classes in order (list slots of their family-quartet lists).
+constexpr int NFAMCLS = 8;
+__host__ __device__ inline int fam_slot(int c) { return c <= 4 ? c : c - 1; }
+__host__ __device__ inline int fam_slot_class(int j) { return j <= 4 ? j : j + 1; }
 // Family-pair types: the pair types of the family classes (ss, sp, sd, pp, pd).
 __host__ __device__ inline bool fam_pair_type(int t) { return t <= 4; }
 cudaError_t launch_family(int c, bool pure, bool warp, const BuildArgs& a, int nsm, cudaStream_t st);

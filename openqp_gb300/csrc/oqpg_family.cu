@@ -23,7 +23,8 @@
 // the member's shells).  Only the classes whose members x elements block fits
 // in registers are built this way ((ss|ss), (ss|sp), (ss|sd), (ss|pp),
 // (ss|pd), (sp|sp), (sp|sd), (sp|pp): fam_class); the other quartets of
-// family shells stay shell quartets.  Plain FP64 SCF builds only (fam_on).
+// family shells stay shell quartets.  SCF builds in the FP64 and FP32-split
+// modes (fam_on); the family quartets are evaluated in FP64 in both.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -136,13 +137,15 @@ __global__ void __launch_bounds__(256) k_lists_fam(const ListArgs a) {
     }
     __syncthreads();
     if (threadIdx.x < NCLASS_SD && cnt[threadIdx.x]) {
-      base[threadIdx.x] = atomicAdd(&a.counts[NCLASS + threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
+      base[threadIdx.x] =
+          atomicAdd(&a.counts[fam_list_index(threadIdx.x)], (unsigned long long)cnt[threadIdx.x]);
       atomicAdd(&a.fam_members[threadIdx.x], (unsigned long long)mcnt[threadIdx.x]);
     }
     __syncthreads();
     if (cl >= 0 && a.write) {
       const unsigned long long pos = base[cl] + slot;
-      if (pos < a.caps[NCLASS + cl]) a.lists[NCLASS + cl][pos] = ent;
+      const int li = fam_list_index(cl);
+      if (pos < a.caps[li]) a.lists[li][pos] = ent;
     }
     __syncthreads();
   }
@@ -387,9 +390,12 @@ cudaError_t launch_family(int c, bool pure, bool warp, const BuildArgs& a, int n
 // ---------------------------------------------------------------------------
 // Host: the family tables.
 
+// Not in the double-float modes: there the shell quartets of the family
+// classes are cheaper in double-float than the family quartets in FP64
+// ((H2O)32 cc-pVDZ: df 7.38 builds/s with shell quartets, 5.86 with FP64
+// family quartets; mixed-df 9.58 and 6.26).
 bool fam_on(const oqpg_ctx* c, const Job& job) {
-  return c->fam_enabled && c->nfpair > 0 && !split_on(c) && !df_on(c) && !job.gen && job.inv_mu2 == 0.0 &&
-         !petite_on(c, job);
+  return c->fam_enabled && c->nfpair > 0 && !df_on(c) && !job.gen && job.inv_mu2 == 0.0 && !petite_on(c, job);
 }
 
 namespace {

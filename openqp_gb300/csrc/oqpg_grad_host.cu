@@ -35,15 +35,15 @@ struct GListArgs {
   const int* atom;
   double cj, ck, cutoff, cutoff2;
   double tau32;                 // bound below tau32: FP32 list (0: none)
-  unsigned long long* counts;   // NLIST: FP64 lists, then FP32 lists
-  uint2* lists[NLIST];
-  unsigned long long caps[NLIST];
+  unsigned long long* counts;   // NLIST_SHELL: FP64 lists, then FP32 lists
+  uint2* lists[NLIST_SHELL];
+  unsigned long long caps[NLIST_SHELL];
   int write;
 };
 
 __global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
-  __shared__ unsigned cnt[NLIST];
-  __shared__ unsigned long long base[NLIST];
+  __shared__ unsigned cnt[NLIST_SHELL];
+  __shared__ unsigned long long base[NLIST_SHELL];
   __shared__ int s_len;
   const int P = blockIdx.x;
   if (a.gpairs[P].pcnt == 0) return;
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
   const double* dj = a.dsh + (long long)ij.y * a.ns;
   const int ati = a.atom[ij.x], atj = a.atom[ij.y];
   for (int s0 = 0; s0 < len; s0 += blockDim.x) {
-    if (threadIdx.x < NLIST) cnt[threadIdx.x] = 0;
+    if (threadIdx.x < NLIST_SHELL) cnt[threadIdx.x] = 0;
     __syncthreads();
     const int s = s0 + threadIdx.x;
     const int Q = s < len ? a.sorted_idx[s] : 0x7fffffff;
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
       }
     }
     __syncthreads();
-    if (threadIdx.x < NLIST && cnt[threadIdx.x])
+    if (threadIdx.x < NLIST_SHELL && cnt[threadIdx.x])
       base[threadIdx.x] = atomicAdd(&a.counts[threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
     __syncthreads();
     if (c >= 0 && a.write) {
@@ -285,8 +285,8 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
     GK(cudaStreamSynchronize(st));  // matsf is freed at the end of this scope
   }
   if ((rc = gupload(c->d_dshg, dsh, st))) return rc;
-  GK(c->d_gcounts.ensure(sizeof(unsigned long long) * NLIST));
-  GK(c->d_gwork.ensure(sizeof(unsigned long long) * NLIST));
+  GK(c->d_gcounts.ensure(sizeof(unsigned long long) * NLIST_SHELL));
+  GK(c->d_gwork.ensure(sizeof(unsigned long long) * NLIST_SHELL));
   GK(c->d_gcnt.ensure(sizeof(unsigned long long) * 2));
   GK(c->d_de.ensure(sizeof(double) * 3 * c->natom));
   GListArgs la{};
@@ -306,17 +306,17 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
   la.cutoff2 = 0.5 * cutoff;
   la.tau32 = split ? c->tau_f32 : 0.0;
   la.counts = c->d_gcounts.as<unsigned long long>();
-  unsigned long long counts[NLIST];
+  unsigned long long counts[NLIST_SHELL];
   for (int pass = 0; pass < 3; ++pass) {
     la.write = 1;
-    for (int k = 0; k < NLIST; ++k) { la.lists[k] = c->d_glists[k].as<uint2>(); la.caps[k] = c->gcaps[k]; }
-    GK(cudaMemsetAsync(c->d_gcounts.p, 0, sizeof(unsigned long long) * NLIST, st));
+    for (int k = 0; k < NLIST_SHELL; ++k) { la.lists[k] = c->d_glists[k].as<uint2>(); la.caps[k] = c->gcaps[k]; }
+    GK(cudaMemsetAsync(c->d_gcounts.p, 0, sizeof(unsigned long long) * NLIST_SHELL, st));
     k_grad_lists<<<c->npair, 256, 0, st>>>(la);
     GK(cudaGetLastError());
     GK(cudaMemcpyAsync(counts, c->d_gcounts.p, sizeof(counts), cudaMemcpyDeviceToHost, st));
     GK(cudaStreamSynchronize(st));
     bool ok = true;
-    for (int k = 0; k < NLIST; ++k)
+    for (int k = 0; k < NLIST_SHELL; ++k)
       if (counts[k] > c->gcaps[k]) {
         ok = false;
         const unsigned long long cap = counts[k] + counts[k] / 8 + 1024;
@@ -327,7 +327,7 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
     if (pass == 2) return DEV_ERR;
   }
   GK(cudaMemsetAsync(c->d_de.p, 0, sizeof(double) * 3 * c->natom, st));
-  GK(cudaMemsetAsync(c->d_gwork.p, 0, sizeof(unsigned long long) * NLIST, st));
+  GK(cudaMemsetAsync(c->d_gwork.p, 0, sizeof(unsigned long long) * NLIST_SHELL, st));
   GK(cudaMemsetAsync(c->d_gcnt.p, 0, sizeof(unsigned long long) * 2, st));
   GradArgs g{};
   g.shells = c->d_shells.as<ShellDev>();
@@ -375,7 +375,7 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
   g.de = c->d_de.as<double>();
   g.counters = c->d_gcnt.as<unsigned long long>();
   double listed = 0, listed32 = 0;
-  for (int li = NLIST - 1; li >= 0; --li) {
+  for (int li = NLIST_SHELL - 1; li >= 0; --li) {
     if (!counts[li]) continue;
     const int cl = li % NCLASS;
     const bool f32 = li >= NCLASS;

@@ -1051,8 +1051,8 @@ int size_lists(oqpg_ctx* c, BuildBufs& B, const unsigned long long* counts, cuda
   CK(cudaMemcpyAsync(B.caps.p, B.cap, sizeof(B.cap), cudaMemcpyHostToDevice, st));
   int split[NLIST];
   for (int k = 0; k < NLIST; ++k) {
-    const int cl = k % NCLASS;
-    B.team[k] = list_team(c, cl, B.cap[k]) ? 1 : 0;
+    const int cl = list_class(k);
+    B.team[k] = k < NLIST_SHELL && list_team(c, cl, B.cap[k]) ? 1 : 0;
     split[k] = class_info(cl).prim ? head_bins(eff_split(c, cl, B.team[k] != 0)) : 0;
   }
   CK(cudaMemcpyAsync(B.split.p, split, sizeof(split), cudaMemcpyHostToDevice, st));
@@ -1109,8 +1109,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   CK(cudaMemsetAsync(B.hist.p, 0, sizeof(unsigned long long) * NLIST * NBIN, st));
   const float lo = (float)(1e-4 * c->tau * (1.0 - 1e-4));
   unsigned long long* counts = B.counts.as<unsigned long long>();
-  // the second list of a family class holds family quartets in family builds
-  auto fam_list = [&](int k) { return B.fam && k >= NCLASS && fam_class(k - NCLASS); };
+  auto fam_list = [&](int k) { return k >= NLIST_SHELL; };
   for (int k = 0; k < NLIST; ++k) {
     if (!B.cap[k]) continue;
     const long long cap = (long long)B.cap[k];
@@ -1187,12 +1186,26 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   unsigned long long* ranges = B.ranges.as<unsigned long long>();
   // heaviest classes first
   for (int cl = NCLASS - 1; cl >= 0; --cl) {
-    if (!B.cap[cl] && !B.cap[NCLASS + cl]) continue;
+    const int fli = fam_class(cl) ? fam_list_index(cl) : -1;
+    if (!B.cap[cl] && !B.cap[NCLASS + cl] && !(fli >= 0 && B.fam && B.cap[fli])) continue;
     if (timing) CK(cudaEventRecord(c->evc[cl][0], st));
     a.chunk = c->tune.chunk[cl];
     a.ctas_per_sm = c->tune.ctas_per_sm[cl];
     for (int prec = 0; prec < 2; ++prec) {
       const int li = cl + prec * NCLASS;
+      if (prec == 1 && fli >= 0 && B.fam && B.cap[fli]) {
+        // family quartets (FP64): the heavy head warp per quartet, the rest thread per quartet
+        a.counters = B.primc.as<unsigned long long>() + fli;
+        a.quartets = B.slists[fli].as<uint2>();
+        a.nquartets = (long long)B.cap[fli];
+        a.range = ranges + 4 * fli;
+        a.work = B.work.as<unsigned long long>() + NLIST + fli;
+        CK(launch_family(cl, c->pure, true, a, c->nsm, st));
+        a.range = ranges + 4 * fli + 2;
+        a.work = B.work.as<unsigned long long>() + fli;
+        CK(launch_family(cl, c->pure, false, a, c->nsm, st));
+        nlaunch += 2;
+      }
       if (timing && prec == 1) CK(cudaEventRecord(c->evc[cl][2], st));   // FP64 launches done
       if (!B.cap[li]) continue;
       const int fl = prec ? MODE_F32 : (df_on(c) ? MODE_DF : 0);
@@ -1200,17 +1213,6 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
       a.quartets = B.slists[li].as<uint2>();
       a.nquartets = (long long)B.cap[li];
       a.team = B.team[li];
-      if (prec == 1 && B.fam && fam_class(cl)) {
-        // family quartets: the heavy head warp per quartet, the rest thread per quartet
-        a.range = ranges + 4 * li;
-        a.work = B.work.as<unsigned long long>() + NLIST + li;
-        CK(launch_family(cl, c->pure, true, a, c->nsm, st));
-        a.range = ranges + 4 * li + 2;
-        a.work = B.work.as<unsigned long long>() + li;
-        CK(launch_family(cl, c->pure, false, a, c->nsm, st));
-        nlaunch += 2;
-        continue;
-      }
       if (class_info(cl).prim && eff_split(c, cl, B.team[li] != 0) < 64) {
         // quartets with >= 2^split primitive quartets (a prefix of the sorted
         // list) go to the warp-per-quartet primitive-parallel kernel
@@ -1267,17 +1269,16 @@ void record_stats(oqpg_ctx* c, const BuildBufs& B, int nlaunch, bool timing) {
   const unsigned long long* fmq = B.h_rb + 1 + 2 * NLIST;   // member quartets of the family lists
   for (int k = 0; k < NCLASS; ++k) {
     // quartets: the shell quartets evaluated (a family quartet counts its members)
-    const bool fl = B.fam && fam_class(k);
-    const unsigned long long q = cnt[k] + (fl ? fmq[k] : cnt[NCLASS + k]);
+    const int fli = fam_class(k) ? fam_list_index(k) : -1;
+    const bool fl = fli >= 0 && B.fam;
+    const unsigned long long q = cnt[k] + cnt[NCLASS + k] + (fl ? fmq[k] : 0ull);
     nq += (double)q;
     S[7 + k] = (double)q;
-    S[7 + NCLASS + k] = (double)nprim[k] + (double)nprim[NCLASS + k];
-    if (!fl) {
-      q32 += (double)cnt[NCLASS + k];
-      p32 += (double)nprim[NCLASS + k];
-    }
+    S[7 + NCLASS + k] = (double)nprim[k] + (double)nprim[NCLASS + k] + (fl ? (double)nprim[fli] : 0.0);
+    q32 += (double)cnt[NCLASS + k];
+    p32 += (double)nprim[NCLASS + k];
     float tk = 0, t32 = 0;
-    if (timing && (B.cap[k] || B.cap[NCLASS + k])) {
+    if (timing && (B.cap[k] || B.cap[NCLASS + k] || (fl && B.cap[fli]))) {
       cudaEventElapsedTime(&tk, c->evc[k][0], c->evc[k][1]);
       cudaEventElapsedTime(&t32, c->evc[k][2], c->evc[k][1]);
     }

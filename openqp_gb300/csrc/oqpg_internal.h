@@ -39,6 +39,15 @@ struct MolDev {
   long long dsh0;  // first element of its ns x ns shell-density block
 };
 
+// Quartet lists of a build: the FP64 shell-quartet list of every class, the
+// FP32 lists of the precision split, then the family-quartet lists of the
+// shell-family classes (FP64).
+constexpr int NLIST_SHELL = 2 * NCLASS;
+constexpr int NLIST = NLIST_SHELL + NFAMCLS;
+__host__ __device__ inline int fam_list_index(int c) { return NLIST_SHELL + fam_slot(c); }
+// the class of list k
+__host__ __device__ inline int list_class(int k) { return k < NLIST_SHELL ? k % NCLASS : fam_slot_class(k - NLIST_SHELL); }
+
 struct ListArgs {
   int npair;                // pairs of the whole batch (one CTA each)
   const MolDev* mols;
@@ -54,9 +63,9 @@ struct ListArgs {
   const unsigned long long* dmax_bits;  // per molecule
   double tau;
   double tau_f32;               // quartets with bound < tau_f32 go to the FP32 lists (0: none)
-  unsigned long long* counts;   // 2 NCLASS: FP64 lists, then FP32 lists
-  uint2* lists[2 * NCLASS];
-  unsigned long long caps[2 * NCLASS];
+  unsigned long long* counts;   // NLIST: FP64 lists, FP32 lists, family lists
+  uint2* lists[NLIST];
+  unsigned long long caps[NLIST];
   int write;
   // petite list (one molecule): shell images of the symmetry operations,
   // map[op ns + s]; sym_bits = (density asymmetry, density scale) as FP64 bits,
@@ -67,7 +76,7 @@ struct ListArgs {
   const unsigned long long* sym_bits;
   // shell families: k_lists leaves the quartets of the family classes with a
   // member-sharing side (pair_fam_multi) to k_lists_fam, which lists family
-  // quartets into the second list of those classes
+  // quartets into the family lists
   int fam;
   const unsigned char* pair_fam_multi;   // per pair: its family pair has more than one member
   int nfpair;
@@ -267,7 +276,6 @@ cudaError_t launch_grad_a(int c, const GradArgs& g, bool f32, int nsm, cudaStrea
 cudaError_t launch_grad_b(int c, const GradArgs& g, bool f32, int nsm, cudaStream_t st);
 cudaError_t launch_grad_f(int c, const GradArgs& g, int nsm, cudaStream_t st);  // classes with f, FP64
 
-constexpr int NLIST = 2 * NCLASS;  // FP64 lists, then the FP32 lists of the precision split
 
 // Per-build device buffers of one build pipeline (a context has one for its
 // direct builds and one owned by its captured graph).
@@ -367,8 +375,8 @@ struct oqpg_ctx {
   std::vector<int> coff;
   oqpg::DevBuf d_gpairs, d_gprims, d_galpha, d_gprimsf, d_galphaf, d_coff, d_atom, d_gmat, d_gmatf, d_dshg,
       d_gcounts, d_gwork, d_de, d_gcnt;
-  oqpg::DevBuf d_glists[oqpg::NLIST];   // FP64 lists, then the FP32 lists of the precision split
-  unsigned long long gcaps[oqpg::NLIST] = {0};
+  oqpg::DevBuf d_glists[oqpg::NLIST_SHELL];   // FP64 lists, then the FP32 lists of the precision split
+  unsigned long long gcaps[oqpg::NLIST_SHELL] = {0};
   double grad_stats[5] = {0, 0, 0, 0, 0};  // quartets listed, evaluated, primitive quartets, ms, FP32 listed
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t evc[oqpg::NCLASS][3] = {};   // class start, after its FP64 launches, end

@@ -97,3 +97,28 @@ def test_families_in_a_batch(gpu, oracle_lib):
     fs = bb.fock_jk(dens)
     for bas, d, f in zip(bases, dens, fs):
         assert np.abs(f - oracle_lib.Oracle(bas).fock_jk(d[0])).max() < TOL
+
+
+@pytest.mark.parametrize("mode", ["mixed", "mixed-fast", "df", "mixed-df"])
+def test_families_in_precision_modes(gpu, oracle_lib, mode):
+    """In the FP32-split modes the family quartets stay FP64 and the other
+    shell quartets follow the split; the double-float modes list shell
+    quartets only.  The mode's own bounds hold with families on and off (max
+    |dF| 1e-6 for the FP32 split, 1e-10 for double-float), and the same shell
+    quartets are evaluated."""
+    from openqp_gb300 import workloads
+    bas = workloads.water_cluster_basis(4, workloads.cube_edge_like_c1(4), 6, "cc-pvdz", spherical=True)
+    d = workloads.density(bas, 20, 3)
+    ref = oracle_lib.Oracle(bas).fock_jk(d)
+    fb = gpu.FockBuilder(bas)
+    fb.set_precision(mode, 1e-6)
+    f_on, f_off, st_on, st_off = _on_off(fb, d)
+    tol = 1e-10 if mode == "df" else 1e-6
+    assert np.abs(f_on - ref).max() < tol
+    assert np.abs(f_off - ref).max() < tol
+    assert st_on["quartets"] == st_off["quartets"]
+    if mode in ("mixed", "mixed-fast"):
+        assert 0 < st_on["f32_quartets"] < st_off["f32_quartets"]
+    else:
+        assert st_on["f32_quartets"] == st_off["f32_quartets"]
+        assert st_on["prim_quartets"] == st_off["prim_quartets"]
