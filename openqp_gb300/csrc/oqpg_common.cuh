@@ -53,9 +53,9 @@ constexpr unsigned PAIR_MASK = 0x3fffffffu;
 __host__ __device__ inline unsigned entry_pair(unsigned x) { return x & PAIR_MASK; }
 __host__ __device__ inline int entry_wlog2(unsigned x) { return (int)(x >> 30); }
 
-// Shell families: s shells on one atom whose primitives have the same
-// exponents (the generally contracted shells of correlation-consistent sets,
-// e.g. the 1s and 2s of O in cc-pVDZ), at most two per family.  A family pair
+// Shell families: two s shells on one atom whose primitive exponents are the
+// same, or one's among the other's (the generally contracted shells of
+// correlation-consistent sets, e.g. the 1s and 2s of O in cc-pVDZ).  A family pair
 // (two families, or a family and another shell) has up to FAM_MAX member
 // shell pairs that share every primitive pair's geometry and differ only in
 // the contraction coefficients, so one primitive integral serves them all.
@@ -122,6 +122,7 @@ struct BuildArgs {
   const PairDev* fpairs;         // family pairs: representative shells, union primitive range
   const FamMem* fmem;
   const PrimPair* fprims;        // union primitive pairs
+  const PrimPairF* fprimsf;      // FP32 copy (the FP32 family quartets of the precision split)
   const FamCoef* fcoef;          // per union primitive pair: the members' K/p
 };
 

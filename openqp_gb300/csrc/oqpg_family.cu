@@ -24,7 +24,8 @@
 // in registers are built this way ((ss|ss), (ss|sp), (ss|sd), (ss|pp),
 // (ss|pd), (sp|sp), (sp|sd), (sp|pp): fam_class); the other quartets of
 // family shells stay shell quartets.  SCF builds in the FP64 and FP32-split
-// modes (fam_on); the family quartets are evaluated in FP64 in both.
+// modes (fam_on); in the split, a family quartet runs in FP32 when every
+// member combination it lists would (their bounds below the threshold).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -57,8 +58,9 @@ __device__ __forceinline__ unsigned fam_mask_transpose(unsigned m) {
 }
 
 __global__ void __launch_bounds__(256) k_lists_fam(const ListArgs a) {
-  __shared__ unsigned cnt[NCLASS_SD], mcnt[NCLASS_SD];
-  __shared__ unsigned long long base[NCLASS_SD];
+  // per (precision, class): FP64 family lists, then FP32
+  __shared__ unsigned cnt[2 * NCLASS_SD], mcnt[2 * NCLASS_SD];
+  __shared__ unsigned long long base[2 * NCLASS_SD];
   __shared__ int s_len;
   const int FP = blockIdx.x;
   const int mi = a.fpair_mol[FP];
@@ -88,12 +90,13 @@ __global__ void __launch_bounds__(256) k_lists_fam(const ListArgs a) {
   const double* dshd = a.dsh + M.dsh0;
   const int tFP = a.fpair_type[FP];
   const float tlo = (float)(a.tau * (1.0 - 1e-5)), thi = (float)(a.tau * (1.0 + 1e-5));
+  const float mlo = (float)(a.tau_f32 * (1.0 - 1e-5)), mhi = (float)(a.tau_f32 * (1.0 + 1e-5));
   for (int s0 = 0; s0 < len; s0 += blockDim.x) {
-    if (threadIdx.x < NCLASS_SD) cnt[threadIdx.x] = mcnt[threadIdx.x] = 0;
+    if (threadIdx.x < 2 * NCLASS_SD) cnt[threadIdx.x] = mcnt[threadIdx.x] = 0;
     __syncthreads();
     const int s = s0 + threadIdx.x;
     const int FQ = s < len ? sorted_idx[f0 + s] : 0x7fffffff;
-    int cl = -1;
+    int cl = -1, li = 0;
     unsigned slot = 0;
     uint2 ent = make_uint2(0u, 0u);
     if (FQ <= FP) {
@@ -102,6 +105,7 @@ __global__ void __launch_bounds__(256) k_lists_fam(const ListArgs a) {
       const int c = tFP <= tFQ ? class_index(tFP, tFQ) : class_index(tFQ, tFP);
       if ((mp.n > 1 || mq.n > 1) && fam_class(c)) {
         unsigned mask = 0;
+        bool f32 = a.tau_f32 > 0.0;   // every passing combination below the split threshold
 #pragma unroll
         for (int m = 0; m < FAM_MAX; ++m) {
           if (m >= mp.n) break;
@@ -120,32 +124,47 @@ __global__ void __launch_bounds__(256) k_lists_fam(const ListArgs a) {
             if (a.q[P > Q ? P : Q] * dmax < a.tau) continue;   // pair screen of the larger pair index
             const int2 kl = a.pair_ij[Q];
             const float tf = quartet_value_f32(a, ns, dshf, di, dj, dij4, qPf, Q, kl);
+            double t = -1.0;  // exact test value, computed only near a threshold
             bool pass;
             if (tf < tlo) pass = false;
             else if (tf > thi) pass = true;
-            else pass = !(quartet_value(a, ns, dshd, ij, qP, Q, kl) < a.tau);
-            if (pass) mask |= 1u << (4 * m + n);
+            else {
+              t = quartet_value(a, ns, dshd, ij, qP, Q, kl);
+              pass = !(t < a.tau);
+            }
+            if (pass) {
+              mask |= 1u << (4 * m + n);
+              // the shell-quartet path's split decision for this combination
+              if (f32 && !(tf < mlo)) {
+                if (tf > mhi) f32 = false;
+                else {
+                  if (t < 0.0) t = quartet_value(a, ns, dshd, ij, qP, Q, kl);
+                  f32 = t < a.tau_f32;
+                }
+              }
+            }
           }
         }
         if (mask) {
           cl = c;
+          li = f32 ? 1 : 0;
           ent = tFP <= tFQ ? fam_entry(FP, FQ, mask) : fam_entry(FQ, FP, fam_mask_transpose(mask));
-          slot = atomicAdd(&cnt[c], 1u);
-          atomicAdd(&mcnt[c], (unsigned)__popc(mask));
+          slot = atomicAdd(&cnt[li * NCLASS_SD + c], 1u);
+          atomicAdd(&mcnt[li * NCLASS_SD + c], (unsigned)__popc(mask));
         }
       }
     }
     __syncthreads();
-    if (threadIdx.x < NCLASS_SD && cnt[threadIdx.x]) {
-      base[threadIdx.x] =
-          atomicAdd(&a.counts[fam_list_index(threadIdx.x)], (unsigned long long)cnt[threadIdx.x]);
-      atomicAdd(&a.fam_members[threadIdx.x], (unsigned long long)mcnt[threadIdx.x]);
+    if (threadIdx.x < 2 * NCLASS_SD && cnt[threadIdx.x]) {
+      const int p = threadIdx.x / NCLASS_SD, c = threadIdx.x % NCLASS_SD;
+      base[threadIdx.x] = atomicAdd(&a.counts[fam_list_index(c, p)], (unsigned long long)cnt[threadIdx.x]);
+      atomicAdd(&a.fam_members[p * NCLASS + c], (unsigned long long)mcnt[threadIdx.x]);
     }
     __syncthreads();
     if (cl >= 0 && a.write) {
-      const unsigned long long pos = base[cl] + slot;
-      const int li = fam_list_index(cl);
-      if (pos < a.caps[li]) a.lists[li][pos] = ent;
+      const unsigned long long pos = base[li * NCLASS_SD + cl] + slot;
+      const int k = fam_list_index(cl, li);
+      if (pos < a.caps[k]) a.lists[k][pos] = ent;
     }
     __syncthreads();
   }
@@ -162,32 +181,48 @@ struct FamCls {
 
 // The primitive-quartet screen of member combination (m, n):
 // (K_m/p K_n/q)^2 < prim_cut2 (p + q) drops it (int_rotaxis.F90:629), in FP32
-// outside the narrow band around the cutoff, else in FP64.
-__device__ __forceinline__ bool fam_keep(const BuildArgs& a, float r, double spm, double sqn, const PrimPair* bp,
+// outside the narrow band around the cutoff, else in FP64; the FP32 family
+// quartets decide in FP32 at the middle of the band, as the FP32 shell
+// quartets do.
+template <typename T>
+__device__ __forceinline__ bool fam_keep(const BuildArgs& a, float r, T spm, T sqn, const PrimPair* bp,
                                          const PrimPair* kp) {
   if (r < a.prim_cut_lo) return false;
   if (r > a.prim_cut_hi) return true;
-  const double f = spm * sqn;
+  const double f = (double)spm * (double)sqn;
   return !(f * f < a.prim_cut2 * (__ldg(&bp->p) + __ldg(&kp->p)));
 }
+template <>
+__device__ __forceinline__ bool fam_keep<float>(const BuildArgs& a, float r, float, float, const PrimPair*,
+                                                const PrimPair*) {
+  return !(r < 0.5f * (a.prim_cut_lo + a.prim_cut_hi));
+}
+
+// union primitive pairs and member factors in the kernel's arithmetic type
+template <typename T> __device__ __forceinline__ const typename PrimT<T>::type* fprims_of(const BuildArgs& a);
+template <> __device__ __forceinline__ const PrimPair* fprims_of<double>(const BuildArgs& a) { return a.fprims; }
+template <> __device__ __forceinline__ const PrimPairF* fprims_of<float>(const BuildArgs& a) { return a.fprimsf; }
+template <typename T> __device__ __forceinline__ T fam_coef(const FamCoef& c, int m);
+template <> __device__ __forceinline__ double fam_coef<double>(const FamCoef& c, int m) { return __ldg(&c.sp[m]); }
+template <> __device__ __forceinline__ float fam_coef<float>(const FamCoef& c, int m) { return __ldg(&c.spf[m]); }
 
 // Accumulators of one family quartet in one lane, with the ket factors of
 // the current ket primitive (the union primitive quartets arrive in
 // increasing c = kq nP + kb, so they are loaded once per ket primitive).
-template <int LA, int LB, int LC, int LD>
+template <int LA, int LB, int LC, int LD, typename T>
 struct FamAcc {
   using F = FamCls<LA, LB, LC, LD>;
-  double acc[F::NACC];
-  double sq[F::MK];
+  T acc[F::NACC];
+  T sq[F::MK];
   float sqf[F::MK];
   int kq = -1;
 };
 
-template <int LA, int LB, int LC, int LD>
-__device__ __forceinline__ void fam_acc_init(FamAcc<LA, LB, LC, LD>& s) {
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void fam_acc_init(FamAcc<LA, LB, LC, LD, T>& s) {
   using F = FamCls<LA, LB, LC, LD>;
 #pragma unroll
-  for (int i = 0; i < F::NACC; ++i) s.acc[i] = 0.0;
+  for (int i = 0; i < F::NACC; ++i) s.acc[i] = (T)0;
   s.kq = -1;
 }
 
@@ -197,44 +232,48 @@ __device__ __forceinline__ void fam_acc_init(FamAcc<LA, LB, LC, LD>& s) {
 // nb, nk: members of the two family pairs.  (Taking the ket factors out of
 // each ket-primitive row instead, NE x nb FMAs per quartet plus a flush per
 // row, measured slower: after screening the rows are short.)
-template <int LA, int LB, int LC, int LD>
-__device__ __forceinline__ void fam_body(const BuildArgs& a, const PrimPair* bpp, const PrimPair* kpp,
-                                         const FamCoef* bco, const FamCoef* kco, int cb, int cq, const double AB[3],
-                                         const double CD[3], int nb, int nk, FamAcc<LA, LB, LC, LD>& s) {
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void fam_body(const BuildArgs& a, const typename PrimT<T>::type* bpp,
+                                         const typename PrimT<T>::type* kpp, const FamCoef* bco,
+                                         const FamCoef* kco, int cb, int cq, const T AB[3], const T CD[3], int nb,
+                                         int nk, FamAcc<LA, LB, LC, LD, T>& s) {
   using F = FamCls<LA, LB, LC, LD>;
   constexpr int NE = F::NE, MB = F::MB, MK = F::MK;
   if (cq != s.kq) {
     s.kq = cq;
 #pragma unroll
     for (int n = 0; n < MK; ++n) {
-      s.sq[n] = __ldg(&kco[cq].sp[n]);
+      s.sq[n] = fam_coef<T>(kco[cq], n);
       s.sqf[n] = fabsf(__ldg(&kco[cq].spf[n]));
     }
   }
-  double v[NE];
+  T v[NE];
 #pragma unroll
-  for (int e = 0; e < NE; ++e) v[e] = 0.0;
-  prim_body<LA, LB, LC, LD, double, false, true>(a, bpp, kpp, cb, cq, AB, CD, v);
+  for (int e = 0; e < NE; ++e) v[e] = (T)0;
+  prim_body<LA, LB, LC, LD, T, false, true>(a, bpp, kpp, cb, cq, AB, CD, v);
   const float rs = rsqrtf(prim_screen(bpp + cb).y + prim_screen(kpp + cq).y);
+  // FP64 band decisions read the FP64 union pairs
+  const PrimPair* bp64 = a.fprims + (bpp - fprims_of<T>(a)) + cb;
+  const PrimPair* kp64 = a.fprims + (kpp - fprims_of<T>(a)) + cq;
 #pragma unroll
   for (int m = 0; m < MB; ++m) {
     if (m >= nb) break;
-    const double spm = __ldg(&bco[cb].sp[m]);
+    const T spm = fam_coef<T>(bco[cb], m);
     const float spmf = fabsf(__ldg(&bco[cb].spf[m]));
     if constexpr (NE == 1) {
-      const double t = spm * v[0];
+      const T t = spm * v[0];
 #pragma unroll
       for (int n = 0; n < MK; ++n) {
         if (n >= nk) break;
-        const bool keep = fam_keep(a, spmf * s.sqf[n] * rs, spm, s.sq[n], bpp + cb, kpp + cq);
-        s.acc[m * MK + n] = fma(keep ? s.sq[n] : 0.0, t, s.acc[m * MK + n]);
+        const bool keep = fam_keep<T>(a, spmf * s.sqf[n] * rs, spm, s.sq[n], bp64, kp64);
+        s.acc[m * MK + n] = fma(keep ? s.sq[n] : (T)0, t, s.acc[m * MK + n]);
       }
     } else {
 #pragma unroll
       for (int n = 0; n < MK; ++n) {
         if (n >= nk) break;
-        const bool keep = fam_keep(a, spmf * s.sqf[n] * rs, spm, s.sq[n], bpp + cb, kpp + cq);
-        const double f = keep ? spm * s.sq[n] : 0.0;
+        const bool keep = fam_keep<T>(a, spmf * s.sqf[n] * rs, spm, s.sq[n], bp64, kp64);
+        const T f = keep ? spm * s.sq[n] : (T)0;
 #pragma unroll
         for (int e = 0; e < NE; ++e) s.acc[(m * MK + n) * NE + e] = fma(f, v[e], s.acc[(m * MK + n) * NE + e]);
       }
@@ -243,25 +282,26 @@ __device__ __forceinline__ void fam_body(const BuildArgs& a, const PrimPair* bpp
 }
 
 // Family quartet geometry: representative shells of the two family pairs.
-__device__ __forceinline__ void fam_geometry(const BuildArgs& a, const PairDev& P, const PairDev& Q, double AB[3],
-                                             double CD[3]) {
+template <typename T>
+__device__ __forceinline__ void fam_geometry(const BuildArgs& a, const PairDev& P, const PairDev& Q, T AB[3],
+                                             T CD[3]) {
   const ShellDev SA = a.shells[P.sha], SB = a.shells[P.shb], SC = a.shells[Q.sha], SD = a.shells[Q.shb];
-  AB[0] = SA.x - SB.x; AB[1] = SA.y - SB.y; AB[2] = SA.z - SB.z;
-  CD[0] = SC.x - SD.x; CD[1] = SC.y - SD.y; CD[2] = SC.z - SD.z;
+  AB[0] = (T)(SA.x - SB.x); AB[1] = (T)(SA.y - SB.y); AB[2] = (T)(SA.z - SB.z);
+  CD[0] = (T)(SC.x - SD.x); CD[1] = (T)(SC.y - SD.y); CD[2] = (T)(SC.z - SD.z);
 }
 
 // Member combination k = m MK + n of a family quartet digested as the shell
 // quartet (member m of the bra family pair | member n of the ket's): its
 // block is copied out of acc by compile-time selects (one epilogue instance).
-template <int LA, int LB, int LC, int LD, bool PURE>
+template <int LA, int LB, int LC, int LD, bool PURE, typename T>
 __device__ __forceinline__ void fam_digest(const BuildArgs& a, const FamMem& mb, const FamMem& mk, int k,
-                                           const double* acc) {
+                                           const T* acc) {
   using F = FamCls<LA, LB, LC, LD>;
   constexpr int NE = F::NE, MB = F::MB, MK = F::MK;
-  double blk[NE];
+  T blk[NE];
   int P = 0, Q = 0;
 #pragma unroll
-  for (int e = 0; e < NE; ++e) blk[e] = 0.0;
+  for (int e = 0; e < NE; ++e) blk[e] = (T)0;
 #pragma unroll
   for (int kk = 0; kk < MB * MK; ++kk)
     if (kk == k) {
@@ -270,15 +310,16 @@ __device__ __forceinline__ void fam_digest(const BuildArgs& a, const FamMem& mb,
       P = mb.m[kk / MK];
       Q = mk.m[kk % MK];
     }
-  small_epilogue<LA, LB, LC, LD, PURE, false, double>(a, make_uint2((unsigned)P, (unsigned)Q), a.pairs[P], a.pairs[Q],
-                                                     blk);
+  small_epilogue<LA, LB, LC, LD, PURE, false, T>(a, make_uint2((unsigned)P, (unsigned)Q), a.pairs[P], a.pairs[Q],
+                                                blk);
 }
 
 // Thread per family quartet (the light ones): warps take chunks of the list
 // sorted by union primitive quartets, like k_small.
-template <int LA, int LB, int LC, int LD, bool PURE>
+template <int LA, int LB, int LC, int LD, bool PURE, typename T>
 __global__ void __launch_bounds__(128) k_fam_small(const BuildArgs a) {
   using F = FamCls<LA, LB, LC, LD>;
+  using PP = typename PrimT<T>::type;
   constexpr int MB = F::MB, MK = F::MK;
   const int lane = threadIdx.x & 31;
   const uint2* quartets;
@@ -295,20 +336,20 @@ __global__ void __launch_bounds__(128) k_fam_small(const BuildArgs a) {
       const unsigned mask = fam_mask(e);
       const PairDev P = a.fpairs[e.x & FAM_IDX_MASK], Q = a.fpairs[e.y & FAM_IDX_MASK];
       const FamMem mb = a.fmem[e.x & FAM_IDX_MASK], mk = a.fmem[e.y & FAM_IDX_MASK];
-      double AB[3], CD[3];
+      T AB[3], CD[3];
       fam_geometry(a, P, Q, AB, CD);
-      FamAcc<LA, LB, LC, LD> s;
+      FamAcc<LA, LB, LC, LD, T> s;
       fam_acc_init(s);
-      const PrimPair* bpp = a.fprims + P.poff;
-      const PrimPair* kpp = a.fprims + Q.poff;
+      const PP* bpp = fprims_of<T>(a) + P.poff;
+      const PP* kpp = fprims_of<T>(a) + Q.poff;
       const FamCoef* bco = a.fcoef + P.poff;
       const FamCoef* kco = a.fcoef + Q.poff;
       prim_loop_lane(a, bpp, kpp, P.pcnt, Q.pcnt, 0, 1, nprim, [&](int cb, int cq) {
-        fam_body<LA, LB, LC, LD>(a, bpp, kpp, bco, kco, cb, cq, AB, CD, mb.n, mk.n, s);
+        fam_body<LA, LB, LC, LD, T>(a, bpp, kpp, bco, kco, cb, cq, AB, CD, mb.n, mk.n, s);
       });
 #pragma unroll 1
       for (int k = 0; k < MB * MK; ++k)
-        if ((mask >> (4 * (k / MK) + k % MK)) & 1u) fam_digest<LA, LB, LC, LD, PURE>(a, mb, mk, k, s.acc);
+        if ((mask >> (4 * (k / MK) + k % MK)) & 1u) fam_digest<LA, LB, LC, LD, PURE, T>(a, mb, mk, k, s.acc);
     }
   }
   if (a.counters && nprim) atomicAdd(a.counters, nprim);
@@ -317,9 +358,10 @@ __global__ void __launch_bounds__(128) k_fam_small(const BuildArgs a) {
 // One warp per heavy family quartet: the lanes share its union primitive
 // quartets (dealt as in k_prim), the member blocks are summed over the warp,
 // and lane k digests member combination k.
-template <int LA, int LB, int LC, int LD, bool PURE>
+template <int LA, int LB, int LC, int LD, bool PURE, typename T>
 __global__ void __launch_bounds__(128) k_fam_warp(const BuildArgs a) {
   using F = FamCls<LA, LB, LC, LD>;
+  using PP = typename PrimT<T>::type;
   constexpr int NE = F::NE, MB = F::MB, MK = F::MK;
   const int lane = threadIdx.x & 31;
   const uint2* quartets;
@@ -333,25 +375,25 @@ __global__ void __launch_bounds__(128) k_fam_warp(const BuildArgs a) {
     const unsigned mask = fam_mask(e);
     const PairDev P = a.fpairs[e.x & FAM_IDX_MASK], Q = a.fpairs[e.y & FAM_IDX_MASK];
     const FamMem mb = a.fmem[e.x & FAM_IDX_MASK], mk = a.fmem[e.y & FAM_IDX_MASK];
-    double AB[3], CD[3];
+    T AB[3], CD[3];
     fam_geometry(a, P, Q, AB, CD);
-    FamAcc<LA, LB, LC, LD> s;
+    FamAcc<LA, LB, LC, LD, T> s;
     fam_acc_init(s);
-    const PrimPair* bpp = a.fprims + P.poff;
-    const PrimPair* kpp = a.fprims + Q.poff;
+    const PP* bpp = fprims_of<T>(a) + P.poff;
+    const PP* kpp = fprims_of<T>(a) + Q.poff;
     const FamCoef* bco = a.fcoef + P.poff;
     const FamCoef* kco = a.fcoef + Q.poff;
     prim_loop_warp(a, bpp, kpp, P.pcnt, Q.pcnt, lane, nprim, [&](int cb, int cq) {
-      fam_body<LA, LB, LC, LD>(a, bpp, kpp, bco, kco, cb, cq, AB, CD, mb.n, mk.n, s);
+      fam_body<LA, LB, LC, LD, T>(a, bpp, kpp, bco, kco, cb, cq, AB, CD, mb.n, mk.n, s);
     });
-    double* acc = s.acc;
+    T* acc = s.acc;
     // warp sums of the listed combinations (the mask is uniform over the warp)
 #pragma unroll
     for (int k = 0; k < MB * MK; ++k) {
       if (!((mask >> (4 * (k / MK) + k % MK)) & 1u)) continue;
 #pragma unroll
       for (int i = 0; i < NE; ++i) {
-        double v = acc[k * NE + i];
+        T v = acc[k * NE + i];
 #pragma unroll
         for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
         acc[k * NE + i] = v;
@@ -359,30 +401,34 @@ __global__ void __launch_bounds__(128) k_fam_warp(const BuildArgs a) {
     }
     static_assert(MB * MK <= 32, "one lane per member combination");
     if (lane < MB * MK && ((mask >> (4 * (lane / MK) + lane % MK)) & 1u))
-      fam_digest<LA, LB, LC, LD, PURE>(a, mb, mk, lane, acc);
+      fam_digest<LA, LB, LC, LD, PURE, T>(a, mb, mk, lane, acc);
   }
   if (a.counters && nprim) atomicAdd(a.counters, nprim);
 }
 
 template <int LA, int LB, int LC, int LD, bool PURE>
-cudaError_t launch_fam_cls(bool warp, const BuildArgs& a, int nsm, cudaStream_t st) {
-  if (warp) return launch_persistent(k_fam_warp<LA, LB, LC, LD, PURE>, 0, 4, a, nsm, st);
-  return launch_persistent(k_fam_small<LA, LB, LC, LD, PURE>, 0, 128, a, nsm, st);
+cudaError_t launch_fam_cls(bool warp, bool f32, const BuildArgs& a, int nsm, cudaStream_t st) {
+  if (f32) {
+    if (warp) return launch_persistent(k_fam_warp<LA, LB, LC, LD, PURE, float>, 0, 4, a, nsm, st);
+    return launch_persistent(k_fam_small<LA, LB, LC, LD, PURE, float>, 0, 128, a, nsm, st);
+  }
+  if (warp) return launch_persistent(k_fam_warp<LA, LB, LC, LD, PURE, double>, 0, 4, a, nsm, st);
+  return launch_persistent(k_fam_small<LA, LB, LC, LD, PURE, double>, 0, 128, a, nsm, st);
 }
 
-cudaError_t launch_family(int c, bool pure, bool warp, const BuildArgs& a, int nsm, cudaStream_t st) {
+cudaError_t launch_family(int c, bool pure, bool warp, bool f32, const BuildArgs& a, int nsm, cudaStream_t st) {
   switch (c) {
-    case 0: return launch_fam_cls<0, 0, 0, 0, false>(warp, a, nsm, st);
-    case 1: return launch_fam_cls<0, 0, 0, 1, false>(warp, a, nsm, st);
-    case 2: return pure ? launch_fam_cls<0, 0, 0, 2, true>(warp, a, nsm, st)
-                        : launch_fam_cls<0, 0, 0, 2, false>(warp, a, nsm, st);
-    case 3: return launch_fam_cls<0, 0, 1, 1, false>(warp, a, nsm, st);
-    case 4: return pure ? launch_fam_cls<0, 0, 1, 2, true>(warp, a, nsm, st)
-                        : launch_fam_cls<0, 0, 1, 2, false>(warp, a, nsm, st);
-    case 6: return launch_fam_cls<0, 1, 0, 1, false>(warp, a, nsm, st);
-    case 7: return pure ? launch_fam_cls<0, 1, 0, 2, true>(warp, a, nsm, st)
-                        : launch_fam_cls<0, 1, 0, 2, false>(warp, a, nsm, st);
-    case 8: return launch_fam_cls<0, 1, 1, 1, false>(warp, a, nsm, st);
+    case 0: return launch_fam_cls<0, 0, 0, 0, false>(warp, f32, a, nsm, st);
+    case 1: return launch_fam_cls<0, 0, 0, 1, false>(warp, f32, a, nsm, st);
+    case 2: return pure ? launch_fam_cls<0, 0, 0, 2, true>(warp, f32, a, nsm, st)
+                        : launch_fam_cls<0, 0, 0, 2, false>(warp, f32, a, nsm, st);
+    case 3: return launch_fam_cls<0, 0, 1, 1, false>(warp, f32, a, nsm, st);
+    case 4: return pure ? launch_fam_cls<0, 0, 1, 2, true>(warp, f32, a, nsm, st)
+                        : launch_fam_cls<0, 0, 1, 2, false>(warp, f32, a, nsm, st);
+    case 6: return launch_fam_cls<0, 1, 0, 1, false>(warp, f32, a, nsm, st);
+    case 7: return pure ? launch_fam_cls<0, 1, 0, 2, true>(warp, f32, a, nsm, st)
+                        : launch_fam_cls<0, 1, 0, 2, false>(warp, f32, a, nsm, st);
+    case 8: return launch_fam_cls<0, 1, 1, 1, false>(warp, f32, a, nsm, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -585,6 +631,13 @@ int family_tables(oqpg_ctx* c, double cutoff) {
   if (e == cudaSuccess) e = upload_vec(c->d_fpairs, fpairs, st);
   if (e == cudaSuccess) e = upload_vec(c->d_fmem, fmem, st);
   if (e == cudaSuccess) e = upload_vec(c->d_fprims, fprims, st);
+  std::vector<PrimPairF> fprimsf(fprims.size());   // FP32 copy for the FP32 family quartets
+  for (size_t i = 0; i < fprims.size(); ++i) {
+    const PrimPair& q = fprims[i];
+    fprimsf[i] = PrimPairF{(float)q.p, (float)q.hp, (float)q.px, (float)q.py, (float)q.pz,
+                           (float)q.ax, (float)q.ay, (float)q.az, (float)q.sp, 0.0f};
+  }
+  if (e == cudaSuccess) e = upload_vec(c->d_fprimsf, fprimsf, st);
   if (e == cudaSuccess) e = upload_vec(c->d_fcoef, fcoef, st);
   if (e == cudaSuccess) e = upload_vec(c->d_fpair_mol, fmol, st);
   if (e == cudaSuccess) e = upload_vec(c->d_fpair_type, ftype, st);

@@ -858,7 +858,7 @@ void ctx_free(oqpg_ctx* c) {
                     &c->d_gpairs, &c->d_gprims, &c->d_galpha, &c->d_gprimsf, &c->d_galphaf, &c->d_coff,
                     &c->d_atom, &c->d_gmat, &c->d_gmatf, &c->d_dshg, &c->d_gcounts, &c->d_gwork, &c->d_de,
                     &c->d_gcnt, &c->d_q_att, &c->d_qf_att, &c->d_sorted_idx_att, &c->d_sorted_q_att,
-                    &c->d_fpairs, &c->d_fmem, &c->d_fprims, &c->d_fcoef, &c->d_fpair_mol, &c->d_fpair_type,
+                    &c->d_fpairs, &c->d_fmem, &c->d_fprims, &c->d_fprimsf, &c->d_fcoef, &c->d_fpair_mol, &c->d_fpair_type,
                     &c->d_fq, &c->d_fsorted_idx, &c->d_fsorted_q, &c->d_fmol0, &c->d_fmoln,
                     &c->d_pair_fam_multi, &c->d_fmsorted_idx, &c->d_fmsorted_q, &c->d_fmmol0, &c->d_fmmoln};
   for (DevBuf* b : bufs) b->release();
@@ -913,7 +913,7 @@ int ensure_bufs(oqpg_ctx* c, BuildBufs& B, const Job& job) {
   CK(B.dsh.ensure(sizeof(double) * std::max<long long>(c->dsh_elems, 1)));
   CK(B.dshf.ensure(sizeof(float) * std::max<long long>(c->dsh_elems, 1)));
   CK(B.dmax.ensure(sizeof(unsigned long long) * c->nmol));
-  CK(B.counts.ensure(sizeof(unsigned long long) * (NLIST + NCLASS)));   // + family member quartets
+  CK(B.counts.ensure(sizeof(unsigned long long) * (NLIST + 2 * NCLASS)));   // + family member quartets
   CK(B.primc.ensure(sizeof(unsigned long long) * NLIST));
   CK(B.hist.ensure(sizeof(unsigned long long) * NLIST * NBIN));
   CK(B.cursor.ensure(sizeof(unsigned long long) * NLIST * NBIN));
@@ -926,7 +926,7 @@ int ensure_bufs(oqpg_ctx* c, BuildBufs& B, const Job& job) {
     CK(B.sym.ensure(sizeof(unsigned long long) * 2));
     CK(B.fsk.ensure(sizeof(double) * (size_t)c->ntri * std::max(job.nfocks, 1)));
   }
-  if (!B.h_rb) CK(cudaMallocHost(&B.h_rb, sizeof(unsigned long long) * (1 + 2 * NLIST + NCLASS)));
+  if (!B.h_rb) CK(cudaMallocHost(&B.h_rb, sizeof(unsigned long long) * (1 + 2 * NLIST + 2 * NCLASS)));
   return OK;
 }
 
@@ -1067,7 +1067,7 @@ int count_lists(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, unsi
   if ((rc = issue_densities(c, B, job, st))) return rc;
   ListArgs la = list_args(c, B, job);
   la.write = 0;
-  CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * (NLIST + NCLASS), st));
+  CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * (NLIST + 2 * NCLASS), st));
   k_lists<<<c->npair, 256, 0, st>>>(la);
   CK(cudaGetLastError());
   if (la.fam) {
@@ -1096,7 +1096,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   ListArgs la = list_args(c, B, job);
   la.write = 1;
   B.fam = la.fam != 0;
-  CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * (NLIST + NCLASS), st));
+  CK(cudaMemsetAsync(B.counts.p, 0, sizeof(unsigned long long) * (NLIST + 2 * NCLASS), st));
   k_lists<<<c->npair, 256, 0, st>>>(la);
   CK(cudaGetLastError());
   ++nlaunch;
@@ -1182,31 +1182,39 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   a.fpairs = c->d_fpairs.as<PairDev>();
   a.fmem = c->d_fmem.as<FamMem>();
   a.fprims = c->d_fprims.as<PrimPair>();
+  a.fprimsf = c->d_fprimsf.as<PrimPairF>();
   a.fcoef = c->d_fcoef.as<FamCoef>();
   unsigned long long* ranges = B.ranges.as<unsigned long long>();
   // heaviest classes first
+  // family quartets of class cl in precision f32: the heavy head warp per
+  // quartet, the rest thread per quartet
+  auto launch_fam_list = [&](int cl, int f32) -> int {
+    const int fli = fam_list_index(cl, f32);
+    if (!B.fam || !B.cap[fli]) return OK;
+    a.counters = B.primc.as<unsigned long long>() + fli;
+    a.quartets = B.slists[fli].as<uint2>();
+    a.nquartets = (long long)B.cap[fli];
+    a.range = ranges + 4 * fli;
+    a.work = B.work.as<unsigned long long>() + NLIST + fli;
+    CK(launch_family(cl, c->pure, true, f32 != 0, a, c->nsm, st));
+    a.range = ranges + 4 * fli + 2;
+    a.work = B.work.as<unsigned long long>() + fli;
+    CK(launch_family(cl, c->pure, false, f32 != 0, a, c->nsm, st));
+    nlaunch += 2;
+    return OK;
+  };
   for (int cl = NCLASS - 1; cl >= 0; --cl) {
-    const int fli = fam_class(cl) ? fam_list_index(cl) : -1;
-    if (!B.cap[cl] && !B.cap[NCLASS + cl] && !(fli >= 0 && B.fam && B.cap[fli])) continue;
+    const bool fc = B.fam && fam_class(cl);
+    if (!B.cap[cl] && !B.cap[NCLASS + cl] && !(fc && (B.cap[fam_list_index(cl, 0)] || B.cap[fam_list_index(cl, 1)])))
+      continue;
     if (timing) CK(cudaEventRecord(c->evc[cl][0], st));
     a.chunk = c->tune.chunk[cl];
     a.ctas_per_sm = c->tune.ctas_per_sm[cl];
     for (int prec = 0; prec < 2; ++prec) {
       const int li = cl + prec * NCLASS;
-      if (prec == 1 && fli >= 0 && B.fam && B.cap[fli]) {
-        // family quartets (FP64): the heavy head warp per quartet, the rest thread per quartet
-        a.counters = B.primc.as<unsigned long long>() + fli;
-        a.quartets = B.slists[fli].as<uint2>();
-        a.nquartets = (long long)B.cap[fli];
-        a.range = ranges + 4 * fli;
-        a.work = B.work.as<unsigned long long>() + NLIST + fli;
-        CK(launch_family(cl, c->pure, true, a, c->nsm, st));
-        a.range = ranges + 4 * fli + 2;
-        a.work = B.work.as<unsigned long long>() + fli;
-        CK(launch_family(cl, c->pure, false, a, c->nsm, st));
-        nlaunch += 2;
-      }
+      if (prec == 1 && fc && (rc = launch_fam_list(cl, 0))) return rc;
       if (timing && prec == 1) CK(cudaEventRecord(c->evc[cl][2], st));   // FP64 launches done
+      if (prec == 1 && fc && (rc = launch_fam_list(cl, 1))) return rc;
       if (!B.cap[li]) continue;
       const int fl = prec ? MODE_F32 : (df_on(c) ? MODE_DF : 0);
       a.counters = B.primc.as<unsigned long long>() + li;
@@ -1248,7 +1256,7 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   CK(cudaMemcpyAsync(B.h_rb + 1 + NLIST, B.primc.p, sizeof(unsigned long long) * NLIST, cudaMemcpyDeviceToHost,
                      st));
   CK(cudaMemcpyAsync(B.h_rb + 1 + 2 * NLIST, B.counts.as<unsigned long long>() + NLIST,
-                     sizeof(unsigned long long) * NCLASS, cudaMemcpyDeviceToHost, st));
+                     sizeof(unsigned long long) * 2 * NCLASS, cudaMemcpyDeviceToHost, st));
   if (nlaunch_out) *nlaunch_out = nlaunch;
   return OK;
 }
@@ -1266,19 +1274,21 @@ void record_stats(oqpg_ctx* c, const BuildBufs& B, int nlaunch, bool timing) {
   double* S = c->last_stats;
   S[1] = 0;
   double nq = 0, q32 = 0, p32 = 0;
-  const unsigned long long* fmq = B.h_rb + 1 + 2 * NLIST;   // member quartets of the family lists
+  const unsigned long long* fmq = B.h_rb + 1 + 2 * NLIST;   // member quartets of the family lists (FP64, FP32)
   for (int k = 0; k < NCLASS; ++k) {
     // quartets: the shell quartets evaluated (a family quartet counts its members)
-    const int fli = fam_class(k) ? fam_list_index(k) : -1;
-    const bool fl = fli >= 0 && B.fam;
-    const unsigned long long q = cnt[k] + cnt[NCLASS + k] + (fl ? fmq[k] : 0ull);
+    const bool fl = B.fam && fam_class(k);
+    const int f64l = fl ? fam_list_index(k, 0) : 0, f32l = fl ? fam_list_index(k, 1) : 0;
+    const unsigned long long q32k = cnt[NCLASS + k] + (fl ? fmq[NCLASS + k] : 0ull);
+    const unsigned long long q = cnt[k] + q32k + (fl ? fmq[k] : 0ull);
+    const double p32k = (double)nprim[NCLASS + k] + (fl ? (double)nprim[f32l] : 0.0);
     nq += (double)q;
     S[7 + k] = (double)q;
-    S[7 + NCLASS + k] = (double)nprim[k] + (double)nprim[NCLASS + k] + (fl ? (double)nprim[fli] : 0.0);
-    q32 += (double)cnt[NCLASS + k];
-    p32 += (double)nprim[NCLASS + k];
+    S[7 + NCLASS + k] = (double)nprim[k] + p32k + (fl ? (double)nprim[f64l] : 0.0);
+    q32 += (double)q32k;
+    p32 += p32k;
     float tk = 0, t32 = 0;
-    if (timing && (B.cap[k] || B.cap[NCLASS + k] || (fl && B.cap[fli]))) {
+    if (timing && (B.cap[k] || B.cap[NCLASS + k] || (fl && (B.cap[f64l] || B.cap[f32l])))) {
       cudaEventElapsedTime(&tk, c->evc[k][0], c->evc[k][1]);
       cudaEventElapsedTime(&t32, c->evc[k][2], c->evc[k][1]);
     }

@@ -41,12 +41,14 @@ struct MolDev {
 
 // Quartet lists of a build: the FP64 shell-quartet list of every class, the
 // FP32 lists of the precision split, then the family-quartet lists of the
-// shell-family classes (FP64).
+// shell-family classes (FP64, then FP32).
 constexpr int NLIST_SHELL = 2 * NCLASS;
-constexpr int NLIST = NLIST_SHELL + NFAMCLS;
-__host__ __device__ inline int fam_list_index(int c) { return NLIST_SHELL + fam_slot(c); }
+constexpr int NLIST = NLIST_SHELL + 2 * NFAMCLS;
+__host__ __device__ inline int fam_list_index(int c, int f32 = 0) { return NLIST_SHELL + f32 * NFAMCLS + fam_slot(c); }
 // the class of list k
-__host__ __device__ inline int list_class(int k) { return k < NLIST_SHELL ? k % NCLASS : fam_slot_class(k - NLIST_SHELL); }
+__host__ __device__ inline int list_class(int k) {
+  return k < NLIST_SHELL ? k % NCLASS : fam_slot_class((k - NLIST_SHELL) % NFAMCLS);
+}
 
 struct ListArgs {
   int npair;                // pairs of the whole batch (one CTA each)
@@ -93,7 +95,7 @@ struct ListArgs {
   const double* fmsorted_q;              // by descending bound (segment at fmmol0, fmmoln entries)
   const int* fmmol0;
   const int* fmmoln;
-  unsigned long long* fam_members;       // per class: member quartets listed (statistics)
+  unsigned long long* fam_members;       // per class: member quartets listed, FP64 then FP32 (statistics)
 };
 
 // The quartet screen of k_lists (int2.F90:975-986) for bra pair (shells ij,
@@ -288,7 +290,7 @@ struct BuildBufs {
   bool sized = false;
   bool fam = false;                    // the last build issued listed family quartets
   // pinned readback: [0] flag, [1, 1+NLIST) counts, then NLIST primitive
-  // counts, then NCLASS member quartets of the family lists
+  // counts, then the member quartets of the family lists (NCLASS FP64, NCLASS FP32)
   unsigned long long* h_rb = nullptr;
   void release() {
     DevBuf* b[] = {&dj, &dk, &djf, &dkf, &djdf, &dkdf, &gj, &gk, &dsh, &dshf, &dmax, &counts, &primc, &hist,
@@ -341,7 +343,7 @@ struct oqpg_ctx {
   // shell families (oqpg_family.cu): on by default; tables at the current cutoff
   bool fam_enabled = true;
   int nfpair = 0, nfam_multi = 0;   // family pairs; those with more than one member
-  oqpg::DevBuf d_fpairs, d_fmem, d_fprims, d_fcoef, d_fpair_mol, d_fpair_type, d_fq, d_fsorted_idx, d_fsorted_q,
+  oqpg::DevBuf d_fpairs, d_fmem, d_fprims, d_fprimsf, d_fcoef, d_fpair_mol, d_fpair_type, d_fq, d_fsorted_idx, d_fsorted_q,
       d_fmol0, d_fmoln, d_pair_fam_multi, d_fmsorted_idx, d_fmsorted_q, d_fmmol0, d_fmmoln;
   // precision split: 0 = every quartet in FP64, 1 = bound < tau_f32 in FP32
   int precision_mode = 0;

@@ -101,9 +101,9 @@ def test_families_in_a_batch(gpu, oracle_lib):
 
 @pytest.mark.parametrize("mode", ["mixed", "mixed-fast", "df", "mixed-df"])
 def test_families_in_precision_modes(gpu, oracle_lib, mode):
-    """In the FP32-split modes the family quartets stay FP64 and the other
-    shell quartets follow the split; the double-float modes list shell
-    quartets only.  The mode's own bounds hold with families on and off (max
+    """In the FP32-split modes a family quartet runs in FP32 when all the
+    member quartets it lists are below the threshold, else in FP64; the
+    double-float modes list shell quartets only.  The mode's own bounds hold with families on and off (max
     |dF| 1e-6 for the FP32 split, 1e-10 for double-float), and the same shell
     quartets are evaluated."""
     from openqp_gb300 import workloads
@@ -118,7 +118,7 @@ def test_families_in_precision_modes(gpu, oracle_lib, mode):
     assert np.abs(f_off - ref).max() < tol
     assert st_on["quartets"] == st_off["quartets"]
     if mode in ("mixed", "mixed-fast"):
-        assert 0 < st_on["f32_quartets"] < st_off["f32_quartets"]
+        assert 0 < st_on["f32_quartets"] <= st_off["f32_quartets"]
     else:
         assert st_on["f32_quartets"] == st_off["f32_quartets"]
         assert st_on["prim_quartets"] == st_off["prim_quartets"]
