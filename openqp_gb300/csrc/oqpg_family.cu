@@ -439,7 +439,8 @@ cudaError_t launch_family(int c, bool pure, bool warp, bool f32, const BuildArgs
 // Not in the double-float modes: there the shell quartets of the family
 // classes are cheaper in double-float than the family quartets in FP64
 // ((H2O)32 cc-pVDZ: df 7.38 builds/s with shell quartets, 5.86 with FP64
-// family quartets; mixed-df 9.58 and 6.26).
+// family quartets; mixed-df 9.60 with shell quartets, 7.79 with FP32 and
+// FP64 family quartets).
 bool fam_on(const oqpg_ctx* c, const Job& job) {
   return c->fam_enabled && c->nfpair > 0 && !df_on(c) && !job.gen && job.inv_mu2 == 0.0 && !petite_on(c, job);
 }
