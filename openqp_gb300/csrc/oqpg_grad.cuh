@@ -24,6 +24,8 @@
 //
 //   k_grad_lane : small classes; one warp per quartet, the lanes split the
 //                 primitive quartets, each lane keeps its 2D tables in registers.
+//   k_grad_small: the same classes, one thread per quartet (the light
+//                 quartets of a list sorted by primitive-pair product).
 //   k_grad_team : larger classes; one warp per quartet, the tables of each
 //                 primitive quartet go to shared memory (one root x dimension
 //                 per lane), derivative tables are built by all lanes, each
@@ -71,6 +73,7 @@ struct GradArgs {
   double* de;               // 3 x natom, accumulated
   unsigned long long* counters;  // [0] primitive quartets evaluated, [1] quartets evaluated
   int ctas_per_sm;
+  int small;                // lane classes: one thread per quartet (k_grad_small)
 };
 
 template <typename T> struct GAcc;
@@ -185,12 +188,12 @@ __device__ __forceinline__ T warp_sum(T v) {
 }
 
 // Reduce the lanes' 9 partial sums (A, B, C x xyz), apply f, add to de.
+// dE/dR of one quartet (one lane's acc) into de: f = 1/2 for A = B, C = D,
+// AB = CD each; D from translational invariance.
 template <typename T>
-__device__ __forceinline__ void grad_store(const GradArgs& g, const PairDev& P, const PairDev& Q, uint2 qd,
-                                           T* acc, int lane) {
-#pragma unroll
-  for (int k = 0; k < 9; ++k) acc[k] = warp_sum(acc[k]);
-  if (lane == 0) {
+__device__ __forceinline__ void grad_write(const GradArgs& g, const PairDev& P, const PairDev& Q, uint2 qd,
+                                           const T* acc) {
+  {
     double f = 1.0;
     if (P.sha == P.shb) f *= 0.5;
     if (Q.sha == Q.shb) f *= 0.5;
@@ -205,6 +208,15 @@ __device__ __forceinline__ void grad_store(const GradArgs& g, const PairDev& P, 
       atomicAdd(g.de + 3 * at[3] + x, -(a + b + c));
     }
   }
+}
+
+// warp-shared quartet: sum the lanes' acc, lane 0 writes
+template <typename T>
+__device__ __forceinline__ void grad_store(const GradArgs& g, const PairDev& P, const PairDev& Q, uint2 qd,
+                                           T* acc, int lane) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) acc[k] = warp_sum(acc[k]);
+  if (lane == 0) grad_write(g, P, Q, qd, acc);
 }
 
 template <typename T>
@@ -229,13 +241,78 @@ __device__ __forceinline__ bool grad_prim_skip(const GradArgs& g, T pfac, T dabm
   return a < (T)sqrt(g.dtol2) * rs || a * dabmax < (T)sqrt(g.dabcut2) * rs;
 }
 
+// One primitive quartet (bra kb, ket kq) of a contracted quartet: skipped by
+// grd2's primitive screens (returns false), or its derivative integrals
+// contracted with the density block gam into acc (dA, dB, dC per dimension).
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ bool grad_prim_body(const GradArgs& g, const typename PrimT<T>::type* prims,
+                                               const PairDev& P, const PairDev& Q, int kb, int kq, const T AB[3],
+                                               const T CD[3], const T* gam, T dabmax, T* acc) {
+  using K = Cls<LA, LB, LC, LD>;
+  using G = GCls<LA, LB, LC, LD>;
+  using PP = typename PrimT<T>::type;
+  constexpr int NE = K::NE, NR = G::NR, N2DX = G::N2DX;
+  PP bp, kp;
+  prim_load(prims + P.poff + kb, bp);
+  prim_load(prims + Q.poff + kq, kp);
+  if (grad_prim_skip<T>(g, bp.sp * kp.sp, dabmax, fma(bp.p * kp.p, (T)g.inv_mu2, bp.p + kp.p))) return false;
+  PrimQuartet<T> pqd;
+  prim_setup<T, true>(bp, kp, pqd, (T)g.inv_mu2);
+  const T a2 = (T)2 * GAcc<T>::alpha(g, P.poff + kb);
+  const T b2 = (T)2 * bp.p - a2;
+  const T c2 = (T)2 * GAcc<T>::alpha(g, Q.poff + kq);
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    T u, w;
+    rys_node_weight<NR, T>(pqd.X, r, g.roots_f32 != 0, u, w);
+    w *= pqd.pref;
+    const T uq = u * pqd.qi, up = u * pqd.pi;
+    const T b00 = (T)0.5 * pqd.inv * u;
+    const T b10 = fma(-bp.hp, uq, bp.hp);
+    const T b01 = fma(-kp.hp, up, kp.hp);
+    T X[3][N2DX];
+    const T PA[3] = {bp.ax, bp.ay, bp.az}, QC[3] = {kp.ax, kp.ay, kp.az};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const T c00 = fma(-uq, pqd.PQ[d], PA[d]);
+      const T d00 = fma(up, pqd.PQ[d], QC[d]);
+      twod<LA + 1, LB, LC + 1, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01, AB[d], CD[d],
+                                      [&](int i, T v) { X[d][i] = v; });
+    }
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+      T I[3], dA[3], dB[3], dC[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const int o = G::xoff(e, d);
+        const int ea = cart_e(LA, G::ia(e), d), eb = cart_e(LB, G::ib(e), d), ec = cart_e(LC, G::ic(e), d);
+        I[d] = X[d][o];
+        const T up1 = X[d][o + G::SA];
+        dA[d] = a2 * up1;
+        if (ea > 0) dA[d] = fma(-(T)ea, X[d][o - G::SA], dA[d]);
+        dB[d] = b2 * fma(AB[d], I[d], up1);
+        if (eb > 0) dB[d] = fma(-(T)eb, X[d][o - G::SB], dB[d]);
+        dC[d] = c2 * X[d][o + G::SC];
+        if (ec > 0) dC[d] = fma(-(T)ec, X[d][o - G::SC], dC[d]);
+      }
+      const T ge = gam[e];
+      const T tz = ge * I[2];
+      const T yz = I[1] * tz, xz = I[0] * tz, xy = I[0] * I[1] * ge;
+      acc[0] = fma(dA[0], yz, acc[0]); acc[1] = fma(dA[1], xz, acc[1]); acc[2] = fma(dA[2], xy, acc[2]);
+      acc[3] = fma(dB[0], yz, acc[3]); acc[4] = fma(dB[1], xz, acc[4]); acc[5] = fma(dB[2], xy, acc[5]);
+      acc[6] = fma(dC[0], yz, acc[6]); acc[7] = fma(dC[1], xz, acc[7]); acc[8] = fma(dC[2], xy, acc[8]);
+    }
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 template <int LA, int LB, int LC, int LD, typename T>
 __global__ void __launch_bounds__(128) k_grad_lane(const GradArgs g) {
   using K = Cls<LA, LB, LC, LD>;
   using G = GCls<LA, LB, LC, LD>;
   using PP = typename PrimT<T>::type;
-  constexpr int NE = K::NE, NR = G::NR, N2DX = G::N2DX;
+  constexpr int NE = K::NE;
   __shared__ T s_gam[4][NE];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* gam = s_gam[warp];
@@ -267,58 +344,7 @@ __global__ void __launch_bounds__(128) k_grad_lane(const GradArgs g) {
     const int nP = P.pcnt, nQ = Q.pcnt;
     for (int pq = lane; pq < nP * nQ; pq += 32) {
       const int kq = pq / nP, kb = pq - kq * nP;
-      PP bp, kp;
-      prim_load(prims + P.poff + kb, bp);
-      prim_load(prims + Q.poff + kq, kp);
-      if (grad_prim_skip<T>(g, bp.sp * kp.sp, dabmax, fma(bp.p * kp.p, (T)g.inv_mu2, bp.p + kp.p))) continue;
-      ++nprim;
-      PrimQuartet<T> pqd;
-      prim_setup<T, true>(bp, kp, pqd, (T)g.inv_mu2);
-      const T a2 = (T)2 * GAcc<T>::alpha(g, P.poff + kb);
-      const T b2 = (T)2 * bp.p - a2;
-      const T c2 = (T)2 * GAcc<T>::alpha(g, Q.poff + kq);
-#pragma unroll
-      for (int r = 0; r < NR; ++r) {
-        T u, w;
-        rys_node_weight<NR, T>(pqd.X, r, g.roots_f32 != 0, u, w);
-        w *= pqd.pref;
-        const T uq = u * pqd.qi, up = u * pqd.pi;
-        const T b00 = (T)0.5 * pqd.inv * u;
-        const T b10 = fma(-bp.hp, uq, bp.hp);
-        const T b01 = fma(-kp.hp, up, kp.hp);
-        T X[3][N2DX];
-        const T PA[3] = {bp.ax, bp.ay, bp.az}, QC[3] = {kp.ax, kp.ay, kp.az};
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          const T c00 = fma(-uq, pqd.PQ[d], PA[d]);
-          const T d00 = fma(up, pqd.PQ[d], QC[d]);
-          twod<LA + 1, LB, LC + 1, LD, T>(d == 2 ? w : (T)1, c00, d00, b00, b10, b01, AB[d], CD[d],
-                                          [&](int i, T v) { X[d][i] = v; });
-        }
-#pragma unroll
-        for (int e = 0; e < NE; ++e) {
-          T I[3], dA[3], dB[3], dC[3];
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            const int o = G::xoff(e, d);
-            const int ea = cart_e(LA, G::ia(e), d), eb = cart_e(LB, G::ib(e), d), ec = cart_e(LC, G::ic(e), d);
-            I[d] = X[d][o];
-            const T up1 = X[d][o + G::SA];
-            dA[d] = a2 * up1;
-            if (ea > 0) dA[d] = fma(-(T)ea, X[d][o - G::SA], dA[d]);
-            dB[d] = b2 * fma(AB[d], I[d], up1);
-            if (eb > 0) dB[d] = fma(-(T)eb, X[d][o - G::SB], dB[d]);
-            dC[d] = c2 * X[d][o + G::SC];
-            if (ec > 0) dC[d] = fma(-(T)ec, X[d][o - G::SC], dC[d]);
-          }
-          const T ge = gam[e];
-          const T tz = ge * I[2];
-          const T yz = I[1] * tz, xz = I[0] * tz, xy = I[0] * I[1] * ge;
-          acc[0] = fma(dA[0], yz, acc[0]); acc[1] = fma(dA[1], xz, acc[1]); acc[2] = fma(dA[2], xy, acc[2]);
-          acc[3] = fma(dB[0], yz, acc[3]); acc[4] = fma(dB[1], xz, acc[4]); acc[5] = fma(dB[2], xy, acc[5]);
-          acc[6] = fma(dC[0], yz, acc[6]); acc[7] = fma(dC[1], xz, acc[7]); acc[8] = fma(dC[2], xy, acc[8]);
-        }
-      }
+      if (grad_prim_body<LA, LB, LC, LD, T>(g, prims, P, Q, kb, kq, AB, CD, gam, dabmax, acc)) ++nprim;
     }
     grad_store<T>(g, P, Q, qd, acc, lane);
     __syncwarp();
@@ -326,6 +352,55 @@ __global__ void __launch_bounds__(128) k_grad_lane(const GradArgs g) {
   if (g.counters) {
     if (nprim) atomicAdd(g.counters, nprim);
     if (lane == 0 && nq) atomicAdd(g.counters + 1, nq);
+  }
+}
+
+// Thread per quartet for the same classes (the light quartets of a list
+// sorted by primitive-pair product, heaviest first): warps take chunks of
+// 32 quartets, each lane runs its quartet's primitive quartets alone, with
+// the density block in registers.
+template <int LA, int LB, int LC, int LD, typename T>
+__global__ void __launch_bounds__(128) k_grad_small(const GradArgs g) {
+  using K = Cls<LA, LB, LC, LD>;
+  using G = GCls<LA, LB, LC, LD>;
+  using PP = typename PrimT<T>::type;
+  constexpr int NE = K::NE;
+  const int lane = threadIdx.x & 31;
+  const PP* prims = GAcc<T>::prims(g);
+  unsigned long long nprim = 0, nq = 0;
+  for (;;) {
+    const long long base = grab(g.work, 32u, lane);
+    if (base >= g.nquartets) break;
+    const long long t = base + lane;
+    if (t >= g.nquartets) continue;
+    const uint2 qd = g.quartets[t];
+    PairDev P, Q;
+    T AB[3], CD[3];
+    int ro[4];
+    quartet_setup<T>(g, qd, P, Q, AB, CD, ro);
+    T gam[NE];
+    T dabmax = 0;
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+      const T v = gamma_elem<T>(g, ro[0] + G::ia(e), ro[1] + G::ib(e), ro[2] + G::ic(e), ro[3] + G::id(e));
+      gam[e] = v;
+      const T nrm = (T)(cart_norm(LA, G::ia(e)) * cart_norm(LB, G::ib(e)) * cart_norm(LC, G::ic(e)) *
+                        cart_norm(LD, G::id(e)));
+      dabmax = fmax(dabmax, g.pure ? fabs(v) : fabs(v) / nrm);
+    }
+    if ((double)dabmax * __ldg(g.q + qd.x) * __ldg(g.q + qd.y) < g.cutoff2) continue;
+    ++nq;
+    T acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) acc[k] = 0;
+    for (int kq = 0; kq < Q.pcnt; ++kq)
+      for (int kb = 0; kb < P.pcnt; ++kb)
+        if (grad_prim_body<LA, LB, LC, LD, T>(g, prims, P, Q, kb, kq, AB, CD, gam, dabmax, acc)) ++nprim;
+    grad_write(g, P, Q, qd, acc);
+  }
+  if (g.counters) {
+    if (nprim) atomicAdd(g.counters, nprim);
+    if (nq) atomicAdd(g.counters + 1, nq);
   }
 }
 
@@ -561,10 +636,22 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
 template <int LA, int LB, int LC, int LD>
 constexpr bool grad_lane_class() { return 3 * GCls<LA, LB, LC, LD>::N2DX <= 48; }
 
+// g.small: the thread-per-quartet kernel (lane classes only)
 template <int LA, int LB, int LC, int LD, typename T>
 cudaError_t launch_grad_t(const GradArgs& g, int nsm, cudaStream_t st) {
   if (g.nquartets <= 0) return cudaSuccess;
   if constexpr (grad_lane_class<LA, LB, LC, LD>()) {
+    if (g.small) {
+      auto kern = k_grad_small<LA, LB, LC, LD, T>;
+      int per_sm = 1;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0);
+      if (g.ctas_per_sm > 0 && g.ctas_per_sm < per_sm) per_sm = g.ctas_per_sm;
+      if (per_sm < 1) per_sm = 1;
+      long long blocks = (g.nquartets + 127) / 128;
+      if (blocks > (long long)nsm * per_sm) blocks = (long long)nsm * per_sm;
+      kern<<<(unsigned)blocks, 128, 0, st>>>(g);
+      return cudaGetLastError();
+    }
     auto kern = k_grad_lane<LA, LB, LC, LD, T>;
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0);

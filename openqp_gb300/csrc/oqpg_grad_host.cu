@@ -41,6 +41,13 @@ struct GListArgs {
   int write;
 };
 
+// The classes whose gradient kernels keep the 2D tables in registers
+// (grad_lane_class in oqpg_grad.cuh: 3 (la+2)(lb+1)(lc+2)(ld+1) <= 48).
+bool grad_lane_class_rt(int c) {
+  const ClassInfo& ci = class_info(c);
+  return 3 * (ci.l[0] + 2) * (ci.l[1] + 1) * (ci.l[2] + 2) * (ci.l[3] + 1) <= 48;
+}
+
 __global__ void __launch_bounds__(256) k_grad_lists(const GListArgs a) {
   __shared__ unsigned cnt[NLIST_SHELL];
   __shared__ unsigned long long base[NLIST_SHELL];
@@ -286,7 +293,7 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
   }
   if ((rc = gupload(c->d_dshg, dsh, st))) return rc;
   GK(c->d_gcounts.ensure(sizeof(unsigned long long) * NLIST_SHELL));
-  GK(c->d_gwork.ensure(sizeof(unsigned long long) * NLIST_SHELL));
+  GK(c->d_gwork.ensure(sizeof(unsigned long long) * 2 * NLIST_SHELL));
   GK(c->d_gcnt.ensure(sizeof(unsigned long long) * 2));
   GK(c->d_de.ensure(sizeof(double) * 3 * c->natom));
   GListArgs la{};
@@ -326,8 +333,66 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
     if (ok) break;
     if (pass == 2) return DEV_ERR;
   }
+  // the lists of the lane classes sorted by primitive-pair product, heaviest
+  // first (counting sort on the device, cursors from the host): quartets of
+  // at least 2^8 primitive quartets run warp per quartet (k_grad_lane), the
+  // rest thread per quartet (k_grad_small)
+  unsigned long long head[NLIST_SHELL] = {0};
+  bool sorted[NLIST_SHELL] = {false};
+  {
+    unsigned long long off[NLIST_SHELL + 1] = {0};
+    for (int li = 0; li < NLIST_SHELL; ++li) {
+      sorted[li] = counts[li] > 0 && grad_lane_class_rt(li % NCLASS);
+      off[li + 1] = off[li] + (sorted[li] ? counts[li] : 0);
+    }
+    if (off[NLIST_SHELL] > 0) {
+      GK(c->d_gbins.ensure(off[NLIST_SHELL]));
+      GK(c->d_ghist.ensure(sizeof(unsigned long long) * NLIST_SHELL * NBIN));
+      GK(c->d_gcur.ensure(sizeof(unsigned long long) * NLIST_SHELL * NBIN));
+      GK(cudaMemsetAsync(c->d_ghist.p, 0, sizeof(unsigned long long) * NLIST_SHELL * NBIN, st));
+      unsigned char* bins = c->d_gbins.as<unsigned char>();
+      unsigned long long* hist = c->d_ghist.as<unsigned long long>();
+      for (int li = 0; li < NLIST_SHELL; ++li) {
+        if (!sorted[li]) continue;
+        if (c->gscaps[li] < c->gcaps[li]) {
+          GK(c->d_gslists[li].ensure(sizeof(uint2) * c->gcaps[li]));
+          c->gscaps[li] = c->gcaps[li];
+        }
+        k_bin_hist<<<(unsigned)std::min<unsigned long long>((counts[li] + 255) / 256, c->nsm * 4ULL), 256, 0, st>>>(
+            c->d_glists[li].as<uint2>(), (long long)counts[li], nullptr, c->d_gpairs.as<PairDev>(), nullptr, 0.0f,
+            PAIR_MASK, 0xffffffffu, bins + off[li], hist + li * NBIN);
+        GK(cudaGetLastError());
+      }
+      std::vector<unsigned long long> h_hist((size_t)NLIST_SHELL * NBIN), h_cur((size_t)NLIST_SHELL * NBIN);
+      GK(cudaMemcpyAsync(h_hist.data(), hist, sizeof(unsigned long long) * h_hist.size(), cudaMemcpyDeviceToHost, st));
+      GK(cudaStreamSynchronize(st));
+      const int nb_head = head_bins(PRIM_SPLIT_LOG2);
+      for (int li = 0; li < NLIST_SHELL; ++li) {
+        if (!sorted[li]) continue;
+        unsigned long long sum = 0;
+        for (int b = 0; b < NBIN; ++b) {
+          h_cur[(size_t)li * NBIN + b] = sum;
+          sum += h_hist[(size_t)li * NBIN + b];
+          if (b < nb_head) head[li] = sum;
+        }
+        if (sum != counts[li]) return DEV_ERR;
+      }
+      GK(cudaMemcpyAsync(c->d_gcur.p, h_cur.data(), sizeof(unsigned long long) * h_cur.size(), cudaMemcpyHostToDevice,
+                         st));
+      const long long chunk = 4096;
+      for (int li = 0; li < NLIST_SHELL; ++li) {
+        if (!sorted[li]) continue;
+        k_bin_scatter<<<(unsigned)((counts[li] + chunk - 1) / chunk), 256, 0, st>>>(
+            c->d_glists[li].as<uint2>(), (long long)counts[li], nullptr, c->d_gpairs.as<PairDev>(), PAIR_MASK,
+            0xffffffffu, bins + off[li], c->d_gcur.as<unsigned long long>() + li * NBIN,
+            c->d_gslists[li].as<uint2>(), chunk, nullptr);
+        GK(cudaGetLastError());
+      }
+      GK(cudaStreamSynchronize(st));   // h_cur is freed at the end of this scope
+    }
+  }
   GK(cudaMemsetAsync(c->d_de.p, 0, sizeof(double) * 3 * c->natom, st));
-  GK(cudaMemsetAsync(c->d_gwork.p, 0, sizeof(unsigned long long) * NLIST_SHELL, st));
+  GK(cudaMemsetAsync(c->d_gwork.p, 0, sizeof(unsigned long long) * 2 * NLIST_SHELL, st));
   GK(cudaMemsetAsync(c->d_gcnt.p, 0, sizeof(unsigned long long) * 2, st));
   GradArgs g{};
   g.shells = c->d_shells.as<ShellDev>();
@@ -381,11 +446,29 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
     const bool f32 = li >= NCLASS;
     listed += (double)counts[li];
     if (f32) listed32 += (double)counts[li];
+    auto launch = [&]() {
+      return cl < 15 ? launch_grad_a(cl, g, f32, c->nsm, st)
+                     : cl < NCLASS_SD ? launch_grad_b(cl, g, f32, c->nsm, st) : launch_grad_f(cl, g, c->nsm, st);
+    };
+    if (sorted[li]) {
+      const uint2* sl = c->d_gslists[li].as<uint2>();
+      g.quartets = sl;                       // heavy head: warp per quartet
+      g.nquartets = (long long)head[li];
+      g.work = c->d_gwork.as<unsigned long long>() + li;
+      g.small = 0;
+      GK(launch());
+      g.quartets = sl + head[li];            // the rest: thread per quartet
+      g.nquartets = (long long)(counts[li] - head[li]);
+      g.work = c->d_gwork.as<unsigned long long>() + NLIST_SHELL + li;
+      g.small = 1;
+      GK(launch());
+      g.small = 0;
+      continue;
+    }
     g.quartets = c->d_glists[li].as<uint2>();
     g.nquartets = (long long)counts[li];
     g.work = c->d_gwork.as<unsigned long long>() + li;
-    GK(cl < 15 ? launch_grad_a(cl, g, f32, c->nsm, st)
-               : cl < NCLASS_SD ? launch_grad_b(cl, g, f32, c->nsm, st) : launch_grad_f(cl, g, c->nsm, st));
+    GK(launch());
   }
   std::vector<double> h_de(3 * c->natom);
   unsigned long long h_cnt[2];

@@ -865,6 +865,10 @@ void ctx_free(oqpg_ctx* c) {
   c->hb.release();
   c->gb.release();
   for (auto& b : c->d_glists) b.release();
+  for (auto& b : c->d_gslists) b.release();
+  c->d_gbins.release();
+  c->d_ghist.release();
+  c->d_gcur.release();
   if (c->h_in) cudaFreeHost(c->h_in);
   if (c->h_out) cudaFreeHost(c->h_out);
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);

@@ -379,6 +379,9 @@ struct oqpg_ctx {
       d_gcounts, d_gwork, d_de, d_gcnt;
   oqpg::DevBuf d_glists[oqpg::NLIST_SHELL];   // FP64 lists, then the FP32 lists of the precision split
   unsigned long long gcaps[oqpg::NLIST_SHELL] = {0};
+  oqpg::DevBuf d_gslists[oqpg::NLIST_SHELL];  // the lane classes' lists sorted by primitive-pair product
+  unsigned long long gscaps[oqpg::NLIST_SHELL] = {0};
+  oqpg::DevBuf d_gbins, d_ghist, d_gcur;
   double grad_stats[5] = {0, 0, 0, 0, 0};  // quartets listed, evaluated, primitive quartets, ms, FP32 listed
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t evc[oqpg::NCLASS][3] = {};   // class start, after its FP64 launches, end
