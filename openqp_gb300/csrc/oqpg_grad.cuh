@@ -63,6 +63,7 @@ struct GradArgs {
   double cutoff2;           // quartet skipped if dabmax Q_P Q_Q < cutoff / 2
   double dtol2;             // (sp sq)^2 < dtol2 (p + q): primitive quartet skipped
   double dabcut2;           // (sp sq)^2 dabmax^2 < dabcut2 (p + q): skipped
+  float sdtol, sdab;        // sqrt(dtol2), sqrt(dabcut2) for the FP32 pre-screen
   // MRSF form (mrsf != 0): eleven Cartesian-effective matrices d2a, d2b, p2a,
   // p2b, ball, bo2v, bo1v, bco1, bco2, o21v, co12 at mm + m ncart^2 and the
   // coefficients of grd2_mrsf_compute_data_t_get_density (mq with sgnk)
@@ -241,6 +242,24 @@ __device__ __forceinline__ bool grad_prim_skip(const GradArgs& g, T pfac, T dabm
   return a < (T)sqrt(g.dtol2) * rs || a * dabmax < (T)sqrt(g.dabcut2) * rs;
 }
 
+// grd2's primitive screens for primitive pairs b and k: kept or skipped.  In
+// FP64 kernels the tests run in FP32 first (no FP64 square root) and in FP64
+// only within 1e-4 of a threshold.
+template <typename T>
+__device__ __forceinline__ bool grad_prim_keep(const GradArgs& g, const typename PrimT<T>::type* b,
+                                               const typename PrimT<T>::type* k, T dabmax) {
+  if constexpr (std::is_same<T, double>::value) {
+    const float2 bs = prim_screen(b), ks = prim_screen(k);
+    const float af = fabsf(bs.x * ks.x);
+    const float rsf = sqrtf(fmaf(bs.y * ks.y, (float)g.inv_mu2, bs.y + ks.y));
+    const float t1 = g.sdtol * rsf, t2 = g.sdab * rsf, a2 = af * (float)dabmax;
+    if (af < t1 * 0.9999f || a2 < t2 * 0.9999f) return false;
+    if (af > t1 * 1.0001f && a2 > t2 * 1.0001f) return true;
+  }
+  const T pb = __ldg(&b->p), pk = __ldg(&k->p);
+  return !grad_prim_skip<T>(g, __ldg(&b->sp) * __ldg(&k->sp), dabmax, fma(pb * pk, (T)g.inv_mu2, pb + pk));
+}
+
 // One primitive quartet (bra kb, ket kq) of a contracted quartet: skipped by
 // grd2's primitive screens (returns false), or its derivative integrals
 // contracted with the density block gam into acc (dA, dB, dC per dimension).
@@ -252,10 +271,10 @@ __device__ __forceinline__ bool grad_prim_body(const GradArgs& g, const typename
   using G = GCls<LA, LB, LC, LD>;
   using PP = typename PrimT<T>::type;
   constexpr int NE = K::NE, NR = G::NR, N2DX = G::N2DX;
+  if (!grad_prim_keep<T>(g, prims + P.poff + kb, prims + Q.poff + kq, dabmax)) return false;
   PP bp, kp;
   prim_load(prims + P.poff + kb, bp);
   prim_load(prims + Q.poff + kq, kp);
-  if (grad_prim_skip<T>(g, bp.sp * kp.sp, dabmax, fma(bp.p * kp.p, (T)g.inv_mu2, bp.p + kp.p))) return false;
   PrimQuartet<T> pqd;
   prim_setup<T, true>(bp, kp, pqd, (T)g.inv_mu2);
   const T a2 = (T)2 * GAcc<T>::alpha(g, P.poff + kb);
@@ -512,10 +531,7 @@ __global__ void __launch_bounds__(128) k_grad_team(const GradArgs g) {
         const int cand = c0 + lane;
         if (cand < total) {
           const int kq = cand / nP, kb = cand - kq * nP;
-          const PP* b = prims + P.poff + kb;
-          const PP* k = prims + Q.poff + kq;
-          const T pb = __ldg(&b->p), pk = __ldg(&k->p);
-          keep = !grad_prim_skip<T>(g, __ldg(&b->sp) * __ldg(&k->sp), dabmax, fma(pb * pk, (T)g.inv_mu2, pb + pk));
+          keep = grad_prim_keep<T>(g, prims + P.poff + kb, prims + Q.poff + kq, dabmax);
         }
       }
       unsigned mask = __ballot_sync(0xffffffffu, keep);

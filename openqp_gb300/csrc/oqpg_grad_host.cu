@@ -437,6 +437,8 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
   if (zbig > 1e7) dabcut /= 10;
   g.dtol2 = 1e-40;
   g.dabcut2 = dabcut * dabcut;
+  g.sdtol = (float)std::sqrt(g.dtol2);
+  g.sdab = (float)std::sqrt(g.dabcut2);
   g.de = c->d_de.as<double>();
   g.counters = c->d_gcnt.as<unsigned long long>();
   double listed = 0, listed32 = 0;
