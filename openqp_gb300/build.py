@@ -17,7 +17,7 @@ LIB = os.path.join(OUT, "libopenqp_gb300.so")
 SOURCES = ["oqpg_cls_%d.cu" % g for g in (17, 15, 14, 16, 2, 3, 4, 18, 13, 12, 11, 10, 9, 8, 7, 6, 5, 1, 0)] + \
     ["oqpg_grad_cls_f%d.cu" % g for g in range(5)] + \
     ["oqpg_grad_cls_a.cu", "oqpg_grad_cls_b.cu", "oqpg_host.cu", "oqpg_noalloc.cu", "oqpg_onee.cu", "oqpg_grad_host.cu",
-     "oqpg_response.cu", "oqpg_sigma.cu", "oqpg_petite.cu", "oqpg_family.cu"]
+     "oqpg_response.cu", "oqpg_sigma.cu", "oqpg_petite.cu", "oqpg_family.cu", "oqpg_family_df.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-diag-suppress", "128,177,550"]

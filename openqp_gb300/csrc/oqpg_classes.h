@@ -85,7 +85,11 @@ __host__ __device__ inline int fam_slot(int c) { return c <= 4 ? c : c - 1; }
 __host__ __device__ inline int fam_slot_class(int j) { return j <= 4 ? j : j + 1; }
 // Family-pair types: the pair types of the family classes (ss, sp, sd, pp, pd).
 __host__ __device__ inline bool fam_pair_type(int t) { return t <= 4; }
-cudaError_t launch_family(int c, bool pure, bool warp, bool f32, const BuildArgs& a, int nsm, cudaStream_t st);
+// kind: FAM_FP64, FAM_F32 (FP32 family quartets of the split) or FAM_DF
+// (double-float, the df modes)
+constexpr int FAM_FP64 = 0, FAM_F32 = 1, FAM_DF = 2;
+cudaError_t launch_family(int c, bool pure, bool warp, int kind, const BuildArgs& a, int nsm, cudaStream_t st);
+cudaError_t launch_family_df(int c, bool pure, bool warp, const BuildArgs& a, int nsm, cudaStream_t st);
 
 // Thread per quartet by default from this many quartets per SM in a list
 // (four waves of 128-thread CTAs at two CTAs per SM, the occupancy at 255

@@ -71,6 +71,10 @@ struct FamCoef {
   double sp[FAM_MAX];
   float spf[FAM_MAX];
 };
+// the members' K/p as double-float pairs (hi, lo), for the df family kernels
+struct FamCoefDF {
+  float2 sp[FAM_MAX];
+};
 // Family-quartet list entries: family pair indices in the low 24 bits of x
 // and y, and the member combinations (m of x, n of y) that pass the quartet
 // screen as bit 4m + n of a 16-bit mask, bits 0-7 in the top byte of x and
@@ -123,7 +127,9 @@ struct BuildArgs {
   const FamMem* fmem;
   const PrimPair* fprims;        // union primitive pairs
   const PrimPairF* fprimsf;      // FP32 copy (the FP32 family quartets of the precision split)
+  const PrimPairDF* fprimsdf;    // double-float copy (the double-float modes)
   const FamCoef* fcoef;          // per union primitive pair: the members' K/p
+  const FamCoefDF* fcoefdf;      // and as double-float pairs
 };
 
 // ---------------------------------------------------------------------------

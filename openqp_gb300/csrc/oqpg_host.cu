@@ -858,7 +858,8 @@ void ctx_free(oqpg_ctx* c) {
                     &c->d_gpairs, &c->d_gprims, &c->d_galpha, &c->d_gprimsf, &c->d_galphaf, &c->d_coff,
                     &c->d_atom, &c->d_gmat, &c->d_gmatf, &c->d_dshg, &c->d_gcounts, &c->d_gwork, &c->d_de,
                     &c->d_gcnt, &c->d_q_att, &c->d_qf_att, &c->d_sorted_idx_att, &c->d_sorted_q_att,
-                    &c->d_fpairs, &c->d_fmem, &c->d_fprims, &c->d_fprimsf, &c->d_fcoef, &c->d_fpair_mol, &c->d_fpair_type,
+                    &c->d_fpairs, &c->d_fmem, &c->d_fprims, &c->d_fprimsf, &c->d_fprimsdf, &c->d_fcoef,
+                    &c->d_fcoefdf, &c->d_fpair_mol, &c->d_fpair_type,
                     &c->d_fq, &c->d_fsorted_idx, &c->d_fsorted_q, &c->d_fmol0, &c->d_fmoln,
                     &c->d_pair_fam_multi, &c->d_fmsorted_idx, &c->d_fmsorted_q, &c->d_fmmol0, &c->d_fmmoln};
   for (DevBuf* b : bufs) b->release();
@@ -1187,6 +1188,8 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   a.fmem = c->d_fmem.as<FamMem>();
   a.fprims = c->d_fprims.as<PrimPair>();
   a.fprimsf = c->d_fprimsf.as<PrimPairF>();
+  a.fprimsdf = c->d_fprimsdf.as<PrimPairDF>();
+  a.fcoefdf = c->d_fcoefdf.as<FamCoefDF>();
   a.fcoef = c->d_fcoef.as<FamCoef>();
   unsigned long long* ranges = B.ranges.as<unsigned long long>();
   // heaviest classes first
@@ -1200,10 +1203,11 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
     a.nquartets = (long long)B.cap[fli];
     a.range = ranges + 4 * fli;
     a.work = B.work.as<unsigned long long>() + NLIST + fli;
-    CK(launch_family(cl, c->pure, true, f32 != 0, a, c->nsm, st));
+    const int kind = f32 ? FAM_F32 : (df_on(c) ? FAM_DF : FAM_FP64);
+    CK(launch_family(cl, c->pure, true, kind, a, c->nsm, st));
     a.range = ranges + 4 * fli + 2;
     a.work = B.work.as<unsigned long long>() + fli;
-    CK(launch_family(cl, c->pure, false, f32 != 0, a, c->nsm, st));
+    CK(launch_family(cl, c->pure, false, kind, a, c->nsm, st));
     nlaunch += 2;
     return OK;
   };

@@ -343,7 +343,7 @@ struct oqpg_ctx {
   // shell families (oqpg_family.cu): on by default; tables at the current cutoff
   bool fam_enabled = true;
   int nfpair = 0, nfam_multi = 0;   // family pairs; those with more than one member
-  oqpg::DevBuf d_fpairs, d_fmem, d_fprims, d_fprimsf, d_fcoef, d_fpair_mol, d_fpair_type, d_fq, d_fsorted_idx, d_fsorted_q,
+  oqpg::DevBuf d_fpairs, d_fmem, d_fprims, d_fprimsf, d_fprimsdf, d_fcoef, d_fcoefdf, d_fpair_mol, d_fpair_type, d_fq, d_fsorted_idx, d_fsorted_q,
       d_fmol0, d_fmoln, d_pair_fam_multi, d_fmsorted_idx, d_fmsorted_q, d_fmmol0, d_fmmoln;
   // precision split: 0 = every quartet in FP64, 1 = bound < tau_f32 in FP32
   int precision_mode = 0;

@@ -102,10 +102,10 @@ def test_families_in_a_batch(gpu, oracle_lib):
 @pytest.mark.parametrize("mode", ["mixed", "mixed-fast", "df", "mixed-df"])
 def test_families_in_precision_modes(gpu, oracle_lib, mode):
     """In the FP32-split modes a family quartet runs in FP32 when all the
-    member quartets it lists are below the threshold, else in FP64; the
-    double-float modes list shell quartets only.  The mode's own bounds hold with families on and off (max
-    |dF| 1e-6 for the FP32 split, 1e-10 for double-float), and the same shell
-    quartets are evaluated."""
+    member quartets it lists are below the threshold, else in FP64 (in
+    double-float in the df modes).  The mode's own bounds hold with families
+    on and off (max |dF| 1e-6 for the FP32 split, 1e-10 for double-float),
+    the same shell quartets are evaluated, from fewer primitive integrals."""
     from openqp_gb300 import workloads
     bas = workloads.water_cluster_basis(4, workloads.cube_edge_like_c1(4), 6, "cc-pvdz", spherical=True)
     d = workloads.density(bas, 20, 3)
@@ -117,8 +117,8 @@ def test_families_in_precision_modes(gpu, oracle_lib, mode):
     assert np.abs(f_on - ref).max() < tol
     assert np.abs(f_off - ref).max() < tol
     assert st_on["quartets"] == st_off["quartets"]
-    if mode in ("mixed", "mixed-fast"):
-        assert 0 < st_on["f32_quartets"] <= st_off["f32_quartets"]
+    assert st_on["prim_quartets"] < st_off["prim_quartets"]
+    if mode == "df":
+        assert st_on["f32_quartets"] == st_off["f32_quartets"] == 0
     else:
-        assert st_on["f32_quartets"] == st_off["f32_quartets"]
-        assert st_on["prim_quartets"] == st_off["prim_quartets"]
+        assert 0 < st_on["f32_quartets"] <= st_off["f32_quartets"]
