@@ -326,9 +326,9 @@ int oqpg_get_kernel_family(const oqpg_ctx* ctx, int* family, int* available);
  * contracted shells of cc-pVXZ sets, which OpenQP stores as separate
  * segmented shells) share their primitive integrals in the (ss|ss), (ss|sp),
  * (ss|sd), (ss|pp), (ss|pd), (sp|sp), (sp|sd) and (sp|pp) classes of SCF
- * builds in the FP64 and FP32-split precision modes (in the split a family
- * quartet runs in FP32 when every member quartet it lists is below the
- * threshold; the double-float modes list shell quartets only): one primitive
+ * builds in every precision mode (in the split a family quartet runs in
+ * FP32 when every member quartet it lists is below the threshold, else in
+ * FP64, or double-float in the df modes): one primitive
  * integral per family quartet, added to every member shell quartet with its
  * own contraction factors, primitive screens, quartet screen, element cutoff
  * and digestion, so the result is the reference's shell-by-shell sum.

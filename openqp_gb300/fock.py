@@ -307,7 +307,7 @@ class FockBuilder:
         """Share the primitive integrals of two s shells on one atom whose
         exponents are equal or nested (cc-pVXZ's generally contracted shells)
         in the s-rich classes
-        ((ss|ss) .. (ss|pd), (sp|sp), (sp|sd), (sp|pp)) of plain FP64 SCF builds
+        ((ss|ss) .. (ss|pd), (sp|sp), (sp|sd), (sp|pp)) of SCF builds, every precision mode
         (default on); off: every shell quartet on its own."""
         rc = lib().oqpg_set_shell_families(self.h, 1 if on else 0)
         if rc != 0:
