@@ -306,9 +306,9 @@ class FockBuilder:
     def set_shell_families(self, on):
         """Share the primitive integrals of two s shells on one atom whose
         exponents are equal or nested (cc-pVXZ's generally contracted shells)
-        in the s-rich classes
-        ((ss|ss) .. (ss|pd), (sp|sp), (sp|sd), (sp|pp)) of SCF builds, every precision mode
-        (default on); off: every shell quartet on its own."""
+        in the s-rich classes ((ss|ss) .. (ss|pd), (sp|sp), (sp|sd), (sp|pp))
+        of SCF builds in every precision mode (default on); off: every shell
+        quartet on its own."""
         rc = lib().oqpg_set_shell_families(self.h, 1 if on else 0)
         if rc != 0:
             raise FockError(rc, "oqpg_set_shell_families")
