@@ -255,7 +255,8 @@ int oqpg_fock_jk_device(oqpg_ctx* ctx, const double* d_device, double* f_device,
                         double sc, void* stream);
 
 /* A plain-FP64 build of the packed densities on device buffers (as
- * oqpg_fock_jk_device in precision mode 0 with the built-in launch defaults)
+ * oqpg_fock_jk_device in precision mode 0, with fixed launch parameters: the
+ * primitive-parallel head at 2^8 primitive quartets and full grids)
  * for callers that cannot allocate device memory while they build Fock
  * matrices (a host whose own pool allocator owns all device memory, or a loop
  * that cannot take the device synchronisation of cudaMalloc/cudaFree).  It
@@ -302,7 +303,9 @@ int oqpg_graph_info(const oqpg_ctx* ctx, int* captures, int* replays, int* kerne
  * oqpg_class_l (null: leave unchanged): split_log2 -- quartets with
  * >= 2^split_log2 surviving primitive quartets run the primitive-parallel
  * kernel, one warp per quartet with the lanes on its primitives (64: never;
- * -1, the default: 8 for thread-per-quartet lists, 4 for warp-per-quartet
+ * -1, the default: for thread-per-quartet lists sized on the device from the
+ * list's own primitive-quartet histogram, 6 to 8, lower for short lists whose
+ * heaviest quartets would otherwise outlast the rest; 4 for warp-per-quartet
  * ones); chunk -- quartets a warp takes per work grab in the thread-per-quartet
  * kernels (multiple of 32); ctas_per_sm -- grid cap per SM (0: as many as
  * fit).  The autotuner of the Python front end picks them.  No counterpart in

@@ -385,7 +385,7 @@ int grad_run(oqpg_ctx* c, std::vector<double>& mats, int nmat, const GammaSpec& 
         k_bin_scatter<<<(unsigned)((counts[li] + chunk - 1) / chunk), 256, 0, st>>>(
             c->d_glists[li].as<uint2>(), (long long)counts[li], nullptr, c->d_gpairs.as<PairDev>(), PAIR_MASK,
             0xffffffffu, bins + off[li], c->d_gcur.as<unsigned long long>() + li * NBIN,
-            c->d_gslists[li].as<uint2>(), chunk, nullptr);
+            c->d_gslists[li].as<uint2>(), chunk, nullptr, nullptr);
         GK(cudaGetLastError());
       }
       GK(cudaStreamSynchronize(st));   // h_cur is freed at the end of this scope

@@ -364,36 +364,92 @@ __global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const un
 
 // Each CTA takes a contiguous chunk, reserves its per-bin ranges once, then
 // places its entries (bins: the bins k_bin_hist stored; null: recomputed from
-// the primitive counts).
-__global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ list, long long n,
+// the primitive counts).  fmem (family lists): within its block of each bin
+// the CTA places the family quartets ordered by member pattern (members of
+// the bra and of the ket family pair, most first), so that the lanes of a
+// warp of the thread-per-family-quartet kernel, which take consecutive
+// entries, run member loops and digestions of the same length.
+__device__ __forceinline__ int fam_pattern(const FamMem* __restrict__ fmem, uint2 q) {
+  const int nb = min(max(__ldg(&fmem[q.x & FAM_IDX_MASK].n), 1), FAM_MAX);
+  const int nk = min(max(__ldg(&fmem[q.y & FAM_IDX_MASK].n), 1), FAM_MAX);
+  return (FAM_MAX - nb) * FAM_MAX + (FAM_MAX - nk);
+}
+
+__global__ void __launch_bounds__(1024) k_bin_scatter(const uint2* __restrict__ list, long long n,
                                                      const unsigned long long* n_dev,
                                                      const PairDev* __restrict__ pairs, unsigned xmask,
                                                      unsigned ymask, const unsigned char* __restrict__ bins,
                                                      unsigned long long* cursors, uint2* out, long long chunk,
-                                                     const unsigned* flag) {
+                                                     const unsigned* flag, const FamMem* __restrict__ fmem) {
+  constexpr int NPAT = FAM_MAX * FAM_MAX;
   __shared__ unsigned h[NBIN];
   __shared__ unsigned long long b[NBIN];
+  __shared__ unsigned hp[NBIN * NPAT];
   if (flag && *flag) return;  // a list overflowed: the cursors were not written
   n = list_len(n, n_dev);
   const long long lo = blockIdx.x * chunk;
   if (lo >= n) return;
   const long long hi = lo + chunk < n ? lo + chunk : n;
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x) h[i] = 0;
+  if (fmem)
+    for (int i = threadIdx.x; i < NBIN * NPAT; i += blockDim.x) hp[i] = 0;
   __syncthreads();
-  for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x)
-    atomicAdd(&h[bins ? bins[t] : prim_bin(pairs, list[t], xmask, ymask)], 1u);
+  for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+    const int bin = bins ? bins[t] : prim_bin(pairs, list[t], xmask, ymask);
+    atomicAdd(&h[bin], 1u);
+    if (fmem) atomicAdd(&hp[bin * NPAT + fam_pattern(fmem, list[t])], 1u);
+  }
   __syncthreads();
   for (int i = threadIdx.x; i < NBIN; i += blockDim.x) {
     b[i] = h[i] ? atomicAdd(&cursors[i], (unsigned long long)h[i]) : 0ull;
     h[i] = 0;
+    if (fmem) {  // exclusive scan of the bin's pattern counts: each pattern's offset in the bin's block
+      unsigned s = 0;
+      for (int p = 0; p < NPAT; ++p) {
+        const unsigned v = hp[i * NPAT + p];
+        hp[i * NPAT + p] = s;
+        s += v;
+      }
+    }
   }
   __syncthreads();
   for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
     const uint2 q = list[t];
     const int bin = bins ? bins[t] : prim_bin(pairs, q, xmask, ymask);
-    const unsigned r = atomicAdd(&h[bin], 1u);
+    const unsigned r = fmem ? atomicAdd(&hp[bin * NPAT + fam_pattern(fmem, q)], 1u) : atomicAdd(&h[bin], 1u);
     out[b[bin] + r] = q;
   }
+}
+
+// Smallest primitive-quartet count of bin b (work_bin's inverse, lower edge).
+__device__ __forceinline__ double bin_count(int b) {
+  const int k = NBIN - 1 - b;
+  if (k < BIN_EXACT - 1) return (double)(k + 1);
+  const int e = (k - (BIN_EXACT - 25)) >> 2, q = (k - (BIN_EXACT - 25)) & 3;
+  return ldexp(1.0, e) * (q == 0 ? 1.0 : q == 1 ? 1.18920712 : q == 2 ? 1.41421356 : 1.68179283);
+}
+
+// Head of a thread-per-quartet list sized from the list (SPLIT_ADAPTIVE).  A
+// thread-per-quartet kernel cannot end before its slowest lane, which runs
+// the primitive quartets of its heaviest quartet one after another.  When
+// the whole list spread over every lane of the GPU (32 x 4 x nsm) is only a
+// few times that chain (short lists, heavy quartets), the heaviest quartets
+// dominate the launch: they go to the primitive-parallel kernel, whose 32
+// lanes share one quartet.  The head takes the quartets with at least 2^s
+// primitive quartets, 2^s the largest power of two up to
+// npq / (2 x 32 x 4 x nsm) within [2^6, 2^8] (2^8, the fixed default, for
+// lists that fill the GPU many times over; 2^6 keeps two or more primitive
+// quartets per lane of the warp kernel).  Measured: (H2O)16 6-31G(d) build
+// 20.4 -> 17.2 ms; (H2O)32 cc-pVDZ 0.4 % faster.  (Dividing by a further 4,
+// for the four warps that share a sub-partition's FP64 pipe, took more
+// quartets of the (H2O)32 cc-pVDZ lists to the warp kernel and was slower:
+// (sp|pd) 11.2 -> 11.6 ms, (ss|pd) 4.8 -> 5.3 ms.)
+__device__ __forceinline__ int adaptive_head_bins(const unsigned long long* hist, int nsm) {
+  double npq = 0.0;
+  for (int b = 0; b < NBIN; ++b) npq += (double)hist[b] * bin_count(b);
+  const double c = npq / (2.0 * 32.0 * 4.0 * (double)nsm);
+  const int s = c >= 256.0 ? 8 : (c >= 128.0 ? 7 : 6);
+  return head_bins(s);
 }
 
 // Device-side bookkeeping of a device-driven build, one thread per list (one
@@ -401,12 +457,13 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const uint2* __restrict__ l
 // and the two work ranges of the sorted list, [0, head) for the
 // primitive-parallel kernel and [head, count) for the class kernel, head = the
 // entries in the bins of >= 2^split primitive quartets (split_bins[list] bins;
-// 0 for none).  If any list's count exceeded its capacity, overflow is set
-// and every range is empty: the scatter and the class kernels then do
-// nothing and the build is redone by the host.
+// 0 for none; SPLIT_ADAPTIVE: sized here, adaptive_head_bins).  If any list's
+// count exceeded its capacity, overflow is set and every range is empty: the
+// scatter and the class kernels then do nothing and the build is redone by
+// the host.
 __global__ void k_bin_scan(const unsigned long long* counts, const unsigned long long* caps, const int* split_bins,
                            const unsigned long long* hist, unsigned long long* cursors, unsigned long long* ranges,
-                           unsigned* overflow) {
+                           unsigned* overflow, int nsm) {
   __shared__ unsigned s_over;
   const int li = threadIdx.x;
   if (li == 0) s_over = 0;
@@ -423,7 +480,7 @@ __global__ void k_bin_scan(const unsigned long long* counts, const unsigned long
     return;
   }
   unsigned long long s = 0, head = 0;
-  const int nb = split_bins[li];
+  const int nb = split_bins[li] == SPLIT_ADAPTIVE ? adaptive_head_bins(hist + li * NBIN, nsm) : split_bins[li];
   for (int b = 0; b < NBIN; ++b) {
     cursors[li * NBIN + b] = s;
     s += hist[li * NBIN + b];
@@ -1058,7 +1115,10 @@ int size_lists(oqpg_ctx* c, BuildBufs& B, const unsigned long long* counts, cuda
   for (int k = 0; k < NLIST; ++k) {
     const int cl = list_class(k);
     B.team[k] = k < NLIST_SHELL && list_team(c, cl, B.cap[k]) ? 1 : 0;
-    split[k] = class_info(cl).prim ? head_bins(eff_split(c, cl, B.team[k] != 0)) : 0;
+    // default-tuned thread-per-quartet lists: the head is sized on the device
+    split[k] = !class_info(cl).prim                            ? 0
+             : (c->tune.split_log2[cl] < 0 && B.team[k] == 0) ? SPLIT_ADAPTIVE
+                                                               : head_bins(eff_split(c, cl, B.team[k] != 0));
   }
   CK(cudaMemcpyAsync(B.split.p, split, sizeof(split), cudaMemcpyHostToDevice, st));
   CK(cudaStreamSynchronize(st));  // the host arrays above are stack memory
@@ -1129,18 +1189,21 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   static_assert(NLIST <= 128, "k_bin_scan runs one thread per list in one 128-thread CTA");
   k_bin_scan<<<1, 128, 0, st>>>(counts, B.caps.as<unsigned long long>(), B.split.as<int>(),
                                B.hist.as<unsigned long long>(), B.cursor.as<unsigned long long>(),
-                               B.ranges.as<unsigned long long>(), B.flag.as<unsigned>());
+                               B.ranges.as<unsigned long long>(), B.flag.as<unsigned>(), c->nsm);
   CK(cudaGetLastError());
   ++nlaunch;
-  const long long chunk = 4096;
   for (int k = 0; k < NLIST; ++k) {
     if (!B.cap[k]) continue;
     const long long cap = (long long)B.cap[k];
     const bool fl = fam_list(k);
-    k_bin_scatter<<<(unsigned)((cap + chunk - 1) / chunk), 256, 0, st>>>(
+    // family lists: longer blocks per CTA (so each bin's pattern runs are
+    // longer) with more threads (so each thread's loops stay as short)
+    const long long chunk = fl ? 16384 : 4096;
+    k_bin_scatter<<<(unsigned)((cap + chunk - 1) / chunk), fl ? 1024 : 256, 0, st>>>(
         B.lists[k].as<uint2>(), cap, counts + k, (fl ? c->d_fpairs : c->d_pairs).as<PairDev>(),
         fl ? FAM_IDX_MASK : PAIR_MASK, fl ? FAM_IDX_MASK : 0xffffffffu, B.bins[k].as<unsigned char>(),
-        B.cursor.as<unsigned long long>() + k * NBIN, B.slists[k].as<uint2>(), chunk, B.flag.as<unsigned>());
+        B.cursor.as<unsigned long long>() + k * NBIN, B.slists[k].as<uint2>(), chunk, B.flag.as<unsigned>(),
+        fl ? c->d_fmem.as<FamMem>() : nullptr);
     CK(cudaGetLastError());
     ++nlaunch;
   }

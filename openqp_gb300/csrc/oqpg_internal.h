@@ -20,13 +20,16 @@ enum Status { OK = 0, NOT_INIT = 1, NO_MEM = 2, UNSUPPORTED = 3, DEV_ERR = 4 };
 constexpr int NBIN = 128;
 constexpr int BIN_EXACT = 64;
 // Bins 0 .. head_bins(s) - 1 hold the quartets with at least 2^s primitive quartets.
-inline int head_bins(int s) {
+__host__ __device__ inline int head_bins(int s) {
   if (s < 0) return NBIN;
   if (s > 30) return 0;
   const int b = (1 << s) < BIN_EXACT ? (1 << s) - 1 : 4 * s + BIN_EXACT - 25;
   return b > NBIN - 1 ? 0 : NBIN - b;
 }
 constexpr int PRIM_SPLIT_LOG2 = 8;  // >= 256 primitive quartets: warp per quartet
+// split_bins entry of a list whose head the device sizes from the list itself
+// (k_bin_scan: the default of thread-per-quartet lists)
+constexpr int SPLIT_ADAPTIVE = -1;
 
 // One molecule of a context (a context holds a batch of one or more).  Its
 // shells, pairs and AO rows are contiguous ranges of the context's tables;
@@ -160,10 +163,10 @@ __global__ void k_bin_hist(const uint2* __restrict__ list, long long n, const un
 __global__ void k_bin_scatter(const uint2* __restrict__ list, long long n, const unsigned long long* n_dev,
                               const PairDev* __restrict__ pairs, unsigned xmask, unsigned ymask,
                               const unsigned char* __restrict__ bins, unsigned long long* cursors, uint2* out,
-                              long long chunk, const unsigned* flag);
+                              long long chunk, const unsigned* flag, const FamMem* __restrict__ fmem);
 __global__ void k_bin_scan(const unsigned long long* counts, const unsigned long long* caps, const int* split_bins,
                            const unsigned long long* hist, unsigned long long* cursors, unsigned long long* ranges,
-                           unsigned* overflow);
+                           unsigned* overflow, int nsm);
 // (does nothing when *flag != 0: a list overflowed and the build is redone)
 __global__ void k_finalize(const double* __restrict__ gj, const double* __restrict__ gk, int nk,
                            const MolDev* __restrict__ mols, int nmol, long long ntri_total, int stride,

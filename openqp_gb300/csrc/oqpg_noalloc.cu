@@ -6,9 +6,10 @@
 // out-of-memory or fragmentation from allocations made behind its back, and a
 // latency-critical SCF loop cannot afford the device-wide synchronisation a
 // cudaMalloc/cudaFree pair may cause.  For them oqpg_fock_jk_noalloc runs the
-// plain-FP64 build of oqpg_fock_jk_device (precision mode 0, the built-in
-// launch defaults, whatever the context's precision split and tuning say;
-// the context's cutoff applies), with every per-build buffer (densities, J/K
+// plain-FP64 build of oqpg_fock_jk_device (precision mode 0, fixed launch
+// parameters: the primitive-parallel head at 2^8 primitive quartets and full
+// grids, whatever the context's precision split and tuning say; the
+// context's cutoff applies), with every per-build buffer (densities, J/K
 // accumulators, shell densities, quartet lists, counters) carved out of one
 // file-scope device array of fixed size, so it calls no cudaMalloc, cudaFree
 // or allocating library routine.  The read-only tables of the molecule
@@ -188,7 +189,7 @@ extern "C" int oqpg_fock_jk_noalloc(oqpg_ctx* c, const double* d_device, double*
     const long long chunk = 4096;
     k_bin_scatter<<<(unsigned)((h_counts[k] + chunk - 1) / chunk), 256, 0, st>>>(
         lists + off[k], (long long)h_counts[k], nullptr, c->d_pairs.as<PairDev>(), PAIR_MASK, 0xffffffffu, nullptr,
-        cursor + k * NBIN, slists + off[k], chunk, nullptr);
+        cursor + k * NBIN, slists + off[k], chunk, nullptr, nullptr);
     NK(cudaGetLastError());
   }
   // integrals and digestion
