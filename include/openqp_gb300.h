@@ -256,7 +256,7 @@ int oqpg_fock_jk_device(oqpg_ctx* ctx, const double* d_device, double* f_device,
 
 /* A plain-FP64 build of the packed densities on device buffers (as
  * oqpg_fock_jk_device in precision mode 0, with fixed launch parameters: the
- * primitive-parallel head at 2^8 primitive quartets and full grids)
+ * primitive-parallel head at 2^8 primitive quartets, no tuned grid caps)
  * for callers that cannot allocate device memory while they build Fock
  * matrices (a host whose own pool allocator owns all device memory, or a loop
  * that cannot take the device synchronisation of cudaMalloc/cudaFree).  It

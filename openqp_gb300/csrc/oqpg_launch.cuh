@@ -58,6 +58,18 @@ cudaError_t launch_team(int kind, const BuildArgs& a, int nsm, cudaStream_t st) 
   }
 }
 
+// The FP64 thread-per-quartet (pp|pp) kernel (81 block elements beside the
+// 2D tables: 255 registers and a 368-byte stack frame) runs one CTA of four
+// warps per SM unless a grid cap is tuned.  Measured against two CTAs per SM
+// (its register limit): (H2O)32 cc-pVDZ 10.1 -> 6.9 ms, (H2O)16 6-31G(d)
+// 0.48 -> 0.42 ms.  The same cap for the other thread-per-quartet kernels
+// with a stack frame was slower on C40H82 6-31G(d): (sp|sd) 19.0 -> 21.9 ms,
+// (sd|pd) 8.7 -> 9.5 ms, (sp|dd) 4.4 -> 4.8 ms.
+template <int LA, int LB, int LC, int LD, typename T>
+constexpr bool small_one_cta() {
+  return LA == 1 && LB == 1 && LC == 1 && LD == 1 && std::is_same<T, double>::value;
+}
+
 template <int LA, int LB, int LC, int LD, bool PURE, typename T>
 cudaError_t launch_fock(int kind, const BuildArgs& a, int nsm, cudaStream_t st) {
   if constexpr (only_team<LA, LB, LC, LD>()) {
@@ -67,6 +79,11 @@ cudaError_t launch_fock(int kind, const BuildArgs& a, int nsm, cudaStream_t st) 
       if (a.team) return launch_team<LA, LB, LC, LD, PURE, T>(kind, a, nsm, st);
     }
     if (kind == MODE_PRIM) return launch_persistent(k_prim<LA, LB, LC, LD, PURE, T>, 0, 4, a, nsm, st);
+    if (small_one_cta<LA, LB, LC, LD, T>() && a.ctas_per_sm == 0) {
+      BuildArgs b = a;
+      b.ctas_per_sm = 1;
+      return launch_persistent(k_small<LA, LB, LC, LD, PURE, false, T>, 0, 128, b, nsm, st);
+    }
     return launch_persistent(k_small<LA, LB, LC, LD, PURE, false, T>, 0, 128, a, nsm, st);
   }
 }

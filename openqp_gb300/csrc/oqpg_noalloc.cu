@@ -7,8 +7,8 @@
 // latency-critical SCF loop cannot afford the device-wide synchronisation a
 // cudaMalloc/cudaFree pair may cause.  For them oqpg_fock_jk_noalloc runs the
 // plain-FP64 build of oqpg_fock_jk_device (precision mode 0, fixed launch
-// parameters: the primitive-parallel head at 2^8 primitive quartets and full
-// grids, whatever the context's precision split and tuning say; the
+// parameters: the primitive-parallel head at 2^8 primitive quartets and no
+// tuned grid caps, whatever the context's precision split and tuning say; the
 // context's cutoff applies), with every per-build buffer (densities, J/K
 // accumulators, shell densities, quartet lists, counters) carved out of one
 // file-scope device array of fixed size, so it calls no cudaMalloc, cudaFree
