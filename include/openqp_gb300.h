@@ -303,10 +303,11 @@ int oqpg_graph_info(const oqpg_ctx* ctx, int* captures, int* replays, int* kerne
  * oqpg_class_l (null: leave unchanged): split_log2 -- quartets with
  * >= 2^split_log2 surviving primitive quartets run the primitive-parallel
  * kernel, one warp per quartet with the lanes on its primitives (64: never;
- * -1, the default: for thread-per-quartet lists sized on the device from the
- * list's own primitive-quartet histogram, 6 to 8, lower for short lists whose
- * heaviest quartets would otherwise outlast the rest; 4 for warp-per-quartet
- * ones); chunk -- quartets a warp takes per work grab in the thread-per-quartet
+ * -1, the default: for thread-per-quartet lists of builds with at most 32
+ * densities sized on the device from the list's own primitive-quartet
+ * histogram, 6 to 8, lower for short lists whose heaviest quartets would
+ * otherwise outlast the rest, 8 in builds with more densities; 4 for
+ * warp-per-quartet ones); chunk -- quartets a warp takes per work grab in the thread-per-quartet
  * kernels (multiple of 32); ctas_per_sm -- grid cap per SM (0: as many as
  * fit).  The autotuner of the Python front end picks them.  No counterpart in
  * the reference. */

@@ -443,7 +443,13 @@ __device__ __forceinline__ double bin_count(int b) {
 // 20.4 -> 17.2 ms; (H2O)32 cc-pVDZ 0.4 % faster.  (Dividing by a further 4,
 // for the four warps that share a sub-partition's FP64 pipe, took more
 // quartets of the (H2O)32 cc-pVDZ lists to the warp kernel and was slower:
-// (sp|pd) 11.2 -> 11.6 ms, (ss|pd) 4.8 -> 5.3 ms.)
+// (sp|pd) 11.2 -> 11.6 ms, (ss|pd) 4.8 -> 5.3 ms.)  The primitive-parallel
+// kernel digests each quartet on one lane, so builds with many densities
+// (more than 32 Coulomb and exchange densities: the MRSF sigma build of 8
+// vectors digests 88) keep the fixed 2^8: measured on (H2O)16 6-31G(d), the
+// MRSF build took 114.4 ms with the adaptive head and 108.2 ms without it,
+// the TD build of 8 vectors (24 densities) 28.5 and 31.0 ms.
+constexpr int ADAPTIVE_MAX_DENSITIES = 32;
 __device__ __forceinline__ int adaptive_head_bins(const unsigned long long* hist, int nsm) {
   double npq = 0.0;
   for (int b = 0; b < NBIN; ++b) npq += (double)hist[b] * bin_count(b);
@@ -457,13 +463,14 @@ __device__ __forceinline__ int adaptive_head_bins(const unsigned long long* hist
 // and the two work ranges of the sorted list, [0, head) for the
 // primitive-parallel kernel and [head, count) for the class kernel, head = the
 // entries in the bins of >= 2^split primitive quartets (split_bins[list] bins;
-// 0 for none; SPLIT_ADAPTIVE: sized here, adaptive_head_bins).  If any list's
+// 0 for none; SPLIT_ADAPTIVE: sized here, adaptive_head_bins, when adaptive
+// is set, else 2^PRIM_SPLIT_LOG2).  If any list's
 // count exceeded its capacity, overflow is set and every range is empty: the
 // scatter and the class kernels then do nothing and the build is redone by
 // the host.
 __global__ void k_bin_scan(const unsigned long long* counts, const unsigned long long* caps, const int* split_bins,
                            const unsigned long long* hist, unsigned long long* cursors, unsigned long long* ranges,
-                           unsigned* overflow, int nsm) {
+                           unsigned* overflow, int nsm, int adaptive) {
   __shared__ unsigned s_over;
   const int li = threadIdx.x;
   if (li == 0) s_over = 0;
@@ -480,7 +487,9 @@ __global__ void k_bin_scan(const unsigned long long* counts, const unsigned long
     return;
   }
   unsigned long long s = 0, head = 0;
-  const int nb = split_bins[li] == SPLIT_ADAPTIVE ? adaptive_head_bins(hist + li * NBIN, nsm) : split_bins[li];
+  const int nb = split_bins[li] != SPLIT_ADAPTIVE ? split_bins[li]
+                 : adaptive                      ? adaptive_head_bins(hist + li * NBIN, nsm)
+                                                 : head_bins(PRIM_SPLIT_LOG2);
   for (int b = 0; b < NBIN; ++b) {
     cursors[li * NBIN + b] = s;
     s += hist[li * NBIN + b];
@@ -1189,7 +1198,8 @@ int issue_build(oqpg_ctx* c, BuildBufs& B, const Job& job, cudaStream_t st, bool
   static_assert(NLIST <= 128, "k_bin_scan runs one thread per list in one 128-thread CTA");
   k_bin_scan<<<1, 128, 0, st>>>(counts, B.caps.as<unsigned long long>(), B.split.as<int>(),
                                B.hist.as<unsigned long long>(), B.cursor.as<unsigned long long>(),
-                               B.ranges.as<unsigned long long>(), B.flag.as<unsigned>(), c->nsm);
+                               B.ranges.as<unsigned long long>(), B.flag.as<unsigned>(), c->nsm,
+                               nj + nk <= ADAPTIVE_MAX_DENSITIES ? 1 : 0);
   CK(cudaGetLastError());
   ++nlaunch;
   for (int k = 0; k < NLIST; ++k) {

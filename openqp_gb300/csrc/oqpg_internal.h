@@ -166,7 +166,7 @@ __global__ void k_bin_scatter(const uint2* __restrict__ list, long long n, const
                               long long chunk, const unsigned* flag, const FamMem* __restrict__ fmem);
 __global__ void k_bin_scan(const unsigned long long* counts, const unsigned long long* caps, const int* split_bins,
                            const unsigned long long* hist, unsigned long long* cursors, unsigned long long* ranges,
-                           unsigned* overflow, int nsm);
+                           unsigned* overflow, int nsm, int adaptive);
 // (does nothing when *flag != 0: a list overflowed and the build is redone)
 __global__ void k_finalize(const double* __restrict__ gj, const double* __restrict__ gk, int nk,
                            const MolDev* __restrict__ mols, int nmol, long long ntri_total, int stride,
