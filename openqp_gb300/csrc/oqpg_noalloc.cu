@@ -39,7 +39,7 @@ constexpr int MAX_DEVICES = 64;
 // process exits.  All calls on a device share it and it keeps the last call's
 // contents; each call clears what must start at zero.  Calls that overlap on
 // the GPU (two streams, two host threads) race on it.
-__device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
 std::mutex g_noalloc_mutex;
 void* g_scratch_addr[MAX_DEVICES] = {nullptr};
