@@ -459,7 +459,7 @@ __device__ __forceinline__ int adaptive_head_bins(const unsigned long long* hist
 }
 
 // Device-side bookkeeping of a device-driven build, one thread per list (one
-// CTA of 64 threads): the exclusive scan of its bin counts (scatter cursors)
+// CTA of 128 threads): the exclusive scan of its bin counts (scatter cursors)
 // and the two work ranges of the sorted list, [0, head) for the
 // primitive-parallel kernel and [head, count) for the class kernel, head = the
 // entries in the bins of >= 2^split primitive quartets (split_bins[list] bins;
