@@ -212,10 +212,15 @@ int oqpg_sig_iter_device(const double* bvec, int nv, double* sigma, void* stream
 void routec_fock_jk_cam(const double* d, double* f, const int* nbf, const int* nfocks, const double* cam,
                         int* info);
 
-/* Release the process-global context. */
+/* Release the process-global context (no counterpart in the reference, whose
+ * int2 state lives in module variables for the life of the process). */
 void routec_fock_finalize(void);
 
 /* ---- explicit-context API -------------------------------------------- */
+/* No counterpart in the reference: the oqpg_* entry points take an explicit
+ * context instead of the routec_* seams' process-global one, and serve the
+ * Python/torch front end (device buffers, caller streams), batches of
+ * molecules, captured graphs, tuning and statistics. */
 
 typedef struct oqpg_ctx oqpg_ctx;
 
